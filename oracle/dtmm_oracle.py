@@ -1,0 +1,1232 @@
+"""CPU restatement of dtmm's ``transfer_field`` hot path (numpy/scipy, complex128).
+
+TEST INFRASTRUCTURE -- THIS IS THE ORACLE, NOT THE PRODUCT.
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import it, and only as the checker / the timed CPU baseline.
+The product (``dtmm_gb300``) never imports this module.
+
+Parity pin: every function below restates the reference function cited in
+its docstring (paths are relative to the reference project root).  The whole
+restatement is pinned against outputs of the unmodified reference itself,
+run in the build container under a pure-Python numba stand-in; those outputs
+are committed as golden fixtures under ``tests/golden/`` together with the
+script that produced them (``tests/golden/make_golden.py``), and
+``tests/test_oracle_golden.py`` checks this module against them.  The
+reference's own known-answer vectors for the k-grid maps
+(``dtmm/test/test_wave.py``) and its dot-product property checks
+(``dtmm/test/test_linalg.py``) are checked as well.
+
+Scope (matches the product): ``method="4x4"`` with reflection mode 1 (the
+k-space "effective" split-step operator) and ``method="2x2"`` with reflection
+mode 0, diffraction >= 1 (diffraction > 1 = tent-window mode grouping),
+npass >= 1 for 4x4 (norm "fft"), nstep >= 1, scalar or per-ray beta/phi or
+beta/phi estimated from the field, real or complex eps, isotropic / uniaxial /
+biaxial voxels, isotropic effective layers (eff_data 0).
+"""
+from __future__ import annotations
+
+import os
+import warnings
+
+import numpy as np
+import scipy.fft as _sfft
+
+FDTYPE = np.float64
+CDTYPE = np.complex128
+
+# defaults of the reference's shipped ini file (dtmm/dtmm.ini, dtmm/conf.py:459-522)
+BETAMAX = 0.8
+SMOOTH = 0.1
+N_COVER = 1.5
+DEFAULTS = {
+    "nin": N_COVER,
+    "nout": N_COVER,
+    # the ini value is read with its quotes (dtmm/conf.py:506), so the
+    # default never equals "4x4" and routes to the 2x2 method
+    "method": '"2x2"',
+    "npass": 1,
+    "diffraction": 1,
+    "reflection": None,
+    "eff_data": 0,
+    "betamax": BETAMAX,
+}
+DTMM_NORM_FFT = 1 << 0
+DTMM_NORM_REF = 1 << 1
+
+_WORKERS = int(os.environ.get("DTMM_ORACLE_THREADS", os.cpu_count() or 1))
+
+
+def set_workers(n):
+    """Number of threads used by the oracle's FFTs."""
+    global _WORKERS
+    _WORKERS = max(1, int(n))
+
+
+def fft2(a):
+    """Unnormalised 2D FFT over the last two axes (dtmm/fft.py:277, scipy backend :178-200)."""
+    return _sfft.fft2(np.asarray(a, CDTYPE), workers=_WORKERS)
+
+
+def ifft2(a):
+    """1/N-normalised inverse 2D FFT over the last two axes (dtmm/fft.py:306)."""
+    return _sfft.ifft2(np.asarray(a, CDTYPE), workers=_WORKERS)
+
+
+# --------------------------------------------------------------------------
+# k-space grids (dtmm/wave.py)
+# --------------------------------------------------------------------------
+def k0(wavelength, pixelsize=1.0):
+    """Vacuum wavenumber in pixel units, 2*pi/lambda*pixelsize (dtmm/wave.py:280)."""
+    return np.asarray(2 * np.pi / np.asarray(wavelength) * pixelsize, FDTYPE)
+
+
+def betaphi(shape, k):
+    """beta, phi of every FFT-grid eigenwave (dtmm/wave.py:54)."""
+    k = np.abs(np.asarray(k, FDTYPE)[..., None, None])
+    ay, ax = (np.asarray(np.fft.fftfreq(n), FDTYPE) for n in shape[-2:])
+    xx, yy = np.meshgrid(ax, ay, indexing="xy")
+    beta = (2 * np.pi / k) * np.sqrt(xx ** 2 + yy ** 2)
+    phi = np.arctan2(yy, xx)
+    return beta, phi
+
+
+def betaxy(shape, k):
+    """beta_x, beta_y of every FFT-grid eigenwave (dtmm/wave.py:84)."""
+    k = np.asarray(k, FDTYPE)[..., None, None]
+    ay, ax = (np.asarray(np.fft.fftfreq(n), FDTYPE) for n in shape[-2:])
+    xx, yy = np.meshgrid(ax, ay, indexing="xy")
+    scale = 2 * np.pi / k
+    return scale * xx, scale * yy
+
+
+# --------------------------------------------------------------------------
+# small dense algebra on (..., n, n) stacks (dtmm/linalg.py)
+# --------------------------------------------------------------------------
+def inv(m):
+    """Batched 2x2 / 4x4 complex inverse; an exactly singular matrix maps to 0.
+
+    Restates ``inv`` (dtmm/linalg.py:521, ``_inv4x4`` :460, ``_inv2x2`` :428):
+    adjugate over determinant, with ``det == 0`` giving an all-zero result.
+    The 4x4 adjugate is formed from the 2x2 minors of the top and bottom row
+    pairs (Laplace expansion by complementary minors).
+    """
+    m = np.asarray(m, CDTYPE)
+    n = m.shape[-1]
+    out = np.empty_like(m)
+    if n == 2:
+        a, b, c, d = m[..., 0, 0], m[..., 0, 1], m[..., 1, 0], m[..., 1, 1]
+        det = a * d - b * c
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r = np.where(det == 0, 0.0, 1.0 / np.where(det == 0, 1.0, det))
+        out[..., 0, 0] = d * r
+        out[..., 0, 1] = -b * r
+        out[..., 1, 0] = -c * r
+        out[..., 1, 1] = a * r
+        return out
+    if n != 4:
+        raise ValueError("only 2x2 and 4x4 matrices are supported")
+    a = [[m[..., i, j] for j in range(4)] for i in range(4)]
+    s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1]
+    s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2]
+    s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3]
+    s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2]
+    s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3]
+    s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3]
+    c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3]
+    c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3]
+    c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2]
+    c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3]
+    c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2]
+    c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1]
+    det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(det == 0, 0.0, 1.0 / np.where(det == 0, 1.0, det))
+    adj = [
+        [a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3,
+         -a[0][1] * c5 + a[0][2] * c4 - a[0][3] * c3,
+         a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3,
+         -a[2][1] * s5 + a[2][2] * s4 - a[2][3] * s3],
+        [-a[1][0] * c5 + a[1][2] * c2 - a[1][3] * c1,
+         a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1,
+         -a[3][0] * s5 + a[3][2] * s2 - a[3][3] * s1,
+         a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1],
+        [a[1][0] * c4 - a[1][1] * c2 + a[1][3] * c0,
+         -a[0][0] * c4 + a[0][1] * c2 - a[0][3] * c0,
+         a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0,
+         -a[2][0] * s4 + a[2][1] * s2 - a[2][3] * s0],
+        [-a[1][0] * c3 + a[1][1] * c1 - a[1][2] * c0,
+         a[0][0] * c3 - a[0][1] * c1 + a[0][2] * c0,
+         -a[3][0] * s3 + a[3][1] * s1 - a[3][2] * s0,
+         a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0],
+    ]
+    for i in range(4):
+        for j in range(4):
+            out[..., i, j] = adj[i][j] * r
+    return out
+
+
+def dotmm(a, b):
+    """Batched matrix product (dtmm/linalg.py:1046)."""
+    return np.matmul(np.asarray(a, CDTYPE), np.asarray(b, CDTYPE))
+
+
+def dotmdm(a, d, b):
+    """a . diag(d) . b per element (dtmm/linalg.py:1233)."""
+    return np.matmul(np.asarray(a, CDTYPE) * np.asarray(d, CDTYPE)[..., None, :], np.asarray(b, CDTYPE))
+
+
+def dotmf(a, f):
+    """Per-pixel matrix times a (..., n, H, W) field (dtmm/linalg.py:979, ``_dotmf4``/``_dotmf2`` :833/:852)."""
+    return np.einsum("...hwij,...jhw->...ihw", np.asarray(a, CDTYPE), np.asarray(f, CDTYPE), optimize=True)
+
+
+def dotmdmf(a, d, b, f):
+    """a . diag(d) . b . f per pixel (dtmm/linalg.py:1002, ``_dotmdmf4`` :905)."""
+    return dotmf(dotmdm(a, d, b), f)
+
+
+def dotmv(a, v):
+    """Matrix times vector per element (dtmm/linalg.py:1219)."""
+    return np.einsum("...ij,...j->...i", np.asarray(a, CDTYPE), np.asarray(v, CDTYPE))
+
+
+# --------------------------------------------------------------------------
+# rotations (dtmm/rotation.py)
+# --------------------------------------------------------------------------
+def rotation_vector2(angle):
+    """(cos, sin) of an angle array (dtmm/rotation.py:36)."""
+    angle = np.asarray(angle, FDTYPE)
+    return np.stack([np.cos(angle), np.sin(angle)], axis=-1)
+
+
+def _rotation_matrix_uniaxial(theta, phi):
+    """R = R_phi . R_theta (dtmm/rotation.py:176)."""
+    ct, st, cp, sp = np.cos(theta), np.sin(theta), np.cos(phi), np.sin(phi)
+    R = np.zeros(np.shape(theta) + (3, 3), FDTYPE)
+    R[..., 0, 0] = ct * cp
+    R[..., 0, 1] = -sp
+    R[..., 0, 2] = cp * st
+    R[..., 1, 0] = ct * sp
+    R[..., 1, 1] = cp
+    R[..., 1, 2] = st * sp
+    R[..., 2, 0] = -st
+    R[..., 2, 2] = ct
+    return R
+
+
+def _rotation_matrix(psi, theta, phi):
+    """Full Euler rotation R_phi . R_theta . R_psi (dtmm/rotation.py:125)."""
+    cps, sps = np.cos(psi), np.sin(psi)
+    ct, st = np.cos(theta), np.sin(theta)
+    cp, sp = np.cos(phi), np.sin(phi)
+    R = np.empty(np.shape(theta) + (3, 3), FDTYPE)
+    R[..., 0, 0] = ct * (cp * cps) - sp * sps
+    R[..., 0, 1] = -ct * (cp * sps) - sp * cps
+    R[..., 0, 2] = cp * st
+    R[..., 1, 0] = ct * (sp * cps) + cp * sps
+    R[..., 1, 1] = cp * cps - ct * (sp * sps)
+    R[..., 1, 2] = st * sp
+    R[..., 2, 0] = -cps * st
+    R[..., 2, 1] = st * sps
+    R[..., 2, 2] = ct
+    return R
+
+
+def _rotate_diagonal_tensor(R, diag):
+    """R . diag . R^T as 6 independent entries (dtmm/rotation.py:285)."""
+    out = np.empty(R.shape[:-2] + (6,), CDTYPE)
+    d0, d1, d2 = diag[..., 0], diag[..., 1], diag[..., 2]
+    for i in range(3):
+        out[..., i] = d0 * R[..., i, 0] ** 2 + d1 * R[..., i, 1] ** 2 + d2 * R[..., i, 2] ** 2
+    for k, (i, j) in zip((3, 4, 5), ((0, 1), (0, 2), (1, 2))):
+        out[..., k] = d0 * R[..., i, 0] * R[..., j, 0] + d1 * R[..., i, 1] * R[..., j, 1] + d2 * R[..., i, 2] * R[..., j, 2]
+    return out
+
+
+def _dotr2m(rv, F):
+    """Rotate a field matrix about z by (cos, sin) = rv (dtmm/linalg.py:674)."""
+    r0 = rv[..., 0][..., None]
+    r1 = rv[..., 1][..., None]
+    out = np.empty_like(F)
+    out[..., 0, :] = F[..., 0, :] * r0 - F[..., 2, :] * r1
+    out[..., 1, :] = F[..., 1, :] * r0 + F[..., 3, :] * r1
+    out[..., 2, :] = F[..., 0, :] * r1 + F[..., 2, :] * r0
+    out[..., 3, :] = -F[..., 1, :] * r1 + F[..., 3, :] * r0
+    return out
+
+
+# --------------------------------------------------------------------------
+# Berreman eigen-solve (dtmm/tmm.py)
+# --------------------------------------------------------------------------
+def _alphaf_iso(beta, eps0):
+    """Isotropic eigenvalues and field matrix, phi = 0 frame (dtmm/tmm.py:124)."""
+    n = beta.shape[0]
+    alpha = np.zeros((n, 4), CDTYPE)
+    F = np.zeros((n, 4, 4), CDTYPE)
+    aout = np.sqrt(eps0 - beta ** 2)
+    ok = aout != 0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        gp = np.where(ok, eps0 / np.where(ok, aout, 1.0), 0.0)
+    gs = -aout
+    alpha[:, 0] = aout
+    alpha[:, 1] = -aout
+    alpha[:, 2] = aout
+    alpha[:, 3] = -aout
+    F[:, 0, 0] = 0.5
+    F[:, 0, 1] = 0.5
+    F[:, 1, 0] = 0.5 * gp
+    F[:, 1, 1] = -0.5 * gp
+    F[:, 2, 2] = 0.5
+    F[:, 2, 3] = 0.5
+    F[:, 3, 2] = 0.5 * gs
+    F[:, 3, 3] = -0.5 * gs
+    alpha[~ok] = 0.0
+    F[~ok] = 0.0
+    return alpha, F
+
+
+def _alphaf_uniaxial(beta, eps0, R):
+    """Analytic uniaxial eigenvalues and column-normalised field matrix (dtmm/tmm.py:157)."""
+    n = beta.shape[0]
+    alpha = np.empty((n, 4), CDTYPE)
+    F = np.empty((n, 4, 4), CDTYPE)
+    ct = R[:, 2, 2]
+    st = -R[:, 2, 0]
+    st2 = st * st
+    ct2 = ct * ct
+    sf = -R[:, 0, 1]
+    cf = R[:, 1, 1]
+    eps11 = eps0[:, 0]
+    delta = eps0[:, 2] - eps11
+    z = beta == 0.0
+    nz = ~z
+    # beta == 0 branch
+    evs = np.empty(n, CDTYPE)
+    evpp = np.empty(n, CDTYPE)
+    evpm = np.empty(n, CDTYPE)
+    ev02 = np.empty(n, CDTYPE)
+    if z.any():
+        e11 = eps11[z]
+        ev02[z] = e11
+        evs[z] = np.sqrt(e11)
+        u = e11 + delta[z] * ct2[z]
+        w = e11 * (e11 + delta[z])
+        sq = np.sqrt(u * w) / u
+        evpp[z] = sq
+        evpm[z] = -sq
+    if nz.any():
+        e11 = eps11[nz]
+        b = beta[nz]
+        e02 = e11 - b * b
+        ev02[nz] = e02
+        evs[nz] = np.sqrt(e02)
+        u = e11 + delta[nz] * ct2[nz]
+        gama = b * cf[nz]
+        v = gama * delta[nz] * 2 * st[nz] * ct[nz]
+        w = gama * gama * (delta[nz] * st2[nz]) - e11 * (e02 + delta[nz])
+        sq = np.sqrt(v * v - 4 * u * w) / 2 / u
+        v = v / 2 / u
+        evpp[nz] = -v + sq
+        evpm[nz] = -v - sq
+    alpha[:, 0] = evpp
+    alpha[:, 1] = evpm
+    alpha[:, 2] = evs
+    alpha[:, 3] = -evs
+    if z.any():
+        e11, s, c, es = eps11[z], sf[z], cf[z], evs[z]
+        pp, pm = evpp[z], evpm[z]
+        F[z, 0, 2] = -es * s
+        F[z, 1, 2] = -e11 * s
+        F[z, 2, 2] = es * c
+        F[z, 3, 2] = -e11 * c
+        F[z, 0, 3] = -es * s
+        F[z, 1, 3] = e11 * s
+        F[z, 2, 3] = es * c
+        F[z, 3, 3] = e11 * c
+        F[z, 0, 0] = c
+        F[z, 1, 0] = pp * c
+        F[z, 2, 0] = s
+        F[z, 3, 0] = -pp * s
+        F[z, 0, 1] = c
+        F[z, 1, 1] = pm * c
+        F[z, 2, 1] = s
+        F[z, 3, 1] = -pm * s
+    if nz.any():
+        e11, es, e02 = eps11[nz], evs[nz], ev02[nz]
+        pp, pm = evpp[nz], evpm[nz]
+        sfst = R[nz, 1, 2]
+        cfst = R[nz, 0, 2]
+        ctbeta = ct[nz] * beta[nz]
+        ctbetaeps11 = ctbeta / e11
+        eps11sfst = e11 * sfst
+        evssfst = es * sfst
+        evscfst = es * cfst
+        evsctbeta = es * ctbeta
+        ev02cfst = e02 * cfst
+        ev02cfsteps11 = ev02cfst / e11
+        F[nz, 0, 2] = evssfst
+        F[nz, 1, 2] = eps11sfst
+        F[nz, 2, 2] = ctbeta - evscfst
+        F[nz, 3, 2] = ev02cfst - evsctbeta
+        F[nz, 0, 3] = -evssfst
+        F[nz, 1, 3] = eps11sfst
+        F[nz, 2, 3] = evscfst + ctbeta
+        F[nz, 3, 3] = ev02cfst + evsctbeta
+        F[nz, 0, 0] = pp * ctbetaeps11 - ev02cfsteps11
+        F[nz, 1, 0] = ctbeta - pp * cfst
+        F[nz, 2, 0] = -sfst
+        F[nz, 3, 0] = pp * sfst
+        F[nz, 0, 1] = -pm * ctbetaeps11 + ev02cfsteps11
+        F[nz, 1, 1] = pm * cfst - ctbeta
+        F[nz, 2, 1] = sfst
+        F[nz, 3, 1] = -pm * sfst
+    norm = np.sqrt((F.real ** 2 + F.imag ** 2).sum(axis=1))
+    F = F / norm[:, None, :]
+    return alpha, F
+
+
+def _auxiliary_matrix(beta, eps):
+    """Berreman auxiliary 4x4 matrix in the phi = 0 frame (dtmm/tmm.py:100)."""
+    n = beta.shape[0]
+    L = np.zeros((n, 4, 4), CDTYPE)
+    eps2m = 1.0 / eps[:, 2]
+    e4 = eps[:, 4] * eps2m
+    e5 = eps[:, 5] * eps2m
+    L[:, 0, 0] = -beta * e4
+    L[:, 0, 1] = 1.0 - beta * beta * eps2m
+    L[:, 0, 2] = -beta * e5
+    L[:, 1, 0] = eps[:, 0] - eps[:, 4] * e4
+    L[:, 1, 1] = L[:, 0, 0]
+    L[:, 1, 2] = eps[:, 3] - eps[:, 5] * e4
+    L[:, 2, 3] = -1.0
+    L[:, 3, 0] = -L[:, 1, 2]
+    L[:, 3, 1] = -L[:, 0, 2]
+    L[:, 3, 2] = beta * beta + eps[:, 5] * e5 - eps[:, 1]
+    return L
+
+
+def _poynting_columns(F):
+    """z-Poynting of every column of a field matrix (dtmm/tmm.py:293)."""
+    return (F[:, 0, :].real * F[:, 1, :].real + F[:, 0, :].imag * F[:, 1, :].imag) - (
+        F[:, 2, :].real * F[:, 3, :].real + F[:, 2, :].imag * F[:, 3, :].imag
+    )
+
+
+def _alphaf_biaxial(beta, phi, eps0, epsa):
+    """General eigen-solve and Poynting sort (dtmm/tmm.py:395-401, ``_copy_sorted`` :300)."""
+    R = _rotation_matrix(epsa[:, 0], epsa[:, 1], epsa[:, 2] - phi)
+    eps = _rotate_diagonal_tensor(R, eps0)
+    L = _auxiliary_matrix(beta, eps)
+    a0, F0 = np.linalg.eig(L)
+    n = beta.shape[0]
+    alpha = np.empty((n, 4), CDTYPE)
+    F = np.empty((n, 4, 4), CDTYPE)
+    p = _poynting_columns(F0)
+    for m in range(n):
+        i, j, ok = 0, 1, True
+        for k in range(4):
+            if p[m, k] >= 0.0:
+                if i >= 4:
+                    ok = False
+                if ok:
+                    alpha[m, i] = a0[m, k]
+                    F[m, :, i] = F0[m, :, k]
+                i += 2
+            else:
+                if j >= 4:
+                    ok = False
+                if ok:
+                    alpha[m, j] = a0[m, k]
+                    F[m, :, j] = F0[m, :, k]
+                j += 2
+        if not ok:
+            print("Could not sort eigenvectors! Proceed with caution!")
+            alpha[m] = np.nan
+            F[m] = 0.0
+    return alpha, F
+
+
+def alphaf(beta=None, phi=None, epsv=None, epsa=None):
+    """Eigenvalues alpha (..., 4) and field matrix F (..., 4, 4).
+
+    Restates ``alphaf`` (dtmm/tmm.py:435) -> ``_alphaf_vec`` (dtmm/tmm.py:372):
+    the isotropic / uniaxial / biaxial branch is chosen per element by exact
+    equality of the eps eigenvalues, the solution is found in the plane of
+    incidence (phi = 0) and rotated back by phi.
+    """
+    beta = np.asarray(0.0 if beta is None else beta, FDTYPE)
+    phi = np.asarray(0.0 if phi is None else phi, FDTYPE)
+    epsv = np.asarray((1.0, 1.0, 1.0) if epsv is None else epsv, CDTYPE)
+    epsa = np.asarray((0.0, 0.0, 0.0) if epsa is None else epsa, FDTYPE)
+    shape = np.broadcast_shapes(beta.shape, phi.shape, epsv.shape[:-1], epsa.shape[:-1])
+    b = np.broadcast_to(beta, shape).reshape(-1)
+    p = np.broadcast_to(phi, shape).reshape(-1)
+    ev = np.broadcast_to(epsv[..., :3], shape + (3,)).reshape(-1, 3)
+    ea = np.broadcast_to(epsa[..., :3], shape + (3,)).reshape(-1, 3)
+    n = b.shape[0]
+    alpha = np.empty((n, 4), CDTYPE)
+    F = np.empty((n, 4, 4), CDTYPE)
+    iso = (ev[:, 0] == ev[:, 1]) & (ev[:, 1] == ev[:, 2])
+    uni = (ev[:, 0] == ev[:, 1]) & ~iso
+    bi = ~(ev[:, 0] == ev[:, 1])
+    if iso.any():
+        alpha[iso], F[iso] = _alphaf_iso(b[iso], ev[iso, 0])
+    if uni.any():
+        R = _rotation_matrix_uniaxial(ea[uni, 1], ea[uni, 2] - p[uni])
+        alpha[uni], F[uni] = _alphaf_uniaxial(b[uni], ev[uni], R)
+    if bi.any():
+        alpha[bi], F[bi] = _alphaf_biaxial(b[bi], p[bi], ev[bi], ea[bi])
+    F = _dotr2m(rotation_vector2(p), F)
+    return alpha.reshape(shape + (4,)), F.reshape(shape + (4, 4))
+
+
+def alphaffi(beta=None, phi=None, epsv=None, epsa=None):
+    """alphaf plus the inverse field matrix (dtmm/tmm.py:466)."""
+    a, f = alphaf(beta, phi, epsv, epsa)
+    return a, f, inv(f)
+
+
+def E_mat(fmat, mode=None):
+    """E-field rows of the field matrix (dtmm/tmm.py:974).
+
+    mode +1 / -1: the 2x2 block of forward / backward modes; mode None: the
+    4x4 "Epn" matrix with the forward block at [::2, ::2] and the backward
+    block at [1::2, 1::2].
+    """
+    fmat = np.asarray(fmat)
+    if mode == +1:
+        return fmat[..., ::2, ::2].copy()
+    if mode == -1:
+        return fmat[..., ::2, 1::2].copy()
+    out = np.zeros_like(fmat)
+    out[..., ::2, ::2] = fmat[..., ::2, ::2]
+    out[..., 1::2, 1::2] = fmat[..., ::2, 1::2]
+    return out
+
+
+def E2H_mat(fmat, mode=+1):
+    """H-from-E matrix B . A^-1 of one propagation direction (dtmm/tmm.py:1051)."""
+    if mode == +1:
+        A, B = fmat[..., ::2, ::2], fmat[..., 1::2, ::2]
+    else:
+        A, B = fmat[..., ::2, 1::2], fmat[..., 1::2, 1::2]
+    return dotmm(B, inv(A))
+
+
+def phasem(alpha, kd):
+    """exp(i kd alpha) (dtmm/tmm.py:584-596)."""
+    kd = np.asarray(kd, FDTYPE)[..., None]
+    return np.exp(1j * kd * np.asarray(alpha, CDTYPE))
+
+
+def phase_mat(alpha, kd, mode=None):
+    """Phase diagonal, optionally of one direction only (dtmm/tmm.py:599)."""
+    alpha = np.asarray(alpha)
+    if mode == +1:
+        return phasem(alpha[..., ::2], kd)
+    if mode == -1:
+        return phasem(alpha[..., 1::2], kd)
+    return phasem(alpha, kd)
+
+
+def alphaEEi(beta, phi, epsv, epsa, mode=+1):
+    """2x2 E eigen-data of one direction and its inverse (dtmm/tmm.py:509-582)."""
+    alpha, f = alphaf(beta, phi, epsv, epsa)
+    e = E_mat(f, mode=mode)
+    alpha = alpha[..., ::2] if mode == 1 else alpha[..., 1::2]
+    return alpha, e, inv(e)
+
+
+# --------------------------------------------------------------------------
+# effective-medium diffraction matrices (dtmm/diffract.py, dtmm/matrix.py)
+# --------------------------------------------------------------------------
+def diffraction_alphaf(shape, ks, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), betamax=BETAMAX):
+    """Per-k eigen-data of a homogeneous layer; beta >= betamax zeroed (dtmm/diffract.py:22)."""
+    ks = np.abs(np.asarray(ks))
+    beta, phi = betaphi(shape, ks)
+    alpha, f = alphaf(beta, phi, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE))
+    mask = beta >= betamax
+    f[mask] = 0.0
+    alpha[mask] = 0.0
+    return alpha, f
+
+
+def diffraction_alphaffi(shape, ks, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), betamax=BETAMAX):
+    """diffraction_alphaf plus inverse (dtmm/diffract.py:47)."""
+    ks = np.abs(np.asarray(ks))
+    beta, phi = betaphi(shape, ks)
+    alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
+    mask = beta >= betamax
+    fi[mask] = 0.0
+    f[mask] = 0.0
+    alpha[mask] = 0.0
+    return alpha, f, fi
+
+
+def E_diffraction_alphaEEi(shape, ks, epsv=(1, 1, 1), epsa=(0.0, 0.0, 0.0), mode=+1, betamax=BETAMAX):
+    """2x2 per-k E eigen-data; beta >= betamax zeroed (dtmm/diffract.py:79)."""
+    ks = np.abs(np.asarray(ks))
+    beta, phi = betaphi(shape, ks)
+    alpha, j, ji = alphaEEi(beta, phi, epsv, epsa, mode=mode)
+    mask = beta >= betamax
+    ji[mask] = 0.0
+    j[mask] = 0.0
+    alpha[mask] = 0.0
+    return alpha, j, ji
+
+
+def phase_matrix(alpha, kd, mode=None):
+    """Phase diagonal with optional direction mask (dtmm/diffract.py:113)."""
+    kd = np.asarray(kd, FDTYPE)
+    out = phase_mat(alpha, kd[..., None, None])
+    if mode in ("t", +1):
+        out[..., 1::2] = 0.0
+    elif mode in ("r", -1):
+        out[..., ::2] = 0.0
+    return out
+
+
+def tr_mat(fmatin, fmatout, fmatini=None, mode=+1):
+    """2x2 interface transmission / reflection matrices (dtmm/tmm.py:925, ``Etri_mat`` :1025, ``S_mat`` :850)."""
+    if fmatini is None:
+        fmatini = inv(fmatin)
+    er = E_mat(fmatin, mode=-mode)
+    et = E_mat(fmatout, mode=mode)
+    A = E_mat(fmatin, mode=mode)
+    S = dotmm(fmatini, fmatout)
+    if mode == +1:
+        St, Sr = S[..., ::2, ::2], S[..., 1::2, 0::2]
+    else:
+        St, Sr = S[..., 1::2, 1::2], S[..., 0::2, 1::2]
+    ei = dotmm(inv(St), inv(A))
+    eri = dotmm(Sr, ei)
+    return dotmm(et, ei), dotmm(er, eri)
+
+
+def E_tr_matrix(shape, ks, epsv_in=(1.0, 1.0, 1.0), epsa_in=(0.0, 0.0, 0.0), epsv_out=(1.0, 1.0, 1.0),
+                epsa_out=(0.0, 0.0, 0.0), mode=+1, betamax=BETAMAX):
+    """Per-k Fresnel t, r matrices between two homogeneous layers (dtmm/diffract.py:215)."""
+    _, fin, fini = diffraction_alphaffi(shape, ks, epsv_in, epsa_in, betamax)
+    _, fout, _ = diffraction_alphaffi(shape, ks, epsv_out, epsa_out, betamax)
+    return tr_mat(fin, fout, fmatini=fini, mode=mode)
+
+
+def E_diffraction_matrix(shape, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1, betamax=BETAMAX):
+    """2x2 E-basis diffraction over d (dtmm/diffract.py:173)."""
+    ks = np.asarray(ks, FDTYPE)
+    alpha, j, ji = E_diffraction_alphaEEi(shape, ks, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE), mode, betamax)
+    return dotmdm(j, phase_matrix(alpha, ks * d), ji)
+
+
+def projection_matrix(shape, ks, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1, betamax=BETAMAX):
+    """Per-k projection onto forward (+1) or backward (-1) modes (dtmm/diffract.py:242)."""
+    ks = np.asarray(ks, FDTYPE)
+    alpha, f, fi = diffraction_alphaffi(shape, ks, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE), betamax)
+    pmat = phase_matrix(alpha, np.zeros_like(ks), mode=mode)
+    return dotmdm(f, pmat, fi)
+
+
+def diffract(field, dmat):
+    """fft2 -> per-k matrix -> ifft2 (dtmm/diffract.py:254)."""
+    return ifft2(dotmf(dmat, fft2(field)))
+
+
+def E_correction_matrix(beta, phi, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1):
+    """Inverse phase of the beam's own 2x2 E mode over d (dtmm/matrix.py:32)."""
+    alpha, j, ji = alphaEEi(beta, phi, epsv, epsa, mode=mode)
+    return dotmdm(j, phase_matrix(alpha, -np.asarray(ks) * d), ji)
+
+
+def first_E_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1, betamax=BETAMAX):
+    """correction . diffraction, 2x2 (dtmm/matrix.py:54)."""
+    dmat = E_diffraction_matrix(shape, ks, d, epsv, epsa, mode=mode, betamax=betamax)
+    cmat = E_correction_matrix(beta, phi, ks, d, epsv, epsa, mode=mode)
+    return dotmm(cmat, dmat)
+
+
+def second_E_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1, betamax=BETAMAX):
+    """diffraction . correction, 2x2 (dtmm/matrix.py:47)."""
+    dmat = E_diffraction_matrix(shape, ks, d, epsv, epsa, mode=mode, betamax=betamax)
+    cmat = E_correction_matrix(beta, phi, ks, d, epsv, epsa, mode=mode)
+    return dotmm(dmat, cmat)
+
+
+def first_Epn_diffraction_matrix(shape, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
+    """field -> Epn diffraction over d: E . P . F^-1 (dtmm/matrix.py:110)."""
+    ks = np.asarray(ks, FDTYPE)
+    alpha, f, fi = diffraction_alphaffi(shape, ks, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE), betamax)
+    return dotmdm(E_mat(f), phase_mat(alpha, (ks * d)[..., None, None]), fi)
+
+
+def second_Epn_diffraction_matrix(shape, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
+    """Epn -> field diffraction over d: F . P . E^-1 (dtmm/matrix.py:121)."""
+    ks = np.asarray(ks, FDTYPE)
+    alpha, f = diffraction_alphaf(shape, ks, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE), betamax)
+    return dotmdm(f, phase_mat(alpha, (ks * d)[..., None, None]), inv(E_mat(f)))
+
+
+def Epn_correction_matrix(beta, phi, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0)):
+    """Inverse phase of the beam's own Epn modes over d (dtmm/matrix.py:133)."""
+    alpha, f = alphaf(beta, phi, epsv, epsa)
+    pmat = phase_mat(alpha, (-np.asarray(ks) * d)[..., None, None])
+    e = E_mat(f)
+    return dotmdm(e, pmat, inv(e))
+
+
+def first_corrected_Epn_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
+    """(dtmm/matrix.py:142)"""
+    return dotmm(Epn_correction_matrix(beta, phi, ks, d, epsv, epsa),
+                 first_Epn_diffraction_matrix(shape, ks, d, epsv, epsa, betamax=betamax))
+
+
+def second_corrected_Epn_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
+    """(dtmm/matrix.py:160)"""
+    return dotmm(second_Epn_diffraction_matrix(shape, ks, d, epsv, epsa, betamax=betamax),
+                 Epn_correction_matrix(beta, phi, ks, d, epsv, epsa))
+
+
+# --------------------------------------------------------------------------
+# mode grouping windows (dtmm/mode.py)
+# --------------------------------------------------------------------------
+def _tent(db, typ):
+    """One axis of a tent window, open-ended at the grid edges (dtmm/mode.py:18-40)."""
+    c = 1.0 - np.abs(db)
+    neg = c < 0.0
+    c = np.where(neg, 0.0, c)
+    if typ < 0:
+        c = np.where(~neg & (db < 0), 1.0, c)
+    elif typ > 0:
+        c = np.where(~neg & (db > 0), 1.0, c)
+    return c
+
+
+def _nearest_offset(off, d):
+    """Offset folded to the nearest multiple of d (dtmm/mode.py:54-70)."""
+    a = np.mod(off, d)
+    b = np.mod(off, -d)
+    return np.where(np.abs(a) > np.abs(b), b, a)
+
+
+def fft_windows(bx, by, n, betax_off=0.0, betay_off=0.0, betamax=BETAMAX):
+    """n*n tent windows over (beta_x, beta_y) (dtmm/mode.py:52 with ``fft_window`` :11)."""
+    d = 2 * betamax / (n - 1)
+    xoff = _nearest_offset(np.asarray(betax_off, FDTYPE), d)
+    yoff = _nearest_offset(np.asarray(betay_off, FDTYPE), d)
+    ax = np.linspace(-betamax, betamax, n)
+    step = ax[1] - ax[0]
+    beta = (bx ** 2 + by ** 2) ** 0.5
+    # a per-ray offset broadcasts as an extra loop dimension in front of the
+    # grid's own loop dimensions, as in the reference's gufunc call
+    xoff_b = xoff[..., None, None]
+    yoff_b = yoff[..., None, None]
+    out = []
+    for i, cx0 in enumerate(ax):
+        xt = -1 if i == 0 else (1 if i == n - 1 else 0)
+        cx = _tent((bx - (cx0 + xoff_b)) / step, xt)
+        for j, cy0 in enumerate(ax):
+            yt = -1 if j == 0 else (1 if j == n - 1 else 0)
+            cy = _tent((by - (cy0 + yoff_b)) / step, yt)
+            coeff = np.where(beta >= betamax, 0.0, cx * cy)
+            out.append(np.where(coeff > 0.0, coeff, 0.0))
+    return np.asarray(out)
+
+
+def fft_mask(shape, ks, n, betax_off=0.0, betay_off=0.0, betamax=BETAMAX):
+    """Non-empty windows and their intensity-weighted mean beta, phi (dtmm/mode.py:104-139).
+
+    The mean is taken over every axis of the grid, wavelengths included
+    (``fft_betaxy_mean``, dtmm/mode.py:108).
+    """
+    bx, by = betaxy(shape[-2:], np.asarray(ks, FDTYPE)[..., None])
+    w = fft_windows(bx, by, n, betax_off, betay_off, betamax)
+    axis = tuple(range(-bx.ndim, 0))
+    w2 = w ** 2
+    norm = w2.sum(axis=axis)
+    sx = (bx * w2).sum(axis=axis)
+    sy = (by * w2).sum(axis=axis)
+    mask = norm > 0
+    mx = np.divide(sx, norm, where=mask, out=sx.copy())
+    my = np.divide(sy, norm, where=mask, out=sy.copy())
+    betas = (mx ** 2 + my ** 2) ** 0.5
+    phis = np.arctan2(my, mx)
+    nonzero = np.asarray([not np.all(x == 0.0) for x in w])
+    return w[nonzero], (betas[nonzero], phis[nonzero])
+
+
+# --------------------------------------------------------------------------
+# field helpers (dtmm/field.py, dtmm/transfer.py, dtmm/denoise.py)
+# --------------------------------------------------------------------------
+def field2intensity(field):
+    """z-Poynting per pixel of a (..., 4, H, W) field (dtmm/field.py:780)."""
+    f = np.asarray(field)
+    return (f[..., 0, :, :].real * f[..., 1, :, :].real + f[..., 0, :, :].imag * f[..., 1, :, :].imag) - (
+        f[..., 2, :, :].real * f[..., 3, :, :].real + f[..., 2, :, :].imag * f[..., 3, :, :].imag
+    )
+
+
+def total_intensity(field):
+    """Pixel sum of field2intensity (dtmm/transfer.py:200)."""
+    i = field2intensity(field)
+    return i.sum(axis=(-2, -1))
+
+
+def normalize_field(field, intensity_in, intensity_out):
+    """Scale each k so its intensity matches the reference, |ratio| clamped to 1 (dtmm/transfer.py:67)."""
+    intensity_in = intensity_in.copy()
+    intensity_out = intensity_out.copy()
+    m = intensity_out == 0.0
+    intensity_out[m] = 1.0
+    intensity_in[m] = 0.0
+    fact = (intensity_in / intensity_out)[..., None, :, :]
+    fact = np.abs(np.clip(fact, -1, 1))
+    return field * fact
+
+
+def project_normalized_fft(field, dmat):
+    """Project in k-space and restore each mode's intensity (dtmm/transfer.py:78, ref=None)."""
+    f1 = fft2(field)
+    i1 = field2intensity(f1)
+    f2 = dotmf(dmat, f1)
+    i2 = field2intensity(f2)
+    return ifft2(normalize_field(f2, i1, i2))
+
+
+def exp_notch_filter(x, x0, sigma):
+    """Attenuation around beta = x0 (dtmm/denoise.py:21)."""
+    return np.asarray((1 - np.exp(-np.abs(x - x0).clip(0, x0) / sigma)) / (1 - np.exp(-x0 / sigma)), FDTYPE)
+
+
+def denoise_fftfield(ffield, ks, beta, smooth):
+    """(dtmm/denoise.py:31)"""
+    b, _ = betaphi(ffield.shape[-2:], ks)
+    return ffield * exp_notch_filter(b, beta, smooth)[..., None, :, :]
+
+
+def denoise_field(field, ks, beta, smooth):
+    """(dtmm/denoise.py:24)"""
+    return ifft2(denoise_fftfield(fft2(field), ks, beta, smooth))
+
+
+def refind2eps(n):
+    """n**2 (dtmm/data.py:1065)."""
+    return np.asarray(n) ** 2
+
+
+def transmitted_field(field, ks, n=1.0, betamax=BETAMAX):
+    """Forward-propagating part of a field in medium n (dtmm/transfer.py:270)."""
+    eps = refind2eps([n] * 3)
+    pmat = projection_matrix(field.shape[-2:], ks, epsv=eps, epsa=(0.0, 0.0, 0.0), mode=+1, betamax=betamax)
+    return diffract(field, pmat)
+
+
+def reflected_field(field, ks, n=1.0, betamax=BETAMAX):
+    """Backward-propagating part of a field in medium n (dtmm/transfer.py:295)."""
+    eps = refind2eps([n] * 3)
+    pmat = projection_matrix(field.shape[-2:], ks, epsv=eps, epsa=(0.0, 0.0, 0.0), mode=-1, betamax=betamax)
+    return diffract(field, pmat)
+
+
+def blackman(shape):
+    """2D radial Blackman window (dtmm/window.py:33)."""
+    ay, ax = (np.arange(-n / 2.0 + 0.5, n / 2.0 + 0.5) for n in shape)
+    xx, yy = np.meshgrid(ax, ay, indexing="xy")
+    ny, nx = (n / 2 for n in shape)
+    r = ((xx / nx) ** 2 + (yy / ny) ** 2) ** 0.5
+    out = 0.42 + 0.5 * np.cos(np.pi * r) + 0.08 * np.cos(2 * np.pi * r)
+    out[r >= 1.0] = 0.0
+    return out
+
+
+def field2betaphi(field_in, ks, multiray=False):
+    """Mean beta, phi of a field (dtmm/field.py:492, ``mean_betaphi`` :866, ``_fft_betaphi`` :846)."""
+    f = fft2(field_in * blackman(field_in.shape[-2:]))
+    bx, by = betaxy(field_in.shape[-2:], ks)
+    s = f.real ** 2 + f.imag ** 2
+    sx = (s * bx[..., None, :, :]).sum(axis=(-3, -2, -1))
+    sy = (s * by[..., None, :, :]).sum(axis=(-3, -2, -1))
+    ss = s.sum(axis=(-3, -2, -1))
+    beta = (sx ** 2 + sy ** 2) ** 0.5 / ss
+    phi = np.arctan2(sy, sx)
+    if field_in.ndim > 4 and multiray:
+        ax = tuple(range(1, field_in.ndim - 3))
+        return beta.mean(axis=ax), phi.mean(axis=ax)
+    return beta.mean(), phi.mean()
+
+
+def _validate_betaphi(beta, phi, extendeddim=0):
+    """Broadcastable beta, phi (dtmm/transfer.py:43)."""
+    if beta is None or phi is None:
+        raise ValueError("Both beta and phi must be defined!")
+    beta = np.asarray(beta, FDTYPE)
+    phi = np.asarray(phi, FDTYPE)
+    if beta.ndim != phi.ndim:
+        raise ValueError("Beta nad phi should have same dimensions!")
+    if beta.ndim == 1:
+        if len(beta) != len(phi):
+            raise ValueError("Beta nad phi should have same length!")
+        for _ in range(extendeddim):
+            beta = beta[..., None]
+            phi = phi[..., None]
+    elif beta.ndim != 0:
+        raise ValueError("Only length 1 or scalar values are supported for beta and phi")
+    else:
+        for _ in range(extendeddim + 1):
+            beta = beta[..., None]
+            phi = phi[..., None]
+    return beta, phi
+
+
+# --------------------------------------------------------------------------
+# optical data and layer lists (dtmm/data.py, dtmm/transfer.py)
+# --------------------------------------------------------------------------
+def validate_optical_block(block, shape=None):
+    """(thickness (L,), eps (L,h,w,3), angles (L,h,w,3)) (dtmm/data.py:534, non-dispersive)."""
+    thickness, material, angles = block
+    thickness = np.asarray(thickness, FDTYPE)
+    material = np.asarray(material)
+    material = np.asarray(material, CDTYPE if np.iscomplexobj(material) else FDTYPE)
+    angles = np.asarray(angles, FDTYPE)
+    if thickness.ndim == 0:
+        thickness = thickness[None]
+        material = material[None, ...]
+        angles = angles[None, ...]
+    elif thickness.ndim != 1:
+        raise ValueError("Thickess dimension should be 1.")
+    if material.ndim == 2:
+        material = material[:, None, None, :]
+    elif material.ndim == 3:
+        material = material[:, None, :, :]
+    elif material.ndim != 4:
+        raise ValueError("Invalid material dimensions.")
+    n = len(thickness)
+    target = (n, 1, 1, 3) if shape is None else (n,) + tuple(shape) + (3,)
+    np.broadcast_shapes(material.shape, target)
+    np.broadcast_shapes(angles.shape, target)
+    return thickness, material, angles
+
+
+def validate_optical_data(data, shape=None):
+    """List of validated blocks (dtmm/data.py:645)."""
+    if isinstance(data, list):
+        if shape is None:
+            raise ValueError("For heterogeneous data, you must provide the `shape` argument.")
+        return [validate_optical_block(d, shape) for d in data]
+    warnings.warn("A single-block optical data must be a list of length 1.", DeprecationWarning)
+    return validate_optical_data([data], shape)
+
+
+def _isotropic_mean(epsv):
+    """Mean of (e0+e1+e2)/3 over every voxel (``effective_block`` symmetry 0, dtmm/data.py:1364-1392;
+    ``_uniaxial_order`` order 0, dtmm/data.py:1217)."""
+    m = (epsv[..., 0] + epsv[..., 1] + epsv[..., 2]) / 3.0
+    return np.asarray(m.mean())
+
+
+def _layers_list(block, nin, nout, nstep, is_first, is_last):
+    """Layer and effective-layer lists with the input/output media (dtmm/transfer.py:926)."""
+    d, epsv, epsa = block
+    substeps = np.broadcast_to(np.asarray(nstep), (len(d),))
+    layers = [(int(n), (t / n, ev, ea)) for n, t, ev, ea in zip(substeps, d, epsv, epsa)]
+    eps_in = refind2eps([nin] * 3)
+    eps_out = refind2eps([nout] * 3)
+    zero = np.zeros(3, FDTYPE)
+    if is_first:
+        layers.insert(0, (1, (0.0, np.broadcast_to(eps_in, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
+    if is_last:
+        layers.append((1, (0.0, np.broadcast_to(eps_out, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
+    m = _isotropic_mean(epsv)
+    ev_eff = np.asarray([m, m, m])
+    ev_eff = ev_eff.astype(CDTYPE if np.iscomplexobj(ev_eff) else FDTYPE)
+    eff = [(int(n), (t / n, ev_eff, zero)) for n, t in zip(substeps, d)]
+    if is_first:
+        eff.insert(0, (1, (0.0, eps_in, zero)))
+    if is_last:
+        eff.append((1, (0.0, eps_out, zero)))
+    return layers, eff
+
+
+def _create_layers(optical_data, nin, nout, nstep):
+    """(dtmm/transfer.py:978)"""
+    layers, eff = [], []
+    nb = len(optical_data)
+    for i, block in enumerate(optical_data):
+        l, e = _layers_list(block, nin, nout, nstep, i == 0, i == nb - 1)
+        layers += l
+        eff += e
+    return layers, eff
+
+
+# --------------------------------------------------------------------------
+# layer propagators (dtmm/propagate_4x4.py, dtmm/propagate_2x2.py)
+# --------------------------------------------------------------------------
+def _transfer_ray_4x4_1(field, ks, layer, dmat1, dmat2, beta, phi, nsteps):
+    """dmat1 -> ifft2 -> E.P.E^-1 -> fft2 -> dmat2, nsteps times (dtmm/propagate_4x4.py:80)."""
+    d, epsv, epsa = layer
+    kd = ks * d
+    alpha, f = alphaf(beta, phi, epsv, epsa)
+    p = phasem(alpha, kd[..., None, None])
+    e = E_mat(f)
+    ei = inv(e)
+    for _ in range(nsteps):
+        field = dotmf(dmat1, field)
+        field = ifft2(field)
+        field = dotmdmf(e, p, ei, field)
+        field = fft2(field)
+        field = dotmf(dmat2, field)
+    return field
+
+
+def propagate_4x4_effective_1(field, ks, layer, eff_layer, beta, phi, nsteps, diffraction, betamax):
+    """(dtmm/propagate_4x4.py:376)"""
+    d_eff, epsv_eff, epsa_eff = eff_layer
+    shape = field.shape[-2:]
+    if diffraction == 1:
+        dmat1 = first_corrected_Epn_diffraction_matrix(shape, ks, beta, phi, d_eff / 2, epsv_eff, epsa_eff, betamax)
+        dmat2 = second_corrected_Epn_diffraction_matrix(shape, ks, beta, phi, d_eff / 2, epsv_eff, epsa_eff, betamax)
+        return _transfer_ray_4x4_1(field, ks, layer, dmat1, dmat2, beta, phi, nsteps)
+    if diffraction > 1:
+        try:
+            bshape = beta.shape
+            b0, p0 = beta[..., 0], phi[..., 0]
+        except IndexError:
+            bshape = ()
+            b0, p0 = beta, phi
+        windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), b0 * np.cos(p0), b0 * np.sin(p0), betamax)
+        n = len(windows)
+        betas = betas.reshape((n,) + bshape)
+        phis = phis.reshape((n,) + bshape)
+        dm1 = first_corrected_Epn_diffraction_matrix(shape, ks, betas, phis, d_eff / 2, epsv_eff, epsa_eff, betamax)
+        dm2 = second_corrected_Epn_diffraction_matrix(shape, ks, betas, phis, d_eff / 2, epsv_eff, epsa_eff, betamax)
+        fout = np.zeros_like(field)
+        for w, b, p, m1, m2 in zip(windows, betas, phis, dm1, dm2):
+            fout = fout + _transfer_ray_4x4_1(field * w, ks, layer, m1, m2, b, p, nsteps)
+        return fout
+    raise ValueError("Invalid diffraction value")
+
+
+def _transfer_ray_2x2_1(fft_field, ks, layer, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat=None):
+    """2x2 E-only split step; ``tmat`` is the interface transmission applied
+    before the first step when reflections are on and no reflected waves are
+    tracked (dtmm/propagate_2x2.py:19-87)."""
+    d, epsv, epsa = layer
+    if tmat is not None:
+        fft_field = dotmf(tmat, fft_field)
+    alpha, fmat = alphaf(beta, phi, epsv, epsa)
+    e = E_mat(fmat, mode=mode)
+    ei = inv(e)
+    p = phase_mat(alpha, (ks * d)[..., None, None], mode=mode)
+    for _ in range(nsteps):
+        if dmat1 is not None:
+            fft_field = dotmf(dmat1, fft_field)
+        field = ifft2(fft_field)
+        field = dotmdmf(e, p, ei, field)
+        fft_field = fft2(field)
+        if dmat2 is not None:
+            fft_field = dotmf(dmat2, fft_field)
+    if mode == +1 and bulk is not None:
+        field = ifft2(fft_field)
+        e2h = E2H_mat(fmat, mode=mode)
+        bulk[..., 1::2, :, :] += dotmf(e2h, field)
+        bulk[..., ::2, :, :] += field
+    return fft_field
+
+
+def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, nsteps, diffraction, betamax, mode,
+                              bulk, reflection=0):
+    """(dtmm/propagate_2x2.py:193, no reflected-wave tracking, split_diffraction ignored)"""
+    d_out, epsv_out, epsa_out = eff_out
+    shape = field.shape[-2:]
+    tmat = None
+    if reflection:
+        tmat, _ = E_tr_matrix(shape, ks, epsv_in=eff_in[1], epsa_in=eff_in[2], epsv_out=epsv_out, epsa_out=epsa_out,
+                              mode=mode, betamax=betamax)
+    if diffraction <= 1:
+        if diffraction == 1:
+            dmat1 = first_E_diffraction_matrix(shape, ks, beta, phi, d_out / 2, epsv_out, epsa_out, mode, betamax)
+            dmat2 = second_E_diffraction_matrix(shape, ks, beta, phi, d_out / 2, epsv_out, epsa_out, mode, betamax)
+        else:
+            dmat1 = dmat2 = None
+        return _transfer_ray_2x2_1(field, ks, layer_out, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat)
+    try:
+        bshape = beta.shape
+        b0, p0 = beta[..., 0], phi[..., 0]
+    except IndexError:
+        bshape = ()
+        b0, p0 = beta, phi
+    windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), b0 * np.cos(p0), b0 * np.sin(p0), betamax)
+    n = len(windows)
+    betas = betas.reshape((n,) + bshape)
+    phis = phis.reshape((n,) + bshape)
+    dm1 = first_E_diffraction_matrix(shape, ks, betas, phis, d_out / 2, epsv_out, epsa_out, mode, betamax)
+    dm2 = second_E_diffraction_matrix(shape, ks, betas, phis, d_out / 2, epsv_out, epsa_out, mode, betamax)
+    fout = np.zeros_like(field)
+    for w, b, p, m1, m2 in zip(windows, betas, phis, dm1, dm2):
+        fout = fout + _transfer_ray_2x2_1(field * w, ks, layer_out, m1, m2, b, p, nsteps, mode, bulk, tmat)
+    return fout
+
+
+# --------------------------------------------------------------------------
+# drivers (dtmm/transfer.py)
+# --------------------------------------------------------------------------
+def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
+                 reflection, multiray, norm, smooth, betamax, ret_bulk, out):
+    """4x4 pass x layer sweep in k-space, reflection mode 1 (dtmm/transfer.py:618-884)."""
+    if reflection not in (1, 2, 3, 4):
+        raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
+    if reflection != 1:
+        raise NotImplementedError("oracle covers 4x4 reflection mode 1")
+    if smooth < 0:
+        smooth = 0.0
+    if norm != DTMM_NORM_FFT:
+        raise NotImplementedError("oracle covers norm=DTMM_NORM_FFT")
+    field_in, wavelengths, pixelsize = field_data
+    shape = field_in.shape[-2:]
+    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
+    ks = k0(wavelengths, pixelsize)
+    n = len(layers)
+    if beta is None and phi is None:
+        beta, phi = field2betaphi(field_in, ks, multiray)
+    beta, phi = _validate_betaphi(beta, phi, extendeddim=field_in.ndim - 2)
+    if out is None:
+        if ret_bulk:
+            bulk_out = np.zeros((n,) + field_in.shape, CDTYPE)
+            bulk_out[0] = field_in
+            field_in = bulk_out[0]
+            field_out = bulk_out[-1]
+        else:
+            bulk_out = None
+            field_out = np.zeros_like(field_in)
+    else:
+        if ret_bulk:
+            bulk_out = out
+            bulk_out[0] = field_in
+            field_in = bulk_out[0]
+            field_out = bulk_out[-1]
+        else:
+            bulk_out = None
+            field_out = out
+        field_out[...] = reflected_field(field_out, ks, n=nin, betamax=betamax)
+    indices = list(range(1, n - 1))
+    field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
+    field = field_in.copy()
+    i0 = field2intensity(field0).sum(axis=(-2, -1))
+    if not (0 <= diffraction < np.inf):
+        raise NotImplementedError("oracle covers finite diffraction")
+    field = fft2(field)
+    if npass > 1:
+        pin_mat = projection_matrix(shape, ks, epsv=refind2eps([nin] * 3), mode=+1, betamax=betamax)
+        pout_mat = projection_matrix(shape, ks, epsv=refind2eps([nout] * 3), mode=+1, betamax=betamax)
+    for i in range(npass):
+        direction = (-1) ** i
+        for j in indices:
+            nsub, (thickness, ev, ea) = layers[j]
+            _, (de, ee, ae) = eff_layers[j]
+            field = propagate_4x4_effective_1(field, ks, (thickness * direction, ev, ea), (de * direction, ee, ae),
+                                              beta, phi, nsub, diffraction, betamax)
+            if bulk_out is not None:
+                bulk_out[j] = field
+        indices.reverse()
+        field = ifft2(field)
+        if npass > 1:
+            if i % 2 == 0:
+                if i == 0:
+                    field = field - field_out
+                if i != npass - 1:
+                    sigma = smooth * (npass - i) / npass
+                    field = project_normalized_fft(field, pout_mat)
+                    field = denoise_field(field, ks, nin, sigma)
+                field_out[...] = field_out + field
+                field = field_out.copy()
+            else:
+                field_in[...] = field
+                if i != npass - 1:
+                    sigma = smooth * (npass - i) / npass
+                    ff = dotmf(pin_mat, fft2(field))
+                    ff = denoise_fftfield(ff, ks, nin, sigma)
+                    field = ifft2(ff)
+                    i0f = total_intensity(field)
+                    fact = (i0 / i0f)[..., None, None, None]
+                    field = field * fact
+                    field_out[...] = field_out * fact
+                    field_in[...] = field_in * fact
+                    field = field0 - field
+                    field_in[...] = field_in + field
+            field = fft2(field)
+        else:
+            field_out[...] = field
+    if ret_bulk:
+        bulk_out[1:-1] = ifft2(bulk_out[1:-1])
+        return bulk_out, wavelengths, pixelsize
+    return field_out, wavelengths, pixelsize
+
+
+def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
+                 reflection, multiray, betamax, ret_bulk, out):
+    """2x2 interface sweep in k-space, one pass (dtmm/transfer.py:1009-1183)."""
+    if reflection not in (0, 1, 2):
+        raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
+    if reflection not in (0, 1) or npass != 1:
+        raise NotImplementedError("oracle covers 2x2 with reflection 0/1 and npass 1")
+    if ret_bulk:
+        raise NotImplementedError("oracle covers ret_bulk for 4x4 only")
+    field_in, wavelengths, pixelsize = field_data
+    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
+    ks = k0(wavelengths, pixelsize)
+    n = len(layers) - 1
+    if beta is None and phi is None:
+        beta, phi = field2betaphi(field_in, ks, multiray)
+    beta, phi = _validate_betaphi(beta, phi, extendeddim=field_in.ndim - 2)
+    if out is None:
+        field_out = np.zeros_like(field_in)
+    else:
+        out[...] = 0.0
+        field_out = out
+    if not (0 < diffraction < np.inf):
+        raise NotImplementedError("oracle covers 0 < diffraction < inf for 2x2")
+    field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
+    field = fft2(field0[..., ::2, :, :])
+    for j in range(n):
+        jout = j + 1
+        nsub, (thickness, ev, ea) = layers[jout]
+        _, eff_in = eff_layers[j]
+        _, (de, ee, ae) = eff_layers[jout]
+        bulk = field_out if jout == n else None
+        field = propagate_2x2_effective_1(field, ks, (thickness, ev, ea), eff_in, (de, ee, ae), beta, phi, nsub,
+                                          diffraction, betamax, +1, bulk, reflection)
+    return field_out, wavelengths, pixelsize
+
+
+def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout=None, npass=None, nstep=1,
+                   diffraction=None, reflection=None, method=None, multiray=False, norm=DTMM_NORM_FFT,
+                   betamax=None, smooth=SMOOTH, split_rays=False, split_diffraction=False,
+                   split_wavelengths=False, split_layers=False, eff_data=None, ret_bulk=False, out=None):
+    """Restates ``transfer_field`` (dtmm/transfer.py:322-552) for the covered options."""
+    opt = lambda name, v: DEFAULTS[name] if v is None else v
+    nin, nout = opt("nin", nin), opt("nout", nout)
+    method, npass = opt("method", method), opt("npass", npass)
+    eff_data = opt("eff_data", eff_data)
+    diffraction, reflection = opt("diffraction", diffraction), opt("reflection", reflection)
+    betamax = opt("betamax", betamax)
+    if eff_data not in (0, "isotropic"):
+        raise NotImplementedError("oracle covers isotropic effective data")
+    if split_rays or split_wavelengths or split_layers:
+        raise NotImplementedError("oracle covers unsplit transfer")
+    if method == "4x4" and npass > 1 and diffraction == False:  # noqa: E712
+        warnings.warn("The 4x4 method with diffraction disabled is not yet supported for input fields with beta >0.")
+    if npass == -1 or npass == np.inf:
+        raise NotImplementedError("oracle covers finite npass")
+    if reflection is None:
+        reflection = 0 if method == "2x2" else 1
+        if method == "4x4" and diffraction == 0:
+            reflection = 2
+        if npass > 1:
+            reflection = 1
+            if diffraction > 1 and method == "2x2":
+                reflection = 2
+    field_in, wavelengths, pixelsize = field_data
+    od = validate_optical_data(optical_data, shape=field_in.shape[-2:])
+    if method == "4x4":
+        return transfer_4x4((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
+                            diffraction, reflection, multiray, norm, smooth, betamax, ret_bulk, out)
+    return transfer_2x2((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
+                        diffraction, reflection, multiray, betamax, ret_bulk, out)

@@ -1,0 +1,124 @@
+"""Case records of the golden transfer_field fixtures.
+
+Each case fixes the grid, wavelengths, material generator and seed, the
+illumination and the ``transfer_field`` keyword arguments.  ``build_inputs``
+rebuilds ``(field_data, optical_data)`` for a case with a given
+``illumination_data`` implementation (the reference's when generating the
+fixtures, the product's or the fixture's stored field when testing).
+"""
+import numpy as np
+
+from dtmm_gb300 import samples
+
+
+def _twisted(shape, nlayers, seed, **kw):
+    return samples.twisted_nematic(shape, nlayers, seed=seed, **kw)
+
+
+def _absorbing(shape, nlayers, seed):
+    d, _, epsa = samples.twisted_nematic(shape, nlayers, seed=seed, amplitude=0.3)
+    epsv = np.broadcast_to(np.asarray((2.25 + 0.04j, 2.25 + 0.04j, 2.89 + 0.09j)), epsa.shape)
+    return d, epsv, epsa
+
+
+def _mixed_voxels(shape, nlayers, seed):
+    """Isotropic and uniaxial voxels side by side, plus an isotropic layer."""
+    d, epsv, epsa = samples.twisted_nematic(shape, nlayers, seed=seed, amplitude=0.3)
+    epsv = np.array(epsv)
+    rng = np.random.Generator(np.random.PCG64(seed + 3))
+    kind = rng.integers(0, 3, size=epsv.shape[:-1])
+    epsv[kind == 0] = (2.3, 2.3, 2.3)
+    epsv[kind == 2] = (2.4, 2.4, 2.6)
+    epsv[0] = (2.2, 2.2, 2.2)
+    return d, epsv, epsa
+
+
+MATERIALS = {
+    "twisted": _twisted,
+    "inplane": lambda shape, nlayers, seed, **kw: samples.inplane_nematic(shape, nlayers, seed=seed, **kw),
+    "absorbing": _absorbing,
+    "mixed": _mixed_voxels,
+}
+
+CASES = {
+    # BASELINE config 0 at full size: 64x64, 20 layers, 550 nm, 100 nm pixels
+    "cfg0_4x4": dict(shape=(64, 64), nlayers=20, wavelengths=[550.0], pixelsize=100.0,
+                     material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.2)), seed=0,
+                     illum=dict(jones=(1, 0)),
+                     transfer=dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)),
+    # BASELINE config 1 options (4x4, diffraction 3, npass 3, both polarisations) on a small grid
+    "cfg1_small": dict(shape=(24, 30), nlayers=4, wavelengths=[400.0, 600.0], pixelsize=50.0,
+                       material=("twisted", dict(no=1.52, ne=1.71, amplitude=0.3)), seed=1,
+                       illum=dict(),
+                       transfer=dict(method="4x4", diffraction=3, npass=3, beta=0.0, phi=0.0)),
+    # BASELINE config 3 options (2x2, diffraction 5, no reflection) on a small grid
+    "cfg3_small": dict(shape=(30, 24), nlayers=4, wavelengths=[450.0, 550.0, 650.0], pixelsize=100.0,
+                       material=("inplane", dict(no=1.5, ne=1.6)), seed=3,
+                       illum=dict(),
+                       transfer=dict(method="2x2", diffraction=5, reflection=0, beta=0.0, phi=0.0)),
+    "twox2_d1_offaxis": dict(shape=(20, 28), nlayers=6, wavelengths=[500.0, 600.0], pixelsize=100.0,
+                             material=("twisted", dict()), seed=4,
+                             illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                             transfer=dict(method="2x2", diffraction=1, beta=0.1, phi=0.3)),
+    "twox2_d3_offaxis": dict(shape=(20, 24), nlayers=3, wavelengths=[520.0], pixelsize=100.0,
+                             material=("twisted", dict()), seed=5,
+                             illum=dict(beta=0.2, phi=0.3),
+                             transfer=dict(method="2x2", diffraction=3, beta=0.2, phi=0.3)),
+    "fourx4_offaxis_npass2": dict(shape=(16, 20), nlayers=3, wavelengths=[500.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=6,
+                                  illum=dict(beta=0.15, phi=0.7, jones=(1, 0.5j)),
+                                  transfer=dict(method="4x4", diffraction=1, npass=2, beta=0.15, phi=0.7)),
+    "fourx4_d3_offaxis": dict(shape=(18, 16), nlayers=3, wavelengths=[520.0, 640.0], pixelsize=80.0,
+                              material=("twisted", dict()), seed=7,
+                              illum=dict(beta=0.1, phi=0.4, jones=(0, 1)),
+                              transfer=dict(method="4x4", diffraction=3, beta=0.1, phi=0.4)),
+    "fourx4_multiray": dict(shape=(16, 16), nlayers=3, wavelengths=[520.0, 620.0], pixelsize=100.0,
+                            material=("twisted", dict()), seed=8,
+                            illum=dict(beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0], jones=(1, 0)),
+                            transfer=dict(method="4x4", diffraction=1, multiray=True,
+                                          beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0])),
+    "fourx4_autobeta": dict(shape=(16, 18), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                            material=("twisted", dict()), seed=9,
+                            illum=dict(beta=0.1, phi=0.2, jones=(1, 0)),
+                            transfer=dict(method="4x4", diffraction=1)),
+    "fourx4_absorbing": dict(shape=(16, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                             material=("absorbing", dict()), seed=11,
+                             illum=dict(beta=0.05, jones=(1, 0)),
+                             transfer=dict(method="4x4", diffraction=1, beta=0.05, phi=0.0)),
+    "fourx4_mixed_voxels": dict(shape=(14, 16), nlayers=3, wavelengths=[600.0], pixelsize=100.0,
+                                material=("mixed", dict()), seed=12,
+                                illum=dict(beta=0.1, phi=1.0, jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, beta=0.1, phi=1.0)),
+    "fourx4_nstep2": dict(shape=(16, 16), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                          material=("twisted", dict(thickness=2.0)), seed=13,
+                          illum=dict(jones=(1, 0)),
+                          transfer=dict(method="4x4", diffraction=1, nstep=2, beta=0.0, phi=0.0)),
+    "fourx4_d3_nstep2": dict(shape=(16, 16), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                             material=("twisted", dict(thickness=2.0)), seed=14,
+                             illum=dict(jones=(1, 0)),
+                             transfer=dict(method="4x4", diffraction=3, nstep=2, beta=0.0, phi=0.0)),
+    "fourx4_bulk": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                        material=("twisted", dict()), seed=15,
+                        illum=dict(jones=(1, 0)),
+                        transfer=dict(method="4x4", diffraction=1, beta=0.0, phi=0.0, ret_bulk=True)),
+    "default_method": dict(shape=(16, 16), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                           material=("twisted", dict()), seed=16,
+                           illum=dict(jones=(1, 0)),
+                           transfer=dict(beta=0.0, phi=0.0)),
+    "fourx4_nin_nout": dict(shape=(16, 16), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                            material=("twisted", dict()), seed=17,
+                            illum=dict(jones=(1, 0), n=1.0),
+                            transfer=dict(method="4x4", diffraction=1, npass=3, nin=1.0, nout=1.33,
+                                          betamax=0.9, beta=0.0, phi=0.0)),
+}
+
+
+def build_optical_data(case):
+    kind, kw = case["material"]
+    return [MATERIALS[kind](case["shape"], case["nlayers"], case["seed"], **kw)]
+
+
+def build_inputs(case, illumination_data):
+    illum = dict(case["illum"])
+    field_data = illumination_data(case["shape"], case["wavelengths"], pixelsize=case["pixelsize"], **illum)
+    return field_data, build_optical_data(case)

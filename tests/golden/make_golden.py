@@ -1,0 +1,96 @@
+"""Generate the golden transfer_field fixtures from the unmodified reference.
+
+Run in the build container (where the reference tree is present):
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py cfg0_4x4   # one case
+
+Each case builds its inputs with the reference's own ``illumination_data``
+and the seeded director generators of ``dtmm_gb300.samples``, runs
+``dtmm.transfer_field`` (complex128, numba replaced by a pure-Python stand-in,
+see ``refload.py``) and stores ``field_in``, the returned field and, for
+npass > 1, the reference's in-place update of ``field_in`` as
+``tests/golden/<case>.npz``.  The optical data is not stored: the case
+record (``CASES`` below) rebuilds it deterministically from its seed.
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from golden_cases import CASES, build_inputs  # noqa: E402
+
+
+def run_case(name, dtmm):
+    case = CASES[name]
+    field_data, optical_data = build_inputs(case, dtmm.illumination_data)
+    field_in = field_data[0]
+    saved_in = field_in.copy()
+    kwargs = dict(case["transfer"])
+    t0 = time.time()
+    out = dtmm.transfer_field(field_data, optical_data, **kwargs)
+    dt = time.time() - t0
+    field_out = out[0]
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        field_in=saved_in,
+        field_out=np.asarray(field_out),
+        field_in_after=field_in,
+        wavelengths=np.asarray(field_data[1]),
+        pixelsize=np.asarray(field_data[2]),
+    )
+    print("%-22s %6.1fs  out %s" % (name, dt, np.asarray(field_out).shape))
+
+
+def save_wave_kat(dtmm):
+    """Known-answer k-grid maps held by the reference's own tests (dtmm/test/test_wave.py:21-69)."""
+    import importlib
+
+    tw = importlib.import_module("dtmm.test.test_wave")
+    t = tw.TestWave("test_betaphi")
+    t.setUp()
+    np.savez_compressed(os.path.join(HERE, "kat_wave.npz"), shape=np.asarray(t.shape), ks=np.asarray(t.ks, float),
+                        beta=t.beta, phi=t.phi, betax=t.betax, betay=t.betay)
+    print("kat_wave               shape %s ks %s" % (t.shape, t.ks))
+
+
+def save_alphaf_kat(dtmm):
+    """Reference alphaf / inv / E_mat on random uniaxial and isotropic voxels, both beta branches."""
+    rng = np.random.Generator(np.random.PCG64(1234))
+    n = 64
+    beta = rng.uniform(0.0, 0.8, n)
+    beta[:8] = 0.0
+    phi = rng.uniform(-np.pi, np.pi, n)
+    no = rng.uniform(1.3, 1.7, n)
+    ne = no + rng.uniform(-0.2, 0.3, n)
+    ne[8:16] = no[8:16]
+    epsv = np.stack([no ** 2, no ** 2, ne ** 2], axis=-1).astype(np.complex128)
+    epsv[16:24] = epsv[16:24] + np.asarray([0.02j, 0.02j, 0.05j])
+    epsa = np.stack([np.zeros(n), rng.uniform(0, np.pi, n), rng.uniform(-np.pi, np.pi, n)], axis=-1)
+    alpha, f = dtmm.tmm.alphaf(beta, phi, epsv, epsa)
+    fi = dtmm.linalg.inv(f)
+    np.savez_compressed(os.path.join(HERE, "kat_alphaf.npz"), beta=beta, phi=phi, epsv=epsv, epsa=epsa,
+                        alpha=alpha, f=f, fi=fi)
+    print("kat_alphaf             %d voxels" % n)
+
+
+def main(argv):
+    import refload
+
+    dtmm = refload.load_reference()
+    names = argv[1:] or (["kat"] + list(CASES))
+    for name in names:
+        if name == "kat":
+            save_wave_kat(dtmm)
+            save_alphaf_kat(dtmm)
+        else:
+            run_case(name, dtmm)
+
+
+if __name__ == "__main__":
+    main(sys.argv)
