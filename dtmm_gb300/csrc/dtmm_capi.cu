@@ -1,0 +1,623 @@
+// Host orchestration of one transfer_field call on the GPU, exported through
+// the C ABI declared in include/dtmm_gb300.h.
+//
+// One call enqueues, on the caller's stream:
+//   set-up      : FFT tables, effective medium, window statistics/tables
+//   per pass    : k-space entry table, then per (sub)layer a fused column
+//                 kernel and a fused row kernel, then the k-space exit table
+//   between passes (4x4, npass > 1): projection / normalisation / notch
+//                 filtering and the total-intensity rescale of the reference
+//                 (dtmm/transfer.py:815-873)
+// No host synchronisation happens inside the call; all scratch lives in the
+// caller's workspace.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dtmm_gb300.h"
+#include "dtmm_kernels.cuh"
+
+using namespace dtmm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(DTMM_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+#define CKL(what)                                                                                    \
+  do {                                                                                               \
+    cudaError_t e_ = cudaGetLastError();                                                             \
+    if (e_ != cudaSuccess) return fail(DTMM_ECUDA, "launch %s: %s", what, cudaGetErrorString(e_)); \
+  } while (0)
+
+bool make_plan(int n, FFTPlan& p) {
+  p.n = n;
+  p.nr = 0;
+  int m = n;
+  while (m % 4 == 0 && p.nr < 14) { p.r[p.nr++] = 4; m /= 4; }
+  while (m % 2 == 0 && p.nr < 14) { p.r[p.nr++] = 2; m /= 2; }
+  const int odd[3] = {3, 5, 7};
+  for (int q : odd)
+    while (m % q == 0 && p.nr < 14) { p.r[p.nr++] = q; m /= q; }
+  return m == 1 && n >= 1;
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Workspace layout (byte offsets), shared by the size query and the call.
+struct Layout {
+  int C;        // state components (4 or 2)
+  int ny, nx, nwin;
+  int nlay_sub; // total sub-steps
+  bool cache_ops;
+  size_t cplx;  // bytes of one complex
+  size_t HW;
+  size_t small, twH, permH, twW, permW, cx, cy, kfirst, klast, kdiag, pin, pout;
+  size_t F, X, U, field0, op;
+  size_t op_one;  // bytes of one layer's operators
+  size_t total;
+};
+
+int check_desc(const dtmm_transfer_desc* d) {
+  if (d == nullptr) return fail(DTMM_EINVAL, "null descriptor");
+  if (d->height < 1 || d->width < 1) return fail(DTMM_EINVAL, "grid must be at least 1x1");
+  if (d->height > 16384 || d->width > 16384) return fail(DTMM_ENOTSUP, "grid side above 16384");
+  if (d->nlam < 1 || d->npol < 1 || d->nray < 1) return fail(DTMM_EINVAL, "empty image axes");
+  if (d->method != 4 && d->method != 2) return fail(DTMM_EINVAL, "method must be 4 (4x4) or 2 (2x2)");
+  if (d->diffraction < 1) return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path");
+  if (d->method == 4 && d->reflection != 1) return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1 on this path");
+  if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
+    return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
+  if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
+  if (d->method == 2 && d->npass != 1) return fail(DTMM_ENOTSUP, "2x2 supports npass = 1 on this path");
+  if (d->precision != DTMM_PRECISION_MIXED && d->precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "unknown precision");
+  if (d->nlayers < 1) return fail(DTMM_EINVAL, "no layers");
+  if (!d->thickness || !d->nstep || !d->ks || !d->beta || !d->phi) return fail(DTMM_EINVAL, "null host array");
+  if (!d->epsv || !d->epsa) return fail(DTMM_EINVAL, "null material pointer");
+  for (int l = 0; l < d->nlayers; ++l)
+    if (d->nstep[l] < 1) return fail(DTMM_EINVAL, "nstep must be >= 1");
+  if (d->diffraction > 1)
+    for (int l = 0; l < d->nlayers; ++l)
+      if (d->nstep[l] != 1) return fail(DTMM_ENOTSUP, "nstep > 1 with diffraction > 1 is not supported on this path");
+  FFTPlan p;
+  if (!make_plan(d->height, p) || !make_plan(d->width, p))
+    return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", d->height, d->width);
+  if (d->betamax <= 0) return fail(DTMM_EINVAL, "betamax must be > 0");
+  return DTMM_OK;
+}
+
+Layout layout_of(const dtmm_transfer_desc* d) {
+  Layout L{};
+  const size_t H = d->height, W = d->width;
+  const size_t NI = (size_t)d->nray * d->npol * d->nlam;
+  L.HW = H * W;
+  L.C = d->method == 4 ? 4 : 2;
+  L.cplx = d->precision == DTMM_PRECISION_DOUBLE ? 16 : 8;
+  const size_t rsz = L.cplx / 2;
+  const int n = d->diffraction;
+  L.nx = L.ny = n > 1 ? n : 1;
+  L.nwin = L.nx * L.ny;
+  L.nlay_sub = 0;
+  for (int l = 0; l < d->nlayers; ++l) L.nlay_sub += d->nstep[l];
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  const size_t nrw = (size_t)d->nray * L.nwin;
+  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 3 * nrw + 4 + 3 * NI + 8));
+  L.twH = take(L.cplx * H);
+  L.permH = take(sizeof(int) * H);
+  L.twW = take(L.cplx * W);
+  L.permW = take(sizeof(int) * W);
+  L.cx = take(rsz * d->nray * L.nx * d->nlam * W);
+  L.cy = take(rsz * d->nray * L.ny * d->nlam * H);
+  const size_t kt = (size_t)d->nlam * L.HW;
+  L.kfirst = take(L.cplx * kt * 16);
+  L.klast = take(L.cplx * kt * (16 > 8 * (size_t)d->nray ? 16 : 8 * (size_t)d->nray));
+  L.kdiag = take(L.cplx * kt * 2);
+  const bool passes = d->method == 4 && d->npass > 1;
+  L.pin = take(passes ? L.cplx * kt * 16 : 0);
+  L.pout = take((passes || d->method == 4) ? L.cplx * kt * 16 : 0);
+  const size_t field = L.cplx * NI * 4 * L.HW;
+  L.F = take(field);
+  L.X = take(field);
+  L.U = take(field * (size_t)(L.ny > 1 ? L.ny : 1));
+  L.field0 = take(passes ? field : 0);
+  L.op_one = L.cplx * nrw * OP_REC * L.HW;
+  const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
+  L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
+  L.op = take(L.op_one * (L.cache_ops ? (size_t)d->nlayers : 1));
+  L.total = off;
+  return L;
+}
+
+// host-side window offsets: the beam offset folded to the nearest multiple of
+// the window spacing (dtmm/mode.py:54-70)
+double fold(double off, double d) {
+  double a = std::fmod(off, d);
+  if (a != 0.0 && ((a < 0) != (d < 0))) a += d;  // numpy.mod sign convention
+  double b = std::fmod(off, -d);
+  if (b != 0.0 && ((b < 0) != (-d < 0))) b += -d;
+  return std::fabs(a) > std::fabs(b) ? b : a;
+}
+
+template <typename R>
+struct Engine {
+  const dtmm_transfer_desc& d;
+  const dtmm_transfer_io& io;
+  const Layout& L;
+  unsigned char* ws;
+  cudaStream_t st;
+  Grid g;
+  FFTPlan pH, pW;
+  int NI;
+
+  cpx<R>* P(size_t off) const { return (cpx<R>*)(ws + off); }
+  template <typename T>
+  T* A(size_t off) const { return (T*)(ws + off); }
+
+  // small area: ks | beta | phi | xoff | yoff | wbeta | wphi | wzero(int) | eps_eff(2) | i0 | i0f | fact
+  double* ks() const { return A<double>(L.small); }
+  double* rbeta() const { return ks() + d.nlam; }
+  double* rphi() const { return rbeta() + d.nray; }
+  double* xoff() const { return rphi() + d.nray; }
+  double* yoff() const { return xoff() + d.nray; }
+  double* wbeta() const { return yoff() + d.nray; }
+  double* wphi() const { return wbeta() + (size_t)d.nray * L.nwin; }
+  int* wzero() const { return (int*)(wphi() + (size_t)d.nray * L.nwin); }
+  double* epseff() const { return (double*)(wzero()) + (size_t)d.nray * L.nwin; }
+  double* i0() const { return epseff() + 4; }
+  double* i0f() const { return i0() + NI; }
+  double* fact() const { return i0f() + NI; }
+
+  int launch_rows(cpx<R>* data, int C, bool inv, double scale) {
+    const int nlines = NI * C * d.height;
+    int lpb = 4096 / d.width;
+    if (lpb < 1) lpb = 1;
+    if (lpb > 16) lpb = 16;
+    const size_t smem = (size_t)lpb * d.width * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
+    const int blocks = (nlines + lpb - 1) / lpb;
+    if (inv) {
+      CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_fft_rows<R, true><<<blocks, 256, smem, st>>>(data, nlines, d.width, pW, P(L.twW), A<int>(L.permW), scale, lpb);
+    } else {
+      CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_fft_rows<R, false><<<blocks, 256, smem, st>>>(data, nlines, d.width, pW, P(L.twW), A<int>(L.permW), scale, lpb);
+    }
+    CKL("k_fft_rows");
+    return DTMM_OK;
+  }
+
+  int tile_cols(int cm, bool two) const {
+    const size_t per = (size_t)cm * d.height * sizeof(cpx<R>) * (two ? 2 : 1);
+    int tc = 1;
+    while (tc < 16 && per * (tc * 2) <= 72 * 1024) tc *= 2;
+    if (tc > d.width) tc = d.width;
+    return tc;
+  }
+
+  int launch_col(const cpx<R>* in, cpx<R>* out, int cin, int cout, int kop, const void* ktab, int ny,
+                 const R* cy, bool do_fwd, bool inverse_out, double scale, size_t ktab_ray_stride = 0) {
+    ColParams p;
+    p.ktab_ray_stride = ktab_ray_stride;
+    p.cin = cin;
+    p.cout = cout;
+    p.kop = kop;
+    p.ktab = ktab;
+    p.ny = ny;
+    p.cy = cy;
+    p.do_fwd = do_fwd;
+    p.inverse_out = inverse_out;
+    p.out_scale = scale;
+    p.plan = pH;
+    p.tw = P(L.twH);
+    p.perm = A<int>(L.permH);
+    const int cm = cin > cout ? cin : cout;
+    p.tc = tile_cols(cm, true);
+    const size_t smem = 2 * (size_t)cm * d.height * p.tc * sizeof(cpx<R>) + d.height * (sizeof(cpx<R>) + sizeof(int));
+    CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((d.width + p.tc - 1) / p.tc, NI);
+    k_layer_col<R><<<grid, 256, smem, st>>>(p, g, in, out);
+    CKL("k_layer_col");
+    return DTMM_OK;
+  }
+
+  int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const cpx<R>* op, double dir) {
+    RowParams p;
+    p.C = L.C;
+    p.nx = L.nx;
+    p.ny = L.ny;
+    p.cx = L.nx > 1 ? (const void*)A<R>(L.cx) : nullptr;
+    p.wzero = L.nwin > 1 ? wzero() : nullptr;
+    p.op = op;
+    p.ks = ks();
+    p.dir = dir;
+    p.in_scale = 1.0 / ((double)d.width * (double)d.height);
+    p.plan = pW;
+    p.tw = P(L.twW);
+    p.perm = A<int>(L.permW);
+    p.identity_op = 0;
+    const size_t smem = (size_t)(2 * d.npol + 1) * L.C * d.width * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
+    CK(cudaFuncSetAttribute(k_layer_row<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int threads = d.width < 256 ? ((d.width + 31) / 32) * 32 : 256;
+    dim3 grid(d.height, d.nray * d.nlam);
+    k_layer_row<R><<<grid, threads, smem, st>>>(p, g, Ub, Xb);
+    CKL("k_layer_row");
+    return DTMM_OK;
+  }
+
+  int launch_ktab(int what, double dd, cpx<R>* tab, int proj_mode = 1, double eps_re = 0, double eps_im = 0,
+                  bool eff = true) {
+    KTabParams p;
+    memset(&p, 0, sizeof(p));
+    p.what = what;
+    p.proj_mode = proj_mode;
+    p.eps_dev = eff ? epseff() : nullptr;
+    p.eps = mk<double>(eps_re, eps_im);
+    p.d = dd;
+    p.betamax = d.betamax;
+    p.ks = ks();
+    p.with_t = d.reflection ? 1 : 0;
+    p.eps_in = mk<double>(d.nin * d.nin, 0.0);
+    p.eps_out = mk<double>(d.nout * d.nout, 0.0);
+    p.eps_p = mk<double>(d.nin * d.nin, 0.0);
+    p.nwin_axis = L.nx;
+    p.wbeta = wbeta();
+    p.wphi = wphi();
+    p.wzero = wzero();
+    p.win = winp();
+    const int n = d.nlam * d.height * d.width;
+    // the 2x2 exit table depends on the ray's windows: one slab per ray
+    const int rays = (what == KT_2OUT) ? d.nray : 1;
+    for (int r = 0; r < rays; ++r) {
+      p.ray = r;
+      k_ktab<R><<<(n + 127) / 128, 128, 0, st>>>(p, g, tab + (size_t)r * n * 8);
+      CKL("k_ktab");
+    }
+    return DTMM_OK;
+  }
+
+  WinParams winp() const {
+    WinParams w;
+    w.n = d.diffraction;
+    w.betamax = d.betamax;
+    w.step = 0;
+    if (d.diffraction > 1) {
+      // numpy.linspace(-betamax, betamax, n): step = ax[1] - ax[0]
+      const double st = (2.0 * d.betamax) / (d.diffraction - 1);
+      const double a0 = -d.betamax, a1 = -d.betamax + 1 * st;
+      w.step = (d.diffraction - 1 == 1) ? (d.betamax - a0) : (a1 - a0);
+    }
+    w.xoff = xoff();
+    w.yoff = yoff();
+    w.ks = ks();
+    return w;
+  }
+
+  int voxel_ops(int layer, double dsub, cpx<R>* op) {
+    OpParams p;
+    memset(&p, 0, sizeof(p));
+    p.eps_dev = epseff();
+    p.epsv = d.epsv;
+    p.epsa = d.epsa;
+    for (int i = 0; i < 3; ++i) {
+      p.ev_s[i] = d.epsv_strides[i];
+      p.ea_s[i] = d.epsa_strides[i];
+    }
+    p.eps_complex = d.eps_complex;
+    p.layer = layer;
+    p.d = dsub;
+    p.wbeta = wbeta();
+    p.wphi = wphi();
+    p.nwin = L.nwin;
+    p.four = d.method == 4;
+    dim3 grid((unsigned)((L.HW + 127) / 128), d.nray * L.nwin);
+    k_voxel_op<R><<<grid, 128, 0, st>>>(p, g, op);
+    CKL("k_voxel_op");
+    return DTMM_OK;
+  }
+
+  int setup() {
+    // host scalars -> workspace
+    std::vector<double> h(d.nlam + 4 * d.nray);
+    for (int i = 0; i < d.nlam; ++i) h[i] = d.ks[i];
+    const double dwin = d.diffraction > 1 ? 2.0 * d.betamax / (d.diffraction - 1) : 1.0;
+    for (int r = 0; r < d.nray; ++r) {
+      h[d.nlam + r] = d.beta[r];
+      h[d.nlam + d.nray + r] = d.phi[r];
+      h[d.nlam + 2 * d.nray + r] = fold(d.beta[r] * std::cos(d.phi[r]), dwin);
+      h[d.nlam + 3 * d.nray + r] = fold(d.beta[r] * std::sin(d.phi[r]), dwin);
+    }
+    CK(cudaMemcpyAsync(ks(), h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st));
+    // FFT tables
+    k_fft_tables<R><<<(d.height + 255) / 256, 256, 0, st>>>(pH, P(L.twH), A<int>(L.permH));
+    CKL("k_fft_tables");
+    k_fft_tables<R><<<(d.width + 255) / 256, 256, 0, st>>>(pW, P(L.twW), A<int>(L.permW));
+    CKL("k_fft_tables");
+    // effective medium
+    k_eps_mean<<<1, 1024, 0, st>>>(d.epsv, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
+                                   d.nlayers, d.height, d.width, epseff());
+    CKL("k_eps_mean");
+    // windows
+    if (d.diffraction > 1) {
+      WinParams w = winp();
+      dim3 gs(L.nwin, d.nray);
+      k_window_stats<<<gs, 256, 0, st>>>(w, g, wbeta(), wphi(), wzero());
+      CKL("k_window_stats");
+      dim3 gt(8, d.nlam, d.nray);
+      k_window_tables<R><<<gt, 256, 0, st>>>(w, g, A<R>(L.cx), A<R>(L.cy));
+      CKL("k_window_tables");
+    } else {
+      CK(cudaMemcpyAsync(wbeta(), rbeta(), sizeof(double) * d.nray, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(wphi(), rphi(), sizeof(double) * d.nray, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemsetAsync(wzero(), 0, sizeof(int) * d.nray, st));
+    }
+    return DTMM_OK;
+  }
+
+  // ordered list of sub-steps of one pass: (layer index, signed thickness)
+  void substeps(int dir, std::vector<std::pair<int, double>>& out) const {
+    out.clear();
+    for (int q = 0; q < d.nlayers; ++q) {
+      const int l = dir > 0 ? q : d.nlayers - 1 - q;
+      const double ds = d.thickness[l] / d.nstep[l];
+      for (int s = 0; s < d.nstep[l]; ++s) out.push_back({l, ds});
+    }
+  }
+
+  // state F (real space, 4 components) -> propagated through all layers -> F
+  int sweep4(int pass, cpx<R>* bulk) {
+    const double dir = (pass % 2 == 0) ? 1.0 : -1.0;
+    std::vector<std::pair<int, double>> sub;
+    substeps(pass % 2 == 0 ? 1 : -1, sub);
+    cpx<R>* F = P(L.F);
+    cpx<R>* X = P(L.X);
+    cpx<R>* U = P(L.U);
+    int rc;
+    if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
+    if ((rc = launch_ktab(KT_D1, dir * sub.front().second / 2, P(L.kfirst)))) return rc;
+    double dprev = 0.0;
+    int cur_layer = -1;
+    for (size_t s = 0; s < sub.size(); ++s) {
+      const int l = sub[s].first;
+      const double ds = sub[s].second;
+      const cpx<R>* op;
+      if (L.cache_ops) {
+        op = (const cpx<R>*)(ws + L.op + L.op_one * (size_t)l);
+        if (pass == 0 && l != cur_layer && (rc = voxel_ops(l, ds, (cpx<R>*)op))) return rc;
+      } else {
+        op = P(L.op);
+        if (l != cur_layer && (rc = voxel_ops(l, ds, P(L.op)))) return rc;
+      }
+      cur_layer = l;
+      if (s == 0) {
+        rc = launch_col(F, U, 4, 4, KOP_MAT, P(L.kfirst), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
+                        1.0);
+      } else {
+        if ((rc = launch_ktab(KT_DIAG, dir * 0.5 * (dprev + ds), P(L.kdiag)))) return rc;
+        rc = launch_col(X, U, 4, 4, KOP_DIAG, P(L.kdiag), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
+                        1.0);
+      }
+      if (rc) return rc;
+      if ((rc = launch_row(U, X, op, dir))) return rc;
+      dprev = ds;
+      const bool last_of_layer = (s + 1 == sub.size()) || (sub[s + 1].first != l);
+      if (bulk && last_of_layer) {
+        // bulk[l + 1] = ifft2(D2 . X) (dtmm/transfer.py:758-764, :878-880)
+        cpx<R>* slab = bulk + (size_t)(l + 1) * NI * 4 * L.HW;
+        if ((rc = launch_ktab(KT_D2, dir * ds / 2, P(L.klast)))) return rc;
+        if ((rc = launch_col(X, slab, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+        if ((rc = launch_rows(slab, 4, true, 1.0 / d.width))) return rc;
+      }
+    }
+    if ((rc = launch_ktab(KT_D2, dir * sub.back().second / 2, P(L.klast)))) return rc;
+    if ((rc = launch_col(X, U, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;
+    CK(cudaMemcpyAsync(F, U, sizeof(cpx<R>) * (size_t)NI * 4 * L.HW, cudaMemcpyDeviceToDevice, st));
+    return DTMM_OK;
+  }
+
+  // f (real space) -> notch * P . fft2(f) [with per-k normalisation] -> ifft2 -> f
+  int project(cpx<R>* f, const cpx<R>* Ptab, bool normalize, double sigma) {
+    int rc;
+    cpx<R>* K = P(L.U);
+    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(f, K, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;
+    NotchParams nt;
+    nt.on = 1;
+    nt.x0 = d.nin;
+    nt.sigma = sigma;
+    nt.ks = ks();
+    const size_t n = (size_t)NI * L.HW;
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, normalize ? 1 : 0, nt);
+    CKL("k_kproject");
+    if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
+    return launch_rows(f, 4, true, 1.0 / d.width);
+  }
+
+  // f <- ifft2(P . fft2(src))
+  int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab) {
+    int rc;
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    if (f != src) CK(cudaMemcpyAsync(f, src, bytes, cudaMemcpyDeviceToDevice, st));
+    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(f, P(L.U), 4, 4, KOP_MAT, Ptab, 1, nullptr, true, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_rows(P(L.U), 4, true, 1.0 / d.width))) return rc;
+    CK(cudaMemcpyAsync(f, P(L.U), bytes, cudaMemcpyDeviceToDevice, st));
+    return DTMM_OK;
+  }
+
+  int axpby(cpx<R>* out, const cpx<R>* x, const double* ax, double sx, const cpx<R>* y, const double* by, double sy) {
+    const size_t n = (size_t)NI * 4 * L.HW;
+    k_axpby<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, x, ax, sx, y, by, sy, g, 4);
+    CKL("k_axpby");
+    return DTMM_OK;
+  }
+
+  int run4() {
+    int rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* F = P(L.F);
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    const int npass = d.npass;
+    // out= given: keep only its backward-propagating part (dtmm/transfer.py:674)
+    if (io.out_given) {
+      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pout), -1, d.nin * d.nin, 0.0, false))) return rc;
+      if ((rc = diffract(fout, fout, P(L.pout)))) return rc;
+    } else {
+      CK(cudaMemsetAsync(fout, 0, bytes, st));
+    }
+    cpx<R>* field0 = nullptr;
+    if (npass > 1) {
+      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pin), 1, d.nin * d.nin, 0.0, false))) return rc;
+      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pout), 1, d.nout * d.nout, 0.0, false))) return rc;
+      field0 = P(L.field0);
+      if ((rc = diffract(field0, fin, P(L.pin)))) return rc;
+      k_total_intensity<R><<<NI, 256, 0, st>>>(field0, g, i0());
+      CKL("k_total_intensity");
+    }
+    CK(cudaMemcpyAsync(F, fin, bytes, cudaMemcpyDeviceToDevice, st));
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    for (int i = 0; i < npass; ++i) {
+      if ((rc = sweep4(i, bulk))) return rc;
+      if (npass > 1) {
+        const double sigma = d.smooth * (npass - i) / npass;
+        if (i % 2 == 0) {
+          if (i == 0 && (rc = axpby(F, F, nullptr, 1.0, fout, nullptr, -1.0))) return rc;
+          if (i != npass - 1 && (rc = project(F, P(L.pout), true, sigma))) return rc;
+          if ((rc = axpby(fout, fout, nullptr, 1.0, F, nullptr, 1.0))) return rc;
+          CK(cudaMemcpyAsync(F, fout, bytes, cudaMemcpyDeviceToDevice, st));
+        } else {
+          CK(cudaMemcpyAsync(fin, F, bytes, cudaMemcpyDeviceToDevice, st));
+          if (i != npass - 1) {
+            if ((rc = project(F, P(L.pin), false, sigma))) return rc;
+            k_total_intensity<R><<<NI, 256, 0, st>>>(F, g, i0f());
+            CKL("k_total_intensity");
+            k_ratio<<<(NI + 255) / 256, 256, 0, st>>>(i0(), i0f(), fact(), NI);
+            CKL("k_ratio");
+            if ((rc = axpby(F, F, fact(), 1.0, nullptr, nullptr, 0.0))) return rc;
+            if ((rc = axpby(fout, fout, fact(), 1.0, nullptr, nullptr, 0.0))) return rc;
+            if ((rc = axpby(fin, fin, fact(), 1.0, nullptr, nullptr, 0.0))) return rc;
+            if ((rc = axpby(F, field0, nullptr, 1.0, F, nullptr, -1.0))) return rc;
+            if ((rc = axpby(fin, fin, nullptr, 1.0, F, nullptr, 1.0))) return rc;
+          }
+        }
+      } else {
+        CK(cudaMemcpyAsync(fout, F, bytes, cudaMemcpyDeviceToDevice, st));
+      }
+    }
+    return DTMM_OK;
+  }
+
+  int run2() {
+    int rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* F = P(L.F);
+    cpx<R>* X = P(L.X);
+    cpx<R>* U = P(L.U);
+    const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    std::vector<std::pair<int, double>> sub;
+    substeps(1, sub);
+    CK(cudaMemcpyAsync(F, fin, bytes4, cudaMemcpyDeviceToDevice, st));
+    if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
+    // entry: transmitted part in n_in, interface n_in -> effective, half step
+    if ((rc = launch_ktab(KT_2IN, sub.front().second / 2, P(L.kfirst)))) return rc;
+    double dprev = 0.0;
+    int cur_layer = -1;
+    for (size_t s = 0; s < sub.size(); ++s) {
+      const int l = sub[s].first;
+      const double ds = sub[s].second;
+      if (l != cur_layer && (rc = voxel_ops(l, ds, P(L.op)))) return rc;
+      cur_layer = l;
+      const R* cy = L.ny > 1 ? A<R>(L.cy) : nullptr;
+      if (s == 0) {
+        rc = launch_col(F, U, 4, 2, KOP_MAT, P(L.kfirst), L.ny, cy, true, true, 1.0);
+      } else {
+        if ((rc = launch_ktab(KT_DIAG, 0.5 * (dprev + ds), P(L.kdiag)))) return rc;
+        rc = launch_col(X, U, 2, 2, KOP_DIAG, P(L.kdiag), L.ny, cy, true, true, 1.0);
+      }
+      if (rc) return rc;
+      if ((rc = launch_row(U, X, P(L.op), 1.0))) return rc;
+      dprev = ds;
+    }
+    // exit: half step, interface effective -> n_out, windows and E -> H
+    if ((rc = launch_ktab(KT_2OUT, sub.back().second / 2, P(L.klast)))) return rc;
+    if ((rc = launch_col(X, U, 2, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height,
+                         (size_t)d.nlam * L.HW * 8)))
+      return rc;
+    if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;
+    CK(cudaMemcpyAsync(fout, U, bytes4, cudaMemcpyDeviceToDevice, st));
+    return DTMM_OK;
+  }
+};
+
+template <typename R>
+int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws, const Layout& L, cudaStream_t st) {
+  Engine<R> e{*d, *io, L, (unsigned char*)ws, st};
+  e.g.H = d->height;
+  e.g.W = d->width;
+  e.NI = d->nray * d->npol * d->nlam;
+  e.g.NI = e.NI;
+  e.g.nlam = d->nlam;
+  e.g.npol = d->npol;
+  e.g.nray = d->nray;
+  make_plan(d->height, e.pH);
+  make_plan(d->width, e.pW);
+  int rc = e.setup();
+  if (rc) return rc;
+  return d->method == 4 ? e.run4() : e.run2();
+}
+
+}  // namespace
+
+extern "C" {
+
+int dtmm_abi_version(void) { return 1; }
+
+const char* dtmm_last_error(void) { return g_err.c_str(); }
+
+size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc) {
+  if (check_desc(desc) != DTMM_OK) return 0;
+  return layout_of(desc).total;
+}
+
+int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
+                  void* stream) {
+  g_err.clear();
+  int rc = check_desc(desc);
+  if (rc) return rc;
+  if (io == nullptr || io->field_in == nullptr || io->field_out == nullptr) return fail(DTMM_EINVAL, "null field buffer");
+  if (io->bulk != nullptr && desc->method != 4) return fail(DTMM_ENOTSUP, "bulk output is implemented for 4x4");
+  Layout L = layout_of(desc);
+  if (workspace == nullptr || workspace_bytes < L.total)
+    return fail(DTMM_ENOSPACE, "workspace of %zu bytes, %zu needed", workspace_bytes, L.total);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (desc->precision == DTMM_PRECISION_DOUBLE) return run_engine<double>(desc, io, workspace, L, st);
+  return run_engine<float>(desc, io, workspace, L, st);
+}
+
+}  // extern "C"

@@ -1,0 +1,1039 @@
+// Kernels of the GB300 field-transfer engine (the hot path of dtmm's
+// transfer_field).  All kernels are templated on the bulk real type R
+// (float = complex64 bulk, double = complex128 bulk); eigen-solves, k-space
+// operator tables and window statistics are always computed in FP64.
+//
+// Data layout in HBM
+//   field / state arrays : [image][component][H][W] interleaved complex,
+//                          image = (ray * npol + pol) * nlam + lam
+//                          (the reference's ([rays],[pols],lambda,4,H,W) order)
+//   window-row buffers   : [j][image][component][H][W]
+//   layer operators      : [ray][window][record][H][W]   (14 complex records)
+//   k-space tables       : [lam][H][W][rows][cols]
+#pragma once
+
+#include "dtmm_common.cuh"
+
+namespace dtmm {
+
+constexpr int OP_REC = 14;  // records of one per-voxel layer operator
+
+enum KOp { KOP_NONE = 0, KOP_DIAG = 1, KOP_MAT = 2 };
+
+struct Grid {
+  int H, W;       // grid
+  int NI;         // images
+  int nlam, npol, nray;
+};
+
+__device__ __forceinline__ int img_lam(const Grid& g, int img) { return img % g.nlam; }
+__device__ __forceinline__ int img_ray(const Grid& g, int img) { return img / (g.nlam * g.npol); }
+
+// fftfreq(n)[i] * n
+__host__ __device__ __forceinline__ int fsigned(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
+
+// ---------------------------------------------------------------------------
+// FP64 Berreman eigen-data of an isotropic medium, in the phi = 0 frame, then
+// rotated by phi (dtmm/tmm.py:124 and :372 with _dotr2m, dtmm/linalg.py:674).
+// ---------------------------------------------------------------------------
+__device__ inline void iso_alphaf(double beta, double phi, cpx<double> eps, cpx<double> alpha[4],
+                                  cpx<double> F[4][4]) {
+  cpx<double> a = csqrt_d(mk<double>(eps.re - beta * beta, eps.im));
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) F[i][j] = mk<double>(0.0, 0.0);
+  if (a.re == 0.0 && a.im == 0.0) {
+    for (int i = 0; i < 4; ++i) alpha[i] = mk<double>(0.0, 0.0);
+    return;
+  }
+  cpx<double> gp = cdiv(eps, a);
+  alpha[0] = a;
+  alpha[1] = -a;
+  alpha[2] = a;
+  alpha[3] = -a;
+  F[0][0] = mk<double>(0.5, 0.0);
+  F[0][1] = mk<double>(0.5, 0.0);
+  F[1][0] = gp * 0.5;
+  F[1][1] = gp * -0.5;
+  F[2][2] = mk<double>(0.5, 0.0);
+  F[2][3] = mk<double>(0.5, 0.0);
+  F[3][2] = a * -0.5;
+  F[3][3] = a * 0.5;
+  double s, c;
+  sincos(phi, &s, &c);
+  for (int j = 0; j < 4; ++j) {
+    cpx<double> f0 = F[0][j], f1 = F[1][j], f2 = F[2][j], f3 = F[3][j];
+    F[0][j] = f0 * c - f2 * s;
+    F[1][j] = f1 * c + f3 * s;
+    F[2][j] = f0 * s + f2 * c;
+    F[3][j] = f3 * c - f1 * s;
+  }
+}
+
+// 4x4 complex inverse by the adjugate (2x2 complementary minors); an exactly
+// singular matrix maps to zero (dtmm/linalg.py:460-518).
+__device__ inline void inv4(const cpx<double> a[4][4], cpx<double> o[4][4]) {
+  cpx<double> s0 = a[0][0] * a[1][1] - a[1][0] * a[0][1];
+  cpx<double> s1 = a[0][0] * a[1][2] - a[1][0] * a[0][2];
+  cpx<double> s2 = a[0][0] * a[1][3] - a[1][0] * a[0][3];
+  cpx<double> s3 = a[0][1] * a[1][2] - a[1][1] * a[0][2];
+  cpx<double> s4 = a[0][1] * a[1][3] - a[1][1] * a[0][3];
+  cpx<double> s5 = a[0][2] * a[1][3] - a[1][2] * a[0][3];
+  cpx<double> c5 = a[2][2] * a[3][3] - a[3][2] * a[2][3];
+  cpx<double> c4 = a[2][1] * a[3][3] - a[3][1] * a[2][3];
+  cpx<double> c3 = a[2][1] * a[3][2] - a[3][1] * a[2][2];
+  cpx<double> c2 = a[2][0] * a[3][3] - a[3][0] * a[2][3];
+  cpx<double> c1 = a[2][0] * a[3][2] - a[3][0] * a[2][2];
+  cpx<double> c0 = a[2][0] * a[3][1] - a[3][0] * a[2][1];
+  cpx<double> det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+  cpx<double> r = (det.re == 0.0 && det.im == 0.0) ? mk<double>(0.0, 0.0) : cdiv(mk<double>(1.0, 0.0), det);
+  o[0][0] = (a[1][1] * c5 - a[1][2] * c4 + a[1][3] * c3) * r;
+  o[0][1] = (-a[0][1] * c5 + a[0][2] * c4 - a[0][3] * c3) * r;
+  o[0][2] = (a[3][1] * s5 - a[3][2] * s4 + a[3][3] * s3) * r;
+  o[0][3] = (-a[2][1] * s5 + a[2][2] * s4 - a[2][3] * s3) * r;
+  o[1][0] = (-a[1][0] * c5 + a[1][2] * c2 - a[1][3] * c1) * r;
+  o[1][1] = (a[0][0] * c5 - a[0][2] * c2 + a[0][3] * c1) * r;
+  o[1][2] = (-a[3][0] * s5 + a[3][2] * s2 - a[3][3] * s1) * r;
+  o[1][3] = (a[2][0] * s5 - a[2][2] * s2 + a[2][3] * s1) * r;
+  o[2][0] = (a[1][0] * c4 - a[1][1] * c2 + a[1][3] * c0) * r;
+  o[2][1] = (-a[0][0] * c4 + a[0][1] * c2 - a[0][3] * c0) * r;
+  o[2][2] = (a[3][0] * s4 - a[3][1] * s2 + a[3][3] * s0) * r;
+  o[2][3] = (-a[2][0] * s4 + a[2][1] * s2 - a[2][3] * s0) * r;
+  o[3][0] = (-a[1][0] * c3 + a[1][1] * c1 - a[1][2] * c0) * r;
+  o[3][1] = (a[0][0] * c3 - a[0][1] * c1 + a[0][2] * c0) * r;
+  o[3][2] = (-a[3][0] * s3 + a[3][1] * s1 - a[3][2] * s0) * r;
+  o[3][3] = (a[2][0] * s3 - a[2][1] * s1 + a[2][2] * s0) * r;
+}
+
+__device__ inline void inv2(const cpx<double> a[2][2], cpx<double> o[2][2]) {
+  cpx<double> det = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+  cpx<double> r = (det.re == 0.0 && det.im == 0.0) ? mk<double>(0.0, 0.0) : cdiv(mk<double>(1.0, 0.0), det);
+  o[0][0] = a[1][1] * r;
+  o[0][1] = -a[0][1] * r;
+  o[1][0] = -a[1][0] * r;
+  o[1][1] = a[0][0] * r;
+}
+
+// ---------------------------------------------------------------------------
+// Per-voxel layer operator (FP64 eigen-solve) for one (ray, window).
+//
+// The real-space step of the reference's split-step layer operator is
+// E . diag(exp(i kd alpha)) . E^-1 acting on the "Epn" field (E-field rows of
+// forward / backward modes), wrapped by the beam-phase correction C_w of the
+// effective medium (dtmm/propagate_4x4.py:80-101, dtmm/matrix.py:133-174).
+// For an isotropic effective medium C_w is a scalar per direction,
+// exp(-/+ i k0 d/2 a_w) with a_w = sqrt(eps_eff - beta_w^2), so
+// C_w M C_w = E . diag(exp(i k0 d (alpha_m -/+ a_w))) . E^-1 per block.
+// Stored per voxel (14 complex records): forward block E (4), 1/det, phase
+// arguments d*(alpha_0 - a_w), d*(alpha_2 - a_w); backward block E (4),
+// 1/det, d*(alpha_1 + a_w), d*(alpha_3 + a_w).  E . P . E^-1 does not depend
+// on the scale of E's columns, so the reference's column normalisation
+// (dtmm/tmm.py:280-289) is skipped; a singular block (det == 0) zeroes the
+// whole operator, as the reference's inverse does.
+// ---------------------------------------------------------------------------
+struct OpParams {
+  const double* eps_dev;  // if set: (re, im) of the effective medium, overrides eps_eff
+  const void* epsv;      // (L?,H?,W?,3) float64 or complex128
+  const double* epsa;    // (L?,H?,W?,3) float64
+  long long ev_s[3];     // element strides of epsv over (layer, y, x) (0 = broadcast)
+  long long ea_s[3];
+  int eps_complex;
+  int layer;
+  double d;              // sub-step thickness (pixels), direction not included
+  const double* wbeta;   // [ray][nwin]
+  const double* wphi;
+  cpx<double> eps_eff;
+  int nwin;
+  int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
+};
+
+template <typename R>
+__global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int rw = blockIdx.y;  // ray * nwin + window
+  if (pix >= HW) return;
+  const int y = pix / g.W, x = pix - y * g.W;
+  const double beta = p.wbeta[rw], phi = p.wphi[rw];
+  const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
+  const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
+  cpx<double> ev[3];
+  if (p.eps_complex) {
+    const cpx<double>* e = (const cpx<double>*)p.epsv + eo;
+    ev[0] = e[0];
+    ev[1] = e[1];
+    ev[2] = e[2];
+  } else {
+    const double* e = (const double*)p.epsv + eo;
+    ev[0] = mk<double>(e[0], 0.0);
+    ev[1] = mk<double>(e[1], 0.0);
+    ev[2] = mk<double>(e[2], 0.0);
+  }
+  const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
+  if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
+  cpx<double> aw = csqrt_d(mk<double>(p.eps_eff.re - beta * beta, p.eps_eff.im));
+
+  cpx<double> E[2][4];  // rows Ex, Ey of the four mode columns
+  cpx<double> al[4];
+  bool zero = false;
+  const cpx<double> z0 = mk<double>(0.0, 0.0);
+  if (ev[0].re == ev[1].re && ev[0].im == ev[1].im && ev[1].re == ev[2].re && ev[1].im == ev[2].im) {
+    cpx<double> a = csqrt_d(mk<double>(ev[0].re - beta * beta, ev[0].im));
+    if (a.re == 0.0 && a.im == 0.0) zero = true;
+    al[0] = a;
+    al[1] = -a;
+    al[2] = a;
+    al[3] = -a;
+    const cpx<double> h = mk<double>(0.5, 0.0);
+    E[0][0] = h; E[1][0] = z0;
+    E[0][1] = h; E[1][1] = z0;
+    E[0][2] = z0; E[1][2] = h;
+    E[0][3] = z0; E[1][3] = h;
+  } else {
+    // uniaxial, optic axis rotated by (theta, azimuth - phi) (dtmm/tmm.py:157-278,
+    // rotation dtmm/rotation.py:176-194 via :390)
+    double st, ct, sf, cf;
+    sincos(theta, &st, &ct);
+    sincos(azim - phi, &sf, &cf);
+    const double cfst = cf * st, sfst = st * sf;
+    const cpx<double> eps11 = ev[0];
+    const cpx<double> delta = ev[2] - eps11;
+    cpx<double> ev02, evs, evpp, evpm;
+    if (beta == 0.0) {
+      ev02 = eps11;
+      evs = csqrt_d(ev02);
+      cpx<double> u = eps11 + delta * (ct * ct);
+      cpx<double> w = eps11 * (ev02 + delta);
+      cpx<double> sq = cdiv(csqrt_d(u * w), u);
+      evpp = sq;
+      evpm = -sq;
+      E[0][0] = mk<double>(cf, 0.0); E[1][0] = mk<double>(sf, 0.0);
+      E[0][1] = mk<double>(cf, 0.0); E[1][1] = mk<double>(sf, 0.0);
+      E[0][2] = evs * (-sf);         E[1][2] = evs * cf;
+      E[0][3] = evs * (-sf);         E[1][3] = evs * cf;
+    } else {
+      ev02 = mk<double>(eps11.re - beta * beta, eps11.im);
+      evs = csqrt_d(ev02);
+      cpx<double> u = eps11 + delta * (ct * ct);
+      const double gama = beta * cf;
+      cpx<double> v = delta * (gama * 2.0 * st * ct);
+      cpx<double> w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
+      cpx<double> u2 = u * 2.0;
+      cpx<double> sq = cdiv(csqrt_d(v * v - u * w * 4.0), u2);
+      cpx<double> vh = cdiv(v, u2);
+      evpp = sq - vh;
+      evpm = -vh - sq;
+      const double ctbeta = ct * beta;
+      cpx<double> ie = cdiv(mk<double>(1.0, 0.0), eps11);
+      cpx<double> ev02cf = ev02 * cfst;
+      E[0][0] = (evpp * ctbeta - ev02cf) * ie;  E[1][0] = mk<double>(-sfst, 0.0);
+      E[0][1] = (ev02cf - evpm * ctbeta) * ie;  E[1][1] = mk<double>(sfst, 0.0);
+      E[0][2] = evs * sfst;                     E[1][2] = mk<double>(ctbeta, 0.0) - evs * cfst;
+      E[0][3] = evs * (-sfst);                  E[1][3] = evs * cfst + mk<double>(ctbeta, 0.0);
+    }
+    al[0] = evpp;
+    al[1] = evpm;
+    al[2] = evs;
+    al[3] = -evs;
+  }
+  // rotate the E rows back by the beam azimuth phi
+  double sp, cp;
+  sincos(phi, &sp, &cp);
+  for (int m = 0; m < 4; ++m) {
+    cpx<double> ex = E[0][m], ey = E[1][m];
+    E[0][m] = ex * cp - ey * sp;
+    E[1][m] = ex * sp + ey * cp;
+  }
+  // forward block: modes 0, 2 ; backward block: modes 1, 3
+  cpx<double> detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
+  cpx<double> detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
+  const bool zf = (detf.re == 0.0 && detf.im == 0.0);
+  const bool zb = (detb.re == 0.0 && detb.im == 0.0);
+  if (zf || (p.four && zb)) zero = true;
+  cpx<double> rec[OP_REC];
+  if (zero) {
+    for (int i = 0; i < OP_REC; ++i) rec[i] = z0;
+  } else {
+    rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
+    rec[4] = cdiv(mk<double>(1.0, 0.0), detf);
+    rec[5] = (al[0] - aw) * p.d;
+    rec[6] = (al[2] - aw) * p.d;
+    if (p.four) {
+      rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
+      rec[11] = cdiv(mk<double>(1.0, 0.0), detb);
+      rec[12] = (al[1] + aw) * p.d;
+      rec[13] = (al[3] + aw) * p.d;
+    } else {
+      for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
+    }
+  }
+  cpx<R>* o = op + (size_t)rw * OP_REC * HW + pix;
+  const int nrec = p.four ? OP_REC : 7;
+  for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Window statistics and 1D window weight tables (diffraction > 1).
+//
+// Window (i, j) of the n x n grid is the tent cx_i(beta_x) * cy_j(beta_y),
+// open-ended at the grid edges, zero for beta >= betamax, with centres on
+// linspace(-betamax, betamax, n) shifted by the folded beam offset
+// (dtmm/mode.py:11-70).  Its mean beta, phi is the window^2-weighted mean of
+// (beta_x, beta_y) over every wavelength and k (dtmm/mode.py:104-130).
+// ---------------------------------------------------------------------------
+struct WinParams {
+  int n;               // diffraction (windows per axis)
+  double betamax;
+  double step;         // centre spacing
+  const double* xoff;  // [ray] folded offsets
+  const double* yoff;
+  const double* ks;    // [lam]
+};
+
+__device__ __forceinline__ double tent(double db, int typ) {
+  double c = 1.0 - fabs(db);
+  if (c < 0.0) return 0.0;
+  if (typ < 0 && db < 0) return 1.0;
+  if (typ > 0 && db > 0) return 1.0;
+  return c;
+}
+
+__device__ __forceinline__ double win_center(const WinParams& w, int i) {
+  // numpy.linspace(-betamax, betamax, n)[i]
+  if (i == w.n - 1) return w.betamax;
+  double step = (2.0 * w.betamax) / (w.n - 1);
+  return -w.betamax + i * step;
+}
+
+// one block per (ray, window): sums of w^2 bx, w^2 by, w^2 over (lam, ky, kx)
+__global__ void k_window_stats(WinParams w, Grid g, double* wbeta, double* wphi, int* wzero) {
+  const int ray = blockIdx.y, win = blockIdx.x;
+  const int i = win / w.n, j = win % w.n;
+  const int xt = (i == 0) ? -1 : ((i == w.n - 1) ? 1 : 0);
+  const int yt = (j == 0) ? -1 : ((j == w.n - 1) ? 1 : 0);
+  const double cx0 = win_center(w, i) + w.xoff[ray];
+  const double cy0 = win_center(w, j) + w.yoff[ray];
+  double sx = 0, sy = 0, sn = 0;
+  int nz = 0;
+  const int total = g.nlam * g.H * g.W;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int lam = t / (g.H * g.W);
+    const int k = t - lam * g.H * g.W;
+    const int ky = k / g.W, kx = k - ky * g.W;
+    const double l = 2.0 * M_PI / w.ks[lam];
+    const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
+    const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
+    const double b = sqrt(bx * bx + by * by);
+    double c = 0.0;
+    if (b < w.betamax) c = tent((bx - cx0) / w.step, xt) * tent((by - cy0) / w.step, yt);
+    if (c > 0.0) {
+      nz = 1;
+      const double c2 = c * c;
+      sx += bx * c2;
+      sy += by * c2;
+      sn += c2;
+    }
+  }
+  __shared__ double red[3][256];
+  __shared__ int rz[256];
+  red[0][threadIdx.x] = sx;
+  red[1][threadIdx.x] = sy;
+  red[2][threadIdx.x] = sn;
+  rz[threadIdx.x] = nz;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+      rz[threadIdx.x] |= rz[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double mx = red[0][0], my = red[1][0], mn = red[2][0];
+    if (mn > 0) {
+      mx /= mn;
+      my /= mn;
+    }
+    const int idx = ray * w.n * w.n + win;
+    wbeta[idx] = sqrt(mx * mx + my * my);
+    wphi[idx] = atan2(my, mx);
+    wzero[idx] = rz[0] ? 0 : 1;
+  }
+}
+
+// cx[ray][i][lam][kx] and cy[ray][j][lam][ky]; the beta >= betamax cut is
+// carried by the diffraction operators, which vanish there.
+template <typename R>
+__global__ void k_window_tables(WinParams w, Grid g, R* cx, R* cy) {
+  const int ray = blockIdx.z;
+  const int lam = blockIdx.y;
+  const int nmax = g.H > g.W ? g.H : g.W;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w.n * nmax; t += gridDim.x * blockDim.x) {
+    const int i = t / nmax, k = t - i * nmax;
+    const int typ = (i == 0) ? -1 : ((i == w.n - 1) ? 1 : 0);
+    const double l = 2.0 * M_PI / w.ks[lam];
+    if (k < g.W) {
+      const double bx = l * ((double)fsigned(k, g.W) * (1.0 / g.W));
+      cx[(((size_t)ray * w.n + i) * g.nlam + lam) * g.W + k] = (R)tent((bx - (win_center(w, i) + w.xoff[ray])) / w.step, typ);
+    }
+    if (k < g.H) {
+      const double by = l * ((double)fsigned(k, g.H) * (1.0 / g.H));
+      cy[(((size_t)ray * w.n + i) * g.nlam + lam) * g.H + k] = (R)tent((by - (win_center(w, i) + w.yoff[ray])) / w.step, typ);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 k-space operator tables of the isotropic effective medium, one matrix
+// per (lam, ky, kx).  beta >= betamax zeroes the eigen-data (and hence the
+// operator), as the reference's diffraction matrices do
+// (dtmm/diffract.py:22-70).
+// ---------------------------------------------------------------------------
+enum KTab {
+  KT_D1 = 0,     // 4x4 field -> Epn over d: E . P(d) . F^-1          (dtmm/matrix.py:110)
+  KT_D2 = 1,     // 4x4 Epn -> field over d: F . P(d) . E^-1          (dtmm/matrix.py:121)
+  KT_PROJ = 2,   // 4x4 forward projection F . diag(1,0,1,0) . F^-1   (dtmm/diffract.py:242)
+  KT_DIAG = 3,   // (e+, e-) = exp(+/- i k0 d a_k)                    (D1 . D2 of two half steps)
+  KT_2IN = 4,    // 2x4 [E(d) . t_in] . P_in[rows Ex, Ey]   (2x2 method entry)
+  KT_2OUT = 5,   // 4x2 [sum_w win_w ; sum_w win_w E2H_w] . t_out . E(d)   (2x2 method exit)
+};
+
+struct KTabParams {
+  int what;
+  int proj_mode;       // KT_PROJ: +1 forward, -1 backward modes
+  const double* eps_dev; // if set: (re, im) of the effective medium, overrides eps
+  double d;            // phase thickness (pixels, signed)
+  cpx<double> eps;     // effective medium (or the projection medium)
+  cpx<double> eps_in;  // 2x2: medium below the stack (entry interface n_in -> effective)
+  cpx<double> eps_out; // 2x2: medium above the stack (exit interface, and the E2H medium)
+  cpx<double> eps_p;   // 2x2 entry: projection medium of the input field
+  int with_t;          // 2x2: apply the interface transmission
+  double betamax;
+  const double* ks;
+  // KT_2OUT windows
+  int nwin_axis;       // n (1 = no windows)
+  const double* wbeta;
+  const double* wphi;
+  const int* wzero;
+  WinParams win;
+  int ray;
+};
+
+__device__ inline void betaphi_k(const Grid& g, double ks, int ky, int kx, double& beta, double& phi) {
+  const double xx = (double)fsigned(kx, g.W) * (1.0 / g.W);
+  const double yy = (double)fsigned(ky, g.H) * (1.0 / g.H);
+  beta = (2.0 * M_PI / fabs(ks)) * sqrt(xx * xx + yy * yy);
+  phi = atan2(yy, xx);
+}
+
+// iso eigen-data at grid point k with the betamax cut
+__device__ inline void iso_k(double beta, double phi, cpx<double> eps, double betamax, cpx<double> al[4],
+                             cpx<double> F[4][4], cpx<double> Fi[4][4]) {
+  iso_alphaf(beta, phi, eps, al, F);
+  inv4(F, Fi);
+  if (beta >= betamax) {
+    for (int i = 0; i < 4; ++i) {
+      al[i] = mk<double>(0.0, 0.0);
+      for (int j = 0; j < 4; ++j) F[i][j] = Fi[i][j] = mk<double>(0.0, 0.0);
+    }
+  }
+}
+
+// transmission of the 2x2 interface in -> out at k (dtmm/tmm.py:925-1049)
+__device__ inline void tmat_k(double beta, double phi, cpx<double> ein, cpx<double> eout, double betamax,
+                              cpx<double> t[2][2]) {
+  cpx<double> al[4], Fin[4][4], Finv[4][4], Fout[4][4], Fouti[4][4];
+  iso_k(beta, phi, ein, betamax, al, Fin, Finv);
+  iso_k(beta, phi, eout, betamax, al, Fout, Fouti);
+  cpx<double> St[2][2], A[2][2], Sti[2][2], Ai[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      cpx<double> s = mk<double>(0.0, 0.0);
+      for (int q = 0; q < 4; ++q) s = s + Finv[2 * i][q] * Fout[q][2 * j];
+      St[i][j] = s;
+      A[i][j] = Fin[2 * i][2 * j];
+    }
+  inv2(St, Sti);
+  inv2(A, Ai);
+  cpx<double> ei[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) ei[i][j] = Sti[i][0] * Ai[0][j] + Sti[i][1] * Ai[1][j];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) t[i][j] = Fout[2 * i][0] * ei[0][j] + Fout[2 * i][2] * ei[1][j];
+}
+
+template <typename R>
+__global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
+  const int HW = g.H * g.W;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nlam * HW) return;
+  const int lam = t / HW, k = t - lam * HW;
+  const int ky = k / g.W, kx = k - ky * g.W;
+  const double ks = p.ks[lam];
+  double beta, phi;
+  betaphi_k(g, ks, ky, kx, beta, phi);
+  cpx<double> al[4], F[4][4], Fi[4][4];
+  if (p.eps_dev != nullptr) p.eps = mk<double>(p.eps_dev[0], p.eps_dev[1]);
+  if (p.what == KT_DIAG) {
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    const bool masked = (beta >= p.betamax) || (al[0].re == 0.0 && al[0].im == 0.0);
+    cpx<double> ep = masked ? mk<double>(0.0, 0.0) : cexp_i(al[0] * (ks * p.d));
+    cpx<double> em = masked ? mk<double>(0.0, 0.0) : cexp_i(al[1] * (ks * p.d));
+    tab[(size_t)t * 2 + 0] = cvt<R>(ep);
+    tab[(size_t)t * 2 + 1] = cvt<R>(em);
+    return;
+  }
+  if (p.what == KT_D1 || p.what == KT_D2 || p.what == KT_PROJ) {
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    cpx<double> ph[4];
+    for (int m = 0; m < 4; ++m) ph[m] = cexp_i(al[m] * (ks * p.d));
+    cpx<double> M[4][4];
+    if (p.what == KT_PROJ) {
+      const int m0 = p.proj_mode > 0 ? 0 : 1;
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+          M[i][j] = F[i][m0] * Fi[m0][j] + F[i][m0 + 2] * Fi[m0 + 2][j];
+    } else {
+      cpx<double> E[4][4];
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) E[i][j] = mk<double>(0.0, 0.0);
+      E[0][0] = F[0][0]; E[0][2] = F[0][2]; E[2][0] = F[2][0]; E[2][2] = F[2][2];
+      E[1][1] = F[0][1]; E[1][3] = F[0][3]; E[3][1] = F[2][1]; E[3][3] = F[2][3];
+      if (p.what == KT_D1) {
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) {
+            cpx<double> s = mk<double>(0.0, 0.0);
+            for (int m = 0; m < 4; ++m) s = s + E[i][m] * ph[m] * Fi[m][j];
+            M[i][j] = s;
+          }
+      } else {
+        cpx<double> Ei[4][4];
+        inv4(E, Ei);
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) {
+            cpx<double> s = mk<double>(0.0, 0.0);
+            for (int m = 0; m < 4; ++m) s = s + F[i][m] * ph[m] * Ei[m][j];
+            M[i][j] = s;
+          }
+      }
+    }
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(M[i][j]);
+    return;
+  }
+  // 2x2 method: E-basis diffraction over d, e(d) * I for the isotropic medium
+  // (dtmm/diffract.py:173 with alphaEEi; masked -> 0)
+  iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+  cpx<double> Ed[2][2], Edi[2][2], Edm[2][2];
+  Ed[0][0] = F[0][0]; Ed[0][1] = F[0][2]; Ed[1][0] = F[2][0]; Ed[1][1] = F[2][2];
+  inv2(Ed, Edi);
+  const cpx<double> pd0 = cexp_i(al[0] * (ks * p.d)), pd2 = cexp_i(al[2] * (ks * p.d));
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) Edm[i][j] = Ed[i][0] * pd0 * Edi[0][j] + Ed[i][1] * pd2 * Edi[1][j];
+  cpx<double> T[2][2];
+  if (p.with_t) {
+    if (p.what == KT_2IN)
+      tmat_k(beta, phi, p.eps_in, p.eps, p.betamax, T);
+    else
+      tmat_k(beta, phi, p.eps, p.eps_out, p.betamax, T);
+  } else {
+    T[0][0] = T[1][1] = mk<double>(1.0, 0.0);
+    T[0][1] = T[1][0] = mk<double>(0.0, 0.0);
+  }
+  if (p.what == KT_2IN) {
+    // rows Ex, Ey of the forward projection in the input medium
+    cpx<double> alp[4], Fp[4][4], Fpi[4][4], P[2][4];
+    iso_k(beta, phi, p.eps_p, p.betamax, alp, Fp, Fpi);
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 4; ++j) P[i][j] = Fp[2 * i][0] * Fpi[0][j] + Fp[2 * i][2] * Fpi[2][j];
+    cpx<double> DT[2][2];
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) DT[i][j] = Edm[i][0] * T[0][j] + Edm[i][1] * T[1][j];
+    cpx<R>* o = tab + (size_t)t * 8;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(DT[i][0] * P[0][j] + DT[i][1] * P[1][j]);
+    return;
+  }
+  // KT_2OUT: [sum_w win_w ; sum_w win_w E2H_w] . T . E(d), masked
+  cpx<double> TD[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) TD[i][j] = T[i][0] * Edm[0][j] + T[i][1] * Edm[1][j];
+  double wsum = 0.0;
+  cpx<double> H[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) H[i][j] = mk<double>(0.0, 0.0);
+  const int n = p.nwin_axis;
+  const int nw = n * n;
+  for (int w = 0; w < nw; ++w) {
+    double c = 1.0;
+    const int idx = p.ray * nw + w;
+    if (n > 1) {
+      if (p.wzero[idx]) continue;
+      const int i = w / n, j = w % n;
+      const int xt = (i == 0) ? -1 : ((i == n - 1) ? 1 : 0);
+      const int yt = (j == 0) ? -1 : ((j == n - 1) ? 1 : 0);
+      const double l = 2.0 * M_PI / ks;
+      const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
+      const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
+      const double b = sqrt(bx * bx + by * by);
+      c = 0.0;
+      if (b < p.win.betamax)
+        c = tent((bx - (win_center(p.win, i) + p.win.xoff[p.ray])) / p.win.step, xt) *
+            tent((by - (win_center(p.win, j) + p.win.yoff[p.ray])) / p.win.step, yt);
+      if (c == 0.0) continue;
+    }
+    // E2H of the outgoing medium for the window's beam (dtmm/tmm.py:1051)
+    cpx<double> alw[4], Fw[4][4];
+    iso_alphaf(p.wbeta[idx], p.wphi[idx], p.eps_out, alw, Fw);
+    cpx<double> A[2][2], Ai[2][2];
+    A[0][0] = Fw[0][0]; A[0][1] = Fw[0][2]; A[1][0] = Fw[2][0]; A[1][1] = Fw[2][2];
+    inv2(A, Ai);
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) H[i][j] = H[i][j] + (Fw[2 * i + 1][0] * Ai[0][j] + Fw[2 * i + 1][2] * Ai[1][j]) * c;
+    wsum += c;
+  }
+  const bool masked = beta >= p.betamax;
+  cpx<R>* o = tab + (size_t)t * 8;
+  // rows: Ex, Hy, Ey, Hx of the output field; columns: Ex, Ey of the state
+  for (int j = 0; j < 2; ++j) {
+    cpx<double> ex = masked ? mk<double>(0.0, 0.0) : TD[0][j] * wsum;
+    cpx<double> ey = masked ? mk<double>(0.0, 0.0) : TD[1][j] * wsum;
+    cpx<double> hy = masked ? mk<double>(0.0, 0.0) : H[0][0] * TD[0][j] + H[0][1] * TD[1][j];
+    cpx<double> hx = masked ? mk<double>(0.0, 0.0) : H[1][0] * TD[0][j] + H[1][1] * TD[1][j];
+    o[0 * 2 + j] = cvt<R>(ex);
+    o[1 * 2 + j] = cvt<R>(hy);
+    o[2 * 2 + j] = cvt<R>(ey);
+    o[3 * 2 + j] = cvt<R>(hx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused column pass of one layer step (all along ky, one tile of TC columns
+// of one image):
+//   forward column FFT -> k-space operator -> for each window row j:
+//   cy_j * (.) -> inverse column FFT (scaled) -> U_j.
+// Input X: [image][cin][H][W] (rows already transformed along x).
+// ---------------------------------------------------------------------------
+struct ColParams {
+  int cin, cout;
+  int kop;                 // KOp
+  size_t ktab_ray_stride;  // elements between the tables of consecutive rays (0 = shared)
+  const void* ktab;        // KOP_DIAG: [lam][H][W][2]; KOP_MAT: [lam][H][W][cout][cin]
+  int ny;                  // window rows (1 = no windows)
+  const void* cy;          // [ray][j][lam][H] (null = weight 1)
+  int do_fwd;              // 1: transform along y first (input spatial in y)
+  int inverse_out;         // 1: inverse column FFT on the way out
+  double out_scale;
+  FFTPlan plan;
+  const void* tw;          // twiddles of H
+  const int* perm;         // digit reversal of H
+  int tc;                  // columns per block
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cpx<R>* __restrict__ X,
+                                                   cpx<R>* __restrict__ U) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = g.H, W = g.W, TC = p.tc;
+  const int CM = p.cin > p.cout ? p.cin : p.cout;
+  // tile element (y, c, xc) at (y * CM + c) * TC + xc: line (c, xc) is
+  // l = c * TC + xc with unit line stride and element stride CM * TC
+  cpx<R>* T = (cpx<R>*)smem_raw;              // [H][CM][TC]
+  cpx<R>* Tm = T + (size_t)CM * H * TC;       // [H][CM][TC] (window work buffer)
+  cpx<R>* tw = Tm + (size_t)CM * H * TC;      // [H]
+  int* perm = (int*)(tw + H);                 // [H]
+  const int es = CM * TC;
+  const int img = blockIdx.y;
+  const int x0 = blockIdx.x * TC;
+  const int lam = img_lam(g, img), ray = img_ray(g, img);
+  for (int t = threadIdx.x; t < H; t += blockDim.x) {
+    tw[t] = ((const cpx<R>*)p.tw)[t];
+    perm[t] = p.perm[t];
+  }
+  __syncthreads();
+  // load (scatter into digit-reversed rows when transforming)
+  const int nin = p.cin * H * TC;
+  for (int t = threadIdx.x; t < nin; t += blockDim.x) {
+    const int c = t / (H * TC), r = t - c * H * TC;
+    const int y = r / TC, xc = r - y * TC;
+    const int x = x0 + xc;
+    cpx<R> v = (x < W) ? X[(((size_t)img * p.cin + c) * H + y) * W + x] : mk<R>(0, 0);
+    const int ys = p.do_fwd ? perm[y] : y;
+    T[((size_t)ys * CM + c) * TC + xc] = v;
+  }
+  __syncthreads();
+  if (p.do_fwd) fft_dit<R, false>(T, es, 1, p.cin * TC, true, tw, p.plan);
+  // k-space operator
+  if (p.kop != KOP_NONE) {
+    const int nk = H * TC;
+    for (int t = threadIdx.x; t < nk; t += blockDim.x) {
+      const int ky = t / TC, xc = t - ky * TC;
+      const int kx = x0 + xc;
+      if (kx >= W) continue;
+      const size_t kidx = ((size_t)lam * H + ky) * W + kx;
+      cpx<R>* v = T + (size_t)ky * es + xc;
+      if (p.kop == KOP_DIAG) {
+        const cpx<R>* e = (const cpx<R>*)p.ktab + kidx * 2;
+        const cpx<R> ep = e[0], em = e[1];
+        for (int c = 0; c < p.cin; ++c) v[c * TC] = v[c * TC] * (((c & 1) == 0 || p.cin == 2) ? ep : em);
+      } else {
+        const cpx<R>* m = (const cpx<R>*)p.ktab + ray * p.ktab_ray_stride + kidx * p.cout * p.cin;
+        cpx<R> vin[4], vout[4];
+        for (int c = 0; c < p.cin; ++c) vin[c] = v[c * TC];
+        for (int co = 0; co < p.cout; ++co) {
+          cpx<R> s = mk<R>(0, 0);
+          for (int ci = 0; ci < p.cin; ++ci) s = cfma(m[co * p.cin + ci], vin[ci], s);
+          vout[co] = s;
+        }
+        for (int co = 0; co < p.cout; ++co) v[co * TC] = vout[co];
+      }
+    }
+    __syncthreads();
+  }
+  const int C = p.cout;
+  const R sc = (R)p.out_scale;
+  for (int j = 0; j < p.ny; ++j) {
+    cpx<R>* buf = T;
+    if (p.cy != nullptr) {
+      const R* cyj = (const R*)p.cy + (((size_t)ray * p.ny + j) * g.nlam + lam) * H;
+      for (int t = threadIdx.x; t < H * C * TC; t += blockDim.x) {
+        const int y = t / (C * TC), r = t - y * C * TC;
+        const size_t o = (size_t)y * es + r;
+        Tm[o] = T[o] * cyj[y];
+      }
+      buf = Tm;
+      __syncthreads();
+    }
+    if (p.inverse_out) fft_dif<R, true>(buf, es, 1, C * TC, true, tw, p.plan);
+    cpx<R>* Uj = U + (size_t)j * g.NI * C * H * W;
+    for (int t = threadIdx.x; t < C * H * TC; t += blockDim.x) {
+      const int c = t / (H * TC), r = t - c * H * TC;
+      const int y = r / TC, xc = r - y * TC;
+      const int x = x0 + xc;
+      if (x >= W) continue;
+      const int ys = p.inverse_out ? perm[y] : y;
+      Uj[(((size_t)img * C + c) * H + y) * W + x] = buf[((size_t)ys * CM + c) * TC + xc] * sc;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fused row pass of one layer step, one row y of all polarisations of one
+// (ray, lam) group:
+//   for each window (i, j): cx_i * U_j -> inverse row FFT -> per-voxel
+//   operator of window (i, j) -> accumulate; then forward row FFT -> X.
+// The accumulator lives in digit-reversed order, which is exactly the input
+// order the forward transform wants.
+// ---------------------------------------------------------------------------
+struct RowParams {
+  int C;                 // 4 (Epn) or 2 (E)
+  int nx, ny;            // windows per axis (1, 1 without windows)
+  const void* cx;        // [ray][i][lam][W] (null = weight 1)
+  const int* wzero;      // [ray][nx*ny]
+  const void* op;        // [ray][win][OP_REC][H][W]
+  const double* ks;      // [lam]
+  double dir;            // propagation direction (+1 / -1)
+  double in_scale;       // 1/W of the inverse row transform (and 1/H of the column one)
+  FFTPlan plan;
+  const void* tw;
+  const int* perm;
+  int identity_op;       // 1: unit operator (no material), used by tests
+};
+
+template <typename R>
+__device__ __forceinline__ cpx<R> phase_of(cpx<R> arg, R k) {
+  return cexp_i(mk<R>(arg.re * k, arg.im * k));
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cpx<R>* __restrict__ U,
+                                                   cpx<R>* __restrict__ X) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int W = g.W, H = g.H, C = p.C, NP = g.npol;
+  cpx<R>* ub = (cpx<R>*)smem_raw;           // [NP][C][W]   U_j rows (natural order)
+  cpx<R>* acc = ub + (size_t)NP * C * W;    // [NP][C][W]   accumulator (digit-reversed)
+  cpx<R>* tmp = acc + (size_t)NP * C * W;   // [C][W]       window work buffer
+  cpx<R>* tw = tmp + (size_t)C * W;         // [W]
+  int* perm = (int*)(tw + W);               // [W]
+  const int y = blockIdx.x;
+  const int grp = blockIdx.y;               // ray * nlam + lam
+  const int ray = grp / g.nlam, lam = grp - ray * g.nlam;
+  const int HW = H * W;
+  const int nwin = p.nx * p.ny;
+  for (int t = threadIdx.x; t < W; t += blockDim.x) {
+    tw[t] = ((const cpx<R>*)p.tw)[t];
+    perm[t] = p.perm[t];
+  }
+  for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) acc[t] = mk<R>(0, 0);
+  const R kphase = (R)(p.ks[lam] * p.dir);
+  const R sc = (R)p.in_scale;
+  __syncthreads();
+  for (int j = 0; j < p.ny; ++j) {
+    const cpx<R>* Uj = U + (size_t)j * g.NI * C * HW;
+    for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) {
+      const int pol = t / (C * W), r = t - pol * C * W;
+      const int c = r / W, x = r - c * W;
+      const int img = (ray * NP + pol) * g.nlam + lam;
+      ub[t] = Uj[(((size_t)img * C + c) * H + y) * W + x];
+    }
+    __syncthreads();
+    for (int i = 0; i < p.nx; ++i) {
+      const int w = i * p.ny + j;
+      if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
+      const R* cxi = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+      const cpx<R>* opw = (const cpx<R>*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      for (int pol = 0; pol < NP; ++pol) {
+        for (int t = threadIdx.x; t < C * W; t += blockDim.x) {
+          const int x = t % W;
+          cpx<R> v = ub[(size_t)pol * C * W + t];
+          tmp[t] = cxi ? v * cxi[x] : v;
+        }
+        __syncthreads();
+        fft_dif<R, true>(tmp, 1, W, C, false, tw, p.plan);
+        for (int x = threadIdx.x; x < W; x += blockDim.x) {
+          const int q = perm[x];
+          cpx<R>* a = acc + (size_t)pol * C * W;
+          if (p.identity_op) {
+            for (int c = 0; c < C; ++c) a[c * W + q] = a[c * W + q] + tmp[c * W + q] * sc;
+            continue;
+          }
+          // forward block acts on components (0, 2) of Epn, or (0, 1) of E
+          const int c0 = 0, c1 = (C == 4) ? 2 : 1;
+          {
+            const cpx<R> e00 = opw[0 * HW + x], e01 = opw[1 * HW + x], e10 = opw[2 * HW + x], e11 = opw[3 * HW + x];
+            const cpx<R> idet = opw[4 * HW + x];
+            const cpx<R> p0 = phase_of(opw[5 * HW + x], kphase) * idet;
+            const cpx<R> p1 = phase_of(opw[6 * HW + x], kphase) * idet;
+            const cpx<R> h0 = tmp[c0 * W + q] * sc, h1 = tmp[c1 * W + q] * sc;
+            const cpx<R> w0 = (e11 * h0 - e01 * h1) * p0;
+            const cpx<R> w1 = (e00 * h1 - e10 * h0) * p1;
+            a[c0 * W + q] = a[c0 * W + q] + e00 * w0 + e01 * w1;
+            a[c1 * W + q] = a[c1 * W + q] + e10 * w0 + e11 * w1;
+          }
+          if (C == 4) {
+            const cpx<R> e00 = opw[7 * HW + x], e01 = opw[8 * HW + x], e10 = opw[9 * HW + x], e11 = opw[10 * HW + x];
+            const cpx<R> idet = opw[11 * HW + x];
+            const cpx<R> p0 = phase_of(opw[12 * HW + x], kphase) * idet;
+            const cpx<R> p1 = phase_of(opw[13 * HW + x], kphase) * idet;
+            const cpx<R> h0 = tmp[1 * W + q] * sc, h1 = tmp[3 * W + q] * sc;
+            const cpx<R> w0 = (e11 * h0 - e01 * h1) * p0;
+            const cpx<R> w1 = (e00 * h1 - e10 * h0) * p1;
+            a[1 * W + q] = a[1 * W + q] + e00 * w0 + e01 * w1;
+            a[3 * W + q] = a[3 * W + q] + e10 * w0 + e11 * w1;
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+  fft_dit<R, false>(acc, 1, W, NP * C, false, tw, p.plan);
+  for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) {
+    const int pol = t / (C * W), r = t - pol * C * W;
+    const int c = r / W, x = r - c * W;
+    const int img = (ray * NP + pol) * g.nlam + lam;
+    X[(((size_t)img * C + c) * H + y) * W + x] = acc[t];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain row FFT of every (image, component, y) line, in place.
+// ---------------------------------------------------------------------------
+template <typename R, bool INV>
+__global__ void __launch_bounds__(256) k_fft_rows(cpx<R>* __restrict__ data, int nlines, int W, FFTPlan plan,
+                                                  const cpx<R>* __restrict__ twg, const int* __restrict__ permg,
+                                                  double scale, int lpb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cpx<R>* s = (cpx<R>*)smem_raw;
+  cpx<R>* tw = s + (size_t)lpb * W;
+  int* perm = (int*)(tw + W);
+  for (int t = threadIdx.x; t < W; t += blockDim.x) {
+    tw[t] = twg[t];
+    perm[t] = permg[t];
+  }
+  __syncthreads();
+  const int l0 = blockIdx.x * lpb;
+  const int nl = min(lpb, nlines - l0);
+  for (int t = threadIdx.x; t < nl * W; t += blockDim.x) {
+    const int l = t / W, x = t - l * W;
+    cpx<R> v = data[(size_t)(l0 + l) * W + x];
+    s[l * W + (INV ? x : perm[x])] = v;
+  }
+  __syncthreads();
+  if (INV)
+    fft_dif<R, true>(s, 1, W, nl, false, tw, plan);
+  else
+    fft_dit<R, false>(s, 1, W, nl, false, tw, plan);
+  const R sc = (R)scale;
+  for (int t = threadIdx.x; t < nl * W; t += blockDim.x) {
+    const int l = t / W, x = t - l * W;
+    data[(size_t)(l0 + l) * W + x] = s[l * W + (INV ? perm[x] : x)] * sc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Between-pass helpers of the 4x4 multi-pass (reflection) iteration
+// (dtmm/transfer.py:815-873).  Arrays are [image][4][H][W].
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ double poynting(const cpx<R> f[4]) {
+  return (double)(f[0].re * f[1].re + f[0].im * f[1].im) - (double)(f[2].re * f[3].re + f[2].im * f[3].im);
+}
+
+struct NotchParams {
+  int on;
+  double x0, sigma, betamax_unused;
+  const double* ks;
+};
+
+__device__ __forceinline__ double notch_k(const NotchParams& n, const Grid& g, int lam, int ky, int kx) {
+  if (!n.on) return 1.0;
+  double beta, phi;
+  betaphi_k(g, n.ks[lam], ky, kx, beta, phi);
+  double a = fabs(beta - n.x0);
+  if (a > n.x0) a = n.x0;
+  if (a < 0.0) a = 0.0;
+  return (1.0 - exp(-a / n.sigma)) / (1.0 - exp(-n.x0 / n.sigma));
+}
+
+// k-space: f <- notch * P . f, optionally with the per-k intensity renormalisation
+// of project_normalized_fft (dtmm/transfer.py:67-90).
+template <typename R>
+__global__ void k_kproject(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ P, Grid g, int normalize, NotchParams nt) {
+  const int HW = g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * HW) return;
+  const int img = (int)(t / HW), k = (int)(t - (size_t)img * HW);
+  const int lam = img % g.nlam;
+  const int ky = k / g.W, kx = k - ky * g.W;
+  cpx<R> v[4], o[4];
+  for (int c = 0; c < 4; ++c) v[c] = f[((size_t)img * 4 + c) * HW + k];
+  const cpx<R>* m = P + ((size_t)lam * HW + k) * 16;
+  for (int i = 0; i < 4; ++i) {
+    cpx<R> s = mk<R>(0, 0);
+    for (int j = 0; j < 4; ++j) s = cfma(m[i * 4 + j], v[j], s);
+    o[i] = s;
+  }
+  double fact = 1.0;
+  if (normalize) {
+    double i1 = poynting(v), i2 = poynting(o);
+    if (i2 == 0.0) {
+      i2 = 1.0;
+      i1 = 0.0;
+    }
+    fact = i1 / i2;
+    if (fact <= -1) fact = -1;
+    if (fact >= 1) fact = 1;
+    fact = fabs(fact);
+  }
+  fact *= notch_k(nt, g, lam, ky, kx);
+  for (int c = 0; c < 4; ++c) f[((size_t)img * 4 + c) * HW + k] = o[c] * (R)fact;
+}
+
+// per-image pixel sums of the z-Poynting component, FP64 accumulation
+template <typename R>
+__global__ void k_total_intensity(const cpx<R>* __restrict__ f, Grid g, double* out) {
+  const int HW = g.H * g.W;
+  const int img = blockIdx.x;
+  double s = 0.0;
+  for (int k = threadIdx.x; k < HW; k += blockDim.x) {
+    cpx<R> v[4];
+    for (int c = 0; c < 4; ++c) v[c] = f[((size_t)img * 4 + c) * HW + k];
+    s += poynting(v);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[img] = red[0];
+}
+
+// elementwise: out = a*x + b*y with per-image real factors (null = 1)
+template <typename R>
+__global__ void k_axpby(cpx<R>* out, const cpx<R>* x, const double* ax, double sx, const cpx<R>* y, const double* by,
+                        double sy, Grid g, int C) {
+  const size_t per = (size_t)C * g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * per) return;
+  const int img = (int)(t / per);
+  double fa = sx * (ax ? ax[img] : 1.0);
+  cpx<R> r = x ? x[t] * (R)fa : mk<R>(0, 0);
+  if (y) {
+    double fb = sy * (by ? by[img] : 1.0);
+    r = r + y[t] * (R)fb;
+  }
+  out[t] = r;
+}
+
+// per-image ratio a / b (the total-intensity rescale of odd passes)
+__global__ void k_ratio(const double* a, const double* b, double* out, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) out[t] = a[t] / b[t];
+}
+
+// copy between precisions / layouts: dst[image][c][..] = src[image][c_map[c]][..]
+template <typename RD, typename RS>
+__global__ void k_convert(cpx<RD>* dst, const cpx<RS>* src, size_t n) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) dst[t] = mk<RD>((RD)src[t].re, (RD)src[t].im);
+}
+
+// FFT twiddles exp(-2 pi i t / N) (FP64, then rounded) and digit reversal
+template <typename R>
+__global__ void k_fft_tables(FFTPlan plan, cpx<R>* tw, int* perm) {
+  const int n = plan.n;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * (double)t / (double)n, &s, &c);
+    tw[t] = mk<R>((R)c, (R)s);
+    int m = t, pos = 0, stride = n;
+    for (int q = plan.nr - 1; q >= 0; --q) {
+      stride /= plan.r[q];
+      pos += (m % plan.r[q]) * stride;
+      m /= plan.r[q];
+    }
+    perm[t] = pos;
+  }
+}
+
+// isotropic effective medium: mean over every voxel of (e0 + e1 + e2) / 3
+// (effective_block with symmetry 0, dtmm/data.py:1364-1392), FP64
+__global__ void k_eps_mean(const void* epsv, int eps_complex, long long s0, long long s1, long long s2, int L, int H,
+                           int W, double* out) {
+  const long long n = (long long)L * H * W;
+  double sr = 0.0, si = 0.0;
+  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+    const int l = (int)(t / ((long long)H * W));
+    const long long r = t - (long long)l * H * W;
+    const int y = (int)(r / W), x = (int)(r - (long long)y * W);
+    const long long o = l * s0 + y * s1 + x * s2;
+    if (eps_complex) {
+      const cpx<double>* e = (const cpx<double>*)epsv + o;
+      sr += (e[0].re + e[1].re + e[2].re) / 3.0;
+      si += (e[0].im + e[1].im + e[2].im) / 3.0;
+    } else {
+      const double* e = (const double*)epsv + o;
+      sr += (e[0] + e[1] + e[2]) / 3.0;
+    }
+  }
+  __shared__ double red[2][1024];
+  red[0][threadIdx.x] = sr;
+  red[1][threadIdx.x] = si;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + st];
+      red[1][threadIdx.x] += red[1][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = red[0][0] / (double)n;
+    out[1] = red[1][0] / (double)n;
+  }
+}
+
+}  // namespace dtmm

@@ -1,0 +1,441 @@
+"""Drop-in ``transfer_field`` backed by the GB300 engine.
+
+Same signature, defaults, option resolution, return values and in-place
+behaviour as the reference's ``dtmm.transfer.transfer_field``
+(dtmm/transfer.py:322-552).  Option resolution and the data model are Python;
+the transfer itself is one call into the CUDA library
+(``include/dtmm_gb300.h``).  Options outside the GPU path raise
+``NotImplementedError`` -- there is no CPU fallback.
+
+Extension: ``precision=`` selects the bulk arithmetic, "double" (complex128,
+the reference's precision, the default) or "mixed" (complex64 bulk with the
+FP64 eigen-solve and operator tables); ``set_precision`` changes the default.
+"""
+from __future__ import annotations
+
+import ctypes
+import warnings
+
+import numpy as np
+
+from . import _lib
+
+# reference defaults (dtmm/dtmm.ini read by dtmm/conf.py:459-531)
+BETAMAX = 0.8
+SMOOTH = 0.1
+N_COVER = 1.5
+DTMM_NORM_FFT = 1 << 0
+DTMM_NORM_REF = 1 << 1
+
+_defaults = {
+    "nin": N_COVER,
+    "nout": N_COVER,
+    # the ini file stores method = "2x2" and the reference reads the quotes
+    # too (dtmm/conf.py:506): the default is the string '"2x2"', which selects
+    # the 2x2 method and makes reflection resolve to 1
+    "method": '"2x2"',
+    "npass": 1,
+    "diffraction": 1,
+    "reflection": None,
+    "eff_data": 0,
+    "betamax": BETAMAX,
+}
+_precision = ["double"]
+
+
+def set_precision(p):
+    """Default bulk precision: "double" (complex128) or "mixed" (complex64 bulk, FP64 eigen-solve)."""
+    if p not in ("double", "mixed"):
+        raise ValueError("precision must be 'double' or 'mixed'")
+    old = _precision[0]
+    _precision[0] = p
+    return old
+
+
+def get_default_config_option(name, value=None):
+    """(dtmm/conf.py:531)"""
+    return _defaults[name] if value is None else value
+
+
+def k0(wavelength, pixelsize=1.0):
+    """2*pi/wavelength*pixelsize (dtmm/wave.py:280)."""
+    return np.asarray(2 * np.pi / np.asarray(wavelength) * pixelsize, np.float64)
+
+
+# ---------------------------------------------------------------------------
+# optical data (dtmm/data.py:534-682, non-dispersive blocks)
+# ---------------------------------------------------------------------------
+def _validate_block(block, shape):
+    thickness, material, angles = block
+    if callable(material):
+        raise NotImplementedError("dispersive (callable) material data: use split_wavelengths=True")
+    thickness = np.asarray(thickness, np.float64)
+    material = np.asarray(material)
+    material = material.astype(np.complex128 if np.iscomplexobj(material) else np.float64, copy=False)
+    angles = np.asarray(angles, np.float64)
+    if thickness.ndim == 0:
+        thickness = thickness[None]
+        material = material[None, ...]
+        angles = angles[None, ...]
+    elif thickness.ndim != 1:
+        raise ValueError("Thickess dimension should be 1.")
+    if material.ndim == 2:
+        material = material[:, None, None, :]
+    elif material.ndim == 3:
+        material = material[:, None, :, :]
+    elif material.ndim != 4:
+        raise ValueError("Invalid material dimensions.")
+    if angles.ndim == 2:
+        angles = angles[:, None, None, :]
+    elif angles.ndim == 3:
+        angles = angles[:, None, :, :]
+    n = len(thickness)
+    target = (n,) + tuple(shape) + (3,)
+    np.broadcast_shapes(material.shape, target)
+    np.broadcast_shapes(angles.shape, target)
+    return thickness, material, angles
+
+
+def validate_optical_data(data, shape):
+    if isinstance(data, list):
+        return [_validate_block(b, shape) for b in data]
+    warnings.warn("A single-block optical data must be a list of length 1. Converting optical data to list. "
+                  "In the future, exception will be raised.", DeprecationWarning)
+    return validate_optical_data([data], shape)
+
+
+def _compact(a, full_shape):
+    """Device-upload form of a broadcastable (L,h,w,3) array: the distinct data
+    plus element strides of the (layer, y, x) axes (0 on broadcast axes)."""
+    a = np.asarray(a)
+    b = np.broadcast_to(a, full_shape)
+    idx = []
+    for ax in range(3):
+        idx.append(slice(None) if (b.strides[ax] != 0 and b.shape[ax] > 1) else slice(0, 1))
+    base = np.ascontiguousarray(b[tuple(idx)])
+    strides = []
+    step = 3
+    for ax in (2, 1, 0):
+        strides.append(step if base.shape[ax] > 1 else 0)
+        step *= base.shape[ax]
+    return base, tuple(reversed(strides))
+
+
+# ---------------------------------------------------------------------------
+# beam direction estimate for beta=None (dtmm/field.py:492, :866; window.py:33)
+# ---------------------------------------------------------------------------
+def _blackman(shape):
+    ay, ax = (np.arange(-n / 2.0 + 0.5, n / 2.0 + 0.5) for n in shape)
+    xx, yy = np.meshgrid(ax, ay, indexing="xy")
+    ny, nx = (n / 2 for n in shape)
+    r = ((xx / nx) ** 2 + (yy / ny) ** 2) ** 0.5
+    out = 0.42 + 0.5 * np.cos(np.pi * r) + 0.08 * np.cos(2 * np.pi * r)
+    out[r >= 1.0] = 0.0
+    return out
+
+
+def _field2betaphi(field, ks, multiray):
+    """Mean beta, phi of the input field; runs on the GPU with torch.fft on the
+    already-uploaded field (input analysis before the transfer)."""
+    import torch
+
+    f = torch.fft.fft2(field * torch.as_tensor(_blackman(field.shape[-2:]), device=field.device, dtype=field.real.dtype))
+    h, w = field.shape[-2:]
+    fx = torch.as_tensor(np.fft.fftfreq(w), device=field.device, dtype=torch.float64)
+    fy = torch.as_tensor(np.fft.fftfreq(h), device=field.device, dtype=torch.float64)
+    l = (2 * np.pi / torch.as_tensor(np.asarray(ks, np.float64), device=field.device))[:, None, None]
+    bx = l * fx[None, None, :]
+    by = l * fy[None, :, None]
+    s = (f.real.double() ** 2 + f.imag.double() ** 2)
+    sx = (s * bx[:, None]).sum(dim=(-3, -2, -1))
+    sy = (s * by[:, None]).sum(dim=(-3, -2, -1))
+    ss = s.sum(dim=(-3, -2, -1))
+    beta = (sx ** 2 + sy ** 2) ** 0.5 / ss
+    phi = torch.atan2(sy, sx)
+    beta = beta.cpu().numpy()
+    phi = phi.cpu().numpy()
+    if field.ndim > 4 and multiray:
+        ax = tuple(range(1, field.ndim - 3))
+        return beta.mean(axis=ax), phi.mean(axis=ax)
+    return beta.mean(), phi.mean()
+
+
+# ---------------------------------------------------------------------------
+# the engine call
+# ---------------------------------------------------------------------------
+class _Material:
+    """Optical block resident on the device (uploaded once per call, or kept by the caller)."""
+
+    def __init__(self, block, shape, device):
+        import torch
+
+        d, epsv, epsa = block
+        L = len(d)
+        full = (L,) + tuple(shape) + (3,)
+        ev, self.ev_strides = _compact(epsv, full)
+        ea, self.ea_strides = _compact(epsa, full)
+        self.eps_complex = bool(np.iscomplexobj(ev))
+        if self.eps_complex:
+            ev = ev.astype(np.complex128)
+        else:
+            ev = ev.astype(np.float64)
+        flat = ev.reshape(-1, 3)
+        if not np.all(flat[:, 0] == flat[:, 1]):
+            raise NotImplementedError(
+                "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
+        self.epsv = torch.from_numpy(np.ascontiguousarray(ev)).to(device)
+        self.epsa = torch.from_numpy(np.ascontiguousarray(ea.astype(np.float64))).to(device)
+        self.thickness = np.asarray(d, np.float64)
+        self.nlayers = L
+
+
+def _engine_call(field_dev, out_dev, bulk_dev, out_given, mat, ks, beta, phi, nray, npol, nlam, method,
+                 diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, stream=None):
+    import torch
+
+    lib = _lib.load()
+    h, w = field_dev.shape[-2:]
+    L = mat.nlayers
+    thick = np.ascontiguousarray(mat.thickness, np.float64)
+    nst = np.ascontiguousarray(np.broadcast_to(np.asarray(nstep, np.int32), (L,)), np.int32)
+    ksa = np.ascontiguousarray(ks, np.float64)
+    ba = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float64).reshape(-1), (nray,)), np.float64)
+    pa = np.ascontiguousarray(np.broadcast_to(np.asarray(phi, np.float64).reshape(-1), (nray,)), np.float64)
+    d = _lib.TransferDesc()
+    d.height, d.width = int(h), int(w)
+    d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
+    d.method = 4 if method == "4x4" else 2
+    d.diffraction = int(diffraction)
+    d.reflection = int(reflection)
+    d.npass = int(npass)
+    d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
+    d.betamax, d.nin, d.nout, d.smooth = float(betamax), float(nin), float(nout), float(smooth)
+    d.nlayers = L
+    d.thickness = thick.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.nstep = nst.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    d.epsv = mat.epsv.data_ptr()
+    d.eps_complex = int(mat.eps_complex)
+    d.epsv_strides[:] = mat.ev_strides
+    d.epsa = mat.epsa.data_ptr()
+    d.epsa_strides[:] = mat.ea_strides
+    d.ks = ksa.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.beta = ba.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.phi = pa.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.op_cache_bytes = 0
+    nbytes = lib.dtmm_transfer_workspace_size(ctypes.byref(d))
+    if nbytes == 0:
+        _lib.check(_lib.DTMM_EINVAL if "not supported" not in _lib.last_error() and "factor" not in _lib.last_error()
+                   else _lib.DTMM_ENOTSUP)
+    ws = torch.empty(int(nbytes), dtype=torch.uint8, device=field_dev.device)
+    io = _lib.TransferIO()
+    io.field_in = field_dev.data_ptr()
+    io.field_out = out_dev.data_ptr()
+    io.out_given = int(out_given)
+    io.bulk = bulk_dev.data_ptr() if bulk_dev is not None else None
+    if stream is None:
+        stream = torch.cuda.current_stream(field_dev.device).cuda_stream
+    _lib.check(lib.dtmm_transfer(ctypes.byref(d), ctypes.byref(io), ctypes.c_void_p(ws.data_ptr()),
+                                 ctypes.c_size_t(int(nbytes)), ctypes.c_void_p(stream)))
+    return ws
+
+
+def _require_cuda():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("dtmm_gb300.transfer_field needs a CUDA GPU (the engine has no CPU path)")
+    return torch
+
+
+def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
+                     diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision):
+    torch = _require_cuda()
+    if method == "4x4":
+        if reflection not in (1, 2, 3, 4):
+            raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
+    elif reflection not in (0, 1, 2):
+        raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
+    if method != "4x4" and npass > 1 and reflection == 0:
+        raise ValueError("Reflection mode `0` not compatible with npass > 1")
+    if reflection not in ((1,) if method == "4x4" else (0, 1)):
+        raise NotImplementedError("reflection mode %d (real-space reflections) is outside the GPU engine" % reflection)
+    if method != "4x4" and npass != 1:
+        raise NotImplementedError("the 2x2 method with npass > 1 is outside the GPU engine")
+    if not (0 <= diffraction < np.inf):
+        raise NotImplementedError("full (modal) diffraction is outside the GPU engine")
+    if diffraction == 0:
+        if method == "4x4":
+            raise ValueError("Invalid diffraction value")
+        raise NotImplementedError("diffraction=0 is outside the GPU engine")
+    if norm != DTMM_NORM_FFT and method == "4x4" and npass > 1:
+        raise NotImplementedError("norm modes other than DTMM_NORM_FFT are outside the GPU engine")
+    if smooth < 0:
+        smooth = 0.0
+    field_in = np.asarray(field_in)
+    if field_in.ndim < 4:
+        raise ValueError("Invald field dimensions")
+    shape = field_in.shape[-2:]
+    nlam = field_in.shape[-4]
+    wavelengths = np.asarray(wavelengths)
+    if wavelengths.ndim != 1 or len(wavelengths) != nlam:
+        raise ValueError("Incompatible wavelengths shape.")
+    od = validate_optical_data(optical_data, shape)
+    if len(od) != 1:
+        raise NotImplementedError("optical data with more than one block is outside the GPU engine")
+    if ret_bulk and method != "4x4":
+        raise NotImplementedError("ret_bulk is implemented for the 4x4 method")
+    ks = k0(wavelengths, pixelsize)
+    cdt = torch.complex128 if precision == "double" else torch.complex64
+    dev = torch.device("cuda", torch.cuda.current_device())
+    field_dev = torch.from_numpy(np.ascontiguousarray(field_in, np.complex128)).to(dev)
+    if beta is None and phi is None:
+        beta, phi = _field2betaphi(field_dev, ks, multiray)
+    elif beta is None or phi is None:
+        raise ValueError("Both beta and phi must be defined!")
+    beta = np.asarray(beta, np.float64)
+    phi = np.asarray(phi, np.float64)
+    if beta.ndim != phi.ndim:
+        raise ValueError("Beta nad phi should have same dimensions!")
+    if beta.ndim == 1:
+        if len(beta) != len(phi):
+            raise ValueError("Beta nad phi should have same length!")
+        nray = len(beta)
+        if field_in.ndim < 5 or field_in.shape[0] != nray:
+            if nray == 1:
+                beta, phi = beta[0], phi[0]
+                nray = 1
+            else:
+                raise ValueError("per-ray beta needs the rays on the first field axis")
+    elif beta.ndim != 0:
+        raise ValueError("Only length 1 or scalar values are supported for beta and phi")
+    else:
+        nray = 1
+    nimg = int(np.prod(field_in.shape[:-3]))
+    npol = nimg // (nray * nlam)
+    mat = _Material(od[0], shape, dev)
+    fdev = field_dev.to(cdt).contiguous()
+    L = mat.nlayers
+    bulk_dev = None
+    if ret_bulk:
+        bulk_dev = torch.zeros((L + 2,) + tuple(field_in.shape), dtype=cdt, device=dev)
+        bulk_dev[0] = fdev
+        fin_dev = bulk_dev[0]
+        fout_dev = bulk_dev[-1]
+        out_given = 0
+        if out is not None:
+            ob = np.asarray(out)
+            bulk_dev[-1] = torch.from_numpy(np.ascontiguousarray(ob[-1], np.complex128)).to(dev).to(cdt)
+            out_given = 1
+    else:
+        fin_dev = fdev
+        if out is not None and method == "4x4":
+            fout_dev = torch.from_numpy(np.ascontiguousarray(out, np.complex128)).to(dev).to(cdt).contiguous()
+            out_given = 1
+        else:
+            fout_dev = torch.empty_like(fdev)
+            out_given = 0
+    _engine_call(fin_dev, fout_dev, bulk_dev, out_given, mat, ks, beta, phi, nray, npol, nlam, method, diffraction,
+                 reflection, npass, nstep, betamax, nin, nout, smooth, precision)
+    if ret_bulk:
+        res = bulk_dev.to(torch.complex128).cpu().numpy()
+        if out is not None:
+            out[...] = res
+            res = out
+        return res
+    res = fout_dev.to(torch.complex128).cpu().numpy()
+    if npass > 1 and method == "4x4":
+        # the reference rewrites the caller's input with the reflected field
+        field_in[...] = fin_dev.to(torch.complex128).cpu().numpy()
+    if out is not None:
+        out[...] = res
+        res = out
+    return res
+
+
+def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout=None, npass=None, nstep=1,
+                   diffraction=None, reflection=None, method=None, multiray=False, norm=DTMM_NORM_FFT,
+                   betamax=None, smooth=SMOOTH, split_rays=False, split_diffraction=False,
+                   split_wavelengths=False, split_layers=False, eff_data=None, ret_bulk=False, out=None,
+                   precision=None):
+    """Transfer input field data through optical data (dtmm/transfer.py:322).
+
+    Returns ``(field_out, wavelengths, pixelsize)``; with npass > 1 the input
+    field array is overwritten with the reflected field, as in the reference.
+    See the reference documentation for the meaning of every argument.
+    ``split_diffraction`` only trades memory for time in the reference and
+    has no effect here.
+    """
+    nin = get_default_config_option("nin", nin)
+    nout = get_default_config_option("nout", nout)
+    method = get_default_config_option("method", method)
+    npass = get_default_config_option("npass", npass)
+    eff_data = get_default_config_option("eff_data", eff_data)
+    diffraction = get_default_config_option("diffraction", diffraction)
+    reflection = get_default_config_option("reflection", reflection)
+    betamax = get_default_config_option("betamax", betamax)
+    precision = _precision[0] if precision is None else precision
+    if precision not in ("double", "mixed"):
+        raise ValueError("precision must be 'double' or 'mixed'")
+    if method == "4x4" and npass > 1 and diffraction == False:  # noqa: E712 (reference semantics)
+        warnings.warn("The 4x4 method with diffraction disabled is not yet supported for input fields with beta "
+                      ">0. Use 2x2 method insted.")
+    if npass == -1 or npass == np.inf:
+        raise NotImplementedError("npass=-1 (exact modal transfer, dtmm/tmm3d.py) is outside the GPU engine")
+    if reflection is None:
+        reflection = 0 if method == "2x2" else 1
+        if method == "4x4" and diffraction == 0:
+            reflection = 2
+        if npass > 1:
+            reflection = 1
+            if diffraction > 1 and method == "2x2":
+                reflection = 2
+    if eff_data not in (0, "isotropic"):
+        raise NotImplementedError("only isotropic effective data (eff_data=0) is supported by the GPU engine")
+    if split_layers:
+        raise NotImplementedError("split_layers is outside the GPU engine")
+    field_in, wavelengths, pixelsize = field_data
+    if split_wavelengths and not isinstance(field_in, tuple) and not ret_bulk:
+        field_in = np.asarray(field_in)
+        out_field = np.empty_like(field_in) if out is None else out
+        for i in range(len(wavelengths)):
+            fi = field_in[..., i:i + 1, :, :, :]
+            fcopy = np.array(fi)
+            r = transfer_field((fcopy, np.asarray(wavelengths)[i:i + 1], pixelsize), optical_data, beta, phi, nin,
+                               nout, npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
+                               split_rays, split_diffraction, False, False, eff_data, False, None, precision)
+            out_field[..., i, :, :, :] = r[0][..., 0, :, :, :]
+            if npass > 1:
+                field_in[..., i, :, :, :] = fcopy[..., 0, :, :, :]
+        return out_field, wavelengths, pixelsize
+    if isinstance(field_in, tuple):
+        outs = []
+        olist = out if out is not None else [None] * len(field_in)
+        for f, wl, o in zip(field_in, wavelengths, olist):
+            r = transfer_field((f, [wl] if np.ndim(wl) == 0 else wl, pixelsize), optical_data, beta, phi, nin, nout,
+                               npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
+                               split_rays, split_diffraction, False, False, eff_data, ret_bulk, o, precision)
+            outs.append(r)
+        return tuple(outs)
+    if split_rays:
+        field_in = np.asarray(field_in)
+        nrays = len(field_in)
+        res = np.empty((len(optical_data[0][0]) + 2,) + field_in.shape, np.complex128) if ret_bulk else \
+            (np.empty_like(field_in) if out is None else out)
+        bl = [None] * nrays if beta is None else list(np.broadcast_to(beta, (nrays,)))
+        pl = [None] * nrays if phi is None else list(np.broadcast_to(phi, (nrays,)))
+        for i in range(nrays):
+            fi = field_in[i]
+            r = _transfer_single(fi, wavelengths, pixelsize, optical_data, bl[i], pl[i], nin, nout, npass, nstep,
+                                 diffraction, reflection, method, False, norm, betamax, smooth, ret_bulk, None,
+                                 precision)
+            if ret_bulk:
+                res[:, i] = r
+            else:
+                res[i] = r
+        return res, wavelengths, pixelsize
+    res = _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
+                           diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision)
+    return res, wavelengths, pixelsize
+
+
+__all__ = ["transfer_field", "set_precision", "DTMM_NORM_FFT", "DTMM_NORM_REF"]

@@ -1,0 +1,107 @@
+/*
+ * dtmm_gb300 -- C ABI of the GB300 field-transfer engine.
+ *
+ * The reference (dtmm, pure Python + numba) has no FFI; its drop-in boundary
+ * is the Python call
+ *     dtmm.transfer_field(field_data, optical_data, beta, phi, nin, nout,
+ *                         npass, nstep, diffraction, reflection, method, ...)
+ * (dtmm/transfer.py:322-552) with the method drivers transfer_4x4
+ * (dtmm/transfer.py:618-884) and transfer_2x2 (dtmm/transfer.py:1009-1183).
+ * This ABI replaces the body of those drivers: option resolution, input
+ * validation and the (field, wavelengths, pixelsize) / (thickness, eps,
+ * angles) data model stay in the Python layer (dtmm_gb300/transfer.py), which
+ * calls dtmm_transfer() once per transfer_field call.
+ *
+ * All pointers in dtmm_transfer_io and the material pointers in the
+ * descriptor are device pointers; all other arrays in the descriptor are host
+ * arrays read during the call.  Every function returns DTMM_OK (0) or a
+ * negative status; dtmm_last_error() describes the last failure of the
+ * calling thread.  No exception crosses the ABI.
+ */
+#ifndef DTMM_GB300_H
+#define DTMM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DTMM_OK 0
+#define DTMM_EINVAL (-1)      /* invalid argument (ValueError in the reference)         */
+#define DTMM_ENOSPACE (-2)    /* workspace smaller than dtmm_transfer_workspace_size() */
+#define DTMM_ECUDA (-3)       /* a CUDA call failed                                     */
+#define DTMM_ENOTSUP (-4)     /* option combination outside this engine                 */
+
+#define DTMM_PRECISION_MIXED 0  /* complex64 bulk, FP64 eigen-solve and operator tables */
+#define DTMM_PRECISION_DOUBLE 1 /* complex128 bulk (the reference's default precision)  */
+
+typedef struct dtmm_transfer_desc {
+  /* grid and images: images = nray * npol * nlam, in the reference's
+     ([rays], [pols], wavelength) axis order */
+  int height, width;
+  int nlam, npol, nray;
+  /* method and options (resolved by the caller as dtmm/transfer.py:433-465 does) */
+  int method;        /* 4 = "4x4", 2 = "2x2"                                   */
+  int diffraction;   /* >= 1; n > 1 groups modes into n x n windows             */
+  int reflection;    /* 4x4: 1 ; 2x2: 0 or 1                                    */
+  int npass;         /* 4x4: >= 1 ; 2x2: 1                                      */
+  int precision;     /* DTMM_PRECISION_*                                        */
+  double betamax, nin, nout, smooth;
+  /* layers of the (single) optical block */
+  int nlayers;
+  const double* thickness; /* host [nlayers], pixels                          */
+  const int* nstep;        /* host [nlayers], sub-steps per layer (>= 1)      */
+  /* material, device pointers; strides in elements of the (layer, y, x)
+     axes, 0 for a broadcast axis; the last axis (3 values) is contiguous */
+  const void* epsv;        /* float64 or complex128 eigenvalues                 */
+  int eps_complex;
+  long long epsv_strides[3];
+  const double* epsa;      /* float64 Euler angles (psi, theta, phi)            */
+  long long epsa_strides[3];
+  /* beams, host arrays */
+  const double* ks;        /* [nlam] 2*pi*pixelsize/wavelength                  */
+  const double* beta;      /* [nray]                                            */
+  const double* phi;       /* [nray]                                            */
+  /* upper bound on the bytes of cached per-layer operators (npass > 1 reuses
+     them across passes when they fit); 0 selects the default (48 GiB) */
+  size_t op_cache_bytes;
+} dtmm_transfer_desc;
+
+typedef struct dtmm_transfer_io {
+  /* [images][4][height][width] complex (complex64 for MIXED, complex128 for
+     DOUBLE).  field_in is rewritten in place with the reflected field when
+     npass > 1 (dtmm/transfer.py:843-866), as the reference does. */
+  void* field_in;
+  void* field_out;
+  int out_given;  /* 4x4: field_out holds the caller's out= array; its reflected
+                     part is kept (dtmm/transfer.py:674) */
+  /* optional (4x4): [(nlayers + 2)][images][4][H][W]; when set, receives the
+     field after every layer (ret_bulk); field_in/field_out must then point at
+     its first / last slab */
+  void* bulk;
+} dtmm_transfer_io;
+
+/* ABI version of this header (1). */
+int dtmm_abi_version(void);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* dtmm_last_error(void);
+
+/* Device workspace (bytes) that dtmm_transfer needs for this descriptor;
+   0 on an invalid descriptor (see dtmm_last_error). */
+size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc);
+
+/* Transfer the input field through the optical block: the work of
+   transfer_4x4 / transfer_2x2 (dtmm/transfer.py:618, :1009) for the
+   k-space ("effective", reflection mode 1 / 0-1) split-step method.
+   `stream` is a cudaStream_t (NULL = legacy default stream).  The call
+   enqueues the work and returns; results are ready when the stream is. */
+int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
+                  size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DTMM_GB300_H */

@@ -1,0 +1,86 @@
+"""The C-ABI library builds, loads and validates descriptors without a GPU."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from dtmm_gb300 import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    import re
+
+    text = open(os.path.join(ROOT, "include", "dtmm_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(dtmm_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = _declared_symbols()
+    assert set(declared) == set(_lib.ABI_SYMBOLS)
+    out = subprocess.run(["nm", "-D", "--defined-only", _build.lib_path()], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    for name in declared:
+        assert name in exported, name
+        assert getattr(lib, name) is not None
+
+
+def test_abi_version(lib):
+    assert lib.dtmm_abi_version() == 1
+
+
+def _desc(**kw):
+    d = _lib.TransferDesc()
+    d.height, d.width, d.nlam, d.npol, d.nray = 16, 16, 1, 1, 1
+    d.method, d.diffraction, d.reflection, d.npass, d.precision = 4, 1, 1, 1, 0
+    d.betamax, d.nin, d.nout, d.smooth = 0.8, 1.5, 1.5, 0.1
+    th = np.ones(3)
+    ns = np.ones(3, np.int32)
+    arr = np.zeros(1)
+    d._keep = (th, ns, arr)
+    d.nlayers = 3
+    d.thickness = th.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.nstep = ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    d.ks = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.beta = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.phi = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.epsv = 1
+    d.epsa = 1
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def test_workspace_size_positive_for_valid_desc(lib):
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc())) > 16 * 16 * 4 * 8
+
+
+@pytest.mark.parametrize("field,value,needle", [
+    ("method", 3, "method"),
+    ("diffraction", 0, "diffraction"),
+    ("reflection", 2, "reflection"),
+    ("height", 11, "factor"),
+    ("npass", 0, "npass"),
+])
+def test_invalid_descriptors_are_rejected(lib, field, value, needle):
+    d = _desc(**{field: value})
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) == 0
+    assert needle in _lib.last_error()
+
+
+def test_transfer_rejects_small_workspace(lib):
+    d = _desc()
+    io = _lib.TransferIO()
+    io.field_in = 1
+    io.field_out = 1
+    rc = lib.dtmm_transfer(ctypes.byref(d), ctypes.byref(io), ctypes.c_void_p(1), 16, None)
+    assert rc == _lib.DTMM_ENOSPACE
+    assert "workspace" in _lib.last_error()
