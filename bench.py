@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Throughput of dtmm's transfer_field hot path on GB300.
+
+Workload (the precision configuration of the reference's benchmark set):
+4x4 method, npass = 3 (reflections), diffraction = 3 (9 mode windows),
+256 x 256 grid, 60 layers of 1 pixel, 50 nm pixels, 9 wavelengths
+380-780 nm, x and y polarisations at normal incidence, seeded twisted nematic
+(no 1.52, ne 1.71, 8-mode perturbation of amplitude 0.3 rad), complex64 bulk
+with the FP64 eigen-solve.  One step = one whole transfer_field of that
+workload; the unit is voxel x wavelength updates (H*W*layers*lambdas*
+polarisations*passes = 2.12e8 per step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  `value` times steps with inputs resident in HBM
+(CUDA events, L2 flushed between steps); `e2e` times the drop-in call on
+host numpy buffers (pinned), host<->device copies included.  The reference
+arm (`--impl reference`) times the CPU restatement of the reference's
+algorithm (numba is not installable here, so the reference's own numba path
+cannot run) on the host cores over a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "voxel·λ updates/s vs plain c128 GPU at ≤1e-4 err; served p50/p99 latency"
+UNIT = "voxel·λ updates/s"
+SHAPE = (256, 256)
+NLAYERS = 60
+WAVELENGTHS = np.linspace(380.0, 780.0, 9)
+PIXELSIZE = 50.0
+OPTS = dict(method="4x4", diffraction=3, npass=3, beta=0.0, phi=0.0)
+# bytes that one voxel.lambda update must move at least: one read and one write of
+# the 4-component complex64 field, plus the 48-byte material record amortised
+# over the 9 wavelengths x 2 polarisations that share it
+BYTES_PER_UPDATE = 2 * 4 * 8 + 48.0 / (len(WAVELENGTHS) * 2)
+CONFIG = {
+    "workload": "transfer_field 4x4 npass=3 diffraction=3, 256x256 grid, 60 layers, 9 wavelengths 380-780 nm, "
+                "x+y polarisation, twisted nematic (no 1.52, ne 1.71, amp 0.3), complex64 bulk + FP64 eigen-solve",
+    "grid": "256x256", "layers": 60, "wavelengths": 9, "polarisations": 2, "passes": 3, "windows": 9,
+    "l2": "flushed between timed steps (256 MiB write)",
+}
+
+
+def inputs(nlayers=NLAYERS):
+    from dtmm_gb300 import illumination_data, samples
+
+    fd = illumination_data(SHAPE, WAVELENGTHS, pixelsize=PIXELSIZE)
+    od = [samples.twisted_nematic(SHAPE, nlayers, no=1.52, ne=1.71, amplitude=0.3, seed=1)]
+    return fd, od
+
+
+def updates_of(field, nlayers, npass):
+    return int(np.prod(field.shape[:-3])) * field.shape[-2] * field.shape[-1] * nlayers * npass
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle (CPU restatement of the reference) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample_rate():
+    """updates/s of the CPU restatement on 1 layer x 1 pass of the same grid, wavelengths and polarisations."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import dtmm_oracle
+    from dtmm_gb300 import illumination_data, samples
+
+    cores = len(os.sched_getaffinity(0))
+    dtmm_oracle.set_workers(cores)
+    fd = illumination_data(SHAPE, WAVELENGTHS, pixelsize=PIXELSIZE)
+    od = [samples.twisted_nematic(SHAPE, 1, no=1.52, ne=1.71, amplitude=0.3, seed=1)]
+    kw = dict(OPTS)
+    kw["npass"] = 1
+    t0 = time.perf_counter()
+    dtmm_oracle.transfer_field((fd[0].copy(), fd[1], fd[2]), od, **kw)
+    dt = time.perf_counter() - t0
+    upd = updates_of(fd[0], 1, 1)
+    return upd / dt, cores, dt
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        busy = [v for v in sm if mx and v > 0.3 * max(mx)]
+        return {"sm_mhz": float(np.median(busy or sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the dominant kernel, from the committed ncu summary (None if absent)."""
+    p = os.path.join(ROOT, "profiles", "layer_row_traffic.json")
+    if os.path.exists(p):
+        return json.load(open(p)).get("dram_bytes_per_launch_full")
+    return None
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    rates = []
+    for i in range(args.warmup + args.steps):
+        rate, cores, dt = cpu_sample_rate()
+        if i >= args.warmup:
+            rates.append(rate)
+    value = float(np.median(rates))
+    sample = "1 of 60 layers, 1 of 3 passes, full 256x256 grid, 9 wavelengths, 2 polarisations per step"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": CONFIG,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference's algorithm (numpy/scipy, complex128); the reference's numba "
+                "path needs numba, which is not installed on this image",
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-c128", action="store_true", help="skip the complex128 comparison run")
+    ap.add_argument("--layers", type=int, default=NLAYERS, help="layers (profiling runs use fewer; same kernels)")
+    ap.add_argument("--npass", type=int, default=OPTS["npass"])
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+
+    import dtmm_gb300
+    from dtmm_gb300.transfer import plan_transfer
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    dev = torch.device("cuda", local)
+    fd, od = inputs(args.layers)
+    OPTS["npass"] = args.npass
+    if args.layers != NLAYERS or args.npass != 3:
+        CONFIG["workload"] += " [reduced: %d layers, npass %d]" % (args.layers, args.npass)
+        CONFIG["layers"] = args.layers
+        CONFIG["passes"] = args.npass
+    field_np = fd[0]
+    plan = plan_transfer(field_np.shape, fd[1], fd[2], od, precision="mixed", device=dev, **OPTS)
+    fin0 = torch.from_numpy(field_np).to(dev).to(plan.dtype).contiguous()
+    fin = torch.empty_like(fin0)
+    fout = torch.empty_like(fin0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(timed=False):
+        fin.copy_(fin0)  # the transfer rewrites its input in place (npass > 1)
+        return plan.run(fin, fout, timed=timed)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream(dev)
+    times, ktimes = [], []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            kt = step(timed=True)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            ktimes.append(kt)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier()
+    clocks = clk.summary()
+    total_ms = float(sum(times))
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    upd = plan.updates
+    value = upd * args.steps * world / (total_ms / 1e3)
+    out_mixed = fout.to(torch.complex128).cpu().numpy()
+
+    # dominant kernel: the fused row pass
+    row_ms = sum(k.layer_row_ms for k in ktimes)
+    row_n = sum(k.layer_row_launches for k in ktimes)
+    col_ms = sum(k.layer_col_ms for k in ktimes)
+    op_ms = sum(k.voxel_op_ms for k in ktimes)
+    launches = sum(k.total_launches for k in ktimes)
+    upd_per_row_launch = int(np.prod(field_np.shape[:-3])) * SHAPE[0] * SHAPE[1]
+    row_avg_s = row_ms / row_n / 1e3
+    achieved = BYTES_PER_UPDATE * upd_per_row_launch / row_avg_s / 1e9
+    peak, peak_kind = measured_peaks()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_traffic(), "kernel": "k_layer_row<float>", "peak_source": peak_kind,
+                "kernel_share": row_ms / total_ms,
+                "device_ms_per_step": {"layer_row": row_ms / args.steps, "layer_col": col_ms / args.steps,
+                                       "voxel_op": op_ms / args.steps}}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64", "data": "synthetic", "config": CONFIG, "roofline": roofline, "gpu_launches": launches,
+        "clocks": clocks, "wall_s_timed_region": wall, "updates_per_step": upd,
+    }
+
+    # complex128 drop-in on the same workload (the "plain c128 GPU" comparison)
+    if not args.no_c128 and rank == 0:
+        plan64 = plan_transfer(field_np.shape, fd[1], fd[2], od, precision="double", device=dev, **OPTS)
+        f64 = torch.from_numpy(field_np).to(dev).contiguous()
+        fi64 = torch.empty_like(f64)
+        fo64 = torch.empty_like(f64)
+        fi64.copy_(f64)
+        plan64.run(fi64, fo64)
+        torch.cuda.synchronize()
+        fi64.copy_(f64)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        flush.zero_()
+        e0.record()
+        plan64.run(fi64, fo64)
+        e1.record()
+        e1.synchronize()
+        c128_ms = e0.elapsed_time(e1)
+        ref = fo64.cpu().numpy()
+        result["c128"] = {"value": upd / (c128_ms / 1e3), "ms_per_step": c128_ms,
+                          "mixed_speedup": (upd / (total_ms / args.steps / 1e3)) / (upd / (c128_ms / 1e3)),
+                          "mixed_rel_l2_vs_c128": float(np.linalg.norm(out_mixed - ref) / np.linalg.norm(ref))}
+        del plan64, f64, fi64, fo64
+
+    # end to end through the drop-in call on host buffers
+    if not args.no_e2e:
+        pinned = torch.empty(field_np.shape, dtype=torch.complex128).pin_memory()
+        pinned_np = pinned.numpy()
+        e2e = []
+        for i in range(1 + args.steps):
+            pinned_np[...] = field_np
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = dtmm_gb300.transfer_field((pinned_np, fd[1], fd[2]), od, precision="mixed", **OPTS)
+            torch.cuda.synchronize()
+            if i > 0:
+                e2e.append(time.perf_counter() - t0)
+        e2e_s = float(np.median(e2e))
+        fbytes = field_np.size * 16
+        mat_bytes = od[0][2].nbytes + 24 + od[0][0].nbytes
+        result["e2e"] = {"value": upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": fbytes + mat_bytes,
+                         "d2h_bytes_per_step": 2 * fbytes, "ms_per_step": e2e_s * 1e3}
+
+    if rank == 0 and not args.no_cpu and world == 1:
+        rate, cores, dt = cpu_sample_rate()
+        result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": "1 of 60 layers, 1 of 3 passes, full 256x256 grid, 9 wavelengths, "
+                                            "2 polarisations (%.1f s of CPU work)" % dt}
+    if rank == 0:
+        print(json.dumps(result))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

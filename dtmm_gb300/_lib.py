@@ -19,7 +19,8 @@ DTMM_ENOTSUP = -4
 PRECISION_MIXED = 0
 PRECISION_DOUBLE = 1
 
-ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer")
+ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
+               "dtmm_transfer_timed")
 
 
 class TransferDesc(ctypes.Structure):
@@ -50,6 +51,7 @@ class TransferDesc(ctypes.Structure):
         ("beta", ctypes.POINTER(ctypes.c_double)),
         ("phi", ctypes.POINTER(ctypes.c_double)),
         ("op_cache_bytes", ctypes.c_size_t),
+        ("real_path", ctypes.c_int),
     ]
 
 
@@ -59,6 +61,18 @@ class TransferIO(ctypes.Structure):
         ("field_out", ctypes.c_void_p),
         ("out_given", ctypes.c_int),
         ("bulk", ctypes.c_void_p),
+    ]
+
+
+class KernelTimes(ctypes.Structure):
+    _fields_ = [
+        ("layer_row_ms", ctypes.c_double),
+        ("layer_col_ms", ctypes.c_double),
+        ("voxel_op_ms", ctypes.c_double),
+        ("layer_row_launches", ctypes.c_int),
+        ("layer_col_launches", ctypes.c_int),
+        ("voxel_op_launches", ctypes.c_int),
+        ("total_launches", ctypes.c_int),
     ]
 
 
@@ -93,6 +107,9 @@ def load(build_if_missing=True):
     lib.dtmm_transfer.restype = ctypes.c_int
     lib.dtmm_transfer.argtypes = [ctypes.POINTER(TransferDesc), ctypes.POINTER(TransferIO), ctypes.c_void_p,
                                   ctypes.c_size_t, ctypes.c_void_p]
+    lib.dtmm_transfer_timed.restype = ctypes.c_int
+    lib.dtmm_transfer_timed.argtypes = [ctypes.POINTER(TransferDesc), ctypes.POINTER(TransferIO), ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(KernelTimes)]
     if lib.dtmm_abi_version() != 1:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,6 +46,7 @@ int fail(int code, const char* fmt, ...) {
   } while (0)
 #define CKL(what)                                                                                    \
   do {                                                                                               \
+    ++launches;                                                                                      \
     cudaError_t e_ = cudaGetLastError();                                                             \
     if (e_ != cudaSuccess) return fail(DTMM_ECUDA, "launch %s: %s", what, cudaGetErrorString(e_)); \
   } while (0)
@@ -63,6 +65,9 @@ bool make_plan(int n, FFTPlan& p) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+constexpr int kPartBlocks = 1216;  // blocks of the effective-medium reduction
+constexpr int kWinChunks = 64;     // blocks per window of the window statistics
+
 // Workspace layout (byte offsets), shared by the size query and the call.
 struct Layout {
   int C;        // state components (4 or 2)
@@ -71,7 +76,7 @@ struct Layout {
   bool cache_ops;
   size_t cplx;  // bytes of one complex
   size_t HW;
-  size_t small, twH, permH, twW, permW, cx, cy, kfirst, klast, kdiag, pin, pout;
+  size_t small, part, twH, permH, twW, permW, cx, cy, kfirst, klast, kdiag, pin, pout;
   size_t F, X, U, field0, op;
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -127,6 +132,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 3 * nrw + 4 + 3 * NI + 8));
+  L.part = take(sizeof(double) * std::max<size_t>(2 * kPartBlocks, 4 * kWinChunks * nrw));
   L.twH = take(L.cplx * H);
   L.permH = take(sizeof(int) * H);
   L.twW = take(L.cplx * W);
@@ -163,8 +169,40 @@ double fold(double off, double d) {
   return std::fabs(a) > std::fabs(b) ? b : a;
 }
 
+// optional device-time accounting (dtmm_transfer_timed)
+struct Prof {
+  std::vector<cudaEvent_t> ev[3];  // row, col, op: begin/end pairs
+  int launches = 0;
+  ~Prof() {
+    for (auto& v : ev)
+      for (cudaEvent_t e : v) cudaEventDestroy(e);
+  }
+  void mark(int kind, cudaStream_t st) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, st);
+    ev[kind].push_back(e);
+  }
+  double total(int kind) const {
+    double ms = 0;
+    for (size_t i = 0; i + 1 < ev[kind].size(); i += 2) {
+      float t = 0;
+      cudaEventElapsedTime(&t, ev[kind][i], ev[kind][i + 1]);
+      ms += t;
+    }
+    return ms;
+  }
+};
+enum { PROF_ROW = 0, PROF_COL = 1, PROF_OP = 2 };
+
 template <typename R>
 struct Engine {
+  Prof* prof = nullptr;
+  int launches = 0;
+  double diag_d = std::nan("");  // thickness the inter-layer k-space table was built for
+  void mark(int kind) {
+    if (prof) prof->mark(kind, st);
+  }
   const dtmm_transfer_desc& d;
   const dtmm_transfer_io& io;
   const Layout& L;
@@ -173,6 +211,10 @@ struct Engine {
   Grid g;
   FFTPlan pH, pW;
   int NI;
+
+  Engine(const dtmm_transfer_desc& d_, const dtmm_transfer_io& io_, const Layout& L_, unsigned char* ws_,
+         cudaStream_t st_)
+      : d(d_), io(io_), L(L_), ws(ws_), st(st_) {}
 
   cpx<R>* P(size_t off) const { return (cpx<R>*)(ws + off); }
   template <typename T>
@@ -239,12 +281,40 @@ struct Engine {
     const size_t smem = 2 * (size_t)cm * d.height * p.tc * sizeof(cpx<R>) + d.height * (sizeof(cpx<R>) + sizeof(int));
     CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((d.width + p.tc - 1) / p.tc, NI);
+    mark(PROF_COL);
     k_layer_col<R><<<grid, 256, smem, st>>>(p, g, in, out);
+    mark(PROF_COL);
     CKL("k_layer_col");
     return DTMM_OK;
   }
 
-  int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const cpx<R>* op, double dir) {
+  bool real_ops() const { return d.real_path && !d.eps_complex; }
+
+  // wavelengths per row block: as many as fit ~100 KB of shared memory
+  int row_group() const {
+    const size_t per = 2 * (size_t)d.npol * L.C * d.width * sizeof(cpx<R>);
+    int G = (int)((100 * 1024) / per);
+    if (G < 1) G = 1;
+    if (G > d.nlam) G = d.nlam;
+    return G;
+  }
+
+  template <int C, bool REAL>
+  int launch_row_t(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
+    const size_t smem = 2 * (size_t)p.G * d.npol * C * d.width * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
+    if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels x %d polarisations too large for one block", d.width, d.npol);
+    CK(cudaFuncSetAttribute(k_layer_row<R, C, REAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int threads = d.width < 256 ? ((d.width + 31) / 32) * 32 : 256;
+    const int ngrp = (d.nlam + p.G - 1) / p.G;
+    dim3 grid(d.height, d.nray * ngrp);
+    mark(PROF_ROW);
+    k_layer_row<R, C, REAL><<<grid, threads, smem, st>>>(p, g, Ub, Xb);
+    mark(PROF_ROW);
+    CKL("k_layer_row");
+    return DTMM_OK;
+  }
+
+  int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const void* op, double dir) {
     RowParams p;
     p.C = L.C;
     p.nx = L.nx;
@@ -258,14 +328,10 @@ struct Engine {
     p.plan = pW;
     p.tw = P(L.twW);
     p.perm = A<int>(L.permW);
-    p.identity_op = 0;
-    const size_t smem = (size_t)(2 * d.npol + 1) * L.C * d.width * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
-    CK(cudaFuncSetAttribute(k_layer_row<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int threads = d.width < 256 ? ((d.width + 31) / 32) * 32 : 256;
-    dim3 grid(d.height, d.nray * d.nlam);
-    k_layer_row<R><<<grid, threads, smem, st>>>(p, g, Ub, Xb);
-    CKL("k_layer_row");
-    return DTMM_OK;
+    p.G = row_group();
+    const bool re = real_ops();
+    if (L.C == 4) return re ? launch_row_t<4, true>(p, Ub, Xb) : launch_row_t<4, false>(p, Ub, Xb);
+    return re ? launch_row_t<2, true>(p, Ub, Xb) : launch_row_t<2, false>(p, Ub, Xb);
   }
 
   int launch_ktab(int what, double dd, cpx<R>* tab, int proj_mode = 1, double eps_re = 0, double eps_im = 0,
@@ -297,6 +363,14 @@ struct Engine {
       CKL("k_ktab");
     }
     return DTMM_OK;
+  }
+
+  // (e+, e-) table of the merged half steps; rebuilt only when the thickness changes
+  int diag_table(double dd) {
+    if (dd == diag_d) return DTMM_OK;
+    int rc = launch_ktab(KT_DIAG, dd, P(L.kdiag));
+    if (rc == DTMM_OK) diag_d = dd;
+    return rc;
   }
 
   WinParams winp() const {
@@ -334,7 +408,12 @@ struct Engine {
     p.nwin = L.nwin;
     p.four = d.method == 4;
     dim3 grid((unsigned)((L.HW + 127) / 128), d.nray * L.nwin);
-    k_voxel_op<R><<<grid, 128, 0, st>>>(p, g, op);
+    mark(PROF_OP);
+    if (real_ops())
+      k_voxel_op<R, true><<<grid, 128, 0, st>>>(p, g, op);
+    else
+      k_voxel_op<R, false><<<grid, 128, 0, st>>>(p, g, op);
+    mark(PROF_OP);
     CKL("k_voxel_op");
     return DTMM_OK;
   }
@@ -357,15 +436,26 @@ struct Engine {
     k_fft_tables<R><<<(d.width + 255) / 256, 256, 0, st>>>(pW, P(L.twW), A<int>(L.permW));
     CKL("k_fft_tables");
     // effective medium
-    k_eps_mean<<<1, 1024, 0, st>>>(d.epsv, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
-                                   d.nlayers, d.height, d.width, epseff());
-    CKL("k_eps_mean");
+    {
+      const long long nvox = (long long)d.nlayers * d.height * d.width;
+      int blocks = (int)((nvox + 1023) / 1024);
+      if (blocks > kPartBlocks) blocks = kPartBlocks;
+      k_eps_mean<<<blocks, 256, 0, st>>>(d.epsv, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1],
+                                         d.epsv_strides[2], d.nlayers, d.height, d.width, A<double>(L.part));
+      CKL("k_eps_mean");
+      k_eps_final<<<1, 32, 0, st>>>(A<double>(L.part), blocks, nvox, epseff());
+      CKL("k_eps_final");
+    }
     // windows
     if (d.diffraction > 1) {
       WinParams w = winp();
-      dim3 gs(L.nwin, d.nray);
-      k_window_stats<<<gs, 256, 0, st>>>(w, g, wbeta(), wphi(), wzero());
+      // partial sums over many blocks, then the per-window means
+      dim3 gs(kWinChunks, L.nwin, d.nray);
+      k_window_stats<<<gs, 256, 0, st>>>(w, g, A<double>(L.part));
       CKL("k_window_stats");
+      k_window_final<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(A<double>(L.part), kWinChunks, wbeta(), wphi(),
+                                                                    wzero(), L.nwin * d.nray);
+      CKL("k_window_final");
       dim3 gt(8, d.nlam, d.nray);
       k_window_tables<R><<<gt, 256, 0, st>>>(w, g, A<R>(L.cx), A<R>(L.cy));
       CKL("k_window_tables");
@@ -416,7 +506,7 @@ struct Engine {
         rc = launch_col(F, U, 4, 4, KOP_MAT, P(L.kfirst), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
                         1.0);
       } else {
-        if ((rc = launch_ktab(KT_DIAG, dir * 0.5 * (dprev + ds), P(L.kdiag)))) return rc;
+        if ((rc = diag_table(dir * 0.5 * (dprev + ds)))) return rc;
         rc = launch_col(X, U, 4, 4, KOP_DIAG, P(L.kdiag), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
                         1.0);
       }
@@ -557,7 +647,7 @@ struct Engine {
       if (s == 0) {
         rc = launch_col(F, U, 4, 2, KOP_MAT, P(L.kfirst), L.ny, cy, true, true, 1.0);
       } else {
-        if ((rc = launch_ktab(KT_DIAG, 0.5 * (dprev + ds), P(L.kdiag)))) return rc;
+        if ((rc = diag_table(0.5 * (dprev + ds)))) return rc;
         rc = launch_col(X, U, 2, 2, KOP_DIAG, P(L.kdiag), L.ny, cy, true, true, 1.0);
       }
       if (rc) return rc;
@@ -576,8 +666,10 @@ struct Engine {
 };
 
 template <typename R>
-int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws, const Layout& L, cudaStream_t st) {
-  Engine<R> e{*d, *io, L, (unsigned char*)ws, st};
+int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws, const Layout& L, cudaStream_t st,
+               Prof* prof, int* launches) {
+  Engine<R> e(*d, *io, L, (unsigned char*)ws, st);
+  e.prof = prof;
   e.g.H = d->height;
   e.g.W = d->width;
   e.NI = d->nray * d->npol * d->nlam;
@@ -588,8 +680,24 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   make_plan(d->height, e.pH);
   make_plan(d->width, e.pW);
   int rc = e.setup();
+  if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();
+  if (launches) *launches = e.launches;
+  return rc;
+}
+
+int transfer_impl(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
+                  void* stream, Prof* prof, int* launches) {
+  g_err.clear();
+  int rc = check_desc(desc);
   if (rc) return rc;
-  return d->method == 4 ? e.run4() : e.run2();
+  if (io == nullptr || io->field_in == nullptr || io->field_out == nullptr) return fail(DTMM_EINVAL, "null field buffer");
+  if (io->bulk != nullptr && desc->method != 4) return fail(DTMM_ENOTSUP, "bulk output is implemented for 4x4");
+  Layout L = layout_of(desc);
+  if (workspace == nullptr || workspace_bytes < L.total)
+    return fail(DTMM_ENOSPACE, "workspace of %zu bytes, %zu needed", workspace_bytes, L.total);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (desc->precision == DTMM_PRECISION_DOUBLE) return run_engine<double>(desc, io, workspace, L, st, prof, launches);
+  return run_engine<float>(desc, io, workspace, L, st, prof, launches);
 }
 
 }  // namespace
@@ -607,17 +715,27 @@ size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc) {
 
 int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
                   void* stream) {
-  g_err.clear();
-  int rc = check_desc(desc);
+  return transfer_impl(desc, io, workspace, workspace_bytes, stream, nullptr, nullptr);
+}
+
+int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
+                        size_t workspace_bytes, void* stream, dtmm_kernel_times* times) {
+  Prof prof;
+  int launches = 0;
+  int rc = transfer_impl(desc, io, workspace, workspace_bytes, stream, &prof, &launches);
   if (rc) return rc;
-  if (io == nullptr || io->field_in == nullptr || io->field_out == nullptr) return fail(DTMM_EINVAL, "null field buffer");
-  if (io->bulk != nullptr && desc->method != 4) return fail(DTMM_ENOTSUP, "bulk output is implemented for 4x4");
-  Layout L = layout_of(desc);
-  if (workspace == nullptr || workspace_bytes < L.total)
-    return fail(DTMM_ENOSPACE, "workspace of %zu bytes, %zu needed", workspace_bytes, L.total);
-  cudaStream_t st = (cudaStream_t)stream;
-  if (desc->precision == DTMM_PRECISION_DOUBLE) return run_engine<double>(desc, io, workspace, L, st);
-  return run_engine<float>(desc, io, workspace, L, st);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return fail(DTMM_ECUDA, "cudaStreamSynchronize: %s", cudaGetErrorString(e));
+  if (times) {
+    times->layer_row_ms = prof.total(PROF_ROW);
+    times->layer_col_ms = prof.total(PROF_COL);
+    times->voxel_op_ms = prof.total(PROF_OP);
+    times->layer_row_launches = (int)prof.ev[PROF_ROW].size() / 2;
+    times->layer_col_launches = (int)prof.ev[PROF_COL].size() / 2;
+    times->voxel_op_launches = (int)prof.ev[PROF_OP].size() / 2;
+    times->total_launches = launches;
+  }
+  return DTMM_OK;
 }
 
 }  // extern "C"

@@ -117,13 +117,14 @@ __device__ __forceinline__ cpx<R> twid(const cpx<R>* tw, int idx) {
   return w;
 }
 
-template <typename R, bool INV>
-__device__ __forceinline__ void dft_small(cpx<R>* v, int rad, const cpx<R>* tw, int n) {
-  if (rad == 2) {
+// R-point DFT in registers (R compile-time)
+template <typename R, int RAD, bool INV>
+__device__ __forceinline__ void dft_reg(cpx<R>* v, const cpx<R>* tw, int n) {
+  if constexpr (RAD == 2) {
     cpx<R> a = v[0], b = v[1];
     v[0] = a + b;
     v[1] = a - b;
-  } else if (rad == 4) {
+  } else if constexpr (RAD == 4) {
     cpx<R> s02 = v[0] + v[2], d02 = v[0] - v[2], s13 = v[1] + v[3], d13 = v[1] - v[3];
     // forward: W4 = -i ; inverse: W4 = +i
     cpx<R> jd = INV ? mk<R>(-d13.im, d13.re) : mk<R>(d13.im, -d13.re);
@@ -132,82 +133,129 @@ __device__ __forceinline__ void dft_small(cpx<R>* v, int rad, const cpx<R>* tw, 
     v[1] = d02 + jd;
     v[3] = d02 - jd;
   } else {
-    cpx<R> in[7];
-    for (int i = 0; i < rad; ++i) in[i] = v[i];
-    const int step = n / rad;
-    for (int q = 0; q < rad; ++q) {
+    cpx<R> in[RAD];
+#pragma unroll
+    for (int i = 0; i < RAD; ++i) in[i] = v[i];
+    const int step = n / RAD;
+#pragma unroll
+    for (int q = 0; q < RAD; ++q) {
       cpx<R> acc = in[0];
-      for (int i = 1; i < rad; ++i) acc = cfma(in[i], twid<R, INV>(tw, ((q * i) % rad) * step), acc);
+#pragma unroll
+      for (int i = 1; i < RAD; ++i) acc = cfma(in[i], twid<R, INV>(tw, ((q * i) % RAD) * step), acc);
       v[q] = acc;
     }
   }
 }
 
-// decimation in time: digit-reversed in, natural out
+// one butterfly of one pass; `ns` = length of the sub-transforms combined so far
+template <typename R, int RAD, bool INV, bool DIT>
+__device__ __forceinline__ void butterfly(cpx<R>* line, int es, int b, int ns, int nsh, int tstep, const cpx<R>* tw,
+                                          int n) {
+  int k, g;
+  if (nsh >= 0) {
+    k = b & (ns - 1);
+    g = b >> nsh;
+  } else {
+    g = b / ns;
+    k = b - g * ns;
+  }
+  cpx<R>* ptr = line + (g * ns * RAD + k) * es;
+  const int stride = ns * es;
+  cpx<R> v[RAD];
+  if (DIT) {
+    v[0] = ptr[0];
+#pragma unroll
+    for (int r = 1; r < RAD; ++r) v[r] = ptr[r * stride] * twid<R, INV>(tw, k * r * tstep);
+    dft_reg<R, RAD, INV>(v, tw, n);
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) ptr[r * stride] = v[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) v[r] = ptr[r * stride];
+    dft_reg<R, RAD, INV>(v, tw, n);
+    ptr[0] = v[0];
+#pragma unroll
+    for (int r = 1; r < RAD; ++r) ptr[r * stride] = v[r] * twid<R, INV>(tw, k * r * tstep);
+  }
+}
+
+__device__ __forceinline__ int log2_or_neg(int x) { return (x & (x - 1)) == 0 ? __ffs(x) - 1 : -1; }
+
+// One pass over `nlines` lines by a group of `nthr` threads (thread index `tid`).
+// line_fastest: consecutive threads take consecutive lines.
+template <typename R, bool INV, bool DIT>
+__device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, bool line_fastest, const cpx<R>* tw,
+                                         int n, int rad, int ns, int tid, int nthr) {
+  const int nb = n / rad;
+  const int total = nb * nlines;
+  const int tstep = n / (ns * rad);
+  const int nsh = log2_or_neg(ns);
+  for (int t = tid; t < total; t += nthr) {
+    int line, b;
+    if (line_fastest) {
+      line = t % nlines;
+      b = t / nlines;
+    } else {
+      b = t % nb;
+      line = t / nb;
+    }
+    cpx<R>* ln = s + line * ls;
+    switch (rad) {
+      case 4: butterfly<R, 4, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      case 2: butterfly<R, 2, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+    }
+  }
+}
+
+// decimation in time over the whole block: digit-reversed in, natural out
 template <typename R, bool INV>
 __device__ void fft_dit(cpx<R>* s, int es, int ls, int nlines, bool line_fastest, const cpx<R>* tw,
                         const FFTPlan& p) {
-  const int n = p.n;
   int ns = 1;
   for (int ip = 0; ip < p.nr; ++ip) {
-    const int rad = p.r[ip];
-    const int nb = n / rad;
-    const int total = nb * nlines;
-    const int tstep = n / (ns * rad);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      int line, b;
-      if (line_fastest) {
-        line = t % nlines;
-        b = t / nlines;
-      } else {
-        b = t % nb;
-        line = t / nb;
-      }
-      const int k = b % ns;
-      const int base = (b / ns) * ns * rad + k;
-      cpx<R>* ptr = s + line * ls + base * es;
-      cpx<R> v[7];
-      v[0] = ptr[0];
-      for (int r = 1; r < rad; ++r) v[r] = ptr[r * ns * es] * twid<R, INV>(tw, k * r * tstep);
-      dft_small<R, INV>(v, rad, tw, n);
-      for (int r = 0; r < rad; ++r) ptr[r * ns * es] = v[r];
-    }
-    ns *= rad;
+    fft_pass<R, INV, true>(s, es, ls, nlines, line_fastest, tw, p.n, p.r[ip], ns, threadIdx.x, blockDim.x);
+    ns *= p.r[ip];
     __syncthreads();
   }
 }
 
-// transposed network: natural in, digit-reversed out
+// transposed network over the whole block: natural in, digit-reversed out
 template <typename R, bool INV>
 __device__ void fft_dif(cpx<R>* s, int es, int ls, int nlines, bool line_fastest, const cpx<R>* tw,
                         const FFTPlan& p) {
-  const int n = p.n;
-  int ns = n;
+  int ns = p.n;
   for (int ip = p.nr - 1; ip >= 0; --ip) {
-    const int rad = p.r[ip];
-    ns /= rad;
-    const int nb = n / rad;
-    const int total = nb * nlines;
-    const int tstep = n / (ns * rad);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      int line, b;
-      if (line_fastest) {
-        line = t % nlines;
-        b = t / nlines;
-      } else {
-        b = t % nb;
-        line = t / nb;
-      }
-      const int k = b % ns;
-      const int base = (b / ns) * ns * rad + k;
-      cpx<R>* ptr = s + line * ls + base * es;
-      cpx<R> v[7];
-      for (int r = 0; r < rad; ++r) v[r] = ptr[r * ns * es];
-      dft_small<R, INV>(v, rad, tw, n);
-      ptr[0] = v[0];
-      for (int r = 1; r < rad; ++r) ptr[r * ns * es] = v[r] * twid<R, INV>(tw, k * r * tstep);
-    }
+    ns /= p.r[ip];
+    fft_pass<R, INV, false>(s, es, ls, nlines, line_fastest, tw, p.n, p.r[ip], ns, threadIdx.x, blockDim.x);
     __syncthreads();
+  }
+}
+
+// the same, one warp per line: warp w transforms lines w, w + nwarps, ...
+// (only warp-level synchronisation between passes)
+template <typename R, bool INV, bool DIT>
+__device__ void fft_lines_warp(cpx<R>* s, int ls, int nlines, const cpx<R>* tw, const FFTPlan& p) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int l = warp; l < nlines; l += nwarps) {
+    cpx<R>* ln = s + l * ls;
+    if (DIT) {
+      int ns = 1;
+      for (int ip = 0; ip < p.nr; ++ip) {
+        fft_pass<R, INV, true>(ln, 1, 0, 1, false, tw, p.n, p.r[ip], ns, lane, 32);
+        ns *= p.r[ip];
+        __syncwarp();
+      }
+    } else {
+      int ns = p.n;
+      for (int ip = p.nr - 1; ip >= 0; --ip) {
+        ns /= p.r[ip];
+        fft_pass<R, INV, false>(ln, 1, 0, 1, false, tw, p.n, p.r[ip], ns, lane, 32);
+        __syncwarp();
+      }
+    }
   }
 }
 

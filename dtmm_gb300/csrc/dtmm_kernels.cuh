@@ -12,6 +12,8 @@
 //   k-space tables       : [lam][H][W][rows][cols]
 #pragma once
 
+#include <type_traits>
+
 #include "dtmm_common.cuh"
 
 namespace dtmm {
@@ -146,8 +148,68 @@ struct OpParams {
   int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
 };
 
-template <typename R>
-__global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
+// Records per voxel and window, [ray][window][record][H][W]: complex, or real
+// when the host has proven the real path (real eps above beta^2 everywhere).
+
+// Uniaxial / isotropic E rows and eigenvalues in real FP64 arithmetic, valid
+// when every eigenvalue and the effective medium exceed beta^2 (then every
+// radicand of the solve is positive; the host proves this before selecting
+// the real path).  Same formulas as the complex path below.
+__device__ inline bool voxel_E_real(double beta, double phi, const double ev[3], double theta, double azim,
+                                    double E[2][4], double al[4]) {
+  if (ev[0] == ev[1] && ev[1] == ev[2]) {
+    const double a = sqrt(ev[0] - beta * beta);
+    al[0] = a; al[1] = -a; al[2] = a; al[3] = -a;
+    E[0][0] = 0.5; E[1][0] = 0.0;
+    E[0][1] = 0.5; E[1][1] = 0.0;
+    E[0][2] = 0.0; E[1][2] = 0.5;
+    E[0][3] = 0.0; E[1][3] = 0.5;
+    return a == 0.0;
+  }
+  double st, ct, sf, cf;
+  sincos(theta, &st, &ct);
+  sincos(azim - phi, &sf, &cf);
+  const double cfst = cf * st, sfst = st * sf;
+  const double eps11 = ev[0], delta = ev[2] - eps11;
+  double ev02, evs, evpp, evpm;
+  if (beta == 0.0) {
+    ev02 = eps11;
+    evs = sqrt(ev02);
+    const double u = eps11 + delta * (ct * ct);
+    const double w = eps11 * (ev02 + delta);
+    const double sq = sqrt(u * w) / u;
+    evpp = sq;
+    evpm = -sq;
+    E[0][0] = cf;        E[1][0] = sf;
+    E[0][1] = cf;        E[1][1] = sf;
+    E[0][2] = -evs * sf; E[1][2] = evs * cf;
+    E[0][3] = -evs * sf; E[1][3] = evs * cf;
+  } else {
+    ev02 = eps11 - beta * beta;
+    evs = sqrt(ev02);
+    const double u = eps11 + delta * (ct * ct);
+    const double gama = beta * cf;
+    const double v = delta * (gama * 2.0 * st * ct);
+    const double w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
+    const double u2 = u * 2.0;
+    const double sq = sqrt(v * v - u * w * 4.0) / u2;
+    const double vh = v / u2;
+    evpp = sq - vh;
+    evpm = -vh - sq;
+    const double ctbeta = ct * beta;
+    const double ie = 1.0 / eps11;
+    const double ev02cf = ev02 * cfst;
+    E[0][0] = (evpp * ctbeta - ev02cf) * ie;  E[1][0] = -sfst;
+    E[0][1] = (ev02cf - evpm * ctbeta) * ie;  E[1][1] = sfst;
+    E[0][2] = evs * sfst;                     E[1][2] = ctbeta - evs * cfst;
+    E[0][3] = -evs * sfst;                    E[1][3] = evs * cfst + ctbeta;
+  }
+  al[0] = evpp; al[1] = evpm; al[2] = evs; al[3] = -evs;
+  return false;
+}
+
+template <typename R, bool REAL>
+__global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int HW = g.H * g.W;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
   const int rw = blockIdx.y;  // ray * nwin + window
@@ -156,6 +218,42 @@ __global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
   const double beta = p.wbeta[rw], phi = p.wphi[rw];
   const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
   const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
+  const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
+  if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
+  const int nrec = p.four ? OP_REC : 7;
+  double sp, cp;
+  sincos(phi, &sp, &cp);
+  if (REAL) {
+    const double* e = (const double*)p.epsv + eo;
+    const double ev[3] = {e[0], e[1], e[2]};
+    const double aw = sqrt(p.eps_eff.re - beta * beta);
+    double E[2][4], al[4];
+    bool zero = voxel_E_real(beta, phi, ev, theta, azim, E, al);
+    for (int m = 0; m < 4; ++m) {
+      const double ex = E[0][m], ey = E[1][m];
+      E[0][m] = ex * cp - ey * sp;
+      E[1][m] = ex * sp + ey * cp;
+    }
+    const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
+    const double detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
+    if (detf == 0.0 || (p.four && detb == 0.0)) zero = true;
+    double rec[OP_REC];
+    if (zero) {
+      for (int i = 0; i < OP_REC; ++i) rec[i] = 0.0;
+    } else {
+      rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
+      rec[4] = 1.0 / detf;
+      rec[5] = (al[0] - aw) * p.d;
+      rec[6] = (al[2] - aw) * p.d;
+      rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
+      rec[11] = p.four ? 1.0 / detb : 0.0;
+      rec[12] = (al[1] + aw) * p.d;
+      rec[13] = (al[3] + aw) * p.d;
+    }
+    R* o = (R*)opv + (size_t)rw * OP_REC * HW + pix;
+    for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
+    return;
+  }
   cpx<double> ev[3];
   if (p.eps_complex) {
     const cpx<double>* e = (const cpx<double>*)p.epsv + eo;
@@ -168,8 +266,6 @@ __global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
     ev[1] = mk<double>(e[1], 0.0);
     ev[2] = mk<double>(e[2], 0.0);
   }
-  const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
-  if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
   cpx<double> aw = csqrt_d(mk<double>(p.eps_eff.re - beta * beta, p.eps_eff.im));
 
   cpx<double> E[2][4];  // rows Ex, Ey of the four mode columns
@@ -236,8 +332,6 @@ __global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
     al[3] = -evs;
   }
   // rotate the E rows back by the beam azimuth phi
-  double sp, cp;
-  sincos(phi, &sp, &cp);
   for (int m = 0; m < 4; ++m) {
     cpx<double> ex = E[0][m], ey = E[1][m];
     E[0][m] = ex * cp - ey * sp;
@@ -266,8 +360,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, cpx<R>* __restrict__ op) {
       for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
     }
   }
-  cpx<R>* o = op + (size_t)rw * OP_REC * HW + pix;
-  const int nrec = p.four ? OP_REC : 7;
+  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + pix;
   for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
 }
 
@@ -304,18 +397,20 @@ __device__ __forceinline__ double win_center(const WinParams& w, int i) {
   return -w.betamax + i * step;
 }
 
-// one block per (ray, window): sums of w^2 bx, w^2 by, w^2 over (lam, ky, kx)
-__global__ void k_window_stats(WinParams w, Grid g, double* wbeta, double* wphi, int* wzero) {
-  const int ray = blockIdx.y, win = blockIdx.x;
+// partial sums of w^2 bx, w^2 by, w^2 and the non-zero flag over (lam, ky, kx):
+// grid (chunks, window, ray); part[((ray * nwin + win) * chunks + chunk) * 4 + q].
+// The final means add the chunks in a fixed order, so results are bitwise
+// reproducible.
+__global__ void k_window_stats(WinParams w, Grid g, double* part) {
+  const int ray = blockIdx.z, win = blockIdx.y;
   const int i = win / w.n, j = win % w.n;
   const int xt = (i == 0) ? -1 : ((i == w.n - 1) ? 1 : 0);
   const int yt = (j == 0) ? -1 : ((j == w.n - 1) ? 1 : 0);
   const double cx0 = win_center(w, i) + w.xoff[ray];
   const double cy0 = win_center(w, j) + w.yoff[ray];
-  double sx = 0, sy = 0, sn = 0;
-  int nz = 0;
+  double sx = 0, sy = 0, sn = 0, nz = 0;
   const int total = g.nlam * g.H * g.W;
-  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int lam = t / (g.H * g.W);
     const int k = t - lam * g.H * g.W;
     const int ky = k / g.W, kx = k - ky * g.W;
@@ -333,31 +428,35 @@ __global__ void k_window_stats(WinParams w, Grid g, double* wbeta, double* wphi,
       sn += c2;
     }
   }
-  __shared__ double red[3][256];
-  __shared__ int rz[256];
+  __shared__ double red[4][256];
   red[0][threadIdx.x] = sx;
   red[1][threadIdx.x] = sy;
   red[2][threadIdx.x] = sn;
-  rz[threadIdx.x] = nz;
+  red[3][threadIdx.x] = nz;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
-      rz[threadIdx.x] |= rz[threadIdx.x + s];
-    }
+    if (threadIdx.x < s)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    double mx = red[0][0], my = red[1][0], mn = red[2][0];
-    if (mn > 0) {
-      mx /= mn;
-      my /= mn;
-    }
-    const int idx = ray * w.n * w.n + win;
-    wbeta[idx] = sqrt(mx * mx + my * my);
-    wphi[idx] = atan2(my, mx);
-    wzero[idx] = rz[0] ? 0 : 1;
+  if (threadIdx.x < 4)
+    part[(((size_t)ray * w.n * w.n + win) * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_window_final(const double* part, int chunks, double* wbeta, double* wphi, int* wzero, int n) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  double acc[4] = {0, 0, 0, 0};
+  for (int c = 0; c < chunks; ++c)
+    for (int q = 0; q < 4; ++q) acc[q] += part[((size_t)idx * chunks + c) * 4 + q];
+  double mx = acc[0], my = acc[1], mn = acc[2];
+  if (mn > 0) {
+    mx /= mn;
+    my /= mn;
   }
+  wbeta[idx] = sqrt(mx * mx + my * my);
+  wphi[idx] = atan2(my, mx);
+  wzero[idx] = acc[3] > 0 ? 0 : 1;
 }
 
 // cx[ray][i][lam][kx] and cy[ray][j][lam][ky]; the beta >= betamax cut is
@@ -738,101 +837,151 @@ struct RowParams {
   FFTPlan plan;
   const void* tw;
   const int* perm;
-  int identity_op;       // 1: unit operator (no material), used by tests
+  int G;                 // wavelengths per block
 };
 
 template <typename R>
 __device__ __forceinline__ cpx<R> phase_of(cpx<R> arg, R k) {
   return cexp_i(mk<R>(arg.re * k, arg.im * k));
 }
-
 template <typename R>
+__device__ __forceinline__ cpx<R> phase_of(R arg, R k) {
+  R s, c;
+  if constexpr (sizeof(R) == 4)
+    sincosf(arg * k, &s, &c);
+  else
+    sincos(arg * k, &s, &c);
+  return mk<R>(c, s);
+}
+
+// one 2x2 block of the per-voxel operator: out += E . diag(P') . adj(E) . h
+template <typename R, typename T>
+__device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
+                                            cpx<R>& a1) {
+  const cpx<R> w0 = (e[3] * h0 - e[1] * h1) * p0;
+  const cpx<R> w1 = (e[0] * h1 - e[2] * h0) * p1;
+  a0 = a0 + e[0] * w0 + e[1] * w1;
+  a1 = a1 + e[2] * w0 + e[3] * w1;
+}
+
+// Row pass, one row y of a group of G wavelengths (all polarisations) of one
+// ray.  Lines (image, component) are transformed one warp per line; the
+// per-voxel operator records are read once per block and window and the
+// phases once per wavelength.  REAL: records are real (see k_voxel_op).
+template <typename R, int C, bool REAL>
 __global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cpx<R>* __restrict__ U,
                                                    cpx<R>* __restrict__ X) {
+  using T = typename std::conditional<REAL, R, cpx<R>>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int W = g.W, H = g.H, C = p.C, NP = g.npol;
-  cpx<R>* ub = (cpx<R>*)smem_raw;           // [NP][C][W]   U_j rows (natural order)
-  cpx<R>* acc = ub + (size_t)NP * C * W;    // [NP][C][W]   accumulator (digit-reversed)
-  cpx<R>* tmp = acc + (size_t)NP * C * W;   // [C][W]       window work buffer
-  cpx<R>* tw = tmp + (size_t)C * W;         // [W]
-  int* perm = (int*)(tw + W);               // [W]
+  const int W = g.W, H = g.H, NP = g.npol;
+  const int ngrp = (g.nlam + p.G - 1) / p.G;
   const int y = blockIdx.x;
-  const int grp = blockIdx.y;               // ray * nlam + lam
-  const int ray = grp / g.nlam, lam = grp - ray * g.nlam;
+  const int ray = blockIdx.y / ngrp, grp = blockIdx.y - ray * ngrp;
+  const int lam0 = grp * p.G;
+  const int G = min(p.G, g.nlam - lam0);
+  const int nimg = G * NP, nlines = nimg * C;
+  cpx<R>* acc = (cpx<R>*)smem_raw;             // [nlines][W] (digit-reversed)
+  cpx<R>* tmp = acc + (size_t)p.G * NP * C * W; // [nlines][W]
+  cpx<R>* tw = tmp + (size_t)p.G * NP * C * W;  // [W]
+  int* perm = (int*)(tw + W);                   // [W]
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int t = threadIdx.x; t < W; t += blockDim.x) {
     tw[t] = ((const cpx<R>*)p.tw)[t];
     perm[t] = p.perm[t];
   }
-  for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) acc[t] = mk<R>(0, 0);
-  const R kphase = (R)(p.ks[lam] * p.dir);
+  for (int t = threadIdx.x; t < nlines * W; t += blockDim.x) acc[t] = mk<R>(0, 0);
   const R sc = (R)p.in_scale;
   __syncthreads();
+  // line l <-> (image = (g, pol), component c): l = (g * NP + pol) * C + c
   for (int j = 0; j < p.ny; ++j) {
     const cpx<R>* Uj = U + (size_t)j * g.NI * C * HW;
-    for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) {
-      const int pol = t / (C * W), r = t - pol * C * W;
-      const int c = r / W, x = r - c * W;
-      const int img = (ray * NP + pol) * g.nlam + lam;
-      ub[t] = Uj[(((size_t)img * C + c) * H + y) * W + x];
-    }
-    __syncthreads();
     for (int i = 0; i < p.nx; ++i) {
       const int w = i * p.ny + j;
       if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
-      const R* cxi = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
-      const cpx<R>* opw = (const cpx<R>*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
-      for (int pol = 0; pol < NP; ++pol) {
-        for (int t = threadIdx.x; t < C * W; t += blockDim.x) {
-          const int x = t % W;
-          cpx<R> v = ub[(size_t)pol * C * W + t];
-          tmp[t] = cxi ? v * cxi[x] : v;
+      // window-weighted rows, inverse transform (one warp per line)
+      for (int l = warp; l < nlines; l += nwarps) {
+        const int c = l % C, im = l / C;
+        const int gl = im / NP, pol = im - gl * NP;
+        const int lam = lam0 + gl;
+        const int img = (ray * NP + pol) * g.nlam + lam;
+        const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
+        const R* cxi = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+        cpx<R>* dst = tmp + (size_t)l * W;
+        for (int x = lane; x < W; x += 32) {
+          cpx<R> v = src[x];
+          dst[x] = cxi ? v * cxi[x] : v;
         }
-        __syncthreads();
-        fft_dif<R, true>(tmp, 1, W, C, false, tw, p.plan);
-        for (int x = threadIdx.x; x < W; x += blockDim.x) {
-          const int q = perm[x];
-          cpx<R>* a = acc + (size_t)pol * C * W;
-          if (p.identity_op) {
-            for (int c = 0; c < C; ++c) a[c * W + q] = a[c * W + q] + tmp[c * W + q] * sc;
-            continue;
-          }
-          // forward block acts on components (0, 2) of Epn, or (0, 1) of E
-          const int c0 = 0, c1 = (C == 4) ? 2 : 1;
-          {
-            const cpx<R> e00 = opw[0 * HW + x], e01 = opw[1 * HW + x], e10 = opw[2 * HW + x], e11 = opw[3 * HW + x];
-            const cpx<R> idet = opw[4 * HW + x];
-            const cpx<R> p0 = phase_of(opw[5 * HW + x], kphase) * idet;
-            const cpx<R> p1 = phase_of(opw[6 * HW + x], kphase) * idet;
-            const cpx<R> h0 = tmp[c0 * W + q] * sc, h1 = tmp[c1 * W + q] * sc;
-            const cpx<R> w0 = (e11 * h0 - e01 * h1) * p0;
-            const cpx<R> w1 = (e00 * h1 - e10 * h0) * p1;
-            a[c0 * W + q] = a[c0 * W + q] + e00 * w0 + e01 * w1;
-            a[c1 * W + q] = a[c1 * W + q] + e10 * w0 + e11 * w1;
-          }
-          if (C == 4) {
-            const cpx<R> e00 = opw[7 * HW + x], e01 = opw[8 * HW + x], e10 = opw[9 * HW + x], e11 = opw[10 * HW + x];
-            const cpx<R> idet = opw[11 * HW + x];
-            const cpx<R> p0 = phase_of(opw[12 * HW + x], kphase) * idet;
-            const cpx<R> p1 = phase_of(opw[13 * HW + x], kphase) * idet;
-            const cpx<R> h0 = tmp[1 * W + q] * sc, h1 = tmp[3 * W + q] * sc;
-            const cpx<R> w0 = (e11 * h0 - e01 * h1) * p0;
-            const cpx<R> w1 = (e00 * h1 - e10 * h0) * p1;
-            a[1 * W + q] = a[1 * W + q] + e00 * w0 + e01 * w1;
-            a[3 * W + q] = a[3 * W + q] + e10 * w0 + e11 * w1;
-          }
+        __syncwarp();
+        int ns = p.plan.n;
+        for (int ip = p.plan.nr - 1; ip >= 0; --ip) {
+          ns /= p.plan.r[ip];
+          fft_pass<R, true, false>(dst, 1, 0, 1, false, tw, p.plan.n, p.plan.r[ip], ns, lane, 32);
+          __syncwarp();
         }
-        __syncthreads();
       }
+      __syncthreads();
+      // per-voxel operator of window w
+      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      for (int x = threadIdx.x; x < W; x += blockDim.x) {
+        const int q = perm[x];
+        T ef[4], arg_f[2], idf;
+        T eb[4], arg_b[2], idb;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
+        idf = opw[(size_t)4 * HW + x];
+        arg_f[0] = opw[(size_t)5 * HW + x];
+        arg_f[1] = opw[(size_t)6 * HW + x];
+        if (C == 4) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
+          idb = opw[(size_t)11 * HW + x];
+          arg_b[0] = opw[(size_t)12 * HW + x];
+          arg_b[1] = opw[(size_t)13 * HW + x];
+        }
+        for (int gl = 0; gl < G; ++gl) {
+          const R kph = (R)(p.ks[lam0 + gl] * p.dir);
+          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
+          cpx<R> pb0, pb1;
+          if (C == 4) {
+            pb0 = phase_of(arg_b[0], kph) * idb;
+            pb1 = phase_of(arg_b[1], kph) * idb;
+          }
+          for (int pol = 0; pol < NP; ++pol) {
+            const int l0 = (gl * NP + pol) * C;
+            const cpx<R>* h = tmp + (size_t)l0 * W + q;
+            cpx<R>* a = acc + (size_t)l0 * W + q;
+            if (C == 4) {
+              cpx<R> a0 = a[0], a1 = a[W], a2 = a[2 * W], a3 = a[3 * W];
+              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[2 * W] * sc, a0, a2);
+              apply_block<R, T>(eb, pb0, pb1, h[W] * sc, h[3 * W] * sc, a1, a3);
+              a[0] = a0; a[W] = a1; a[2 * W] = a2; a[3 * W] = a3;
+            } else {
+              cpx<R> a0 = a[0], a1 = a[W];
+              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[W] * sc, a0, a1);
+              a[0] = a0; a[W] = a1;
+            }
+          }
+        }
+      }
+      __syncthreads();
     }
   }
-  fft_dit<R, false>(acc, 1, W, NP * C, false, tw, p.plan);
-  for (int t = threadIdx.x; t < NP * C * W; t += blockDim.x) {
-    const int pol = t / (C * W), r = t - pol * C * W;
-    const int c = r / W, x = r - c * W;
-    const int img = (ray * NP + pol) * g.nlam + lam;
-    X[(((size_t)img * C + c) * H + y) * W + x] = acc[t];
+  // forward row transform of the accumulator (digit-reversed in, natural out) and store
+  for (int l = warp; l < nlines; l += nwarps) {
+    cpx<R>* ln = acc + (size_t)l * W;
+    int ns = 1;
+    for (int ip = 0; ip < p.plan.nr; ++ip) {
+      fft_pass<R, false, true>(ln, 1, 0, 1, false, tw, p.plan.n, p.plan.r[ip], ns, lane, 32);
+      ns *= p.plan.r[ip];
+      __syncwarp();
+    }
+    const int c = l % C, im = l / C;
+    const int gl = im / NP, pol = im - gl * NP;
+    const int img = (ray * NP + pol) * g.nlam + lam0 + gl;
+    cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
+    for (int x = lane; x < W; x += 32) dst[x] = ln[x];
   }
 }
 
@@ -1002,10 +1151,10 @@ __global__ void k_fft_tables(FFTPlan plan, cpx<R>* tw, int* perm) {
 // isotropic effective medium: mean over every voxel of (e0 + e1 + e2) / 3
 // (effective_block with symmetry 0, dtmm/data.py:1364-1392), FP64
 __global__ void k_eps_mean(const void* epsv, int eps_complex, long long s0, long long s1, long long s2, int L, int H,
-                           int W, double* out) {
+                           int W, double* part) {
   const long long n = (long long)L * H * W;
   double sr = 0.0, si = 0.0;
-  for (long long t = threadIdx.x; t < n; t += blockDim.x) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int l = (int)(t / ((long long)H * W));
     const long long r = t - (long long)l * H * W;
     const int y = (int)(r / W), x = (int)(r - (long long)y * W);
@@ -1019,7 +1168,7 @@ __global__ void k_eps_mean(const void* epsv, int eps_complex, long long s0, long
       sr += (e[0] + e[1] + e[2]) / 3.0;
     }
   }
-  __shared__ double red[2][1024];
+  __shared__ double red[2][256];
   red[0][threadIdx.x] = sr;
   red[1][threadIdx.x] = si;
   __syncthreads();
@@ -1031,9 +1180,21 @@ __global__ void k_eps_mean(const void* epsv, int eps_complex, long long s0, long
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    out[0] = red[0][0] / (double)n;
-    out[1] = red[1][0] / (double)n;
+    part[blockIdx.x * 2 + 0] = red[0][0];
+    part[blockIdx.x * 2 + 1] = red[1][0];
   }
+}
+
+// fixed-order sum of the block partials -> mean (re, im)
+__global__ void k_eps_final(const double* part, int blocks, long long n, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double sr = 0, si = 0;
+  for (int b = 0; b < blocks; ++b) {
+    sr += part[2 * b];
+    si += part[2 * b + 1];
+  }
+  out[0] = sr / (double)n;
+  out[1] = si / (double)n;
 }
 
 }  // namespace dtmm

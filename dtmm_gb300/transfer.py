@@ -183,73 +183,127 @@ class _Material:
         if not np.all(flat[:, 0] == flat[:, 1]):
             raise NotImplementedError(
                 "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
+        self.eps_min = float(np.min(ev)) if not self.eps_complex else None
         self.epsv = torch.from_numpy(np.ascontiguousarray(ev)).to(device)
         self.epsa = torch.from_numpy(np.ascontiguousarray(ea.astype(np.float64))).to(device)
         self.thickness = np.asarray(d, np.float64)
         self.nlayers = L
 
 
-def _engine_call(field_dev, out_dev, bulk_dev, out_given, mat, ks, beta, phi, nray, npol, nlam, method,
-                 diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, stream=None):
-    import torch
+class DevicePlan:
+    """One resolved transfer bound to the device: descriptor, material and
+    workspace, reusable for many input fields of the same shape.
 
-    lib = _lib.load()
-    h, w = field_dev.shape[-2:]
-    L = mat.nlayers
-    thick = np.ascontiguousarray(mat.thickness, np.float64)
-    nst = np.ascontiguousarray(np.broadcast_to(np.asarray(nstep, np.int32), (L,)), np.int32)
-    ksa = np.ascontiguousarray(ks, np.float64)
-    ba = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float64).reshape(-1), (nray,)), np.float64)
-    pa = np.ascontiguousarray(np.broadcast_to(np.asarray(phi, np.float64).reshape(-1), (nray,)), np.float64)
-    d = _lib.TransferDesc()
-    d.height, d.width = int(h), int(w)
-    d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
-    d.method = 4 if method == "4x4" else 2
-    d.diffraction = int(diffraction)
-    d.reflection = int(reflection)
-    d.npass = int(npass)
-    d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
-    d.betamax, d.nin, d.nout, d.smooth = float(betamax), float(nin), float(nout), float(smooth)
-    d.nlayers = L
-    d.thickness = thick.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    d.nstep = nst.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-    d.epsv = mat.epsv.data_ptr()
-    d.eps_complex = int(mat.eps_complex)
-    d.epsv_strides[:] = mat.ev_strides
-    d.epsa = mat.epsa.data_ptr()
-    d.epsa_strides[:] = mat.ea_strides
-    d.ks = ksa.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    d.beta = ba.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    d.phi = pa.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    d.op_cache_bytes = 0
-    nbytes = lib.dtmm_transfer_workspace_size(ctypes.byref(d))
-    if nbytes == 0:
-        _lib.check(_lib.DTMM_EINVAL if "not supported" not in _lib.last_error() and "factor" not in _lib.last_error()
-                   else _lib.DTMM_ENOTSUP)
-    ws = torch.empty(int(nbytes), dtype=torch.uint8, device=field_dev.device)
-    io = _lib.TransferIO()
-    io.field_in = field_dev.data_ptr()
-    io.field_out = out_dev.data_ptr()
-    io.out_given = int(out_given)
-    io.bulk = bulk_dev.data_ptr() if bulk_dev is not None else None
-    if stream is None:
-        stream = torch.cuda.current_stream(field_dev.device).cuda_stream
-    _lib.check(lib.dtmm_transfer(ctypes.byref(d), ctypes.byref(io), ctypes.c_void_p(ws.data_ptr()),
-                                 ctypes.c_size_t(int(nbytes)), ctypes.c_void_p(stream)))
-    return ws
+    ``run(field_in, field_out)`` takes device tensors of shape
+    ``(images..., 4, H, W)`` in the plan's complex dtype and enqueues the
+    transfer on the current stream (nothing is copied to or from the host).
+    """
+
+    def __init__(self, field_shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
+                 nstep, betamax, nin, nout, smooth, precision, device):
+        import torch
+
+        self.lib = _lib.load()
+        self.device = device
+        self.precision = precision
+        self.dtype = torch.complex128 if precision == "double" else torch.complex64
+        self.field_shape = tuple(field_shape)
+        self.mat = mat
+        h, w = field_shape[-2:]
+        L = mat.nlayers
+        self._keep = dict(
+            thick=np.ascontiguousarray(mat.thickness, np.float64),
+            nst=np.ascontiguousarray(np.broadcast_to(np.asarray(nstep, np.int32), (L,)), np.int32),
+            ks=np.ascontiguousarray(ks, np.float64),
+            beta=np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float64).reshape(-1), (nray,)), np.float64),
+            phi=np.ascontiguousarray(np.broadcast_to(np.asarray(phi, np.float64).reshape(-1), (nray,)), np.float64),
+        )
+        k = self._keep
+        d = _lib.TransferDesc()
+        d.height, d.width = int(h), int(w)
+        d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
+        d.method = 4 if method == "4x4" else 2
+        d.diffraction = int(diffraction)
+        d.reflection = int(reflection)
+        d.npass = int(npass)
+        d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
+        d.betamax, d.nin, d.nout, d.smooth = float(betamax), float(nin), float(nout), float(smooth)
+        d.nlayers = L
+        d.thickness = k["thick"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.nstep = k["nst"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        d.epsv = mat.epsv.data_ptr()
+        d.eps_complex = int(mat.eps_complex)
+        d.epsv_strides[:] = mat.ev_strides
+        d.epsa = mat.epsa.data_ptr()
+        d.epsa_strides[:] = mat.ea_strides
+        d.ks = k["ks"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.beta = k["beta"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.phi = k["phi"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.op_cache_bytes = 0
+        # real-arithmetic eigen-solve when every radicand is provably positive:
+        # real eps with all eigenvalues above the largest beam beta squared
+        bmax = max(float(betamax), float(np.max(np.abs(k["beta"]))))
+        d.real_path = int(mat.eps_min is not None and mat.eps_min > bmax * bmax)
+        self.desc = d
+        self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
+        if self.nbytes == 0:
+            msg = _lib.last_error()
+            raise (NotImplementedError if ("supported" in msg or "factor" in msg or "above" in msg) else ValueError)(msg)
+        self.workspace = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        self.updates = int(np.prod(field_shape[:-3])) * int(h) * int(w) * int(k["nst"].sum()) * int(npass)
+
+    def run(self, field_in, field_out, bulk=None, out_given=False, timed=False, stream=None):
+        import torch
+
+        io = _lib.TransferIO()
+        io.field_in = field_in.data_ptr()
+        io.field_out = field_out.data_ptr()
+        io.out_given = int(out_given)
+        io.bulk = bulk.data_ptr() if bulk is not None else None
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device).cuda_stream
+        args = (ctypes.byref(self.desc), ctypes.byref(io), ctypes.c_void_p(self.workspace.data_ptr()),
+                ctypes.c_size_t(self.nbytes), ctypes.c_void_p(stream))
+        if timed:
+            t = _lib.KernelTimes()
+            _lib.check(self.lib.dtmm_transfer_timed(*args, ctypes.byref(t)))
+            return t
+        _lib.check(self.lib.dtmm_transfer(*args))
+        return None
 
 
-def _require_cuda():
-    import torch
-
-    if not torch.cuda.is_available():
-        raise RuntimeError("dtmm_gb300.transfer_field needs a CUDA GPU (the engine has no CPU path)")
-    return torch
-
-
-def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
-                     diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision):
+def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, phi=0.0, nin=None, nout=None,
+                  npass=None, nstep=1, diffraction=None, reflection=None, method=None, betamax=None, smooth=SMOOTH,
+                  precision=None, device=None):
+    """Resolve options like transfer_field and bind a DevicePlan (explicit beta, phi)."""
     torch = _require_cuda()
+    nin = get_default_config_option("nin", nin)
+    nout = get_default_config_option("nout", nout)
+    method = get_default_config_option("method", method)
+    npass = get_default_config_option("npass", npass)
+    diffraction = get_default_config_option("diffraction", diffraction)
+    reflection = get_default_config_option("reflection", reflection)
+    betamax = get_default_config_option("betamax", betamax)
+    precision = _precision[0] if precision is None else precision
+    if reflection is None:
+        reflection = 0 if method == "2x2" else 1
+        if npass > 1:
+            reflection = 1
+    _check_path(method, reflection, npass, diffraction, DTMM_NORM_FFT)
+    shape = tuple(field_shape[-2:])
+    od = validate_optical_data(optical_data, shape)
+    if len(od) != 1:
+        raise NotImplementedError("optical data with more than one block is outside the GPU engine")
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    beta = np.asarray(beta, np.float64)
+    nray = 1 if beta.ndim == 0 else len(beta)
+    nlam = field_shape[-4]
+    npol = int(np.prod(field_shape[:-3])) // (nray * nlam)
+    return DevicePlan(field_shape, _Material(od[0], shape, dev), k0(wavelengths, pixelsize), beta, phi, nray, npol,
+                      nlam, method, diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, dev)
+
+
+def _check_path(method, reflection, npass, diffraction, norm):
     if method == "4x4":
         if reflection not in (1, 2, 3, 4):
             raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
@@ -269,6 +323,20 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         raise NotImplementedError("diffraction=0 is outside the GPU engine")
     if norm != DTMM_NORM_FFT and method == "4x4" and npass > 1:
         raise NotImplementedError("norm modes other than DTMM_NORM_FFT are outside the GPU engine")
+
+
+def _require_cuda():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("dtmm_gb300.transfer_field needs a CUDA GPU (the engine has no CPU path)")
+    return torch
+
+
+def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
+                     diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision):
+    torch = _require_cuda()
+    _check_path(method, reflection, npass, diffraction, norm)
     if smooth < 0:
         smooth = 0.0
     field_in = np.asarray(field_in)
@@ -334,8 +402,9 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         else:
             fout_dev = torch.empty_like(fdev)
             out_given = 0
-    _engine_call(fin_dev, fout_dev, bulk_dev, out_given, mat, ks, beta, phi, nray, npol, nlam, method, diffraction,
-                 reflection, npass, nstep, betamax, nin, nout, smooth, precision)
+    plan = DevicePlan(field_in.shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
+                      nstep, betamax, nin, nout, smooth, precision, dev)
+    plan.run(fin_dev, fout_dev, bulk=bulk_dev, out_given=out_given)
     if ret_bulk:
         res = bulk_dev.to(torch.complex128).cpu().numpy()
         if out is not None:
@@ -438,4 +507,4 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     return res, wavelengths, pixelsize
 
 
-__all__ = ["transfer_field", "set_precision", "DTMM_NORM_FFT", "DTMM_NORM_REF"]
+__all__ = ["transfer_field", "plan_transfer", "DevicePlan", "set_precision", "DTMM_NORM_FFT", "DTMM_NORM_REF"]

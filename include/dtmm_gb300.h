@@ -66,6 +66,11 @@ typedef struct dtmm_transfer_desc {
   /* upper bound on the bytes of cached per-layer operators (npass > 1 reuses
      them across passes when they fit); 0 selects the default (48 GiB) */
   size_t op_cache_bytes;
+  /* 1: the caller guarantees real eps whose every eigenvalue (and hence the
+     effective medium) exceeds max(betamax, beta)^2; every radicand of the
+     eigen-solve is then positive and the engine uses real FP64 arithmetic and
+     half-size operator records.  Ignored for complex eps. */
+  int real_path;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -81,6 +86,17 @@ typedef struct dtmm_transfer_io {
      its first / last slab */
   void* bulk;
 } dtmm_transfer_io;
+
+/* Device-time accounting of one dtmm_transfer_timed call. */
+typedef struct dtmm_kernel_times {
+  double layer_row_ms;     /* fused row kernels (inverse row FFTs, per-voxel operators, forward row FFT) */
+  double layer_col_ms;     /* fused column kernels (column FFTs, k-space operator, window split)        */
+  double voxel_op_ms;      /* FP64 per-voxel layer-operator builds                                       */
+  int layer_row_launches;
+  int layer_col_launches;
+  int voxel_op_launches;
+  int total_launches;      /* every kernel launched by the call                                          */
+} dtmm_kernel_times;
 
 /* ABI version of this header (1). */
 int dtmm_abi_version(void);
@@ -99,6 +115,14 @@ size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc);
    enqueues the work and returns; results are ready when the stream is. */
 int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
                   size_t workspace_bytes, void* stream);
+
+/* dtmm_transfer plus device-time accounting: CUDA events are recorded on
+   `stream` around every fused row / column kernel and operator build; the
+   call synchronises the stream before it returns and fills *times.  Same
+   computation and results as dtmm_transfer; no counterpart in the reference
+   (which has no profiling hooks), used by the benchmark's roofline figures. */
+int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
+                        size_t workspace_bytes, void* stream, dtmm_kernel_times* times);
 
 #ifdef __cplusplus
 }
