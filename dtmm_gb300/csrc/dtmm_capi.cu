@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
@@ -60,6 +61,8 @@ bool make_plan(int n, FFTPlan& p) {
   const int odd[3] = {3, 5, 7};
   for (int q : odd)
     while (m % q == 0 && p.nr < 14) { p.r[p.nr++] = q; m /= q; }
+  p.rbits = 0;
+  for (int i = 0; i < p.nr; ++i) p.rbits |= (unsigned long long)p.r[i] << (3 * i);
   return m == 1 && n >= 1;
 }
 
@@ -292,8 +295,15 @@ struct Engine {
 
   // wavelengths per row block: as many as fit ~100 KB of shared memory
   int row_group() const {
-    const size_t per = 2 * (size_t)d.npol * L.C * d.width * sizeof(cpx<R>);
-    int G = (int)((100 * 1024) / per);
+    const size_t per = 2 * (size_t)d.npol * L.C * (d.width | 1) * sizeof(cpx<R>);
+    // about 16 lines per block (measured best for 256-pixel rows), within ~100 KB
+    int G = 16 / (d.npol * L.C);
+    if (G < 1) G = 1;
+    if ((size_t)G * per > 100 * 1024) G = (int)((100 * 1024) / per);
+    if (const char* e = getenv("DTMM_ROW_GROUP")) {  // tuning override
+      const int v = atoi(e);
+      if (v >= 1 && (size_t)v * per <= 200 * 1024) G = v;
+    }
     if (G < 1) G = 1;
     if (G > d.nlam) G = d.nlam;
     return G;
@@ -301,10 +311,13 @@ struct Engine {
 
   template <int C, bool REAL>
   int launch_row_t(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
-    const size_t smem = 2 * (size_t)p.G * d.npol * C * d.width * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
+    const size_t smem = 2 * (size_t)p.G * d.npol * C * (d.width | 1) * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
     if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels x %d polarisations too large for one block", d.width, d.npol);
     CK(cudaFuncSetAttribute(k_layer_row<R, C, REAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int threads = d.width < 256 ? ((d.width + 31) / 32) * 32 : 256;
+    // a multiple of the line count (fixed line per thread in the FFT passes)
+    const int nl = p.G * d.npol * C;
+    int threads = nl <= 256 ? (256 / nl) * nl : 256;
+    if (d.width < 256 && nl <= 32) threads = std::max(nl, ((d.width + 31) / 32) * 32 / nl * nl);
     const int ngrp = (d.nlam + p.G - 1) / p.G;
     dim3 grid(d.height, d.nray * ngrp);
     mark(PROF_ROW);
@@ -394,6 +407,7 @@ struct Engine {
     OpParams p;
     memset(&p, 0, sizeof(p));
     p.eps_dev = epseff();
+    p.permW = A<int>(L.permW);
     p.epsv = d.epsv;
     p.epsa = d.epsa;
     for (int i = 0; i < 3; ++i) {

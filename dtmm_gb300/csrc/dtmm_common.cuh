@@ -108,7 +108,10 @@ struct FFTPlan {
   int n;
   int nr;
   int r[14];
+  unsigned long long rbits;  // r[i] in bits [3i, 3i+3): read without dynamic indexing
 };
+
+__device__ __forceinline__ int plan_radix(const FFTPlan& p, int i) { return (int)((p.rbits >> (3 * i)) & 7ull); }
 
 template <typename R, bool INV>
 __device__ __forceinline__ cpx<R> twid(const cpx<R>* tw, int idx) {
@@ -190,6 +193,22 @@ __device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, 
   const int total = nb * nlines;
   const int tstep = n / (ns * rad);
   const int nsh = log2_or_neg(ns);
+  if (line_fastest && nthr % nlines == 0) {
+    // each thread keeps one line; butterflies advance by nthr / nlines
+    const int line = tid % nlines;
+    const int bstep = nthr / nlines;
+    cpx<R>* ln = s + line * ls;
+    for (int b = tid / nlines; b < nb; b += bstep) {
+      switch (rad) {
+        case 4: butterfly<R, 4, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        case 2: butterfly<R, 2, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      }
+    }
+    return;
+  }
   for (int t = tid; t < total; t += nthr) {
     int line, b;
     if (line_fastest) {
@@ -216,8 +235,9 @@ __device__ void fft_dit(cpx<R>* s, int es, int ls, int nlines, bool line_fastest
                         const FFTPlan& p) {
   int ns = 1;
   for (int ip = 0; ip < p.nr; ++ip) {
-    fft_pass<R, INV, true>(s, es, ls, nlines, line_fastest, tw, p.n, p.r[ip], ns, threadIdx.x, blockDim.x);
-    ns *= p.r[ip];
+    const int rad = plan_radix(p, ip);
+    fft_pass<R, INV, true>(s, es, ls, nlines, line_fastest, tw, p.n, rad, ns, threadIdx.x, blockDim.x);
+    ns *= rad;
     __syncthreads();
   }
 }
@@ -228,8 +248,9 @@ __device__ void fft_dif(cpx<R>* s, int es, int ls, int nlines, bool line_fastest
                         const FFTPlan& p) {
   int ns = p.n;
   for (int ip = p.nr - 1; ip >= 0; --ip) {
-    ns /= p.r[ip];
-    fft_pass<R, INV, false>(s, es, ls, nlines, line_fastest, tw, p.n, p.r[ip], ns, threadIdx.x, blockDim.x);
+    const int rad = plan_radix(p, ip);
+    ns /= rad;
+    fft_pass<R, INV, false>(s, es, ls, nlines, line_fastest, tw, p.n, rad, ns, threadIdx.x, blockDim.x);
     __syncthreads();
   }
 }
@@ -244,15 +265,17 @@ __device__ void fft_lines_warp(cpx<R>* s, int ls, int nlines, const cpx<R>* tw, 
     if (DIT) {
       int ns = 1;
       for (int ip = 0; ip < p.nr; ++ip) {
-        fft_pass<R, INV, true>(ln, 1, 0, 1, false, tw, p.n, p.r[ip], ns, lane, 32);
-        ns *= p.r[ip];
+        const int rad = plan_radix(p, ip);
+        fft_pass<R, INV, true>(ln, 1, 0, 1, false, tw, p.n, rad, ns, lane, 32);
+        ns *= rad;
         __syncwarp();
       }
     } else {
       int ns = p.n;
       for (int ip = p.nr - 1; ip >= 0; --ip) {
-        ns /= p.r[ip];
-        fft_pass<R, INV, false>(ln, 1, 0, 1, false, tw, p.n, p.r[ip], ns, lane, 32);
+        const int rad = plan_radix(p, ip);
+        ns /= rad;
+        fft_pass<R, INV, false>(ln, 1, 0, 1, false, tw, p.n, rad, ns, lane, 32);
         __syncwarp();
       }
     }

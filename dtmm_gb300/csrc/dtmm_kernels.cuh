@@ -133,6 +133,7 @@ __device__ inline void inv2(const cpx<double> a[2][2], cpx<double> o[2][2]) {
 // whole operator, as the reference's inverse does.
 // ---------------------------------------------------------------------------
 struct OpParams {
+  const int* permW;       // digit reversal of the row length: records of pixel x go to slot permW[x]
   const double* eps_dev;  // if set: (re, im) of the effective medium, overrides eps_eff
   const void* epsv;      // (L?,H?,W?,3) float64 or complex128
   const double* epsa;    // (L?,H?,W?,3) float64
@@ -250,7 +251,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       rec[12] = (al[1] + aw) * p.d;
       rec[13] = (al[3] + aw) * p.d;
     }
-    R* o = (R*)opv + (size_t)rw * OP_REC * HW + pix;
+    R* o = (R*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + p.permW[x];
     for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
     return;
   }
@@ -360,7 +361,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
     }
   }
-  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + pix;
+  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + p.permW[x];
   for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
 }
 
@@ -865,33 +866,34 @@ __device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, 
 }
 
 // Row pass, one row y of a group of G wavelengths (all polarisations) of one
-// ray.  Lines (image, component) are transformed one warp per line; the
-// per-voxel operator records are read once per block and window and the
-// phases once per wavelength.  REAL: records are real (see k_voxel_op).
+// ray.  The (image, component) lines sit at an odd line stride and every FFT
+// pass interleaves butterflies across lines (consecutive threads, consecutive
+// lines), which keeps shared-memory access free of bank conflicts and turns
+// twiddle reads into broadcasts.  The per-voxel step walks the digit-reversed
+// slots q of the inverse transform's output (x = iperm[q]) and accumulates in
+// the same slots, the input order of the forward transform.  Operator records
+// are read once per block and window, phases once per wavelength.
+// REAL: records are real (see k_voxel_op).
 template <typename R, int C, bool REAL>
-__global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cpx<R>* __restrict__ U,
+__global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const cpx<R>* __restrict__ U,
                                                    cpx<R>* __restrict__ X) {
   using T = typename std::conditional<REAL, R, cpx<R>>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int W = g.W, H = g.H, NP = g.npol;
+  const int LS = W | 1;
   const int ngrp = (g.nlam + p.G - 1) / p.G;
   const int y = blockIdx.x;
   const int ray = blockIdx.y / ngrp, grp = blockIdx.y - ray * ngrp;
   const int lam0 = grp * p.G;
   const int G = min(p.G, g.nlam - lam0);
   const int nimg = G * NP, nlines = nimg * C;
-  cpx<R>* acc = (cpx<R>*)smem_raw;             // [nlines][W] (digit-reversed)
-  cpx<R>* tmp = acc + (size_t)p.G * NP * C * W; // [nlines][W]
-  cpx<R>* tw = tmp + (size_t)p.G * NP * C * W;  // [W]
-  int* perm = (int*)(tw + W);                   // [W]
+  cpx<R>* acc = (cpx<R>*)smem_raw;                 // [lines][LS] (digit-reversed)
+  cpx<R>* tmp = acc + (size_t)p.G * NP * C * LS;   // [lines][LS]
+  cpx<R>* tw = tmp + (size_t)p.G * NP * C * LS;    // [W]
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int t = threadIdx.x; t < W; t += blockDim.x) {
-    tw[t] = ((const cpx<R>*)p.tw)[t];
-    perm[t] = p.perm[t];
-  }
-  for (int t = threadIdx.x; t < nlines * W; t += blockDim.x) acc[t] = mk<R>(0, 0);
+  for (int t = threadIdx.x; t < W; t += blockDim.x) tw[t] = ((const cpx<R>*)p.tw)[t];
+  for (int t = threadIdx.x; t < nlines * LS; t += blockDim.x) acc[t] = mk<R>(0, 0);
   const R sc = (R)p.in_scale;
   __syncthreads();
   // line l <-> (image = (g, pol), component c): l = (g * NP + pol) * C + c
@@ -900,45 +902,39 @@ __global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cp
     for (int i = 0; i < p.nx; ++i) {
       const int w = i * p.ny + j;
       if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
-      // window-weighted rows, inverse transform (one warp per line)
-      for (int l = warp; l < nlines; l += nwarps) {
+      // window-weighted rows (natural order, coalesced)
+      for (int l = 0; l < nlines; ++l) {
         const int c = l % C, im = l / C;
         const int gl = im / NP, pol = im - gl * NP;
         const int lam = lam0 + gl;
         const int img = (ray * NP + pol) * g.nlam + lam;
         const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
-        const R* cxi = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
-        cpx<R>* dst = tmp + (size_t)l * W;
-        for (int x = lane; x < W; x += 32) {
+        const R* cxl = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+        cpx<R>* dst = tmp + (size_t)l * LS;
+        for (int x = threadIdx.x; x < W; x += blockDim.x) {
           cpx<R> v = src[x];
-          dst[x] = cxi ? v * cxi[x] : v;
-        }
-        __syncwarp();
-        int ns = p.plan.n;
-        for (int ip = p.plan.nr - 1; ip >= 0; --ip) {
-          ns /= p.plan.r[ip];
-          fft_pass<R, true, false>(dst, 1, 0, 1, false, tw, p.plan.n, p.plan.r[ip], ns, lane, 32);
-          __syncwarp();
+          dst[x] = cxl ? v * cxl[x] : v;
         }
       }
       __syncthreads();
-      // per-voxel operator of window w
+      fft_dif<R, true>(tmp, 1, LS, nlines, true, tw, p.plan);
+      // per-voxel operator of window w; records are stored in the row's
+      // digit-reversed order (slot q), so these loads are coalesced
       const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
-      for (int x = threadIdx.x; x < W; x += blockDim.x) {
-        const int q = perm[x];
+      for (int q = threadIdx.x; q < W; q += blockDim.x) {
         T ef[4], arg_f[2], idf;
         T eb[4], arg_b[2], idb;
 #pragma unroll
-        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
-        idf = opw[(size_t)4 * HW + x];
-        arg_f[0] = opw[(size_t)5 * HW + x];
-        arg_f[1] = opw[(size_t)6 * HW + x];
+        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + q];
+        idf = opw[(size_t)4 * HW + q];
+        arg_f[0] = opw[(size_t)5 * HW + q];
+        arg_f[1] = opw[(size_t)6 * HW + q];
         if (C == 4) {
 #pragma unroll
-          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
-          idb = opw[(size_t)11 * HW + x];
-          arg_b[0] = opw[(size_t)12 * HW + x];
-          arg_b[1] = opw[(size_t)13 * HW + x];
+          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + q];
+          idb = opw[(size_t)11 * HW + q];
+          arg_b[0] = opw[(size_t)12 * HW + q];
+          arg_b[1] = opw[(size_t)13 * HW + q];
         }
         for (int gl = 0; gl < G; ++gl) {
           const R kph = (R)(p.ks[lam0 + gl] * p.dir);
@@ -950,17 +946,17 @@ __global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cp
           }
           for (int pol = 0; pol < NP; ++pol) {
             const int l0 = (gl * NP + pol) * C;
-            const cpx<R>* h = tmp + (size_t)l0 * W + q;
-            cpx<R>* a = acc + (size_t)l0 * W + q;
+            const cpx<R>* h = tmp + (size_t)l0 * LS + q;
+            cpx<R>* a = acc + (size_t)l0 * LS + q;
             if (C == 4) {
-              cpx<R> a0 = a[0], a1 = a[W], a2 = a[2 * W], a3 = a[3 * W];
-              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[2 * W] * sc, a0, a2);
-              apply_block<R, T>(eb, pb0, pb1, h[W] * sc, h[3 * W] * sc, a1, a3);
-              a[0] = a0; a[W] = a1; a[2 * W] = a2; a[3 * W] = a3;
+              cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
+              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[2 * LS] * sc, a0, a2);
+              apply_block<R, T>(eb, pb0, pb1, h[LS] * sc, h[3 * LS] * sc, a1, a3);
+              a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
             } else {
-              cpx<R> a0 = a[0], a1 = a[W];
-              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[W] * sc, a0, a1);
-              a[0] = a0; a[W] = a1;
+              cpx<R> a0 = a[0], a1 = a[LS];
+              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[LS] * sc, a0, a1);
+              a[0] = a0; a[LS] = a1;
             }
           }
         }
@@ -969,19 +965,14 @@ __global__ void __launch_bounds__(256) k_layer_row(RowParams p, Grid g, const cp
     }
   }
   // forward row transform of the accumulator (digit-reversed in, natural out) and store
-  for (int l = warp; l < nlines; l += nwarps) {
-    cpx<R>* ln = acc + (size_t)l * W;
-    int ns = 1;
-    for (int ip = 0; ip < p.plan.nr; ++ip) {
-      fft_pass<R, false, true>(ln, 1, 0, 1, false, tw, p.plan.n, p.plan.r[ip], ns, lane, 32);
-      ns *= p.plan.r[ip];
-      __syncwarp();
-    }
+  fft_dit<R, false>(acc, 1, LS, nlines, true, tw, p.plan);
+  for (int l = 0; l < nlines; ++l) {
     const int c = l % C, im = l / C;
     const int gl = im / NP, pol = im - gl * NP;
     const int img = (ray * NP + pol) * g.nlam + lam0 + gl;
     cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
-    for (int x = lane; x < W; x += 32) dst[x] = ln[x];
+    const cpx<R>* src = acc + (size_t)l * LS;
+    for (int x = threadIdx.x; x < W; x += blockDim.x) dst[x] = src[x];
   }
 }
 
