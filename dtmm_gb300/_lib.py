@@ -20,7 +20,8 @@ PRECISION_MIXED = 0
 PRECISION_DOUBLE = 1
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
-               "dtmm_transfer_timed")
+               "dtmm_transfer_timed", "dtmm_transfer_noalloc")
+STATIC_SCRATCH_BYTES = 64 << 20
 
 
 class TransferDesc(ctypes.Structure):
@@ -110,6 +111,8 @@ def load(build_if_missing=True):
     lib.dtmm_transfer_timed.restype = ctypes.c_int
     lib.dtmm_transfer_timed.argtypes = [ctypes.POINTER(TransferDesc), ctypes.POINTER(TransferIO), ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(KernelTimes)]
+    lib.dtmm_transfer_noalloc.restype = ctypes.c_int
+    lib.dtmm_transfer_noalloc.argtypes = [ctypes.POINTER(TransferDesc), ctypes.POINTER(TransferIO), ctypes.c_void_p]
     if lib.dtmm_abi_version() != 1:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib

@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -714,6 +715,32 @@ int transfer_impl(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, vo
   return run_engine<float>(desc, io, workspace, L, st, prof, launches);
 }
 
+// ---------------------------------------------------------------------------
+// Static device scratch for dtmm_transfer_noalloc.  In host code the name
+// g_static_scratch is only a host-side stand-in for the device array, so the
+// device address is resolved once per device with cudaGetSymbolAddress.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_static_scratch[DTMM_STATIC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_ptr[kMaxDevices] = {};
+
+int static_scratch(void** out) {
+  int dev = -1;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(DTMM_EINVAL, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (g_scratch_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return fail(DTMM_ECUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+    g_scratch_ptr[dev] = p;
+  }
+  *out = g_scratch_ptr[dev];
+  return DTMM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -730,6 +757,19 @@ size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc) {
 int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
                   void* stream) {
   return transfer_impl(desc, io, workspace, workspace_bytes, stream, nullptr, nullptr);
+}
+
+int dtmm_transfer_noalloc(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* stream) {
+  g_err.clear();
+  int rc = check_desc(desc);
+  if (rc) return rc;
+  const size_t need = layout_of(desc).total;
+  if (need > DTMM_STATIC_SCRATCH_BYTES)
+    return fail(DTMM_ENOSPACE, "transfer needs %zu bytes of scratch; the static scratch holds %zu", need,
+                (size_t)DTMM_STATIC_SCRATCH_BYTES);
+  void* ws = nullptr;
+  if ((rc = static_scratch(&ws))) return rc;
+  return transfer_impl(desc, io, ws, DTMM_STATIC_SCRATCH_BYTES, stream, nullptr, nullptr);
 }
 
 int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,

@@ -124,6 +124,31 @@ int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, vo
 int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
                         size_t workspace_bytes, void* stream, dtmm_kernel_times* times);
 
+/* Capacity of the library's static device scratch (64 MiB), see dtmm_transfer_noalloc. */
+#define DTMM_STATIC_SCRATCH_BYTES ((size_t)64 << 20)
+
+/* dtmm_transfer without any device allocation, for callers that cannot
+   allocate device memory when they call: plugin hosts that hand the engine
+   only their own input/output buffers and keep every other allocation to
+   themselves, and latency-bound loops whose budget a cudaMalloc (which can
+   synchronise or fail under memory pressure) would break.  The workspace is a
+   file-scope device array of DTMM_STATIC_SCRATCH_BYTES that every GPU loading
+   the library holds until the process exits; the caller still passes the
+   input and output fields.  No counterpart in the reference (which allocates
+   numpy temporaries freely).
+   - The first call on a device resolves the array's device address
+     (cudaGetSymbolAddress) with that device current; make that first call
+     before any stream capture.
+   - Transfers whose workspace (dtmm_transfer_workspace_size) exceeds the
+     array are rejected with DTMM_ENOSPACE and a message giving both sizes.
+   - Every call shares the one array: calls that overlap on the GPU (other
+     streams, other host threads) race and must be serialised by the caller.
+     No part of the scratch has to start at zero: every buffer is written
+     before it is read, so a call is unaffected by the previous call's
+     leftovers.
+   - Calls no cudaMalloc, cudaFree or allocating library routine. */
+int dtmm_transfer_noalloc(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
