@@ -81,7 +81,8 @@ struct Layout {
   size_t cplx;  // bytes of one complex
   size_t HW;
   size_t small, part, twH, permH, twW, permW, cx, cy, kfirst, klast, kdiag, pin, pout;
-  size_t F, X, U, field0, op;
+  size_t F, X, U, field0, op, Xw, Xa;
+  bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
 };
@@ -105,9 +106,6 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (!d->epsv || !d->epsa) return fail(DTMM_EINVAL, "null material pointer");
   for (int l = 0; l < d->nlayers; ++l)
     if (d->nstep[l] < 1) return fail(DTMM_EINVAL, "nstep must be >= 1");
-  if (d->diffraction > 1)
-    for (int l = 0; l < d->nlayers; ++l)
-      if (d->nstep[l] != 1) return fail(DTMM_ENOTSUP, "nstep > 1 with diffraction > 1 is not supported on this path");
   FFTPlan p;
   if (!make_plan(d->height, p) || !make_plan(d->width, p))
     return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", d->height, d->width);
@@ -155,6 +153,12 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.X = take(field);
   L.U = take(field * (size_t)(L.ny > 1 ? L.ny : 1));
   L.field0 = take(passes ? field : 0);
+  L.chains = false;
+  if (L.nwin > 1)
+    for (int l = 0; l < d->nlayers; ++l)
+      if (d->nstep[l] > 1) L.chains = true;
+  L.Xw = take(L.chains ? field : 0);
+  L.Xa = take(L.chains ? field : 0);
   L.op_one = L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
@@ -265,9 +269,12 @@ struct Engine {
   }
 
   int launch_col(const cpx<R>* in, cpx<R>* out, int cin, int cout, int kop, const void* ktab, int ny,
-                 const R* cy, bool do_fwd, bool inverse_out, double scale, size_t ktab_ray_stride = 0) {
+                 const R* cy, bool do_fwd, bool inverse_out, double scale, size_t ktab_ray_stride = 0,
+                 int j_only = -1) {
     ColParams p;
     p.ktab_ray_stride = ktab_ray_stride;
+    p.j_only = j_only;
+    p.cy_rows = L.ny;
     p.cin = cin;
     p.cout = cout;
     p.kop = kop;
@@ -312,15 +319,16 @@ struct Engine {
 
   template <int C, bool REAL>
   int launch_row_t(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
-    const size_t smem = 2 * (size_t)p.G * d.npol * C * (d.width | 1) * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
-    if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels x %d polarisations too large for one block", d.width, d.npol);
+    const size_t smem = 2 * (size_t)p.G * p.PB * C * (d.width | 1) * sizeof(cpx<R>) + d.width * (sizeof(cpx<R>) + sizeof(int));
+    if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
     CK(cudaFuncSetAttribute(k_layer_row<R, C, REAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // a multiple of the line count (fixed line per thread in the FFT passes)
-    const int nl = p.G * d.npol * C;
+    const int nl = p.G * p.PB * C;
     int threads = nl <= 256 ? (256 / nl) * nl : 256;
     if (d.width < 256 && nl <= 32) threads = std::max(nl, ((d.width + 31) / 32) * 32 / nl * nl);
     const int ngrp = (d.nlam + p.G - 1) / p.G;
-    dim3 grid(d.height, d.nray * ngrp);
+    const int npg = (d.npol + p.PB - 1) / p.PB;
+    dim3 grid(d.height, d.nray * ngrp * npg);
     mark(PROF_ROW);
     k_layer_row<R, C, REAL><<<grid, threads, smem, st>>>(p, g, Ub, Xb);
     mark(PROF_ROW);
@@ -328,8 +336,61 @@ struct Engine {
     return DTMM_OK;
   }
 
-  int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const void* op, double dir) {
+  // register-transform row kernel: float bulk, W = N1 * N2 in {64 ... 1024}
+  bool row_reg() const { return sizeof(R) == 4 && (d.width == 64 || d.width == 128 || d.width == 256 ||
+                                                   d.width == 512 || d.width == 1024); }
+
+  int row_group_reg() const {
+    const int perG = d.npol * L.C;  // lines per wavelength
+    const int n1 = d.width >= 1024 ? 32 : (d.width >= 256 ? 16 : 8);
+    const size_t line_bytes = 2 * (size_t)d.width * sizeof(cpx<R>);
+    // about 8 lines per block measured best (256-pixel rows, 4x4, 2 polarisations)
+    int G = std::max(1, 8 / perG);
+    if (const char* e = getenv("DTMM_ROW_GROUP")) {
+      const int v = atoi(e);
+      if (v >= 1) G = v;
+    }
+    while (G > 1 && ((size_t)G * perG * line_bytes > 110 * 1024 || G * perG * n1 > 512)) --G;
+    return std::min(G, d.nlam);
+  }
+
+  template <int C, bool REAL, int N1, int N2>
+  int launch_row_reg_t(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
+    const int nl = p.G * p.PB * C;
+    const size_t smem = 2 * (size_t)nl * d.width * sizeof(cpx<R>) + d.width * sizeof(cpx<R>);
+    if (smem > 220 * 1024 || nl * N1 > 512)
+      return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
+    auto kern = k_layer_row_reg<R, C, REAL, N1, N2>;
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int threads = std::max(((nl * N1 + 31) / 32) * 32, 32);
+    const int ngrp = (d.nlam + p.G - 1) / p.G;
+    const int npg = (d.npol + p.PB - 1) / p.PB;
+    dim3 grid(d.height, d.nray * ngrp * npg);
+    mark(PROF_ROW);
+    kern<<<grid, threads, smem, st>>>(p, g, Ub, Xb);
+    mark(PROF_ROW);
+    CKL("k_layer_row_reg");
+    return DTMM_OK;
+  }
+
+  template <int C, bool REAL>
+  int launch_row_reg(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
+    switch (d.width) {
+      case 64: return launch_row_reg_t<C, REAL, 8, 8>(p, Ub, Xb);
+      case 128: return launch_row_reg_t<C, REAL, 8, 16>(p, Ub, Xb);
+      case 256: return launch_row_reg_t<C, REAL, 16, 16>(p, Ub, Xb);
+      case 512: return launch_row_reg_t<C, REAL, 16, 32>(p, Ub, Xb);
+      default: return launch_row_reg_t<C, REAL, 32, 32>(p, Ub, Xb);
+    }
+  }
+
+  int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const void* op, double dir, int win_only = -1, bool use_cx = true,
+                 bool accumulate = false) {
     RowParams p;
+    p.win_only = win_only;
+    p.use_cx = use_cx ? 1 : 0;
+    p.accumulate = accumulate ? 1 : 0;
+    p.PB = d.npol;
     p.C = L.C;
     p.nx = L.nx;
     p.ny = L.ny;
@@ -342,8 +403,16 @@ struct Engine {
     p.plan = pW;
     p.tw = P(L.twW);
     p.perm = A<int>(L.permW);
-    p.G = row_group();
     const bool re = real_ops();
+    if (row_reg()) {
+      p.G = row_group_reg();
+      const int n1 = d.width >= 1024 ? 32 : (d.width >= 256 ? 16 : 8);
+      if (2 * (size_t)d.npol * L.C * d.width * sizeof(cpx<R>) > 200 * 1024 || d.npol * L.C * n1 > 512) p.PB = 1;
+      if (L.C == 4) return re ? launch_row_reg<4, true>(p, Ub, Xb) : launch_row_reg<4, false>(p, Ub, Xb);
+      return re ? launch_row_reg<2, true>(p, Ub, Xb) : launch_row_reg<2, false>(p, Ub, Xb);
+    }
+    p.G = row_group();
+    if (2 * (size_t)d.npol * L.C * (d.width | 1) * sizeof(cpx<R>) > 200 * 1024) p.PB = 1;
     if (L.C == 4) return re ? launch_row_t<4, true>(p, Ub, Xb) : launch_row_t<4, false>(p, Ub, Xb);
     return re ? launch_row_t<2, true>(p, Ub, Xb) : launch_row_t<2, false>(p, Ub, Xb);
   }
@@ -408,7 +477,7 @@ struct Engine {
     OpParams p;
     memset(&p, 0, sizeof(p));
     p.eps_dev = epseff();
-    p.permW = A<int>(L.permW);
+    p.permW = row_reg() ? nullptr : A<int>(L.permW);
     p.epsv = d.epsv;
     p.epsa = d.epsa;
     for (int i = 0; i < 3; ++i) {
@@ -482,63 +551,116 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // ordered list of sub-steps of one pass: (layer index, signed thickness)
-  void substeps(int dir, std::vector<std::pair<int, double>>& out) const {
+  // layer order of one pass
+  void layer_order(int dir, std::vector<int>& out) const {
     out.clear();
-    for (int q = 0; q < d.nlayers; ++q) {
-      const int l = dir > 0 ? q : d.nlayers - 1 - q;
-      const double ds = d.thickness[l] / d.nstep[l];
-      for (int s = 0; s < d.nstep[l]; ++s) out.push_back({l, ds});
+    for (int q = 0; q < d.nlayers; ++q) out.push_back(dir > 0 ? q : d.nlayers - 1 - q);
+  }
+
+  // One layer of `nst` sub-steps of thickness ds (signed by dir).  `in` holds
+  // the state entering the layer (rows transformed along x), cin components;
+  // the entry k-space operator is (kop0, ktab0).  Result: state in *out.
+  // Without windows, or with one sub-step, every sub-step is one column and
+  // one row pass.  With windows and several sub-steps each window follows its
+  // own chain through the sub-steps (the reference applies the window once,
+  // then all sub-steps to that part), and the chains are summed.
+  int layer(const cpx<R>* in, int cin, int kop0, const void* ktab0, size_t ktab0_ray, cpx<R>*& out, const void* op,
+            double dir, int nst, double ds) {
+    int rc;
+    const int C = L.C;
+    cpx<R>* U = P(L.U);
+    const R* cy = L.ny > 1 ? A<R>(L.cy) : nullptr;
+    if (L.nwin == 1 || nst == 1) {
+      cpx<R>* X = P(L.X);
+      for (int s = 0; s < nst; ++s) {
+        if (s == 0) {
+          if ((rc = launch_col(in, U, cin, C, kop0, ktab0, L.ny, cy, true, true, 1.0, ktab0_ray))) return rc;
+        } else {
+          if ((rc = diag_table(dir * ds))) return rc;
+          if ((rc = launch_col(X, U, C, C, KOP_DIAG, P(L.kdiag), 1, nullptr, true, true, 1.0))) return rc;
+        }
+        if ((rc = launch_row(U, X, op, dir))) return rc;
+      }
+      out = X;
+      return DTMM_OK;
     }
+    cpx<R>* Xw = P(L.Xw);
+    cpx<R>* Xa = P(L.Xa);
+    for (int w = 0; w < L.nwin; ++w) {
+      const int j = w % L.ny;
+      for (int s = 0; s < nst; ++s) {
+        cpx<R>* dst = (s + 1 == nst) ? Xa : Xw;
+        if (s == 0) {
+          if ((rc = launch_col(in, U, cin, C, kop0, ktab0, 1, cy, true, true, 1.0, ktab0_ray, j))) return rc;
+        } else {
+          if ((rc = diag_table(dir * ds))) return rc;
+          if ((rc = launch_col(Xw, U, C, C, KOP_DIAG, P(L.kdiag), 1, nullptr, true, true, 1.0))) return rc;
+        }
+        if ((rc = launch_row(U, dst, op, dir, w, s == 0, s + 1 == nst && w > 0))) return rc;
+      }
+    }
+    out = Xa;
+    return DTMM_OK;
+  }
+
+  // operators of layer l (cached across passes when they fit)
+  int layer_ops(int pass, int l, double ds, const void*& op) {
+    if (L.cache_ops) {
+      op = (const void*)(ws + L.op + L.op_one * (size_t)l);
+      if (pass == 0) return voxel_ops(l, ds, (cpx<R>*)op);
+      return DTMM_OK;
+    }
+    op = P(L.op);
+    return voxel_ops(l, ds, P(L.op));
   }
 
   // state F (real space, 4 components) -> propagated through all layers -> F
   int sweep4(int pass, cpx<R>* bulk) {
     const double dir = (pass % 2 == 0) ? 1.0 : -1.0;
-    std::vector<std::pair<int, double>> sub;
-    substeps(pass % 2 == 0 ? 1 : -1, sub);
+    std::vector<int> order;
+    layer_order(pass % 2 == 0 ? 1 : -1, order);
     cpx<R>* F = P(L.F);
-    cpx<R>* X = P(L.X);
     cpx<R>* U = P(L.U);
     int rc;
     if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
-    if ((rc = launch_ktab(KT_D1, dir * sub.front().second / 2, P(L.kfirst)))) return rc;
+    const cpx<R>* cur = F;
     double dprev = 0.0;
-    int cur_layer = -1;
-    for (size_t s = 0; s < sub.size(); ++s) {
-      const int l = sub[s].first;
-      const double ds = sub[s].second;
-      const cpx<R>* op;
-      if (L.cache_ops) {
-        op = (const cpx<R>*)(ws + L.op + L.op_one * (size_t)l);
-        if (pass == 0 && l != cur_layer && (rc = voxel_ops(l, ds, (cpx<R>*)op))) return rc;
-      } else {
-        op = P(L.op);
-        if (l != cur_layer && (rc = voxel_ops(l, ds, P(L.op)))) return rc;
-      }
-      cur_layer = l;
-      if (s == 0) {
-        rc = launch_col(F, U, 4, 4, KOP_MAT, P(L.kfirst), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
-                        1.0);
+    for (size_t q = 0; q < order.size(); ++q) {
+      const int l = order[q];
+      const int nst = d.nstep[l];
+      const double ds = d.thickness[l] / nst;
+      const void* op;
+      if ((rc = layer_ops(pass, l, ds, op))) return rc;
+      int kop;
+      const void* ktab;
+      if (q == 0) {
+        if ((rc = launch_ktab(KT_D1, dir * ds / 2, P(L.kfirst)))) return rc;
+        kop = KOP_MAT;
+        ktab = P(L.kfirst);
       } else {
         if ((rc = diag_table(dir * 0.5 * (dprev + ds)))) return rc;
-        rc = launch_col(X, U, 4, 4, KOP_DIAG, P(L.kdiag), L.ny, L.ny > 1 ? A<R>(L.cy) : nullptr, true, true,
-                        1.0);
+        kop = KOP_DIAG;
+        ktab = P(L.kdiag);
       }
-      if (rc) return rc;
-      if ((rc = launch_row(U, X, op, dir))) return rc;
+      cpx<R>* out = nullptr;
+      if ((rc = layer(cur, 4, kop, ktab, 0, out, op, dir, nst, ds))) return rc;
+      // keep the layer result out of the buffers the next layer writes
+      if (out != P(L.X) && q + 1 < order.size() && L.chains) {
+        CK(cudaMemcpyAsync(P(L.X), out, sizeof(cpx<R>) * (size_t)NI * 4 * L.HW, cudaMemcpyDeviceToDevice, st));
+        out = P(L.X);
+      }
+      cur = out;
       dprev = ds;
-      const bool last_of_layer = (s + 1 == sub.size()) || (sub[s + 1].first != l);
-      if (bulk && last_of_layer) {
+      if (bulk) {
         // bulk[l + 1] = ifft2(D2 . X) (dtmm/transfer.py:758-764, :878-880)
         cpx<R>* slab = bulk + (size_t)(l + 1) * NI * 4 * L.HW;
         if ((rc = launch_ktab(KT_D2, dir * ds / 2, P(L.klast)))) return rc;
-        if ((rc = launch_col(X, slab, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+        if ((rc = launch_col(cur, slab, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
         if ((rc = launch_rows(slab, 4, true, 1.0 / d.width))) return rc;
       }
     }
-    if ((rc = launch_ktab(KT_D2, dir * sub.back().second / 2, P(L.klast)))) return rc;
-    if ((rc = launch_col(X, U, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_ktab(KT_D2, dir * dprev / 2, P(L.klast)))) return rc;
+    if ((rc = launch_col(cur, U, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
     if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;
     CK(cudaMemcpyAsync(F, U, sizeof(cpx<R>) * (size_t)NI * 4 * L.HW, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;
@@ -642,36 +764,45 @@ struct Engine {
     cpx<R>* fin = (cpx<R>*)io.field_in;
     cpx<R>* fout = (cpx<R>*)io.field_out;
     cpx<R>* F = P(L.F);
-    cpx<R>* X = P(L.X);
     cpx<R>* U = P(L.U);
     const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
-    std::vector<std::pair<int, double>> sub;
-    substeps(1, sub);
+    std::vector<int> order;
+    layer_order(1, order);
     CK(cudaMemcpyAsync(F, fin, bytes4, cudaMemcpyDeviceToDevice, st));
     if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
-    // entry: transmitted part in n_in, interface n_in -> effective, half step
-    if ((rc = launch_ktab(KT_2IN, sub.front().second / 2, P(L.kfirst)))) return rc;
+    const cpx<R>* cur = F;
+    int cin = 4;
     double dprev = 0.0;
-    int cur_layer = -1;
-    for (size_t s = 0; s < sub.size(); ++s) {
-      const int l = sub[s].first;
-      const double ds = sub[s].second;
-      if (l != cur_layer && (rc = voxel_ops(l, ds, P(L.op)))) return rc;
-      cur_layer = l;
-      const R* cy = L.ny > 1 ? A<R>(L.cy) : nullptr;
-      if (s == 0) {
-        rc = launch_col(F, U, 4, 2, KOP_MAT, P(L.kfirst), L.ny, cy, true, true, 1.0);
+    for (size_t q = 0; q < order.size(); ++q) {
+      const int l = order[q];
+      const int nst = d.nstep[l];
+      const double ds = d.thickness[l] / nst;
+      if ((rc = voxel_ops(l, ds, P(L.op)))) return rc;
+      int kop;
+      const void* ktab;
+      if (q == 0) {
+        // entry: transmitted part in n_in, interface n_in -> effective, half step
+        if ((rc = launch_ktab(KT_2IN, ds / 2, P(L.kfirst)))) return rc;
+        kop = KOP_MAT;
+        ktab = P(L.kfirst);
       } else {
         if ((rc = diag_table(0.5 * (dprev + ds)))) return rc;
-        rc = launch_col(X, U, 2, 2, KOP_DIAG, P(L.kdiag), L.ny, cy, true, true, 1.0);
+        kop = KOP_DIAG;
+        ktab = P(L.kdiag);
       }
-      if (rc) return rc;
-      if ((rc = launch_row(U, X, P(L.op), 1.0))) return rc;
+      cpx<R>* out = nullptr;
+      if ((rc = layer(cur, cin, kop, ktab, 0, out, P(L.op), 1.0, nst, ds))) return rc;
+      if (out != P(L.X) && q + 1 < order.size() && L.chains) {
+        CK(cudaMemcpyAsync(P(L.X), out, sizeof(cpx<R>) * (size_t)NI * 2 * L.HW, cudaMemcpyDeviceToDevice, st));
+        out = P(L.X);
+      }
+      cur = out;
+      cin = 2;
       dprev = ds;
     }
     // exit: half step, interface effective -> n_out, windows and E -> H
-    if ((rc = launch_ktab(KT_2OUT, sub.back().second / 2, P(L.klast)))) return rc;
-    if ((rc = launch_col(X, U, 2, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height,
+    if ((rc = launch_ktab(KT_2OUT, dprev / 2, P(L.klast)))) return rc;
+    if ((rc = launch_col(cur, U, 2, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height,
                          (size_t)d.nlam * L.HW * 8)))
       return rc;
     if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;

@@ -133,7 +133,7 @@ __device__ inline void inv2(const cpx<double> a[2][2], cpx<double> o[2][2]) {
 // whole operator, as the reference's inverse does.
 // ---------------------------------------------------------------------------
 struct OpParams {
-  const int* permW;       // digit reversal of the row length: records of pixel x go to slot permW[x]
+  const int* permW;       // digit reversal of the row length: records of pixel x go to slot permW[x] (null: x)
   const double* eps_dev;  // if set: (re, im) of the effective medium, overrides eps_eff
   const void* epsv;      // (L?,H?,W?,3) float64 or complex128
   const double* epsa;    // (L?,H?,W?,3) float64
@@ -251,7 +251,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       rec[12] = (al[1] + aw) * p.d;
       rec[13] = (al[3] + aw) * p.d;
     }
-    R* o = (R*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + p.permW[x];
+    R* o = (R*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + (p.permW ? p.permW[x] : x);
     for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
     return;
   }
@@ -361,7 +361,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
     }
   }
-  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + p.permW[x];
+  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + (p.permW ? p.permW[x] : x);
   for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
 }
 
@@ -721,6 +721,8 @@ struct ColParams {
   const void* ktab;        // KOP_DIAG: [lam][H][W][2]; KOP_MAT: [lam][H][W][cout][cin]
   int ny;                  // window rows (1 = no windows)
   const void* cy;          // [ray][j][lam][H] (null = weight 1)
+  int j_only;              // >= 0: emit only window row j_only (into U slot 0)
+  int cy_rows;             // window rows in the cy table (ray stride = cy_rows * nlam * H)
   int do_fwd;              // 1: transform along y first (input spatial in y)
   int inverse_out;         // 1: inverse column FFT on the way out
   double out_scale;
@@ -792,10 +794,11 @@ __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cp
   }
   const int C = p.cout;
   const R sc = (R)p.out_scale;
-  for (int j = 0; j < p.ny; ++j) {
+  for (int jj = 0; jj < p.ny; ++jj) {
+    const int j = p.j_only >= 0 ? p.j_only : jj;
     cpx<R>* buf = T;
     if (p.cy != nullptr) {
-      const R* cyj = (const R*)p.cy + (((size_t)ray * p.ny + j) * g.nlam + lam) * H;
+      const R* cyj = (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H;
       for (int t = threadIdx.x; t < H * C * TC; t += blockDim.x) {
         const int y = t / (C * TC), r = t - y * C * TC;
         const size_t o = (size_t)y * es + r;
@@ -805,7 +808,7 @@ __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cp
       __syncthreads();
     }
     if (p.inverse_out) fft_dif<R, true>(buf, es, 1, C * TC, true, tw, p.plan);
-    cpx<R>* Uj = U + (size_t)j * g.NI * C * H * W;
+    cpx<R>* Uj = U + (size_t)jj * g.NI * C * H * W;
     for (int t = threadIdx.x; t < C * H * TC; t += blockDim.x) {
       const int c = t / (H * TC), r = t - c * H * TC;
       const int y = r / TC, xc = r - y * TC;
@@ -839,6 +842,10 @@ struct RowParams {
   const void* tw;
   const int* perm;
   int G;                 // wavelengths per block
+  int PB;                // polarisations per block
+  int win_only;          // >= 0: only this window (its own sub-step chain), -1: all
+  int use_cx;            // apply the window's beta_x weight (first sub-step of a chain)
+  int accumulate;        // add the result to X instead of overwriting it
 };
 
 template <typename R>
@@ -879,17 +886,20 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
                                                    cpx<R>* __restrict__ X) {
   using T = typename std::conditional<REAL, R, cpx<R>>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int W = g.W, H = g.H, NP = g.npol;
+  const int W = g.W, H = g.H;
   const int LS = W | 1;
   const int ngrp = (g.nlam + p.G - 1) / p.G;
+  const int npg = (g.npol + p.PB - 1) / p.PB;
   const int y = blockIdx.x;
-  const int ray = blockIdx.y / ngrp, grp = blockIdx.y - ray * ngrp;
-  const int lam0 = grp * p.G;
+  const int pg = blockIdx.y % npg, rg = blockIdx.y / npg;
+  const int ray = rg / ngrp, grp = rg - ray * ngrp;
+  const int lam0 = grp * p.G, pol0 = pg * p.PB;
   const int G = min(p.G, g.nlam - lam0);
+  const int NP = min(p.PB, g.npol - pol0);  // polarisations of this block
   const int nimg = G * NP, nlines = nimg * C;
   cpx<R>* acc = (cpx<R>*)smem_raw;                 // [lines][LS] (digit-reversed)
-  cpx<R>* tmp = acc + (size_t)p.G * NP * C * LS;   // [lines][LS]
-  cpx<R>* tw = tmp + (size_t)p.G * NP * C * LS;    // [W]
+  cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * LS; // [lines][LS]
+  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * LS;  // [W]
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
   for (int t = threadIdx.x; t < W; t += blockDim.x) tw[t] = ((const cpx<R>*)p.tw)[t];
@@ -898,18 +908,20 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
   __syncthreads();
   // line l <-> (image = (g, pol), component c): l = (g * NP + pol) * C + c
   for (int j = 0; j < p.ny; ++j) {
-    const cpx<R>* Uj = U + (size_t)j * g.NI * C * HW;
+    // a single-window chain reads the one window row the column pass emitted
+    const cpx<R>* Uj = U + (size_t)(p.win_only >= 0 ? 0 : j) * g.NI * C * HW;
     for (int i = 0; i < p.nx; ++i) {
       const int w = i * p.ny + j;
+      if (p.win_only >= 0 && w != p.win_only) continue;
       if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
       // window-weighted rows (natural order, coalesced)
       for (int l = 0; l < nlines; ++l) {
         const int c = l % C, im = l / C;
-        const int gl = im / NP, pol = im - gl * NP;
+        const int gl = im / NP, pol = pol0 + im - gl * NP;
         const int lam = lam0 + gl;
-        const int img = (ray * NP + pol) * g.nlam + lam;
+        const int img = (ray * g.npol + pol) * g.nlam + lam;
         const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
-        const R* cxl = p.cx ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+        const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
         cpx<R>* dst = tmp + (size_t)l * LS;
         for (int x = threadIdx.x; x < W; x += blockDim.x) {
           cpx<R> v = src[x];
@@ -968,11 +980,132 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
   fft_dit<R, false>(acc, 1, LS, nlines, true, tw, p.plan);
   for (int l = 0; l < nlines; ++l) {
     const int c = l % C, im = l / C;
-    const int gl = im / NP, pol = im - gl * NP;
-    const int img = (ray * NP + pol) * g.nlam + lam0 + gl;
+    const int gl = im / NP, pol = pol0 + im - gl * NP;
+    const int img = (ray * g.npol + pol) * g.nlam + lam0 + gl;
     cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
     const cpx<R>* src = acc + (size_t)l * LS;
-    for (int x = threadIdx.x; x < W; x += blockDim.x) dst[x] = src[x];
+    for (int x = threadIdx.x; x < W; x += blockDim.x) dst[x] = p.accumulate ? dst[x] + src[x] : src[x];
+  }
+}
+
+// Row pass for power-of-two rows W = N1 * N2 (float bulk): the same work as
+// k_layer_row with every line transformed in registers by a group of N1
+// lanes (line_fft_2step); the transforms leave natural order, so the
+// per-voxel step, the accumulator and the operator records are in natural
+// order and only the per-voxel step needs block-wide barriers.
+template <typename R, int C, bool REAL, int N1, int N2>
+__global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
+                                                         cpx<R>* __restrict__ X) {
+  using T = typename std::conditional<REAL, R, cpx<R>>::type;
+  constexpr int W = N1 * N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = g.H;
+  const int ngrp = (g.nlam + p.G - 1) / p.G;
+  const int npg = (g.npol + p.PB - 1) / p.PB;
+  const int y = blockIdx.x;
+  const int pg = blockIdx.y % npg, rg = blockIdx.y / npg;
+  const int ray = rg / ngrp, grp = rg - ray * ngrp;
+  const int lam0 = grp * p.G, pol0 = pg * p.PB;
+  const int G = min(p.G, g.nlam - lam0);
+  const int NP = min(p.PB, g.npol - pol0);  // polarisations of this block
+  const int nlines = G * NP * C;
+  cpx<R>* acc = (cpx<R>*)smem_raw;                 // [lines][W]
+  cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * W;  // [lines][W] exchange and transformed rows
+  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * W;   // [W]  exp(-2 pi i e / W)
+  const int HW = H * W;
+  const int nwin = p.nx * p.ny;
+  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  for (int e = threadIdx.x; e < nlines * W; e += blockDim.x) acc[e] = mk<R>(0, 0);
+  const R sc = (R)p.in_scale;
+  __syncthreads();
+  const int line = threadIdx.x / N1, t = threadIdx.x % N1;
+  const bool active = line < nlines;
+  // the lane's twiddles W_N^(t k1) in registers when they fit
+  constexpr bool TWREG = N2 <= 16;
+  cpx<R> trow[TWREG ? N2 : 1];
+  if (TWREG) {
+#pragma unroll
+    for (int k1 = 0; k1 < (TWREG ? N2 : 1); ++k1) trow[k1] = tw[(t * k1) & (W - 1)];
+  }
+  const int c = line % C, im = line / C;
+  const int gl = im / NP, pol = pol0 + im - gl * NP;
+  const int lam = lam0 + gl;
+  const int img = (ray * g.npol + pol) * g.nlam + lam;
+  cpx<R>* xl = tmp + (size_t)line * W;
+  for (int j = 0; j < p.ny; ++j) {
+    // a single-window chain reads the one window row the column pass emitted
+    const cpx<R>* Uj = U + (size_t)(p.win_only >= 0 ? 0 : j) * g.NI * C * HW;
+    for (int i = 0; i < p.nx; ++i) {
+      const int w = i * p.ny + j;
+      if (p.win_only >= 0 && w != p.win_only) continue;
+      if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
+      if (active) {
+        const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
+        const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+        cpx<R> v[N2];
+#pragma unroll
+        for (int m = 0; m < N2; ++m) {
+          cpx<R> a = src[t + N1 * m];
+          v[m] = cxl ? a * cxl[t + N1 * m] : a;
+        }
+        line_fft_2step<R, N1, N2, true>(v, xl, TWREG ? trow : nullptr, tw, t);
+#pragma unroll
+        for (int m = 0; m < N2; ++m) xl[t + N1 * m] = v[m] * sc;
+      }
+      __syncthreads();
+      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      for (int x = threadIdx.x; x < W; x += blockDim.x) {
+        T ef[4], arg_f[2], idf;
+        T eb[4], arg_b[2], idb;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
+        idf = opw[(size_t)4 * HW + x];
+        arg_f[0] = opw[(size_t)5 * HW + x];
+        arg_f[1] = opw[(size_t)6 * HW + x];
+        if (C == 4) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
+          idb = opw[(size_t)11 * HW + x];
+          arg_b[0] = opw[(size_t)12 * HW + x];
+          arg_b[1] = opw[(size_t)13 * HW + x];
+        }
+        for (int g2 = 0; g2 < G; ++g2) {
+          const R kph = (R)(p.ks[lam0 + g2] * p.dir);
+          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
+          cpx<R> pb0, pb1;
+          if (C == 4) {
+            pb0 = phase_of(arg_b[0], kph) * idb;
+            pb1 = phase_of(arg_b[1], kph) * idb;
+          }
+          for (int q = 0; q < NP; ++q) {
+            const int l0 = (g2 * NP + q) * C;
+            const cpx<R>* h = tmp + (size_t)l0 * W + x;
+            cpx<R>* a = acc + (size_t)l0 * W + x;
+            if (C == 4) {
+              cpx<R> a0 = a[0], a1 = a[W], a2 = a[2 * W], a3 = a[3 * W];
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * W], a0, a2);
+              apply_block<R, T>(eb, pb0, pb1, h[W], h[3 * W], a1, a3);
+              a[0] = a0; a[W] = a1; a[2 * W] = a2; a[3 * W] = a3;
+            } else {
+              cpx<R> a0 = a[0], a1 = a[W];
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[W], a0, a1);
+              a[0] = a0; a[W] = a1;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (active) {
+    cpx<R> v[N2];
+    const cpx<R>* al = acc + (size_t)line * W;
+#pragma unroll
+    for (int m = 0; m < N2; ++m) v[m] = al[t + N1 * m];
+    line_fft_2step<R, N1, N2, false>(v, xl, TWREG ? trow : nullptr, tw, t);
+    cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
+#pragma unroll
+    for (int m = 0; m < N2; ++m) dst[t + N1 * m] = p.accumulate ? dst[t + N1 * m] + v[m] : v[m];
   }
 }
 
