@@ -80,7 +80,9 @@ struct Layout {
   bool cache_ops;
   size_t cplx;  // bytes of one complex
   size_t HW;
-  size_t small, part, twH, permH, twW, permW, cx, cy, kfirst, klast, kdiag, pin, pout;
+  size_t small, part, twH, permH, twW, permW, cx, cy;
+  size_t slots, slot_bytes, dslots, dslot_bytes;
+  int nslots, ndslots;
   size_t F, X, U, field0, op, Xw, Xa;
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
@@ -133,7 +135,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     return o;
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
-  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 3 * nrw + 4 + 3 * NI + 8));
+  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 5 * nrw + 4 + 3 * NI + 8));
   L.part = take(sizeof(double) * std::max<size_t>(2 * kPartBlocks, 4 * kWinChunks * nrw));
   L.twH = take(L.cplx * H);
   L.permH = take(sizeof(int) * H);
@@ -142,12 +144,15 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.cx = take(rsz * d->nray * L.nx * d->nlam * W);
   L.cy = take(rsz * d->nray * L.ny * d->nlam * H);
   const size_t kt = (size_t)d->nlam * L.HW;
-  L.kfirst = take(L.cplx * kt * 16);
-  L.klast = take(L.cplx * kt * (16 > 8 * (size_t)d->nray ? 16 : 8 * (size_t)d->nray));
-  L.kdiag = take(L.cplx * kt * 2);
   const bool passes = d->method == 4 && d->npass > 1;
-  L.pin = take(passes ? L.cplx * kt * 16 : 0);
-  L.pout = take((passes || d->method == 4) ? L.cplx * kt * 16 : 0);
+  // k-space table slots: entry / exit / projection tables (reused across
+  // passes when they repeat) and the inter-layer diagonal tables
+  L.nslots = passes ? 6 : 3;
+  L.slot_bytes = L.cplx * kt * (16 > 8 * (size_t)d->nray ? 16 : 8 * (size_t)d->nray);
+  L.slots = take(L.slot_bytes * L.nslots);
+  L.ndslots = 2;
+  L.dslot_bytes = L.cplx * kt * 2;
+  L.dslots = take(L.dslot_bytes * L.ndslots);
   const size_t field = L.cplx * NI * 4 * L.HW;
   L.F = take(field);
   L.X = take(field);
@@ -207,7 +212,15 @@ template <typename R>
 struct Engine {
   Prof* prof = nullptr;
   int launches = 0;
-  double diag_d = std::nan("");  // thickness the inter-layer k-space table was built for
+  // k-space table cache of this call: (kind, thickness, medium) -> slot
+  struct Slot {
+    int what = -1;
+    double d = 0, e = 0;
+    int mode = 0;
+    long long used = 0;
+  };
+  Slot slot[8], dslot[2];
+  long long tick = 0;
   void mark(int kind) {
     if (prof) prof->mark(kind, st);
   }
@@ -237,7 +250,9 @@ struct Engine {
   double* wbeta() const { return yoff() + d.nray; }
   double* wphi() const { return wbeta() + (size_t)d.nray * L.nwin; }
   int* wzero() const { return (int*)(wphi() + (size_t)d.nray * L.nwin); }
-  double* epseff() const { return (double*)(wzero()) + (size_t)d.nray * L.nwin; }
+  double* wcos() const { return (double*)(wzero()) + (size_t)d.nray * L.nwin; }
+  double* wsin() const { return wcos() + (size_t)d.nray * L.nwin; }
+  double* epseff() const { return wsin() + (size_t)d.nray * L.nwin; }
   double* i0() const { return epseff() + 4; }
   double* i0f() const { return i0() + NI; }
   double* fact() const { return i0f() + NI; }
@@ -268,6 +283,37 @@ struct Engine {
     return tc;
   }
 
+  bool col_reg() const { return sizeof(R) == 4 && (d.height == 64 || d.height == 128 || d.height == 256 ||
+                                                   d.height == 512 || d.height == 1024); }
+
+  template <int N1, int N2>
+  int launch_col_reg_t(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
+    int tx = std::max(1, 256 / (C * N1));
+    if (tx > d.width) tx = d.width;
+    while (tx > 1 && (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) > 100 * 1024) tx /= 2;
+    p.tc = tx;
+    const size_t smem = (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
+    auto kern = k_layer_col_reg<R, N1, N2>;
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int threads = std::max(32, ((C * tx * N1 + 31) / 32) * 32);
+    dim3 grid((d.width + tx - 1) / tx, NI);
+    mark(PROF_COL);
+    kern<<<grid, threads, smem, st>>>(p, g, in, out);
+    mark(PROF_COL);
+    CKL("k_layer_col_reg");
+    return DTMM_OK;
+  }
+
+  int launch_col_reg(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
+    switch (d.height) {
+      case 64: return launch_col_reg_t<8, 8>(p, in, out, C);
+      case 128: return launch_col_reg_t<8, 16>(p, in, out, C);
+      case 256: return launch_col_reg_t<16, 16>(p, in, out, C);
+      case 512: return launch_col_reg_t<16, 32>(p, in, out, C);
+      default: return launch_col_reg_t<32, 32>(p, in, out, C);
+    }
+  }
+
   int launch_col(const cpx<R>* in, cpx<R>* out, int cin, int cout, int kop, const void* ktab, int ny,
                  const R* cy, bool do_fwd, bool inverse_out, double scale, size_t ktab_ray_stride = 0,
                  int j_only = -1) {
@@ -288,6 +334,7 @@ struct Engine {
     p.tw = P(L.twH);
     p.perm = A<int>(L.permH);
     const int cm = cin > cout ? cin : cout;
+    if (col_reg() && cin == cout && (kop == KOP_NONE || kop == KOP_DIAG)) return launch_col_reg(p, in, out, cin);
     p.tc = tile_cols(cm, true);
     const size_t smem = 2 * (size_t)cm * d.height * p.tc * sizeof(cpx<R>) + d.height * (sizeof(cpx<R>) + sizeof(int));
     CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -448,13 +495,36 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // (e+, e-) table of the merged half steps; rebuilt only when the thickness changes
-  int diag_table(double dd) {
-    if (dd == diag_d) return DTMM_OK;
-    int rc = launch_ktab(KT_DIAG, dd, P(L.kdiag));
-    if (rc == DTMM_OK) diag_d = dd;
-    return rc;
+  // table of kind `what` for thickness dd (medium eps_re for projections),
+  // built once per call and reused while its slot is not needed for another
+  int table(int what, double dd, const cpx<R>*& out, int proj_mode = 1, double eps_re = 0.0) {
+    const bool diag = what == KT_DIAG;
+    Slot* sl = diag ? dslot : slot;
+    const int n = diag ? L.ndslots : L.nslots;
+    int pick = 0;
+    for (int i = 0; i < n; ++i) {
+      if (sl[i].what == what && sl[i].d == dd && sl[i].e == eps_re && sl[i].mode == proj_mode) {
+        sl[i].used = ++tick;
+        out = P((diag ? L.dslots : L.slots) + (size_t)i * (diag ? L.dslot_bytes : L.slot_bytes));
+        return DTMM_OK;
+      }
+      if (sl[i].used < sl[pick].used) pick = i;
+    }
+    cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
+    int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false) : launch_ktab(what, dd, dst);
+    if (rc) return rc;
+    sl[pick].what = what;
+    sl[pick].d = dd;
+    sl[pick].e = eps_re;
+    sl[pick].mode = proj_mode;
+    sl[pick].used = ++tick;
+    out = dst;
+    return DTMM_OK;
   }
+
+  const cpx<R>* kdiag_cur = nullptr;
+  // (e+, e-) table of the merged half steps
+  int diag_table(double dd) { return table(KT_DIAG, dd, kdiag_cur); }
 
   WinParams winp() const {
     WinParams w;
@@ -489,9 +559,11 @@ struct Engine {
     p.d = dsub;
     p.wbeta = wbeta();
     p.wphi = wphi();
+    p.wcos = wcos();
+    p.wsin = wsin();
     p.nwin = L.nwin;
     p.four = d.method == 4;
-    dim3 grid((unsigned)((L.HW + 127) / 128), d.nray * L.nwin);
+    dim3 grid((unsigned)((L.HW + 127) / 128), d.nray);
     mark(PROF_OP);
     if (real_ops())
       k_voxel_op<R, true><<<grid, 128, 0, st>>>(p, g, op);
@@ -538,7 +610,7 @@ struct Engine {
       k_window_stats<<<gs, 256, 0, st>>>(w, g, A<double>(L.part));
       CKL("k_window_stats");
       k_window_final<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(A<double>(L.part), kWinChunks, wbeta(), wphi(),
-                                                                    wzero(), L.nwin * d.nray);
+                                                                    wzero(), wcos(), wsin(), L.nwin * d.nray);
       CKL("k_window_final");
       dim3 gt(8, d.nlam, d.nray);
       k_window_tables<R><<<gt, 256, 0, st>>>(w, g, A<R>(L.cx), A<R>(L.cy));
@@ -547,6 +619,8 @@ struct Engine {
       CK(cudaMemcpyAsync(wbeta(), rbeta(), sizeof(double) * d.nray, cudaMemcpyDeviceToDevice, st));
       CK(cudaMemcpyAsync(wphi(), rphi(), sizeof(double) * d.nray, cudaMemcpyDeviceToDevice, st));
       CK(cudaMemsetAsync(wzero(), 0, sizeof(int) * d.nray, st));
+      k_sincos<<<(d.nray + 127) / 128, 128, 0, st>>>(wphi(), wcos(), wsin(), d.nray);
+      CKL("k_sincos");
     }
     return DTMM_OK;
   }
@@ -577,7 +651,7 @@ struct Engine {
           if ((rc = launch_col(in, U, cin, C, kop0, ktab0, L.ny, cy, true, true, 1.0, ktab0_ray))) return rc;
         } else {
           if ((rc = diag_table(dir * ds))) return rc;
-          if ((rc = launch_col(X, U, C, C, KOP_DIAG, P(L.kdiag), 1, nullptr, true, true, 1.0))) return rc;
+          if ((rc = launch_col(X, U, C, C, KOP_DIAG, kdiag_cur, 1, nullptr, true, true, 1.0))) return rc;
         }
         if ((rc = launch_row(U, X, op, dir))) return rc;
       }
@@ -594,7 +668,7 @@ struct Engine {
           if ((rc = launch_col(in, U, cin, C, kop0, ktab0, 1, cy, true, true, 1.0, ktab0_ray, j))) return rc;
         } else {
           if ((rc = diag_table(dir * ds))) return rc;
-          if ((rc = launch_col(Xw, U, C, C, KOP_DIAG, P(L.kdiag), 1, nullptr, true, true, 1.0))) return rc;
+          if ((rc = launch_col(Xw, U, C, C, KOP_DIAG, kdiag_cur, 1, nullptr, true, true, 1.0))) return rc;
         }
         if ((rc = launch_row(U, dst, op, dir, w, s == 0, s + 1 == nst && w > 0))) return rc;
       }
@@ -634,13 +708,14 @@ struct Engine {
       int kop;
       const void* ktab;
       if (q == 0) {
-        if ((rc = launch_ktab(KT_D1, dir * ds / 2, P(L.kfirst)))) return rc;
+        const cpx<R>* t1;
+        if ((rc = table(KT_D1, dir * ds / 2, t1))) return rc;
         kop = KOP_MAT;
-        ktab = P(L.kfirst);
+        ktab = t1;
       } else {
         if ((rc = diag_table(dir * 0.5 * (dprev + ds)))) return rc;
         kop = KOP_DIAG;
-        ktab = P(L.kdiag);
+        ktab = kdiag_cur;
       }
       cpx<R>* out = nullptr;
       if ((rc = layer(cur, 4, kop, ktab, 0, out, op, dir, nst, ds))) return rc;
@@ -654,13 +729,15 @@ struct Engine {
       if (bulk) {
         // bulk[l + 1] = ifft2(D2 . X) (dtmm/transfer.py:758-764, :878-880)
         cpx<R>* slab = bulk + (size_t)(l + 1) * NI * 4 * L.HW;
-        if ((rc = launch_ktab(KT_D2, dir * ds / 2, P(L.klast)))) return rc;
-        if ((rc = launch_col(cur, slab, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+        const cpx<R>* t2;
+        if ((rc = table(KT_D2, dir * ds / 2, t2))) return rc;
+        if ((rc = launch_col(cur, slab, 4, 4, KOP_MAT, t2, 1, nullptr, true, true, 1.0 / d.height))) return rc;
         if ((rc = launch_rows(slab, 4, true, 1.0 / d.width))) return rc;
       }
     }
-    if ((rc = launch_ktab(KT_D2, dir * dprev / 2, P(L.klast)))) return rc;
-    if ((rc = launch_col(cur, U, 4, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height))) return rc;
+    const cpx<R>* t2;
+    if ((rc = table(KT_D2, dir * dprev / 2, t2))) return rc;
+    if ((rc = launch_col(cur, U, 4, 4, KOP_MAT, t2, 1, nullptr, true, true, 1.0 / d.height))) return rc;
     if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;
     CK(cudaMemcpyAsync(F, U, sizeof(cpx<R>) * (size_t)NI * 4 * L.HW, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;
@@ -712,17 +789,19 @@ struct Engine {
     const int npass = d.npass;
     // out= given: keep only its backward-propagating part (dtmm/transfer.py:674)
     if (io.out_given) {
-      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pout), -1, d.nin * d.nin, 0.0, false))) return rc;
-      if ((rc = diffract(fout, fout, P(L.pout)))) return rc;
+      const cpx<R>* pback;
+      if ((rc = table(KT_PROJ, 0.0, pback, -1, d.nin * d.nin))) return rc;
+      if ((rc = diffract(fout, fout, pback))) return rc;
     } else {
       CK(cudaMemsetAsync(fout, 0, bytes, st));
     }
     cpx<R>* field0 = nullptr;
+    const cpx<R>* pin = nullptr;
+    const cpx<R>* pout = nullptr;
     if (npass > 1) {
-      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pin), 1, d.nin * d.nin, 0.0, false))) return rc;
-      if ((rc = launch_ktab(KT_PROJ, 0.0, P(L.pout), 1, d.nout * d.nout, 0.0, false))) return rc;
+      if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
       field0 = P(L.field0);
-      if ((rc = diffract(field0, fin, P(L.pin)))) return rc;
+      if ((rc = diffract(field0, fin, pin))) return rc;
       k_total_intensity<R><<<NI, 256, 0, st>>>(field0, g, i0());
       CKL("k_total_intensity");
     }
@@ -734,13 +813,17 @@ struct Engine {
         const double sigma = d.smooth * (npass - i) / npass;
         if (i % 2 == 0) {
           if (i == 0 && (rc = axpby(F, F, nullptr, 1.0, fout, nullptr, -1.0))) return rc;
-          if (i != npass - 1 && (rc = project(F, P(L.pout), true, sigma))) return rc;
+          if (i != npass - 1) {
+            if ((rc = table(KT_PROJ, 0.0, pout, 1, d.nout * d.nout))) return rc;
+            if ((rc = project(F, pout, true, sigma))) return rc;
+          }
           if ((rc = axpby(fout, fout, nullptr, 1.0, F, nullptr, 1.0))) return rc;
           CK(cudaMemcpyAsync(F, fout, bytes, cudaMemcpyDeviceToDevice, st));
         } else {
           CK(cudaMemcpyAsync(fin, F, bytes, cudaMemcpyDeviceToDevice, st));
           if (i != npass - 1) {
-            if ((rc = project(F, P(L.pin), false, sigma))) return rc;
+            if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
+            if ((rc = project(F, pin, false, sigma))) return rc;
             k_total_intensity<R><<<NI, 256, 0, st>>>(F, g, i0f());
             CKL("k_total_intensity");
             k_ratio<<<(NI + 255) / 256, 256, 0, st>>>(i0(), i0f(), fact(), NI);
@@ -782,13 +865,14 @@ struct Engine {
       const void* ktab;
       if (q == 0) {
         // entry: transmitted part in n_in, interface n_in -> effective, half step
-        if ((rc = launch_ktab(KT_2IN, ds / 2, P(L.kfirst)))) return rc;
+        const cpx<R>* t1;
+        if ((rc = table(KT_2IN, ds / 2, t1))) return rc;
         kop = KOP_MAT;
-        ktab = P(L.kfirst);
+        ktab = t1;
       } else {
         if ((rc = diag_table(0.5 * (dprev + ds)))) return rc;
         kop = KOP_DIAG;
-        ktab = P(L.kdiag);
+        ktab = kdiag_cur;
       }
       cpx<R>* out = nullptr;
       if ((rc = layer(cur, cin, kop, ktab, 0, out, P(L.op), 1.0, nst, ds))) return rc;
@@ -801,8 +885,9 @@ struct Engine {
       dprev = ds;
     }
     // exit: half step, interface effective -> n_out, windows and E -> H
-    if ((rc = launch_ktab(KT_2OUT, dprev / 2, P(L.klast)))) return rc;
-    if ((rc = launch_col(cur, U, 2, 4, KOP_MAT, P(L.klast), 1, nullptr, true, true, 1.0 / d.height,
+    const cpx<R>* t2;
+    if ((rc = table(KT_2OUT, dprev / 2, t2))) return rc;
+    if ((rc = launch_col(cur, U, 2, 4, KOP_MAT, t2, 1, nullptr, true, true, 1.0 / d.height,
                          (size_t)d.nlam * L.HW * 8)))
       return rc;
     if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;

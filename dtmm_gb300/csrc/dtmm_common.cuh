@@ -402,4 +402,33 @@ __device__ __forceinline__ void line_fft_2step(cpx<R> (&v)[N2], cpx<R>* xch, con
   __syncwarp();
 }
 
+// line_fft_2step with the exchange buffer at a stride (element e at xch[e * xs])
+template <typename R, int N1, int N2, bool INV>
+__device__ __forceinline__ void line_fft_2step_strided(cpx<R> (&v)[N2], cpx<R>* xch, int xs, const cpx<R>* trow,
+                                                       const cpx<R>* twn, int t) {
+  RegDFT<R, N2, INV>::run(v);
+#pragma unroll
+  for (int k1 = 1; k1 < N2; ++k1) {
+    cpx<R> w = trow ? trow[k1] : twn[(t * k1) & (N1 * N2 - 1)];
+    if (INV) w.im = -w.im;
+    v[k1] = v[k1] * w;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k1 = 0; k1 < N2; ++k1) xch[(k1 * N1 + (t ^ (k1 & (N1 - 1)))) * xs] = v[k1];
+  __syncwarp();
+  constexpr int J = N2 / N1;
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    cpx<R> u[N1];
+    const int k1 = t + N1 * j;
+#pragma unroll
+    for (int sidx = 0; sidx < N1; ++sidx) u[sidx] = xch[(k1 * N1 + (sidx ^ t)) * xs];
+    RegDFT<R, N1, INV>::run(u);
+#pragma unroll
+    for (int k2 = 0; k2 < N1; ++k2) v[j + J * k2] = u[k2];
+  }
+  __syncwarp();
+}
+
 }  // namespace dtmm

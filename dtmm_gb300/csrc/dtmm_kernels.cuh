@@ -144,6 +144,8 @@ struct OpParams {
   double d;              // sub-step thickness (pixels), direction not included
   const double* wbeta;   // [ray][nwin]
   const double* wphi;
+  const double* wcos;    // cos, sin of wphi
+  const double* wsin;
   cpx<double> eps_eff;
   int nwin;
   int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
@@ -156,7 +158,7 @@ struct OpParams {
 // when every eigenvalue and the effective medium exceed beta^2 (then every
 // radicand of the solve is positive; the host proves this before selecting
 // the real path).  Same formulas as the complex path below.
-__device__ inline bool voxel_E_real(double beta, double phi, const double ev[3], double theta, double azim,
+__device__ inline bool voxel_E_real(double beta, const double ev[3], double st, double ct, double sf, double cf,
                                     double E[2][4], double al[4]) {
   if (ev[0] == ev[1] && ev[1] == ev[2]) {
     const double a = sqrt(ev[0] - beta * beta);
@@ -167,9 +169,6 @@ __device__ inline bool voxel_E_real(double beta, double phi, const double ev[3],
     E[0][3] = 0.0; E[1][3] = 0.5;
     return a == 0.0;
   }
-  double st, ct, sf, cf;
-  sincos(theta, &st, &ct);
-  sincos(azim - phi, &sf, &cf);
   const double cfst = cf * st, sfst = st * sf;
   const double eps11 = ev[0], delta = ev[2] - eps11;
   double ev02, evs, evpp, evpm;
@@ -213,48 +212,62 @@ template <typename R, bool REAL>
 __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int HW = g.H * g.W;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  const int rw = blockIdx.y;  // ray * nwin + window
+  const int ray = blockIdx.y;
   if (pix >= HW) return;
   const int y = pix / g.W, x = pix - y * g.W;
-  const double beta = p.wbeta[rw], phi = p.wphi[rw];
   const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
   const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
   const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
   if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
   const int nrec = p.four ? OP_REC : 7;
-  double sp, cp;
-  sincos(phi, &sp, &cp);
+  const size_t slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
+  // the voxel's trigonometry, shared by every window
+  double st, ct, sa, ca;
+  sincos(theta, &st, &ct);
+  sincos(azim, &sa, &ca);
   if (REAL) {
     const double* e = (const double*)p.epsv + eo;
     const double ev[3] = {e[0], e[1], e[2]};
-    const double aw = sqrt(p.eps_eff.re - beta * beta);
-    double E[2][4], al[4];
-    bool zero = voxel_E_real(beta, phi, ev, theta, azim, E, al);
-    for (int m = 0; m < 4; ++m) {
-      const double ex = E[0][m], ey = E[1][m];
-      E[0][m] = ex * cp - ey * sp;
-      E[1][m] = ex * sp + ey * cp;
+    for (int w = 0; w < p.nwin; ++w) {
+      const int rw = ray * p.nwin + w;
+      const double beta = p.wbeta[rw];
+      const double cp = p.wcos[rw], sp = p.wsin[rw];
+      // cos / sin of (azimuth - phi) by the angle-difference identities
+      const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
+      const double aw = sqrt(p.eps_eff.re - beta * beta);
+      double E[2][4], al[4];
+      bool zero = voxel_E_real(beta, ev, st, ct, sf, cf, E, al);
+      for (int m = 0; m < 4; ++m) {
+        const double ex = E[0][m], ey = E[1][m];
+        E[0][m] = ex * cp - ey * sp;
+        E[1][m] = ex * sp + ey * cp;
+      }
+      const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
+      const double detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
+      if (detf == 0.0 || (p.four && detb == 0.0)) zero = true;
+      double rec[OP_REC];
+      if (zero) {
+        for (int i = 0; i < OP_REC; ++i) rec[i] = 0.0;
+      } else {
+        rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
+        rec[4] = 1.0 / detf;
+        rec[5] = (al[0] - aw) * p.d;
+        rec[6] = (al[2] - aw) * p.d;
+        rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
+        rec[11] = p.four ? 1.0 / detb : 0.0;
+        rec[12] = (al[1] + aw) * p.d;
+        rec[13] = (al[3] + aw) * p.d;
+      }
+      R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
+      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
     }
-    const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
-    const double detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
-    if (detf == 0.0 || (p.four && detb == 0.0)) zero = true;
-    double rec[OP_REC];
-    if (zero) {
-      for (int i = 0; i < OP_REC; ++i) rec[i] = 0.0;
-    } else {
-      rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
-      rec[4] = 1.0 / detf;
-      rec[5] = (al[0] - aw) * p.d;
-      rec[6] = (al[2] - aw) * p.d;
-      rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
-      rec[11] = p.four ? 1.0 / detb : 0.0;
-      rec[12] = (al[1] + aw) * p.d;
-      rec[13] = (al[3] + aw) * p.d;
-    }
-    R* o = (R*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + (p.permW ? p.permW[x] : x);
-    for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
     return;
   }
+  for (int w = 0; w < p.nwin; ++w) {
+    const int rw = ray * p.nwin + w;
+    const double beta = p.wbeta[rw];
+    const double cp = p.wcos[rw], sp = p.wsin[rw];
+    const double cfw = ca * cp + sa * sp, sfw = sa * cp - ca * sp;
   cpx<double> ev[3];
   if (p.eps_complex) {
     const cpx<double>* e = (const cpx<double>*)p.epsv + eo;
@@ -268,7 +281,6 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     ev[2] = mk<double>(e[2], 0.0);
   }
   cpx<double> aw = csqrt_d(mk<double>(p.eps_eff.re - beta * beta, p.eps_eff.im));
-
   cpx<double> E[2][4];  // rows Ex, Ey of the four mode columns
   cpx<double> al[4];
   bool zero = false;
@@ -288,9 +300,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   } else {
     // uniaxial, optic axis rotated by (theta, azimuth - phi) (dtmm/tmm.py:157-278,
     // rotation dtmm/rotation.py:176-194 via :390)
-    double st, ct, sf, cf;
-    sincos(theta, &st, &ct);
-    sincos(azim - phi, &sf, &cf);
+    const double sf = sfw, cf = cfw;
     const double cfst = cf * st, sfst = st * sf;
     const cpx<double> eps11 = ev[0];
     const cpx<double> delta = ev[2] - eps11;
@@ -361,8 +371,9 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
     }
   }
-  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + (size_t)y * g.W + (p.permW ? p.permW[x] : x);
+  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + slot;
   for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -444,7 +455,8 @@ __global__ void k_window_stats(WinParams w, Grid g, double* part) {
     part[(((size_t)ray * w.n * w.n + win) * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = red[threadIdx.x][0];
 }
 
-__global__ void k_window_final(const double* part, int chunks, double* wbeta, double* wphi, int* wzero, int n) {
+__global__ void k_window_final(const double* part, int chunks, double* wbeta, double* wphi, int* wzero, double* wcos,
+                               double* wsin, int n) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= n) return;
   double acc[4] = {0, 0, 0, 0};
@@ -457,6 +469,7 @@ __global__ void k_window_final(const double* part, int chunks, double* wbeta, do
   }
   wbeta[idx] = sqrt(mx * mx + my * my);
   wphi[idx] = atan2(my, mx);
+  sincos(wphi[idx], wsin + idx, wcos + idx);
   wzero[idx] = acc[3] > 0 ? 0 : 1;
 }
 
@@ -492,7 +505,7 @@ enum KTab {
   KT_D1 = 0,     // 4x4 field -> Epn over d: E . P(d) . F^-1          (dtmm/matrix.py:110)
   KT_D2 = 1,     // 4x4 Epn -> field over d: F . P(d) . E^-1          (dtmm/matrix.py:121)
   KT_PROJ = 2,   // 4x4 forward projection F . diag(1,0,1,0) . F^-1   (dtmm/diffract.py:242)
-  KT_DIAG = 3,   // (e+, e-) = exp(+/- i k0 d a_k)                    (D1 . D2 of two half steps)
+  KT_DIAG = 3,   // (e+, e-) = exp(+/- i k0 d a_k), stored [lam][kx][ky] (D1 . D2 of two half steps)
   KT_2IN = 4,    // 2x4 [E(d) . t_in] . P_in[rows Ex, Ey]   (2x2 method entry)
   KT_2OUT = 5,   // 4x2 [sum_w win_w ; sum_w win_w E2H_w] . t_out . E(d)   (2x2 method exit)
 };
@@ -525,11 +538,35 @@ __device__ inline void betaphi_k(const Grid& g, double ks, int ky, int kx, doubl
   phi = atan2(yy, xx);
 }
 
+// Inverse of the isotropic field matrix in closed form: F = M . blockdiag(A, B)
+// with M the rotation of the (Ex, Ey) and (Hy, Hx) row pairs by phi,
+// A = [[1/2, 1/2], [gp/2, -gp/2]], B = [[1/2, 1/2], [-a/2, a/2]]; hence
+// F^-1 = blockdiag(A^-1, B^-1) . M^T with A^-1 = [[1, 1/gp], [1, -1/gp]],
+// B^-1 = [[1, -1/a], [1, 1/a]] (zero when a = 0, as the reference's inverse
+// of the zero matrix).
+__device__ inline void iso_inv(double phi, cpx<double> eps, cpx<double> a, cpx<double> Fi[4][4]) {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) Fi[i][j] = mk<double>(0.0, 0.0);
+  if (a.re == 0.0 && a.im == 0.0) return;
+  const cpx<double> igp = cdiv(a, eps);               // 1 / gp = a / eps
+  const cpx<double> ia = cdiv(mk<double>(1.0, 0.0), a);
+  double s, c;
+  sincos(phi, &s, &c);
+  // M^T maps (Ex, Hy, Ey, Hx) to the unrotated frame:
+  //   Ex0 = c Ex + s Ey, Ey0 = -s Ex + c Ey, Hy0 = c Hy - s Hx, Hx0 = s Hy + c Hx
+  // modes 0, 1 use (Ex0, Hy0); modes 2, 3 use (Ey0, Hx0)
+  const cpx<double> one = mk<double>(1.0, 0.0);
+  Fi[0][0] = one * c; Fi[0][2] = one * s; Fi[0][1] = igp * c; Fi[0][3] = igp * (-s);
+  Fi[1][0] = one * c; Fi[1][2] = one * s; Fi[1][1] = igp * (-c); Fi[1][3] = igp * s;
+  Fi[2][0] = one * (-s); Fi[2][2] = one * c; Fi[2][1] = ia * (-s); Fi[2][3] = ia * (-c);
+  Fi[3][0] = one * (-s); Fi[3][2] = one * c; Fi[3][1] = ia * s; Fi[3][3] = ia * c;
+}
+
 // iso eigen-data at grid point k with the betamax cut
 __device__ inline void iso_k(double beta, double phi, cpx<double> eps, double betamax, cpx<double> al[4],
                              cpx<double> F[4][4], cpx<double> Fi[4][4]) {
   iso_alphaf(beta, phi, eps, al, F);
-  inv4(F, Fi);
+  iso_inv(phi, eps, al[0], Fi);
   if (beta >= betamax) {
     for (int i = 0; i < 4; ++i) {
       al[i] = mk<double>(0.0, 0.0);
@@ -578,8 +615,10 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     const bool masked = (beta >= p.betamax) || (al[0].re == 0.0 && al[0].im == 0.0);
     cpx<double> ep = masked ? mk<double>(0.0, 0.0) : cexp_i(al[0] * (ks * p.d));
     cpx<double> em = masked ? mk<double>(0.0, 0.0) : cexp_i(al[1] * (ks * p.d));
-    tab[(size_t)t * 2 + 0] = cvt<R>(ep);
-    tab[(size_t)t * 2 + 1] = cvt<R>(em);
+    // column-major (lam, kx, ky) so that column passes read it coalesced
+    const size_t tt = ((size_t)lam * g.W + kx) * g.H + ky;
+    tab[tt * 2 + 0] = cvt<R>(ep);
+    tab[tt * 2 + 1] = cvt<R>(em);
     return;
   }
   if (p.what == KT_D1 || p.what == KT_D2 || p.what == KT_PROJ) {
@@ -775,7 +814,7 @@ __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cp
       const size_t kidx = ((size_t)lam * H + ky) * W + kx;
       cpx<R>* v = T + (size_t)ky * es + xc;
       if (p.kop == KOP_DIAG) {
-        const cpx<R>* e = (const cpx<R>*)p.ktab + kidx * 2;
+        const cpx<R>* e = (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H + ky) * 2;
         const cpx<R> ep = e[0], em = e[1];
         for (int c = 0; c < p.cin; ++c) v[c * TC] = v[c * TC] * (((c & 1) == 0 || p.cin == 2) ? ep : em);
       } else {
@@ -818,6 +857,76 @@ __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cp
       Uj[(((size_t)img * C + c) * H + y) * W + x] = buf[((size_t)ys * CM + c) * TC + xc] * sc;
     }
     __syncthreads();
+  }
+}
+
+// Column pass for power-of-two heights H = N1 * N2 (float bulk) with the
+// k-space operator KOP_NONE or KOP_DIAG: a tile of TX columns x C components
+// of one image is loaded with coalesced row reads into shared memory (odd row
+// stride), every (component, column) line is transformed in registers by a
+// group of N1 lanes that uses its own tile column as exchange buffer, the
+// diagonal operator and the window weights act in registers, and results go
+// back through the tile to coalesced row writes.
+template <typename R, int N1, int N2>
+__global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
+                                                         cpx<R>* __restrict__ U) {
+  constexpr int H = N1 * N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int W = g.W, TX = p.tc, C = p.cin;
+  const int RS = C * TX + 1;                       // tile row stride (odd)
+  cpx<R>* tile = (cpx<R>*)smem_raw;                // [H][RS]
+  cpx<R>* tw = tile + (size_t)H * RS;              // [H] exp(-2 pi i e / H)
+  const int img = blockIdx.y;
+  const int x0 = blockIdx.x * TX;
+  const int lam = img_lam(g, img), ray = img_ray(g, img);
+  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  // a half-warp covers one tile row (C x TX contiguous slots): conflict-free
+  const int CT = C * TX;
+  const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;
+  const int lcc = lc / TX, lxc = lc - lcc * TX;
+  const bool lin = (int)threadIdx.x < ystep * CT && x0 + lxc < W;
+  const cpx<R>* xsrc = X + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+  if (lin)
+    for (int y = threadIdx.x / CT; y < H; y += ystep) tile[y * RS + lc] = xsrc[(size_t)y * W];
+  __syncthreads();
+  const int l = threadIdx.x / N1, t = threadIdx.x % N1;
+  const int nlines = C * TX;
+  const bool active = l < nlines;
+  const int c = l / TX, xc = l - c * TX;
+  const int kx = x0 + xc;
+  cpx<R>* col = tile + l;  // line element e at col[e * RS]
+  constexpr bool TWREG = false;  // twiddles from the shared table: fewer registers, more resident blocks
+  cpx<R> trow[1];
+  cpx<R> v[N2];
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < N2; ++m) v[m] = col[(t + N1 * m) * RS];
+  }
+  __syncwarp();
+  if (active && p.do_fwd) line_fft_2step_strided<R, N1, N2, false>(v, col, RS, TWREG ? trow : nullptr, tw, t);
+  if (active && p.kop == KOP_DIAG && kx < W) {
+    const cpx<R>* e = (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H) * 2;
+    const bool fwd = ((c & 1) == 0) || C == 2;
+#pragma unroll
+    for (int m = 0; m < N2; ++m) v[m] = v[m] * e[(t + N1 * m) * 2 + (fwd ? 0 : 1)];
+  }
+  const R sc = (R)p.out_scale;
+  for (int jj = 0; jj < p.ny; ++jj) {
+    const int j = p.j_only >= 0 ? p.j_only : jj;
+    __syncthreads();  // the previous window's stores have read the tile
+    if (active) {
+      cpx<R> u[N2];
+      const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
+#pragma unroll
+      for (int m = 0; m < N2; ++m) u[m] = cyj ? v[m] * cyj[t + N1 * m] : v[m];
+      if (p.inverse_out) line_fft_2step_strided<R, N1, N2, true>(u, col, RS, TWREG ? trow : nullptr, tw, t);
+#pragma unroll
+      for (int m = 0; m < N2; ++m) col[(t + N1 * m) * RS] = u[m] * sc;
+    }
+    __syncthreads();
+    cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+    if (lin)
+      for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tile[y * RS + lc];
   }
 }
 
@@ -1319,6 +1428,12 @@ __global__ void k_eps_final(const double* part, int blocks, long long n, double*
   }
   out[0] = sr / (double)n;
   out[1] = si / (double)n;
+}
+
+// cos, sin of the beam azimuths (one window per ray)
+__global__ void k_sincos(const double* phi, double* c, double* sn, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) sincos(phi[i], sn + i, c + i);
 }
 
 }  // namespace dtmm

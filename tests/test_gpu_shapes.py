@@ -20,6 +20,12 @@ SHAPES = [
     ((4, 1024), dict(method="4x4", diffraction=1, beta=0.0, phi=0.0)),
     ((30, 42), dict(method="4x4", diffraction=3, npass=1, beta=0.0, phi=0.0)),
     ((27, 35), dict(method="2x2", diffraction=5, reflection=0, beta=0.0, phi=0.0)),
+    # tall grids: the register-transform column pass
+    ((128, 16), dict(method="4x4", diffraction=3, npass=2, beta=0.0, phi=0.0)),
+    ((256, 8), dict(method="4x4", diffraction=1, npass=1, beta=0.1, phi=0.5)),
+    ((512, 6), dict(method="2x2", diffraction=3, reflection=0, beta=0.0, phi=0.0)),
+    ((1024, 4), dict(method="4x4", diffraction=1, npass=3, beta=0.0, phi=0.0)),
+    ((256, 256), dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)),
 ]
 
 
