@@ -273,7 +273,7 @@ def main():
     achieved = BYTES_PER_UPDATE * upd_per_row_launch / row_avg_s / 1e9
     peak, peak_kind = measured_peaks()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": ncu_traffic(), "kernel": "k_layer_row<float>", "peak_source": peak_kind,
+                "traffic": ncu_traffic(), "kernel": "k_layer_row_reg<float,4,real,16,16>", "peak_source": peak_kind,
                 "kernel_share": row_ms / total_ms,
                 "device_ms_per_step": {"layer_row": row_ms / args.steps, "layer_col": col_ms / args.steps,
                                        "voxel_op": op_ms / args.steps}}

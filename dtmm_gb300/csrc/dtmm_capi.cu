@@ -135,7 +135,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     return o;
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
-  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 5 * nrw + 4 + 3 * NI + 8));
+  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 6 * nrw + 4 + 3 * NI + 8));
   L.part = take(sizeof(double) * std::max<size_t>(2 * kPartBlocks, 4 * kWinChunks * nrw));
   L.twH = take(L.cplx * H);
   L.permH = take(sizeof(int) * H);
@@ -252,7 +252,8 @@ struct Engine {
   int* wzero() const { return (int*)(wphi() + (size_t)d.nray * L.nwin); }
   double* wcos() const { return (double*)(wzero()) + (size_t)d.nray * L.nwin; }
   double* wsin() const { return wcos() + (size_t)d.nray * L.nwin; }
-  double* epseff() const { return wsin() + (size_t)d.nray * L.nwin; }
+  double* waw() const { return wsin() + (size_t)d.nray * L.nwin; }
+  double* epseff() const { return waw() + (size_t)d.nray * L.nwin; }
   double* i0() const { return epseff() + 4; }
   double* i0f() const { return i0() + NI; }
   double* fact() const { return i0f() + NI; }
@@ -561,6 +562,7 @@ struct Engine {
     p.wphi = wphi();
     p.wcos = wcos();
     p.wsin = wsin();
+    p.waw = waw();
     p.nwin = L.nwin;
     p.four = d.method == 4;
     dim3 grid((unsigned)((L.HW + 127) / 128), d.nray);
@@ -585,7 +587,14 @@ struct Engine {
       h[d.nlam + 2 * d.nray + r] = fold(d.beta[r] * std::cos(d.phi[r]), dwin);
       h[d.nlam + 3 * d.nray + r] = fold(d.beta[r] * std::sin(d.phi[r]), dwin);
     }
-    CK(cudaMemcpyAsync(ks(), h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, st));
+    for (size_t o = 0; o < h.size(); o += 64) {
+      Scalars64 sc;
+      sc.n = (int)std::min<size_t>(64, h.size() - o);
+      sc.off = (int)o;
+      for (int i = 0; i < sc.n; ++i) sc.v[i] = h[o + i];
+      k_set_scalars<<<1, 64, 0, st>>>(sc, ks());
+      CKL("k_set_scalars");
+    }
     // FFT tables
     k_fft_tables<R><<<(d.height + 255) / 256, 256, 0, st>>>(pH, P(L.twH), A<int>(L.permH));
     CKL("k_fft_tables");
@@ -622,6 +631,8 @@ struct Engine {
       k_sincos<<<(d.nray + 127) / 128, 128, 0, st>>>(wphi(), wcos(), wsin(), d.nray);
       CKL("k_sincos");
     }
+    k_window_aw<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(wbeta(), epseff(), waw(), L.nwin * d.nray);
+    CKL("k_window_aw");
     return DTMM_OK;
   }
 

@@ -146,6 +146,7 @@ struct OpParams {
   const double* wphi;
   const double* wcos;    // cos, sin of wphi
   const double* wsin;
+  const double* waw;     // real path: sqrt(eps_eff - wbeta^2)
   cpx<double> eps_eff;
   int nwin;
   int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
@@ -191,9 +192,9 @@ __device__ inline bool voxel_E_real(double beta, const double ev[3], double st, 
     const double gama = beta * cf;
     const double v = delta * (gama * 2.0 * st * ct);
     const double w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
-    const double u2 = u * 2.0;
-    const double sq = sqrt(v * v - u * w * 4.0) / u2;
-    const double vh = v / u2;
+    const double iu2 = 0.5 / u;
+    const double sq = sqrt(v * v - u * w * 4.0) * iu2;
+    const double vh = v * iu2;
     evpp = sq - vh;
     evpm = -vh - sq;
     const double ctbeta = ct * beta;
@@ -234,7 +235,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       const double cp = p.wcos[rw], sp = p.wsin[rw];
       // cos / sin of (azimuth - phi) by the angle-difference identities
       const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
-      const double aw = sqrt(p.eps_eff.re - beta * beta);
+      const double aw = p.waw[rw];
       double E[2][4], al[4];
       bool zero = voxel_E_real(beta, ev, st, ct, sf, cf, E, al);
       for (int m = 0; m < 4; ++m) {
@@ -624,7 +625,11 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   if (p.what == KT_D1 || p.what == KT_D2 || p.what == KT_PROJ) {
     iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
     cpx<double> ph[4];
-    for (int m = 0; m < 4; ++m) ph[m] = cexp_i(al[m] * (ks * p.d));
+    if (p.what != KT_PROJ) {
+      // alpha = (a, -a, a, -a): two exponentials
+      ph[0] = ph[2] = cexp_i(al[0] * (ks * p.d));
+      ph[1] = ph[3] = cexp_i(al[1] * (ks * p.d));
+    }
     cpx<double> M[4][4];
     if (p.what == KT_PROJ) {
       const int m0 = p.proj_mode > 0 ? 0 : 1;
@@ -645,8 +650,22 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
             M[i][j] = s;
           }
       } else {
+        // E of an isotropic medium: each direction's 2x2 block is the rotation
+        // of diag(1/2, 1/2) by phi, so E^-1 = 2 x (rotation by -phi) per block
+        // (zero where the eigen-data are cut)
         cpx<double> Ei[4][4];
-        inv4(E, Ei);
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) Ei[i][j] = mk<double>(0.0, 0.0);
+        const bool cut = (beta >= p.betamax) || (al[0].re == 0.0 && al[0].im == 0.0);
+        if (!cut) {
+          double sp, cp;
+          sincos(phi, &sp, &cp);
+          // Epn rows/cols: forward block on (0, 2), backward block on (1, 3)
+          Ei[0][0] = mk<double>(2 * cp, 0); Ei[0][2] = mk<double>(2 * sp, 0);
+          Ei[2][0] = mk<double>(-2 * sp, 0); Ei[2][2] = mk<double>(2 * cp, 0);
+          Ei[1][1] = mk<double>(2 * cp, 0); Ei[1][3] = mk<double>(2 * sp, 0);
+          Ei[3][1] = mk<double>(-2 * sp, 0); Ei[3][3] = mk<double>(2 * cp, 0);
+        }
         for (int i = 0; i < 4; ++i)
           for (int j = 0; j < 4; ++j) {
             cpx<double> s = mk<double>(0.0, 0.0);
@@ -1428,6 +1447,23 @@ __global__ void k_eps_final(const double* part, int blocks, long long n, double*
   }
   out[0] = sr / (double)n;
   out[1] = si / (double)n;
+}
+
+// sqrt(eps_eff - beta_w^2) per window (real path)
+__global__ void k_window_aw(const double* wbeta, const double* eps_eff, double* aw, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) aw[i] = sqrt(eps_eff[0] - wbeta[i] * wbeta[i]);
+}
+
+// Per-call host scalars travel as kernel arguments (captured by value in a
+// CUDA graph), 64 at a time.
+struct Scalars64 {
+  double v[64];
+  int n, off;
+};
+__global__ void k_set_scalars(Scalars64 s, double* dst) {
+  const int i = threadIdx.x;
+  if (i < s.n) dst[s.off + i] = s.v[i];
 }
 
 // cos, sin of the beam azimuths (one window per ray)
