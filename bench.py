@@ -176,6 +176,185 @@ def run_reference(args, rank):
     }))
 
 
+# ---------------------------------------------------------------------------
+# batching: 48 heterogeneous instances as one CUDA graph
+# ---------------------------------------------------------------------------
+def field_bytes_per_update(nlam, nfields, cbytes=8):
+    return 2 * 4 * cbytes + 48.0 / (nlam * nfields)
+
+
+def time_replays(fn, steps, dev):
+    stream = torch_mod().cuda.current_stream(dev)
+    times = []
+    for _ in range(steps):
+        e0 = torch_mod().cuda.Event(enable_timing=True)
+        e1 = torch_mod().cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return times
+
+
+def torch_mod():
+    import torch
+
+    return torch
+
+
+def run_batch(args, dev, ninst=48, seed=0):
+    import torch
+
+    from dtmm_gb300 import samples
+    from dtmm_gb300.batch import TransferBatch, build_instance
+    from dtmm_gb300.tune import Autotuner
+
+    specs = samples.instance_specs(ninst, seed=seed)
+    tuner = Autotuner()
+    t0 = time.perf_counter()
+    inst = [build_instance(s, precision="mixed", device=dev, tuner=tuner) for s in specs]
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    batch = TransferBatch(nstreams=args.streams, device=dev)
+    for (plan, fin, fout), s in zip(inst, specs):
+        batch.add(plan, fin, fout, tag=s["index"])
+    # one eager pass, counting the library's kernel launches per instance
+    launches = 0
+    for plan, fin, fout in inst:
+        launches += plan.run(fin, fout, timed=True).total_launches
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch.capture(warm=False)
+    capture_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        batch.replay()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index or 0) as clk:
+        times = time_replays(batch.replay, args.steps, dev)
+    clocks = clk.summary()
+    ms = float(np.mean(times))
+    upd = batch.updates
+    value = upd / (ms / 1e3)
+    alg_bytes = sum(p.updates * field_bytes_per_update(len(s["wavelengths"]), 14) for (p, _, _), s in zip(inst, specs))
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    in_bytes = sum(fin.numel() * fin.element_size() for _, fin, _ in inst)
+    # one graph launch vs the same plans launched one after another on one stream
+    def serial():
+        for plan, fin, fout in inst:
+            plan.run(fin, fout)
+    serial()
+    torch.cuda.synchronize()
+    serial_ms = float(np.mean(time_replays(serial, 1, dev)))
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic",
+        "config": {"workload": "batch: %d seeded 4x4 transfer_field instances (diffraction 1, npass 1) as one CUDA "
+                               "graph; grids log-uniform 64-512 rounded to 7-smooth multiples of 16, 20-120 "
+                               "layers, 1-9 wavelengths in 400-700 nm, 7 rays (beta 0, +-0.1, +-0.2 at phi 0; "
+                               "+-0.1 at phi 90 deg), x+y polarisation, twisted nematic (no 1.5, ne 1.7, amp 0.2), "
+                               "complex64 bulk + FP64 eigen-solve, autotuned launch shapes" % ninst,
+                   "instances": ninst, "streams": args.streams,
+                   "l2": "inputs larger than L2 (%.1f GB of input fields)" % (in_bytes / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "whole graph (algorithmic bytes / graph time)",
+                     "peak_source": peak_kind},
+        "gpu_launches": launches * args.steps, "clocks": clocks, "updates_per_step": upd,
+        "graph": {"build_s": build_s, "capture_s": capture_s, "serial_one_stream_ms": serial_ms,
+                  "graph_speedup_vs_serial": serial_ms / ms,
+                  "tuned": {k: v for k, v in sorted(tuner.cache.items())}},
+    }
+    # end to end: host inputs in pinned memory, copies in, one graph launch, copies out
+    if not args.no_e2e:
+        hin = [torch.empty(fin.shape, dtype=fin.dtype).pin_memory() for _, fin, _ in inst]
+        hout = [torch.empty(fout.shape, dtype=fout.dtype).pin_memory() for _, _, fout in inst]
+        for h, (_, fin, _) in zip(hin, inst):
+            h.copy_(fin)
+        def e2e_step():
+            for h, (_, fin, _) in zip(hin, inst):
+                fin.copy_(h, non_blocking=True)
+            batch.replay()
+            for h, (_, _, fout) in zip(hout, inst):
+                h.copy_(fout, non_blocking=True)
+        e2e_step()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            e2e_step()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        e2e_s = float(np.median(ts))
+        result["e2e"] = {"value": upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": in_bytes,
+                         "d2h_bytes_per_step": in_bytes, "ms_per_step": e2e_s * 1e3}
+    # complex128 comparison on a seeded subset (the full batch in complex128 takes minutes)
+    if not args.no_c128:
+        sub = specs[:args.c128_subset]
+        res = {}
+        outs = {}
+        for prec in ("mixed", "double"):
+            ii = [build_instance(s, precision=prec, device=dev) for s in sub]
+            b = TransferBatch(nstreams=args.streams, device=dev)
+            for plan, fin, fout in ii:
+                b.add(plan, fin, fout)
+            b.capture()
+            b.replay()
+            torch.cuda.synchronize()
+            t = float(np.mean(time_replays(b.replay, 1, dev)))
+            res[prec] = b.updates / (t / 1e3)
+            outs[prec] = [fout.to(torch.complex128).cpu().numpy() for _, _, fout in ii]
+            del ii, b
+            torch.cuda.empty_cache()
+        err = max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(outs["mixed"], outs["double"]))
+        result["c128"] = {"subset": len(sub), "value": res["double"], "mixed_value": res["mixed"],
+                          "mixed_speedup": res["mixed"] / res["double"], "mixed_rel_l2_vs_c128_max": err}
+    return result
+
+
+# ---------------------------------------------------------------------------
+# serving: Poisson stream of requests, continuous batching under an HBM budget
+# ---------------------------------------------------------------------------
+def run_serve(args, dev):
+    import torch
+
+    from dtmm_gb300 import samples
+    from dtmm_gb300.serve import TransferServer, poisson_trace, pretune
+    from dtmm_gb300.tune import Autotuner
+
+    specs = samples.instance_specs(args.requests, seed=1, rays=None)
+    tuner = Autotuner()
+    t0 = time.perf_counter()
+    pretune(tuner, specs, device=dev)
+    tune_s = time.perf_counter() - t0
+    # warm-up: a few requests through the same server (allocator pools, lazy loading)
+    srv = TransferServer(precision="mixed", hbm_budget=args.hbm_budget, max_active=args.slots, tuner=tuner,
+                         device=dev)
+    srv.serve(poisson_trace(specs[:min(16, len(specs))], args.rate, seed=2))
+    torch.cuda.synchronize()
+    trace = poisson_trace(specs, args.rate, seed=3)
+    with ClockSampler(dev.index or 0) as clk:
+        st = srv.serve(trace)
+    clocks = clk.summary()
+    offered = sum(samples.spec_updates(s) for s in specs) / max(st["arrival_span_s"], 1e-9)
+    return {
+        "metric": METRIC, "value": st["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": st["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64", "data": "synthetic",
+        "config": {"workload": "serving: Poisson stream of %d 4x4 transfer_field requests at %g req/s (diffraction 1,"
+                               " npass 1, normal incidence, x+y polarisation), grids log-uniform 64-512, 20-120 "
+                               "layers, 1-9 wavelengths, twisted nematic built on the device, complex64 bulk + FP64 "
+                               "eigen-solve; continuous batching over %d stream slots, %g GB HBM admission budget"
+                               % (args.requests, args.rate, args.slots, args.hbm_budget / 1e9),
+                   "requests": args.requests, "rate": args.rate, "slots": args.slots,
+                   "hbm_budget_bytes": args.hbm_budget},
+        "latency_ms": st["latency_ms"], "queue_ms": st["queue_ms"], "requests_per_s": st["requests_per_s"],
+        "offered_updates_per_s": offered, "peak_active": st["peak_active"],
+        "peak_budget_bytes": st["peak_budget_bytes"], "pretune_s": tune_s, "clocks": clocks,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,6 +366,15 @@ def main():
     ap.add_argument("--no-c128", action="store_true", help="skip the complex128 comparison run")
     ap.add_argument("--layers", type=int, default=NLAYERS, help="layers (profiling runs use fewer; same kernels)")
     ap.add_argument("--npass", type=int, default=OPTS["npass"])
+    ap.add_argument("--workload", default="precision", choices=["precision", "batch", "serve"],
+                    help="precision: 256x256 4x4 npass 3 (default); batch: 48 instances in one graph; "
+                         "serve: Poisson request stream")
+    ap.add_argument("--streams", type=int, default=8, help="batch: streams in the graph")
+    ap.add_argument("--c128-subset", type=int, default=8, help="batch: instances of the complex128 comparison")
+    ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the trace")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrival rate (req/s)")
+    ap.add_argument("--slots", type=int, default=16, help="serve: concurrent request slots")
+    ap.add_argument("--hbm-budget", type=float, default=150e9, help="serve: admission budget (bytes)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -212,6 +400,21 @@ def main():
             dist.barrier()
 
     dev = torch.device("cuda", local)
+    if args.workload in ("batch", "serve"):
+        # independent replicas: every rank runs the whole workload on its own GPU
+        res = run_batch(args, dev) if args.workload == "batch" else run_serve(args, dev)
+        barrier()
+        if dist is not None:
+            t = torch.tensor([res["ms_per_step"]], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            res["ms_per_step"] = float(t.item())
+            res["value"] = res["value"] * world
+            res["n_gpus"] = world
+        if rank == 0:
+            print(json.dumps(res))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     fd, od = inputs(args.layers)
     OPTS["npass"] = args.npass
     if args.layers != NLAYERS or args.npass != 3:

@@ -20,7 +20,8 @@ PRECISION_MIXED = 0
 PRECISION_DOUBLE = 1
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
-               "dtmm_transfer_timed", "dtmm_transfer_noalloc")
+               "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field")
+ABI_VERSION = 2
 STATIC_SCRATCH_BYTES = 64 << 20
 
 
@@ -53,6 +54,9 @@ class TransferDesc(ctypes.Structure):
         ("phi", ctypes.POINTER(ctypes.c_double)),
         ("op_cache_bytes", ctypes.c_size_t),
         ("real_path", ctypes.c_int),
+        ("row_group", ctypes.c_int),
+        ("col_tile", ctypes.c_int),
+        ("fft_schedule", ctypes.c_int),
     ]
 
 
@@ -113,7 +117,10 @@ def load(build_if_missing=True):
                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.POINTER(KernelTimes)]
     lib.dtmm_transfer_noalloc.restype = ctypes.c_int
     lib.dtmm_transfer_noalloc.argtypes = [ctypes.POINTER(TransferDesc), ctypes.POINTER(TransferIO), ctypes.c_void_p]
-    if lib.dtmm_abi_version() != 1:
+    lib.dtmm_planewave_field.restype = ctypes.c_int
+    lib.dtmm_planewave_field.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    if lib.dtmm_abi_version() != ABI_VERSION:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib
     return lib

@@ -53,17 +53,20 @@ int fail(int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(DTMM_ECUDA, "launch %s: %s", what, cudaGetErrorString(e_)); \
   } while (0)
 
-bool make_plan(int n, FFTPlan& p) {
+// radix schedule of one line transform: radix-8 (when `rad8`) or radix-4
+// passes first, then 2, 3, 5, 7
+bool make_plan(int n, FFTPlan& p, bool rad8 = false) {
   p.n = n;
   p.nr = 0;
   int m = n;
+  while (rad8 && m % 8 == 0 && p.nr < 14) { p.r[p.nr++] = 8; m /= 8; }
   while (m % 4 == 0 && p.nr < 14) { p.r[p.nr++] = 4; m /= 4; }
   while (m % 2 == 0 && p.nr < 14) { p.r[p.nr++] = 2; m /= 2; }
   const int odd[3] = {3, 5, 7};
   for (int q : odd)
     while (m % q == 0 && p.nr < 14) { p.r[p.nr++] = q; m /= q; }
   p.rbits = 0;
-  for (int i = 0; i < p.nr; ++i) p.rbits |= (unsigned long long)p.r[i] << (3 * i);
+  for (int i = 0; i < p.nr; ++i) p.rbits |= (unsigned long long)(p.r[i] & 7) << (3 * i);
   return m == 1 && n >= 1;
 }
 
@@ -112,6 +115,8 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (!make_plan(d->height, p) || !make_plan(d->width, p))
     return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", d->height, d->width);
   if (d->betamax <= 0) return fail(DTMM_EINVAL, "betamax must be > 0");
+  if (d->row_group < 0 || d->col_tile < 0 || d->fft_schedule < 0 || d->fft_schedule > 3)
+    return fail(DTMM_EINVAL, "invalid tuning fields");
   return DTMM_OK;
 }
 
@@ -280,16 +285,19 @@ struct Engine {
     const size_t per = (size_t)cm * d.height * sizeof(cpx<R>) * (two ? 2 : 1);
     int tc = 1;
     while (tc < 16 && per * (tc * 2) <= 72 * 1024) tc *= 2;
+    if (d.col_tile > 0 && per * d.col_tile <= 200 * 1024) tc = d.col_tile;
     if (tc > d.width) tc = d.width;
     return tc;
   }
 
-  bool col_reg() const { return sizeof(R) == 4 && (d.height == 64 || d.height == 128 || d.height == 256 ||
-                                                   d.height == 512 || d.height == 1024); }
+  bool col_reg() const { return sizeof(R) == 4 && d.fft_schedule <= 1 &&
+                                (d.height == 64 || d.height == 128 || d.height == 256 || d.height == 512 ||
+                                 d.height == 1024); }
 
   template <int N1, int N2>
   int launch_col_reg_t(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
     int tx = std::max(1, 256 / (C * N1));
+    if (d.col_tile > 0 && d.col_tile * C * N1 <= 512) tx = d.col_tile;
     if (tx > d.width) tx = d.width;
     while (tx > 1 && (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) > 100 * 1024) tx /= 2;
     p.tc = tx;
@@ -306,12 +314,16 @@ struct Engine {
   }
 
   int launch_col_reg(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
-    switch (d.height) {
-      case 64: return launch_col_reg_t<8, 8>(p, in, out, C);
-      case 128: return launch_col_reg_t<8, 16>(p, in, out, C);
-      case 256: return launch_col_reg_t<16, 16>(p, in, out, C);
-      case 512: return launch_col_reg_t<16, 32>(p, in, out, C);
-      default: return launch_col_reg_t<32, 32>(p, in, out, C);
+    if constexpr (sizeof(R) != 4) {
+      return fail(DTMM_ENOTSUP, "register column transform is complex64 only");
+    } else {
+      switch (d.height) {
+        case 64: return launch_col_reg_t<8, 8>(p, in, out, C);
+        case 128: return launch_col_reg_t<8, 16>(p, in, out, C);
+        case 256: return launch_col_reg_t<16, 16>(p, in, out, C);
+        case 512: return launch_col_reg_t<16, 32>(p, in, out, C);
+        default: return launch_col_reg_t<32, 32>(p, in, out, C);
+      }
     }
   }
 
@@ -356,10 +368,7 @@ struct Engine {
     int G = 16 / (d.npol * L.C);
     if (G < 1) G = 1;
     if ((size_t)G * per > 100 * 1024) G = (int)((100 * 1024) / per);
-    if (const char* e = getenv("DTMM_ROW_GROUP")) {  // tuning override
-      const int v = atoi(e);
-      if (v >= 1 && (size_t)v * per <= 200 * 1024) G = v;
-    }
+    if (d.row_group > 0 && (size_t)d.row_group * per <= 200 * 1024) G = d.row_group;
     if (G < 1) G = 1;
     if (G > d.nlam) G = d.nlam;
     return G;
@@ -385,8 +394,8 @@ struct Engine {
   }
 
   // register-transform row kernel: float bulk, W = N1 * N2 in {64 ... 1024}
-  bool row_reg() const { return sizeof(R) == 4 && (d.width == 64 || d.width == 128 || d.width == 256 ||
-                                                   d.width == 512 || d.width == 1024); }
+  bool row_reg() const { return sizeof(R) == 4 && d.fft_schedule <= 1 &&
+                                (d.width == 64 || d.width == 128 || d.width == 256 || d.width == 512 || d.width == 1024); }
 
   int row_group_reg() const {
     const int perG = d.npol * L.C;  // lines per wavelength
@@ -394,10 +403,7 @@ struct Engine {
     const size_t line_bytes = 2 * (size_t)d.width * sizeof(cpx<R>);
     // about 8 lines per block measured best (256-pixel rows, 4x4, 2 polarisations)
     int G = std::max(1, 8 / perG);
-    if (const char* e = getenv("DTMM_ROW_GROUP")) {
-      const int v = atoi(e);
-      if (v >= 1) G = v;
-    }
+    if (d.row_group > 0) G = d.row_group;
     while (G > 1 && ((size_t)G * perG * line_bytes > 110 * 1024 || G * perG * n1 > 512)) --G;
     return std::min(G, d.nlam);
   }
@@ -423,12 +429,16 @@ struct Engine {
 
   template <int C, bool REAL>
   int launch_row_reg(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
-    switch (d.width) {
-      case 64: return launch_row_reg_t<C, REAL, 8, 8>(p, Ub, Xb);
-      case 128: return launch_row_reg_t<C, REAL, 8, 16>(p, Ub, Xb);
-      case 256: return launch_row_reg_t<C, REAL, 16, 16>(p, Ub, Xb);
-      case 512: return launch_row_reg_t<C, REAL, 16, 32>(p, Ub, Xb);
-      default: return launch_row_reg_t<C, REAL, 32, 32>(p, Ub, Xb);
+    if constexpr (sizeof(R) != 4) {
+      return fail(DTMM_ENOTSUP, "register row transform is complex64 only");
+    } else {
+      switch (d.width) {
+        case 64: return launch_row_reg_t<C, REAL, 8, 8>(p, Ub, Xb);
+        case 128: return launch_row_reg_t<C, REAL, 8, 16>(p, Ub, Xb);
+        case 256: return launch_row_reg_t<C, REAL, 16, 16>(p, Ub, Xb);
+        case 512: return launch_row_reg_t<C, REAL, 16, 32>(p, Ub, Xb);
+        default: return launch_row_reg_t<C, REAL, 32, 32>(p, Ub, Xb);
+      }
     }
   }
 
@@ -919,8 +929,8 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   e.g.nlam = d->nlam;
   e.g.npol = d->npol;
   e.g.nray = d->nray;
-  make_plan(d->height, e.pH);
-  make_plan(d->width, e.pW);
+  make_plan(d->height, e.pH, d->fft_schedule == 3);
+  make_plan(d->width, e.pW, d->fft_schedule == 3);
   int rc = e.setup();
   if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();
   if (launches) *launches = e.launches;
@@ -972,7 +982,7 @@ int static_scratch(void** out) {
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 1; }
+int dtmm_abi_version(void) { return 2; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 
@@ -1016,6 +1026,27 @@ int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* 
     times->voxel_op_launches = (int)prof.ev[PROF_OP].size() / 2;
     times->total_launches = launches;
   }
+  return DTMM_OK;
+}
+
+int dtmm_planewave_field(int height, int width, int nimg, const void* coef, const int* my, const int* mx,
+                         int precision, void* field, void* stream) {
+  g_err.clear();
+  if (height < 1 || width < 1) return fail(DTMM_EINVAL, "grid must be at least 1x1");
+  if (nimg < 1 || nimg > 65535) return fail(DTMM_EINVAL, "image count %d outside 1..65535", nimg);
+  if (!coef || !my || !mx || !field) return fail(DTMM_EINVAL, "null pointer");
+  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "invalid precision");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long hw = (long long)height * width;
+  const int bx = (int)std::min<long long>((hw + 255) / 256, 1216);
+  dim3 grid(bx, nimg);
+  if (precision == DTMM_PRECISION_DOUBLE)
+    k_planewave<double><<<grid, 256, 0, st>>>((cpx<double>*)field, (const cpx<double>*)coef, my, mx, height, width);
+  else
+    k_planewave<float><<<grid, 256, 0, st>>>((cpx<float>*)field, (const cpx<double>*)coef, my, mx, height, width);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_planewave: %s", cudaGetErrorString(e));
   return DTMM_OK;
 }
 

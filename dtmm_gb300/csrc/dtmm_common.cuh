@@ -108,10 +108,13 @@ struct FFTPlan {
   int n;
   int nr;
   int r[14];
-  unsigned long long rbits;  // r[i] in bits [3i, 3i+3): read without dynamic indexing
+  unsigned long long rbits;  // r[i] & 7 in bits [3i, 3i+3) (0 codes radix 8): read without dynamic indexing
 };
 
-__device__ __forceinline__ int plan_radix(const FFTPlan& p, int i) { return (int)((p.rbits >> (3 * i)) & 7ull); }
+__device__ __forceinline__ int plan_radix(const FFTPlan& p, int i) {
+  const int c = (int)((p.rbits >> (3 * i)) & 7ull);
+  return c ? c : 8;
+}
 
 template <typename R, bool INV>
 __device__ __forceinline__ cpx<R> twid(const cpx<R>* tw, int idx) {
@@ -135,6 +138,27 @@ __device__ __forceinline__ void dft_reg(cpx<R>* v, const cpx<R>* tw, int n) {
     v[2] = s02 - s13;
     v[1] = d02 + jd;
     v[3] = d02 - jd;
+  } else if constexpr (RAD == 8) {
+    // two 4-point DFTs (even / odd samples) joined by W8^k = exp(-+ i pi k / 4)
+    cpx<R> e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    dft_reg<R, 4, INV>(e, tw, n);
+    dft_reg<R, 4, INV>(o, tw, n);
+    const R h = (R)0.70710678118654752440084436210485;  // 1 / sqrt(2)
+    const cpx<R> a = o[1], b = o[2], c = o[3];
+    if (INV) {
+      o[1] = mk<R>(h * (a.re - a.im), h * (a.re + a.im));
+      o[2] = mk<R>(-b.im, b.re);
+      o[3] = mk<R>(-h * (c.re + c.im), h * (c.re - c.im));
+    } else {
+      o[1] = mk<R>(h * (a.re + a.im), h * (a.im - a.re));
+      o[2] = mk<R>(b.im, -b.re);
+      o[3] = mk<R>(h * (c.im - c.re), -h * (c.re + c.im));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = e[k] + o[k];
+      v[k + 4] = e[k] - o[k];
+    }
   } else {
     cpx<R> in[RAD];
 #pragma unroll
@@ -182,6 +206,14 @@ __device__ __forceinline__ void butterfly(cpx<R>* line, int es, int b, int ns, i
   }
 }
 
+// radix-8 butterflies as a call: its 8 live complex values then cost
+// registers only inside the call, not in every kernel that can take the pass
+template <typename R, bool INV, bool DIT>
+__device__ __noinline__ void butterfly8(cpx<R>* line, int es, int b, int ns, int nsh, int tstep, const cpx<R>* tw,
+                                        int n) {
+  butterfly<R, 8, INV, DIT>(line, es, b, ns, nsh, tstep, tw, n);
+}
+
 __device__ __forceinline__ int log2_or_neg(int x) { return (x & (x - 1)) == 0 ? __ffs(x) - 1 : -1; }
 
 // One pass over `nlines` lines by a group of `nthr` threads (thread index `tid`).
@@ -204,6 +236,7 @@ __device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, 
         case 2: butterfly<R, 2, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
         case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
         case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        case 8: butterfly8<R, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
         default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       }
     }
@@ -224,6 +257,7 @@ __device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, 
       case 2: butterfly<R, 2, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      case 8: butterfly8<R, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
     }
   }

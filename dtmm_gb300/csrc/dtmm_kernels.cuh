@@ -1472,4 +1472,30 @@ __global__ void k_sincos(const double* phi, double* c, double* sn, int n) {
   if (i < n) sincos(phi[i], sn + i, c + i);
 }
 
+// ---------------------------------------------------------------------------
+// Plane-wave input fields (the grid of illumination_data, dtmm/field.py:586):
+// out[i][c][y][x] = coef[i][c] * exp(2 pi i (my[i] y / H + mx[i] x / W)).
+// The phase numerator (my y mod H) W + (mx x mod W) H is exact integer
+// arithmetic, so sincospi sees an argument in [0, 4).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_planewave(cpx<R>* __restrict__ out, const cpx<double>* __restrict__ coef,
+                            const int* __restrict__ my, const int* __restrict__ mx, int H, int W) {
+  const int img = blockIdx.y;
+  const long long HW = (long long)H * W;
+  const long long iy = ((long long)my[img] % H + H) % H, ix = ((long long)mx[img] % W + W) % W;
+  cpx<double> c[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c[k] = coef[(size_t)img * 4 + k];
+  cpx<R>* o = out + (size_t)img * 4 * HW;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < HW; t += (long long)gridDim.x * blockDim.x) {
+    const long long y = t / W, x = t - y * W;
+    const long long num = ((iy * y) % H) * W + ((ix * x) % W) * H;
+    double s, co;
+    sincospi(2.0 * (double)num / (double)HW, &s, &co);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      o[k * HW + t] = mk<R>((R)(c[k].re * co - c[k].im * s), (R)(c[k].re * s + c[k].im * co));
+  }
+}
 }  // namespace dtmm

@@ -1,10 +1,19 @@
-"""Input field data: plane-wave illumination (host-side, numpy).
+"""Input field data: plane-wave illumination.
 
 ``illumination_data`` mirrors ``dtmm.field.illumination_data``
 (dtmm/field.py:586-713) for the eigenmode case (``window=None``), which is
-how the reference builds the inputs of ``transfer_field``.  It prepares the
-caller's input tuple ``(field, wavelengths, pixelsize)`` on the host before
-any transfer starts; it is not part of the transfer path.
+how the reference builds the inputs of ``transfer_field``.
+
+The reference builds each plane wave on the full grid, replaces it by the
+FFT-grid mode of largest power (``wave2eigenwave``, dtmm/wave.py:432), then
+filters the field through the diffraction operator of the cover medium in
+k-space (``diffracted_field``, dtmm/diffract.py:301) and rescales its total
+intensity.  A field made of one FFT mode stays one mode under those steps, so
+every image of the result is ``coef[c] * exp(2 pi i (my * y / H + mx * x / W))``:
+``illumination_modes`` computes the per-image 4-vectors ``coef`` and the mode
+indices (my, mx) with O(H + W) work per wave, and the grid is filled either on
+the host (``illumination_data``) or on the device by the library's
+``dtmm_planewave_field`` kernel (``illumination_device``).
 """
 from __future__ import annotations
 
@@ -70,18 +79,122 @@ def _intensity(field):
         f[..., 2, :, :].real * f[..., 3, :, :].real + f[..., 2, :, :].imag * f[..., 3, :, :].imag)
 
 
-def _nearest_eigenwave(waves):
-    """Replace each 2D wave by the FFT-grid plane wave of largest power (dtmm/wave.py:432)."""
-    shape = waves.shape
-    flat = waves.reshape((-1,) + shape[-2:])
-    out = np.empty(flat.shape, np.complex128)
-    for i, w in enumerate(flat):
-        s = np.abs(np.fft.fft2(w)) ** 2
-        ii, jj = np.unravel_index(np.argmax(s), s.shape)
-        f = np.zeros(s.shape, np.complex128)
-        f[ii, jj] = s.sum() ** 0.5
-        out[i] = np.fft.ifft2(f)
-    return out.reshape(shape)
+def _peak_bins(k, n):
+    """FFT bin of largest power of exp(i k a), a = -n//2+1 ... n//2 (one axis of wave2eigenwave)."""
+    a = np.arange(-n // 2 + 1.0, n // 2 + 1.0)
+    w = np.exp(1j * np.asarray(k, np.float64)[..., None] * a)
+    return np.argmax(np.abs(np.fft.fft(w, axis=-1)) ** 2, axis=-1)
+
+
+def _intensity_vec(c):
+    return (c[..., 0].real * c[..., 1].real + c[..., 0].imag * c[..., 1].imag) - (
+        c[..., 2].real * c[..., 3].real + c[..., 2].imag * c[..., 3].imag)
+
+
+def illumination_modes(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, intensity=1.0, n=None,
+                       focus=0.0, backdir=False, jones=None, diffraction=True, betamax=BETAMAX):
+    """Per-image 4-vectors and FFT modes of the plane-wave illumination.
+
+    Returns ``(coef, my, mx)``: ``coef`` complex128 of shape
+    ``([nrays,] [2,] nwavelengths, 4)`` and integer mode indices ``my``,
+    ``mx`` of shape ``([nrays,] [2,] nwavelengths)``, such that image ``i``
+    of ``illumination_data(...)[0]`` is
+    ``coef[i, c] * exp(2 pi i (my[i] * y / H + mx[i] * x / W))``.
+    """
+    n = N_COVER if n is None else n
+    h, w = shape
+    wavelengths = np.asarray(wavelengths)
+    ks = 2 * np.pi / wavelengths * pixelsize
+    if ks.ndim != 1:
+        raise ValueError("Wavelengths should be 1D array")
+    if jones is None:
+        intensity = intensity / 2.0
+    _beta = np.asarray(beta, np.float64)
+    _phi = np.asarray(phi, np.float64)
+    if _beta.ndim > 1 or _phi.ndim > 1 or _beta.ndim != _phi.ndim:
+        raise NotImplementedError("illumination_modes: beta and phi must both be scalars or 1D ray arrays")
+    multi = _beta.ndim == 1
+    nrays = len(_beta) if multi else 1
+    b = _beta[:, None] if multi else _beta
+    p = _phi[:, None] if multi else _phi
+    # mode indices per (ray, wavelength): the plane wave of wave.py:376 with
+    # x along columns and y along rows, reduced to its strongest FFT bin
+    kx = ks * b * np.cos(p)
+    ky = ks * b * np.sin(p)
+    mx = _peak_bins(kx, w)
+    my = _peak_bins(ky, h)
+    # 4-vector of the eigenmode amplitude (field.py:586 with window=None)
+    fm = _iso_fmat(_beta, _phi, n * n)  # (rays, 4, 4) or (4, 4)
+
+    def one(pol):
+        pol = np.asarray(pol, np.complex128)
+        pol = pol / np.sqrt(pol[0] * np.conj(pol[0]) + pol[1] * np.conj(pol[1]))
+        c, s = np.cos(-_phi), np.sin(-_phi)
+        jv0 = c * pol[0] - s * pol[1]
+        jv1 = s * pol[0] + c * pol[1]
+        a = np.zeros(np.shape(jv0) + (4,), np.complex128)
+        if backdir:
+            a[..., 1] = jv0
+            a[..., 3] = jv1
+        else:
+            a[..., 0] = jv0
+            a[..., 2] = jv1
+        v = np.einsum("...ij,...j->...i", fm, a)  # (rays, 4) or (4,)
+        return np.broadcast_to(v[..., None, :], v.shape[:-1] + (len(ks), 4))
+
+    if jones is None:
+        coef = np.stack([one((1, 0)), one((0, 1))], axis=-3)
+    else:
+        coef = np.array(one(jones))
+    myb = my[..., None, :] if jones is None else my
+    mxb = mx[..., None, :] if jones is None else mx
+    myb, mxb = np.broadcast_to(myb, coef.shape[:-1]), np.broadcast_to(mxb, coef.shape[:-1])
+    inten = np.asarray(intensity, np.float64)
+    if inten.ndim == 1 and multi:
+        inten = inten.reshape((nrays,) + (1,) * (coef.ndim - 2))
+    elif inten.ndim != 0:
+        raise NotImplementedError("illumination_modes: intensity must be a scalar or one value per ray")
+    norm = np.broadcast_to((inten / nrays) ** 0.5, coef.shape[:-1]).astype(np.float64)
+    if diffraction:
+        # diffracted_field with d = -focus (diffract.py:301, :125) at the mode's own k
+        kabs = np.abs(ks)
+        lam_axis = np.arange(len(ks))
+        lam = np.broadcast_to(lam_axis, coef.shape[:-1])
+        fx = np.fft.fftfreq(w)[mxb]
+        fy = np.fft.fftfreq(h)[myb]
+        beta_k = (2 * np.pi / kabs[lam]) * np.sqrt(fx ** 2 + fy ** 2)
+        phi_k = np.arctan2(fy, fx)
+        F = _iso_fmat(beta_k, phi_k, n * n)
+        a = np.sqrt(n * n - beta_k ** 2 + 0j)
+        alpha = np.stack([a, -a, a, -a], axis=-1)
+        cut = beta_k >= betamax
+        F[cut] = 0.0
+        Fi = _inv4(F)
+        alpha[cut] = 0.0
+        ph = np.exp(1j * (ks[lam] * (-focus))[..., None] * alpha)
+        if backdir:
+            ph[..., ::2] = 0.0
+        else:
+            ph[..., 1::2] = 0.0
+        D = np.matmul(F * ph[..., None, :], Fi)
+        c2 = np.einsum("...ij,...j->...i", D, coef)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ratio = (_intensity_vec(coef) / _intensity_vec(c2)) ** 0.5
+        coef = c2
+        norm = norm * ratio
+    coef = coef * norm[..., None]
+    return coef, np.ascontiguousarray(myb, np.int32), np.ascontiguousarray(mxb, np.int32)
+
+
+def planewave_grid(shape, my, mx):
+    """exp(2 pi i (my * y / H + mx * x / W)) on the (H, W) grid (exact phase reduction)."""
+    h, w = shape
+    y = np.arange(h)
+    x = np.arange(w)
+    my = np.asarray(my)[..., None, None]
+    mx = np.asarray(mx)[..., None, None]
+    num = ((my * y[:, None]) % h) * w + ((mx * x[None, :]) % w) * h
+    return np.exp(2j * np.pi * (num / float(h * w)))
 
 
 def illumination_data(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, intensity=1.0, n=None,
@@ -90,88 +203,50 @@ def illumination_data(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, inte
     """Forward (or backward) plane-wave illumination ``(field, wavelengths, pixelsize)``.
 
     Field shape: ``([nrays,] [2,] nwavelengths, 4, H, W)``; the polarisation
-    axis is present when ``jones is None``.
+    axis is present when ``jones is None``.  Built on the host.
     """
     if window is not None or eigenmodes is False:
         raise NotImplementedError("illumination_data: only window=None (eigenmode) input is supported")
-    n = N_COVER if n is None else n
-    wavelengths = np.asarray(wavelengths)
-    ks = 2 * np.pi / wavelengths * pixelsize
-    if ks.ndim != 1:
-        raise ValueError("Wavelengths should be 1D array")
-    if jones is None:
-        intensity = intensity / 2.0
-    mode = -1 if backdir else +1
-    _beta = np.asarray(beta, np.float64)
-    _phi = np.asarray(phi, np.float64)
-    _int = np.asarray(intensity, np.float64)
-    nrays = len(_beta) if _beta.ndim > 0 else 1
-    b = _beta[:, None] if _beta.ndim == 1 else _beta
-    p = _phi[:, None] if _phi.ndim == 1 else _phi
-    # plane waves (dtmm/wave.py:376), normalised to the corner pixel
-    k = ks[..., None, None]
-    bb = np.asarray(b)[..., None, None]
-    pp = np.asarray(p)[..., None, None]
-    ay, ax = (np.arange(-l // 2 + 1.0, l // 2 + 1.0) for l in shape)
-    xx, yy = np.meshgrid(ax, ay, indexing="xy")
-    waves = np.exp(1j * ((k * bb * np.cos(pp)) * xx + (k * bb * np.sin(pp)) * yy))
-    waves = waves / waves[..., 0, 0][..., None, None]
-    waves = _nearest_eigenwave(waves)
-    b = _beta[:, None, None, None] if _beta.ndim == 1 else _beta[..., None, None]
-    p = _phi[:, None, None, None] if _phi.ndim == 1 else _phi[..., None, None]
-    intensity = _int[..., None, None, None, None]
-    fmat = _iso_fmat(b, p, n * n)
+    coef, my, mx = illumination_modes(shape, wavelengths, pixelsize, beta, phi, intensity, n, focus, backdir, jones,
+                                      diffraction, betamax)
+    field = coef[..., :, None, None] * planewave_grid(shape, my, mx)[..., None, :, :]
+    return field, np.asarray(wavelengths), pixelsize
 
-    def one(pol):
-        pol = np.asarray(pol, np.complex128)
-        pol = pol / np.sqrt(pol[0] * np.conj(pol[0]) + pol[1] * np.conj(pol[1]))
-        c, s = np.cos(-p), np.sin(-p)
-        jv0 = c * pol[0] - s * pol[1]
-        jv1 = s * pol[0] + c * pol[1]
-        amp = np.broadcast_arrays(jv0, waves)
-        a = np.zeros(np.broadcast_shapes(np.shape(jv0), waves.shape) + (4,), np.complex128)
-        if mode == +1:
-            a[..., 0] = jv0
-            a[..., 2] = jv1
-        else:
-            a[..., 1] = jv0
-            a[..., 3] = jv1
-        a = a * amp[1][..., None]
-        fv = np.einsum("...ij,...j->...i", fmat, a)
-        return np.moveaxis(fv, -1, -3)
 
-    if jones is None:
-        f1, f2 = one((1, 0)), one((0, 1))
-        sh = list(f1.shape)
-        sh.insert(-4, 2)
-        field = np.empty(sh, np.complex128)
-        field[..., 0, :, :, :, :] = f1
-        field[..., 1, :, :, :, :] = f2
-    else:
-        field = one(jones).copy()
-    i1 = _intensity(field)
-    norm = np.ones_like(i1)
-    norm[:, ...] = (intensity / nrays) ** 0.5
-    if diffraction:
-        # diffracted_field with d = -focus, mode "t"/"r" (dtmm/diffract.py:301, :125)
-        beta_k, phi_k = _fftfreq_grid(shape, ks)
-        F = _iso_fmat(beta_k, phi_k, n * n)
-        a = np.sqrt(n * n - beta_k ** 2 + 0j)
-        alpha = np.stack([a, -a, a, -a], axis=-1)
-        F[beta_k >= betamax] = 0.0
-        Fi = _inv4(F)
-        alpha[beta_k >= betamax] = 0.0
-        ph = np.exp(1j * (ks * (-focus))[:, None, None, None] * alpha)
-        if mode == +1:
-            ph[..., 1::2] = 0.0
-        else:
-            ph[..., ::2] = 0.0
-        D = np.matmul(F * ph[..., None, :], Fi)
-        ff = np.fft.fft2(field)
-        ff = np.einsum("...hwij,...jhw->...ihw", D, ff)
-        field = np.fft.ifft2(ff)
-        i2 = _intensity(field)
-        ratio = (i1.sum((-2, -1)) / i2.sum((-2, -1))) ** 0.5
-        norm = norm * ratio[..., None, None]
-    field = field * norm[..., None, :, :]
-    return field, wavelengths, pixelsize
+def illumination_device(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, intensity=1.0, n=None,
+                        focus=0.0, backdir=False, jones=None, diffraction=True, betamax=BETAMAX,
+                        precision="double", device=None, out=None, stream=None):
+    """``illumination_data`` with the grid filled on the device.
+
+    Returns a device tensor of the field (complex128 for ``precision="double"``,
+    complex64 for "mixed"), written by the ``dtmm_planewave_field`` kernel;
+    ``out`` may supply the destination tensor.
+    """
+    import ctypes
+
+    import torch
+
+    from . import _lib
+
+    coef, my, mx = illumination_modes(shape, wavelengths, pixelsize, beta, phi, intensity, n, focus, backdir, jones,
+                                      diffraction, betamax)
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    dtype = torch.complex128 if precision == "double" else torch.complex64
+    fshape = coef.shape[:-1] + (4,) + tuple(shape)
+    if out is None:
+        out = torch.empty(fshape, dtype=dtype, device=dev)
+    elif tuple(out.shape) != fshape or out.dtype != dtype or not out.is_contiguous():
+        raise ValueError("out must be a contiguous %s tensor of shape %s" % (dtype, fshape))
+    nimg = int(np.prod(coef.shape[:-1]))
+    c = torch.from_numpy(np.ascontiguousarray(coef.reshape(nimg, 4))).to(dev)
+    iy = torch.from_numpy(my.reshape(nimg)).to(dev)
+    ix = torch.from_numpy(mx.reshape(nimg)).to(dev)
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    lib = _lib.load()
+    _lib.check(lib.dtmm_planewave_field(int(shape[0]), int(shape[1]), nimg, ctypes.c_void_p(c.data_ptr()),
+                                        ctypes.c_void_p(iy.data_ptr()), ctypes.c_void_p(ix.data_ptr()),
+                                        _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED,
+                                        ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream)))
+    out._dtmm_keep = (c, iy, ix)  # the uploads stay alive until the kernel has read them
+    return out

@@ -20,12 +20,10 @@ from __future__ import annotations
 import numpy as np
 
 
-def smooth_field(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0):
-    """(H, W) sum of ``nmodes`` random cosine modes, bounded by ``amplitude``."""
+def _smooth_modes(shape, nmodes, kmax, seed):
     h, w = shape
     rng = np.random.Generator(np.random.PCG64(seed))
-    y, x = np.meshgrid(np.arange(h, dtype=np.float64), np.arange(w, dtype=np.float64), indexing="ij")
-    out = np.zeros((h, w), np.float64)
+    modes = []
     for _ in range(nmodes):
         while True:
             kx, ky = rng.integers(-kmax, kmax + 1, size=2)
@@ -34,7 +32,30 @@ def smooth_field(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0):
         cx = np.round(kx * max(w, 64) / 64.0)
         cy = np.round(ky * max(h, 64) / 64.0)
         ph = rng.uniform(0.0, 2 * np.pi)
+        modes.append((float(cx), float(cy), float(ph)))
+    return modes
+
+
+def smooth_field(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0):
+    """(H, W) sum of ``nmodes`` random cosine modes, bounded by ``amplitude``."""
+    h, w = shape
+    y, x = np.meshgrid(np.arange(h, dtype=np.float64), np.arange(w, dtype=np.float64), indexing="ij")
+    out = np.zeros((h, w), np.float64)
+    for cx, cy, ph in _smooth_modes(shape, nmodes, kmax, seed):
         out += np.cos(2 * np.pi * (cx * x / w + cy * y / h) + ph)
+    return out * (amplitude / nmodes)
+
+
+def smooth_field_device(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0, device=None):
+    """``smooth_field`` evaluated on the device (same modes; cosines to FP64 rounding)."""
+    import torch
+
+    h, w = shape
+    y = torch.arange(h, dtype=torch.float64, device=device)[:, None]
+    x = torch.arange(w, dtype=torch.float64, device=device)[None, :]
+    out = torch.zeros((h, w), dtype=torch.float64, device=device)
+    for cx, cy, ph in _smooth_modes(shape, nmodes, kmax, seed):
+        out += torch.cos(2 * np.pi * (cx * x / w + cy * y / h) + ph)
     return out * (amplitude / nmodes)
 
 
@@ -77,3 +98,101 @@ def inplane_nematic(shape, nlayers, no=1.5, ne=1.6, amplitude=np.pi / 2, nmodes=
     epsv = np.broadcast_to(np.asarray((no * no, no * no, ne * ne), np.float64), (nlayers, h, w, 3))
     d = np.full((nlayers,), float(thickness))
     return d, epsv, epsa
+
+
+def twisted_nematic_device(shape, nlayers, no=1.5, ne=1.7, twist=np.pi / 2, tilt=0.3, amplitude=0.2,
+                           nmodes=8, kmax=4, thickness=1.0, seed=0, device=None, host_modes=True):
+    """``twisted_nematic`` built on the device as a ``DeviceMaterial``.
+
+    With ``host_modes`` the (H, W) perturbation fields come from the host
+    (``smooth_field``) and the (L, H, W, 3) angle array is filled on the
+    device with the same operation order as the host generator, so both give
+    identical values.  Without it the perturbations are evaluated on the
+    device too (``smooth_field_device``): no host work that grows with the
+    grid, values equal to the host ones to FP64 rounding.
+    """
+    import torch
+
+    from .transfer import DeviceMaterial
+
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    h, w = shape
+    if host_modes:
+        dphi = torch.from_numpy(smooth_field(shape, nmodes, kmax, amplitude, seed=seed)).to(dev)
+        dtilt = torch.from_numpy(smooth_field(shape, nmodes, kmax, amplitude, seed=seed + 7919)).to(dev)
+    else:
+        dphi = smooth_field_device(shape, nmodes, kmax, amplitude, seed=seed, device=dev)
+        dtilt = smooth_field_device(shape, nmodes, kmax, amplitude, seed=seed + 7919, device=dev)
+    z = torch.arange(nlayers, dtype=torch.float64, device=dev)
+    epsa = torch.empty((nlayers, h, w, 3), dtype=torch.float64, device=dev)
+    epsa[..., 0] = 0.0
+    epsa[..., 1] = (np.pi / 2 - (dtilt + tilt))[None]
+    epsa[..., 2] = (z * twist / nlayers)[:, None, None] + dphi[None]
+    epsv = torch.tensor((no * no, no * no, ne * ne), dtype=torch.float64, device=dev)
+    return DeviceMaterial(np.full((nlayers,), float(thickness)), epsv, epsa, shape,
+                          eps_min=min(no * no, ne * ne), uniaxial=True)
+
+
+# ---------------------------------------------------------------------------
+# batch / serving workloads: many heterogeneous 4x4 instances
+# ---------------------------------------------------------------------------
+def _is_7smooth(n):
+    for q in (2, 3, 5, 7):
+        while n % q == 0:
+            n //= q
+    return n == 1
+
+
+# grid sides the engine's transforms factor (2, 3, 5, 7), multiples of 16
+FFT_SIDES = tuple(n for n in range(64, 513, 16) if _is_7smooth(n))
+
+# seven incidence rays: beta in {0, +-0.1, +-0.2} along phi = 0, and +-0.1
+# along phi = 90 degrees; a negative beta is the ray (|beta|, phi + pi)
+BATCH_RAYS = ((0.0, 0.0), (0.1, 0.0), (-0.1, 0.0), (0.2, 0.0), (-0.2, 0.0), (0.1, np.pi / 2), (-0.1, np.pi / 2))
+
+
+def fft_side(x, sides=FFT_SIDES):
+    """The supported side nearest to ``x`` on a log scale."""
+    s = np.asarray(sides, np.float64)
+    return int(s[np.argmin(np.abs(np.log(s) - np.log(float(x))))])
+
+
+def ray_directions(rays=BATCH_RAYS):
+    """(beta, phi) arrays with negative beta mapped to (|beta|, phi + pi)."""
+    b = np.asarray([r[0] for r in rays], np.float64)
+    p = np.asarray([r[1] for r in rays], np.float64)
+    return np.abs(b), np.where(b < 0, p + np.pi, p)
+
+
+def instance_specs(n, seed=0, sides=(64, 512), layers=(20, 120), nwavelengths=(1, 9), band=(400.0, 700.0),
+                   rays=BATCH_RAYS, pixelsize=100.0):
+    """Seeded specs of ``n`` heterogeneous 4x4 transfers.
+
+    Grid side log-uniform in ``sides`` (rounded to ``FFT_SIDES``), layer count
+    uniform in ``layers``, wavelength count uniform in ``nwavelengths`` spread
+    evenly over ``band`` (its centre for one), the given rays (``None`` for a
+    single normal-incidence ray), and the twisted-nematic director of
+    ``twisted_nematic`` with a per-instance seed.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lo, hi = np.log(sides[0]), np.log(sides[1])
+    out = []
+    for i in range(n):
+        side = fft_side(np.exp(rng.uniform(lo, hi)))
+        nl = int(rng.integers(layers[0], layers[1] + 1))
+        nw = int(rng.integers(nwavelengths[0], nwavelengths[1] + 1))
+        wl = np.linspace(band[0], band[1], nw) if nw > 1 else np.asarray([0.5 * (band[0] + band[1])])
+        if rays is None:
+            beta, phi = 0.0, 0.0
+        else:
+            beta, phi = ray_directions(rays)
+        out.append(dict(index=i, shape=(side, side), nlayers=nl, wavelengths=wl, pixelsize=float(pixelsize),
+                        beta=beta, phi=phi, seed=int(seed) * 100003 + i))
+    return out
+
+
+def spec_updates(spec, npol=2):
+    """voxel x wavelength updates of one spec (one pass, all fields)."""
+    nray = 1 if np.ndim(spec["beta"]) == 0 else len(spec["beta"])
+    h, w = spec["shape"]
+    return h * w * spec["nlayers"] * len(spec["wavelengths"]) * nray * npol

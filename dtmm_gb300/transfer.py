@@ -190,6 +190,45 @@ class _Material:
         self.nlayers = L
 
 
+class DeviceMaterial:
+    """Optical block already resident on the device.
+
+    ``thickness`` is a host sequence of L layer thicknesses; ``epsv`` and
+    ``epsa`` are device tensors (float64, or complex128 for absorbing
+    ``epsv``) broadcastable to ``(L, H, W, 3)`` -- expanded axes cost no
+    memory and reach the engine as zero strides.  Used by callers that keep
+    director and eps state on the GPU between transfers.
+    """
+
+    def __init__(self, thickness, epsv, epsa, shape, eps_min=None, uniaxial=None):
+        """``eps_min`` (smallest real eps) and ``uniaxial=True`` may be given
+        by a caller that knows them, which skips the device reductions (and
+        their host synchronisation) that would otherwise establish them."""
+        import torch
+
+        self.thickness = np.asarray(thickness, np.float64).reshape(-1)
+        L = len(self.thickness)
+        full = (L,) + tuple(shape) + (3,)
+        ev = epsv.expand(full)
+        ea = epsa.expand(full)
+        if ev.dtype not in (torch.float64, torch.complex128) or ea.dtype != torch.float64:
+            raise ValueError("epsv must be float64 or complex128 and epsa float64")
+        if ev.stride(3) != 1 or ea.stride(3) != 1:
+            raise ValueError("the last (component) axis of epsv and epsa must be contiguous")
+        self.epsv, self.epsa = ev, ea
+        self.ev_strides = tuple(int(x) for x in ev.stride()[:3])
+        self.ea_strides = tuple(int(x) for x in ea.stride()[:3])
+        self.eps_complex = bool(ev.is_complex())
+        if not uniaxial and not bool(torch.all(epsv[..., 0] == epsv[..., 1])):
+            raise NotImplementedError(
+                "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
+        if self.eps_complex:
+            self.eps_min = None
+        else:
+            self.eps_min = float(eps_min) if eps_min is not None else float(epsv.min())
+        self.nlayers = L
+
+
 class DevicePlan:
     """One resolved transfer bound to the device: descriptor, material and
     workspace, reusable for many input fields of the same shape.
@@ -200,7 +239,7 @@ class DevicePlan:
     """
 
     def __init__(self, field_shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
-                 nstep, betamax, nin, nout, smooth, precision, device):
+                 nstep, betamax, nin, nout, smooth, precision, device, tuning=None):
         import torch
 
         self.lib = _lib.load()
@@ -245,12 +284,31 @@ class DevicePlan:
         bmax = max(float(betamax), float(np.max(np.abs(k["beta"]))))
         d.real_path = int(mat.eps_min is not None and mat.eps_min > bmax * bmax)
         self.desc = d
+        self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
         if self.nbytes == 0:
             msg = _lib.last_error()
             raise (NotImplementedError if ("supported" in msg or "factor" in msg or "above" in msg) else ValueError)(msg)
         self.workspace = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
         self.updates = int(np.prod(field_shape[:-3])) * int(h) * int(w) * int(k["nst"].sum()) * int(npass)
+
+    TUNABLES = ("fft_schedule", "row_group", "col_tile")
+
+    def set_tuning(self, fft_schedule=0, row_group=0, col_tile=0):
+        """Launch shapes and line-transform schedule (0 = the engine's own choice).
+
+        ``row_group``/``col_tile`` change only how work is split into blocks
+        (results are bit-identical); ``fft_schedule`` 1/2/3 selects the
+        register two-step transform, radix-4-first or radix-8-first shared
+        memory passes (results agree to rounding).
+        """
+        self.desc.fft_schedule = int(fft_schedule)
+        self.desc.row_group = int(row_group)
+        self.desc.col_tile = int(col_tile)
+
+    @property
+    def tuning(self):
+        return {k: int(getattr(self.desc, k)) for k in self.TUNABLES}
 
     def run(self, field_in, field_out, bulk=None, out_given=False, timed=False, stream=None):
         import torch
@@ -272,10 +330,42 @@ class DevicePlan:
         return None
 
 
+def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffraction=1, npass=1, nstep=1,
+                    precision="mixed"):
+    """Device workspace of one transfer of these sizes (no allocation, no GPU needed)."""
+    lib = _lib.load()
+    d = _lib.TransferDesc()
+    d.height, d.width = int(shape[0]), int(shape[1])
+    d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
+    d.method = 4 if method == "4x4" else 2
+    d.diffraction, d.npass = int(diffraction), int(npass)
+    d.reflection = 1 if method == "4x4" else 0
+    d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
+    d.betamax, d.nin, d.nout, d.smooth = BETAMAX, N_COVER, N_COVER, SMOOTH
+    th = np.ones(int(nlayers))
+    ns = np.full(int(nlayers), int(nstep), np.int32)
+    arr = np.zeros(max(int(nlam), int(nray)))
+    d.nlayers = int(nlayers)
+    d.thickness = th.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.nstep = ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    d.ks = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.beta = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.phi = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    d.epsv = d.epsa = 1  # sizes only: never dereferenced by the size query
+    n = int(lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
+    if n == 0:
+        raise ValueError(_lib.last_error())
+    return n
+
+
 def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, phi=0.0, nin=None, nout=None,
                   npass=None, nstep=1, diffraction=None, reflection=None, method=None, betamax=None, smooth=SMOOTH,
-                  precision=None, device=None):
-    """Resolve options like transfer_field and bind a DevicePlan (explicit beta, phi)."""
+                  precision=None, device=None, tuning=None):
+    """Resolve options like transfer_field and bind a DevicePlan (explicit beta, phi).
+
+    ``optical_data`` is the reference's list with one optical block, or a
+    ``DeviceMaterial`` already on the device.
+    """
     torch = _require_cuda()
     nin = get_default_config_option("nin", nin)
     nout = get_default_config_option("nout", nout)
@@ -291,16 +381,21 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
             reflection = 1
     _check_path(method, reflection, npass, diffraction, DTMM_NORM_FFT)
     shape = tuple(field_shape[-2:])
-    od = validate_optical_data(optical_data, shape)
-    if len(od) != 1:
-        raise NotImplementedError("optical data with more than one block is outside the GPU engine")
     dev = device or torch.device("cuda", torch.cuda.current_device())
+    if isinstance(optical_data, DeviceMaterial):
+        mat = optical_data
+    else:
+        od = validate_optical_data(optical_data, shape)
+        if len(od) != 1:
+            raise NotImplementedError("optical data with more than one block is outside the GPU engine")
+        mat = _Material(od[0], shape, dev)
     beta = np.asarray(beta, np.float64)
     nray = 1 if beta.ndim == 0 else len(beta)
     nlam = field_shape[-4]
     npol = int(np.prod(field_shape[:-3])) // (nray * nlam)
-    return DevicePlan(field_shape, _Material(od[0], shape, dev), k0(wavelengths, pixelsize), beta, phi, nray, npol,
-                      nlam, method, diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, dev)
+    return DevicePlan(field_shape, mat, k0(wavelengths, pixelsize), beta, phi, nray, npol,
+                      nlam, method, diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, dev,
+                      tuning)
 
 
 def _check_path(method, reflection, npass, diffraction, norm):
@@ -507,4 +602,5 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     return res, wavelengths, pixelsize
 
 
-__all__ = ["transfer_field", "plan_transfer", "DevicePlan", "set_precision", "DTMM_NORM_FFT", "DTMM_NORM_REF"]
+__all__ = ["transfer_field", "plan_transfer", "DevicePlan", "DeviceMaterial", "set_precision", "DTMM_NORM_FFT",
+           "DTMM_NORM_REF"]

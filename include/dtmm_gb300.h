@@ -71,6 +71,14 @@ typedef struct dtmm_transfer_desc {
      eigen-solve is then positive and the engine uses real FP64 arithmetic and
      half-size operator records.  Ignored for complex eps. */
   int real_path;
+  /* tuning (0 = built-in choice; results do not depend on row_group and
+     col_tile): wavelengths per row block, columns per column block, and the
+     line transform schedule: 1 = two-step register transform where it
+     applies (power-of-two sides 64..1024, complex64), 2 = shared-memory
+     mixed radix with radix-4 passes first, 3 = the same with radix-8 first */
+  int row_group;
+  int col_tile;
+  int fft_schedule;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -98,7 +106,7 @@ typedef struct dtmm_kernel_times {
   int total_launches;      /* every kernel launched by the call                                          */
 } dtmm_kernel_times;
 
-/* ABI version of this header (1). */
+/* ABI version of this header (2: tuning fields in dtmm_transfer_desc, dtmm_planewave_field). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */
@@ -148,6 +156,21 @@ int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* 
      leftovers.
    - Calls no cudaMalloc, cudaFree or allocating library routine. */
 int dtmm_transfer_noalloc(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* stream);
+
+/* Plane-wave input fields on the device: for every image i < nimg and
+   component c < 4,
+     field[i][c][y][x] = coef[i][c] * exp(2 pi i (my[i] y / height + mx[i] x / width))
+   with the phase reduced exactly (integer arithmetic) before one FP64
+   sincospi.  coef: device complex128 [nimg][4]; my, mx: device int [nimg]
+   (taken modulo height / width); field: device complex64 (precision MIXED)
+   or complex128 (DOUBLE) [nimg][4][height][width].  This is the grid-filling
+   part of the reference's illumination_data (dtmm/field.py:586-713) for
+   eigenmode input, whose waves are single FFT-grid modes (wave2eigenwave,
+   dtmm/wave.py:432) and stay so through its diffraction filter
+   (dtmm/diffract.py:301); the per-image vectors and modes come from the
+   host (dtmm_gb300.illumination.illumination_modes). */
+int dtmm_planewave_field(int height, int width, int nimg, const void* coef, const int* my, const int* mx,
+                         int precision, void* field, void* stream);
 
 #ifdef __cplusplus
 }

@@ -122,3 +122,23 @@ def build_inputs(case, illumination_data):
     illum = dict(case["illum"])
     field_data = illumination_data(case["shape"], case["wavelengths"], pixelsize=case["pixelsize"], **illum)
     return field_data, build_optical_data(case)
+
+
+# illumination_data cases (dtmm/field.py:586): the batch workload's seven rays
+# (negative beta as |beta| with phi + pi), a focus offset, backward waves and
+# a cover index of 1
+ILLUM_CASES = {
+    "rays7": dict(shape=(64, 64), wavelengths=[400.0, 550.0, 700.0], pixelsize=100.0,
+                  beta=[0.0, 0.1, 0.1, 0.2, 0.2, 0.1, 0.1],
+                  phi=[0.0, 0.0, np.pi, 0.0, np.pi, np.pi / 2, 1.5 * np.pi]),
+    "rays7_jones": dict(shape=(48, 40), wavelengths=[450.0, 600.0], pixelsize=100.0,
+                        beta=[0.0, 0.1, 0.1, 0.2, 0.2, 0.1, 0.1],
+                        phi=[0.0, 0.0, np.pi, 0.0, np.pi, np.pi / 2, 1.5 * np.pi], jones=(1, 1j)),
+    "focus": dict(shape=(32, 36), wavelengths=[500.0, 650.0], pixelsize=80.0, beta=0.3, phi=0.4, focus=7.5),
+    "backdir": dict(shape=(30, 24), wavelengths=[550.0], pixelsize=100.0, beta=0.15, phi=-0.8, backdir=True,
+                    jones=(0, 1)),
+    "cover1": dict(shape=(20, 20), wavelengths=[550.0, 600.0], pixelsize=120.0, beta=0.25, phi=2.0, n=1.0,
+                   intensity=2.5),
+    "big_beta": dict(shape=(16, 24), wavelengths=[500.0], pixelsize=100.0, beta=[0.5, 0.7], phi=[0.1, 3.0],
+                     jones=(1, 0)),
+}

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from golden_cases import CASES, build_inputs  # noqa: E402
+from golden_cases import CASES, ILLUM_CASES, build_inputs  # noqa: E402
 
 
 def run_case(name, dtmm):
@@ -79,15 +79,30 @@ def save_alphaf_kat(dtmm):
     print("kat_alphaf             %d voxels" % n)
 
 
+def save_illum(dtmm):
+    """Reference illumination_data fields for ILLUM_CASES, one array per case in illum.npz."""
+    arrays = {}
+    for name, case in ILLUM_CASES.items():
+        kw = dict(case)
+        shape = kw.pop("shape")
+        wl = kw.pop("wavelengths")
+        ps = kw.pop("pixelsize")
+        arrays[name] = np.asarray(dtmm.illumination_data(shape, wl, pixelsize=ps, **kw)[0])
+    np.savez_compressed(os.path.join(HERE, "illum.npz"), **arrays)
+    print("illum                  %d cases" % len(arrays))
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat"] + list(CASES))
+    names = argv[1:] or (["kat", "illum"] + list(CASES))
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
             save_alphaf_kat(dtmm)
+        elif name == "illum":
+            save_illum(dtmm)
         else:
             run_case(name, dtmm)
 

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == 1
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 2
 
 
 def _desc(**kw):
@@ -69,6 +69,9 @@ def test_workspace_size_positive_for_valid_desc(lib):
     ("reflection", 2, "reflection"),
     ("height", 11, "factor"),
     ("npass", 0, "npass"),
+    ("fft_schedule", 4, "tuning"),
+    ("row_group", -1, "tuning"),
+    ("col_tile", -2, "tuning"),
 ])
 def test_invalid_descriptors_are_rejected(lib, field, value, needle):
     d = _desc(**{field: value})
@@ -84,3 +87,24 @@ def test_transfer_rejects_small_workspace(lib):
     rc = lib.dtmm_transfer(ctypes.byref(d), ctypes.byref(io), ctypes.c_void_p(1), 16, None)
     assert rc == _lib.DTMM_ENOSPACE
     assert "workspace" in _lib.last_error()
+
+
+def test_tuning_fields_do_not_change_the_workspace(lib):
+    base = lib.dtmm_transfer_workspace_size(ctypes.byref(_desc()))
+    for kw in ({"fft_schedule": 1}, {"fft_schedule": 3}, {"row_group": 4, "col_tile": 8}):
+        assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == base
+
+
+@pytest.mark.parametrize("args,needle", [
+    ((0, 16, 1, 1, 1, 1, 0, 1), "grid"),
+    ((16, 16, 0, 1, 1, 1, 0, 1), "image count"),
+    ((16, 16, 70000, 1, 1, 1, 0, 1), "image count"),
+    ((16, 16, 2, 0, 1, 1, 0, 1), "null"),
+    ((16, 16, 2, 1, 1, 1, 5, 1), "precision"),
+])
+def test_planewave_rejects_invalid_arguments(lib, args, needle):
+    h, w, n, coef, my, mx, prec, field = args
+    rc = lib.dtmm_planewave_field(h, w, n, ctypes.c_void_p(coef), ctypes.c_void_p(my), ctypes.c_void_p(mx), prec,
+                                  ctypes.c_void_p(field), None)
+    assert rc == _lib.DTMM_EINVAL
+    assert needle in _lib.last_error()
