@@ -219,10 +219,28 @@ def run_batch(args, dev, ninst=48, seed=0):
     batch = TransferBatch(nstreams=args.streams, device=dev)
     for (plan, fin, fout), s in zip(inst, specs):
         batch.add(plan, fin, fout, tag=s["index"])
-    # one eager pass, counting the library's kernel launches per instance
+    # one eager pass, one instance at a time: the library's kernel launches
+    # and device time per kernel family, grouped by grid side
     launches = 0
-    for plan, fin, fout in inst:
-        launches += plan.run(fin, fout, timed=True).total_launches
+    by_side = {}
+    for (plan, fin, fout), s in zip(inst, specs):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        kt = plan.run(fin, fout, timed=True)
+        e1.record()
+        e1.synchronize()
+        launches += kt.total_launches
+        b = by_side.setdefault(str(s["shape"][0]), {"instances": 0, "updates": 0, "ms": 0.0, "row_ms": 0.0,
+                                                      "col_ms": 0.0, "op_ms": 0.0, "tuning": plan.tuning})
+        b["instances"] += 1
+        b["updates"] += plan.updates
+        b["ms"] += e0.elapsed_time(e1)
+        b["row_ms"] += kt.layer_row_ms
+        b["col_ms"] += kt.layer_col_ms
+        b["op_ms"] += kt.voxel_op_ms
+    for b in by_side.values():
+        b["updates_per_s_alone"] = b["updates"] / (b["ms"] / 1e3)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     batch.capture(warm=False)
@@ -263,8 +281,7 @@ def run_batch(args, dev, ninst=48, seed=0):
                      "peak_source": peak_kind},
         "gpu_launches": launches * args.steps, "clocks": clocks, "updates_per_step": upd,
         "graph": {"build_s": build_s, "capture_s": capture_s, "serial_one_stream_ms": serial_ms,
-                  "graph_speedup_vs_serial": serial_ms / ms,
-                  "tuned": {k: v for k, v in sorted(tuner.cache.items())}},
+                  "graph_speedup_vs_serial": serial_ms / ms, "by_side": by_side},
     }
     # end to end: host inputs in pinned memory, copies in, one graph launch, copies out
     if not args.no_e2e:
@@ -311,6 +328,68 @@ def run_batch(args, dev, ninst=48, seed=0):
         result["c128"] = {"subset": len(sub), "value": res["double"], "mixed_value": res["mixed"],
                           "mixed_speedup": res["mixed"] / res["double"], "mixed_rel_l2_vs_c128_max": err}
     return result
+
+
+# ---------------------------------------------------------------------------
+# 2x2 method, memory-bound sweep: 1024x1024, 100 layers, 3 wavelengths, 25 windows
+# ---------------------------------------------------------------------------
+def run_2x2(args, dev):
+    import torch
+
+    from dtmm_gb300 import samples
+    from dtmm_gb300.illumination import illumination_device
+    from dtmm_gb300.transfer import plan_transfer
+
+    shape, nl = (1024, 1024), args.layers if args.layers != NLAYERS else 100
+    wl = np.asarray([450.0, 550.0, 650.0])
+    d, epsv, epsa = samples.inplane_nematic(shape, nl, no=1.5, ne=1.6, seed=4)
+    opts = dict(method="2x2", diffraction=5, reflection=0, beta=0.0, phi=0.0)
+    fin = illumination_device(shape, wl, 100.0, precision="mixed", device=dev)
+    plan = plan_transfer(tuple(fin.shape), wl, 100.0, [(d, epsv, epsa)], precision="mixed", device=dev, **opts)
+    fout = torch.empty_like(fin)
+    for _ in range(args.warmup):
+        plan.run(fin, fout)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    times, kts = [], []
+    stream = torch.cuda.current_stream(dev)
+    with ClockSampler(dev.index or 0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            kts.append(plan.run(fin, fout, timed=True))
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    clocks = clk.summary()
+    ms = float(np.mean(times))
+    upd = plan.updates
+    nf = int(np.prod(fin.shape[:-3])) // len(wl)
+    bpu = 2 * 2 * 8 + 48.0 / (len(wl) * nf)
+    peak, peak_kind = measured_peaks()
+    row_ms = sum(k.layer_row_ms for k in kts)
+    row_n = sum(k.layer_row_launches for k in kts)
+    per_launch = int(np.prod(fin.shape[:-3])) * shape[0] * shape[1]
+    achieved_row = bpu * per_launch / (row_ms / row_n / 1e3) / 1e9
+    return {
+        "metric": METRIC, "value": upd / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": "transfer_field 2x2, diffraction 5 (25 windows), no reflection, 1024x1024 grid, "
+                               "%d layers, 100 nm pixels, wavelengths 450/550/650 nm, x+y polarisation, in-plane "
+                               "nematic (16-mode azimuth, ne 1.6, no 1.5), complex64 bulk + FP64 eigen-solve" % nl,
+                   "l2": "flushed between timed steps (256 MiB write); fields (100 MB) are near L2 size"},
+        "roofline": {"bound": "hbm", "achieved": bpu * upd / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": bpu * upd / (ms / 1e3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                     "kernel": "whole transfer (algorithmic bytes / step time)",
+                     "row_kernel_achieved": achieved_row,
+                     "device_ms_per_step": {"layer_row": row_ms / args.steps,
+                                            "layer_col": sum(k.layer_col_ms for k in kts) / args.steps,
+                                            "voxel_op": sum(k.voxel_op_ms for k in kts) / args.steps}},
+        "gpu_launches": sum(k.total_launches for k in kts), "clocks": clocks, "updates_per_step": upd,
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -366,9 +445,9 @@ def main():
     ap.add_argument("--no-c128", action="store_true", help="skip the complex128 comparison run")
     ap.add_argument("--layers", type=int, default=NLAYERS, help="layers (profiling runs use fewer; same kernels)")
     ap.add_argument("--npass", type=int, default=OPTS["npass"])
-    ap.add_argument("--workload", default="precision", choices=["precision", "batch", "serve"],
+    ap.add_argument("--workload", default="precision", choices=["precision", "batch", "serve", "2x2"],
                     help="precision: 256x256 4x4 npass 3 (default); batch: 48 instances in one graph; "
-                         "serve: Poisson request stream")
+                         "serve: Poisson request stream; 2x2: 1024x1024 2x2 diffraction 5")
     ap.add_argument("--streams", type=int, default=8, help="batch: streams in the graph")
     ap.add_argument("--c128-subset", type=int, default=8, help="batch: instances of the complex128 comparison")
     ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the trace")
@@ -400,9 +479,9 @@ def main():
             dist.barrier()
 
     dev = torch.device("cuda", local)
-    if args.workload in ("batch", "serve"):
+    if args.workload in ("batch", "serve", "2x2"):
         # independent replicas: every rank runs the whole workload on its own GPU
-        res = run_batch(args, dev) if args.workload == "batch" else run_serve(args, dev)
+        res = {"batch": run_batch, "serve": run_serve, "2x2": run_2x2}[args.workload](args, dev)
         barrier()
         if dist is not None:
             t = torch.tensor([res["ms_per_step"]], device=dev)

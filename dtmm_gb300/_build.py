@@ -1,6 +1,7 @@
 """In-tree build of the CUDA library (``dtmm_gb300/_lib/libdtmm_gb300.so``).
 
-One translation unit, compiled for sm_103a with nvcc; no CMake, no torch
+Every ``csrc/*.cu`` unit is compiled for sm_103a with nvcc in parallel (one
+process per unit), then linked into one shared library; no CMake, no torch
 extension machinery.  The library exports the C ABI of
 ``include/dtmm_gb300.h``.
 """
@@ -9,6 +10,7 @@ from __future__ import annotations
 import os
 import shutil
 import subprocess
+from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -53,15 +55,32 @@ def build(force=False, verbose=False):
     if not force and up_to_date():
         return out
     os.makedirs(LIBDIR, exist_ok=True)
+    objdir = os.path.join(LIBDIR, "obj.%d" % os.getpid())
+    os.makedirs(objdir, exist_ok=True)
+    flags = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
+    if verbose:
+        flags.insert(0, "-Xptxas=-v")
+    srcs = sources()
+    objs = [os.path.join(objdir, os.path.basename(f)[:-3] + ".o") for f in srcs]
+
+    def compile_one(i):
+        return subprocess.run([nvcc_path()] + flags + ["-c", srcs[i], "-o", objs[i]], capture_output=True, text=True)
+
+    jobs = max(1, min(len(srcs), os.cpu_count() or 1))
+    with ThreadPoolExecutor(max_workers=jobs) as ex:
+        results = list(ex.map(compile_one, range(len(srcs))))
+    log = "".join(r.stdout + r.stderr for r in results)
+    bad = [srcs[i] for i, r in enumerate(results) if r.returncode != 0]
+    if bad:
+        shutil.rmtree(objdir, ignore_errors=True)
+        raise RuntimeError("nvcc failed on %s:\n%s" % (", ".join(os.path.basename(b) for b in bad), log))
     tmp = out + ".tmp.%d" % os.getpid()
-    cmd = [nvcc_path(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
-           "-I" + os.path.join(ROOT, "include"), "-o", tmp] + sources() + ["-lcudart"]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    r = subprocess.run(cmd, capture_output=True, text=True)
+    r = subprocess.run([nvcc_path(), ARCH, "-shared", "-o", tmp] + objs + ["-lcudart"], capture_output=True,
+                       text=True)
+    shutil.rmtree(objdir, ignore_errors=True)
     if r.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + r.stdout + r.stderr)
+        raise RuntimeError("nvcc link failed:\n" + r.stdout + r.stderr)
     if verbose:
-        print(r.stdout + r.stderr)
+        print(log)
     os.replace(tmp, out)
     return out

@@ -24,6 +24,7 @@
 
 #include "../../include/dtmm_gb300.h"
 #include "dtmm_kernels.cuh"
+#include "dtmm_regkern.cuh"
 
 using namespace dtmm;
 
@@ -290,40 +291,31 @@ struct Engine {
     return tc;
   }
 
-  bool col_reg() const { return sizeof(R) == 4 && d.fft_schedule <= 1 &&
-                                (d.height == 64 || d.height == 128 || d.height == 256 || d.height == 512 ||
-                                 d.height == 1024); }
-
-  template <int N1, int N2>
-  int launch_col_reg_t(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
-    int tx = std::max(1, 256 / (C * N1));
-    if (d.col_tile > 0 && d.col_tile * C * N1 <= 512) tx = d.col_tile;
-    if (tx > d.width) tx = d.width;
-    while (tx > 1 && (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) > 100 * 1024) tx /= 2;
-    p.tc = tx;
-    const size_t smem = (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
-    auto kern = k_layer_col_reg<R, N1, N2>;
-    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int threads = std::max(32, ((C * tx * N1 + 31) / 32) * 32);
-    dim3 grid((d.width + tx - 1) / tx, NI);
-    mark(PROF_COL);
-    kern<<<grid, threads, smem, st>>>(p, g, in, out);
-    mark(PROF_COL);
-    CKL("k_layer_col_reg");
-    return DTMM_OK;
-  }
+  // register-transform column pass: complex64 bulk, sides listed by reg_lanes
+  bool col_reg() const { return sizeof(R) == 4 && d.fft_schedule <= 1 && reg_lanes(d.height) > 0; }
 
   int launch_col_reg(ColParams& p, const cpx<R>* in, cpx<R>* out, int C) {
     if constexpr (sizeof(R) != 4) {
       return fail(DTMM_ENOTSUP, "register column transform is complex64 only");
     } else {
-      switch (d.height) {
-        case 64: return launch_col_reg_t<8, 8>(p, in, out, C);
-        case 128: return launch_col_reg_t<8, 16>(p, in, out, C);
-        case 256: return launch_col_reg_t<16, 16>(p, in, out, C);
-        case 512: return launch_col_reg_t<16, 32>(p, in, out, C);
-        default: return launch_col_reg_t<32, 32>(p, in, out, C);
-      }
+      const int n1 = reg_lanes(d.height);
+      int tx = std::max(1, 256 / (C * n1));
+      if (d.col_tile > 0 && d.col_tile * C * n1 <= 512) tx = d.col_tile;
+      if (tx > d.width) tx = d.width;
+      // two tiles (spectra and exchange) of H x (C tx + 1) complex
+      while (tx > 1 && 2 * (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) > 160 * 1024) tx /= 2;
+      p.tc = tx;
+      RegLaunch rl;
+      rl.smem = 2 * (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
+      rl.threads = std::max(32, ((C * tx * n1 + 31) / 32) * 32);
+      rl.grid = dim3((d.width + tx - 1) / tx, NI);
+      rl.st = st;
+      mark(PROF_COL);
+      const cudaError_t e = col_reg_dispatch(d.height, rl, p, g, in, out);
+      mark(PROF_COL);
+      ++launches;
+      if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_col_reg: %s", cudaGetErrorString(e));
+      return DTMM_OK;
     }
   }
 
@@ -393,14 +385,16 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // register-transform row kernel: float bulk, W = N1 * N2 in {64 ... 1024}
-  bool row_reg() const { return sizeof(R) == 4 && d.fft_schedule <= 1 &&
-                                (d.width == 64 || d.width == 128 || d.width == 256 || d.width == 512 || d.width == 1024); }
+  // register-transform row pass: complex64 bulk, sides listed by reg_lanes
+  // (complex operator records only for power-of-two sides)
+  bool row_reg() const {
+    return sizeof(R) == 4 && d.fft_schedule <= 1 && reg_row_variant(d.width, real_ops());
+  }
 
   int row_group_reg() const {
     const int perG = d.npol * L.C;  // lines per wavelength
-    const int n1 = d.width >= 1024 ? 32 : (d.width >= 256 ? 16 : 8);
-    const size_t line_bytes = 2 * (size_t)d.width * sizeof(cpx<R>);
+    const int n1 = reg_lanes(d.width);
+    const size_t line_bytes = 2 * (size_t)reg_row_stride(n1, d.width) * sizeof(cpx<R>);
     // about 8 lines per block measured best (256-pixel rows, 4x4, 2 polarisations)
     int G = std::max(1, 8 / perG);
     if (d.row_group > 0) G = d.row_group;
@@ -408,37 +402,29 @@ struct Engine {
     return std::min(G, d.nlam);
   }
 
-  template <int C, bool REAL, int N1, int N2>
-  int launch_row_reg_t(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
-    const int nl = p.G * p.PB * C;
-    const size_t smem = 2 * (size_t)nl * d.width * sizeof(cpx<R>) + d.width * sizeof(cpx<R>);
-    if (smem > 220 * 1024 || nl * N1 > 512)
-      return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
-    auto kern = k_layer_row_reg<R, C, REAL, N1, N2>;
-    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int threads = std::max(((nl * N1 + 31) / 32) * 32, 32);
-    const int ngrp = (d.nlam + p.G - 1) / p.G;
-    const int npg = (d.npol + p.PB - 1) / p.PB;
-    dim3 grid(d.height, d.nray * ngrp * npg);
-    mark(PROF_ROW);
-    kern<<<grid, threads, smem, st>>>(p, g, Ub, Xb);
-    mark(PROF_ROW);
-    CKL("k_layer_row_reg");
-    return DTMM_OK;
-  }
-
-  template <int C, bool REAL>
-  int launch_row_reg(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb) {
+  int launch_row_reg(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb, int C, bool re) {
     if constexpr (sizeof(R) != 4) {
       return fail(DTMM_ENOTSUP, "register row transform is complex64 only");
     } else {
-      switch (d.width) {
-        case 64: return launch_row_reg_t<C, REAL, 8, 8>(p, Ub, Xb);
-        case 128: return launch_row_reg_t<C, REAL, 8, 16>(p, Ub, Xb);
-        case 256: return launch_row_reg_t<C, REAL, 16, 16>(p, Ub, Xb);
-        case 512: return launch_row_reg_t<C, REAL, 16, 32>(p, Ub, Xb);
-        default: return launch_row_reg_t<C, REAL, 32, 32>(p, Ub, Xb);
-      }
+      const int n1 = reg_lanes(d.width);
+      const int nl = p.G * p.PB * C;
+      const size_t smem =
+          2 * (size_t)nl * reg_row_stride(n1, d.width) * sizeof(cpx<R>) + d.width * sizeof(cpx<R>);
+      if (smem > 220 * 1024 || nl * n1 > 512)
+        return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
+      RegLaunch rl;
+      rl.smem = smem;
+      rl.threads = std::max(((nl * n1 + 31) / 32) * 32, 32);
+      const int ngrp = (d.nlam + p.G - 1) / p.G;
+      const int npg = (d.npol + p.PB - 1) / p.PB;
+      rl.grid = dim3(d.height, d.nray * ngrp * npg);
+      rl.st = st;
+      mark(PROF_ROW);
+      const cudaError_t e = row_reg_dispatch(d.width, C, re, rl, p, g, Ub, Xb);
+      mark(PROF_ROW);
+      ++launches;
+      if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_row_reg: %s", cudaGetErrorString(e));
+      return DTMM_OK;
     }
   }
 
@@ -464,10 +450,11 @@ struct Engine {
     const bool re = real_ops();
     if (row_reg()) {
       p.G = row_group_reg();
-      const int n1 = d.width >= 1024 ? 32 : (d.width >= 256 ? 16 : 8);
-      if (2 * (size_t)d.npol * L.C * d.width * sizeof(cpx<R>) > 200 * 1024 || d.npol * L.C * n1 > 512) p.PB = 1;
-      if (L.C == 4) return re ? launch_row_reg<4, true>(p, Ub, Xb) : launch_row_reg<4, false>(p, Ub, Xb);
-      return re ? launch_row_reg<2, true>(p, Ub, Xb) : launch_row_reg<2, false>(p, Ub, Xb);
+      const int n1 = reg_lanes(d.width);
+      if (2 * (size_t)d.npol * L.C * reg_row_stride(n1, d.width) * sizeof(cpx<R>) > 200 * 1024 ||
+          d.npol * L.C * n1 > 512)
+        p.PB = 1;
+      return launch_row_reg(p, Ub, Xb, L.C, re);
     }
     p.G = row_group();
     if (2 * (size_t)d.npol * L.C * (d.width | 1) * sizeof(cpx<R>) > 200 * 1024) p.PB = 1;
@@ -575,7 +562,14 @@ struct Engine {
     p.waw = waw();
     p.nwin = L.nwin;
     p.four = d.method == 4;
-    dim3 grid((unsigned)((L.HW + 127) / 128), d.nray);
+    p.nray = d.nray;
+    // every ray of a voxel in one thread (its trigonometry computed once)
+    // while that still leaves at least 4 blocks per SM
+    const int blocks = (int)((L.HW + 127) / 128);
+    int rpt = d.nray;
+    while (rpt > 1 && (long long)blocks * ((d.nray + rpt - 1) / rpt) < 608) rpt = (rpt + 1) / 2;
+    p.rays_per_thread = rpt;
+    dim3 grid((unsigned)blocks, (unsigned)((d.nray + rpt - 1) / rpt));
     mark(PROF_OP);
     if (real_ops())
       k_voxel_op<R, true><<<grid, 128, 0, st>>>(p, g, op);

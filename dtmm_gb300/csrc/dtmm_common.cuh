@@ -316,153 +316,4 @@ __device__ void fft_lines_warp(cpx<R>* s, int ls, int nlines, const cpx<R>* tw, 
   }
 }
 
-// ---------------------------------------------------------------------------
-// In-register DFTs of 2..32 points and a two-step line transform.
-//
-// exp(-2 pi i j / 32) from a quarter-period table of cos(2 pi j / 32),
-// j = 0..8 (mathematical constants); multiplications by 1, -1, +-i are exact
-// swaps / negations.
-// ---------------------------------------------------------------------------
-struct Tw32 {
-  static constexpr double q[9] = {1.0,
-                                  0.98078528040323044912618223613424,
-                                  0.92387953251128675612818318939679,
-                                  0.83146961230254523707878837761791,
-                                  0.70710678118654752440084436210485,
-                                  0.55557023301960222474283081394853,
-                                  0.38268343236508977172845998403040,
-                                  0.19509032201612826784828486847702,
-                                  0.0};
-  __host__ __device__ static constexpr double cos32(int j) {
-    j &= 31;
-    return j < 8 ? q[j] : (j < 16 ? -q[16 - j] : (j < 24 ? -q[j - 16] : q[32 - j]));
-  }
-  __host__ __device__ static constexpr double sin32(int j) { return cos32(j - 8); }
-};
-
-// v * exp(s 2 pi i j / 32), s = -1 forward, +1 inverse
-template <typename R, int J, bool INV>
-__device__ __forceinline__ cpx<R> rot32(cpx<R> v) {
-  constexpr int j = J & 31;
-  if constexpr (j == 0) {
-    return v;
-  } else if constexpr (j == 16) {
-    return mk<R>(-v.re, -v.im);
-  } else if constexpr (j == 8) {
-    return INV ? mk<R>(-v.im, v.re) : mk<R>(v.im, -v.re);
-  } else if constexpr (j == 24) {
-    return INV ? mk<R>(v.im, -v.re) : mk<R>(-v.im, v.re);
-  } else {
-    constexpr R c = (R)Tw32::cos32(j);
-    constexpr R sn = INV ? (R)Tw32::sin32(j) : (R)-Tw32::sin32(j);
-    return mk<R>(v.re * c - v.im * sn, v.re * sn + v.im * c);
-  }
-}
-
-template <typename R, int N, bool INV>
-struct RegDFT {
-  template <int K>
-  __device__ static __forceinline__ void combine(cpx<R>* v, const cpx<R>* e, const cpx<R>* o) {
-    if constexpr (K < N / 2) {
-      const cpx<R> t = rot32<R, K * (32 / N), INV>(o[K]);
-      v[K] = e[K] + t;
-      v[K + N / 2] = e[K] - t;
-      combine<K + 1>(v, e, o);
-    }
-  }
-  __device__ static __forceinline__ void run(cpx<R>* v) {
-    cpx<R> e[N / 2], o[N / 2];
-#pragma unroll
-    for (int i = 0; i < N / 2; ++i) {
-      e[i] = v[2 * i];
-      o[i] = v[2 * i + 1];
-    }
-    RegDFT<R, N / 2, INV>::run(e);
-    RegDFT<R, N / 2, INV>::run(o);
-    combine<0>(v, e, o);
-  }
-};
-template <typename R, bool INV>
-struct RegDFT<R, 1, INV> {
-  __device__ static __forceinline__ void run(cpx<R>*) {}
-};
-template <typename R, bool INV>
-struct RegDFT<R, 2, INV> {
-  __device__ static __forceinline__ void run(cpx<R>* v) {
-    const cpx<R> a = v[0], b = v[1];
-    v[0] = a + b;
-    v[1] = a - b;
-  }
-};
-template <typename R, bool INV>
-struct RegDFT<R, 4, INV> {
-  __device__ static __forceinline__ void run(cpx<R>* v) { dft_reg<R, 4, INV>(v, nullptr, 4); }
-};
-
-// Transform of one N = N1 * N2 point line by a group of N1 consecutive lanes
-// (t = lane within the group).  In: v[m] = x[t + N1 m]; out: v[m] = X[t + N1 m]
-// (natural order on both sides).
-//   X[k1 + N2 k2] = sum_t W_N1^(t k2) W_N^(t k1) sum_m x[t + N1 m] W_N2^(m k1)
-// Step 1 is an N2-point DFT in registers, then the twiddle W_N^(t k1) (`trow`
-// holds W_N^(t k1), k1 = 0..N2-1, forward sign), an exchange through `xch`
-// (N complex, swizzled so that both the writes and the reads are free of bank
-// conflicts), and N2/N1 N1-point DFTs in registers.
-// `trow` holds the lane's twiddles in registers (small N2); with `trow` null
-// they are read from the shared table `twn` (W_N^e, e = 0..N-1).
-template <typename R, int N1, int N2, bool INV>
-__device__ __forceinline__ void line_fft_2step(cpx<R> (&v)[N2], cpx<R>* xch, const cpx<R>* trow, const cpx<R>* twn,
-                                               int t) {
-  RegDFT<R, N2, INV>::run(v);
-#pragma unroll
-  for (int k1 = 1; k1 < N2; ++k1) {
-    cpx<R> w = trow ? trow[k1] : twn[(t * k1) & (N1 * N2 - 1)];
-    if (INV) w.im = -w.im;
-    v[k1] = v[k1] * w;
-  }
-#pragma unroll
-  for (int k1 = 0; k1 < N2; ++k1) xch[k1 * N1 + (t ^ (k1 & (N1 - 1)))] = v[k1];
-  __syncwarp();
-  constexpr int J = N2 / N1;
-#pragma unroll
-  for (int j = 0; j < J; ++j) {
-    cpx<R> u[N1];
-    const int k1 = t + N1 * j;
-#pragma unroll
-    for (int sidx = 0; sidx < N1; ++sidx) u[sidx] = xch[k1 * N1 + (sidx ^ t)];
-    RegDFT<R, N1, INV>::run(u);
-#pragma unroll
-    for (int k2 = 0; k2 < N1; ++k2) v[j + J * k2] = u[k2];
-  }
-  __syncwarp();
-}
-
-// line_fft_2step with the exchange buffer at a stride (element e at xch[e * xs])
-template <typename R, int N1, int N2, bool INV>
-__device__ __forceinline__ void line_fft_2step_strided(cpx<R> (&v)[N2], cpx<R>* xch, int xs, const cpx<R>* trow,
-                                                       const cpx<R>* twn, int t) {
-  RegDFT<R, N2, INV>::run(v);
-#pragma unroll
-  for (int k1 = 1; k1 < N2; ++k1) {
-    cpx<R> w = trow ? trow[k1] : twn[(t * k1) & (N1 * N2 - 1)];
-    if (INV) w.im = -w.im;
-    v[k1] = v[k1] * w;
-  }
-  __syncwarp();
-#pragma unroll
-  for (int k1 = 0; k1 < N2; ++k1) xch[(k1 * N1 + (t ^ (k1 & (N1 - 1)))) * xs] = v[k1];
-  __syncwarp();
-  constexpr int J = N2 / N1;
-#pragma unroll
-  for (int j = 0; j < J; ++j) {
-    cpx<R> u[N1];
-    const int k1 = t + N1 * j;
-#pragma unroll
-    for (int sidx = 0; sidx < N1; ++sidx) u[sidx] = xch[(k1 * N1 + (sidx ^ t)) * xs];
-    RegDFT<R, N1, INV>::run(u);
-#pragma unroll
-    for (int k2 = 0; k2 < N1; ++k2) v[j + J * k2] = u[k2];
-  }
-  __syncwarp();
-}
-
 }  // namespace dtmm

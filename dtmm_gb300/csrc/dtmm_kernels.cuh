@@ -1,38 +1,18 @@
 // Kernels of the GB300 field-transfer engine (the hot path of dtmm's
-// transfer_field).  All kernels are templated on the bulk real type R
+// transfer_field) other than the register-transform row / column passes
+// (dtmm_regkern.cuh).  All kernels are templated on the bulk real type R
 // (float = complex64 bulk, double = complex128 bulk); eigen-solves, k-space
-// operator tables and window statistics are always computed in FP64.
-//
-// Data layout in HBM
-//   field / state arrays : [image][component][H][W] interleaved complex,
-//                          image = (ray * npol + pol) * nlam + lam
-//                          (the reference's ([rays],[pols],lambda,4,H,W) order)
-//   window-row buffers   : [j][image][component][H][W]
-//   layer operators      : [ray][window][record][H][W]   (14 complex records)
-//   k-space tables       : [lam][H][W][rows][cols]
+// operator tables and window statistics are always computed in FP64.  The
+// data layout in HBM is described in dtmm_layer.cuh; k-space tables are
+// [lam][H][W][rows][cols].
 #pragma once
 
 #include <type_traits>
 
 #include "dtmm_common.cuh"
+#include "dtmm_layer.cuh"
 
 namespace dtmm {
-
-constexpr int OP_REC = 14;  // records of one per-voxel layer operator
-
-enum KOp { KOP_NONE = 0, KOP_DIAG = 1, KOP_MAT = 2 };
-
-struct Grid {
-  int H, W;       // grid
-  int NI;         // images
-  int nlam, npol, nray;
-};
-
-__device__ __forceinline__ int img_lam(const Grid& g, int img) { return img % g.nlam; }
-__device__ __forceinline__ int img_ray(const Grid& g, int img) { return img / (g.nlam * g.npol); }
-
-// fftfreq(n)[i] * n
-__host__ __device__ __forceinline__ int fsigned(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
 
 // ---------------------------------------------------------------------------
 // FP64 Berreman eigen-data of an isotropic medium, in the phi = 0 frame, then
@@ -150,6 +130,8 @@ struct OpParams {
   cpx<double> eps_eff;
   int nwin;
   int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
+  int rays_per_thread;   // rays [blockIdx.y * rays_per_thread, ...) share the voxel's trigonometry
+  int nray;
 };
 
 // Records per voxel and window, [ray][window][record][H][W]: complex, or real
@@ -159,8 +141,8 @@ struct OpParams {
 // when every eigenvalue and the effective medium exceed beta^2 (then every
 // radicand of the solve is positive; the host proves this before selecting
 // the real path).  Same formulas as the complex path below.
-__device__ inline bool voxel_E_real(double beta, const double ev[3], double st, double ct, double sf, double cf,
-                                    double E[2][4], double al[4]) {
+__device__ inline bool voxel_E_real(double beta, const double ev[3], double ie, double st, double ct, double sf,
+                                    double cf, double E[2][4], double al[4]) {
   if (ev[0] == ev[1] && ev[1] == ev[2]) {
     const double a = sqrt(ev[0] - beta * beta);
     al[0] = a; al[1] = -a; al[2] = a; al[3] = -a;
@@ -198,7 +180,6 @@ __device__ inline bool voxel_E_real(double beta, const double ev[3], double st, 
     evpp = sq - vh;
     evpm = -vh - sq;
     const double ctbeta = ct * beta;
-    const double ie = 1.0 / eps11;
     const double ev02cf = ev02 * cfst;
     E[0][0] = (evpp * ctbeta - ev02cf) * ie;  E[1][0] = -sfst;
     E[0][1] = (ev02cf - evpm * ctbeta) * ie;  E[1][1] = sfst;
@@ -213,7 +194,8 @@ template <typename R, bool REAL>
 __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int HW = g.H * g.W;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ray = blockIdx.y;
+  const int ray0 = blockIdx.y * p.rays_per_thread;
+  const int ray1 = min(ray0 + p.rays_per_thread, p.nray);
   if (pix >= HW) return;
   const int y = pix / g.W, x = pix - y * g.W;
   const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
@@ -229,15 +211,15 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   if (REAL) {
     const double* e = (const double*)p.epsv + eo;
     const double ev[3] = {e[0], e[1], e[2]};
-    for (int w = 0; w < p.nwin; ++w) {
-      const int rw = ray * p.nwin + w;
+    const double ie = 1.0 / ev[0];  // 1 / eps11, shared by every ray and window
+    for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
       const double beta = p.wbeta[rw];
       const double cp = p.wcos[rw], sp = p.wsin[rw];
       // cos / sin of (azimuth - phi) by the angle-difference identities
       const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
       const double aw = p.waw[rw];
       double E[2][4], al[4];
-      bool zero = voxel_E_real(beta, ev, st, ct, sf, cf, E, al);
+      bool zero = voxel_E_real(beta, ev, ie, st, ct, sf, cf, E, al);
       for (int m = 0; m < 4; ++m) {
         const double ex = E[0][m], ey = E[1][m];
         E[0][m] = ex * cp - ey * sp;
@@ -264,8 +246,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     }
     return;
   }
-  for (int w = 0; w < p.nwin; ++w) {
-    const int rw = ray * p.nwin + w;
+  for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
     const double beta = p.wbeta[rw];
     const double cp = p.wcos[rw], sp = p.wsin[rw];
     const double cfw = ca * cp + sa * sp, sfw = sa * cp - ca * sp;
@@ -765,31 +746,6 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// Fused column pass of one layer step (all along ky, one tile of TC columns
-// of one image):
-//   forward column FFT -> k-space operator -> for each window row j:
-//   cy_j * (.) -> inverse column FFT (scaled) -> U_j.
-// Input X: [image][cin][H][W] (rows already transformed along x).
-// ---------------------------------------------------------------------------
-struct ColParams {
-  int cin, cout;
-  int kop;                 // KOp
-  size_t ktab_ray_stride;  // elements between the tables of consecutive rays (0 = shared)
-  const void* ktab;        // KOP_DIAG: [lam][H][W][2]; KOP_MAT: [lam][H][W][cout][cin]
-  int ny;                  // window rows (1 = no windows)
-  const void* cy;          // [ray][j][lam][H] (null = weight 1)
-  int j_only;              // >= 0: emit only window row j_only (into U slot 0)
-  int cy_rows;             // window rows in the cy table (ray stride = cy_rows * nlam * H)
-  int do_fwd;              // 1: transform along y first (input spatial in y)
-  int inverse_out;         // 1: inverse column FFT on the way out
-  double out_scale;
-  FFTPlan plan;
-  const void* tw;          // twiddles of H
-  const int* perm;         // digit reversal of H
-  int tc;                  // columns per block
-};
-
 template <typename R>
 __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cpx<R>* __restrict__ X,
                                                    cpx<R>* __restrict__ U) {
@@ -877,127 +833,6 @@ __global__ void __launch_bounds__(256) k_layer_col(ColParams p, Grid g, const cp
     }
     __syncthreads();
   }
-}
-
-// Column pass for power-of-two heights H = N1 * N2 (float bulk) with the
-// k-space operator KOP_NONE or KOP_DIAG: a tile of TX columns x C components
-// of one image is loaded with coalesced row reads into shared memory (odd row
-// stride), every (component, column) line is transformed in registers by a
-// group of N1 lanes that uses its own tile column as exchange buffer, the
-// diagonal operator and the window weights act in registers, and results go
-// back through the tile to coalesced row writes.
-template <typename R, int N1, int N2>
-__global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
-                                                         cpx<R>* __restrict__ U) {
-  constexpr int H = N1 * N2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int W = g.W, TX = p.tc, C = p.cin;
-  const int RS = C * TX + 1;                       // tile row stride (odd)
-  cpx<R>* tile = (cpx<R>*)smem_raw;                // [H][RS]
-  cpx<R>* tw = tile + (size_t)H * RS;              // [H] exp(-2 pi i e / H)
-  const int img = blockIdx.y;
-  const int x0 = blockIdx.x * TX;
-  const int lam = img_lam(g, img), ray = img_ray(g, img);
-  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
-  // a half-warp covers one tile row (C x TX contiguous slots): conflict-free
-  const int CT = C * TX;
-  const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;
-  const int lcc = lc / TX, lxc = lc - lcc * TX;
-  const bool lin = (int)threadIdx.x < ystep * CT && x0 + lxc < W;
-  const cpx<R>* xsrc = X + ((size_t)img * C + lcc) * H * W + x0 + lxc;
-  if (lin)
-    for (int y = threadIdx.x / CT; y < H; y += ystep) tile[y * RS + lc] = xsrc[(size_t)y * W];
-  __syncthreads();
-  const int l = threadIdx.x / N1, t = threadIdx.x % N1;
-  const int nlines = C * TX;
-  const bool active = l < nlines;
-  const int c = l / TX, xc = l - c * TX;
-  const int kx = x0 + xc;
-  cpx<R>* col = tile + l;  // line element e at col[e * RS]
-  constexpr bool TWREG = false;  // twiddles from the shared table: fewer registers, more resident blocks
-  cpx<R> trow[1];
-  cpx<R> v[N2];
-  if (active) {
-#pragma unroll
-    for (int m = 0; m < N2; ++m) v[m] = col[(t + N1 * m) * RS];
-  }
-  __syncwarp();
-  if (active && p.do_fwd) line_fft_2step_strided<R, N1, N2, false>(v, col, RS, TWREG ? trow : nullptr, tw, t);
-  if (active && p.kop == KOP_DIAG && kx < W) {
-    const cpx<R>* e = (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H) * 2;
-    const bool fwd = ((c & 1) == 0) || C == 2;
-#pragma unroll
-    for (int m = 0; m < N2; ++m) v[m] = v[m] * e[(t + N1 * m) * 2 + (fwd ? 0 : 1)];
-  }
-  const R sc = (R)p.out_scale;
-  for (int jj = 0; jj < p.ny; ++jj) {
-    const int j = p.j_only >= 0 ? p.j_only : jj;
-    __syncthreads();  // the previous window's stores have read the tile
-    if (active) {
-      cpx<R> u[N2];
-      const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
-#pragma unroll
-      for (int m = 0; m < N2; ++m) u[m] = cyj ? v[m] * cyj[t + N1 * m] : v[m];
-      if (p.inverse_out) line_fft_2step_strided<R, N1, N2, true>(u, col, RS, TWREG ? trow : nullptr, tw, t);
-#pragma unroll
-      for (int m = 0; m < N2; ++m) col[(t + N1 * m) * RS] = u[m] * sc;
-    }
-    __syncthreads();
-    cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
-    if (lin)
-      for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tile[y * RS + lc];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Fused row pass of one layer step, one row y of all polarisations of one
-// (ray, lam) group:
-//   for each window (i, j): cx_i * U_j -> inverse row FFT -> per-voxel
-//   operator of window (i, j) -> accumulate; then forward row FFT -> X.
-// The accumulator lives in digit-reversed order, which is exactly the input
-// order the forward transform wants.
-// ---------------------------------------------------------------------------
-struct RowParams {
-  int C;                 // 4 (Epn) or 2 (E)
-  int nx, ny;            // windows per axis (1, 1 without windows)
-  const void* cx;        // [ray][i][lam][W] (null = weight 1)
-  const int* wzero;      // [ray][nx*ny]
-  const void* op;        // [ray][win][OP_REC][H][W]
-  const double* ks;      // [lam]
-  double dir;            // propagation direction (+1 / -1)
-  double in_scale;       // 1/W of the inverse row transform (and 1/H of the column one)
-  FFTPlan plan;
-  const void* tw;
-  const int* perm;
-  int G;                 // wavelengths per block
-  int PB;                // polarisations per block
-  int win_only;          // >= 0: only this window (its own sub-step chain), -1: all
-  int use_cx;            // apply the window's beta_x weight (first sub-step of a chain)
-  int accumulate;        // add the result to X instead of overwriting it
-};
-
-template <typename R>
-__device__ __forceinline__ cpx<R> phase_of(cpx<R> arg, R k) {
-  return cexp_i(mk<R>(arg.re * k, arg.im * k));
-}
-template <typename R>
-__device__ __forceinline__ cpx<R> phase_of(R arg, R k) {
-  R s, c;
-  if constexpr (sizeof(R) == 4)
-    sincosf(arg * k, &s, &c);
-  else
-    sincos(arg * k, &s, &c);
-  return mk<R>(c, s);
-}
-
-// one 2x2 block of the per-voxel operator: out += E . diag(P') . adj(E) . h
-template <typename R, typename T>
-__device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
-                                            cpx<R>& a1) {
-  const cpx<R> w0 = (e[3] * h0 - e[1] * h1) * p0;
-  const cpx<R> w1 = (e[0] * h1 - e[2] * h0) * p1;
-  a0 = a0 + e[0] * w0 + e[1] * w1;
-  a1 = a1 + e[2] * w0 + e[3] * w1;
 }
 
 // Row pass, one row y of a group of G wavelengths (all polarisations) of one
@@ -1113,127 +948,6 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
     cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
     const cpx<R>* src = acc + (size_t)l * LS;
     for (int x = threadIdx.x; x < W; x += blockDim.x) dst[x] = p.accumulate ? dst[x] + src[x] : src[x];
-  }
-}
-
-// Row pass for power-of-two rows W = N1 * N2 (float bulk): the same work as
-// k_layer_row with every line transformed in registers by a group of N1
-// lanes (line_fft_2step); the transforms leave natural order, so the
-// per-voxel step, the accumulator and the operator records are in natural
-// order and only the per-voxel step needs block-wide barriers.
-template <typename R, int C, bool REAL, int N1, int N2>
-__global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
-                                                         cpx<R>* __restrict__ X) {
-  using T = typename std::conditional<REAL, R, cpx<R>>::type;
-  constexpr int W = N1 * N2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int H = g.H;
-  const int ngrp = (g.nlam + p.G - 1) / p.G;
-  const int npg = (g.npol + p.PB - 1) / p.PB;
-  const int y = blockIdx.x;
-  const int pg = blockIdx.y % npg, rg = blockIdx.y / npg;
-  const int ray = rg / ngrp, grp = rg - ray * ngrp;
-  const int lam0 = grp * p.G, pol0 = pg * p.PB;
-  const int G = min(p.G, g.nlam - lam0);
-  const int NP = min(p.PB, g.npol - pol0);  // polarisations of this block
-  const int nlines = G * NP * C;
-  cpx<R>* acc = (cpx<R>*)smem_raw;                 // [lines][W]
-  cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * W;  // [lines][W] exchange and transformed rows
-  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * W;   // [W]  exp(-2 pi i e / W)
-  const int HW = H * W;
-  const int nwin = p.nx * p.ny;
-  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
-  for (int e = threadIdx.x; e < nlines * W; e += blockDim.x) acc[e] = mk<R>(0, 0);
-  const R sc = (R)p.in_scale;
-  __syncthreads();
-  const int line = threadIdx.x / N1, t = threadIdx.x % N1;
-  const bool active = line < nlines;
-  // the lane's twiddles W_N^(t k1) in registers when they fit
-  constexpr bool TWREG = N2 <= 16;
-  cpx<R> trow[TWREG ? N2 : 1];
-  if (TWREG) {
-#pragma unroll
-    for (int k1 = 0; k1 < (TWREG ? N2 : 1); ++k1) trow[k1] = tw[(t * k1) & (W - 1)];
-  }
-  const int c = line % C, im = line / C;
-  const int gl = im / NP, pol = pol0 + im - gl * NP;
-  const int lam = lam0 + gl;
-  const int img = (ray * g.npol + pol) * g.nlam + lam;
-  cpx<R>* xl = tmp + (size_t)line * W;
-  for (int j = 0; j < p.ny; ++j) {
-    // a single-window chain reads the one window row the column pass emitted
-    const cpx<R>* Uj = U + (size_t)(p.win_only >= 0 ? 0 : j) * g.NI * C * HW;
-    for (int i = 0; i < p.nx; ++i) {
-      const int w = i * p.ny + j;
-      if (p.win_only >= 0 && w != p.win_only) continue;
-      if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
-      if (active) {
-        const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
-        const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
-        cpx<R> v[N2];
-#pragma unroll
-        for (int m = 0; m < N2; ++m) {
-          cpx<R> a = src[t + N1 * m];
-          v[m] = cxl ? a * cxl[t + N1 * m] : a;
-        }
-        line_fft_2step<R, N1, N2, true>(v, xl, TWREG ? trow : nullptr, tw, t);
-#pragma unroll
-        for (int m = 0; m < N2; ++m) xl[t + N1 * m] = v[m] * sc;
-      }
-      __syncthreads();
-      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
-      for (int x = threadIdx.x; x < W; x += blockDim.x) {
-        T ef[4], arg_f[2], idf;
-        T eb[4], arg_b[2], idb;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
-        idf = opw[(size_t)4 * HW + x];
-        arg_f[0] = opw[(size_t)5 * HW + x];
-        arg_f[1] = opw[(size_t)6 * HW + x];
-        if (C == 4) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
-          idb = opw[(size_t)11 * HW + x];
-          arg_b[0] = opw[(size_t)12 * HW + x];
-          arg_b[1] = opw[(size_t)13 * HW + x];
-        }
-        for (int g2 = 0; g2 < G; ++g2) {
-          const R kph = (R)(p.ks[lam0 + g2] * p.dir);
-          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
-          cpx<R> pb0, pb1;
-          if (C == 4) {
-            pb0 = phase_of(arg_b[0], kph) * idb;
-            pb1 = phase_of(arg_b[1], kph) * idb;
-          }
-          for (int q = 0; q < NP; ++q) {
-            const int l0 = (g2 * NP + q) * C;
-            const cpx<R>* h = tmp + (size_t)l0 * W + x;
-            cpx<R>* a = acc + (size_t)l0 * W + x;
-            if (C == 4) {
-              cpx<R> a0 = a[0], a1 = a[W], a2 = a[2 * W], a3 = a[3 * W];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * W], a0, a2);
-              apply_block<R, T>(eb, pb0, pb1, h[W], h[3 * W], a1, a3);
-              a[0] = a0; a[W] = a1; a[2 * W] = a2; a[3 * W] = a3;
-            } else {
-              cpx<R> a0 = a[0], a1 = a[W];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[W], a0, a1);
-              a[0] = a0; a[W] = a1;
-            }
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-  if (active) {
-    cpx<R> v[N2];
-    const cpx<R>* al = acc + (size_t)line * W;
-#pragma unroll
-    for (int m = 0; m < N2; ++m) v[m] = al[t + N1 * m];
-    line_fft_2step<R, N1, N2, false>(v, xl, TWREG ? trow : nullptr, tw, t);
-    cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
-#pragma unroll
-    for (int m = 0; m < N2; ++m) dst[t + N1 * m] = p.accumulate ? dst[t + N1 * m] + v[m] : v[m];
   }
 }
 

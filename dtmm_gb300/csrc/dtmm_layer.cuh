@@ -1,0 +1,106 @@
+// Types and helpers of a layer step shared by every kernel family: the
+// image grid, the row / column pass parameters and the per-voxel operator
+// application.
+//
+// Data layout in HBM
+//   field / state arrays : [image][component][H][W] interleaved complex,
+//                          image = (ray * npol + pol) * nlam + lam
+//                          (the reference's ([rays],[pols],lambda,4,H,W) order)
+//   window-row buffers   : [j][image][component][H][W]
+//   layer operators      : [ray][window][record][H][W]   (14 records)
+#pragma once
+
+#include "dtmm_common.cuh"
+
+namespace dtmm {
+
+constexpr int OP_REC = 14;  // records of one per-voxel layer operator
+
+enum KOp { KOP_NONE = 0, KOP_DIAG = 1, KOP_MAT = 2 };
+
+struct Grid {
+  int H, W;       // grid
+  int NI;         // images
+  int nlam, npol, nray;
+};
+
+__device__ __forceinline__ int img_lam(const Grid& g, int img) { return img % g.nlam; }
+__device__ __forceinline__ int img_ray(const Grid& g, int img) { return img / (g.nlam * g.npol); }
+
+// fftfreq(n)[i] * n
+__host__ __device__ __forceinline__ int fsigned(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
+
+// ---------------------------------------------------------------------------
+// Column pass of one layer step (all along ky, a tile of columns of one
+// image): forward column FFT -> k-space operator -> for each window row j:
+// cy_j * (.) -> inverse column FFT (scaled) -> U_j.
+// Input X: [image][cin][H][W] (rows already transformed along x).
+// ---------------------------------------------------------------------------
+struct ColParams {
+  int cin, cout;
+  int kop;                 // KOp
+  size_t ktab_ray_stride;  // elements between the tables of consecutive rays (0 = shared)
+  const void* ktab;        // KOP_DIAG: [lam][H][W][2]; KOP_MAT: [lam][H][W][cout][cin]
+  int ny;                  // window rows (1 = no windows)
+  const void* cy;          // [ray][j][lam][H] (null = weight 1)
+  int j_only;              // >= 0: emit only window row j_only (into U slot 0)
+  int cy_rows;             // window rows in the cy table (ray stride = cy_rows * nlam * H)
+  int do_fwd;              // 1: transform along y first (input spatial in y)
+  int inverse_out;         // 1: inverse column FFT on the way out
+  double out_scale;
+  FFTPlan plan;
+  const void* tw;          // twiddles of H
+  const int* perm;         // digit reversal of H
+  int tc;                  // columns per block
+};
+
+// ---------------------------------------------------------------------------
+// Row pass of one layer step, one row y of a group of wavelengths and
+// polarisations of one ray: for each window (i, j): cx_i * U_j -> inverse row
+// FFT -> per-voxel operator of window (i, j) -> accumulate; then forward row
+// FFT -> X.
+// ---------------------------------------------------------------------------
+struct RowParams {
+  int C;                 // 4 (Epn) or 2 (E)
+  int nx, ny;            // windows per axis (1, 1 without windows)
+  const void* cx;        // [ray][i][lam][W] (null = weight 1)
+  const int* wzero;      // [ray][nx*ny]
+  const void* op;        // [ray][win][OP_REC][H][W]
+  const double* ks;      // [lam]
+  double dir;            // propagation direction (+1 / -1)
+  double in_scale;       // 1/W of the inverse row transform (and 1/H of the column one)
+  FFTPlan plan;
+  const void* tw;
+  const int* perm;
+  int G;                 // wavelengths per block
+  int PB;                // polarisations per block
+  int win_only;          // >= 0: only this window (its own sub-step chain), -1: all
+  int use_cx;            // apply the window's beta_x weight (first sub-step of a chain)
+  int accumulate;        // add the result to X instead of overwriting it
+};
+
+template <typename R>
+__device__ __forceinline__ cpx<R> phase_of(cpx<R> arg, R k) {
+  return cexp_i(mk<R>(arg.re * k, arg.im * k));
+}
+template <typename R>
+__device__ __forceinline__ cpx<R> phase_of(R arg, R k) {
+  R s, c;
+  if constexpr (sizeof(R) == 4)
+    sincosf(arg * k, &s, &c);
+  else
+    sincos(arg * k, &s, &c);
+  return mk<R>(c, s);
+}
+
+// one 2x2 block of the per-voxel operator: out += E . diag(P') . adj(E) . h
+template <typename R, typename T>
+__device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
+                                            cpx<R>& a1) {
+  const cpx<R> w0 = (e[3] * h0 - e[1] * h1) * p0;
+  const cpx<R> w1 = (e[0] * h1 - e[2] * h0) * p1;
+  a0 = a0 + e[0] * w0 + e[1] * w1;
+  a1 = a1 + e[2] * w0 + e[3] * w1;
+}
+
+}  // namespace dtmm

@@ -1,0 +1,356 @@
+// Row and column passes of a layer step with register line transforms
+// (complex64 bulk, every side N = N1 * N2 that `reg_lanes` lists).
+//
+// Each (image, component) line is transformed by a group of N1 lanes
+// (`TwoStep`); the groups synchronise with their own lane mask, so a warp may
+// hold lines of different activity.  Work per block:
+//   row pass     one row y of G wavelengths x PB polarisations of one ray:
+//                for each window, the weighted row is inverse-transformed into
+//                the line's row buffer, the per-voxel operator accumulates into
+//                the line's accumulator, and the accumulator is transformed
+//                forward and stored (natural order throughout);
+//   column pass  TX columns x C components of one image: coalesced row loads
+//                into tile A, forward column transforms (exchange in tile B,
+//                result back in A), the diagonal k-space operator in A, then
+//                per window row j: A * cy_j -> inverse transform (exchange and
+//                result in B) -> coalesced row stores.
+//
+// The kernels are instantiated per side in separate translation units
+// (dtmm_reg_*.cu) through DTMM_REG_DEFINE; the engine reaches them through the
+// row_reg_<N> / col_reg_<N> functions declared at the end.
+#pragma once
+
+#include <type_traits>
+
+#include "dtmm_layer.cuh"
+#include "dtmm_regfft.cuh"
+
+namespace dtmm {
+
+// lanes [g * N1, g * N1 + N1) of the calling lane's group
+template <int N1>
+__device__ __forceinline__ unsigned group_mask() {
+  if constexpr (N1 >= 32) {
+    return 0xffffffffu;
+  } else {
+    const unsigned lane = threadIdx.x & 31u;
+    return ((1u << N1) - 1u) << (lane & ~(unsigned)(N1 - 1));
+  }
+}
+
+// row buffer stride (complex elements): with N1 = 4 or 8 several line groups
+// share a half-warp, and a stride of W + 4 (W + 8) puts their exchange slots
+// on disjoint banks; W is a multiple of 16 for every listed side
+__host__ __device__ constexpr int reg_row_stride(int n1, int w) { return n1 == 4 ? w + 4 : (n1 == 8 ? w + 8 : w); }
+
+template <typename R, int C, bool REAL, int N1, int N2>
+__global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
+                                                         cpx<R>* __restrict__ X) {
+  using T = typename std::conditional<REAL, R, cpx<R>>::type;
+  using TS = TwoStep<N1, N2>;
+  constexpr int W = N1 * N2;
+  constexpr int LS = reg_row_stride(N1, W);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = g.H;
+  const int ngrp = (g.nlam + p.G - 1) / p.G;
+  const int npg = (g.npol + p.PB - 1) / p.PB;
+  const int y = blockIdx.x;
+  const int pg = blockIdx.y % npg, rg = blockIdx.y / npg;
+  const int ray = rg / ngrp, grp = rg - ray * ngrp;
+  const int lam0 = grp * p.G, pol0 = pg * p.PB;
+  const int G = min(p.G, g.nlam - lam0);
+  const int NP = min(p.PB, g.npol - pol0);  // polarisations of this block
+  const int nlines = G * NP * C;
+  cpx<R>* acc = (cpx<R>*)smem_raw;                  // [lines][LS]
+  cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * LS;  // [lines][LS] exchange and transformed rows
+  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * LS;   // [W]  exp(-2 pi i e / W)
+  const int HW = H * W;
+  const int nwin = p.nx * p.ny;
+  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
+  const R sc = (R)p.in_scale;
+  __syncthreads();
+  const int line = threadIdx.x / N1, t = threadIdx.x % N1;
+  const bool active = line < nlines;
+  const unsigned gm = group_mask<N1>();
+  // the lane's twiddles W_N^(t k1) in registers when they fit
+  constexpr bool TWREG = N2 <= 16;
+  cpx<R> trow[TWREG ? N2 : 1];
+  if (TWREG) {
+#pragma unroll
+    for (int k1 = 0; k1 < (TWREG ? N2 : 1); ++k1) trow[k1] = tw[t * k1];
+  }
+  const int c = line % C, im = line / C;
+  const int gl = im / NP, pol = pol0 + im - gl * NP;
+  const int lam = lam0 + gl;
+  const int img = (ray * g.npol + pol) * g.nlam + lam;
+  cpx<R>* xl = tmp + (size_t)line * LS;
+  for (int j = 0; j < p.ny; ++j) {
+    // a single-window chain reads the one window row the column pass emitted
+    const cpx<R>* Uj = U + (size_t)(p.win_only >= 0 ? 0 : j) * g.NI * C * HW;
+    for (int i = 0; i < p.nx; ++i) {
+      const int w = i * p.ny + j;
+      if (p.win_only >= 0 && w != p.win_only) continue;
+      if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
+      if (active) {
+        const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
+        const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
+        cpx<R> v[N2];
+#pragma unroll
+        for (int m = 0; m < N2; ++m) {
+          cpx<R> a = src[t + N1 * m];
+          v[m] = cxl ? a * cxl[t + N1 * m] : a;
+        }
+        TS::template step1<R, true>(v, xl, 1, TWREG ? trow : nullptr, tw, t);
+        __syncwarp(gm);
+        cpx<R> u[TS::J][N1];
+        TS::template step2<R, true>(u, xl, 1, t);
+        __syncwarp(gm);  // every read of the exchange precedes the results that overwrite it
+        TS::template store<R>(u, xl, 1, t, sc);
+      }
+      __syncthreads();
+      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      for (int x = threadIdx.x; x < W; x += blockDim.x) {
+        T ef[4], arg_f[2], idf;
+        T eb[4], arg_b[2], idb;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
+        idf = opw[(size_t)4 * HW + x];
+        arg_f[0] = opw[(size_t)5 * HW + x];
+        arg_f[1] = opw[(size_t)6 * HW + x];
+        if (C == 4) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
+          idb = opw[(size_t)11 * HW + x];
+          arg_b[0] = opw[(size_t)12 * HW + x];
+          arg_b[1] = opw[(size_t)13 * HW + x];
+        }
+        for (int g2 = 0; g2 < G; ++g2) {
+          const R kph = (R)(p.ks[lam0 + g2] * p.dir);
+          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
+          cpx<R> pb0, pb1;
+          if (C == 4) {
+            pb0 = phase_of(arg_b[0], kph) * idb;
+            pb1 = phase_of(arg_b[1], kph) * idb;
+          }
+          for (int q = 0; q < NP; ++q) {
+            const int l0 = (g2 * NP + q) * C;
+            const cpx<R>* h = tmp + (size_t)l0 * LS + x;
+            cpx<R>* a = acc + (size_t)l0 * LS + x;
+            if (C == 4) {
+              cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
+              apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
+              a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
+            } else {
+              cpx<R> a0 = a[0], a1 = a[LS];
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
+              a[0] = a0; a[LS] = a1;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (active) {
+    cpx<R> v[N2];
+    const cpx<R>* al = acc + (size_t)line * LS;
+#pragma unroll
+    for (int m = 0; m < N2; ++m) v[m] = al[t + N1 * m];
+    TS::template step1<R, false>(v, xl, 1, TWREG ? trow : nullptr, tw, t);
+    __syncwarp(gm);
+    cpx<R> u[TS::J][N1];
+    TS::template step2<R, false>(u, xl, 1, t);
+    cpx<R>* dst = X + (((size_t)img * C + c) * H + y) * W;
+    if constexpr (TS::EVEN) {
+      TS::template to_lane_order<R>(u, v);
+#pragma unroll
+      for (int m = 0; m < N2; ++m) dst[t + N1 * m] = p.accumulate ? dst[t + N1 * m] + v[m] : v[m];
+    } else {
+      __syncwarp(gm);
+      TS::template store<R>(u, xl, 1, t, (R)1);
+      __syncwarp(gm);
+#pragma unroll
+      for (int m = 0; m < N2; ++m) {
+        const cpx<R> r = xl[t + N1 * m];
+        dst[t + N1 * m] = p.accumulate ? dst[t + N1 * m] + r : r;
+      }
+    }
+  }
+}
+
+// Column pass, k-space operator KOP_NONE or KOP_DIAG (see the file comment).
+template <typename R, int N1, int N2>
+__global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
+                                                         cpx<R>* __restrict__ U) {
+  using TS = TwoStep<N1, N2>;
+  constexpr int H = N1 * N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int W = g.W, TX = p.tc, C = p.cin;
+  const int RS = C * TX + 1;                       // tile row stride (odd)
+  cpx<R>* tileA = (cpx<R>*)smem_raw;               // [H][RS] spectra along y (kept across windows)
+  cpx<R>* tileB = tileA + (size_t)H * RS;          // [H][RS] exchange and outgoing rows
+  cpx<R>* tw = tileB + (size_t)H * RS;             // [H] exp(-2 pi i e / H)
+  const int img = blockIdx.y;
+  const int x0 = blockIdx.x * TX;
+  const int lam = img_lam(g, img), ray = img_ray(g, img);
+  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  // a half-warp covers one tile row (C x TX contiguous slots): conflict-free
+  const int CT = C * TX;
+  const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;
+  const int lcc = lc / TX, lxc = lc - lcc * TX;
+  const bool lin = (int)threadIdx.x < ystep * CT && x0 + lxc < W;
+  const cpx<R>* xsrc = X + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+  if (lin)
+    for (int y = threadIdx.x / CT; y < H; y += ystep) tileA[y * RS + lc] = xsrc[(size_t)y * W];
+  __syncthreads();
+  const int l = threadIdx.x / N1, t = threadIdx.x % N1;
+  const int nlines = C * TX;
+  const bool active = l < nlines;
+  const unsigned gm = group_mask<N1>();
+  const int c = l / TX, xc = l - c * TX;
+  const int kx = x0 + xc;
+  cpx<R>* colA = tileA + l;  // line element e at colA[e * RS]
+  cpx<R>* colB = tileB + l;
+  if (active && p.do_fwd) {
+    cpx<R> v[N2];
+#pragma unroll
+    for (int m = 0; m < N2; ++m) v[m] = colA[(t + N1 * m) * RS];
+    TS::template step1<R, false>(v, colB, RS, nullptr, tw, t);
+    __syncwarp(gm);
+    cpx<R> u[TS::J][N1];
+    TS::template step2<R, false>(u, colB, RS, t);
+    TS::template store<R>(u, colA, RS, t, (R)1);
+  }
+  if (active && p.kop == KOP_DIAG && kx < W) {
+    __syncwarp(gm);
+    const cpx<R>* e = (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H) * 2;
+    const bool fwd = ((c & 1) == 0) || C == 2;
+#pragma unroll
+    for (int m = 0; m < N2; ++m) {
+      const int k = t + N1 * m;
+      colA[k * RS] = colA[k * RS] * e[k * 2 + (fwd ? 0 : 1)];
+    }
+  }
+  const R sc = (R)p.out_scale;
+  for (int jj = 0; jj < p.ny; ++jj) {
+    const int j = p.j_only >= 0 ? p.j_only : jj;
+    __syncthreads();  // tile A complete; the previous window's stores have read tile B
+    if (active) {
+      cpx<R> v[N2];
+      const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
+#pragma unroll
+      for (int m = 0; m < N2; ++m) {
+        const cpx<R> a = colA[(t + N1 * m) * RS];
+        v[m] = cyj ? a * cyj[t + N1 * m] : a;
+      }
+      if (p.inverse_out) {
+        TS::template step1<R, true>(v, colB, RS, nullptr, tw, t);
+        __syncwarp(gm);
+        cpx<R> u[TS::J][N1];
+        TS::template step2<R, true>(u, colB, RS, t);
+        __syncwarp(gm);
+        TS::template store<R>(u, colB, RS, t, sc);
+      } else {
+#pragma unroll
+        for (int m = 0; m < N2; ++m) colB[(t + N1 * m) * RS] = v[m] * sc;
+      }
+    }
+    __syncthreads();
+    cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+    if (lin)
+      for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tileB[y * RS + lc];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch glue: one function per side, defined by DTMM_REG_DEFINE in the
+// dtmm_reg_*.cu units.  Geometry (grid, threads, shared bytes) comes from the
+// engine; a variant that is not instantiated returns cudaErrorNotSupported.
+// ---------------------------------------------------------------------------
+struct RegLaunch {
+  dim3 grid;
+  int threads;
+  size_t smem;
+  cudaStream_t st;
+};
+
+// row variants: every (C, REAL) for power-of-two sides, real records for the others
+__host__ __device__ constexpr bool reg_row_variant(int n, bool real) { return reg_lanes(n) > 0 && (real || is_pow2(n)); }
+
+template <int N1, int N2, int C, bool REAL>
+cudaError_t row_reg_variant(const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, void* X) {
+  auto kern = k_layer_row_reg<float, C, REAL, N1, N2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+  if (e != cudaSuccess) return e;
+  kern<<<L.grid, L.threads, L.smem, L.st>>>(p, g, (const cpx<float>*)U, (cpx<float>*)X);
+  return cudaGetLastError();
+}
+
+template <int N1, int N2>
+cudaError_t row_reg_launch(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U,
+                           void* X) {
+  constexpr int N = N1 * N2;
+  if (C == 4 && real) return row_reg_variant<N1, N2, 4, true>(L, p, g, U, X);
+  if (C == 2 && real) return row_reg_variant<N1, N2, 2, true>(L, p, g, U, X);
+  if constexpr (is_pow2(N)) {
+    if (C == 4) return row_reg_variant<N1, N2, 4, false>(L, p, g, U, X);
+    if (C == 2) return row_reg_variant<N1, N2, 2, false>(L, p, g, U, X);
+  }
+  return cudaErrorNotSupported;
+}
+
+template <int N1, int N2>
+cudaError_t col_reg_launch(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {
+  auto kern = k_layer_col_reg<float, N1, N2>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+  if (e != cudaSuccess) return e;
+  kern<<<L.grid, L.threads, L.smem, L.st>>>(p, g, (const cpx<float>*)in, (cpx<float>*)out);
+  return cudaGetLastError();
+}
+
+#define DTMM_REG_SIDES(X) \
+  X(64) X(80) X(96) X(112) X(128) X(144) X(160) X(192) X(224) X(240) X(256) X(288) X(320) X(336) X(384) X(400) \
+  X(432) X(448) X(480) X(512) X(1024)
+
+#define DTMM_REG_DECLARE(N)                                                                                      \
+  cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
+                          void* X);                                                                            \
+  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out);
+
+#define DTMM_REG_DEFINE(N)                                                                                       \
+  cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
+                          void* X) {                                                                           \
+    return row_reg_launch<reg_lanes(N), N / reg_lanes(N)>(C, real, L, p, g, U, X);                             \
+  }                                                                                                            \
+  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {    \
+    return col_reg_launch<reg_lanes(N), N / reg_lanes(N)>(L, p, g, in, out);                                   \
+  }
+
+DTMM_REG_SIDES(DTMM_REG_DECLARE)
+
+// dispatch on the side (cudaErrorNotSupported for a side without a transform)
+inline cudaError_t row_reg_dispatch(int n, int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g,
+                                    const void* U, void* X) {
+  switch (n) {
+#define DTMM_REG_ROW_CASE(N) \
+  case N: return row_reg_##N(C, real, L, p, g, U, X);
+    DTMM_REG_SIDES(DTMM_REG_ROW_CASE)
+#undef DTMM_REG_ROW_CASE
+    default: return cudaErrorNotSupported;
+  }
+}
+
+inline cudaError_t col_reg_dispatch(int n, const RegLaunch& L, const ColParams& p, const Grid& g, const void* in,
+                                    void* out) {
+  switch (n) {
+#define DTMM_REG_COL_CASE(N) \
+  case N: return col_reg_##N(L, p, g, in, out);
+    DTMM_REG_SIDES(DTMM_REG_COL_CASE)
+#undef DTMM_REG_COL_CASE
+    default: return cudaErrorNotSupported;
+  }
+}
+
+}  // namespace dtmm
