@@ -299,14 +299,19 @@ struct Engine {
       return fail(DTMM_ENOTSUP, "register column transform is complex64 only");
     } else {
       const int n1 = reg_lanes(d.height);
+      const size_t tiles = reg_col_tiles(d.height, p.ny);
       int tx = std::max(1, 256 / (C * n1));
-      if (d.col_tile > 0 && d.col_tile * C * n1 <= 512) tx = d.col_tile;
+      // tiles of H x (C tx + 1) complex: about 3 blocks per SM by default
+      size_t cap = tiles == 2 ? 72 * 1024 : 100 * 1024;
+      if (d.col_tile > 0 && d.col_tile * C * n1 <= 512) {
+        tx = d.col_tile;
+        cap = 160 * 1024;
+      }
       if (tx > d.width) tx = d.width;
-      // two tiles (spectra and exchange) of H x (C tx + 1) complex
-      while (tx > 1 && 2 * (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) > 160 * 1024) tx /= 2;
+      while (tx > 1 && tiles * d.height * (C * tx + 1) * sizeof(cpx<R>) > cap) tx /= 2;
       p.tc = tx;
       RegLaunch rl;
-      rl.smem = 2 * (size_t)d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
+      rl.smem = tiles * d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
       rl.threads = std::max(32, ((C * tx * n1 + 31) / 32) * 32);
       rl.grid = dim3((d.width + tx - 1) / tx, NI);
       rl.st = st;

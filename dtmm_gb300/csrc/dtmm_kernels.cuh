@@ -141,8 +141,27 @@ struct OpParams {
 // when every eigenvalue and the effective medium exceed beta^2 (then every
 // radicand of the solve is positive; the host proves this before selecting
 // the real path).  Same formulas as the complex path below.
-__device__ inline bool voxel_E_real(double beta, const double ev[3], double ie, double st, double ct, double sf,
-                                    double cf, double E[2][4], double al[4]) {
+struct VoxelInv {      // per-voxel invariants of the real-path solve
+  double ev[3];        // eps eigenvalues (o, o, e)
+  double ie;           // 1 / eps11
+  double u, iu2;       // eps11 + delta cos^2(theta), 0.5 / u
+  double st, ct;       // sin, cos of the director's polar angle
+};
+
+__device__ inline void voxel_inv(const double* e, double theta, VoxelInv& vi) {
+  vi.ev[0] = e[0];
+  vi.ev[1] = e[1];
+  vi.ev[2] = e[2];
+  sincos(theta, &vi.st, &vi.ct);
+  vi.ie = 1.0 / e[0];
+  vi.u = e[0] + (e[2] - e[0]) * (vi.ct * vi.ct);
+  vi.iu2 = 0.5 / vi.u;
+}
+
+__device__ inline bool voxel_E_real(double beta, const VoxelInv& vi, double sf, double cf, double E[2][4],
+                                    double al[4]) {
+  const double* ev = vi.ev;
+  const double st = vi.st, ct = vi.ct;
   if (ev[0] == ev[1] && ev[1] == ev[2]) {
     const double a = sqrt(ev[0] - beta * beta);
     al[0] = a; al[1] = -a; al[2] = a; al[3] = -a;
@@ -154,13 +173,13 @@ __device__ inline bool voxel_E_real(double beta, const double ev[3], double ie, 
   }
   const double cfst = cf * st, sfst = st * sf;
   const double eps11 = ev[0], delta = ev[2] - eps11;
+  const double u = vi.u, iu2 = vi.iu2;
   double ev02, evs, evpp, evpm;
   if (beta == 0.0) {
     ev02 = eps11;
     evs = sqrt(ev02);
-    const double u = eps11 + delta * (ct * ct);
     const double w = eps11 * (ev02 + delta);
-    const double sq = sqrt(u * w) / u;
+    const double sq = sqrt(u * w) * (2.0 * iu2);
     evpp = sq;
     evpm = -sq;
     E[0][0] = cf;        E[1][0] = sf;
@@ -170,21 +189,19 @@ __device__ inline bool voxel_E_real(double beta, const double ev[3], double ie, 
   } else {
     ev02 = eps11 - beta * beta;
     evs = sqrt(ev02);
-    const double u = eps11 + delta * (ct * ct);
     const double gama = beta * cf;
     const double v = delta * (gama * 2.0 * st * ct);
     const double w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
-    const double iu2 = 0.5 / u;
     const double sq = sqrt(v * v - u * w * 4.0) * iu2;
     const double vh = v * iu2;
     evpp = sq - vh;
     evpm = -vh - sq;
     const double ctbeta = ct * beta;
     const double ev02cf = ev02 * cfst;
-    E[0][0] = (evpp * ctbeta - ev02cf) * ie;  E[1][0] = -sfst;
-    E[0][1] = (ev02cf - evpm * ctbeta) * ie;  E[1][1] = sfst;
-    E[0][2] = evs * sfst;                     E[1][2] = ctbeta - evs * cfst;
-    E[0][3] = -evs * sfst;                    E[1][3] = evs * cfst + ctbeta;
+    E[0][0] = (evpp * ctbeta - ev02cf) * vi.ie;  E[1][0] = -sfst;
+    E[0][1] = (ev02cf - evpm * ctbeta) * vi.ie;  E[1][1] = sfst;
+    E[0][2] = evs * sfst;                        E[1][2] = ctbeta - evs * cfst;
+    E[0][3] = -evs * sfst;                       E[1][3] = evs * cfst + ctbeta;
   }
   al[0] = evpp; al[1] = evpm; al[2] = evs; al[3] = -evs;
   return false;
@@ -204,14 +221,12 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
   const int nrec = p.four ? OP_REC : 7;
   const size_t slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
-  // the voxel's trigonometry, shared by every window
-  double st, ct, sa, ca;
-  sincos(theta, &st, &ct);
+  // the voxel's trigonometry and invariants, shared by every ray and window
+  double sa, ca;
   sincos(azim, &sa, &ca);
   if (REAL) {
-    const double* e = (const double*)p.epsv + eo;
-    const double ev[3] = {e[0], e[1], e[2]};
-    const double ie = 1.0 / ev[0];  // 1 / eps11, shared by every ray and window
+    VoxelInv vi;
+    voxel_inv((const double*)p.epsv + eo, theta, vi);
     for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
       const double beta = p.wbeta[rw];
       const double cp = p.wcos[rw], sp = p.wsin[rw];
@@ -219,7 +234,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
       const double aw = p.waw[rw];
       double E[2][4], al[4];
-      bool zero = voxel_E_real(beta, ev, ie, st, ct, sf, cf, E, al);
+      bool zero = voxel_E_real(beta, vi, sf, cf, E, al);
       for (int m = 0; m < 4; ++m) {
         const double ex = E[0][m], ey = E[1][m];
         E[0][m] = ex * cp - ey * sp;
@@ -246,6 +261,8 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     }
     return;
   }
+  double st, ct;
+  sincos(theta, &st, &ct);
   for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
     const double beta = p.wbeta[rw];
     const double cp = p.wcos[rw], sp = p.wsin[rw];

@@ -10,10 +10,12 @@
 //                the line's accumulator, and the accumulator is transformed
 //                forward and stored (natural order throughout);
 //   column pass  TX columns x C components of one image: coalesced row loads
-//                into tile A, forward column transforms (exchange in tile B,
-//                result back in A), the diagonal k-space operator in A, then
-//                per window row j: A * cy_j -> inverse transform (exchange and
-//                result in B) -> coalesced row stores.
+//                into a tile, forward column transforms, the diagonal k-space
+//                operator, then per window row j: spectra * cy_j -> inverse
+//                transform -> coalesced row stores.  With N2 % N1 == 0 the
+//                spectra stay in registers and one tile serves as loads,
+//                exchange and stores; otherwise they stay in tile A and the
+//                exchange uses tile B (A itself for a single window row).
 //
 // The kernels are instantiated per side in separate translation units
 // (dtmm_reg_*.cu) through DTMM_REG_DEFINE; the engine reaches them through the
@@ -180,6 +182,12 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   }
 }
 
+// tiles of the column pass: N2 % N1 == 0 keeps the spectra in registers (one
+// tile); otherwise the spectra stay in tile A and, with several window rows,
+// the exchange needs tile B
+__host__ __device__ constexpr bool reg_even(int n) { return reg_lanes(n) > 0 && (n / reg_lanes(n)) % reg_lanes(n) == 0; }
+__host__ __device__ constexpr int reg_col_tiles(int n, int ny) { return (!reg_even(n) && ny > 1) ? 2 : 1; }
+
 // Column pass, k-space operator KOP_NONE or KOP_DIAG (see the file comment).
 template <typename R, int N1, int N2>
 __global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
@@ -189,9 +197,10 @@ __global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int W = g.W, TX = p.tc, C = p.cin;
   const int RS = C * TX + 1;                       // tile row stride (odd)
-  cpx<R>* tileA = (cpx<R>*)smem_raw;               // [H][RS] spectra along y (kept across windows)
-  cpx<R>* tileB = tileA + (size_t)H * RS;          // [H][RS] exchange and outgoing rows
-  cpx<R>* tw = tileB + (size_t)H * RS;             // [H] exp(-2 pi i e / H)
+  const int ntiles = reg_col_tiles(H, p.ny);
+  cpx<R>* tileA = (cpx<R>*)smem_raw;               // [H][RS] loaded rows, then spectra along y
+  cpx<R>* tileB = tileA + (size_t)(ntiles - 1) * H * RS;  // [H][RS] exchange and outgoing rows (= A with one tile)
+  cpx<R>* tw = tileA + (size_t)ntiles * H * RS;    // [H] exp(-2 pi i e / H)
   const int img = blockIdx.y;
   const int x0 = blockIdx.x * TX;
   const int lam = img_lam(g, img), ray = img_ray(g, img);
@@ -213,54 +222,106 @@ __global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, c
   const int kx = x0 + xc;
   cpx<R>* colA = tileA + l;  // line element e at colA[e * RS]
   cpx<R>* colB = tileB + l;
-  if (active && p.do_fwd) {
-    cpx<R> v[N2];
-#pragma unroll
-    for (int m = 0; m < N2; ++m) v[m] = colA[(t + N1 * m) * RS];
-    TS::template step1<R, false>(v, colB, RS, nullptr, tw, t);
-    __syncwarp(gm);
-    cpx<R> u[TS::J][N1];
-    TS::template step2<R, false>(u, colB, RS, t);
-    TS::template store<R>(u, colA, RS, t, (R)1);
-  }
-  if (active && p.kop == KOP_DIAG && kx < W) {
-    __syncwarp(gm);
-    const cpx<R>* e = (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H) * 2;
-    const bool fwd = ((c & 1) == 0) || C == 2;
-#pragma unroll
-    for (int m = 0; m < N2; ++m) {
-      const int k = t + N1 * m;
-      colA[k * RS] = colA[k * RS] * e[k * 2 + (fwd ? 0 : 1)];
-    }
-  }
+  const bool diag = active && p.kop == KOP_DIAG && kx < W;
+  const cpx<R>* ek = diag ? (const cpx<R>*)p.ktab + (((size_t)lam * W + kx) * H) * 2 + ((((c & 1) == 0) || C == 2) ? 0 : 1)
+                          : nullptr;
   const R sc = (R)p.out_scale;
-  for (int jj = 0; jj < p.ny; ++jj) {
-    const int j = p.j_only >= 0 ? p.j_only : jj;
-    __syncthreads();  // tile A complete; the previous window's stores have read tile B
+  if constexpr (TS::EVEN) {
+    // spectra in registers, lane order v[m] = X[t + N1 m]
+    cpx<R> v[N2];
     if (active) {
-      cpx<R> v[N2];
-      const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
 #pragma unroll
-      for (int m = 0; m < N2; ++m) {
-        const cpx<R> a = colA[(t + N1 * m) * RS];
-        v[m] = cyj ? a * cyj[t + N1 * m] : a;
-      }
-      if (p.inverse_out) {
-        TS::template step1<R, true>(v, colB, RS, nullptr, tw, t);
+      for (int m = 0; m < N2; ++m) v[m] = colA[(t + N1 * m) * RS];
+      __syncwarp(gm);
+      if (p.do_fwd) {
+        TS::template step1<R, false>(v, colA, RS, nullptr, tw, t);
         __syncwarp(gm);
         cpx<R> u[TS::J][N1];
-        TS::template step2<R, true>(u, colB, RS, t);
-        __syncwarp(gm);
-        TS::template store<R>(u, colB, RS, t, sc);
-      } else {
+        TS::template step2<R, false>(u, colA, RS, t);
+        TS::template to_lane_order<R>(u, v);
+      }
+      if (diag) {
 #pragma unroll
-        for (int m = 0; m < N2; ++m) colB[(t + N1 * m) * RS] = v[m] * sc;
+        for (int m = 0; m < N2; ++m) v[m] = v[m] * ek[(t + N1 * m) * 2];
       }
     }
-    __syncthreads();
-    cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
-    if (lin)
-      for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tileB[y * RS + lc];
+    for (int jj = 0; jj < p.ny; ++jj) {
+      const int j = p.j_only >= 0 ? p.j_only : jj;
+      __syncthreads();  // the previous window's stores (and the forward exchange) are done with the tile
+      if (active) {
+        const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
+        cpx<R> w[N2];
+#pragma unroll
+        for (int m = 0; m < N2; ++m) w[m] = cyj ? v[m] * cyj[t + N1 * m] : v[m];
+        if (p.inverse_out) {
+          TS::template step1<R, true>(w, colA, RS, nullptr, tw, t);
+          __syncwarp(gm);
+          cpx<R> u[TS::J][N1];
+          TS::template step2<R, true>(u, colA, RS, t);
+          __syncwarp(gm);
+          TS::template store<R>(u, colA, RS, t, sc);
+        } else {
+#pragma unroll
+          for (int m = 0; m < N2; ++m) colA[(t + N1 * m) * RS] = w[m] * sc;
+        }
+      }
+      __syncthreads();
+      cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+      if (lin)
+        for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tileA[y * RS + lc];
+    }
+  } else {
+    // spectra in tile A (natural order); exchange in tile B (tile A itself
+    // with one window row: the line is in registers before the exchange)
+    if (active && p.do_fwd) {
+      cpx<R> v[N2];
+#pragma unroll
+      for (int m = 0; m < N2; ++m) v[m] = colA[(t + N1 * m) * RS];
+      __syncwarp(gm);
+      TS::template step1<R, false>(v, colB, RS, nullptr, tw, t);
+      __syncwarp(gm);
+      cpx<R> u[TS::J][N1];
+      TS::template step2<R, false>(u, colB, RS, t);
+      __syncwarp(gm);
+      TS::template store<R>(u, colA, RS, t, (R)1);
+    }
+    if (diag) {
+      __syncwarp(gm);
+#pragma unroll
+      for (int m = 0; m < N2; ++m) {
+        const int k = t + N1 * m;
+        colA[k * RS] = colA[k * RS] * ek[k * 2];
+      }
+    }
+    for (int jj = 0; jj < p.ny; ++jj) {
+      const int j = p.j_only >= 0 ? p.j_only : jj;
+      __syncthreads();  // tile A complete; the previous window's stores have read tile B
+      if (active) {
+        cpx<R> v[N2];
+        const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
+#pragma unroll
+        for (int m = 0; m < N2; ++m) {
+          const cpx<R> a = colA[(t + N1 * m) * RS];
+          v[m] = cyj ? a * cyj[t + N1 * m] : a;
+        }
+        __syncwarp(gm);
+        if (p.inverse_out) {
+          TS::template step1<R, true>(v, colB, RS, nullptr, tw, t);
+          __syncwarp(gm);
+          cpx<R> u[TS::J][N1];
+          TS::template step2<R, true>(u, colB, RS, t);
+          __syncwarp(gm);
+          TS::template store<R>(u, colB, RS, t, sc);
+        } else {
+#pragma unroll
+          for (int m = 0; m < N2; ++m) colB[(t + N1 * m) * RS] = v[m] * sc;
+        }
+      }
+      __syncthreads();
+      cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+      if (lin)
+        for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = tileB[y * RS + lc];
+    }
   }
 }
 

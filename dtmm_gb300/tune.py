@@ -25,7 +25,9 @@ import os
 
 import numpy as np
 
-SIDES_REG = (64, 128, 256, 512, 1024)
+# sides with a register line transform (the library's reg_lanes table); for
+# sides that are not powers of two it covers real operator records only
+SIDES_REG = (64, 80, 96, 112, 128, 144, 160, 192, 224, 240, 256, 288, 320, 336, 384, 400, 432, 448, 480, 512, 1024)
 
 
 def tuning_key(plan):

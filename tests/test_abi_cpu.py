@@ -108,3 +108,23 @@ def test_planewave_rejects_invalid_arguments(lib, args, needle):
                                   ctypes.c_void_p(field), None)
     assert rc == _lib.DTMM_EINVAL
     assert needle in _lib.last_error()
+
+
+def test_tuner_knows_the_register_transform_sides():
+    """The autotuner's list of register-transform sides is the library's table."""
+    import re
+
+    from dtmm_gb300.tune import SIDES_REG
+
+    text = open(os.path.join(ROOT, "dtmm_gb300", "csrc", "dtmm_regfft.cuh")).read()
+    body = text[text.index("constexpr int reg_lanes(int n)"):]
+    body = body[:body.index("default:")]
+    sides = tuple(int(n) for n in re.findall(r"case (\d+):", body))
+    assert sides == SIDES_REG
+    macro = open(os.path.join(ROOT, "dtmm_gb300", "csrc", "dtmm_regkern.cuh")).read()
+    listed = macro[macro.index("#define DTMM_REG_SIDES(X)"):]
+    listed = listed[:listed.index("\n\n")]
+    assert tuple(int(n) for n in re.findall(r"X\((\d+)\)", listed)) == SIDES_REG
+    units = "".join(open(os.path.join(ROOT, "dtmm_gb300", "csrc", f)).read()
+                    for f in sorted(os.listdir(os.path.join(ROOT, "dtmm_gb300", "csrc"))) if f.startswith("dtmm_reg_"))
+    assert sorted(int(n) for n in re.findall(r"DTMM_REG_DEFINE\((\d+)\)", units)) == list(SIDES_REG)
