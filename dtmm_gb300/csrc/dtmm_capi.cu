@@ -141,7 +141,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     return o;
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
-  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 6 * nrw + 4 + 3 * NI + 8));
+  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
   L.part = take(sizeof(double) * std::max<size_t>(2 * kPartBlocks, 4 * kWinChunks * nrw));
   L.twH = take(L.cplx * H);
   L.permH = take(sizeof(int) * H);
@@ -247,7 +247,8 @@ struct Engine {
   template <typename T>
   T* A(size_t off) const { return (T*)(ws + off); }
 
-  // small area: ks | beta | phi | xoff | yoff | wbeta | wphi | wzero(int) | eps_eff(2) | i0 | i0f | fact
+  // small area: ks | beta | phi | xoff | yoff | wbeta | wphi | wzero(int) | wcos | wsin | waw | wev02 |
+  // wevs | wc2 | eps_eff(2) | i0 | i0f | fact
   double* ks() const { return A<double>(L.small); }
   double* rbeta() const { return ks() + d.nlam; }
   double* rphi() const { return rbeta() + d.nray; }
@@ -259,7 +260,10 @@ struct Engine {
   double* wcos() const { return (double*)(wzero()) + (size_t)d.nray * L.nwin; }
   double* wsin() const { return wcos() + (size_t)d.nray * L.nwin; }
   double* waw() const { return wsin() + (size_t)d.nray * L.nwin; }
-  double* epseff() const { return waw() + (size_t)d.nray * L.nwin; }
+  double* wev02() const { return waw() + (size_t)d.nray * L.nwin; }
+  double* wevs() const { return wev02() + (size_t)d.nray * L.nwin; }
+  double* wc2() const { return wevs() + (size_t)d.nray * L.nwin; }
+  double* epseff() const { return wc2() + (size_t)d.nray * L.nwin; }
   double* i0() const { return epseff() + 4; }
   double* i0f() const { return i0() + NI; }
   double* fact() const { return i0f() + NI; }
@@ -357,6 +361,10 @@ struct Engine {
   }
 
   bool real_ops() const { return d.real_path && !d.eps_complex; }
+  // one real eps for every voxel: the real-path solve's window constants are tables
+  bool uniform_real() const {
+    return real_ops() && d.epsv_strides[0] == 0 && d.epsv_strides[1] == 0 && d.epsv_strides[2] == 0;
+  }
 
   // wavelengths per row block: as many as fit ~100 KB of shared memory
   int row_group() const {
@@ -576,10 +584,20 @@ struct Engine {
     p.rays_per_thread = rpt;
     dim3 grid((unsigned)blocks, (unsigned)((d.nray + rpt - 1) / rpt));
     mark(PROF_OP);
-    if (real_ops())
-      k_voxel_op<R, true><<<grid, 128, 0, st>>>(p, g, op);
-    else
-      k_voxel_op<R, false><<<grid, 128, 0, st>>>(p, g, op);
+    p.wev02 = uniform_real() ? wev02() : nullptr;
+    p.wevs = wevs();
+    p.wc2 = wc2();
+    if (real_ops()) {
+      if (p.four)
+        k_voxel_op<R, true, true><<<grid, 128, 0, st>>>(p, g, op);
+      else
+        k_voxel_op<R, true, false><<<grid, 128, 0, st>>>(p, g, op);
+    } else {
+      if (p.four)
+        k_voxel_op<R, false, true><<<grid, 128, 0, st>>>(p, g, op);
+      else
+        k_voxel_op<R, false, false><<<grid, 128, 0, st>>>(p, g, op);
+    }
     mark(PROF_OP);
     CKL("k_voxel_op");
     return DTMM_OK;
@@ -640,7 +658,9 @@ struct Engine {
       k_sincos<<<(d.nray + 127) / 128, 128, 0, st>>>(wphi(), wcos(), wsin(), d.nray);
       CKL("k_sincos");
     }
-    k_window_aw<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(wbeta(), epseff(), waw(), L.nwin * d.nray);
+    k_window_aw<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(wbeta(), epseff(), waw(), L.nwin * d.nray,
+                                                              uniform_real() ? (const double*)d.epsv : nullptr,
+                                                              wev02(), wevs(), wc2());
     CKL("k_window_aw");
     return DTMM_OK;
   }

@@ -132,6 +132,11 @@ struct OpParams {
   int four;              // 1: 4x4 (both blocks), 0: 2x2 (forward block)
   int rays_per_thread;   // rays [blockIdx.y * rays_per_thread, ...) share the voxel's trigonometry
   int nray;
+  // real path with one eps for every voxel: per (ray, window) eps11 - beta^2,
+  // its square root and eps11 (eps11 - beta^2 + delta) (null otherwise)
+  const double* wev02;
+  const double* wevs;
+  const double* wc2;
 };
 
 // Records per voxel and window, [ray][window][record][H][W]: complex, or real
@@ -146,68 +151,79 @@ struct VoxelInv {      // per-voxel invariants of the real-path solve
   double ie;           // 1 / eps11
   double u, iu2;       // eps11 + delta cos^2(theta), 0.5 / u
   double st, ct;       // sin, cos of the director's polar angle
+  double kv, kw;       // 2 delta sin(theta) cos(theta), delta sin^2(theta)
+  bool iso;
 };
 
 __device__ inline void voxel_inv(const double* e, double theta, VoxelInv& vi) {
   vi.ev[0] = e[0];
   vi.ev[1] = e[1];
   vi.ev[2] = e[2];
+  vi.iso = e[0] == e[1] && e[1] == e[2];
   sincos(theta, &vi.st, &vi.ct);
+  const double delta = e[2] - e[0];
   vi.ie = 1.0 / e[0];
-  vi.u = e[0] + (e[2] - e[0]) * (vi.ct * vi.ct);
+  vi.u = e[0] + delta * (vi.ct * vi.ct);
   vi.iu2 = 0.5 / vi.u;
+  vi.kv = delta * (2.0 * vi.st * vi.ct);
+  vi.kw = delta * (vi.st * vi.st);
 }
 
-__device__ inline bool voxel_E_real(double beta, const VoxelInv& vi, double sf, double cf, double E[2][4],
-                                    double al[4]) {
-  const double* ev = vi.ev;
+// Uniaxial / isotropic E rows (Ex, Ey of the four modes) and eigenvalues in
+// real FP64 arithmetic (dtmm/tmm.py:157-278), valid when every eigenvalue
+// and the effective medium exceed beta^2 (the host proves this before
+// selecting the real path).  ev02 = eps11 - beta^2, evs = sqrt(ev02) and
+// c2 = eps11 (ev02 + delta) come from the caller.  Without FOUR only the
+// forward modes 0 and 2 are formed.
+template <bool FOUR>
+__device__ __forceinline__ bool voxel_E_real(double beta, const VoxelInv& vi, double ev02, double evs, double c2,
+                                             double sf, double cf, double E[2][4], double al[4]) {
   const double st = vi.st, ct = vi.ct;
-  if (ev[0] == ev[1] && ev[1] == ev[2]) {
-    const double a = sqrt(ev[0] - beta * beta);
+  if (vi.iso) {
+    const double a = evs;  // sqrt(eps - beta^2)
     al[0] = a; al[1] = -a; al[2] = a; al[3] = -a;
     E[0][0] = 0.5; E[1][0] = 0.0;
-    E[0][1] = 0.5; E[1][1] = 0.0;
     E[0][2] = 0.0; E[1][2] = 0.5;
-    E[0][3] = 0.0; E[1][3] = 0.5;
+    if (FOUR) {
+      E[0][1] = 0.5; E[1][1] = 0.0;
+      E[0][3] = 0.0; E[1][3] = 0.5;
+    }
     return a == 0.0;
   }
   const double cfst = cf * st, sfst = st * sf;
-  const double eps11 = ev[0], delta = ev[2] - eps11;
-  const double u = vi.u, iu2 = vi.iu2;
-  double ev02, evs, evpp, evpm;
+  double evpp, evpm;
   if (beta == 0.0) {
-    ev02 = eps11;
-    evs = sqrt(ev02);
-    const double w = eps11 * (ev02 + delta);
-    const double sq = sqrt(u * w) * (2.0 * iu2);
+    const double sq = sqrt(vi.u * c2) * (2.0 * vi.iu2);
     evpp = sq;
     evpm = -sq;
     E[0][0] = cf;        E[1][0] = sf;
-    E[0][1] = cf;        E[1][1] = sf;
     E[0][2] = -evs * sf; E[1][2] = evs * cf;
-    E[0][3] = -evs * sf; E[1][3] = evs * cf;
+    if (FOUR) {
+      E[0][1] = cf;        E[1][1] = sf;
+      E[0][3] = -evs * sf; E[1][3] = evs * cf;
+    }
   } else {
-    ev02 = eps11 - beta * beta;
-    evs = sqrt(ev02);
     const double gama = beta * cf;
-    const double v = delta * (gama * 2.0 * st * ct);
-    const double w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
-    const double sq = sqrt(v * v - u * w * 4.0) * iu2;
-    const double vh = v * iu2;
+    const double v = vi.kv * gama;
+    const double w = vi.kw * (gama * gama) - c2;
+    const double sq = sqrt(v * v - vi.u * w * 4.0) * vi.iu2;
+    const double vh = v * vi.iu2;
     evpp = sq - vh;
     evpm = -vh - sq;
     const double ctbeta = ct * beta;
     const double ev02cf = ev02 * cfst;
     E[0][0] = (evpp * ctbeta - ev02cf) * vi.ie;  E[1][0] = -sfst;
-    E[0][1] = (ev02cf - evpm * ctbeta) * vi.ie;  E[1][1] = sfst;
     E[0][2] = evs * sfst;                        E[1][2] = ctbeta - evs * cfst;
-    E[0][3] = -evs * sfst;                       E[1][3] = evs * cfst + ctbeta;
+    if (FOUR) {
+      E[0][1] = (ev02cf - evpm * ctbeta) * vi.ie;  E[1][1] = sfst;
+      E[0][3] = -evs * sfst;                       E[1][3] = evs * cfst + ctbeta;
+    }
   }
   al[0] = evpp; al[1] = evpm; al[2] = evs; al[3] = -evs;
   return false;
 }
 
-template <typename R, bool REAL>
+template <typename R, bool REAL, bool FOUR>
 __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int HW = g.H * g.W;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,12 +235,12 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
   const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
   if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
-  const int nrec = p.four ? OP_REC : 7;
+  constexpr int nrec = FOUR ? OP_REC : 7;
   const size_t slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
   // the voxel's trigonometry and invariants, shared by every ray and window
   double sa, ca;
   sincos(azim, &sa, &ca);
-  if (REAL) {
+  if constexpr (REAL) {
     VoxelInv vi;
     voxel_inv((const double*)p.epsv + eo, theta, vi);
     for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
@@ -233,30 +249,48 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       // cos / sin of (azimuth - phi) by the angle-difference identities
       const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
       const double aw = p.waw[rw];
+      double ev02, evs, c2;
+      if (p.wev02 != nullptr) {
+        ev02 = p.wev02[rw];
+        evs = p.wevs[rw];
+        c2 = p.wc2[rw];
+      } else {
+        ev02 = vi.ev[0] - beta * beta;
+        evs = sqrt(ev02);
+        c2 = vi.ev[0] * (ev02 + (vi.ev[2] - vi.ev[0]));
+      }
       double E[2][4], al[4];
-      bool zero = voxel_E_real(beta, vi, sf, cf, E, al);
+      bool zero = voxel_E_real<FOUR>(beta, vi, ev02, evs, c2, sf, cf, E, al);
+      // back to the lab frame: rotate the E rows by the beam azimuth phi
+#pragma unroll
       for (int m = 0; m < 4; ++m) {
+        if (!FOUR && (m & 1)) continue;
         const double ex = E[0][m], ey = E[1][m];
         E[0][m] = ex * cp - ey * sp;
         E[1][m] = ex * sp + ey * cp;
       }
       const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
-      const double detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
-      if (detf == 0.0 || (p.four && detb == 0.0)) zero = true;
-      double rec[OP_REC];
+      double detb = 1.0;
+      if (FOUR) detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
+      if (detf == 0.0 || detb == 0.0) zero = true;
+      double rec[nrec];
       if (zero) {
-        for (int i = 0; i < OP_REC; ++i) rec[i] = 0.0;
+#pragma unroll
+        for (int i = 0; i < nrec; ++i) rec[i] = 0.0;
       } else {
         rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
         rec[4] = 1.0 / detf;
         rec[5] = (al[0] - aw) * p.d;
         rec[6] = (al[2] - aw) * p.d;
-        rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
-        rec[11] = p.four ? 1.0 / detb : 0.0;
-        rec[12] = (al[1] + aw) * p.d;
-        rec[13] = (al[3] + aw) * p.d;
+        if (FOUR) {
+          rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
+          rec[11] = 1.0 / detb;
+          rec[12] = (al[1] + aw) * p.d;
+          rec[13] = (al[3] + aw) * p.d;
+        }
       }
       R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
+#pragma unroll
       for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
     }
     return;
@@ -352,7 +386,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   cpx<double> detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
   const bool zf = (detf.re == 0.0 && detf.im == 0.0);
   const bool zb = (detb.re == 0.0 && detb.im == 0.0);
-  if (zf || (p.four && zb)) zero = true;
+  if (zf || (FOUR && zb)) zero = true;
   cpx<double> rec[OP_REC];
   if (zero) {
     for (int i = 0; i < OP_REC; ++i) rec[i] = z0;
@@ -361,7 +395,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     rec[4] = cdiv(mk<double>(1.0, 0.0), detf);
     rec[5] = (al[0] - aw) * p.d;
     rec[6] = (al[2] - aw) * p.d;
-    if (p.four) {
+    if (FOUR) {
       rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
       rec[11] = cdiv(mk<double>(1.0, 0.0), detb);
       rec[12] = (al[1] + aw) * p.d;
@@ -1181,9 +1215,20 @@ __global__ void k_eps_final(const double* part, int blocks, long long n, double*
 }
 
 // sqrt(eps_eff - beta_w^2) per window (real path)
-__global__ void k_window_aw(const double* wbeta, const double* eps_eff, double* aw, int n) {
+// per (ray, window): a_w = sqrt(eps_eff - beta^2); with one real eps for
+// every voxel (e0 = its first voxel) also eps11 - beta^2, its square root and
+// eps11 (eps11 - beta^2 + delta), the window constants of the real-path solve
+__global__ void k_window_aw(const double* wbeta, const double* eps_eff, double* aw, int n, const double* e0,
+                            double* ev02, double* evs, double* c2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) aw[i] = sqrt(eps_eff[0] - wbeta[i] * wbeta[i]);
+  if (i >= n) return;
+  aw[i] = sqrt(eps_eff[0] - wbeta[i] * wbeta[i]);
+  if (e0 != nullptr) {
+    const double v = e0[0] - wbeta[i] * wbeta[i];
+    ev02[i] = v;
+    evs[i] = sqrt(v);
+    c2[i] = e0[0] * (v + (e0[2] - e0[0]));
+  }
 }
 
 // Per-call host scalars travel as kernel arguments (captured by value in a
