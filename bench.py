@@ -454,6 +454,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrival rate (req/s)")
     ap.add_argument("--slots", type=int, default=16, help="serve: concurrent request slots")
     ap.add_argument("--hbm-budget", type=float, default=150e9, help="serve: admission budget (bytes)")
+    ap.add_argument("--no-batch", action="store_true", help="precision workload: skip the batch summary")
+    ap.add_argument("--no-serve", action="store_true", help="precision workload: skip the serving summary")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -610,6 +612,29 @@ def main():
         result["e2e"] = {"value": upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": fbytes + mat_bytes,
                          "d2h_bytes_per_step": 2 * fbytes, "ms_per_step": e2e_s * 1e3}
 
+    # the batching and serving configurations, summarised on the same line
+    if rank == 0 and not args.no_batch:
+        import copy
+
+        a2 = copy.copy(args)
+        a2.steps, a2.warmup, a2.c128_subset = 2, 1, 4
+        try:
+            b = run_batch(a2, dev)
+            result["batch"] = {k: b[k] for k in ("value", "ms_per_step", "config", "roofline", "gpu_launches",
+                                                  "clocks", "updates_per_step", "e2e", "c128") if k in b}
+            result["batch"]["graph_speedup_vs_serial"] = b["graph"]["graph_speedup_vs_serial"]
+        except Exception as e:  # reported, not fatal for the headline line
+            result["batch"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_serve:
+        try:
+            sv = run_serve(args, dev)
+            result["serve"] = {k: sv[k] for k in ("value", "unit", "config", "latency_ms", "queue_ms",
+                                                   "requests_per_s", "offered_updates_per_s", "peak_active",
+                                                   "peak_budget_bytes", "clocks") if k in sv}
+        except Exception as e:
+            result["serve"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu and world == 1:
         rate, cores, dt = cpu_sample_rate()
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
