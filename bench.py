@@ -421,10 +421,11 @@ def run_serve(args, dev):
         "metric": METRIC, "value": st["updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
         "ms_per_step": st["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64", "data": "synthetic",
-        "config": {"workload": "serving: Poisson stream of %d 4x4 transfer_field requests at %g req/s (diffraction 1,"
-                               " npass 1, normal incidence, x+y polarisation), grids log-uniform 64-512, 20-120 "
-                               "layers, 1-9 wavelengths, twisted nematic built on the device, complex64 bulk + FP64 "
-                               "eigen-solve; continuous batching over %d stream slots, %g GB HBM admission budget"
+        "config": {"workload": "serving: Poisson stream of %d POM simulation requests at %g req/s, each a 4x4 "
+                               "transfer_field (diffraction 1, npass 1, normal incidence, x+y polarisation) and its "
+                               "crossed-polarizer sRGB image, grids log-uniform 64-512, 20-120 layers, 1-9 "
+                               "wavelengths, twisted nematic built on the device, complex64 bulk + FP64 eigen-solve; "
+                               "continuous batching over %d stream slots, %g GB HBM admission budget"
                                % (args.requests, args.rate, args.slots, args.hbm_budget / 1e9),
                    "requests": args.requests, "rate": args.rate, "slots": args.slots,
                    "hbm_budget_bytes": args.hbm_budget},

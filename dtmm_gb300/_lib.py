@@ -20,7 +20,8 @@ PRECISION_MIXED = 0
 PRECISION_DOUBLE = 1
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
-               "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field")
+               "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field", "dtmm_pom_field",
+               "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image")
 ABI_VERSION = 2
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -57,6 +58,20 @@ class TransferDesc(ctypes.Structure):
         ("row_group", ctypes.c_int),
         ("col_tile", ctypes.c_int),
         ("fft_schedule", ctypes.c_int),
+    ]
+
+
+class PomDesc(ctypes.Structure):
+    _fields_ = [
+        ("height", ctypes.c_int),
+        ("width", ctypes.c_int),
+        ("nlam", ctypes.c_int),
+        ("nset", ctypes.c_int),
+        ("npol", ctypes.c_int),
+        ("jvec", ctypes.c_double * 4),
+        ("pmat", ctypes.c_void_p),
+        ("window", ctypes.c_void_p),
+        ("precision", ctypes.c_int),
     ]
 
 
@@ -120,6 +135,17 @@ def load(build_if_missing=True):
     lib.dtmm_planewave_field.restype = ctypes.c_int
     lib.dtmm_planewave_field.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dtmm_pom_field.restype = ctypes.c_int
+    lib.dtmm_pom_field.argtypes = [ctypes.POINTER(PomDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dtmm_field2specter.restype = ctypes.c_int
+    lib.dtmm_field2specter.argtypes = [ctypes.c_int] * 6 + [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dtmm_specter2color.restype = ctypes.c_int
+    lib.dtmm_specter2color.argtypes = [ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    lib.dtmm_pom_image.restype = ctypes.c_int
+    lib.dtmm_pom_image.argtypes = [ctypes.POINTER(PomDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     if lib.dtmm_abi_version() != ABI_VERSION:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib

@@ -999,6 +999,10 @@ int static_scratch(void** out) {
 
 }  // namespace
 
+namespace dtmm {
+std::string& last_error_slot() { return g_err; }
+}
+
 extern "C" {
 
 int dtmm_abi_version(void) { return 2; }

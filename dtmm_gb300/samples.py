@@ -196,3 +196,39 @@ def spec_updates(spec, npol=2):
     nray = 1 if np.ndim(spec["beta"]) == 0 else len(spec["beta"])
     h, w = spec["shape"]
     return h * w * spec["nlayers"] * len(spec["wavelengths"]) * nray * npol
+
+
+# ---------------------------------------------------------------------------
+# colour matching for synthetic POM images
+# ---------------------------------------------------------------------------
+def _lobe(x, mu, s1, s2):
+    s = np.where(x < mu, s1, s2)
+    return np.exp(-0.5 * ((x - mu) / s) ** 2)
+
+
+def analytic_cmf(wavelengths):
+    """CIE 1931 2-degree colour matching functions (x, y, z) at ``wavelengths``
+    (nm) from the multi-lobe piecewise-Gaussian fit of Wyman, Sloan and
+    Shirley, "Simple Analytic Approximations to the CIE XYZ Color Matching
+    Functions", JCGT 2(2), 2013."""
+    x = np.asarray(wavelengths, np.float64)
+    xb = 1.056 * _lobe(x, 599.8, 37.9, 31.0) + 0.362 * _lobe(x, 442.0, 16.0, 26.7) - 0.065 * _lobe(x, 501.1, 20.4, 26.2)
+    yb = 0.821 * _lobe(x, 568.8, 46.9, 40.5) + 0.286 * _lobe(x, 530.9, 16.3, 31.1)
+    zb = 1.217 * _lobe(x, 437.0, 11.8, 36.0) + 0.681 * _lobe(x, 459.0, 26.0, 13.8)
+    return np.stack([xb, yb, zb], axis=-1)
+
+
+def transmission_cmf(wavelengths):
+    """Transmission colour matching function [n, 3] for an equal-energy
+    illuminant sampled at ``wavelengths``: ``analytic_cmf`` weighted by each
+    sample's share of the band and scaled so that unit transmission gives
+    Y = 1 (the role of dtmm.color.load_tcmf for synthetic images)."""
+    wl = np.asarray(wavelengths, np.float64)
+    if wl.size == 1:
+        w = np.ones(1)
+    else:
+        edges = np.concatenate([[wl[0] - 0.5 * (wl[1] - wl[0])], 0.5 * (wl[1:] + wl[:-1]),
+                                [wl[-1] + 0.5 * (wl[-1] - wl[-2])]])
+        w = np.diff(edges)
+    cmf = analytic_cmf(wl) * w[:, None]
+    return cmf / cmf[:, 1].sum()

@@ -12,7 +12,9 @@ layer count and wavelength set) arrive over time.  A single host loop
   field (``illumination_device``) and the bound plan, whose launch shapes
   come from the autotuner's cache -- nothing that grows with the grid is
   computed on the host or copied from it;
-* enqueues the transfer behind that on the same stream and records an event;
+* enqueues the transfer behind that on the same stream, then the request's
+  POM image (x polarizer, crossed analyzer, ``pom.pom_image``), and records an
+  event;
 * retires finished requests (event query, no blocking), frees their memory
   and slot, and records each latency (finish - arrival).
 
@@ -31,7 +33,8 @@ from .transfer import plan_transfer, workspace_bytes
 
 
 class Request:
-    __slots__ = ("rid", "spec", "arrival", "admitted", "finished", "footprint", "updates", "result", "_state")
+    __slots__ = ("rid", "spec", "arrival", "admitted", "finished", "footprint", "updates", "result", "image",
+                 "_state")
 
     def __init__(self, rid, spec, arrival):
         self.rid = int(rid)
@@ -42,6 +45,7 @@ class Request:
         self.footprint = 0
         self.updates = 0
         self.result = None
+        self.image = None
         self._state = None
 
     @property
@@ -60,7 +64,7 @@ class TransferServer:
     """Admit, overlap and retire transfer requests under an HBM budget."""
 
     def __init__(self, precision="mixed", hbm_budget=150e9, max_active=16, tuner=None, device=None,
-                 keep_results=False, npol=2, poll_s=2e-4, **options):
+                 keep_results=False, npol=2, poll_s=2e-4, pom=True, **options):
         import torch
 
         self.device = device or torch.device("cuda", torch.cuda.current_device())
@@ -74,6 +78,14 @@ class TransferServer:
         self.options = dict(method="4x4", diffraction=1, npass=1)
         self.options.update(options)
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(self.max_active)]
+        # POM image of every request: x polarizer on the x / y inputs, crossed
+        # (y) analyzer, equal-energy transmission colour matching
+        self.pom = bool(pom) and self.npol == 2
+        if self.pom:
+            from .pom import jonesvec, polarizer, ray_jonesmat4x4
+
+            self.pom_jvec = jonesvec((1, 0))
+            self.pom_pmat = ray_jonesmat4x4(polarizer(jonesvec((0, 1))))
         self.stats = {}
 
     # -- sizes -----------------------------------------------------------
@@ -110,15 +122,22 @@ class TransferServer:
                 self.tuner.tune(plan)
             fout = torch.empty_like(fin)
             plan.run(fin, fout, stream=s.cuda_stream)
+            image = None
+            if self.pom:
+                from .pom import pom_image
+
+                image = pom_image(fout, samples.transmission_cmf(spec["wavelengths"]), self.pom_jvec, self.pom_pmat,
+                                  stream=s.cuda_stream)
             done = torch.cuda.Event()
             done.record(s)
         req.updates = plan.updates
-        req._state = (plan, mat, fin, fout, done, slot)
+        req._state = (plan, mat, fin, fout, image, done, slot)
 
     def _finish(self, req):
-        plan, mat, fin, fout, done, slot = req._state
+        plan, mat, fin, fout, image, done, slot = req._state
         if self.keep_results:
             req.result = fout.cpu()
+            req.image = image.cpu() if image is not None else None
         req._state = None
         return slot
 
@@ -145,7 +164,7 @@ class TransferServer:
             progressed = False
             still = []
             for r in active:
-                if r._state[4].query():
+                if r._state[5].query():
                     r.finished = time.perf_counter() - t0
                     free.append(self._finish(r))
                     used -= r.footprint

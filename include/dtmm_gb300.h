@@ -106,7 +106,7 @@ typedef struct dtmm_kernel_times {
   int total_launches;      /* every kernel launched by the call                                          */
 } dtmm_kernel_times;
 
-/* ABI version of this header (2: tuning fields in dtmm_transfer_desc, dtmm_planewave_field). */
+/* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */
@@ -171,6 +171,45 @@ int dtmm_transfer_noalloc(const dtmm_transfer_desc* desc, const dtmm_transfer_io
    host (dtmm_gb300.illumination.illumination_modes). */
 int dtmm_planewave_field(int height, int width, int nimg, const void* coef, const int* my, const int* mx,
                          int precision, void* field, void* stream);
+
+/* ------------------------------------------------------------------------
+   POM image formation on transferred fields (dtmm's field viewer pipeline).
+   Fields are device arrays of complex64 (precision MIXED) or complex128
+   (DOUBLE), [set][pol][lam][4][H][W] with npol == 2 (x / y inputs combined
+   with the polarizer jones vector) or [set][lam][4][H][W] with npol == 1.
+   ------------------------------------------------------------------------ */
+typedef struct {
+  int height, width;
+  int nlam;              /* wavelengths */
+  int nset;              /* leading image sets (e.g. rays), summed by the image */
+  int npol;              /* 2: combine the x / y input axis with jvec; 1: no such axis */
+  double jvec[4];        /* polarizer jones vector (re0, im0, re1, im1), npol == 2 */
+  const void* pmat;      /* device complex128 4x4 analyzer matrix for every pixel, or null */
+  const double* window;  /* device H x W real window, or null */
+  int precision;         /* field type */
+} dtmm_pom_desc;
+
+/* calculate_pom_field (dtmm/field_viewer.py:70-143), real-space path
+   without refocus: out[set][lam][4][H][W] = pmat . (window * (j0 Fx + j1 Fy)). */
+int dtmm_pom_field(const dtmm_pom_desc* desc, const void* field, void* out, void* stream);
+
+/* field2specter / field2spectersum (dtmm/field.py:784-847): normal Poynting
+   component Re(f0 f1*) - Re(f2 f3*) of [set][lam][4][H][W] fields, written
+   as spec[set][H][W][lam] (float64), or summed over the sets when sum_sets. */
+int dtmm_field2specter(int height, int width, int nlam, int nset, int sum_sets, int precision, const void* field,
+                       double* spec, void* stream);
+
+/* specter2color (dtmm/color.py:133-224): spec[npix][nlam] (float64) times
+   cmf[nlam][3] (float64) -> XYZ; norm_mode 0 = none, 1 = divide by
+   norm_value, 2 = divide by the image maximum; sRGB (D65) or gray (Y);
+   gamma 0 = none, < 0 = sRGB curve, > 0 = power 1/gamma; rgb[npix][3] float64. */
+int dtmm_specter2color(long long npix, int nlam, const double* spec, const double* cmf, int norm_mode,
+                       double norm_value, double gamma, int gray, double* rgb, void* stream);
+
+/* The three steps fused, one pass over the field: rgb[H][W][3] float32 of
+   the sets' summed specter (norm_mode, gamma, gray as above). */
+int dtmm_pom_image(const dtmm_pom_desc* desc, const void* field, const double* cmf, int norm_mode,
+                   double norm_value, double gamma, int gray, float* rgb, void* stream);
 
 #ifdef __cplusplus
 }

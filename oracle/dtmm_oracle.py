@@ -1230,3 +1230,167 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
                             diffraction, reflection, multiray, norm, smooth, betamax, ret_bulk, out)
     return transfer_2x2((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
                         diffraction, reflection, multiray, betamax, ret_bulk, out)
+
+
+# ---------------------------------------------------------------------------
+# POM image formation (the consumer of transfer_field's output)
+# ---------------------------------------------------------------------------
+def rotation_matrix2(angle):
+    """2D rotation matrix [[c, -s], [s, c]] (dtmm/rotation.py:64-76)."""
+    angle = np.asarray(angle, FDTYPE)
+    c, s = np.cos(angle), np.sin(angle)
+    out = np.empty(c.shape + (2, 2), FDTYPE)
+    out[..., 0, 0] = c
+    out[..., 1, 1] = c
+    out[..., 0, 1] = -s
+    out[..., 1, 0] = s
+    return out
+
+
+def jonesvec(pol, phi=0.0):
+    """Normalised jones vector, viewed in a frame rotated by phi (dtmm/jones.py:55-102)."""
+    pol = np.asarray(pol, CDTYPE)
+    norm = (pol[..., 0] * pol[..., 0].conj() + pol[..., 1] * pol[..., 1].conj()) ** 0.5
+    pol = np.asarray(pol / norm[..., None], CDTYPE)
+    r = rotation_matrix2(-np.asarray(phi))
+    return np.einsum("...ij,...j->...i", r, pol)
+
+
+def polarizer(jones):
+    """Jones polarizer matrix |j><j| (dtmm/jones.py:236-275)."""
+    jones = np.asarray(jones)
+    c, s = jones[..., 0], jones[..., 1]
+    out = np.empty(jones.shape + (2,), CDTYPE)
+    out[..., 0, 0] = c * c.conj()
+    out[..., 0, 1] = c * s.conj()
+    out[..., 1, 0] = s * c.conj()
+    out[..., 1, 1] = s * s.conj()
+    return out
+
+
+def rotated_matrix(jmat, phi):
+    """R^T . jmat . R with R = rotation_matrix2(phi) (dtmm/jones.py:346-369)."""
+    r = np.asarray(rotation_matrix2(phi), CDTYPE)
+    rT = np.swapaxes(r, -1, -2)
+    return np.einsum("...ij,...jk,...kl->...il", rT, np.asarray(jmat), r)
+
+
+def as4x4(jmat):
+    """Jones 2x2 -> eigenfield 4x4: jmat on forward modes, conj(jmat) on backward (dtmm/jones.py:371-398)."""
+    jmat = np.asarray(jmat)
+    out = np.zeros(jmat.shape[:-2] + (4, 4), jmat.dtype)
+    out[..., 0::2, 0::2] = jmat
+    out[..., 1::2, 1::2] = np.conj(jmat)
+    return out
+
+
+def normalize_f(fmat):
+    """Scale the columns of a field matrix to unit |Poynting| (dtmm/tmm.py:701-724)."""
+    fmat = np.asarray(fmat, CDTYPE)
+    p = np.abs((fmat[..., 0, :].real * fmat[..., 1, :].real + fmat[..., 0, :].imag * fmat[..., 1, :].imag)
+               - (fmat[..., 2, :].real * fmat[..., 3, :].real + fmat[..., 2, :].imag * fmat[..., 3, :].imag)) ** 0.5
+    n = np.where(p == 0.0, 0.0, 1.0 / np.where(p == 0.0, 1.0, p))
+    return fmat * n[..., None, :]
+
+
+def jonesmat4x4(jmat, fmat):
+    """F . as4x4(jmat) . F^-1 with F column-normalised (dtmm/jones4.py:75-104)."""
+    fmat = normalize_f(fmat)
+    return dotmm(fmat, dotmm(as4x4(jmat), inv(fmat)))
+
+
+def ray_jonesmat4x4(jmat, beta=0.0, phi=0.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0)):
+    """Jones matrix as a 4x4 field matrix in the laboratory frame (dtmm/jones4.py:205-240)."""
+    alpha, f = alphaf(beta, phi, np.asarray(epsv, CDTYPE), np.asarray(epsa, FDTYPE))
+    return jonesmat4x4(rotated_matrix(jmat, phi), f)
+
+
+def calculate_pom_field(field, jvec=None, pmat=None, dmat=None, window=None):
+    """Polarizer, refocus, analyzer on a transferred field, real-space path
+    (dtmm/field_viewer.py:70-143 with input_fft = output_fft = False):
+    combine the x / y input polarisations with the polarizer jones vector,
+    diffract (dtmm/diffract.py:254-299: fft2, optional per-k matrix, ifft2,
+    optional window), then apply the analyzer matrix per pixel."""
+    field = np.asarray(field)
+    if jvec is not None:
+        if field.shape[-5] != 2:
+            raise ValueError("Invalid field shape.")
+        c, s = jvec
+        field = field[..., 0, :, :, :, :] * c + field[..., 1, :, :, :, :] * s
+    f = fft2(field)
+    if dmat is not None:
+        f = dotmf(dmat, f)
+    out = ifft2(f)
+    if window is not None:
+        out = out * window
+    if pmat is not None:
+        # one matrix for every pixel: dotmf broadcasts it over the grid (broadcast_m, dtmm/linalg.py:967-991)
+        out = np.einsum("...ij,...jhw->...ihw", np.asarray(pmat, CDTYPE), out)
+    return out
+
+
+def field2specter(field):
+    """Normal Poynting component per pixel and wavelength: [..., λ, 4, H, W] ->
+    [..., H, W, λ] (dtmm/field.py:784-808, :824-843)."""
+    f = np.asarray(field)
+    s = (f[..., 0, :, :].real * f[..., 1, :, :].real + f[..., 0, :, :].imag * f[..., 1, :, :].imag) - (
+        f[..., 2, :, :].real * f[..., 3, :, :].real + f[..., 2, :, :].imag * f[..., 3, :, :].imag)
+    return np.moveaxis(s, -3, -1)
+
+
+def field2spectersum(field):
+    """field2specter summed over the leading axis (dtmm/field.py:810-822, :845-847)."""
+    return field2specter(field).sum(axis=-4)
+
+
+XYZ2RGBD65 = np.array([[3.2404542, -1.5371385, -0.4985314],
+                       [-0.9692660, 1.8760108, 0.0415560],
+                       [0.0556434, -0.2040259, 1.0572252]])
+
+
+def spec2xyz(spec, cmf):
+    """sum_i cmf[i, j] spec[i] (dtmm/color.py:112-131)."""
+    return np.einsum("...i,ij->...j", np.asarray(spec, FDTYPE), np.asarray(cmf, FDTYPE))
+
+
+def xyz2srgb(xyz):
+    """Linear sRGB (D65 white) from XYZ (dtmm/color.py:87-99)."""
+    return np.einsum("kj,...j->...k", XYZ2RGBD65, xyz)
+
+
+def xyz2gray(xyz):
+    """(Y, Y, Y) (dtmm/color.py:101-110)."""
+    y = xyz[..., 1]
+    return np.stack([y, y, y], axis=-1)
+
+
+def apply_srgb_gamma(v):
+    """sRGB transfer curve with clipping to [0, 1] (dtmm/color.py:70-85)."""
+    v = np.asarray(v, FDTYPE)
+    lin = np.where(v < 0.0, 0.0, 12.92 * v)
+    pw = np.where(v > 1.0, 1.0, (1 + 0.055) * np.maximum(v, 0.0) ** (1 / 2.4) - 0.055)
+    return np.where(v < 0.0031308, lin, pw)
+
+
+def apply_gamma(v, gamma):
+    """Power-law transfer curve with clipping to [0, 1] (dtmm/color.py:52-68)."""
+    v = np.asarray(v, FDTYPE)
+    return np.where(v > 1.0, 1.0, np.where(v < 0, 0.0, np.maximum(v, 0.0) ** (1.0 / gamma)))
+
+
+def specter2color(spec, cmf, norm=False, gamma=True, gray=False):
+    """Specter -> XYZ -> (normalise) -> sRGB or gray -> transfer curve (dtmm/color.py:133-224)."""
+    cmf = np.asarray(cmf)
+    if cmf.shape[-1] != 3:
+        raise ValueError("Grayscale cmf! Cannot convert to color.")
+    out = spec2xyz(spec, cmf)
+    if norm is True:
+        out = out / out.max()
+    elif norm != 0:
+        out = out / norm
+    out = xyz2gray(out) if gray else xyz2srgb(out)
+    if gamma is True:
+        out = apply_srgb_gamma(out)
+    elif gamma is not False:
+        out = apply_gamma(out, gamma)
+    return out

@@ -142,3 +142,26 @@ ILLUM_CASES = {
     "big_beta": dict(shape=(16, 24), wavelengths=[500.0], pixelsize=100.0, beta=[0.5, 0.7], phi=[0.1, 3.0],
                      jones=(1, 0)),
 }
+
+
+# POM image formation cases on transferred fields of the cases above
+# (dtmm/field_viewer.py:70 calculate_pom_field, dtmm/field.py field2specter,
+# dtmm/color.py specter2color with the reference's own load_tcmf):
+#   source   golden case whose field_out is the input
+#   jvec     polarizer (jones vector, optional frame rotation) combining x / y inputs
+#   analyzer analyzer jones vector and the rotation of its matrix
+#   window   multiply by a separable raised-cosine window
+#   dmat_d   refocus by d pixels in a cover of index 1.5 (field_diffraction_matrix)
+#   summed   field2spectersum over the leading (ray) axis
+POM_CASES = {
+    "pom_crossed": dict(source="cfg1_small", jvec=((1, 0), 0.0), analyzer=((0, 1), 0.0)),
+    "pom_rotated": dict(source="cfg1_small", jvec=((1, 0), np.pi / 8), analyzer=((1, 1), 0.3), window=True,
+                        dmat_d=2.0),
+    "pom_rays_summed": dict(source="fourx4_multiray", jvec=None, analyzer=((0, 1), 0.0), summed=True),
+}
+
+
+def raised_cosine_window(shape):
+    """Separable window 0.5 - 0.5 cos(2 pi (i + 0.5) / n) on both axes."""
+    wy, wx = (0.5 - 0.5 * np.cos(2 * np.pi * (np.arange(n) + 0.5) / n) for n in shape)
+    return wy[:, None] * wx[None, :]

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from golden_cases import CASES, ILLUM_CASES, build_inputs  # noqa: E402
+from golden_cases import CASES, ILLUM_CASES, POM_CASES, build_inputs, raised_cosine_window  # noqa: E402
 
 
 def run_case(name, dtmm):
@@ -92,17 +92,64 @@ def save_illum(dtmm):
     print("illum                  %d cases" % len(arrays))
 
 
+def save_pom(dtmm):
+    """Reference POM pipeline on golden transferred fields, one pom_<case>.npz per POM_CASES entry:
+    the jones vector, analyzer matrix, window, diffraction matrix and cmf it used, the POM
+    field, the specter and RGB images for several specter2color options."""
+    import importlib
+
+    color, diffract, field, field_viewer, jones, jones4 = (
+        importlib.import_module("dtmm." + m) for m in ("color", "diffract", "field", "field_viewer", "jones", "jones4"))
+
+    for name, case in POM_CASES.items():
+        src = np.load(os.path.join(HERE, case["source"] + ".npz"))
+        f = np.array(src["field_out"])
+        wl = np.asarray(src["wavelengths"], float)
+        ps = float(src["pixelsize"])
+        shape = f.shape[-2:]
+        jvec = None if case["jvec"] is None else jones.jonesvec(case["jvec"][0], case["jvec"][1])
+        an = case["analyzer"]
+        jmat = jones.rotated_matrix(jones.polarizer(jones.jonesvec(an[0])), an[1])
+        pmat = jones4.ray_jonesmat4x4(jmat)
+        window = raised_cosine_window(shape) if case.get("window") else None
+        dmat = None
+        if case.get("dmat_d") is not None:
+            ks = 2 * np.pi / wl * ps
+            dmat = diffract.field_diffraction_matrix(shape, ks, d=case["dmat_d"], epsv=(2.25, 2.25, 2.25))
+        # the reference writes its result into `out` (and returns it); without `out` it returns None
+        out = np.empty_like(f[..., 0, :, :, :, :] if jvec is not None else f)
+        pom = field_viewer.calculate_pom_field(f.copy(), jvec, pmat, dmat, window=window, out=out)
+        spec = field.field2spectersum(pom) if case.get("summed") else field.field2specter(pom)
+        cmf = color.load_tcmf(wl)
+        arrays = dict(field_in=f, wavelengths=wl, jvec=np.zeros(2, complex) if jvec is None else np.asarray(jvec),
+                      has_jvec=np.asarray(jvec is not None), pmat=np.asarray(pmat), pom=np.asarray(pom),
+                      spec=np.asarray(spec), cmf=np.asarray(cmf),
+                      rgb=color.specter2color(spec, cmf),
+                      rgb_gray=color.specter2color(spec, cmf, gray=True),
+                      rgb_norm=color.specter2color(spec, cmf, norm=True),
+                      rgb_gamma=color.specter2color(spec, cmf, norm=0.7, gamma=2.2),
+                      rgb_linear=color.specter2color(spec, cmf, norm=0.5, gamma=False))
+        if window is not None:
+            arrays["window"] = window
+        if dmat is not None:
+            arrays["dmat"] = np.asarray(dmat)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print("%-22s pom %s spec %s" % (name, np.asarray(pom).shape, np.asarray(spec).shape))
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES))
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom"])
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
             save_alphaf_kat(dtmm)
         elif name == "illum":
             save_illum(dtmm)
+        elif name == "pom":
+            save_pom(dtmm)
         else:
             run_case(name, dtmm)
 

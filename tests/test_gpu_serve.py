@@ -1,6 +1,7 @@
 """Continuous-batching server (GPU).
 
-Each request's result must be the same whether it runs alone or among other
+Each request's result (transferred field and POM image) must be the same
+whether it runs alone or among other
 requests of different sizes that overlap it on the device (the server gives
 every request its own stream and workspace, so the results are expected to
 be bit-identical; the stated tolerance is the mixed-precision one, rel. L2
@@ -47,6 +48,9 @@ def test_results_alone_equal_results_in_the_mix():
         assert np.all(np.isfinite(a))
         assert rel(b, a) <= TOL
         assert torch.equal(r.result, reqs[i].result)
+        # the request's POM image too
+        assert r.image is not None and r.image.shape == tuple(s["shape"]) + (3,)
+        assert torch.equal(r.image, reqs[i].image)
 
 
 def test_budget_limits_admission():
