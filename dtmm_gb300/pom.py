@@ -10,8 +10,11 @@ sRGB or gray image (``specter2color``, dtmm/color.py:52-224).  ``pom_image``
 does the three steps in one pass per pixel.
 
 Arrays may be numpy (copied to the device and back) or CUDA tensors (results
-stay on the device).  The small jones / 4x4 matrices are built on the host
-(``jonesvec``, ``polarizer``, ``rotated_matrix``, ``ray_jonesmat4x4``).
+stay on the device).  A caller that enqueues the image behind other work on
+the same stream passes ``pmat`` and ``cmf`` as device tensors: a host-to-device
+copy from pageable memory would wait for that work.  The small jones / 4x4
+matrices are built on the host (``jonesvec``, ``polarizer``,
+``rotated_matrix``, ``ray_jonesmat4x4``).
 Refocusing through a diffraction matrix (``dmat``) and k-space inputs are not
 on this path (``NotImplementedError``).
 """
@@ -147,10 +150,12 @@ def _desc(f, jvec, pmat, window):
         d.npol = 1
     d.nset = int(np.prod(lead)) if lead else 1
     if pmat is not None:
-        pm = np.asarray(pmat, np.complex128)
-        if pm.shape != (4, 4):
+        if isinstance(pmat, torch.Tensor):  # already on the device: no upload behind queued work
+            pt = pmat.to(device=f.device, dtype=torch.complex128).contiguous()
+        else:
+            pt = torch.from_numpy(np.ascontiguousarray(np.asarray(pmat, np.complex128))).to(f.device)
+        if tuple(pt.shape) != (4, 4):
             raise NotImplementedError("one 4x4 analyzer matrix for every pixel and wavelength")
-        pt = torch.from_numpy(np.ascontiguousarray(pm)).to(f.device)
         keep.append(pt)
         d.pmat = pt.data_ptr()
     if window is not None:
@@ -285,10 +290,12 @@ def pom_image(field, cmf, jvec=None, pmat=None, window=None, norm=False, gamma=T
     torch = _torch()
     f, host = _dev_field(field)
     d, keep, lead = _desc(f, jvec, pmat, window)
-    cmf = np.asarray(cmf, np.float64)
-    if cmf.shape != (f.shape[-4], 3):
+    if isinstance(cmf, torch.Tensor):  # already on the device: no upload behind queued work
+        c = cmf.to(device=f.device, dtype=torch.float64).contiguous()
+    else:
+        c = torch.from_numpy(np.ascontiguousarray(np.asarray(cmf, np.float64))).to(f.device)
+    if tuple(c.shape) != (f.shape[-4], 3):
         raise ValueError("cmf must have one row per wavelength")
-    c = torch.from_numpy(np.ascontiguousarray(cmf)).to(f.device)
     rgb = torch.empty(tuple(f.shape[-2:]) + (3,), dtype=torch.float32, device=f.device)
     mode, val = _norm_args(norm)
     lib = _lib.load()

@@ -85,7 +85,7 @@ class TransferServer:
             from .pom import jonesvec, polarizer, ray_jonesmat4x4
 
             self.pom_jvec = jonesvec((1, 0))
-            self.pom_pmat = ray_jonesmat4x4(polarizer(jonesvec((0, 1))))
+            self.pom_pmat = torch.from_numpy(ray_jonesmat4x4(polarizer(jonesvec((0, 1))))).to(self.device)
         self.stats = {}
 
     # -- sizes -----------------------------------------------------------
@@ -110,6 +110,10 @@ class TransferServer:
         s = self.streams[slot]
         spec = req.spec
         with torch.cuda.stream(s):
+            # every upload happens here, while the slot's stream is idle: a
+            # copy from pageable memory queued behind the transfer would hold
+            # the host loop until the transfer finished
+            cmf = torch.from_numpy(samples.transmission_cmf(spec["wavelengths"])).to(self.device) if self.pom else None
             mat = samples.twisted_nematic_device(spec["shape"], spec["nlayers"], seed=spec["seed"],
                                                  device=self.device, host_modes=False)
             jones = None if self.npol == 2 else (1, 0)
@@ -126,8 +130,7 @@ class TransferServer:
             if self.pom:
                 from .pom import pom_image
 
-                image = pom_image(fout, samples.transmission_cmf(spec["wavelengths"]), self.pom_jvec, self.pom_pmat,
-                                  stream=s.cuda_stream)
+                image = pom_image(fout, cmf, self.pom_jvec, self.pom_pmat, stream=s.cuda_stream)
             done = torch.cuda.Event()
             done.record(s)
         req.updates = plan.updates
