@@ -631,6 +631,21 @@ __device__ inline void tmat_k(double beta, double phi, cpx<double> ein, cpx<doub
     for (int j = 0; j < 2; ++j) t[i][j] = Fout[2 * i][0] * ei[0][j] + Fout[2 * i][2] * ei[1][j];
 }
 
+// beta and (cos, sin) of phi at grid point k without the angle itself
+__device__ inline void betacs_k(const Grid& g, double ks, int ky, int kx, double& beta, double& c, double& s) {
+  const double xx = (double)fsigned(kx, g.W) * (1.0 / g.W);
+  const double yy = (double)fsigned(ky, g.H) * (1.0 / g.H);
+  const double r = sqrt(xx * xx + yy * yy);
+  beta = (2.0 * M_PI / fabs(ks)) * r;
+  if (r > 0.0) {
+    c = xx / r;
+    s = yy / r;
+  } else {
+    c = 1.0;  // phi = atan2(0, 0) = 0
+    s = 0.0;
+  }
+}
+
 template <typename R>
 __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int HW = g.H * g.W;
@@ -639,76 +654,67 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int lam = t / HW, k = t - lam * HW;
   const int ky = k / g.W, kx = k - ky * g.W;
   const double ks = p.ks[lam];
-  double beta, phi;
-  betaphi_k(g, ks, ky, kx, beta, phi);
-  cpx<double> al[4], F[4][4], Fi[4][4];
   if (p.eps_dev != nullptr) p.eps = mk<double>(p.eps_dev[0], p.eps_dev[1]);
-  if (p.what == KT_DIAG) {
-    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
-    const bool masked = (beta >= p.betamax) || (al[0].re == 0.0 && al[0].im == 0.0);
-    cpx<double> ep = masked ? mk<double>(0.0, 0.0) : cexp_i(al[0] * (ks * p.d));
-    cpx<double> em = masked ? mk<double>(0.0, 0.0) : cexp_i(al[1] * (ks * p.d));
-    // column-major (lam, kx, ky) so that column passes read it coalesced
-    const size_t tt = ((size_t)lam * g.W + kx) * g.H + ky;
-    tab[tt * 2 + 0] = cvt<R>(ep);
-    tab[tt * 2 + 1] = cvt<R>(em);
-    return;
-  }
-  if (p.what == KT_D1 || p.what == KT_D2 || p.what == KT_PROJ) {
-    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
-    cpx<double> ph[4];
-    if (p.what != KT_PROJ) {
-      // alpha = (a, -a, a, -a): two exponentials
-      ph[0] = ph[2] = cexp_i(al[0] * (ks * p.d));
-      ph[1] = ph[3] = cexp_i(al[1] * (ks * p.d));
+  if (p.what == KT_DIAG || p.what == KT_D1 || p.what == KT_D2) {
+    // Closed forms for the isotropic medium (a = sqrt(eps - beta^2), the
+    // eigenvalues (a, -a, a, -a), e+- = exp(+-i a ks d)); they equal the
+    // products of the field matrices E P F^-1 and F P E^-1 written out, with
+    // the same cut: zero where beta >= betamax or a = 0.
+    double beta, c, s;
+    betacs_k(g, ks, ky, kx, beta, c, s);
+    const cpx<double> a = csqrt_d(mk<double>(p.eps.re - beta * beta, p.eps.im));
+    const bool cut = (beta >= p.betamax) || (a.re == 0.0 && a.im == 0.0);
+    const cpx<double> z = mk<double>(0.0, 0.0);
+    const cpx<double> ep = cut ? z : cexp_i(a * (ks * p.d));
+    const cpx<double> em = cut ? z : cexp_i(-a * (ks * p.d));
+    if (p.what == KT_DIAG) {
+      // column-major (lam, kx, ky) so that column passes read it coalesced
+      const size_t tt = ((size_t)lam * g.W + kx) * g.H + ky;
+      tab[tt * 2 + 0] = cvt<R>(ep);
+      tab[tt * 2 + 1] = cvt<R>(em);
+      return;
     }
     cpx<double> M[4][4];
-    if (p.what == KT_PROJ) {
-      const int m0 = p.proj_mode > 0 ? 0 : 1;
-      for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j)
-          M[i][j] = F[i][m0] * Fi[m0][j] + F[i][m0 + 2] * Fi[m0 + 2][j];
-    } else {
-      cpx<double> E[4][4];
-      for (int i = 0; i < 4; ++i)
-        for (int j = 0; j < 4; ++j) E[i][j] = mk<double>(0.0, 0.0);
-      E[0][0] = F[0][0]; E[0][2] = F[0][2]; E[2][0] = F[2][0]; E[2][2] = F[2][2];
-      E[1][1] = F[0][1]; E[1][3] = F[0][3]; E[3][1] = F[2][1]; E[3][3] = F[2][3];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) M[i][j] = z;
+    if (!cut) {
+      const double cc = c * c, ss = s * s, cs = c * s;
       if (p.what == KT_D1) {
-        for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 4; ++j) {
-            cpx<double> s = mk<double>(0.0, 0.0);
-            for (int m = 0; m < 4; ++m) s = s + E[i][m] * ph[m] * Fi[m][j];
-            M[i][j] = s;
-          }
+        // E P F^-1 (dtmm/matrix.py:110): with igp = a / eps, ia = 1 / a,
+        // P = igp c^2 + ia s^2, Q = cs (ia - igp), S = igp s^2 + ia c^2
+        const cpx<double> igp = cdiv(a, p.eps), ia = cdiv(mk<double>(1.0, 0.0), a);
+        const cpx<double> P = igp * cc + ia * ss, Q = (ia - igp) * cs, S = igp * ss + ia * cc;
+        const cpx<double> hp = ep * 0.5, hm = em * 0.5;
+        M[0][0] = hp; M[0][1] = hp * P;  M[0][3] = hp * Q;
+        M[2][1] = -(hp * Q); M[2][2] = hp; M[2][3] = -(hp * S);
+        M[1][0] = hm; M[1][1] = -(hm * P); M[1][3] = -(hm * Q);
+        M[3][1] = hm * Q; M[3][2] = hm; M[3][3] = hm * S;
       } else {
-        // E of an isotropic medium: each direction's 2x2 block is the rotation
-        // of diag(1/2, 1/2) by phi, so E^-1 = 2 x (rotation by -phi) per block
-        // (zero where the eigen-data are cut)
-        cpx<double> Ei[4][4];
-        for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 4; ++j) Ei[i][j] = mk<double>(0.0, 0.0);
-        const bool cut = (beta >= p.betamax) || (al[0].re == 0.0 && al[0].im == 0.0);
-        if (!cut) {
-          double sp, cp;
-          sincos(phi, &sp, &cp);
-          // Epn rows/cols: forward block on (0, 2), backward block on (1, 3)
-          Ei[0][0] = mk<double>(2 * cp, 0); Ei[0][2] = mk<double>(2 * sp, 0);
-          Ei[2][0] = mk<double>(-2 * sp, 0); Ei[2][2] = mk<double>(2 * cp, 0);
-          Ei[1][1] = mk<double>(2 * cp, 0); Ei[1][3] = mk<double>(2 * sp, 0);
-          Ei[3][1] = mk<double>(-2 * sp, 0); Ei[3][3] = mk<double>(2 * cp, 0);
-        }
-        for (int i = 0; i < 4; ++i)
-          for (int j = 0; j < 4; ++j) {
-            cpx<double> s = mk<double>(0.0, 0.0);
-            for (int m = 0; m < 4; ++m) s = s + F[i][m] * ph[m] * Ei[m][j];
-            M[i][j] = s;
-          }
+        // F P E^-1 (dtmm/matrix.py:121): with gp = eps / a,
+        // P = gp c^2 + a s^2, Q = cs (gp - a), S = gp s^2 + a c^2
+        const cpx<double> gp = cdiv(p.eps, a);
+        const cpx<double> P = gp * cc + a * ss, Q = (gp - a) * cs, S = gp * ss + a * cc;
+        M[0][0] = ep; M[0][1] = em;
+        M[1][0] = ep * P; M[1][1] = -(em * P); M[1][2] = ep * Q; M[1][3] = -(em * Q);
+        M[2][2] = ep; M[2][3] = em;
+        M[3][0] = -(ep * Q); M[3][1] = em * Q; M[3][2] = -(ep * S); M[3][3] = em * S;
       }
     }
     cpx<R>* o = tab + (size_t)t * 16;
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(M[i][j]);
+    return;
+  }
+  double beta, phi;
+  betaphi_k(g, ks, ky, kx, beta, phi);
+  cpx<double> al[4], F[4][4], Fi[4][4];
+  if (p.what == KT_PROJ) {
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    // F . diag(modes) . F^-1 over the forward (or backward) pair (dtmm/diffract.py:242)
+    const int m0 = p.proj_mode > 0 ? 0 : 1;
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(F[i][m0] * Fi[m0][j] + F[i][m0 + 2] * Fi[m0 + 2][j]);
     return;
   }
   // 2x2 method: E-basis diffraction over d, e(d) * I for the isotropic medium
