@@ -21,7 +21,7 @@ PRECISION_DOUBLE = 1
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
                "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field", "dtmm_pom_field",
-               "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image")
+               "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image", "dtmm_director2data")
 ABI_VERSION = 2
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -146,6 +146,10 @@ def load(build_if_missing=True):
     lib.dtmm_pom_image.restype = ctypes.c_int
     lib.dtmm_pom_image.argtypes = [ctypes.POINTER(PomDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                    ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dtmm_director2data.restype = ctypes.c_int
+    lib.dtmm_director2data.argtypes = [ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     if lib.dtmm_abi_version() != ABI_VERSION:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib

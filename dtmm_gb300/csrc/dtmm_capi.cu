@@ -307,7 +307,7 @@ struct Engine {
       int tx = std::max(1, 256 / (C * n1));
       // tiles of H x (C tx + 1) complex: about 3 blocks per SM by default
       size_t cap = tiles == 2 ? 72 * 1024 : 100 * 1024;
-      if (d.col_tile > 0 && d.col_tile * C * n1 <= 512) {
+      if (d.col_tile > 0 && d.col_tile * C * n1 <= 256) {  // the kernel's launch bound
         tx = d.col_tile;
         cap = 160 * 1024;
       }

@@ -190,7 +190,7 @@ __host__ __device__ constexpr int reg_col_tiles(int n, int ny) { return (!reg_ev
 
 // Column pass, k-space operator KOP_NONE or KOP_DIAG (see the file comment).
 template <typename R, int N1, int N2>
-__global__ void __launch_bounds__(512, 1) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
+__global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
                                                          cpx<R>* __restrict__ U) {
   using TS = TwoStep<N1, N2>;
   constexpr int H = N1 * N2;

@@ -1,0 +1,74 @@
+"""Optical data from director fields, on the GPU.
+
+``director2data`` mirrors dtmm.data.director2data (dtmm/data.py:277-320): a
+director field [L, H, W, 3] (its length is the order parameter's square)
+becomes the optical block ``(thickness, epsv, epsa)`` of eps eigenvalues and
+Euler angles, computed per voxel by the library's ``dtmm_director2data``
+kernel.  With a CUDA tensor the block stays on the device (``device_material``
+wraps it for ``plan_transfer``); with a numpy array the result comes back as
+numpy, as the reference returns it.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _run(director, mask, no, ne, nhost, scale_factor):
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("dtmm_gb300.data needs a CUDA GPU (there is no CPU path)")
+    host = not isinstance(director, torch.Tensor)
+    d = torch.from_numpy(np.ascontiguousarray(director)) if host else director
+    if d.shape[-1] != 3:
+        raise ValueError("director must have 3 components in its last axis")
+    if d.dtype not in (torch.float32, torch.float64):
+        d = d.to(torch.float64)
+    d = d.cuda().contiguous()
+    dev = d.device
+    m = None
+    if mask is not None:
+        if nhost is None:
+            raise ValueError("nhost must be given with a mask")
+        mt = torch.from_numpy(np.ascontiguousarray(mask)) if not isinstance(mask, torch.Tensor) else mask
+        m = mt.to(device=dev, dtype=torch.uint8).contiguous()
+        if tuple(m.shape) != tuple(d.shape[:-1]):
+            raise ValueError("mask must have the director's shape without its last axis")
+    epsv = torch.empty(d.shape, dtype=torch.float64, device=dev)
+    epsa = torch.empty(d.shape, dtype=torch.float64, device=dev)
+    nvox = int(np.prod(d.shape[:-1]))
+    lib = _lib.load()
+    _lib.check(lib.dtmm_director2data(nvox, ctypes.c_void_p(d.data_ptr()), int(d.dtype == torch.float64),
+                                      ctypes.c_void_p(m.data_ptr() if m is not None else None), float(no), float(ne),
+                                      float(nhost if nhost is not None else 1.0), float(scale_factor),
+                                      ctypes.c_void_p(epsv.data_ptr()), ctypes.c_void_p(epsa.data_ptr()),
+                                      ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    return epsv, epsa, host, (m, d)
+
+
+def director2data(director, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, thickness=None):
+    """Optical block ``(thickness, epsv, epsa)`` from a director field (dtmm/data.py:277)."""
+    epsv, epsa, host, _ = _run(director, mask, no, ne, nhost, scale_factor)
+    nl = epsv.shape[0]
+    thickness = np.ones((nl,)) if thickness is None else np.asarray(thickness, np.float64)
+    if host:
+        return thickness, epsv.cpu().numpy(), epsa.cpu().numpy()
+    return thickness, epsv, epsa
+
+
+def device_material(director, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0,
+                    thickness=None):
+    """``director2data`` kept on the device as a ``DeviceMaterial`` for ``plan_transfer``."""
+    from .transfer import DeviceMaterial
+
+    epsv, epsa, _, _ = _run(director, mask, no, ne, nhost, scale_factor)
+    nl = epsv.shape[0]
+    th = np.ones((nl,)) if thickness is None else np.asarray(thickness, np.float64)
+    return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape)
+
+
+__all__ = ["director2data", "device_material"]

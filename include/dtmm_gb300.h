@@ -211,6 +211,14 @@ int dtmm_specter2color(long long npix, int nlam, const double* spec, const doubl
 int dtmm_pom_image(const dtmm_pom_desc* desc, const void* field, const double* cmf, int norm_mode,
                    double norm_value, double gamma, int gray, float* rgb, void* stream);
 
+/* director2data (dtmm/data.py:277-320) on the device: director[nvox][3]
+   (float64, or float32 when director_double == 0) -> eps eigenvalues
+   epsv[nvox][3] and Euler angles epsa[nvox][3] (float64).  The order
+   parameter is sqrt(|director|) / scale_factor applied to (no^2, no^2, ne^2);
+   voxels where mask[i] == 0 (uint8 [nvox], optional) get nhost^2. */
+int dtmm_director2data(long long nvox, const void* director, int director_double, const void* mask, double no,
+                       double ne, double nhost, double scale_factor, double* epsv, double* epsa, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1394,3 +1394,28 @@ def specter2color(spec, cmf, norm=False, gamma=True, gray=False):
     elif gamma is not False:
         out = apply_gamma(out, gamma)
     return out
+
+
+# ---------------------------------------------------------------------------
+# director -> optical data
+# ---------------------------------------------------------------------------
+def director2data(director, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, thickness=None):
+    """Optical block from a director field (dtmm/data.py:277-320): order
+    parameter sqrt(|d|) (director2order, :963), uniaxial order of
+    (no^2, no^2, ne^2) (_uniaxial_order, :1214), host eps outside the mask,
+    angles (0, atan2(|d_xy|, d_z), atan2(d_y, d_x)) (director2angles, :975)."""
+    d = np.asarray(director, FDTYPE)
+    x, y, z = d[..., 0], d[..., 1], d[..., 2]
+    order = np.sqrt(np.sqrt(x ** 2 + y ** 2 + z ** 2)) / scale_factor
+    eo, ee = no ** 2, ne ** 2
+    m = (eo + eo + ee) / 3.0
+    delta = ee - (eo + eo) / 2.0
+    e1 = np.where(order == 0.0, m, m - 1.0 / 3.0 * order * delta)
+    e3 = np.where(order == 0.0, m, m + 2.0 / 3.0 * order * delta)
+    epsv = np.stack([e1, e1, e3], axis=-1)
+    if mask is not None:
+        epsv[np.logical_not(mask), :] = nhost ** 2
+    epsa = np.stack([np.zeros_like(x), np.arctan2(np.sqrt(x ** 2 + y ** 2), z), np.arctan2(y, x)], axis=-1)
+    if thickness is None:
+        thickness = np.ones((epsv.shape[0],))
+    return thickness, epsv, epsa

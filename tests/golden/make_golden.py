@@ -137,11 +137,27 @@ def save_pom(dtmm):
         print("%-22s pom %s spec %s" % (name, np.asarray(pom).shape, np.asarray(spec).shape))
 
 
+def save_director(dtmm):
+    """Reference director2data on a seeded director field (lengths 0 to 1.3, a masked host region)."""
+    rng = np.random.Generator(np.random.PCG64(77))
+    director = rng.normal(size=(3, 12, 16, 3))
+    director *= (rng.uniform(0.0, 1.3, size=(3, 12, 16)) / np.linalg.norm(director, axis=-1))[..., None]
+    director[0, 0, :4] = 0.0
+    zz, yy, xx = np.meshgrid(np.arange(3), np.arange(12), np.arange(16), indexing="ij")
+    mask = (yy - 6) ** 2 + (xx - 8) ** 2 < 30
+    a = dtmm.data.director2data(director)
+    b = dtmm.data.director2data(director, mask=mask, no=1.52, ne=1.71, nhost=1.4, scale_factor=0.8)
+    np.savez_compressed(os.path.join(HERE, "director.npz"), director=director, mask=mask,
+                        epsv_default=a[1], epsa_default=a[2], thickness_default=a[0],
+                        epsv_masked=b[1], epsa_masked=b[2])
+    print("director               %s" % (director.shape,))
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom"])
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director"])
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
@@ -150,6 +166,8 @@ def main(argv):
             save_illum(dtmm)
         elif name == "pom":
             save_pom(dtmm)
+        elif name == "director":
+            save_director(dtmm)
         else:
             run_case(name, dtmm)
 
