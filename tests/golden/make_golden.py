@@ -153,11 +153,25 @@ def save_director(dtmm):
     print("director               %s" % (director.shape,))
 
 
+def save_files(dtmm):
+    """Reference .dtmf / .dtms files of small seeded data (read back and rewritten by the IO tests)."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    field = (rng.normal(size=(2, 3, 4, 6, 5)) + 1j * rng.normal(size=(2, 3, 4, 6, 5))).astype(np.complex128)
+    dtmm.field.save_field(os.path.join(HERE, "io_field"), (field, np.asarray([450.0, 550.0, 650.0]), 80.0))
+    d = np.asarray([1.0, 2.0, 0.5])
+    epsv = np.broadcast_to(np.asarray([2.25, 2.25, 2.89]), (3, 6, 5, 3)).copy()
+    epsa = rng.uniform(-1, 1, size=(3, 6, 5, 3))
+    epsv2 = (np.full((2, 1, 1, 3), 2.1) + 0.01j).astype(np.complex128)
+    epsa2 = np.zeros((2, 1, 1, 3))
+    dtmm.data.save_stack(os.path.join(HERE, "io_stack"), [(d, epsv, epsa), (np.asarray([3.0, 1.0]), epsv2, epsa2)])
+    print("io files               io_field.dtmf io_stack.dtms")
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director"])
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files"])
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
@@ -168,6 +182,8 @@ def main(argv):
             save_pom(dtmm)
         elif name == "director":
             save_director(dtmm)
+        elif name == "files":
+            save_files(dtmm)
         else:
             run_case(name, dtmm)
 
