@@ -273,25 +273,36 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       double detb = 1.0;
       if (FOUR) detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
       if (detf == 0.0 || detb == 0.0) zero = true;
-      double rec[nrec];
+      // records in the bulk precision; with complex64 records the FP64
+      // determinant is rounded to FP32 and inverted there (correctly rounded
+      // FP32 reciprocal: the stored value differs from the rounded FP64
+      // quotient by at most one FP32 ulp), which spares the FP64 division;
+      // determinants too small for FP32 keep the FP64 division
+      R rec[nrec];
       if (zero) {
 #pragma unroll
-        for (int i = 0; i < nrec; ++i) rec[i] = 0.0;
+        for (int i = 0; i < nrec; ++i) rec[i] = (R)0;
       } else {
-        rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
-        rec[4] = 1.0 / detf;
-        rec[5] = (al[0] - aw) * p.d;
-        rec[6] = (al[2] - aw) * p.d;
+        rec[0] = (R)E[0][0]; rec[1] = (R)E[0][2]; rec[2] = (R)E[1][0]; rec[3] = (R)E[1][2];
+        if constexpr (sizeof(R) == 4)
+          rec[4] = fabs(detf) > 1e-30 ? __frcp_rn((float)detf) : (float)(1.0 / detf);
+        else
+          rec[4] = 1.0 / detf;
+        rec[5] = (R)((al[0] - aw) * p.d);
+        rec[6] = (R)((al[2] - aw) * p.d);
         if (FOUR) {
-          rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
-          rec[11] = 1.0 / detb;
-          rec[12] = (al[1] + aw) * p.d;
-          rec[13] = (al[3] + aw) * p.d;
+          rec[7] = (R)E[0][1]; rec[8] = (R)E[0][3]; rec[9] = (R)E[1][1]; rec[10] = (R)E[1][3];
+          if constexpr (sizeof(R) == 4)
+            rec[11] = fabs(detb) > 1e-30 ? __frcp_rn((float)detb) : (float)(1.0 / detb);
+          else
+            rec[11] = 1.0 / detb;
+          rec[12] = (R)((al[1] + aw) * p.d);
+          rec[13] = (R)((al[3] + aw) * p.d);
         }
       }
       R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
 #pragma unroll
-      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = (R)rec[i];
+      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
     }
     return;
   }
