@@ -206,16 +206,22 @@ struct TwoStep {
 
   __host__ __device__ static __forceinline__ int slot(int k1, int s) { return k1 * N1 + (s ^ (k1 & (N1 - 1))); }
 
+  // Twiddle table in lane-major order: twt[k1 * N1 + t] = W_N^(t k1), so the
+  // N1 lanes of a group read N1 consecutive entries (no bank conflicts)
+  template <typename R>
+  __host__ __device__ static __forceinline__ cpx<R> twiddle_entry(const cpx<R>* tw_natural, int e) {
+    return tw_natural[(e % N1) * (e / N1)];
+  }
+
   // step 1: v[m] = x[t + N1 m] in; DFT over m, twiddle, write to the exchange.
-  // Twiddles W_N^(t k1) come from `trow` (registers) or the table `twn`
-  // (W_N^e, e < N; t k1 < N needs no reduction).
+  // Twiddles W_N^(t k1) come from `trow` (registers) or the lane-major table `twt`.
   template <typename R, bool INV>
   __host__ __device__ static __forceinline__ void step1(cpx<R> (&v)[N2], cpx<R>* xch, int xs, const cpx<R>* trow,
-                                                        const cpx<R>* twn, int t) {
+                                                        const cpx<R>* twt, int t) {
     RegDFTg<R, N2, INV>::run(v);
 #pragma unroll
     for (int k1 = 1; k1 < N2; ++k1) {
-      cpx<R> w = trow ? trow[k1] : twn[t * k1];
+      cpx<R> w = trow ? trow[k1] : twt[k1 * N1 + t];
       if (INV) w.im = -w.im;
       v[k1] = v[k1] * w;
     }

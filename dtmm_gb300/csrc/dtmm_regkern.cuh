@@ -65,10 +65,10 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   const int nlines = G * NP * C;
   cpx<R>* acc = (cpx<R>*)smem_raw;                  // [lines][LS]
   cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * LS;  // [lines][LS] exchange and transformed rows
-  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * LS;   // [W]  exp(-2 pi i e / W)
+  cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * LS;   // [W]  twiddles, lane-major (TwoStep::twiddle_entry)
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
-  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
   for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
   const R sc = (R)p.in_scale;
   __syncthreads();
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   cpx<R> trow[TWREG ? N2 : 1];
   if (TWREG) {
 #pragma unroll
-    for (int k1 = 0; k1 < (TWREG ? N2 : 1); ++k1) trow[k1] = tw[t * k1];
+    for (int k1 = 0; k1 < (TWREG ? N2 : 1); ++k1) trow[k1] = tw[k1 * N1 + t];
   }
   const int c = line % C, im = line / C;
   const int gl = im / NP, pol = pol0 + im - gl * NP;
@@ -200,11 +200,11 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
   const int ntiles = reg_col_tiles(H, p.ny);
   cpx<R>* tileA = (cpx<R>*)smem_raw;               // [H][RS] loaded rows, then spectra along y
   cpx<R>* tileB = tileA + (size_t)(ntiles - 1) * H * RS;  // [H][RS] exchange and outgoing rows (= A with one tile)
-  cpx<R>* tw = tileA + (size_t)ntiles * H * RS;    // [H] exp(-2 pi i e / H)
+  cpx<R>* tw = tileA + (size_t)ntiles * H * RS;    // [H] twiddles, lane-major (TwoStep::twiddle_entry)
   const int img = blockIdx.y;
   const int x0 = blockIdx.x * TX;
   const int lam = img_lam(g, img), ray = img_ray(g, img);
-  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = ((const cpx<R>*)p.tw)[e];
+  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
   // a half-warp covers one tile row (C x TX contiguous slots): conflict-free
   const int CT = C * TX;
   const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;

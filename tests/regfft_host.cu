@@ -82,15 +82,16 @@ static void check_two_step() {
   using TS = TwoStep<N1, N2>;
   constexpr int N = N1 * N2;
   std::vector<C> x = input(N, 3 + INV);
-  std::vector<cpx<double>> xch(N), out(N), tw(N);
+  std::vector<cpx<double>> xch(N), out(N), tw(N), twt(N);
   for (int e = 0; e < N; ++e) {
     const double a = -2.0 * M_PI * e / N;
     tw[e] = mk<double>(std::cos(a), std::sin(a));
   }
+  for (int e = 0; e < N; ++e) twt[e] = TS::twiddle_entry(tw.data(), e);  // lane-major table
   for (int t = 0; t < N1; ++t) {  // step 1, every lane
     cpx<double> v[N2];
     for (int m = 0; m < N2; ++m) v[m] = mk<double>(x[t + N1 * m].real(), x[t + N1 * m].imag());
-    TS::template step1<double, INV>(v, xch.data(), 1, nullptr, tw.data(), t);
+    TS::template step1<double, INV>(v, xch.data(), 1, nullptr, twt.data(), t);
   }
   for (int t = 0; t < N1; ++t) {  // step 2, every lane
     cpx<double> u[TS::J][N1];
