@@ -407,8 +407,7 @@ struct Engine {
   int row_group_reg() const {
     const int perG = d.npol * L.C;  // lines per wavelength
     const int n1 = reg_lanes(d.width);
-    // accumulator + row buffer + staged next-window row, per line
-    const size_t line_bytes = (2 * (size_t)reg_row_stride(n1, d.width) + d.width) * sizeof(cpx<R>);
+    const size_t line_bytes = 2 * (size_t)reg_row_stride(n1, d.width) * sizeof(cpx<R>);
     // about 8 lines per block measured best (256-pixel rows, 4x4, 2 polarisations)
     int G = std::max(1, 8 / perG);
     if (d.row_group > 0) G = d.row_group;
@@ -423,7 +422,7 @@ struct Engine {
       const int n1 = reg_lanes(d.width);
       const int nl = p.G * p.PB * C;
       const size_t smem =
-          (2 * (size_t)nl * reg_row_stride(n1, d.width) + (size_t)nl * d.width + d.width) * sizeof(cpx<R>);
+          2 * (size_t)nl * reg_row_stride(n1, d.width) * sizeof(cpx<R>) + d.width * sizeof(cpx<R>);
       if (smem > 220 * 1024 || nl * n1 > 512)
         return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
       RegLaunch rl;
@@ -465,7 +464,7 @@ struct Engine {
     if (row_reg()) {
       p.G = row_group_reg();
       const int n1 = reg_lanes(d.width);
-      if ((2 * (size_t)reg_row_stride(n1, d.width) + d.width) * d.npol * L.C * sizeof(cpx<R>) > 200 * 1024 ||
+      if (2 * (size_t)d.npol * L.C * reg_row_stride(n1, d.width) * sizeof(cpx<R>) > 200 * 1024 ||
           d.npol * L.C * n1 > 512)
         p.PB = 1;
       return launch_row_reg(p, Ub, Xb, L.C, re);

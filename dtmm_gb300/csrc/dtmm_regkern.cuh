@@ -40,15 +40,6 @@ __device__ __forceinline__ unsigned group_mask() {
   }
 }
 
-// 16-byte asynchronous global -> shared copies (no registers in flight);
-// wait_all returns when every copy of the thread has landed
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 // row buffer stride (complex elements): with N1 = 4 or 8 several line groups
 // share a half-warp, and a stride of W + 4 (W + 8) puts their exchange slots
 // on disjoint banks; W is a multiple of 16 for every listed side
@@ -75,7 +66,6 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   cpx<R>* acc = (cpx<R>*)smem_raw;                  // [lines][LS]
   cpx<R>* tmp = acc + (size_t)p.G * p.PB * C * LS;  // [lines][LS] exchange and transformed rows
   cpx<R>* tw = tmp + (size_t)p.G * p.PB * C * LS;   // [W]  twiddles, lane-major (TwoStep::twiddle_entry)
-  cpx<R>* stage = tw + W;                           // [lines][W] the next window's rows, copied ahead
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
   for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
@@ -97,41 +87,15 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   const int lam = lam0 + gl;
   const int img = (ray * g.npol + pol) * g.nlam + lam;
   cpx<R>* xl = tmp + (size_t)line * LS;
-  // windows in (j, i) order, skipping the other chains' windows and the empty ones
-  auto wanted = [&](int q) {
-    const int w = (q % p.nx) * p.ny + q / p.nx;
-    if (p.win_only >= 0 && w != p.win_only) return false;
-    return !(p.wzero != nullptr && p.wzero[ray * nwin + w]);
-  };
-  auto next_window = [&](int q) {
-    for (++q; q < nwin; ++q)
-      if (wanted(q)) return q;
-    return -1;
-  };
-  // copy the rows of window q's U_j for every line of the block into `stage`
-  auto prefetch = [&](int q) {
-    const int j = q / p.nx;
+  for (int j = 0; j < p.ny; ++j) {
+    // a single-window chain reads the one window row the column pass emitted
     const cpx<R>* Uj = U + (size_t)(p.win_only >= 0 ? 0 : j) * g.NI * C * HW;
-    for (int e = threadIdx.x; e < nlines * (W / 2); e += blockDim.x) {
-      const int l = e / (W / 2), off = (e - l * (W / 2)) * 2;
-      const int cl = l % C, il = l / C;
-      const int gll = il / NP, poll = pol0 + il - gll * NP;
-      const int imgl = (ray * g.npol + poll) * g.nlam + lam0 + gll;
-      cp_async16(stage + (size_t)l * W + off, Uj + (((size_t)imgl * C + cl) * H + y) * W + off);
-    }
-    cp_async_commit();
-  };
-  int q = next_window(-1);
-  if (q >= 0) prefetch(q);
-  while (q >= 0) {
-    const int i = q % p.nx, j = q / p.nx;
-    const int w = i * p.ny + j;
-    cp_async_wait_all();
-    __syncthreads();
-    int qn = -1;
-    {
+    for (int i = 0; i < p.nx; ++i) {
+      const int w = i * p.ny + j;
+      if (p.win_only >= 0 && w != p.win_only) continue;
+      if (p.wzero != nullptr && p.wzero[ray * nwin + w]) continue;
       if (active) {
-        const cpx<R>* src = stage + (size_t)line * W;
+        const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
         const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
         cpx<R> v[N2];
 #pragma unroll
@@ -147,9 +111,6 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
         TS::template store<R>(u, xl, 1, t, sc);
       }
       __syncthreads();
-      // the next window's rows land while this window's operator runs
-      qn = next_window(q);
-      if (qn >= 0) prefetch(qn);
       const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
       for (int x = threadIdx.x; x < W; x += blockDim.x) {
         T ef[4], arg_f[2], idf;
@@ -174,8 +135,8 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
             pb0 = phase_of(arg_b[0], kph) * idb;
             pb1 = phase_of(arg_b[1], kph) * idb;
           }
-          for (int pq = 0; pq < NP; ++pq) {
-            const int l0 = (g2 * NP + pq) * C;
+          for (int q = 0; q < NP; ++q) {
+            const int l0 = (g2 * NP + q) * C;
             const cpx<R>* h = tmp + (size_t)l0 * LS + x;
             cpx<R>* a = acc + (size_t)l0 * LS + x;
             if (C == 4) {
@@ -193,7 +154,6 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
       }
       __syncthreads();
     }
-    q = qn;
   }
   if (active) {
     cpx<R> v[N2];
