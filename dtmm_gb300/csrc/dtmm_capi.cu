@@ -412,7 +412,7 @@ struct Engine {
     int G = std::max(1, 8 / perG);
     if (d.row_group > 0) G = d.row_group;
     while (G > 1 && ((size_t)G * perG * line_bytes > 110 * 1024 || G * perG * n1 > 512)) --G;
-    return std::min(G, d.nlam);
+    return std::min(std::min(G, d.nlam), kMaxRowGroup);
   }
 
   int launch_row_reg(const RowParams& p, const cpx<R>* Ub, cpx<R>* Xb, int C, bool re) {

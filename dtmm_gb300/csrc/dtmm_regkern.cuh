@@ -43,6 +43,9 @@ __device__ __forceinline__ unsigned group_mask() {
 // row buffer stride (complex elements): with N1 = 4 or 8 several line groups
 // share a half-warp, and a stride of W + 4 (W + 8) puts their exchange slots
 // on disjoint banks; W is a multiple of 16 for every listed side
+// wavelengths per row block at most (the engine caps row_group here)
+constexpr int kMaxRowGroup = 64;
+
 __host__ __device__ constexpr int reg_row_stride(int n1, int w) { return n1 == 4 ? w + 4 : (n1 == 8 ? w + 8 : w); }
 
 template <typename R, int C, bool REAL, int N1, int N2>
@@ -70,6 +73,9 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   const int nwin = p.nx * p.ny;
   for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
   for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
+  // phase scale k0 * direction of each wavelength of the block (formed once, in FP64)
+  __shared__ R s_kph[kMaxRowGroup];
+  for (int g2 = threadIdx.x; g2 < G; g2 += blockDim.x) s_kph[g2] = (R)(p.ks[lam0 + g2] * p.dir);
   const R sc = (R)p.in_scale;
   __syncthreads();
   const int line = threadIdx.x / N1, t = threadIdx.x % N1;
@@ -128,7 +134,7 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
           arg_b[1] = opw[(size_t)13 * HW + x];
         }
         for (int g2 = 0; g2 < G; ++g2) {
-          const R kph = (R)(p.ks[lam0 + g2] * p.dir);
+          const R kph = s_kph[g2];
           const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
           cpx<R> pb0, pb1;
           if (C == 4) {
