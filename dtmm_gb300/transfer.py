@@ -310,6 +310,29 @@ class DevicePlan:
     def tuning(self):
         return {k: int(getattr(self.desc, k)) for k in self.TUNABLES}
 
+    def capture(self, field_in, field_out, restore_from=None):
+        """Capture one transfer of ``field_in`` -> ``field_out`` as a CUDA graph.
+
+        With ``restore_from`` the graph first copies it into ``field_in`` (the
+        engine rewrites its input when npass > 1), so every replay computes
+        the same transfer.  Returns the graph; ``graph.replay()`` launches it
+        on the current stream.  Replays are bit-identical to ``run``.
+        """
+        import torch
+
+        st = torch.cuda.Stream(device=self.device)
+        if restore_from is not None:
+            field_in.copy_(restore_from)
+        self.run(field_in, field_out)  # outside the capture: attributes and lazy loading
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st, capture_error_mode="relaxed"):
+            if restore_from is not None:
+                field_in.copy_(restore_from)
+            self.run(field_in, field_out, stream=st.cuda_stream)
+        torch.cuda.synchronize(self.device)
+        return g
+
     def run(self, field_in, field_out, bulk=None, out_given=False, timed=False, stream=None):
         import torch
 
