@@ -21,7 +21,8 @@ PRECISION_DOUBLE = 1
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
                "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field", "dtmm_pom_field",
-               "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image", "dtmm_director2data")
+               "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image", "dtmm_director2data",
+               "dtmm_diffract_workspace_size", "dtmm_diffract")
 ABI_VERSION = 2
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -150,6 +151,10 @@ def load(build_if_missing=True):
     lib.dtmm_director2data.argtypes = [ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dtmm_diffract_workspace_size.restype = ctypes.c_size_t
+    lib.dtmm_diffract_workspace_size.argtypes = [ctypes.c_int] * 5
+    lib.dtmm_diffract.restype = ctypes.c_int
+    lib.dtmm_diffract.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p] * 4 + [ctypes.c_size_t, ctypes.c_void_p]
     if lib.dtmm_abi_version() != ABI_VERSION:
         raise ImportError("dtmm_gb300 library ABI mismatch")
     _LIB = lib

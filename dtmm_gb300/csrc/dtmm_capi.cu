@@ -956,6 +956,122 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// diffract (dtmm/diffract.py:254-299) in real space: fft2 -> per-k 4x4 matrix
+// -> ifft2, with the transfer's own row and column kernels
+// ---------------------------------------------------------------------------
+struct DiffractLayout {
+  size_t twH, permH, twW, permW, dmat, X, total;
+};
+
+DiffractLayout diffract_layout(int H, int W, int nimg, int nlam, int precision) {
+  DiffractLayout L{};
+  const size_t cplx = precision == DTMM_PRECISION_DOUBLE ? 16 : 8;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes);
+    return o;
+  };
+  L.twH = take(cplx * H);
+  L.permH = take(sizeof(int) * H);
+  L.twW = take(cplx * W);
+  L.permW = take(sizeof(int) * W);
+  L.dmat = precision == DTMM_PRECISION_DOUBLE ? 0 : take(cplx * 16 * (size_t)nlam * H * W);
+  L.X = take(cplx * 4 * (size_t)nimg * H * W);
+  L.total = off;
+  return L;
+}
+
+int check_diffract(int H, int W, int nimg, int nlam, int precision) {
+  if (H < 1 || W < 1 || nimg < 1 || nlam < 1) return fail(DTMM_EINVAL, "empty axis");
+  if (nimg % nlam) return fail(DTMM_EINVAL, "image count must be a multiple of the wavelength count");
+  if (nimg > 65535) return fail(DTMM_EINVAL, "too many images");
+  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "invalid precision");
+  FFTPlan p;
+  if (!make_plan(H, p) || !make_plan(W, p))
+    return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", H, W);
+  return DTMM_OK;
+}
+
+template <typename R>
+int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void* in, void* out, unsigned char* ws,
+                  const DiffractLayout& L, cudaStream_t st) {
+  int launches = 0;
+  FFTPlan pH, pW;
+  make_plan(H, pH);
+  make_plan(W, pW);
+  cpx<R>* twH = (cpx<R>*)(ws + L.twH);
+  cpx<R>* twW = (cpx<R>*)(ws + L.twW);
+  int* permH = (int*)(ws + L.permH);
+  int* permW = (int*)(ws + L.permW);
+  k_fft_tables<R><<<(H + 255) / 256, 256, 0, st>>>(pH, twH, permH);
+  CKL("k_fft_tables");
+  k_fft_tables<R><<<(W + 255) / 256, 256, 0, st>>>(pW, twW, permW);
+  CKL("k_fft_tables");
+  const cpx<R>* tab = (const cpx<R>*)dmat;
+  if (sizeof(R) == 4) {
+    const size_t n = 16 * (size_t)nlam * H * W;
+    k_convert<R, double><<<(unsigned)((n + 255) / 256), 256, 0, st>>>((cpx<R>*)(ws + L.dmat),
+                                                                       (const cpx<double>*)dmat, n);
+    CKL("k_convert");
+    tab = (const cpx<R>*)(ws + L.dmat);
+  }
+  cpx<R>* X = (cpx<R>*)(ws + L.X);
+  const size_t bytes = sizeof(cpx<R>) * 4 * (size_t)nimg * H * W;
+  CK(cudaMemcpyAsync(X, in, bytes, cudaMemcpyDeviceToDevice, st));
+  // rows forward (natural in and out)
+  const int nlines = nimg * 4 * H;
+  int lpb = std::max(1, std::min(16, 4096 / W));
+  size_t smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
+  if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", W);
+  CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_fft_rows<R, false><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>(X, nlines, W, pW, twW, permW, 1.0, lpb);
+  CKL("k_fft_rows");
+  // columns: forward transform, the per-k matrix, inverse transform (1/H)
+  Grid g;
+  g.H = H;
+  g.W = W;
+  g.NI = nimg;
+  g.nlam = nlam;
+  g.npol = 1;
+  g.nray = nimg / nlam;
+  ColParams p;
+  memset(&p, 0, sizeof(p));
+  p.cin = p.cout = 4;
+  p.kop = KOP_MAT;
+  p.ktab = tab;
+  p.ktab_ray_stride = 0;
+  p.ny = 1;
+  p.cy = nullptr;
+  p.j_only = -1;
+  p.cy_rows = 1;
+  p.do_fwd = 1;
+  p.inverse_out = 1;
+  p.out_scale = 1.0 / H;
+  p.plan = pH;
+  p.tw = twH;
+  p.perm = permH;
+  const size_t per = 4 * (size_t)H * sizeof(cpx<R>) * 2;
+  int tc = 1;
+  while (tc < 16 && per * (tc * 2) <= 72 * 1024) tc *= 2;
+  if (tc > W) tc = W;
+  p.tc = tc;
+  smem = per * tc + H * (sizeof(cpx<R>) + sizeof(int));
+  if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "column of %d pixels too large for one block", H);
+  CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_layer_col<R><<<dim3((W + tc - 1) / tc, nimg), 256, smem, st>>>(p, g, X, (cpx<R>*)out);
+  CKL("k_layer_col");
+  // rows inverse (1/W)
+  smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
+  CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_fft_rows<R, true><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((cpx<R>*)out, nlines, W, pW, twW, permW,
+                                                                   1.0 / W, lpb);
+  CKL("k_fft_rows");
+  return DTMM_OK;
+}
+
 int transfer_impl(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
                   void* stream, Prof* prof, int* launches) {
   g_err.clear();
@@ -1071,6 +1187,28 @@ int dtmm_planewave_field(int height, int width, int nimg, const void* coef, cons
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_planewave: %s", cudaGetErrorString(e));
   return DTMM_OK;
+}
+
+size_t dtmm_diffract_workspace_size(int height, int width, int nimg, int nlam, int precision) {
+  g_err.clear();
+  if (check_diffract(height, width, nimg, nlam, precision)) return 0;
+  return diffract_layout(height, width, nimg, nlam, precision).total;
+}
+
+int dtmm_diffract(int height, int width, int nimg, int nlam, int precision, const void* dmat, const void* field_in,
+                  void* field_out, void* workspace, size_t workspace_bytes, void* stream) {
+  g_err.clear();
+  int rc = check_diffract(height, width, nimg, nlam, precision);
+  if (rc) return rc;
+  if (!dmat || !field_in || !field_out || !workspace) return fail(DTMM_EINVAL, "null pointer");
+  const DiffractLayout L = diffract_layout(height, width, nimg, nlam, precision);
+  if (workspace_bytes < L.total) return fail(DTMM_ENOSPACE, "workspace too small (%zu < %zu)", workspace_bytes, L.total);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == DTMM_PRECISION_DOUBLE)
+    return diffract_impl<double>(height, width, nimg, nlam, dmat, field_in, field_out, (unsigned char*)workspace, L,
+                                 st);
+  return diffract_impl<float>(height, width, nimg, nlam, dmat, field_in, field_out, (unsigned char*)workspace, L,
+                              st);
 }
 
 }  // extern "C"

@@ -15,8 +15,9 @@ the same stream passes ``pmat`` and ``cmf`` as device tensors: a host-to-device
 copy from pageable memory would wait for that work.  The small jones / 4x4
 matrices are built on the host (``jonesvec``, ``polarizer``,
 ``rotated_matrix``, ``ray_jonesmat4x4``).
-Refocusing through a diffraction matrix (``dmat``) and k-space inputs are not
-on this path (``NotImplementedError``).
+Refocusing goes through a per-k diffraction matrix (``diffract``, the
+library's ``dtmm_diffract``); k-space inputs are not on this path
+(``NotImplementedError``).
 """
 from __future__ import annotations
 
@@ -84,6 +85,37 @@ def ray_jonesmat4x4(jmat, beta=0.0, phi=0.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.
     j4[..., 0::2, 0::2] = jm
     j4[..., 1::2, 1::2] = np.conj(jm)
     return f @ j4 @ np.linalg.inv(f)
+
+
+def field_diffraction_matrix(shape, ks, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), mode="b",
+                             betamax=0.8):
+    """Per-k 4x4 propagation matrix F . diag(exp(i alpha ks d)) . F^-1 of a
+    homogeneous isotropic medium over d pixels (dtmm/diffract.py:125), zero
+    for beta >= betamax; mode "t" / "r" keeps the forward / backward modes
+    only.  Shape (n_wavelengths, H, W, 4, 4), built on the host in FP64."""
+    from .illumination import _fftfreq_grid
+
+    epsv = np.asarray(epsv, np.complex128)
+    if not (epsv[0] == epsv[1] == epsv[2]):
+        raise NotImplementedError("field_diffraction_matrix: isotropic media only")
+    ks = np.abs(np.asarray(ks, np.float64)).reshape(-1)
+    beta, phi = _fftfreq_grid(shape, ks)
+    eps = epsv[0]
+    f = _iso_fmat(beta, phi, eps)
+    a = np.sqrt(eps - beta ** 2 + 0j)
+    alpha = np.stack([a, -a, a, -a], axis=-1)
+    cut = beta >= betamax
+    f[cut] = 0.0
+    alpha[cut] = 0.0
+    fi = np.zeros_like(f)
+    ok = ~cut
+    fi[ok] = np.linalg.inv(f[ok])
+    ph = np.exp(1j * (ks * d)[:, None, None, None] * alpha)
+    if mode in ("t", +1):
+        ph[..., 1::2] = 0.0
+    elif mode in ("r", -1):
+        ph[..., ::2] = 0.0
+    return (f * ph[..., None, :]) @ fi
 
 
 # ---------------------------------------------------------------------------
@@ -171,19 +203,70 @@ def _desc(f, jvec, pmat, window):
 # ---------------------------------------------------------------------------
 # the reference's functions
 # ---------------------------------------------------------------------------
-def calculate_pom_field(field, jvec=None, pmat=None, dmat=None, window=None, input_fft=False, output_fft=False,
-                        out=None):
-    """Polarizer, window and analyzer applied to a transferred field
-    (dtmm/field_viewer.py:70): field [..., (2,) lam, 4, H, W] -> [..., lam, 4, H, W]."""
-    if dmat is not None or input_fft or output_fft:
-        raise NotImplementedError("refocusing (dmat) and k-space fields are outside the GPU POM path")
+def _pom_field_dev(f, jvec, pmat, window):
     torch = _torch()
-    f, host = _dev_field(field)
     d, keep, lead = _desc(f, jvec, pmat, window)
     res = torch.empty(lead + tuple(f.shape[-4:]), dtype=f.dtype, device=f.device)
     lib = _lib.load()
     _lib.check(lib.dtmm_pom_field(ctypes.byref(d), ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(res.data_ptr()),
                                   _stream(f.device)))
+    res._dtmm_keep = keep
+    return res
+
+
+def _diffract_dev(f, dmat):
+    torch = _torch()
+    h, w = f.shape[-2:]
+    nlam = f.shape[-4]
+    nimg = int(np.prod(f.shape[:-3]))
+    dm = dmat if isinstance(dmat, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(dmat, np.complex128))
+    dm = dm.to(device=f.device, dtype=torch.complex128).contiguous()
+    if tuple(dm.shape) != (nlam, h, w, 4, 4):
+        raise ValueError("dmat must have shape (n_wavelengths, H, W, 4, 4)")
+    prec = _precision(f)
+    lib = _lib.load()
+    nbytes = int(lib.dtmm_diffract_workspace_size(int(h), int(w), nimg, int(nlam), prec))
+    if nbytes == 0:
+        raise ValueError(_lib.last_error())
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=f.device)
+    out = torch.empty_like(f)
+    _lib.check(lib.dtmm_diffract(int(h), int(w), nimg, int(nlam), prec, ctypes.c_void_p(dm.data_ptr()),
+                                 ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                 ctypes.c_void_p(ws.data_ptr()), ctypes.c_size_t(nbytes), _stream(f.device)))
+    out._dtmm_keep = (dm, ws)
+    return out
+
+
+def diffract(field, dmat, window=None, out=None):
+    """fft2, per-k 4x4 matrix ``dmat`` (n_wavelengths, H, W, 4, 4), ifft2,
+    optional real-space window (dtmm/diffract.py:254), on the GPU."""
+    f, host = _dev_field(field)
+    res = _diffract_dev(f, dmat)
+    if window is not None:
+        res = _pom_field_dev(res, None, None, window)
+    if host:
+        r = res.cpu().numpy().astype(np.complex128)
+        if out is not None:
+            out[...] = r
+            return out
+        return r
+    return res
+
+
+def calculate_pom_field(field, jvec=None, pmat=None, dmat=None, window=None, input_fft=False, output_fft=False,
+                        out=None):
+    """Polarizer, refocus, window and analyzer applied to a transferred field
+    (dtmm/field_viewer.py:70, real-space path): field [..., (2,) lam, 4, H, W]
+    -> [..., lam, 4, H, W]; ``dmat`` (n_wavelengths, H, W, 4, 4) refocuses
+    through ``diffract``."""
+    if input_fft or output_fft:
+        raise NotImplementedError("k-space fields are outside the GPU POM path")
+    f, host = _dev_field(field)
+    if dmat is None:
+        res = _pom_field_dev(f, jvec, pmat, window)
+    else:
+        g = _pom_field_dev(f, jvec, None, None) if jvec is not None else f
+        res = _pom_field_dev(_diffract_dev(g, dmat), None, pmat, window)
     if host:
         r = res.cpu().numpy().astype(np.complex128)
         if out is not None:
@@ -307,5 +390,5 @@ def pom_image(field, cmf, jvec=None, pmat=None, window=None, norm=False, gamma=T
     return rgb.cpu().numpy() if host else rgb
 
 
-__all__ = ["jonesvec", "polarizer", "rotated_matrix", "ray_jonesmat4x4", "calculate_pom_field", "field2specter",
-           "field2spectersum", "specter2color", "pom_image"]
+__all__ = ["jonesvec", "polarizer", "rotated_matrix", "ray_jonesmat4x4", "field_diffraction_matrix", "diffract",
+           "calculate_pom_field", "field2specter", "field2spectersum", "specter2color", "pom_image"]

@@ -211,6 +211,16 @@ int dtmm_specter2color(long long npix, int nlam, const double* spec, const doubl
 int dtmm_pom_image(const dtmm_pom_desc* desc, const void* field, const double* cmf, int norm_mode,
                    double norm_value, double gamma, int gray, float* rgb, void* stream);
 
+/* diffract (dtmm/diffract.py:254-299) in real space: fft2, a per-k 4x4
+   matrix, ifft2.  field_in / field_out: device [nimg][4][H][W] (complex64
+   for precision MIXED, complex128 for DOUBLE; image i uses wavelength
+   i % nlam); dmat: device complex128 [nlam][H][W][4][4] (the reference's
+   field_diffraction_matrix layout); workspace: caller-provided device
+   memory of dtmm_diffract_workspace_size bytes. */
+size_t dtmm_diffract_workspace_size(int height, int width, int nimg, int nlam, int precision);
+int dtmm_diffract(int height, int width, int nimg, int nlam, int precision, const void* dmat, const void* field_in,
+                  void* field_out, void* workspace, size_t workspace_bytes, void* stream);
+
 /* director2data (dtmm/data.py:277-320) on the device: director[nvox][3]
    (float64, or float32 when director_double == 0) -> eps eigenvalues
    epsv[nvox][3] and Euler angles epsa[nvox][3] (float64).  The order

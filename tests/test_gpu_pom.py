@@ -1,9 +1,10 @@
 """POM image formation kernels against the reference's outputs (GPU).
 
 Fixtures ``tests/golden/pom_*.npz`` hold the reference's POM field, specter
-and colours for each case; the refocused case (diffraction matrix, outside
-the GPU path) is checked against the oracle's chain without refocus.
-Tolerances: POM field 1e-13 relative (complex128) / 1e-6 (complex64);
+and colours for each case (one refocused through a diffraction matrix); the
+fused image kernel has no refocus, so for that case it is checked against the
+oracle's chain without refocus.
+Tolerances: POM field 1e-12 relative (complex128) / 1e-6 (complex64);
 specter 1e-13 relative; colours from a specter 1e-13 absolute; the fused
 float32 image 2e-6 absolute (complex128 field) / 2e-5 (complex64).
 """
@@ -52,12 +53,26 @@ def _expected_pom(case, z, jvec, pmat, win):
 @pytest.mark.parametrize("precision", ["double", "mixed"])
 @pytest.mark.parametrize("name", sorted(POM_CASES))
 def test_pom_field(name, precision):
+    """calculate_pom_field, with the refocus (diffraction matrix) where the case has one."""
     from dtmm_gb300 import pom
 
     case, z, jvec, pmat, win = _inputs(name)
     f = z["field_in"].astype(np.complex128 if precision == "double" else np.complex64)
-    got = pom.calculate_pom_field(f, jvec, pmat, window=win)
-    assert rel(got, _expected_pom(case, z, jvec, pmat, win)) < (1e-13 if precision == "double" else 1e-6)
+    dmat = z["dmat"] if "dmat" in z.files else None
+    got = pom.calculate_pom_field(f, jvec, pmat, dmat, window=win)
+    assert rel(got, z["pom"]) < (1e-12 if precision == "double" else 1e-6)
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_diffract_matches_oracle(precision):
+    import dtmm_oracle as O
+    from dtmm_gb300 import pom
+
+    z = np.load(os.path.join(HERE, "golden", "pom_rotated.npz"))
+    f = z["field_in"][0]  # x-polarised input: (lam, 4, H, W)
+    want = O.diffract(f, z["dmat"])
+    got = pom.diffract(f.astype(np.complex128 if precision == "double" else np.complex64), z["dmat"])
+    assert rel(got, want) < (1e-12 if precision == "double" else 1e-6)
 
 
 @pytest.mark.parametrize("name", sorted(POM_CASES))

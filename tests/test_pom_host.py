@@ -55,3 +55,11 @@ def test_oracle_pom_pipeline_matches_reference(name):
     assert rel(spec, z["spec"]) < 1e-13
     for key, kw in COLOR_OPTS:
         assert np.abs(O.specter2color(z["spec"], z["cmf"], **kw) - z[key]).max() < 1e-14, key
+
+
+def test_field_diffraction_matrix_matches_reference():
+    z = np.load(os.path.join(HERE, "golden", "pom_rotated.npz"))
+    ks = 2 * np.pi / z["wavelengths"] * 50.0  # pixel size of the source case
+    dm = pom.field_diffraction_matrix(z["field_in"].shape[-2:], ks, d=POM_CASES["pom_rotated"]["dmat_d"],
+                                      epsv=(2.25, 2.25, 2.25))
+    assert np.abs(dm - z["dmat"]).max() < 1e-14
