@@ -37,6 +37,11 @@ def deps():
         os.path.join(ROOT, "include", "dtmm_gb300.h")]
 
 
+# per-file options: the Q-tensor eigensolver rounds every sum and product
+# separately, as the double arithmetic it restates does
+FILE_FLAGS = {"dtmm_qdata.cu": ["-fmad=false"]}
+
+
 def lib_path():
     return os.path.join(LIBDIR, LIBNAME)
 
@@ -64,7 +69,9 @@ def build(force=False, verbose=False):
     objs = [os.path.join(objdir, os.path.basename(f)[:-3] + ".o") for f in srcs]
 
     def compile_one(i):
-        return subprocess.run([nvcc_path()] + flags + ["-c", srcs[i], "-o", objs[i]], capture_output=True, text=True)
+        extra = FILE_FLAGS.get(os.path.basename(srcs[i]), [])
+        return subprocess.run([nvcc_path()] + flags + extra + ["-c", srcs[i], "-o", objs[i]], capture_output=True,
+                              text=True)
 
     jobs = max(1, min(len(srcs), os.cpu_count() or 1))
     with ThreadPoolExecutor(max_workers=jobs) as ex:

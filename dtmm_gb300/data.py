@@ -7,6 +7,11 @@ Euler angles, computed per voxel by the library's ``dtmm_director2data``
 kernel.  With a CUDA tensor the block stays on the device (``device_material``
 wraps it for ``plan_transfer``); with a numpy array the result comes back as
 numpy, as the reference returns it.
+
+``Q2data`` mirrors dtmm.data.Q2data (dtmm/data.py:322-371): a Q-tensor field
+[L, H, W, 6] (or [..., 3, 3]) becomes the same optical block through the
+per-voxel eps tensor, its eigen-decomposition and the Euler angles of the
+eigenvector frame (``dtmm_q2data``).
 """
 from __future__ import annotations
 
@@ -60,6 +65,55 @@ def director2data(director, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=
     return thickness, epsv, epsa
 
 
+_Q_ROWS = (0, 1, 2, 0, 0, 1)
+_Q_COLS = (0, 1, 2, 1, 2, 2)
+
+
+def _q_run(tensor, mask, no, ne, nhost, scale_factor, biaxial):
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("dtmm_gb300.data needs a CUDA GPU (there is no CPU path)")
+    host = not isinstance(tensor, torch.Tensor)
+    q = torch.from_numpy(np.ascontiguousarray(tensor)) if host else tensor
+    if q.is_complex():
+        raise ValueError("Q2data takes a real Q tensor")
+    if q.shape[-1] != 6:
+        if tuple(q.shape[-2:]) != (3, 3):
+            raise ValueError("input tensor must be an array of shape (...,6) or (...,3,3)")
+        q = q[..., list(_Q_ROWS), list(_Q_COLS)]
+    q = q.to(dtype=torch.float64).cuda().contiguous()
+    dev = q.device
+    shape = tuple(q.shape[:-1])
+    m = None
+    if mask is not None:
+        if nhost is None:
+            raise ValueError("nhost must be given with a mask")
+        mt = torch.from_numpy(np.ascontiguousarray(mask)) if not isinstance(mask, torch.Tensor) else mask
+        m = mt.to(device=dev, dtype=torch.uint8).contiguous()
+        if tuple(m.shape) != shape:
+            raise ValueError("mask must have the tensor field's shape")
+    epsv = torch.empty(shape + (3,), dtype=torch.float64, device=dev)
+    epsa = torch.empty(shape + (3,), dtype=torch.float64, device=dev)
+    lib = _lib.load()
+    _lib.check(lib.dtmm_q2data(int(np.prod(shape)), ctypes.c_void_p(q.data_ptr()),
+                               ctypes.c_void_p(m.data_ptr() if m is not None else None), float(no), float(ne),
+                               float(nhost if nhost is not None else 1.0), float(scale_factor), int(bool(biaxial)),
+                               ctypes.c_void_p(epsv.data_ptr()), ctypes.c_void_p(epsa.data_ptr()),
+                               ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+    return epsv, epsa, host, (m, q)
+
+
+def Q2data(tensor, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, biaxial=False, thickness=None):
+    """Optical block ``(thickness, epsv, epsa)`` from a Q-tensor field (dtmm/data.py:322)."""
+    epsv, epsa, host, _ = _q_run(tensor, mask, no, ne, nhost, scale_factor, biaxial)
+    nl = epsv.shape[0]
+    thickness = np.ones((nl,)) if thickness is None else np.asarray(thickness, np.float64)
+    if host:
+        return thickness, epsv.cpu().numpy(), epsa.cpu().numpy()
+    return thickness, epsv, epsa
+
+
 def device_material(director, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0,
                     thickness=None):
     """``director2data`` kept on the device as a ``DeviceMaterial`` for ``plan_transfer``."""
@@ -71,4 +125,14 @@ def device_material(director, shape=None, mask=None, no=1.5, ne=1.6, nhost=None,
     return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape)
 
 
-__all__ = ["director2data", "device_material"]
+def q_material(tensor, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, thickness=None):
+    """Uniaxial ``Q2data`` kept on the device as a ``DeviceMaterial`` for ``plan_transfer``."""
+    from .transfer import DeviceMaterial
+
+    epsv, epsa, _, _ = _q_run(tensor, mask, no, ne, nhost, scale_factor, False)
+    nl = epsv.shape[0]
+    th = np.ones((nl,)) if thickness is None else np.asarray(thickness, np.float64)
+    return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape, uniaxial=True)
+
+
+__all__ = ["director2data", "Q2data", "device_material", "q_material"]

@@ -229,6 +229,16 @@ int dtmm_diffract(int height, int width, int nimg, int nlam, int precision, cons
 int dtmm_director2data(long long nvox, const void* director, int director_double, const void* mask, double no,
                        double ne, double nhost, double scale_factor, double* epsv, double* epsa, void* stream);
 
+/* Q2data (dtmm/data.py:322-371) on the device: Q tensors qtensor[nvox][6]
+   (float64: Q00, Q11, Q22, Q01, Q02, Q12) -> eps = (ne^2 - no^2) /
+   scale_factor * Q + (2 no^2 + ne^2) / 3 * I, its eigenvalues epsv[nvox][3]
+   sorted with the most distinct one last and the Euler angles epsa[nvox][3]
+   of its eigenvector frame (float64).  Unless biaxial != 0 the eigenvalues
+   are replaced by their uniaxial order 1; voxels where mask[i] == 0 (uint8
+   [nvox], optional) get nhost^2. */
+int dtmm_q2data(long long nvox, const double* qtensor, const void* mask, double no, double ne, double nhost,
+                double scale_factor, int biaxial, double* epsv, double* epsa, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

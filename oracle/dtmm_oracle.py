@@ -25,6 +25,7 @@ biaxial voxels, isotropic effective layers (eff_data 0).
 """
 from __future__ import annotations
 
+import math
 import os
 import warnings
 
@@ -1416,6 +1417,180 @@ def director2data(director, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=
     if mask is not None:
         epsv[np.logical_not(mask), :] = nhost ** 2
     epsa = np.stack([np.zeros_like(x), np.arctan2(np.sqrt(x ** 2 + y ** 2), z), np.arctan2(y, x)], axis=-1)
+    if thickness is None:
+        thickness = np.ones((epsv.shape[0],))
+    return thickness, epsv, epsa
+
+
+# ---------------------------------------------------------------------------
+# Q tensor -> optical data
+# ---------------------------------------------------------------------------
+def Q2eps(tensor, no=1.5, ne=1.6, scale_factor=1.0):
+    """eps tensor (..., 6) from a Q tensor (..., 6): (ne^2 - no^2)/scale Q + mean eps on the diagonal
+    (dtmm/data.py:432-487)."""
+    q = np.asarray(tensor, FDTYPE)
+    epsa = (ne ** 2 - no ** 2) / scale_factor
+    epsm = (no ** 2 * 2 + ne ** 2) / 3.0
+    out = np.empty_like(q)
+    out[..., 0:3] = epsa * q[..., 0:3] + epsm
+    out[..., 3:] = epsa * q[..., 3:]
+    return out
+
+
+def _cross3(a, b):
+    return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+
+def _sq3(v):
+    # sum of squares in the order 0, 1, 2 (dtmm/linalg.py:14-20)
+    out = 0.0
+    for x in v:
+        out = out + x * x
+    return out
+
+
+def _eigvec_first(a00, a11, a22, a01, a02, a12, ev):
+    """Eigenvector of `ev`: the longest cross product of two rows of A - ev I, normalised
+    (dtmm/linalg.py:44-89)."""
+    r0 = [a00 - ev, a01, a02]
+    r1 = [a01, a11 - ev, a12]
+    r2 = [a02, a12, a22 - ev]
+    c01, c12, c02 = _cross3(r0, r1), _cross3(r1, r2), _cross3(r0, r2)
+    d0, d1, d2 = _sq3(c01), _sq3(c02), _sq3(c12)
+    best, dmax = c01, d0
+    if d1 > dmax:
+        best, dmax = c02, d1
+    if d2 > dmax:
+        best = c12
+    norm = 1.0 / (best[0] * best[0] + best[1] * best[1] + best[2] * best[2]) ** 0.5
+    return [x * norm for x in best]
+
+
+def _eigvec_second(a00, a11, a22, a01, a02, a12, w, ev):
+    """Eigenvector of `ev` orthogonal to w: minimise in the plane orthogonal to w
+    (dtmm/linalg.py:92-160)."""
+    if abs(w[0]) > abs(w[1]):
+        u = [-w[2], 0.0, w[0]]
+    else:
+        u = [0.0, w[2], -w[1]]
+    scale = 1.0 / _sq3(u) ** 0.5
+    u = [x * scale for x in u]
+    v = _cross3(w, u)
+    au = [a00 * u[0] + a01 * u[1] + a02 * u[2], a01 * u[0] + a11 * u[1] + a12 * u[2],
+          a02 * u[0] + a12 * u[1] + a22 * u[2]]
+    m00 = u[0] * au[0] + u[1] * au[1] + u[2] * au[2] - ev
+    av = [a00 * v[0] + a01 * v[1] + a02 * v[2], a01 * v[0] + a11 * v[1] + a12 * v[2],
+          a02 * v[0] + a12 * v[1] + a22 * v[2]]
+    m01 = u[0] * av[0] + u[1] * av[1] + u[2] * av[2]
+    m11 = v[0] * av[0] + v[1] * av[1] + v[2] * av[2] - ev
+    if abs(m00) >= abs(m11):
+        if max(abs(m00), abs(m01)) > 0:
+            if abs(m00) >= abs(m01):
+                m01 = m01 / m00
+                m00 = 1.0 / (1.0 + m01 ** 2) ** 0.5
+                m01 = m01 * m00
+            else:
+                m00 = m00 / m01
+                m01 = 1.0 / (1.0 + m00 ** 2) ** 0.5
+                m00 = m00 * m01
+            return [m01 * u[i] - m00 * v[i] for i in range(3)]
+        return u
+    if max(abs(m11), abs(m01)) > 0:
+        if abs(m11) >= abs(m01):
+            m01 = m01 / m11
+            m11 = 1.0 / (1.0 + m01 ** 2) ** 0.5
+            m01 = m01 * m11
+        else:
+            m11 = m11 / m01
+            m01 = 1.0 / (1.0 + m11 ** 2) ** 0.5
+            m11 = m11 * m01
+        return [m11 * u[i] - m01 * v[i] for i in range(3)]
+    return u
+
+
+def tensor_eig_1(t6):
+    """Eigenvalues and eigenvectors (rows) of one real symmetric 3x3 tensor
+    (t00, t11, t22, t01, t02, t12) by the non-iterative eigensolver of
+    D. Eberly, "A Robust Eigensolver for 3x3 Symmetric Matrices" (Geometric
+    Tools), as used by dtmm/linalg.py:225-300, then sorted so that the third
+    eigenvalue is the most distinct, by a cyclic permutation (dtmm/linalg.py:171-218)."""
+    t00, t11, t22, t01, t02, t12 = (float(x) for x in t6)
+    scale = max(max(abs(t00), abs(t11)), max(abs(t22), abs(t01)), max(abs(t02), abs(t12)))
+    vec = np.eye(3)
+    if scale == 0.0:
+        eig = np.zeros(3)
+    else:
+        s = 1.0 / scale
+        a00, a11, a22, a01, a02, a12 = t00 * s, t11 * s, t22 * s, t01 * s, t02 * s, t12 * s
+        q = (a00 + a11 + a22) / 3
+        b00, b11, b22 = a00 - q, a11 - q, a22 - q
+        norm = a01 ** 2 + a02 ** 2 + a12 ** 2
+        if abs(norm) > 1e-12:
+            p = ((b00 ** 2 + b11 ** 2 + b22 ** 2 + 2 * norm) / 6) ** 0.5
+            c00 = b11 * b22 - a12 * a12
+            c01 = a01 * b22 - a12 * a02
+            c02 = a01 * a12 - b11 * a02
+            half_det = (b00 * c00 - a01 * c01 + a02 * c02) / (p * p * p * 2)
+            half_det = min(max(half_det, -1.0), 1.0)
+            phi = math.acos(half_det) / 3.0
+            e0 = math.cos(phi + 2.09439510239319549) * 2
+            e2 = math.cos(phi) * 2
+            e1 = -(e0 + e2)
+            e0, e1, e2 = e0 * p + q, e1 * p + q, e2 * p + q
+            if half_det >= 0:
+                v2 = _eigvec_first(a00, a11, a22, a01, a02, a12, e2)
+                v1 = _eigvec_second(a00, a11, a22, a01, a02, a12, v2, e1)
+                v0 = _cross3(v1, v2)
+            else:
+                v0 = _eigvec_first(a00, a11, a22, a01, a02, a12, e0)
+                v1 = _eigvec_second(a00, a11, a22, a01, a02, a12, v0, e1)
+                v2 = _cross3(v0, v1)
+            vec = np.array([v0, v1, v2])
+            eig = np.array([e0 * scale, e1 * scale, e2 * scale])
+        else:
+            eig = np.array([a00 * scale, a11 * scale, a22 * scale])
+    m2, m1, m0 = abs(eig[1] - eig[0]), abs(eig[2] - eig[0]), abs(eig[2] - eig[1])
+    i, j, k = 0, 1, 2
+    if m2 > m1 or m2 > m0:
+        i, j, k = (1, 2, 0) if m1 > m0 else (2, 0, 1)
+    return eig[[i, j, k]], vec[[i, j, k]]
+
+
+def rotation_angles_1(R):
+    """Euler angles (psi, theta, phi) of a rotation matrix (dtmm/rotation.py:154-174)."""
+    r22 = max(-1.0, min(1.0, R[2, 2]))
+    theta = np.arccos(r22)
+    if (R[1, 2] == 0.0 and R[0, 2] == 0.0) or theta == 0.0:
+        psi = 0.0
+        phi = np.arccos(max(-1.0, min(1.0, R[1, 1])))
+    else:
+        phi = np.arctan2(R[1, 2], R[0, 2])
+        psi = np.arctan2(R[2, 1], -R[2, 0])
+    return np.array([psi, theta, phi])
+
+
+def Q2data(tensor, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, biaxial=False, thickness=None):
+    """Optical block from a Q tensor field (..., 6) (dtmm/data.py:322-371): eps tensor (Q2eps),
+    its sorted eigenvalues and the Euler angles of the eigenvector matrix (eps2epsva, :489),
+    the uniaxial order 1 of the eigenvalues unless biaxial, host eps outside the mask."""
+    eps = Q2eps(tensor, no, ne, scale_factor)
+    flat = eps.reshape(-1, 6)
+    epsv = np.empty((flat.shape[0], 3))
+    epsa = np.empty((flat.shape[0], 3))
+    for n, t in enumerate(flat):
+        ev, vec = tensor_eig_1(t)
+        epsv[n] = ev
+        epsa[n] = rotation_angles_1(vec.T)  # eigenvectors in columns
+    epsv = epsv.reshape(eps.shape[:-1] + (3,))
+    epsa = epsa.reshape(eps.shape[:-1] + (3,))
+    if not biaxial:
+        m = (epsv[..., 0] + epsv[..., 1] + epsv[..., 2]) / 3.0
+        delta = epsv[..., 2] - (epsv[..., 0] + epsv[..., 1]) / 2.0
+        e1 = m - 1.0 / 3.0 * 1 * delta
+        e3 = m + 2.0 / 3.0 * 1 * delta
+        epsv = np.stack([e1, e1, e3], axis=-1)
+    if mask is not None:
+        epsv[np.logical_not(mask), :] = nhost ** 2
     if thickness is None:
         thickness = np.ones((epsv.shape[0],))
     return thickness, epsv, epsa

@@ -167,11 +167,38 @@ def save_files(dtmm):
     print("io files               io_field.dtmf io_stack.dtms")
 
 
+def save_qtensor(dtmm):
+    """Reference Q2data on seeded Q tensors (uniaxial from random directors with random order,
+    some exactly diagonal, plus small biaxial parts), uniaxial and biaxial variants."""
+    rng = np.random.Generator(np.random.PCG64(91))
+    shape = (2, 6, 7)
+    n = rng.normal(size=shape + (3,))
+    n /= np.linalg.norm(n, axis=-1)[..., None]
+    S = rng.uniform(0.2, 0.9, size=shape)
+    Q = np.empty(shape + (6,))
+    Q[..., 0] = S * (n[..., 0] ** 2 - 1 / 3)
+    Q[..., 1] = S * (n[..., 1] ** 2 - 1 / 3)
+    Q[..., 2] = S * (n[..., 2] ** 2 - 1 / 3)
+    Q[..., 3] = S * n[..., 0] * n[..., 1]
+    Q[..., 4] = S * n[..., 0] * n[..., 2]
+    Q[..., 5] = S * n[..., 1] * n[..., 2]
+    Q[0, 0, :3, :3] = [[-0.2, -0.2, 0.4], [0.4, -0.2, -0.2], [-0.2, 0.4, -0.2]]  # diagonal tensors
+    Q[0, 0, :3, 3:] = 0.0
+    Q[1] += rng.normal(scale=0.02, size=Q[1].shape)
+    mask = rng.uniform(size=shape) > 0.2
+    a = dtmm.data.Q2data(Q)
+    b = dtmm.data.Q2data(Q, mask=mask, no=1.52, ne=1.71, nhost=1.4, scale_factor=0.9)
+    c = dtmm.data.Q2data(Q, biaxial=True)
+    np.savez_compressed(os.path.join(HERE, "qtensor.npz"), Q=Q, mask=mask, epsv=a[1], epsa=a[2],
+                        epsv_masked=b[1], epsa_masked=b[2], epsv_biaxial=c[1], epsa_biaxial=c[2])
+    print("qtensor                %s" % (Q.shape,))
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files"])
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files", "qtensor"])
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
@@ -184,6 +211,8 @@ def main(argv):
             save_director(dtmm)
         elif name == "files":
             save_files(dtmm)
+        elif name == "qtensor":
+            save_qtensor(dtmm)
         else:
             run_case(name, dtmm)
 
