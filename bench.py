@@ -397,6 +397,137 @@ def run_2x2(args, dev):
 
 
 # ---------------------------------------------------------------------------
+# the rows either side of the transfer: POM image, refocus, director / Q-tensor
+# -> optical data; each timed alone on inputs larger than L2
+# ---------------------------------------------------------------------------
+def run_rows(args, dev, cpu=True):
+    import torch
+
+    from dtmm_gb300 import data, pom, samples
+
+    O = None
+    if cpu:  # the oracle, for the CPU baseline legs only
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import dtmm_oracle as O
+    peak, peak_kind = measured_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        ts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    def cpu_rate(fn, items):
+        t0 = time.perf_counter()
+        fn()
+        return items / (time.perf_counter() - t0)
+
+    def row(name, workload, items, unit, nbytes, ms, launches, cpu_value, cpu_sample, cores=1):
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out = {"workload": workload, "value": items / (ms / 1e3), "unit": unit, "ms_per_call": ms,
+               "gpu_launches_per_call": launches,
+               "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                            "bytes_per_call": nbytes, "peak_source": peak_kind}}
+        if cpu_value is not None:
+            out["cpu_baseline"] = {"value": cpu_value, "unit": unit, "cores": cores, "kind": "port",
+                                   "sample": cpu_sample}
+        return name, out
+
+    res = {}
+    wl = WAVELENGTHS
+    cmf_h = samples.transmission_cmf(wl)
+    cmf = torch.from_numpy(cmf_h).to(dev)
+    jvec = pom.jonesvec((1, 0))
+    pmat_h = pom.ray_jonesmat4x4(pom.polarizer(pom.jonesvec((0, 1))))
+    pmat = torch.from_numpy(pmat_h).to(dev)
+
+    # POM image: x / y fields of 9 wavelengths on a 1024^2 grid -> sRGB
+    H = W = 1024
+    f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
+    ms = timed(lambda: pom.pom_image(f, cmf, jvec, pmat, stream=stream.cuda_stream))
+    nbytes = f.numel() * 8 + H * W * 3 * 4
+    cv = None
+    if cpu:
+        fh = f[:, :, :, :512, :512].cpu().numpy().astype(np.complex128)
+        cv = cpu_rate(lambda: O.specter2color(O.field2specter(O.calculate_pom_field(fh, jvec, pmat_h)), cmf_h),
+                      512 * 512 * len(wl))
+    res.update([row("pom_image", "POM image (x polarizer, crossed analyzer, sRGB) of x+y fields, 9 wavelengths, "
+                                 "1024x1024 grid, complex64", H * W * len(wl), "pixel·λ/s", nbytes, ms, 1, cv,
+                    "same pipeline, 512x512 crop, oracle (numpy; FFTs on every core, the rest on one)",
+                    os.cpu_count() or 1)])
+    del f
+
+    # refocus: fft2, per-k 4x4 matrix, ifft2 of x+y fields, 9 wavelengths, 512^2
+    H = W = 512
+    f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
+    ks = 2 * np.pi / wl * PIXELSIZE
+    dm_h = pom.field_diffraction_matrix((H, W), ks, d=-20.0, epsv=(1.5 ** 2,) * 3)
+    dm = torch.from_numpy(dm_h).to(dev)
+    ms = timed(lambda: pom.diffract(f, dm))
+    nbytes = 2 * f.numel() * 8 + dm.numel() * 16
+    cv = None
+    if cpu:
+        fh = f[:, :, :, :256, :256].cpu().numpy().astype(np.complex128)
+        dmh = pom.field_diffraction_matrix((256, 256), ks, d=-20.0, epsv=(1.5 ** 2,) * 3)
+        cv = cpu_rate(lambda: O.diffract(fh, dmh), 2 * 256 * 256 * len(wl))
+    res.update([row("diffract", "refocus by -20 px in n=1.5 (fft2, per-k 4x4 matrix, ifft2) of x+y fields, "
+                                "9 wavelengths, 512x512 grid, complex64 fields, complex128 matrices",
+                    2 * H * W * len(wl), "pixel·λ/s", nbytes, ms, 6, cv,
+                    "same refocus, 256x256 grid, oracle (scipy fft on every core, matrices on one)",
+                    os.cpu_count() or 1)])
+    del f, dm
+
+    # director -> optical data: 128 layers of 512^2
+    L, H, W = 128, 512, 512
+    d = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
+    ms = timed(lambda: data.director2data(d, no=1.52, ne=1.71))
+    nvox = L * H * W
+    cv = None
+    if cpu:
+        dh = d[:32, :256, :256].cpu().numpy()
+        cv = cpu_rate(lambda: O.director2data(dh, no=1.52, ne=1.71), dh.size // 3)
+    res.update([row("director2data", "director2data, 128x512x512 float64 directors", nvox, "voxel/s",
+                    nvox * (24 + 48), ms, 1, cv, "32x256x256 directors, oracle (numpy)")])
+    del d
+
+    # Q tensor -> optical data: 64 layers of 512^2, uniaxial Q of random directors and orders
+    L = 64
+    n = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
+    n = n / n.norm(dim=-1, keepdim=True)
+    S = torch.rand((L, H, W), dtype=torch.float64, device=dev, generator=gen) * 0.7 + 0.2
+    q = torch.stack([S * (n[..., 0] ** 2 - 1 / 3), S * (n[..., 1] ** 2 - 1 / 3), S * (n[..., 2] ** 2 - 1 / 3),
+                     S * n[..., 0] * n[..., 1], S * n[..., 0] * n[..., 2], S * n[..., 1] * n[..., 2]], dim=-1)
+    del n, S
+    ms = timed(lambda: data.Q2data(q, no=1.52, ne=1.71))
+    nvox = L * H * W
+    cv = None
+    if cpu:
+        qh = q[:4, :64, :64].cpu().numpy()
+        cv = cpu_rate(lambda: O.Q2data(qh, no=1.52, ne=1.71), qh.size // 6)
+    name, r = row("q2data", "Q2data (uniaxial), 64x512x512 float64 Q tensors", nvox, "voxel/s", nvox * (48 + 48),
+                  ms, 1, cv, "4x64x64 Q tensors, oracle (per-voxel Python, 1 core)")
+    r["roofline"]["note"] = "FP64-bound: one eigen-solve (acos, 2 cos, 3 sqrt, divides) and 2 atan2 + acos per voxel"
+    res[name] = r
+    del q
+    torch.cuda.synchronize(dev)
+    return res
+
+
+# ---------------------------------------------------------------------------
 # serving: Poisson stream of requests, continuous batching under an HBM budget
 # ---------------------------------------------------------------------------
 def run_serve(args, dev):
@@ -450,9 +581,10 @@ def main():
     ap.add_argument("--no-c128", action="store_true", help="skip the complex128 comparison run")
     ap.add_argument("--layers", type=int, default=NLAYERS, help="layers (profiling runs use fewer; same kernels)")
     ap.add_argument("--npass", type=int, default=OPTS["npass"])
-    ap.add_argument("--workload", default="precision", choices=["precision", "batch", "serve", "2x2"],
+    ap.add_argument("--workload", default="precision", choices=["precision", "batch", "serve", "2x2", "rows"],
                     help="precision: 256x256 4x4 npass 3 (default); batch: 48 instances in one graph; "
-                         "serve: Poisson request stream; 2x2: 1024x1024 2x2 diffraction 5")
+                         "serve: Poisson request stream; 2x2: 1024x1024 2x2 diffraction 5; rows: POM image, "
+                         "refocus, director2data and Q2data kernels")
     ap.add_argument("--streams", type=int, default=8, help="batch: streams in the graph")
     ap.add_argument("--c128-subset", type=int, default=8, help="batch: instances of the complex128 comparison")
     ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the trace")
@@ -461,6 +593,8 @@ def main():
     ap.add_argument("--hbm-budget", type=float, default=150e9, help="serve: admission budget (bytes)")
     ap.add_argument("--no-batch", action="store_true", help="precision workload: skip the batch summary")
     ap.add_argument("--no-serve", action="store_true", help="precision workload: skip the serving summary")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="precision workload: skip the POM / refocus / director / Q-tensor kernel summary")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -486,6 +620,20 @@ def main():
             dist.barrier()
 
     dev = torch.device("cuda", local)
+    if args.workload == "rows":
+        rows = run_rows(args, dev, cpu=not args.no_cpu and rank == 0)
+        if rank == 0:
+            pi = rows["pom_image"]
+            print(json.dumps({"metric": "POM image pixel·λ/s (with the refocus, director2data and Q2data rows)",
+                              "value": pi["value"], "unit": pi["unit"], "n_gpus": 1, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": pi["ms_per_call"], "higher_is_better": True,
+                              "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+                              "config": {"workload": pi["workload"], "l2": "flushed between timed calls"},
+                              "roofline": pi["roofline"], "cpu_baseline": pi.get("cpu_baseline"),
+                              "gpu_launches": args.steps, "rows": rows}))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if args.workload in ("batch", "serve", "2x2"):
         # independent replicas: every rank runs the whole workload on its own GPU
         res = {"batch": run_batch, "serve": run_serve, "2x2": run_2x2}[args.workload](args, dev)
@@ -631,9 +779,9 @@ def main():
                          "d2h_bytes_per_step": 2 * fbytes, "ms_per_step": e2e_s * 1e3}
 
     # the batching and serving configurations, summarised on the same line
-    if rank == 0 and not args.no_batch:
-        import copy
+    import copy
 
+    if rank == 0 and not args.no_batch:
         a2 = copy.copy(args)
         a2.steps, a2.warmup, a2.c128_subset = 2, 1, 4
         try:
@@ -652,6 +800,14 @@ def main():
                                                    "peak_budget_bytes", "clocks") if k in sv}
         except Exception as e:
             result["serve"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_rows:
+        try:
+            a2 = copy.copy(args)
+            a2.steps, a2.warmup = 5, 3
+            result["rows"] = run_rows(a2, dev, cpu=not args.no_cpu and world == 1)
+        except Exception as e:
+            result["rows"] = {"error": "%s: %s" % (type(e).__name__, e)}
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu and world == 1:
         rate, cores, dt = cpu_sample_rate()

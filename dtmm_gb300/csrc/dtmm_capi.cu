@@ -277,10 +277,12 @@ struct Engine {
     const int blocks = (nlines + lpb - 1) / lpb;
     if (inv) {
       CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_fft_rows<R, true><<<blocks, 256, smem, st>>>(data, nlines, d.width, pW, P(L.twW), A<int>(L.permW), scale, lpb);
+      k_fft_rows<R, true><<<blocks, 256, smem, st>>>(data, data, nlines, d.width, pW, P(L.twW), A<int>(L.permW),
+                                                     scale, lpb);
     } else {
       CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_fft_rows<R, false><<<blocks, 256, smem, st>>>(data, nlines, d.width, pW, P(L.twW), A<int>(L.permW), scale, lpb);
+      k_fft_rows<R, false><<<blocks, 256, smem, st>>>(data, data, nlines, d.width, pW, P(L.twW), A<int>(L.permW),
+                                                      scale, lpb);
     }
     CKL("k_fft_rows");
     return DTMM_OK;
@@ -1019,15 +1021,14 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
     tab = (const cpx<R>*)(ws + L.dmat);
   }
   cpx<R>* X = (cpx<R>*)(ws + L.X);
-  const size_t bytes = sizeof(cpx<R>) * 4 * (size_t)nimg * H * W;
-  CK(cudaMemcpyAsync(X, in, bytes, cudaMemcpyDeviceToDevice, st));
-  // rows forward (natural in and out)
+  // rows forward (natural in and out), out of place into the workspace
   const int nlines = nimg * 4 * H;
   int lpb = std::max(1, std::min(16, 4096 / W));
   size_t smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
   if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", W);
   CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_fft_rows<R, false><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>(X, nlines, W, pW, twW, permW, 1.0, lpb);
+  k_fft_rows<R, false><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((const cpx<R>*)in, X, nlines, W, pW, twW, permW,
+                                                                    1.0, lpb);
   CKL("k_fft_rows");
   // columns: forward transform, the per-k matrix, inverse transform (1/H)
   Grid g;
@@ -1066,8 +1067,8 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
   // rows inverse (1/W)
   smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
   CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_fft_rows<R, true><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((cpx<R>*)out, nlines, W, pW, twW, permW,
-                                                                   1.0 / W, lpb);
+  k_fft_rows<R, true><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((cpx<R>*)out, (cpx<R>*)out, nlines, W, pW, twW,
+                                                                   permW, 1.0 / W, lpb);
   CKL("k_fft_rows");
   return DTMM_OK;
 }

@@ -45,10 +45,59 @@ __host__ __device__ __forceinline__ cpx<R> cfma(cpx<R> a, cpx<R> b, cpx<R> c) {
 template <typename R>
 __host__ __device__ __forceinline__ R norm2(cpx<R> a) { return a.re * a.re + a.im * a.im; }
 
+// FP64 -> FP32 with round to nearest even, in integer arithmetic.  The
+// hardware conversion issues at the FP64 rate (about 1/64 of the FP32 rate on
+// this part), which bounds kernels that store FP64 results as FP32.  Every
+// value whose result is a normal float (or whose input is a signed zero) is
+// converted here with INT32 operations: rebias the exponent, keep the top 23
+// mantissa bits and round on the 29 bits dropped (a carry out of the
+// mantissa correctly bumps the exponent, up to infinity).  Results that are
+// float subnormals, overflow, infinities and NaN take the hardware path.
+__host__ __device__ __forceinline__ float f32_rn(double d) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long u;
+  __builtin_memcpy(&u, &d, sizeof(u));
+#endif
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // FP32 biased exponent
+  unsigned bits;
+  if (e >= 1 && e <= 254) {
+    bits = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    bits += (rest > 0x10000000u || (rest == 0x10000000u && (bits & 1u))) ? 1u : 0u;
+  } else if ((hi & 0x7fffffffu) == 0 && lo == 0) {
+    bits = 0;
+  } else {
+    return (float)d;
+  }
+  bits |= hi & 0x80000000u;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(bits);
+#else
+  float f;
+  __builtin_memcpy(&f, &bits, sizeof(f));
+  return f;
+#endif
+}
+
+// a double in the bulk precision R
+template <typename R>
+__host__ __device__ __forceinline__ R to_r(double d);
+template <>
+__host__ __device__ __forceinline__ double to_r<double>(double d) {
+  return d;
+}
+template <>
+__host__ __device__ __forceinline__ float to_r<float>(double d) {
+  return f32_rn(d);
+}
+
 __device__ __forceinline__ cpx<double> cvt_d(cpx<float> a) { return mk<double>(a.re, a.im); }
 __device__ __forceinline__ cpx<double> cvt_d(cpx<double> a) { return a; }
 template <typename R>
-__device__ __forceinline__ cpx<R> cvt(cpx<double> a) { return mk<R>((R)a.re, (R)a.im); }
+__device__ __forceinline__ cpx<R> cvt(cpx<double> a) { return mk<R>(to_r<R>(a.re), to_r<R>(a.im)); }
 
 // Complex division and principal square root in FP64 (used by the
 // eigen-solve).  Division scales by the larger component (Smith's method);

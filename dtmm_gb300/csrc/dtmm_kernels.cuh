@@ -283,21 +283,21 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
 #pragma unroll
         for (int i = 0; i < nrec; ++i) rec[i] = (R)0;
       } else {
-        rec[0] = (R)E[0][0]; rec[1] = (R)E[0][2]; rec[2] = (R)E[1][0]; rec[3] = (R)E[1][2];
+        rec[0] = to_r<R>(E[0][0]); rec[1] = to_r<R>(E[0][2]); rec[2] = to_r<R>(E[1][0]); rec[3] = to_r<R>(E[1][2]);
         if constexpr (sizeof(R) == 4)
-          rec[4] = fabs(detf) > 1e-30 ? __frcp_rn((float)detf) : (float)(1.0 / detf);
+          rec[4] = fabs(detf) > 1e-30 ? __frcp_rn(f32_rn(detf)) : f32_rn(1.0 / detf);
         else
           rec[4] = 1.0 / detf;
-        rec[5] = (R)((al[0] - aw) * p.d);
-        rec[6] = (R)((al[2] - aw) * p.d);
+        rec[5] = to_r<R>((al[0] - aw) * p.d);
+        rec[6] = to_r<R>((al[2] - aw) * p.d);
         if (FOUR) {
-          rec[7] = (R)E[0][1]; rec[8] = (R)E[0][3]; rec[9] = (R)E[1][1]; rec[10] = (R)E[1][3];
+          rec[7] = to_r<R>(E[0][1]); rec[8] = to_r<R>(E[0][3]); rec[9] = to_r<R>(E[1][1]); rec[10] = to_r<R>(E[1][3]);
           if constexpr (sizeof(R) == 4)
-            rec[11] = fabs(detb) > 1e-30 ? __frcp_rn((float)detb) : (float)(1.0 / detb);
+            rec[11] = fabs(detb) > 1e-30 ? __frcp_rn(f32_rn(detb)) : f32_rn(1.0 / detb);
           else
             rec[11] = 1.0 / detb;
-          rec[12] = (R)((al[1] + aw) * p.d);
-          rec[13] = (R)((al[3] + aw) * p.d);
+          rec[12] = to_r<R>((al[1] + aw) * p.d);
+          rec[13] = to_r<R>((al[3] + aw) * p.d);
         }
       }
       R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
@@ -1020,10 +1020,12 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
 }
 
 // ---------------------------------------------------------------------------
-// Plain row FFT of every (image, component, y) line, in place.
+// Plain row FFT of every (image, component, y) line, src -> dst (the same
+// array for an in-place transform: a block reads its lines completely before
+// it writes them, and no other block touches them).
 // ---------------------------------------------------------------------------
 template <typename R, bool INV>
-__global__ void __launch_bounds__(256) k_fft_rows(cpx<R>* __restrict__ data, int nlines, int W, FFTPlan plan,
+__global__ void __launch_bounds__(256) k_fft_rows(const cpx<R>* src, cpx<R>* dst, int nlines, int W, FFTPlan plan,
                                                   const cpx<R>* __restrict__ twg, const int* __restrict__ permg,
                                                   double scale, int lpb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1039,7 +1041,7 @@ __global__ void __launch_bounds__(256) k_fft_rows(cpx<R>* __restrict__ data, int
   const int nl = min(lpb, nlines - l0);
   for (int t = threadIdx.x; t < nl * W; t += blockDim.x) {
     const int l = t / W, x = t - l * W;
-    cpx<R> v = data[(size_t)(l0 + l) * W + x];
+    cpx<R> v = src[(size_t)(l0 + l) * W + x];
     s[l * W + (INV ? x : perm[x])] = v;
   }
   __syncthreads();
@@ -1050,7 +1052,7 @@ __global__ void __launch_bounds__(256) k_fft_rows(cpx<R>* __restrict__ data, int
   const R sc = (R)scale;
   for (int t = threadIdx.x; t < nl * W; t += blockDim.x) {
     const int l = t / W, x = t - l * W;
-    data[(size_t)(l0 + l) * W + x] = s[l * W + (INV ? perm[x] : x)] * sc;
+    dst[(size_t)(l0 + l) * W + x] = s[l * W + (INV ? perm[x] : x)] * sc;
   }
 }
 
@@ -1161,7 +1163,7 @@ __global__ void k_ratio(const double* a, const double* b, double* out, int n) {
 template <typename RD, typename RS>
 __global__ void k_convert(cpx<RD>* dst, const cpx<RS>* src, size_t n) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) dst[t] = mk<RD>((RD)src[t].re, (RD)src[t].im);
+  if (t < n) dst[t] = mk<RD>(to_r<RD>((double)src[t].re), to_r<RD>((double)src[t].im));
 }
 
 // FFT twiddles exp(-2 pi i t / N) (FP64, then rounded) and digit reversal

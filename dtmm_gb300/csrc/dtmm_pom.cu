@@ -30,6 +30,15 @@ int pom_fail(int code, const char* msg) {
 __constant__ double kXYZ2RGB[3][3] = {{3.2404542, -1.5371385, -0.4985314},
                                       {-0.9692660, 1.8760108, 0.0415560},
                                       {0.0556434, -0.2040259, 1.0572252}};
+__constant__ float kXYZ2RGBf[3][3] = {{3.2404542f, -1.5371385f, -0.4985314f},
+                                      {-0.9692660f, 1.8760108f, 0.0415560f},
+                                      {0.0556434f, -0.2040259f, 1.0572252f}};
+template <typename R>
+__device__ __forceinline__ R xyz2rgb_coef(int k, int j);
+template <>
+__device__ __forceinline__ double xyz2rgb_coef<double>(int k, int j) { return kXYZ2RGB[k][j]; }
+template <>
+__device__ __forceinline__ float xyz2rgb_coef<float>(int k, int j) { return kXYZ2RGBf[k][j]; }
 
 struct PomArgs {
   int H, W, nlam, nset, npol;
@@ -38,35 +47,62 @@ struct PomArgs {
   const double* window;       // H x W or null
 };
 
-// one image's field at pixel p, after polarizer, window and analyzer, in
-// the bulk precision R (complex64 fields: FP32 arithmetic)
+// Per-block copies of the small operands in the bulk precision R: every
+// conversion from their FP64 inputs happens once per block, not per pixel
+// (a float <-> double conversion issues at the FP64 rate, about 1/64 of the
+// FP32 rate on this part, and would otherwise bound the kernel).
+constexpr int kStagedLam = 1024;  // colour-matching rows staged in shared memory
+
 template <typename R>
-__device__ __forceinline__ void pom_pixel(const PomArgs& a, const cpx<R>* __restrict__ f, int set, int lam,
-                                          long long p, cpx<R> g[4]) {
+struct PomStage {
+  cpx<R> pm[16];
+  cpx<R> c, s;  // jones vector
+  int has_pm;
+};
+
+template <typename R>
+__device__ __forceinline__ void pom_stage(const PomArgs& a, PomStage<R>& st) {
+  if (threadIdx.x < 16) st.pm[threadIdx.x] = a.pmat ? cvt<R>(a.pmat[threadIdx.x]) : mk<R>((R)0, (R)0);
+  if (threadIdx.x == 0) {
+    st.c = mk<R>((R)a.j0r, (R)a.j0i);
+    st.s = mk<R>((R)a.j1r, (R)a.j1i);
+    st.has_pm = a.pmat != nullptr;
+  }
+}
+
+// one image's field at pixel p, after polarizer, window (w, already in R)
+// and analyzer, in the bulk precision R (complex64 fields: FP32 arithmetic)
+template <typename R>
+__device__ __forceinline__ void pom_pixel(const PomArgs& a, const PomStage<R>& st, const cpx<R>* __restrict__ f,
+                                          int set, int lam, long long p, bool windowed, R w, cpx<R> g[4]) {
   const long long HW = (long long)a.H * a.W;
   if (a.npol == 2) {
     const cpx<R>* fx = f + (((long long)set * 2 + 0) * a.nlam + lam) * 4 * HW + p;
     const cpx<R>* fy = f + (((long long)set * 2 + 1) * a.nlam + lam) * 4 * HW + p;
-    const cpx<R> c = mk<R>((R)a.j0r, (R)a.j0i), s = mk<R>((R)a.j1r, (R)a.j1i);
+    cpx<R> x[4], y[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) g[k] = fx[k * HW] * c + fy[k * HW] * s;
+    for (int k = 0; k < 4; ++k) {
+      x[k] = fx[k * HW];
+      y[k] = fy[k * HW];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) g[k] = x[k] * st.c + y[k] * st.s;
   } else {
     const cpx<R>* fi = f + ((long long)set * a.nlam + lam) * 4 * HW + p;
 #pragma unroll
     for (int k = 0; k < 4; ++k) g[k] = fi[k * HW];
   }
-  if (a.window) {
-    const R w = (R)a.window[p];
+  if (windowed) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) g[k] = g[k] * w;
   }
-  if (a.pmat) {
+  if (st.has_pm) {
     cpx<R> o[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       cpx<R> acc = mk<R>((R)0, (R)0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc = acc + cvt<R>(a.pmat[i * 4 + j]) * g[j];
+      for (int j = 0; j < 4; ++j) acc = acc + st.pm[i * 4 + j] * g[j];
       o[i] = acc;
     }
 #pragma unroll
@@ -82,11 +118,15 @@ __device__ __forceinline__ R poynting(const cpx<R> g[4]) {
 // out[set][lam][4][H][W]
 template <typename R>
 __global__ void k_pom_field(PomArgs a, const cpx<R>* __restrict__ f, cpx<R>* __restrict__ out) {
+  __shared__ PomStage<R> st;
+  pom_stage<R>(a, st);
+  __syncthreads();
   const long long HW = (long long)a.H * a.W;
   const int sl = blockIdx.y, set = sl / a.nlam, lam = sl - set * a.nlam;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (long long)gridDim.x * blockDim.x) {
     cpx<R> g[4];
-    pom_pixel<R>(a, f, set, lam, p, g);
+    const R w = a.window ? (R)a.window[p] : (R)1;
+    pom_pixel<R>(a, st, f, set, lam, p, a.window != nullptr, w, g);
     cpx<R>* o = out + ((long long)set * a.nlam + lam) * 4 * HW + p;
 #pragma unroll
     for (int k = 0; k < 4; ++k) o[k * HW] = g[k];
@@ -117,27 +157,31 @@ __global__ void k_field2specter(int H, int W, int nlam, int nset, int sum, const
 
 // XYZ -> normalise -> linear RGB or gray -> transfer curve
 // norm_div: divisor (0 = none); gamma: 0 none, < 0 sRGB, > 0 power 1/gamma
-__device__ __forceinline__ double srgb_curve(double v) {
-  if (v < 0.0031308) return v < 0.0 ? 0.0 : 12.92 * v;
-  return v > 1.0 ? 1.0 : (1.0 + 0.055) * pow(v, 1.0 / 2.4) - 0.055;
+template <typename R>
+__device__ __forceinline__ R srgb_curve(R v) {
+  if (v < (R)0.0031308) return v < (R)0 ? (R)0 : (R)12.92 * v;
+  return v > (R)1 ? (R)1 : ((R)1 + (R)0.055) * pow(v, (R)1 / (R)2.4) - (R)0.055;
 }
-__device__ __forceinline__ double power_curve(double v, double gamma) {
-  if (v > 1.0) return 1.0;
-  if (v < 0.0) return 0.0;
-  return pow(v, 1.0 / gamma);
+template <typename R>
+__device__ __forceinline__ R power_curve(R v, R gamma) {
+  if (v > (R)1) return (R)1;
+  if (v < (R)0) return (R)0;
+  return pow(v, (R)1 / gamma);
 }
-__device__ __forceinline__ void xyz_to_out(double xyz[3], double norm_div, int gray, double gamma, double rgb[3]) {
-  if (norm_div != 0.0)
+template <typename R>
+__device__ __forceinline__ void xyz_to_out(R xyz[3], R norm_div, int gray, R gamma, R rgb[3]) {
+  if (norm_div != (R)0)
     for (int k = 0; k < 3; ++k) xyz[k] = xyz[k] / norm_div;
   if (gray) {
     rgb[0] = rgb[1] = rgb[2] = xyz[1];
   } else {
-    for (int k = 0; k < 3; ++k) rgb[k] = kXYZ2RGB[k][0] * xyz[0] + kXYZ2RGB[k][1] * xyz[1] + kXYZ2RGB[k][2] * xyz[2];
+    for (int k = 0; k < 3; ++k)
+      rgb[k] = xyz2rgb_coef<R>(k, 0) * xyz[0] + xyz2rgb_coef<R>(k, 1) * xyz[1] + xyz2rgb_coef<R>(k, 2) * xyz[2];
   }
-  if (gamma < 0.0) {
-    for (int k = 0; k < 3; ++k) rgb[k] = srgb_curve(rgb[k]);
-  } else if (gamma > 0.0) {
-    for (int k = 0; k < 3; ++k) rgb[k] = power_curve(rgb[k], gamma);
+  if (gamma < (R)0) {
+    for (int k = 0; k < 3; ++k) rgb[k] = srgb_curve<R>(rgb[k]);
+  } else if (gamma > (R)0) {
+    for (int k = 0; k < 3; ++k) rgb[k] = power_curve<R>(rgb[k], gamma);
   }
 }
 
@@ -154,7 +198,7 @@ __global__ void k_specter2color(long long npix, int nlam, const double* __restri
     }
     double rgb[3];
     if (convert) {
-      xyz_to_out(xyz, norm_div, gray, gamma, rgb);
+      xyz_to_out<double>(xyz, norm_div, gray, gamma, rgb);
     } else {
       rgb[0] = xyz[0];
       rgb[1] = xyz[1];
@@ -166,46 +210,60 @@ __global__ void k_specter2color(long long npix, int nlam, const double* __restri
 
 // normalisation by the image maximum (norm=True): one block finds the
 // maximum of every XYZ value, then converts every pixel in place (the
-// maximum is exact whatever the reduction order)
-template <typename T>
+// maximum is exact whatever the reduction order); arithmetic in R
+template <typename T, typename R>
 __global__ void __launch_bounds__(1024) k_color_by_max(long long npix, int gray, double gamma, T* __restrict__ io) {
-  __shared__ double red[1024];
-  double m = -INFINITY;
-  for (long long i = threadIdx.x; i < npix * 3; i += blockDim.x) m = fmax(m, (double)io[i]);
+  __shared__ R red[1024];
+  R m = -INFINITY;
+  for (long long i = threadIdx.x; i < npix * 3; i += blockDim.x) m = fmax(m, (R)io[i]);
   red[threadIdx.x] = m;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
     __syncthreads();
   }
-  const double mx = red[0];
+  const R mx = red[0];
   for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
-    double xyz[3] = {(double)io[p * 3], (double)io[p * 3 + 1], (double)io[p * 3 + 2]};
-    double rgb[3];
-    xyz_to_out(xyz, mx, gray, gamma, rgb);
+    R xyz[3] = {(R)io[p * 3], (R)io[p * 3 + 1], (R)io[p * 3 + 2]};
+    R rgb[3];
+    xyz_to_out<R>(xyz, mx, gray, (R)gamma, rgb);
     for (int k = 0; k < 3; ++k) io[p * 3 + k] = (T)rgb[k];
   }
 }
 
-// fused: polarizer / window / analyzer, Poynting summed over sets, XYZ, colour
+// fused: polarizer / window / analyzer, Poynting summed over sets, XYZ,
+// colour; every step in the bulk precision R (FP32 for complex64 fields)
 template <typename R, typename T>
-__global__ void k_pom_image(PomArgs a, const cpx<R>* __restrict__ f, const double* __restrict__ cmf,
-                            double norm_div, int gray, double gamma, int convert, T* __restrict__ out) {
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1)
+    k_pom_image(PomArgs a, const cpx<R>* __restrict__ f, const double* __restrict__ cmf, double norm_div, int gray,
+                double gamma, int convert, T* __restrict__ out) {
+  __shared__ PomStage<R> st;
+  __shared__ R s_cmf[kStagedLam * 3];
+  pom_stage<R>(a, st);
+  const int staged = min(a.nlam, kStagedLam);
+  for (int i = threadIdx.x; i < staged * 3; i += blockDim.x) s_cmf[i] = (R)cmf[i];
+  __syncthreads();
+  const R nd = (R)norm_div, gm = (R)gamma;
   const long long HW = (long long)a.H * a.W;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (long long)gridDim.x * blockDim.x) {
-    double xyz[3] = {0.0, 0.0, 0.0};
+    const R w = a.window ? (R)a.window[p] : (R)1;
+    R xyz[3] = {(R)0, (R)0, (R)0};
     for (int lam = 0; lam < a.nlam; ++lam) {
-      double s = 0.0;
+      R s = (R)0;
       for (int set = 0; set < a.nset; ++set) {
         cpx<R> g[4];
-        pom_pixel<R>(a, f, set, lam, p, g);
-        s += (double)poynting<R>(g);
+        pom_pixel<R>(a, st, f, set, lam, p, a.window != nullptr, w, g);
+        s += poynting<R>(g);
       }
-      for (int k = 0; k < 3; ++k) xyz[k] = xyz[k] + cmf[lam * 3 + k] * s;
+      if (lam < kStagedLam) {
+        for (int k = 0; k < 3; ++k) xyz[k] = xyz[k] + s_cmf[lam * 3 + k] * s;
+      } else {
+        for (int k = 0; k < 3; ++k) xyz[k] = xyz[k] + (R)cmf[lam * 3 + k] * s;
+      }
     }
-    double rgb[3];
+    R rgb[3];
     if (convert) {
-      xyz_to_out(xyz, norm_div, gray, gamma, rgb);
+      xyz_to_out<R>(xyz, nd, gray, gm, rgb);
     } else {
       rgb[0] = xyz[0];
       rgb[1] = xyz[1];
@@ -303,7 +361,7 @@ int dtmm_specter2color(long long npix, int nlam, const double* spec, const doubl
                                                             norm_mode != 2, rgb);
   int rc = launched("k_specter2color");
   if (rc || norm_mode != 2) return rc;
-  k_color_by_max<double><<<1, 1024, 0, st>>>(npix, gray, gamma, rgb);
+  k_color_by_max<double, double><<<1, 1024, 0, st>>>(npix, gray, gamma, rgb);
   return launched("k_color_by_max");
 }
 
@@ -326,7 +384,10 @@ int dtmm_pom_image(const dtmm_pom_desc* d, const void* field, const double* cmf,
                                                                norm_mode != 2, rgb);
   rc = launched("k_pom_image");
   if (rc || norm_mode != 2) return rc;
-  k_color_by_max<float><<<1, 1024, 0, st>>>(hw, gray, gamma, rgb);
+  if (d->precision == DTMM_PRECISION_DOUBLE)
+    k_color_by_max<float, double><<<1, 1024, 0, st>>>(hw, gray, gamma, rgb);
+  else
+    k_color_by_max<float, float><<<1, 1024, 0, st>>>(hw, gray, gamma, rgb);
   return launched("k_color_by_max");
 }
 
