@@ -1073,6 +1073,44 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
   return DTMM_OK;
 }
 
+// plane-wave fills (k_planewave for FFT modes, k_wave_window for continuous
+// wave vectors with an optional window): one block per kWaveRows rows of one
+// image, the row and column phase factors in shared memory
+int launch_wave(int H, int W, int nimg, const void* coef, const int* my, const int* mx, const double* kx,
+                const double* ky, const double* window, int precision, void* field, void* stream) {
+  if (H < 1 || W < 1) return fail(DTMM_EINVAL, "grid must be at least 1x1");
+  if (nimg < 1 || nimg > 65535) return fail(DTMM_EINVAL, "image count %d outside 1..65535", nimg);
+  if (!coef || !field || (kx == nullptr && (!my || !mx))) return fail(DTMM_EINVAL, "null pointer");
+  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "invalid precision");
+  const size_t csz = precision == DTMM_PRECISION_DOUBLE ? sizeof(cpx<double>) : sizeof(cpx<float>);
+  const size_t smem = (size_t)(W + kWaveRows) * csz;
+  if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels too long for the plane-wave fill", W);
+  dim3 grid((H + kWaveRows - 1) / kWaveRows, nimg);
+  cudaStream_t st = (cudaStream_t)stream;
+  const cpx<double>* c = (const cpx<double>*)coef;
+  if (precision == DTMM_PRECISION_DOUBLE) {
+    if (kx) {
+      CK(cudaFuncSetAttribute(k_wave_window<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_wave_window<double><<<grid, 256, smem, st>>>((cpx<double>*)field, c, kx, ky, window, H, W);
+    } else {
+      CK(cudaFuncSetAttribute(k_planewave<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_planewave<double><<<grid, 256, smem, st>>>((cpx<double>*)field, c, my, mx, H, W);
+    }
+  } else {
+    if (kx) {
+      CK(cudaFuncSetAttribute(k_wave_window<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_wave_window<float><<<grid, 256, smem, st>>>((cpx<float>*)field, c, kx, ky, window, H, W);
+    } else {
+      CK(cudaFuncSetAttribute(k_planewave<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_planewave<float><<<grid, 256, smem, st>>>((cpx<float>*)field, c, my, mx, H, W);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(DTMM_ECUDA, "plane-wave fill: %s", cudaGetErrorString(e));
+  return DTMM_OK;
+}
+
 int transfer_impl(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace, size_t workspace_bytes,
                   void* stream, Prof* prof, int* launches) {
   g_err.clear();
@@ -1172,21 +1210,83 @@ int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* 
 int dtmm_planewave_field(int height, int width, int nimg, const void* coef, const int* my, const int* mx,
                          int precision, void* field, void* stream) {
   g_err.clear();
-  if (height < 1 || width < 1) return fail(DTMM_EINVAL, "grid must be at least 1x1");
-  if (nimg < 1 || nimg > 65535) return fail(DTMM_EINVAL, "image count %d outside 1..65535", nimg);
-  if (!coef || !my || !mx || !field) return fail(DTMM_EINVAL, "null pointer");
-  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
-    return fail(DTMM_EINVAL, "invalid precision");
+  return launch_wave(height, width, nimg, coef, my, mx, nullptr, nullptr, nullptr, precision, field, stream);
+}
+
+int dtmm_wave_field(int height, int width, int nimg, const void* coef, const double* kx, const double* ky,
+                    const double* window, int precision, void* field, void* stream) {
+  g_err.clear();
+  if (!kx || !ky) return fail(DTMM_EINVAL, "null pointer");
+  return launch_wave(height, width, nimg, coef, nullptr, nullptr, kx, ky, window, precision, field, stream);
+}
+
+int dtmm_field_diffraction_matrix(int height, int width, int nlam, const double* ks, double d, double eps_re,
+                                  double eps_im, int mode, double betamax, void* dmat, void* stream) {
+  g_err.clear();
+  if (height < 1 || width < 1 || nlam < 1) return fail(DTMM_EINVAL, "empty grid or wavelength axis");
+  if (!ks || !dmat) return fail(DTMM_EINVAL, "null pointer");
+  if (mode < -1 || mode > 1) return fail(DTMM_EINVAL, "mode must be 0 (both), 1 (forward) or -1 (backward)");
+  Grid g;
+  memset(&g, 0, sizeof(g));
+  g.H = height;
+  g.W = width;
+  g.nlam = nlam;
   cudaStream_t st = (cudaStream_t)stream;
   const long long hw = (long long)height * width;
-  const int bx = (int)std::min<long long>((hw + 255) / 256, 1216);
-  dim3 grid(bx, nimg);
+  for (int l0 = 0; l0 < nlam; l0 += 64) {
+    KsChunk kc;
+    kc.n = std::min(64, nlam - l0);
+    for (int i = 0; i < kc.n; ++i) kc.ks[i] = ks[l0 + i];
+    const long long n = (long long)kc.n * hw;
+    if (n > (long long)INT32_MAX) return fail(DTMM_EINVAL, "grid too large");
+    k_field_dmat<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(kc, l0, g, mk<double>(eps_re, eps_im), d, mode, betamax,
+                                                             (cpx<double>*)dmat);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_field_dmat: %s", cudaGetErrorString(e));
+  }
+  return DTMM_OK;
+}
+
+int dtmm_field_intensity(int height, int width, int nimg, int precision, const void* field, double* sums,
+                         void* stream) {
+  g_err.clear();
+  if (height < 1 || width < 1 || nimg < 1) return fail(DTMM_EINVAL, "empty field");
+  if (nimg > INT32_MAX / 4) return fail(DTMM_EINVAL, "too many images");
+  if (!field || !sums) return fail(DTMM_EINVAL, "null pointer");
+  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "invalid precision");
+  Grid g;
+  memset(&g, 0, sizeof(g));
+  g.H = height;
+  g.W = width;
+  g.NI = nimg;
+  cudaStream_t st = (cudaStream_t)stream;
   if (precision == DTMM_PRECISION_DOUBLE)
-    k_planewave<double><<<grid, 256, 0, st>>>((cpx<double>*)field, (const cpx<double>*)coef, my, mx, height, width);
+    k_total_intensity<double><<<nimg, 256, 0, st>>>((const cpx<double>*)field, g, sums);
   else
-    k_planewave<float><<<grid, 256, 0, st>>>((cpx<float>*)field, (const cpx<double>*)coef, my, mx, height, width);
+    k_total_intensity<float><<<nimg, 256, 0, st>>>((const cpx<float>*)field, g, sums);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_planewave: %s", cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_total_intensity: %s", cudaGetErrorString(e));
+  return DTMM_OK;
+}
+
+int dtmm_scale_fields(int height, int width, int nimg, int precision, void* field, const double* base,
+                      const double* num, const double* den, void* stream) {
+  g_err.clear();
+  if (height < 1 || width < 1 || nimg < 1 || nimg > 65535) return fail(DTMM_EINVAL, "image count outside 1..65535");
+  if (!field) return fail(DTMM_EINVAL, "null pointer");
+  if ((num == nullptr) != (den == nullptr)) return fail(DTMM_EINVAL, "num and den must be given together");
+  if (precision != DTMM_PRECISION_MIXED && precision != DTMM_PRECISION_DOUBLE)
+    return fail(DTMM_EINVAL, "invalid precision");
+  const long long per = 4LL * height * width;
+  dim3 grid((unsigned)std::min<long long>((per + 255) / 256, 304), nimg);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == DTMM_PRECISION_DOUBLE)
+    k_scale_fields<double><<<grid, 256, 0, st>>>((cpx<double>*)field, per, base, num, den);
+  else
+    k_scale_fields<float><<<grid, 256, 0, st>>>((cpx<float>*)field, per, base, num, den);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_scale_fields: %s", cudaGetErrorString(e));
   return DTMM_OK;
 }
 

@@ -1269,28 +1269,136 @@ __global__ void k_sincos(const double* phi, double* c, double* sn, int n) {
 
 // ---------------------------------------------------------------------------
 // Plane-wave input fields (the grid of illumination_data, dtmm/field.py:586):
-// out[i][c][y][x] = coef[i][c] * exp(2 pi i (my[i] y / H + mx[i] x / W)).
-// The phase numerator (my y mod H) W + (mx x mod W) H is exact integer
-// arithmetic, so sincospi sees an argument in [0, 4).
+// out[i][c][y][x] = coef[i][c] * ex[x] * ey[y] * window[y][x] with
+//   FFT modes (k_planewave):  ex = exp(2 pi i mx x / W), ey = exp(2 pi i my y / H)
+//                             (integer phase numerators reduced exactly, so
+//                             sincospi sees an argument in [0, 2));
+//   continuous (k_wave_window): ex = exp(i kx x), ey = exp(i ky y), the plane
+//                             wave of dtmm/wave.py:376 normalised to 1 at the
+//                             first pixel, times an optional real window.
+// A block fills `rows` rows of one image: the W + rows phase factors are
+// formed once in FP64 into shared memory (in the bulk precision), so the
+// per-pixel work is complex products in R.
 // ---------------------------------------------------------------------------
+constexpr int kWaveRows = 8;
+
+template <typename R>
+__device__ __forceinline__ void wave_rows(cpx<R>* __restrict__ o, const cpx<R>* ex, const cpx<R>* ey,
+                                          const cpx<R> c[4], const double* __restrict__ window, int y0, int ny,
+                                          int W, long long HW) {
+  for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
+    const int r = t / W, x = t - r * W;
+    const long long p = (long long)(y0 + r) * W + x;
+    cpx<R> w = ex[x] * ey[r];
+    if (window) w = w * to_r<R>(window[p]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k * HW + p] = c[k] * w;
+  }
+}
+
 template <typename R>
 __global__ void k_planewave(cpx<R>* __restrict__ out, const cpx<double>* __restrict__ coef,
                             const int* __restrict__ my, const int* __restrict__ mx, int H, int W) {
+  extern __shared__ __align__(16) unsigned char wave_smem[];
+  cpx<R>* ex = (cpx<R>*)wave_smem;
+  cpx<R>* ey = ex + W;
   const int img = blockIdx.y;
+  const int y0 = blockIdx.x * kWaveRows, ny = min(kWaveRows, H - y0);
   const long long HW = (long long)H * W;
   const long long iy = ((long long)my[img] % H + H) % H, ix = ((long long)mx[img] % W + W) % W;
-  cpx<double> c[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) c[k] = coef[(size_t)img * 4 + k];
-  cpx<R>* o = out + (size_t)img * 4 * HW;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < HW; t += (long long)gridDim.x * blockDim.x) {
-    const long long y = t / W, x = t - y * W;
-    const long long num = ((iy * y) % H) * W + ((ix * x) % W) * H;
-    double s, co;
-    sincospi(2.0 * (double)num / (double)HW, &s, &co);
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      o[k * HW + t] = mk<R>((R)(c[k].re * co - c[k].im * s), (R)(c[k].re * s + c[k].im * co));
+  for (int x = threadIdx.x; x < W; x += blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)((ix * x) % W) / (double)W, &s, &c);
+    ex[x] = mk<R>(to_r<R>(c), to_r<R>(s));
   }
+  for (int r = threadIdx.x; r < ny; r += blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)((iy * (y0 + r)) % H) / (double)H, &s, &c);
+    ey[r] = mk<R>(to_r<R>(c), to_r<R>(s));
+  }
+  cpx<R> c[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c[k] = cvt<R>(coef[(size_t)img * 4 + k]);
+  __syncthreads();
+  wave_rows<R>(out + (size_t)img * 4 * HW, ex, ey, c, nullptr, y0, ny, W, HW);
+}
+
+template <typename R>
+__global__ void k_wave_window(cpx<R>* __restrict__ out, const cpx<double>* __restrict__ coef,
+                              const double* __restrict__ kx, const double* __restrict__ ky,
+                              const double* __restrict__ window, int H, int W) {
+  extern __shared__ __align__(16) unsigned char wave_smem[];
+  cpx<R>* ex = (cpx<R>*)wave_smem;
+  cpx<R>* ey = ex + W;
+  const int img = blockIdx.y;
+  const int y0 = blockIdx.x * kWaveRows, ny = min(kWaveRows, H - y0);
+  const long long HW = (long long)H * W;
+  const double kxi = kx[img], kyi = ky[img];
+  for (int x = threadIdx.x; x < W; x += blockDim.x) {
+    double s, c;
+    sincos(kxi * (double)x, &s, &c);
+    ex[x] = mk<R>(to_r<R>(c), to_r<R>(s));
+  }
+  for (int r = threadIdx.x; r < ny; r += blockDim.x) {
+    double s, c;
+    sincos(kyi * (double)(y0 + r), &s, &c);
+    ey[r] = mk<R>(to_r<R>(c), to_r<R>(s));
+  }
+  cpx<R> c[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c[k] = cvt<R>(coef[(size_t)img * 4 + k]);
+  __syncthreads();
+  wave_rows<R>(out + (size_t)img * 4 * HW, ex, ey, c, window, y0, ny, W, HW);
+}
+
+// Field diffraction matrix of a homogeneous isotropic medium eps over d
+// pixels (field_diffraction_matrix, dtmm/diffract.py:125-138):
+// F . diag(exp(i alpha_m k0 d)) . F^-1 per grid k, over both directions
+// (mode 0), the forward modes 0, 2 (+1) or the backward modes 1, 3 (-1);
+// zero where beta >= betamax.  out[lam][ky][kx][4][4] in complex128, for
+// wavelengths lam0 .. lam0 + kc.n - 1 (wavenumbers passed by value).
+struct KsChunk {
+  double ks[64];
+  int n;
+};
+
+__global__ void k_field_dmat(KsChunk kc, int lam0, Grid g, cpx<double> eps, double d, int mode, double betamax,
+                             cpx<double>* __restrict__ out) {
+  const int HW = g.H * g.W;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= kc.n * HW) return;
+  const int l = t / HW, k = t - l * HW;
+  const int ky = k / g.W, kx = k - ky * g.W;
+  const double ks = kc.ks[l];
+  double beta, phi;
+  betaphi_k(g, ks, ky, kx, beta, phi);
+  cpx<double> al[4], F[4][4], Fi[4][4];
+  iso_k(beta, phi, eps, betamax, al, F, Fi);
+  cpx<double> ph[4];
+  for (int m = 0; m < 4; ++m) {
+    const bool keep = mode == 0 || (mode > 0 ? (m % 2 == 0) : (m % 2 == 1));
+    ph[m] = keep ? cexp_i(al[m] * (ks * d)) : mk<double>(0.0, 0.0);
+  }
+  cpx<double>* o = out + ((size_t)(lam0 + l) * HW + k) * 16;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      cpx<double> acc = mk<double>(0.0, 0.0);
+      for (int m = 0; m < 4; ++m) acc = acc + F[i][m] * ph[m] * Fi[m][j];
+      o[i * 4 + j] = acc;
+    }
+}
+
+// field[img] *= base[img] * sqrt(num[img] / den[img]) (num, den null: base only);
+// the factor is formed once per block and applied in R
+template <typename R>
+__global__ void k_scale_fields(cpx<R>* __restrict__ f, long long per, const double* __restrict__ base,
+                               const double* __restrict__ num, const double* __restrict__ den) {
+  const int img = blockIdx.y;
+  double fa = base ? base[img] : 1.0;
+  if (num && den) fa *= sqrt(num[img] / den[img]);
+  const R s = to_r<R>(fa);
+  cpx<R>* o = f + (size_t)img * per;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < per; t += (long long)gridDim.x * blockDim.x)
+    o[t] = o[t] * s;
 }
 }  // namespace dtmm

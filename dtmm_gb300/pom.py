@@ -88,17 +88,31 @@ def ray_jonesmat4x4(jmat, beta=0.0, phi=0.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.
 
 
 def field_diffraction_matrix(shape, ks, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), mode="b",
-                             betamax=0.8):
+                             betamax=0.8, device=None):
     """Per-k 4x4 propagation matrix F . diag(exp(i alpha ks d)) . F^-1 of a
     homogeneous isotropic medium over d pixels (dtmm/diffract.py:125), zero
     for beta >= betamax; mode "t" / "r" keeps the forward / backward modes
-    only.  Shape (n_wavelengths, H, W, 4, 4), built on the host in FP64."""
+    only.  Shape (n_wavelengths, H, W, 4, 4), complex128: built on the host
+    in FP64, or with ``device`` on the GPU by the library's
+    ``dtmm_field_diffraction_matrix`` (a device tensor, nothing on the host
+    grows with the grid)."""
     from .illumination import _fftfreq_grid
 
     epsv = np.asarray(epsv, np.complex128)
     if not (epsv[0] == epsv[1] == epsv[2]):
         raise NotImplementedError("field_diffraction_matrix: isotropic media only")
     ks = np.abs(np.asarray(ks, np.float64)).reshape(-1)
+    if device is not None:
+        torch = _torch()
+        h, w = (int(x) for x in shape)
+        out = torch.empty((len(ks), h, w, 4, 4), dtype=torch.complex128, device=device)
+        m = {"b": 0, 0: 0, "t": 1, 1: 1, "r": -1, -1: -1}[mode]
+        ksa = np.ascontiguousarray(ks)
+        lib = _lib.load()
+        _lib.check(lib.dtmm_field_diffraction_matrix(h, w, len(ks), ksa.ctypes.data_as(ctypes.c_void_p), float(d),
+                                                     float(epsv[0].real), float(epsv[0].imag), m, float(betamax),
+                                                     ctypes.c_void_p(out.data_ptr()), _stream(out.device)))
+        return out
     beta, phi = _fftfreq_grid(shape, ks)
     eps = epsv[0]
     f = _iso_fmat(beta, phi, eps)

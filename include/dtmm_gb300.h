@@ -221,6 +221,37 @@ size_t dtmm_diffract_workspace_size(int height, int width, int nimg, int nlam, i
 int dtmm_diffract(int height, int width, int nimg, int nlam, int precision, const void* dmat, const void* field_in,
                   void* field_out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Plane waves with continuous wave vectors (the windowed branch of
+   illumination_data, dtmm/field.py:586-713; illumination_waves :459 and
+   planewave, dtmm/wave.py:376): field[i][c][y][x] = coef[i][c] *
+   exp(i (kx[i] x + ky[i] y)) * window[y][x].  coef: device complex128
+   [nimg][4]; kx, ky: device float64 [nimg]; window: device float64 [H][W]
+   or null; field: device complex64 (MIXED) or complex128 (DOUBLE). */
+int dtmm_wave_field(int height, int width, int nimg, const void* coef, const double* kx, const double* ky,
+                    const double* window, int precision, void* field, void* stream);
+
+/* Field diffraction matrix of a homogeneous isotropic medium eps = eps_re + i
+   eps_im over d pixels (field_diffraction_matrix, dtmm/diffract.py:125-138):
+   dmat[lam][ky][kx][4][4] (device complex128) = F diag(exp(i alpha k_lam d))
+   F^-1 on the FFT grid, keeping both directions (mode 0), the forward
+   (mode 1) or the backward (mode -1) modes, zero where beta >= betamax.  ks:
+   host float64 [nlam] (2 pi pixelsize / lambda).  The dmat argument of
+   dtmm_diffract. */
+int dtmm_field_diffraction_matrix(int height, int width, int nlam, const double* ks, double d, double eps_re,
+                                  double eps_im, int mode, double betamax, void* dmat, void* stream);
+
+/* Total intensity of each image: sums[i] = sum over pixels of the normal
+   Poynting component (field2intensity, dtmm/field.py:780, summed over the
+   grid).  field: device [nimg][4][H][W]; sums: device float64 [nimg]. */
+int dtmm_field_intensity(int height, int width, int nimg, int precision, const void* field, double* sums,
+                         void* stream);
+
+/* field[i] *= base[i] * sqrt(num[i] / den[i]) (device float64 arrays; base
+   null = 1; num and den both null = no ratio): the intensity rescale of
+   illumination_data after its diffraction step. */
+int dtmm_scale_fields(int height, int width, int nimg, int precision, void* field, const double* base,
+                      const double* num, const double* den, void* stream);
+
 /* director2data (dtmm/data.py:277-320) on the device: director[nvox][3]
    (float64, or float32 when director_double == 0) -> eps eigenvalues
    epsv[nvox][3] and Euler angles epsa[nvox][3] (float64).  The order

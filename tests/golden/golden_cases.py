@@ -165,3 +165,51 @@ def raised_cosine_window(shape):
     """Separable window 0.5 - 0.5 cos(2 pi (i + 0.5) / n) on both axes."""
     wy, wx = (0.5 - 0.5 * np.cos(2 * np.pi * (np.arange(n) + 0.5) / n) for n in shape)
     return wy[:, None] * wx[None, :]
+
+
+# illumination_rays (dtmm/field.py:371): (NA, diameter, smooth)
+RAYS_CASES = {
+    "na02_d5": (0.2, 5, 0.1),
+    "na03_d7": (0.3, 7.4, 0.0),
+    "na015_annulus": (0.15, (2, 6), 0.2),
+    "na025_d9_soft": (0.25, 9, 0.5),
+    "na01_d4_clip": (0.1, 4, 1.5),
+}
+
+# window functions (dtmm/window.py): name -> (function, args)
+WINDOW_CASES = {
+    "aperture_full": ("aperture", ((32, 40), 1.0, 0.05)),
+    "aperture_small": ("aperture", ((24, 24), 0.6, 0.2)),
+    "aperture_annulus": ("aperture", ((30, 26), (0.3, 0.9), 0.1)),
+    "aperture_hard": ("aperture", ((17, 19), 0.8, 0.0)),
+    "blackman": ("blackman", ((32, 40),)),
+    "gaussian": ("gaussian", ((20, 28), 0.6)),
+}
+
+# windowed illumination_data (dtmm/field.py:586 with a window): the window is
+# one of WINDOW_CASES (the reference's own array); rays may come from RAYS_CASES
+ILLUM_WINDOW_CASES = {
+    "win_blackman": dict(shape=(32, 40), wavelengths=[500.0, 600.0], pixelsize=100.0, beta=0.1, phi=0.3,
+                         window="blackman"),
+    "win_rays_focus": dict(shape=(24, 24), wavelengths=[550.0], pixelsize=80.0, rays="na015_annulus",
+                           window="aperture_small", focus=3.0),
+    "win_backdir_jones": dict(shape=(20, 28), wavelengths=[450.0, 650.0], pixelsize=100.0, beta=0.2, phi=-1.0,
+                              jones=(1, 1j), backdir=True, window="gaussian", n=1.0),
+    "win_no_diffraction": dict(shape=(30, 26), wavelengths=[600.0], pixelsize=90.0, beta=0.05, phi=2.0,
+                               window="aperture_annulus", diffraction=False, intensity=3.0),
+}
+
+# load_tcmf (dtmm/color.py:257) options
+TCMF_CASES = {
+    "default": dict(),
+    "nine": dict(wavelengths=list(np.linspace(380.0, 780.0, 9))),
+    "single": dict(wavelengths=[550.0]),
+    "seven_norm2": dict(wavelengths=list(np.linspace(400.0, 700.0, 7)), norm=2),
+    "five_single_wavelength": dict(wavelengths=list(np.linspace(380.0, 780.0, 5)), single_wavelength=True),
+    "eleven_norm0": dict(wavelengths=list(np.linspace(450.0, 650.0, 11)), norm=0),
+    "illuminant_a": dict(wavelengths=list(np.linspace(380.0, 780.0, 9)), illuminant="A"),
+    "cie1964": dict(wavelengths=list(np.linspace(400.0, 700.0, 13)), cmf="CIE1964"),
+    "cmos": dict(wavelengths=list(np.linspace(400.0, 700.0, 9)), cmf="CMOS"),
+}
+TCMF_TABLES = {"CIE1931": "CIE1931XYZ.dat", "CIE1964": "CIE1964XYZ.dat", "CMOS": "CMOSY.dat", "D65": "D65.dat",
+               "A": "A.dat"}

@@ -23,7 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from golden_cases import CASES, ILLUM_CASES, POM_CASES, build_inputs, raised_cosine_window  # noqa: E402
+from golden_cases import (CASES, ILLUM_CASES, ILLUM_WINDOW_CASES, POM_CASES, RAYS_CASES, TCMF_CASES,  # noqa: E402
+                          TCMF_TABLES, WINDOW_CASES, build_inputs, raised_cosine_window)
 
 
 def run_case(name, dtmm):
@@ -194,11 +195,52 @@ def save_qtensor(dtmm):
     print("qtensor                %s" % (Q.shape,))
 
 
+def save_illum_window(dtmm):
+    """Reference windows, ray sets and windowed illumination_data fields (illum_window.npz)."""
+    import importlib
+
+    window = importlib.import_module("dtmm.window")
+    field = importlib.import_module("dtmm.field")
+    arrays = {}
+    for name, (fn, args) in WINDOW_CASES.items():
+        arrays["window_" + name] = np.asarray(getattr(window, fn)(*args))
+    for name, (na, diameter, smooth) in RAYS_CASES.items():
+        b, p, i = field.illumination_rays(na, diameter, smooth)
+        arrays["rays_%s_beta" % name], arrays["rays_%s_phi" % name], arrays["rays_%s_intensity" % name] = b, p, i
+    for name, case in ILLUM_WINDOW_CASES.items():
+        kw = dict(case)
+        shape, wl, ps = kw.pop("shape"), kw.pop("wavelengths"), kw.pop("pixelsize")
+        kw["window"] = arrays["window_" + kw.pop("window")]
+        rays = kw.pop("rays", None)
+        if rays is not None:
+            kw["beta"], kw["phi"], kw["intensity"] = (arrays["rays_%s_%s" % (rays, k)]
+                                                      for k in ("beta", "phi", "intensity"))
+        arrays[name] = np.asarray(dtmm.illumination_data(shape, wl, pixelsize=ps, **kw)[0])
+    np.savez_compressed(os.path.join(HERE, "illum_window.npz"), **arrays)
+    print("illum_window           %d arrays" % len(arrays))
+
+
+def save_tcmf(dtmm):
+    """Reference load_tcmf for TCMF_CASES, with the data tables it read (tcmf.npz)."""
+    import importlib
+
+    color = importlib.import_module("dtmm.color")
+    arrays = {}
+    for key, fname in TCMF_TABLES.items():
+        arrays["table_" + key] = np.loadtxt(os.path.join(color.DATAPATH, fname))
+    for name, kw in TCMF_CASES.items():
+        x, c = color.load_tcmf(retx=True, **kw)
+        arrays[name + "_x"], arrays[name] = np.asarray(x, float), np.asarray(c)
+    np.savez_compressed(os.path.join(HERE, "tcmf.npz"), **arrays)
+    print("tcmf                   %d cases" % len(TCMF_CASES))
+
+
 def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files", "qtensor"])
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files", "qtensor", "illum_window",
+                                                            "tcmf"])
     for name in names:
         if name == "kat":
             save_wave_kat(dtmm)
@@ -213,6 +255,10 @@ def main(argv):
             save_files(dtmm)
         elif name == "qtensor":
             save_qtensor(dtmm)
+        elif name == "illum_window":
+            save_illum_window(dtmm)
+        elif name == "tcmf":
+            save_tcmf(dtmm)
         else:
             run_case(name, dtmm)
 
