@@ -173,7 +173,9 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.op_one = L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
-  L.op = take(L.op_one * (L.cache_ops ? (size_t)d->nlayers : 1));
+  // per-layer cache, or two buffers that alternate between the layer being
+  // swept and the next layer's operators computed beside it
+  L.op = take(L.op_one * (L.cache_ops ? (size_t)d->nlayers : 2));
   L.total = off;
   return L;
 }
@@ -189,6 +191,37 @@ double fold(double off, double d) {
 }
 
 // optional device-time accounting (dtmm_transfer_timed)
+// Side stream of each caller stream, created on first use and kept for the
+// process (at most kMaxSide of them; beyond that the overlap is skipped).
+// The per-layer operators (FP64 eigen-solve) run there ahead of the row /
+// column passes (FP32), so the FP64 pipe works while the FFT passes of the
+// previous layer run.  When the caller's stream is being captured into a
+// graph the stream is created with this thread's capture mode relaxed for
+// the call, and the fork / join become edges of the graph.
+constexpr size_t kMaxSide = 256;
+std::mutex g_side_mu;
+std::vector<std::pair<std::pair<int, cudaStream_t>, cudaStream_t>> g_side;
+
+cudaStream_t side_stream(cudaStream_t origin) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_side_mu);
+  for (auto& e : g_side)
+    if (e.first.first == dev && e.first.second == origin) return e.second;
+  if (g_side.size() >= kMaxSide) return nullptr;
+  cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+  if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess) return nullptr;
+  cudaStream_t s = nullptr;
+  const cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaThreadExchangeStreamCaptureMode(&mode);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  g_side.push_back({{dev, origin}, s});
+  return s;
+}
+
 struct Prof {
   std::vector<cudaEvent_t> ev[3];  // row, col, op: begin/end pairs
   int launches = 0;
@@ -229,6 +262,31 @@ struct Engine {
   long long tick = 0;
   void mark(int kind) {
     if (prof) prof->mark(kind, st);
+  }
+  void mark_on(int kind, cudaStream_t s) {
+    if (prof) prof->mark(kind, s);
+  }
+  // the operators' side stream (null: operators on the caller's stream) and
+  // the events of this call, released when the call has enqueued everything
+  cudaStream_t st2 = nullptr;
+  std::vector<cudaEvent_t> own_events;
+  ~Engine() {
+    for (cudaEvent_t e : own_events) cudaEventDestroy(e);
+  }
+  // an event recorded now on stream s
+  int record(cudaStream_t s, cudaEvent_t& e) {
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    own_events.push_back(e);
+    CK(cudaEventRecord(e, s));
+    return DTMM_OK;
+  }
+  // stream `waiter` waits for everything enqueued so far on stream `s`
+  int wait_for(cudaStream_t waiter, cudaStream_t s) {
+    cudaEvent_t e;
+    int rc = record(s, e);
+    if (rc) return rc;
+    CK(cudaStreamWaitEvent(waiter, e, 0));
+    return DTMM_OK;
   }
   const dtmm_transfer_desc& d;
   const dtmm_transfer_io& io;
@@ -556,7 +614,8 @@ struct Engine {
     return w;
   }
 
-  int voxel_ops(int layer, double dsub, cpx<R>* op) {
+  int voxel_ops(int layer, double dsub, cpx<R>* op, cudaStream_t s = nullptr) {
+    if (s == nullptr) s = st;
     OpParams p;
     memset(&p, 0, sizeof(p));
     p.eps_dev = epseff();
@@ -585,22 +644,22 @@ struct Engine {
     while (rpt > 1 && (long long)blocks * ((d.nray + rpt - 1) / rpt) < 608) rpt = (rpt + 1) / 2;
     p.rays_per_thread = rpt;
     dim3 grid((unsigned)blocks, (unsigned)((d.nray + rpt - 1) / rpt));
-    mark(PROF_OP);
+    mark_on(PROF_OP, s);
     p.wev02 = uniform_real() ? wev02() : nullptr;
     p.wevs = wevs();
     p.wc2 = wc2();
     if (real_ops()) {
       if (p.four)
-        k_voxel_op<R, true, true><<<grid, 128, 0, st>>>(p, g, op);
+        k_voxel_op<R, true, true><<<grid, 128, 0, s>>>(p, g, op);
       else
-        k_voxel_op<R, true, false><<<grid, 128, 0, st>>>(p, g, op);
+        k_voxel_op<R, true, false><<<grid, 128, 0, s>>>(p, g, op);
     } else {
       if (p.four)
-        k_voxel_op<R, false, true><<<grid, 128, 0, st>>>(p, g, op);
+        k_voxel_op<R, false, true><<<grid, 128, 0, s>>>(p, g, op);
       else
-        k_voxel_op<R, false, false><<<grid, 128, 0, st>>>(p, g, op);
+        k_voxel_op<R, false, false><<<grid, 128, 0, s>>>(p, g, op);
     }
-    mark(PROF_OP);
+    mark_on(PROF_OP, s);
     CKL("k_voxel_op");
     return DTMM_OK;
   }
@@ -719,15 +778,59 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // operators of layer l (cached across passes when they fit)
-  int layer_ops(int pass, int l, double ds, const void*& op) {
-    if (L.cache_ops) {
-      op = (const void*)(ws + L.op + L.op_one * (size_t)l);
-      if (pass == 0) return voxel_ops(l, ds, (cpx<R>*)op);
-      return DTMM_OK;
-    }
-    op = P(L.op);
-    return voxel_ops(l, ds, P(L.op));
+  // Operators of the layers of one sweep (layer order `order`, sub-step
+  // thickness ds[q]).  With a side stream they are computed there ahead of
+  // use: every layer at once into the per-layer cache (first pass; later
+  // passes reuse it), or one layer ahead into two alternating buffers, the
+  // side stream waiting until the passes that last read a buffer are queued
+  // before it overwrites it.  Without a side stream: on the caller's stream
+  // just before use.
+  struct OpFeed {
+    std::vector<cudaEvent_t> ready;  // per position q: operators of order[q] complete
+    cudaEvent_t freed[2] = {nullptr, nullptr};
+  };
+
+  cpx<R>* op_buffer(size_t q, int l) const {
+    return L.cache_ops ? (cpx<R>*)(ws + L.op + L.op_one * (size_t)l) : (cpx<R>*)(ws + L.op + L.op_one * (q % 2));
+  }
+
+  int feed_begin(int pass, const std::vector<int>& order, const std::vector<double>& ds, OpFeed& f) {
+    f.ready.assign(order.size(), nullptr);
+    if (L.cache_ops && pass > 0) return DTMM_OK;  // reused
+    if (st2 == nullptr) st2 = side_stream(st);
+    if (st2 == nullptr) return DTMM_OK;
+    int rc = wait_for(st2, st);  // inputs of the operators (setup, earlier passes)
+    if (rc) return rc;
+    const size_t n = L.cache_ops ? order.size() : std::min<size_t>(1, order.size());
+    for (size_t q = 0; q < n; ++q)
+      if ((rc = feed_one(q, order, ds, f))) return rc;
+    return DTMM_OK;
+  }
+
+  int feed_one(size_t q, const std::vector<int>& order, const std::vector<double>& ds, OpFeed& f) {
+    int rc;
+    if (!L.cache_ops && q >= 2) CK(cudaStreamWaitEvent(st2, f.freed[q % 2], 0));
+    if ((rc = voxel_ops(order[q], ds[q], op_buffer(q, order[q]), st2))) return rc;
+    return record(st2, f.ready[q]);
+  }
+
+  // before layer position q: its operators (computed now on the caller's
+  // stream when there is no side stream), the next layer's queued beside it
+  int feed_get(int pass, size_t q, const std::vector<int>& order, const std::vector<double>& ds, OpFeed& f,
+               const void*& op) {
+    int rc;
+    op = op_buffer(q, order[q]);
+    if (L.cache_ops && pass > 0) return DTMM_OK;
+    if (st2 == nullptr) return voxel_ops(order[q], ds[q], (cpx<R>*)op);
+    if (!L.cache_ops && q + 1 < order.size() && (rc = feed_one(q + 1, order, ds, f))) return rc;
+    CK(cudaStreamWaitEvent(st, f.ready[q], 0));
+    return DTMM_OK;
+  }
+
+  // after layer position q has been queued: its buffer may be overwritten
+  int feed_done(size_t q, OpFeed& f) {
+    if (st2 == nullptr || L.cache_ops) return DTMM_OK;
+    return record(st, f.freed[q % 2]);
   }
 
   // state F (real space, 4 components) -> propagated through all layers -> F
@@ -738,15 +841,19 @@ struct Engine {
     cpx<R>* F = P(L.F);
     cpx<R>* U = P(L.U);
     int rc;
+    std::vector<double> dsub(order.size());
+    for (size_t q = 0; q < order.size(); ++q) dsub[q] = d.thickness[order[q]] / d.nstep[order[q]];
+    OpFeed feed;
+    if ((rc = feed_begin(pass, order, dsub, feed))) return rc;
     if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
     const cpx<R>* cur = F;
     double dprev = 0.0;
     for (size_t q = 0; q < order.size(); ++q) {
       const int l = order[q];
       const int nst = d.nstep[l];
-      const double ds = d.thickness[l] / nst;
+      const double ds = dsub[q];
       const void* op;
-      if ((rc = layer_ops(pass, l, ds, op))) return rc;
+      if ((rc = feed_get(pass, q, order, dsub, feed, op))) return rc;
       int kop;
       const void* ktab;
       if (q == 0) {
@@ -761,6 +868,7 @@ struct Engine {
       }
       cpx<R>* out = nullptr;
       if ((rc = layer(cur, 4, kop, ktab, 0, out, op, dir, nst, ds))) return rc;
+      if ((rc = feed_done(q, feed))) return rc;
       // keep the layer result out of the buffers the next layer writes
       if (out != P(L.X) && q + 1 < order.size() && L.chains) {
         CK(cudaMemcpyAsync(P(L.X), out, sizeof(cpx<R>) * (size_t)NI * 4 * L.HW, cudaMemcpyDeviceToDevice, st));
@@ -894,6 +1002,10 @@ struct Engine {
     std::vector<int> order;
     layer_order(1, order);
     CK(cudaMemcpyAsync(F, fin, bytes4, cudaMemcpyDeviceToDevice, st));
+    std::vector<double> dsub(order.size());
+    for (size_t q = 0; q < order.size(); ++q) dsub[q] = d.thickness[order[q]] / d.nstep[order[q]];
+    OpFeed feed;
+    if ((rc = feed_begin(0, order, dsub, feed))) return rc;
     if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
     const cpx<R>* cur = F;
     int cin = 4;
@@ -901,8 +1013,9 @@ struct Engine {
     for (size_t q = 0; q < order.size(); ++q) {
       const int l = order[q];
       const int nst = d.nstep[l];
-      const double ds = d.thickness[l] / nst;
-      if ((rc = voxel_ops(l, ds, P(L.op)))) return rc;
+      const double ds = dsub[q];
+      const void* op;
+      if ((rc = feed_get(0, q, order, dsub, feed, op))) return rc;
       int kop;
       const void* ktab;
       if (q == 0) {
@@ -917,7 +1030,8 @@ struct Engine {
         ktab = kdiag_cur;
       }
       cpx<R>* out = nullptr;
-      if ((rc = layer(cur, cin, kop, ktab, 0, out, P(L.op), 1.0, nst, ds))) return rc;
+      if ((rc = layer(cur, cin, kop, ktab, 0, out, op, 1.0, nst, ds))) return rc;
+      if ((rc = feed_done(q, feed))) return rc;
       if (out != P(L.X) && q + 1 < order.size() && L.chains) {
         CK(cudaMemcpyAsync(P(L.X), out, sizeof(cpx<R>) * (size_t)NI * 2 * L.HW, cudaMemcpyDeviceToDevice, st));
         out = P(L.X);
