@@ -585,7 +585,7 @@ def main():
                     help="precision: 256x256 4x4 npass 3 (default); batch: 48 instances in one graph; "
                          "serve: Poisson request stream; 2x2: 1024x1024 2x2 diffraction 5; rows: POM image, "
                          "refocus, director2data and Q2data kernels")
-    ap.add_argument("--streams", type=int, default=8, help="batch: streams in the graph")
+    ap.add_argument("--streams", type=int, default=2, help="batch: streams in the graph")
     ap.add_argument("--c128-subset", type=int, default=8, help="batch: instances of the complex128 comparison")
     ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrival rate (req/s)")

@@ -30,7 +30,7 @@ class _Item:
 class TransferBatch:
     """A set of device transfers launched together (eagerly or as one CUDA graph)."""
 
-    def __init__(self, nstreams=8, device=None):
+    def __init__(self, nstreams=2, device=None):
         import torch
 
         self.device = device or torch.device("cuda", torch.cuda.current_device())
