@@ -403,6 +403,8 @@ def run_2x2(args, dev):
 def run_rows(args, dev, cpu=True):
     import torch
 
+    only = None if getattr(args, "rows", "all") == "all" else set(args.rows.split(","))
+
     from dtmm_gb300 import data, pom, samples
 
     O = None
@@ -455,74 +457,80 @@ def run_rows(args, dev, cpu=True):
     pmat_h = pom.ray_jonesmat4x4(pom.polarizer(pom.jonesvec((0, 1))))
     pmat = torch.from_numpy(pmat_h).to(dev)
 
-    # POM image: x / y fields of 9 wavelengths on a 1024^2 grid -> sRGB
-    H = W = 1024
-    f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
-    ms = timed(lambda: pom.pom_image(f, cmf, jvec, pmat, stream=stream.cuda_stream))
-    nbytes = f.numel() * 8 + H * W * 3 * 4
-    cv = None
-    if cpu:
-        fh = f[:, :, :, :512, :512].cpu().numpy().astype(np.complex128)
-        cv = cpu_rate(lambda: O.specter2color(O.field2specter(O.calculate_pom_field(fh, jvec, pmat_h)), cmf_h),
-                      512 * 512 * len(wl))
-    res.update([row("pom_image", "POM image (x polarizer, crossed analyzer, sRGB) of x+y fields, 9 wavelengths, "
-                                 "1024x1024 grid, complex64", H * W * len(wl), "pixel·λ/s", nbytes, ms, 1, cv,
-                    "same pipeline, 512x512 crop, oracle (numpy; FFTs on every core, the rest on one)",
-                    os.cpu_count() or 1)])
-    del f
+    def pom_row():
+        # POM image: x / y fields of 9 wavelengths on a 1024^2 grid -> sRGB
+        H = W = 1024
+        f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
+        ms = timed(lambda: pom.pom_image(f, cmf, jvec, pmat, stream=stream.cuda_stream))
+        nbytes = f.numel() * 8 + H * W * 3 * 4
+        cv = None
+        if cpu:
+            fh = f[:, :, :, :512, :512].cpu().numpy().astype(np.complex128)
+            cv = cpu_rate(lambda: O.specter2color(O.field2specter(O.calculate_pom_field(fh, jvec, pmat_h)), cmf_h),
+                          512 * 512 * len(wl))
+        res.update([row("pom_image", "POM image (x polarizer, crossed analyzer, sRGB) of x+y fields, 9 "
+                                     "wavelengths, 1024x1024 grid, complex64", H * W * len(wl), "pixel·λ/s", nbytes,
+                        ms, 1, cv, "same pipeline, 512x512 crop, oracle (numpy; FFTs on every core, the rest on one)",
+                        os.cpu_count() or 1)])
 
-    # refocus: fft2, per-k 4x4 matrix, ifft2 of x+y fields, 9 wavelengths, 512^2
-    H = W = 512
-    f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
-    ks = 2 * np.pi / wl * PIXELSIZE
-    dm_h = pom.field_diffraction_matrix((H, W), ks, d=-20.0, epsv=(1.5 ** 2,) * 3)
-    dm = torch.from_numpy(dm_h).to(dev)
-    ms = timed(lambda: pom.diffract(f, dm))
-    nbytes = 2 * f.numel() * 8 + dm.numel() * 16
-    cv = None
-    if cpu:
-        fh = f[:, :, :, :256, :256].cpu().numpy().astype(np.complex128)
-        dmh = pom.field_diffraction_matrix((256, 256), ks, d=-20.0, epsv=(1.5 ** 2,) * 3)
-        cv = cpu_rate(lambda: O.diffract(fh, dmh), 2 * 256 * 256 * len(wl))
-    res.update([row("diffract", "refocus by -20 px in n=1.5 (fft2, per-k 4x4 matrix, ifft2) of x+y fields, "
-                                "9 wavelengths, 512x512 grid, complex64 fields, complex128 matrices",
-                    2 * H * W * len(wl), "pixel·λ/s", nbytes, ms, 6, cv,
-                    "same refocus, 256x256 grid, oracle (scipy fft on every core, matrices on one)",
-                    os.cpu_count() or 1)])
-    del f, dm
+    def diffract_row():
+        # refocus: fft2, per-k 4x4 matrix, ifft2 of x+y fields, 9 wavelengths, 512^2
+        H = W = 512
+        f = torch.randn((2, len(wl), 4, H, W), dtype=torch.complex64, device=dev, generator=gen)
+        ks = 2 * np.pi / wl * PIXELSIZE
+        dm = pom.field_diffraction_matrix((H, W), ks, d=-20.0, epsv=(1.5 ** 2,) * 3, device=dev)
+        ms = timed(lambda: pom.diffract(f, dm))
+        nbytes = 2 * f.numel() * 8 + dm.numel() * 16
+        cv = None
+        if cpu:
+            fh = f[:, :, :, :256, :256].cpu().numpy().astype(np.complex128)
+            dmh = pom.field_diffraction_matrix((256, 256), ks, d=-20.0, epsv=(1.5 ** 2,) * 3)
+            cv = cpu_rate(lambda: O.diffract(fh, dmh), 2 * 256 * 256 * len(wl))
+        res.update([row("diffract", "refocus by -20 px in n=1.5 (fft2, per-k 4x4 matrix, ifft2) of x+y fields, "
+                                    "9 wavelengths, 512x512 grid, complex64 fields, complex128 matrices",
+                        2 * H * W * len(wl), "pixel·λ/s", nbytes, ms, 6, cv,
+                        "same refocus, 256x256 grid, oracle (scipy fft on every core, matrices on one)",
+                        os.cpu_count() or 1)])
 
-    # director -> optical data: 128 layers of 512^2
-    L, H, W = 128, 512, 512
-    d = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
-    ms = timed(lambda: data.director2data(d, no=1.52, ne=1.71))
-    nvox = L * H * W
-    cv = None
-    if cpu:
-        dh = d[:32, :256, :256].cpu().numpy()
-        cv = cpu_rate(lambda: O.director2data(dh, no=1.52, ne=1.71), dh.size // 3)
-    res.update([row("director2data", "director2data, 128x512x512 float64 directors", nvox, "voxel/s",
-                    nvox * (24 + 48), ms, 1, cv, "32x256x256 directors, oracle (numpy)")])
-    del d
+    def director_row():
+        # director -> optical data: 128 layers of 512^2
+        L, H, W = 128, 512, 512
+        d = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
+        ms = timed(lambda: data.director2data(d, no=1.52, ne=1.71))
+        nvox = L * H * W
+        cv = None
+        if cpu:
+            dh = d[:32, :256, :256].cpu().numpy()
+            cv = cpu_rate(lambda: O.director2data(dh, no=1.52, ne=1.71), dh.size // 3)
+        res.update([row("director2data", "director2data, 128x512x512 float64 directors", nvox, "voxel/s",
+                        nvox * (24 + 48), ms, 1, cv, "32x256x256 directors, oracle (numpy)")])
 
-    # Q tensor -> optical data: 64 layers of 512^2, uniaxial Q of random directors and orders
-    L = 64
-    n = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
-    n = n / n.norm(dim=-1, keepdim=True)
-    S = torch.rand((L, H, W), dtype=torch.float64, device=dev, generator=gen) * 0.7 + 0.2
-    q = torch.stack([S * (n[..., 0] ** 2 - 1 / 3), S * (n[..., 1] ** 2 - 1 / 3), S * (n[..., 2] ** 2 - 1 / 3),
-                     S * n[..., 0] * n[..., 1], S * n[..., 0] * n[..., 2], S * n[..., 1] * n[..., 2]], dim=-1)
-    del n, S
-    ms = timed(lambda: data.Q2data(q, no=1.52, ne=1.71))
-    nvox = L * H * W
-    cv = None
-    if cpu:
-        qh = q[:4, :64, :64].cpu().numpy()
-        cv = cpu_rate(lambda: O.Q2data(qh, no=1.52, ne=1.71), qh.size // 6)
-    name, r = row("q2data", "Q2data (uniaxial), 64x512x512 float64 Q tensors", nvox, "voxel/s", nvox * (48 + 48),
-                  ms, 1, cv, "4x64x64 Q tensors, oracle (per-voxel Python, 1 core)")
-    r["roofline"]["note"] = "FP64-bound: one eigen-solve (acos, 2 cos, 3 sqrt, divides) and 2 atan2 + acos per voxel"
-    res[name] = r
-    del q
+    def q_row():
+        # Q tensor -> optical data: 64 layers of 512^2, uniaxial Q of random directors and orders
+        L, H, W = 64, 512, 512
+        n = torch.randn((L, H, W, 3), dtype=torch.float64, device=dev, generator=gen)
+        n = n / n.norm(dim=-1, keepdim=True)
+        S = torch.rand((L, H, W), dtype=torch.float64, device=dev, generator=gen) * 0.7 + 0.2
+        q = torch.stack([S * (n[..., 0] ** 2 - 1 / 3), S * (n[..., 1] ** 2 - 1 / 3), S * (n[..., 2] ** 2 - 1 / 3),
+                         S * n[..., 0] * n[..., 1], S * n[..., 0] * n[..., 2], S * n[..., 1] * n[..., 2]], dim=-1)
+        del n, S
+        ms = timed(lambda: data.Q2data(q, no=1.52, ne=1.71))
+        nvox = L * H * W
+        cv = None
+        if cpu:
+            qh = q[:4, :64, :64].cpu().numpy()
+            cv = cpu_rate(lambda: O.Q2data(qh, no=1.52, ne=1.71), qh.size // 6)
+        name, r = row("q2data", "Q2data (uniaxial), 64x512x512 float64 Q tensors", nvox, "voxel/s",
+                      nvox * (48 + 48), ms, 1, cv, "4x64x64 Q tensors, oracle (per-voxel Python, 1 core)")
+        r["roofline"]["note"] = ("FP64-bound: one eigen-solve (acos, 2 cos, 3 sqrt, divides) and 2 atan2 + acos "
+                                 "per voxel")
+        res[name] = r
+
+    for name, fn in (("pom_image", pom_row), ("diffract", diffract_row), ("director2data", director_row),
+                     ("q2data", q_row)):
+        if only is None or name in only:
+            fn()
+            torch.cuda.empty_cache()
     torch.cuda.synchronize(dev)
     return res
 
@@ -593,6 +601,8 @@ def main():
     ap.add_argument("--hbm-budget", type=float, default=150e9, help="serve: admission budget (bytes)")
     ap.add_argument("--no-batch", action="store_true", help="precision workload: skip the batch summary")
     ap.add_argument("--no-serve", action="store_true", help="precision workload: skip the serving summary")
+    ap.add_argument("--rows", default="all",
+                    help="rows workload: comma list of pom_image, diffract, director2data, q2data (default all)")
     ap.add_argument("--no-rows", action="store_true",
                     help="precision workload: skip the POM / refocus / director / Q-tensor kernel summary")
     args = ap.parse_args()
@@ -623,7 +633,7 @@ def main():
     if args.workload == "rows":
         rows = run_rows(args, dev, cpu=not args.no_cpu and rank == 0)
         if rank == 0:
-            pi = rows["pom_image"]
+            pi = rows["pom_image"] if "pom_image" in rows else next(iter(rows.values()))
             print(json.dumps({"metric": "POM image pixel·λ/s (with the refocus, director2data and Q2data rows)",
                               "value": pi["value"], "unit": pi["unit"], "n_gpus": 1, "steps": args.steps,
                               "warmup": args.warmup, "ms_per_step": pi["ms_per_call"], "higher_is_better": True,
