@@ -157,16 +157,20 @@ __global__ void k_field2specter(int H, int W, int nlam, int nset, int sum, const
 
 // XYZ -> normalise -> linear RGB or gray -> transfer curve
 // norm_div: divisor (0 = none); gamma: 0 none, < 0 sRGB, > 0 power 1/gamma
+// v^e for v > 0: FP32 through the SFU (__powf, 2^(e log2 v)), whose error is
+// a few ulp, far below the float32 image's resolution; FP64 through pow
+__device__ __forceinline__ float pos_pow(float v, float e) { return __powf(v, e); }
+__device__ __forceinline__ double pos_pow(double v, double e) { return pow(v, e); }
 template <typename R>
 __device__ __forceinline__ R srgb_curve(R v) {
   if (v < (R)0.0031308) return v < (R)0 ? (R)0 : (R)12.92 * v;
-  return v > (R)1 ? (R)1 : ((R)1 + (R)0.055) * pow(v, (R)1 / (R)2.4) - (R)0.055;
+  return v > (R)1 ? (R)1 : ((R)1 + (R)0.055) * pos_pow(v, (R)1 / (R)2.4) - (R)0.055;
 }
 template <typename R>
 __device__ __forceinline__ R power_curve(R v, R gamma) {
   if (v > (R)1) return (R)1;
-  if (v < (R)0) return (R)0;
-  return pow(v, (R)1 / gamma);
+  if (v <= (R)0) return (R)0;
+  return pos_pow(v, (R)1 / gamma);
 }
 template <typename R>
 __device__ __forceinline__ void xyz_to_out(R xyz[3], R norm_div, int gray, R gamma, R rgb[3]) {
