@@ -175,17 +175,15 @@ class _Material:
         ev, self.ev_strides = _compact(epsv, full)
         ea, self.ea_strides = _compact(epsa, full)
         self.eps_complex = bool(np.iscomplexobj(ev))
-        if self.eps_complex:
-            ev = ev.astype(np.complex128)
-        else:
-            ev = ev.astype(np.float64)
+        # no host copies of arrays that already have the engine's dtype and layout
+        ev = np.ascontiguousarray(ev, np.complex128 if self.eps_complex else np.float64)
         flat = ev.reshape(-1, 3)
         if not np.all(flat[:, 0] == flat[:, 1]):
             raise NotImplementedError(
                 "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
         self.eps_min = float(np.min(ev)) if not self.eps_complex else None
-        self.epsv = torch.from_numpy(np.ascontiguousarray(ev)).to(device)
-        self.epsa = torch.from_numpy(np.ascontiguousarray(ea.astype(np.float64))).to(device)
+        self.epsv = torch.from_numpy(ev).to(device)
+        self.epsa = torch.from_numpy(np.ascontiguousarray(ea, np.float64)).to(device)
         self.thickness = np.asarray(d, np.float64)
         self.nlayers = L
 
@@ -529,14 +527,30 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
             out[...] = res
             res = out
         return res
-    res = fout_dev.to(torch.complex128).cpu().numpy()
+    if out is not None:
+        res = _to_host(fout_dev, out)
+    else:
+        res = fout_dev.to(torch.complex128).cpu().numpy()
     if npass > 1 and method == "4x4":
         # the reference rewrites the caller's input with the reflected field
-        field_in[...] = fin_dev.to(torch.complex128).cpu().numpy()
-    if out is not None:
-        out[...] = res
-        res = out
+        _to_host(fin_dev, field_in)
     return res
+
+
+def _to_host(t, dest):
+    """Copy device field ``t`` into the complex128 numpy array ``dest``: straight
+    into its memory when it is a writeable contiguous complex128 array (one
+    device-to-host copy, a DMA when the array is pinned), else through a
+    temporary."""
+    import torch
+
+    t = t.to(torch.complex128)
+    if (isinstance(dest, np.ndarray) and dest.dtype == np.complex128 and dest.flags.c_contiguous
+            and dest.flags.writeable and dest.shape == tuple(t.shape)):
+        torch.from_numpy(dest).copy_(t)
+    else:
+        dest[...] = t.cpu().numpy()
+    return dest
 
 
 def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout=None, npass=None, nstep=1,
