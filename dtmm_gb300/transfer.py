@@ -176,14 +176,14 @@ class _Material:
         ea, self.ea_strides = _compact(epsa, full)
         self.eps_complex = bool(np.iscomplexobj(ev))
         # no host copies of arrays that already have the engine's dtype and layout
-        ev = np.ascontiguousarray(ev, np.complex128 if self.eps_complex else np.float64)
+        ev = np.require(ev, np.complex128 if self.eps_complex else np.float64, ("C", "W"))
         flat = ev.reshape(-1, 3)
         if not np.all(flat[:, 0] == flat[:, 1]):
             raise NotImplementedError(
                 "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
         self.eps_min = float(np.min(ev)) if not self.eps_complex else None
         self.epsv = torch.from_numpy(ev).to(device)
-        self.epsa = torch.from_numpy(np.ascontiguousarray(ea, np.float64)).to(device)
+        self.epsa = torch.from_numpy(np.require(ea, np.float64, ("C", "W"))).to(device)
         self.thickness = np.asarray(d, np.float64)
         self.nlayers = L
 
