@@ -255,6 +255,18 @@ struct TwoStep {
       }
     }
   }
+  // store without a scale
+  template <typename R>
+  __host__ __device__ static __forceinline__ void store(const cpx<R> (&u)[J][N1], cpx<R>* out, int os, int t) {
+#pragma unroll
+    for (int j = 0; j < J; ++j) {
+      const int k1 = t + N1 * j;
+      if (EVEN || k1 < N2) {
+#pragma unroll
+        for (int k2 = 0; k2 < N1; ++k2) out[(k1 + N2 * k2) * os] = u[j][k2];
+      }
+    }
+  }
 
   // EVEN only: step 2's results in the input's register order,
   // v[m] = X[t + N1 m] (k1 = t + N1 j, m = j + J k2)

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
         cpx<R> u[TS::J][N1];
         TS::template step2<R, true>(u, xl, 1, t);
         __syncwarp(gm);  // every read of the exchange precedes the results that overwrite it
-        TS::template store<R>(u, xl, 1, t, sc);
+        TS::template store<R>(u, xl, 1, t);  // the 1/W of the inverse rides on the operator's 1/det
       }
       __syncthreads();
       const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
@@ -123,13 +123,13 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
         T eb[4], arg_b[2], idb;
 #pragma unroll
         for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
-        idf = opw[(size_t)4 * HW + x];
+        idf = opw[(size_t)4 * HW + x] * sc;
         arg_f[0] = opw[(size_t)5 * HW + x];
         arg_f[1] = opw[(size_t)6 * HW + x];
         if (C == 4) {
 #pragma unroll
           for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
-          idb = opw[(size_t)11 * HW + x];
+          idb = opw[(size_t)11 * HW + x] * sc;
           arg_b[0] = opw[(size_t)12 * HW + x];
           arg_b[1] = opw[(size_t)13 * HW + x];
         }
@@ -250,6 +250,9 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
 #pragma unroll
         for (int m = 0; m < N2; ++m) v[m] = v[m] * ek[(t + N1 * m) * 2];
       }
+      // the output scale once on the spectrum, not on every window row's result
+#pragma unroll
+      for (int m = 0; m < N2; ++m) v[m] = v[m] * sc;
     }
     for (int jj = 0; jj < p.ny; ++jj) {
       const int j = p.j_only >= 0 ? p.j_only : jj;
@@ -265,10 +268,10 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
           cpx<R> u[TS::J][N1];
           TS::template step2<R, true>(u, colA, RS, t);
           __syncwarp(gm);
-          TS::template store<R>(u, colA, RS, t, sc);
+          TS::template store<R>(u, colA, RS, t);
         } else {
 #pragma unroll
-          for (int m = 0; m < N2; ++m) colA[(t + N1 * m) * RS] = w[m] * sc;
+          for (int m = 0; m < N2; ++m) colA[(t + N1 * m) * RS] = w[m];
         }
       }
       __syncthreads();
