@@ -60,14 +60,14 @@ bool make_plan(int n, FFTPlan& p, bool rad8 = false) {
   p.n = n;
   p.nr = 0;
   int m = n;
-  while (rad8 && m % 8 == 0 && p.nr < 14) { p.r[p.nr++] = 8; m /= 8; }
-  while (m % 4 == 0 && p.nr < 14) { p.r[p.nr++] = 4; m /= 4; }
-  while (m % 2 == 0 && p.nr < 14) { p.r[p.nr++] = 2; m /= 2; }
-  const int odd[3] = {3, 5, 7};
+  while (rad8 && m % 8 == 0 && p.nr < kMaxPasses) { p.r[p.nr++] = 8; m /= 8; }
+  while (m % 4 == 0 && p.nr < kMaxPasses) { p.r[p.nr++] = 4; m /= 4; }
+  while (m % 2 == 0 && p.nr < kMaxPasses) { p.r[p.nr++] = 2; m /= 2; }
+  const int odd[10] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
   for (int q : odd)
-    while (m % q == 0 && p.nr < 14) { p.r[p.nr++] = q; m /= q; }
+    while (m % q == 0 && p.nr < kMaxPasses) { p.r[p.nr++] = q; m /= q; }
   p.rbits = 0;
-  for (int i = 0; i < p.nr; ++i) p.rbits |= (unsigned long long)(p.r[i] & 7) << (3 * i);
+  for (int i = 0; i < p.nr; ++i) p.rbits |= (unsigned long long)p.r[i] << (5 * i);
   return m == 1 && n >= 1;
 }
 
@@ -114,7 +114,7 @@ int check_desc(const dtmm_transfer_desc* d) {
     if (d->nstep[l] < 1) return fail(DTMM_EINVAL, "nstep must be >= 1");
   FFTPlan p;
   if (!make_plan(d->height, p) || !make_plan(d->width, p))
-    return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", d->height, d->width);
+    return fail(DTMM_ENOTSUP, "grid sides must factor into primes up to 31 (got %dx%d)", d->height, d->width);
   if (d->betamax <= 0) return fail(DTMM_EINVAL, "betamax must be > 0");
   if (d->row_group < 0 || d->col_tile < 0 || d->fft_schedule < 0 || d->fft_schedule > 3)
     return fail(DTMM_EINVAL, "invalid tuning fields");
@@ -1107,7 +1107,7 @@ int check_diffract(int H, int W, int nimg, int nlam, int precision) {
     return fail(DTMM_EINVAL, "invalid precision");
   FFTPlan p;
   if (!make_plan(H, p) || !make_plan(W, p))
-    return fail(DTMM_ENOTSUP, "grid sides must factor into 2, 3, 5 and 7 (got %dx%d)", H, W);
+    return fail(DTMM_ENOTSUP, "grid sides must factor into primes up to 31 (got %dx%d)", H, W);
   return DTMM_OK;
 }
 

@@ -141,7 +141,8 @@ __device__ __forceinline__ cpx<float> cexp_i(cpx<float> z) {
 // ---------------------------------------------------------------------------
 // In-place mixed-radix FFT of lines stored in shared memory.
 //
-// A plan factors N into radices r[0..nr-1] (each 2, 3, 4, 5 or 7).  The
+// A plan factors N into radices r[0..nr-1] (2, 3, 4, 5, 7, 8, or a prime from
+// 11 to 31: those take a generic O(r^2) butterfly as a call).  The
 // decimation-in-time form (`fft_dit`) takes its input in digit-reversed order
 // and leaves the spectrum in natural order; the transposed network
 // (`fft_dif`) takes natural order and leaves digit-reversed order.  Both run
@@ -153,17 +154,16 @@ __device__ __forceinline__ cpx<float> cexp_i(cpx<float> z) {
 // consecutive threads take consecutive lines (conflict-free for tiles whose
 // lines are interleaved columns); otherwise consecutive butterflies of a line.
 // ---------------------------------------------------------------------------
+// at most kMaxPasses radices (every side up to 16384 needs fewer)
+constexpr int kMaxPasses = 12;
 struct FFTPlan {
   int n;
   int nr;
-  int r[14];
-  unsigned long long rbits;  // r[i] & 7 in bits [3i, 3i+3) (0 codes radix 8): read without dynamic indexing
+  int r[kMaxPasses];
+  unsigned long long rbits;  // r[i] in bits [5i, 5i+5): read without dynamic indexing
 };
 
-__device__ __forceinline__ int plan_radix(const FFTPlan& p, int i) {
-  const int c = (int)((p.rbits >> (3 * i)) & 7ull);
-  return c ? c : 8;
-}
+__device__ __forceinline__ int plan_radix(const FFTPlan& p, int i) { return (int)((p.rbits >> (5 * i)) & 31ull); }
 
 template <typename R, bool INV>
 __device__ __forceinline__ cpx<R> twid(const cpx<R>* tw, int idx) {
@@ -263,6 +263,29 @@ __device__ __noinline__ void butterfly8(cpx<R>* line, int es, int b, int ns, int
   butterfly<R, 8, INV, DIT>(line, es, b, ns, nsh, tstep, tw, n);
 }
 
+// butterfly of a prime radix 11 .. 31 (runtime), as a call: the r-point DFT
+// sum_i v_i W_r^(q i) by direct summation
+template <typename R, bool INV, bool DIT>
+__device__ __noinline__ void butterfly_prime(cpx<R>* line, int es, int b, int ns, int tstep, const cpx<R>* tw, int n,
+                                             int rad) {
+  const int g = b / ns, k = b - g * ns;
+  cpx<R>* ptr = line + (g * ns * rad + k) * es;
+  const int stride = ns * es;
+  const int step = n / rad;
+  cpx<R> v[31];
+  for (int r = 0; r < rad; ++r) v[r] = (DIT && r > 0) ? ptr[r * stride] * twid<R, INV>(tw, k * r * tstep) : ptr[r * stride];
+  for (int q = 0; q < rad; ++q) {
+    cpx<R> acc = v[0];
+    int e = 0;  // (q * i) mod rad
+    for (int i = 1; i < rad; ++i) {
+      e += q;
+      if (e >= rad) e -= rad;
+      acc = cfma(v[i], twid<R, INV>(tw, e * step), acc);
+    }
+    ptr[q * stride] = (!DIT && q > 0) ? acc * twid<R, INV>(tw, k * q * tstep) : acc;
+  }
+}
+
 __device__ __forceinline__ int log2_or_neg(int x) { return (x & (x - 1)) == 0 ? __ffs(x) - 1 : -1; }
 
 // One pass over `nlines` lines by a group of `nthr` threads (thread index `tid`).
@@ -286,7 +309,8 @@ __device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, 
         case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
         case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
         case 8: butterfly8<R, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
-        default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        case 7: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+        default: butterfly_prime<R, INV, DIT>(ln, es, b, ns, tstep, tw, n, rad); break;
       }
     }
     return;
@@ -307,7 +331,8 @@ __device__ __forceinline__ void fft_pass(cpx<R>* s, int es, int ls, int nlines, 
       case 3: butterfly<R, 3, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       case 5: butterfly<R, 5, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
       case 8: butterfly8<R, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
-      default: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      case 7: butterfly<R, 7, INV, DIT>(ln, es, b, ns, nsh, tstep, tw, n); break;
+      default: butterfly_prime<R, INV, DIT>(ln, es, b, ns, tstep, tw, n, rad); break;
     }
   }
 }

@@ -67,7 +67,8 @@ def test_workspace_size_positive_for_valid_desc(lib):
     ("method", 3, "method"),
     ("diffraction", 0, "diffraction"),
     ("reflection", 2, "reflection"),
-    ("height", 11, "factor"),
+    ("height", 37, "factor"),
+    ("width", 2 * 41, "factor"),
     ("npass", 0, "npass"),
     ("fft_schedule", 4, "tuning"),
     ("row_group", -1, "tuning"),

@@ -1,7 +1,8 @@
 """Engine vs the oracle over grid shapes: sides with register transforms
 (powers of two 64..1024 and 7-smooth multiples of 16 up to 480: the complex64
-path), odd and other mixed-radix sides (the shared-memory kernels), non-square
-grids.  Tolerances: 1e-10 (complex128), 1e-4 (mixed)."""
+path), odd and other mixed-radix sides (the shared-memory kernels), sides with
+prime factors 11..31, tiny sides, non-square grids.  Tolerances: 1e-10
+(complex128), 1e-4 (mixed)."""
 import numpy as np
 import pytest
 
@@ -36,6 +37,13 @@ SHAPES = [
     ((384, 320), dict(method="2x2", diffraction=1, beta=0.0, phi=0.0)),
     ((400, 432), dict(method="4x4", diffraction=1, npass=3, beta=0.0, phi=0.0)),
     ((480, 448), dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)),
+    # sides with prime factors from 11 to 31 (generic prime butterflies) and tiny sides
+    ((22, 26), dict(method="4x4", diffraction=3, npass=2, beta=0.05, phi=0.3)),
+    ((33, 17), dict(method="2x2", diffraction=3, reflection=0, beta=0.0, phi=0.0)),
+    ((38, 46), dict(method="4x4", diffraction=1, npass=1, beta=0.1, phi=0.5)),
+    ((29, 31), dict(method="4x4", diffraction=1, npass=3, beta=0.0, phi=0.0)),
+    ((3, 4), dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)),
+    ((2, 13), dict(method="2x2", diffraction=1, beta=0.0, phi=0.0)),
 ]
 
 
