@@ -328,6 +328,20 @@ struct Engine {
 
   int launch_rows(cpx<R>* data, int C, bool inv, double scale) {
     const int nlines = NI * C * d.height;
+    if constexpr (sizeof(R) == 4) {
+      if (d.fft_schedule <= 1 && reg_lanes(d.width) > 0) {
+        RegLaunch rl;
+        const int n1 = reg_lanes(d.width), lpb = 256 / n1;
+        rl.threads = lpb * n1;
+        rl.smem = (size_t)(d.width + lpb * reg_row_stride(n1, d.width)) * sizeof(cpx<R>);
+        rl.grid = dim3((unsigned)((nlines + lpb - 1) / lpb));
+        rl.st = st;
+        const cudaError_t e = fft_rows_reg_dispatch(d.width, inv, rl, data, data, nlines, P(L.twW), (float)scale);
+        ++launches;
+        if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_fft_rows_reg: %s", cudaGetErrorString(e));
+        return DTMM_OK;
+      }
+    }
     int lpb = 4096 / d.width;
     if (lpb < 1) lpb = 1;
     if (lpb > 16) lpb = 16;
@@ -408,7 +422,7 @@ struct Engine {
     p.tw = P(L.twH);
     p.perm = A<int>(L.permH);
     const int cm = cin > cout ? cin : cout;
-    if (col_reg() && cin == cout && (kop == KOP_NONE || kop == KOP_DIAG)) return launch_col_reg(p, in, out, cin);
+    if (col_reg() && cin == cout) return launch_col_reg(p, in, out, cin);
     p.tc = tile_cols(cm, true);
     const size_t smem = 2 * (size_t)cm * d.height * p.tc * sizeof(cpx<R>) + d.height * (sizeof(cpx<R>) + sizeof(int));
     CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1137,13 +1151,28 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
   cpx<R>* X = (cpx<R>*)(ws + L.X);
   // rows forward (natural in and out), out of place into the workspace
   const int nlines = nimg * 4 * H;
+  const bool rrows = sizeof(R) == 4 && reg_lanes(W) > 0;
+  RegLaunch rl;
+  if (rrows) {
+    const int n1 = reg_lanes(W), rlpb = 256 / n1;
+    rl.threads = rlpb * n1;
+    rl.smem = (size_t)(W + rlpb * reg_row_stride(n1, W)) * sizeof(cpx<R>);
+    rl.grid = dim3((unsigned)((nlines + rlpb - 1) / rlpb));
+    rl.st = st;
+  }
   int lpb = std::max(1, std::min(16, 4096 / W));
   size_t smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
   if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", W);
-  CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_fft_rows<R, false><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((const cpx<R>*)in, X, nlines, W, pW, twW, permW,
-                                                                    1.0, lpb);
-  CKL("k_fft_rows");
+  if (rrows) {
+    const cudaError_t e = fft_rows_reg_dispatch(W, false, rl, in, X, nlines, twW, 1.0f);
+    ++launches;
+    if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_fft_rows_reg: %s", cudaGetErrorString(e));
+  } else {
+    CK(cudaFuncSetAttribute(k_fft_rows<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fft_rows<R, false><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((const cpx<R>*)in, X, nlines, W, pW, twW,
+                                                                      permW, 1.0, lpb);
+    CKL("k_fft_rows");
+  }
   // columns: forward transform, the per-k matrix, inverse transform (1/H)
   Grid g;
   g.H = H;
@@ -1168,22 +1197,46 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
   p.plan = pH;
   p.tw = twH;
   p.perm = permH;
-  const size_t per = 4 * (size_t)H * sizeof(cpx<R>) * 2;
-  int tc = 1;
-  while (tc < 16 && per * (tc * 2) <= 72 * 1024) tc *= 2;
-  if (tc > W) tc = W;
-  p.tc = tc;
-  smem = per * tc + H * (sizeof(cpx<R>) + sizeof(int));
-  if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "column of %d pixels too large for one block", H);
-  CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_layer_col<R><<<dim3((W + tc - 1) / tc, nimg), 256, smem, st>>>(p, g, X, (cpx<R>*)out);
-  CKL("k_layer_col");
+  if (sizeof(R) == 4 && reg_lanes(H) > 0) {
+    // register column transforms with the matrix exchanged through the tile
+    const int n1 = reg_lanes(H);
+    const size_t tiles = reg_col_tiles(H, 1);
+    int tx = std::max(1, 256 / (4 * n1));
+    if (tx > W) tx = W;
+    while (tx > 1 && tiles * H * (4 * tx + 1) * sizeof(cpx<R>) > 100 * 1024) tx /= 2;
+    p.tc = tx;
+    RegLaunch cl;
+    cl.smem = tiles * H * (4 * tx + 1) * sizeof(cpx<R>) + H * sizeof(cpx<R>);
+    cl.threads = std::max(32, ((4 * tx * n1 + 31) / 32) * 32);
+    cl.grid = dim3((W + tx - 1) / tx, nimg);
+    cl.st = st;
+    const cudaError_t e = col_reg_dispatch(H, cl, p, g, X, out);
+    ++launches;
+    if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_col_reg: %s", cudaGetErrorString(e));
+  } else {
+    const size_t per = 4 * (size_t)H * sizeof(cpx<R>) * 2;
+    int tc = 1;
+    while (tc < 16 && per * (tc * 2) <= 72 * 1024) tc *= 2;
+    if (tc > W) tc = W;
+    p.tc = tc;
+    smem = per * tc + H * (sizeof(cpx<R>) + sizeof(int));
+    if (smem > 220 * 1024) return fail(DTMM_ENOTSUP, "column of %d pixels too large for one block", H);
+    CK(cudaFuncSetAttribute(k_layer_col<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_layer_col<R><<<dim3((W + tc - 1) / tc, nimg), 256, smem, st>>>(p, g, X, (cpx<R>*)out);
+    CKL("k_layer_col");
+  }
   // rows inverse (1/W)
-  smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
-  CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_fft_rows<R, true><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((cpx<R>*)out, (cpx<R>*)out, nlines, W, pW, twW,
-                                                                   permW, 1.0 / W, lpb);
-  CKL("k_fft_rows");
+  if (rrows) {
+    const cudaError_t e = fft_rows_reg_dispatch(W, true, rl, out, out, nlines, twW, (float)(1.0 / W));
+    ++launches;
+    if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_fft_rows_reg: %s", cudaGetErrorString(e));
+  } else {
+    smem = (size_t)lpb * W * sizeof(cpx<R>) + W * (sizeof(cpx<R>) + sizeof(int));
+    CK(cudaFuncSetAttribute(k_fft_rows<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_fft_rows<R, true><<<(nlines + lpb - 1) / lpb, 256, smem, st>>>((cpx<R>*)out, (cpx<R>*)out, nlines, W, pW, twW,
+                                                                     permW, 1.0 / W, lpb);
+    CKL("k_fft_rows");
+  }
   return DTMM_OK;
 }
 

@@ -188,13 +188,56 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   }
 }
 
+// Plain row FFT of `nlines` lines of N = N1 * N2 points, natural order in
+// and out, src -> dst (the same array for in place: a line's group reads it
+// completely before it writes), times `scale`; blockDim / N1 lines per block.
+template <typename R, int N1, int N2, bool INV>
+__global__ void __launch_bounds__(256) k_fft_rows_reg(const cpx<R>* src, cpx<R>* dst, int nlines,
+                                                     const cpx<R>* __restrict__ twg, R scale) {
+  using TS = TwoStep<N1, N2>;
+  constexpr int W = N1 * N2;
+  constexpr int LS = reg_row_stride(N1, W);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cpx<R>* tw = (cpx<R>*)smem_raw;  // [W] twiddles, lane-major
+  cpx<R>* xb = tw + W;             // [lines per block][LS] exchange
+  for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = TS::twiddle_entry(twg, e);
+  __syncthreads();
+  const int lpb = blockDim.x / N1;
+  const int li = threadIdx.x / N1, t = threadIdx.x % N1;
+  const int line = blockIdx.x * lpb + li;
+  if (li >= lpb || line >= nlines) return;  // whole lane groups leave together
+  const unsigned gm = group_mask<N1>();
+  cpx<R>* xl = xb + (size_t)li * LS;
+  const cpx<R>* in = src + (size_t)line * W;
+  cpx<R>* out = dst + (size_t)line * W;
+  cpx<R> v[N2];
+#pragma unroll
+  for (int m = 0; m < N2; ++m) v[m] = in[t + N1 * m];
+  TS::template step1<R, INV>(v, xl, 1, nullptr, tw, t);
+  __syncwarp(gm);
+  cpx<R> u[TS::J][N1];
+  TS::template step2<R, INV>(u, xl, 1, t);
+  if constexpr (TS::EVEN) {
+    TS::template to_lane_order<R>(u, v);
+#pragma unroll
+    for (int m = 0; m < N2; ++m) out[t + N1 * m] = v[m] * scale;
+  } else {
+    __syncwarp(gm);
+    TS::template store<R>(u, xl, 1, t, scale);
+    __syncwarp(gm);
+#pragma unroll
+    for (int m = 0; m < N2; ++m) out[t + N1 * m] = xl[t + N1 * m];
+  }
+}
+
 // tiles of the column pass: N2 % N1 == 0 keeps the spectra in registers (one
 // tile); otherwise the spectra stay in tile A and, with several window rows,
 // the exchange needs tile B
 __host__ __device__ constexpr bool reg_even(int n) { return reg_lanes(n) > 0 && (n / reg_lanes(n)) % reg_lanes(n) == 0; }
 __host__ __device__ constexpr int reg_col_tiles(int n, int ny) { return (!reg_even(n) && ny > 1) ? 2 : 1; }
 
-// Column pass, k-space operator KOP_NONE or KOP_DIAG (see the file comment).
+// Column pass, k-space operator KOP_NONE, KOP_DIAG or KOP_MAT (C x C per k,
+// exchanged through the tile; see the file comment).
 template <typename R, int N1, int N2>
 __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
                                                          cpx<R>* __restrict__ U) {
@@ -254,6 +297,27 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
 #pragma unroll
       for (int m = 0; m < N2; ++m) v[m] = v[m] * sc;
     }
+    if (p.kop == KOP_MAT) {
+      // C x C matrix per k across the components of a column: through tile A
+      __syncthreads();  // every line's forward exchange is done with the tile
+      if (active) {
+#pragma unroll
+        for (int m = 0; m < N2; ++m) colA[(t + N1 * m) * RS] = v[m];
+      }
+      __syncthreads();
+      if (active && kx < W) {
+        const cpx<R>* mt = (const cpx<R>*)p.ktab + ray * p.ktab_ray_stride + (((size_t)lam * H) * W + kx) * C * C + c * C;
+#pragma unroll
+        for (int m = 0; m < N2; ++m) {
+          const int k = t + N1 * m;
+          const cpx<R>* mrow = mt + (size_t)k * W * C * C;
+          const cpx<R>* in = tileA + (size_t)k * RS + xc;
+          cpx<R> acc = mk<R>((R)0, (R)0);
+          for (int j = 0; j < C; ++j) acc = cfma(mrow[j], in[j * TX], acc);
+          v[m] = acc;
+        }
+      }
+    }
     for (int jj = 0; jj < p.ny; ++jj) {
       const int j = p.j_only >= 0 ? p.j_only : jj;
       __syncthreads();  // the previous window's stores (and the forward exchange) are done with the tile
@@ -300,6 +364,29 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
       for (int m = 0; m < N2; ++m) {
         const int k = t + N1 * m;
         colA[k * RS] = colA[k * RS] * ek[k * 2];
+      }
+    }
+    if (p.kop == KOP_MAT) {
+      // C x C matrix per k across the components of a column, in tile A:
+      // every thread reads its k's components, the block syncs, then writes
+      __syncthreads();
+      cpx<R> r[N2];
+      if (active && kx < W) {
+        const cpx<R>* mt = (const cpx<R>*)p.ktab + ray * p.ktab_ray_stride + (((size_t)lam * H) * W + kx) * C * C + c * C;
+#pragma unroll
+        for (int m = 0; m < N2; ++m) {
+          const int k = t + N1 * m;
+          const cpx<R>* mrow = mt + (size_t)k * W * C * C;
+          const cpx<R>* in = tileA + (size_t)k * RS + xc;
+          cpx<R> acc = mk<R>((R)0, (R)0);
+          for (int j = 0; j < C; ++j) acc = cfma(mrow[j], in[j * TX], acc);
+          r[m] = acc;
+        }
+      }
+      __syncthreads();
+      if (active && kx < W) {
+#pragma unroll
+        for (int m = 0; m < N2; ++m) colA[(t + N1 * m) * RS] = r[m];
       }
     }
     for (int jj = 0; jj < p.ny; ++jj) {
@@ -380,6 +467,17 @@ cudaError_t col_reg_launch(const RegLaunch& L, const ColParams& p, const Grid& g
   return cudaGetLastError();
 }
 
+template <int N1, int N2>
+cudaError_t fft_rows_reg_launch(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw,
+                                float scale) {
+  auto kern = inv ? k_fft_rows_reg<float, N1, N2, true> : k_fft_rows_reg<float, N1, N2, false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
+  if (e != cudaSuccess) return e;
+  kern<<<L.grid, L.threads, L.smem, L.st>>>((const cpx<float>*)src, (cpx<float>*)dst, nlines,
+                                             (const cpx<float>*)tw, scale);
+  return cudaGetLastError();
+}
+
 #define DTMM_REG_SIDES(X) \
   X(64) X(80) X(96) X(112) X(128) X(144) X(160) X(192) X(224) X(240) X(256) X(288) X(320) X(336) X(384) X(400) \
   X(432) X(448) X(480) X(512) X(1024)
@@ -387,7 +485,9 @@ cudaError_t col_reg_launch(const RegLaunch& L, const ColParams& p, const Grid& g
 #define DTMM_REG_DECLARE(N)                                                                                      \
   cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
                           void* X);                                                                            \
-  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out);
+  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out);     \
+  cudaError_t fft_rows_reg_##N(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw, \
+                               float scale);
 
 #define DTMM_REG_DEFINE(N)                                                                                       \
   cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
@@ -396,6 +496,10 @@ cudaError_t col_reg_launch(const RegLaunch& L, const ColParams& p, const Grid& g
   }                                                                                                            \
   cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {    \
     return col_reg_launch<reg_lanes(N), N / reg_lanes(N)>(L, p, g, in, out);                                   \
+  }                                                                                                            \
+  cudaError_t fft_rows_reg_##N(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw, \
+                               float scale) {                                                                  \
+    return fft_rows_reg_launch<reg_lanes(N), N / reg_lanes(N)>(inv, L, src, dst, nlines, tw, scale);           \
   }
 
 DTMM_REG_SIDES(DTMM_REG_DECLARE)
@@ -419,6 +523,17 @@ inline cudaError_t col_reg_dispatch(int n, const RegLaunch& L, const ColParams& 
   case N: return col_reg_##N(L, p, g, in, out);
     DTMM_REG_SIDES(DTMM_REG_COL_CASE)
 #undef DTMM_REG_COL_CASE
+    default: return cudaErrorNotSupported;
+  }
+}
+
+inline cudaError_t fft_rows_reg_dispatch(int n, bool inv, const RegLaunch& L, const void* src, void* dst, int nlines,
+                                         const void* tw, float scale) {
+  switch (n) {
+#define DTMM_REG_FFT_CASE(N) \
+  case N: return fft_rows_reg_##N(inv, L, src, dst, nlines, tw, scale);
+    DTMM_REG_SIDES(DTMM_REG_FFT_CASE)
+#undef DTMM_REG_FFT_CASE
     default: return cudaErrorNotSupported;
   }
 }
