@@ -574,7 +574,8 @@ def run_serve(args, dev):
                    "hbm_budget_bytes": args.hbm_budget},
         "latency_ms": st["latency_ms"], "queue_ms": st["queue_ms"], "requests_per_s": st["requests_per_s"],
         "offered_updates_per_s": offered, "peak_active": st["peak_active"],
-        "peak_budget_bytes": st["peak_budget_bytes"], "pretune_s": tune_s, "clocks": clocks,
+        "peak_budget_bytes": st["peak_budget_bytes"], "host_enqueue_s": st["host_enqueue_s"], "pretune_s": tune_s,
+        "clocks": clocks,
     }
 
 
@@ -807,7 +808,8 @@ def main():
             sv = run_serve(args, dev)
             result["serve"] = {k: sv[k] for k in ("value", "unit", "config", "latency_ms", "queue_ms",
                                                    "requests_per_s", "offered_updates_per_s", "peak_active",
-                                                   "peak_budget_bytes", "clocks") if k in sv}
+                                                   "peak_budget_bytes", "host_enqueue_s", "ms_per_step", "clocks")
+                               if k in sv}
         except Exception as e:
             result["serve"] = {"error": "%s: %s" % (type(e).__name__, e)}
         torch.cuda.empty_cache()

@@ -174,8 +174,35 @@ def _mode_vectors(beta, phi, n, jones, backdir, nlam):
     return np.array(one(jones))
 
 
+_MODES_CACHE = {}
+_MODES_CACHE_MAX = 512
+
+
+def _key(x):
+    a = np.asarray(x)
+    return (a.dtype.str, a.shape, a.tobytes())
+
+
 def illumination_modes(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, intensity=1.0, n=None,
                        focus=0.0, backdir=False, jones=None, diffraction=True, betamax=BETAMAX):
+    """Per-image 4-vectors and FFT modes of the plane-wave illumination
+    (``_illumination_modes``), remembered for repeated arguments (a serving
+    loop builds the same illumination for many requests); returns copies."""
+    key = (tuple(int(v) for v in shape), _key(wavelengths), float(pixelsize), _key(beta), _key(phi), _key(intensity),
+           None if n is None else float(n), float(focus), bool(backdir), None if jones is None else _key(jones),
+           bool(diffraction), float(betamax))
+    hit = _MODES_CACHE.get(key)
+    if hit is None:
+        hit = _illumination_modes(shape, wavelengths, pixelsize, beta, phi, intensity, n, focus, backdir, jones,
+                                  diffraction, betamax)
+        if len(_MODES_CACHE) >= _MODES_CACHE_MAX:
+            _MODES_CACHE.pop(next(iter(_MODES_CACHE)))
+        _MODES_CACHE[key] = hit
+    return tuple(a.copy() for a in hit)
+
+
+def _illumination_modes(shape, wavelengths, pixelsize=1.0, beta=0.0, phi=0.0, intensity=1.0, n=None,
+                        focus=0.0, backdir=False, jones=None, diffraction=True, betamax=BETAMAX):
     """Per-image 4-vectors and FFT modes of the plane-wave illumination.
 
     Returns ``(coef, my, mx)``: ``coef`` complex128 of shape

@@ -47,16 +47,19 @@ def smooth_field(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0):
 
 
 def smooth_field_device(shape, nmodes=8, kmax=4, amplitude=0.2, seed=0, device=None):
-    """``smooth_field`` evaluated on the device (same modes; cosines to FP64 rounding)."""
+    """``smooth_field`` evaluated on the device (same modes; cosines to FP64
+    rounding), every mode in one batch of tensor operations."""
     import torch
 
     h, w = shape
-    y = torch.arange(h, dtype=torch.float64, device=device)[:, None]
-    x = torch.arange(w, dtype=torch.float64, device=device)[None, :]
-    out = torch.zeros((h, w), dtype=torch.float64, device=device)
-    for cx, cy, ph in _smooth_modes(shape, nmodes, kmax, seed):
-        out += torch.cos(2 * np.pi * (cx * x / w + cy * y / h) + ph)
-    return out * (amplitude / nmodes)
+    m = np.asarray(_smooth_modes(shape, nmodes, kmax, seed), np.float64)  # (nmodes, 3): cx, cy, phase
+    # per-mode phase slopes along x and y and offsets, one small upload
+    coef = torch.from_numpy(np.stack([2 * np.pi * m[:, 0] / w, 2 * np.pi * m[:, 1] / h, m[:, 2]], axis=1))
+    coef = coef.to(device, non_blocking=False)
+    y = torch.arange(h, dtype=torch.float64, device=device)[None, :, None]
+    x = torch.arange(w, dtype=torch.float64, device=device)[None, None, :]
+    arg = coef[:, 0, None, None] * x + coef[:, 1, None, None] * y + coef[:, 2, None, None]
+    return torch.cos(arg).sum(0) * (amplitude / nmodes)
 
 
 def twisted_nematic(shape, nlayers, no=1.5, ne=1.7, twist=np.pi / 2, tilt=0.3, amplitude=0.2,
@@ -128,7 +131,9 @@ def twisted_nematic_device(shape, nlayers, no=1.5, ne=1.7, twist=np.pi / 2, tilt
     epsa[..., 0] = 0.0
     epsa[..., 1] = (np.pi / 2 - (dtilt + tilt))[None]
     epsa[..., 2] = (z * twist / nlayers)[:, None, None] + dphi[None]
-    epsv = torch.tensor((no * no, no * no, ne * ne), dtype=torch.float64, device=dev)
+    epsv = torch.empty(3, dtype=torch.float64, device=dev)  # filled on the device: no blocking upload
+    epsv[:2] = no * no
+    epsv[2] = ne * ne
     return DeviceMaterial(np.full((nlayers,), float(thickness)), epsv, epsa, shape,
                           eps_min=min(no * no, ne * ne), uniaxial=True)
 

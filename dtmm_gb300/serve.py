@@ -86,7 +86,21 @@ class TransferServer:
 
             self.pom_jvec = jonesvec((1, 0))
             self.pom_pmat = torch.from_numpy(ray_jonesmat4x4(polarizer(jonesvec((0, 1))))).to(self.device)
+        self._cmfs = {}
         self.stats = {}
+
+    def _cmf(self, wavelengths):
+        """Colour-matching table of a wavelength set on the device (uploaded once per set)."""
+        import torch
+
+        from . import samples
+
+        key = np.asarray(wavelengths, np.float64).tobytes()
+        t = self._cmfs.get(key)
+        if t is None:
+            t = torch.from_numpy(samples.transmission_cmf(wavelengths)).to(self.device)
+            self._cmfs[key] = t
+        return t
 
     # -- sizes -----------------------------------------------------------
     def footprint(self, spec):
@@ -113,7 +127,7 @@ class TransferServer:
             # every upload happens here, while the slot's stream is idle: a
             # copy from pageable memory queued behind the transfer would hold
             # the host loop until the transfer finished
-            cmf = torch.from_numpy(samples.transmission_cmf(spec["wavelengths"])).to(self.device) if self.pom else None
+            cmf = self._cmf(spec["wavelengths"]) if self.pom else None
             mat = samples.twisted_nematic_device(spec["shape"], spec["nlayers"], seed=spec["seed"],
                                                  device=self.device, host_modes=False)
             jones = None if self.npol == 2 else (1, 0)
@@ -160,6 +174,7 @@ class TransferServer:
         used = 0.0
         peak_used = 0.0
         peak_active = 0
+        host_s = 0.0  # host time spent building and enqueueing requests
         torch.cuda.synchronize(self.device)
         t0 = time.perf_counter()
         while pending or active:
@@ -180,6 +195,7 @@ class TransferServer:
                 r = pending.popleft()
                 r.admitted = time.perf_counter() - t0
                 self._start(r, free.pop())
+                host_s += time.perf_counter() - t0 - r.admitted
                 used += r.footprint
                 active.append(r)
                 progressed = True
@@ -201,7 +217,7 @@ class TransferServer:
                             mean=float(lat.mean()), max=float(lat.max())),
             queue_ms=dict(p50=float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in reqs], 50)),
                           p99=float(np.percentile([(r.admitted - r.arrival) * 1e3 for r in reqs], 99))),
-            peak_active=peak_active, peak_budget_bytes=peak_used,
+            peak_active=peak_active, peak_budget_bytes=peak_used, host_enqueue_s=host_s,
             arrival_span_s=float(reqs[-1].arrival - reqs[0].arrival) if reqs else 0.0,
         )
         return self.stats
