@@ -99,6 +99,9 @@ class TransferServer:
         t = self._cmfs.get(key)
         if t is None:
             t = torch.from_numpy(samples.transmission_cmf(wavelengths)).to(self.device)
+            # later requests read it from other streams: let the copy land first
+            # (the stream is idle apart from it when a request starts)
+            torch.cuda.current_stream(self.device).synchronize()
             self._cmfs[key] = t
         return t
 
