@@ -598,7 +598,7 @@ def main():
     ap.add_argument("--c128-subset", type=int, default=8, help="batch: instances of the complex128 comparison")
     ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the trace")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: mean arrival rate (req/s)")
-    ap.add_argument("--slots", type=int, default=32, help="serve: concurrent request slots")
+    ap.add_argument("--slots", type=int, default=16, help="serve: concurrent request slots")
     ap.add_argument("--hbm-budget", type=float, default=150e9, help="serve: admission budget (bytes)")
     ap.add_argument("--no-batch", action="store_true", help="precision workload: skip the batch summary")
     ap.add_argument("--no-serve", action="store_true", help="precision workload: skip the serving summary")
