@@ -23,7 +23,8 @@ ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_s
                "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field", "dtmm_pom_field",
                "dtmm_field2specter", "dtmm_specter2color", "dtmm_pom_image", "dtmm_director2data",
                "dtmm_diffract_workspace_size", "dtmm_diffract", "dtmm_q2data", "dtmm_wave_field",
-               "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields")
+               "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields",
+               "dtmm_twisted_nematic_angles")
 ABI_VERSION = 2
 STATIC_SCRATCH_BYTES = 64 << 20
 
@@ -162,6 +163,9 @@ def load(build_if_missing=True):
     lib.dtmm_field_intensity.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 3
     lib.dtmm_scale_fields.restype = ctypes.c_int
     lib.dtmm_scale_fields.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 5
+    lib.dtmm_twisted_nematic_angles.restype = ctypes.c_int
+    lib.dtmm_twisted_nematic_angles.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] + [
+        ctypes.c_double] * 4 + [ctypes.c_void_p, ctypes.c_void_p]
     lib.dtmm_q2data.restype = ctypes.c_int
     lib.dtmm_q2data.argtypes = [ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_double] * 4 + [
         ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]

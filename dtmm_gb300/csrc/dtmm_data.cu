@@ -7,6 +7,7 @@
 // (director2angles, dtmm/data.py:975-990).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <string>
 
@@ -78,6 +79,86 @@ extern "C" int dtmm_director2data(long long nvox, const void* director, int dire
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     dtmm::last_error_slot() = std::string("k_director2data: ") + cudaGetErrorString(e);
+    return DTMM_ECUDA;
+  }
+  return DTMM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Synthetic twisted-nematic Euler angles (the benchmark's seeded director
+// fields, dtmm_gb300.samples.twisted_nematic): per pixel two smooth
+// perturbations d_phi, d_tilt (sums of cosine modes cos(ax x + ay y + c),
+// scaled), then for every layer l
+//   epsa[l][y][x] = (0, pi/2 - (d_tilt + tilt), l * twist / L + d_phi).
+// The modes arrive by value, so building a request needs no upload.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kMaxModes = 16;
+struct ModeSet {
+  int n;
+  double ax[kMaxModes], ay[kMaxModes], c[kMaxModes];
+  double scale;
+};
+
+__device__ double mode_sum(const ModeSet& m, double x, double y) {
+  double s = 0.0;
+  for (int i = 0; i < m.n; ++i) s += cos(m.ax[i] * x + m.ay[i] * y + m.c[i]);
+  return s * m.scale;
+}
+
+__global__ void k_twisted_angles(int L, int H, int W, ModeSet mphi, ModeSet mtilt, double twist, double tilt,
+                                 double* __restrict__ epsa) {
+  const long long HW = (long long)H * W;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < HW; p += (long long)gridDim.x * blockDim.x) {
+    const double y = (double)(p / W), x = (double)(p % W);
+    const double dphi = mode_sum(mphi, x, y);
+    const double th = M_PI / 2 - (mode_sum(mtilt, x, y) + tilt);
+    for (int l = 0; l < L; ++l) {
+      double* e = epsa + ((long long)l * HW + p) * 3;
+      e[0] = 0.0;
+      e[1] = th;
+      e[2] = (double)l * twist / L + dphi;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int dtmm_twisted_nematic_angles(int nlayers, int height, int width, const double* modes, int nmodes,
+                                           double amp_phi, double amp_tilt, double twist, double tilt, double* epsa,
+                                           void* stream) {
+  dtmm::last_error_slot().clear();
+  if (nlayers < 1 || height < 1 || width < 1) {
+    dtmm::last_error_slot() = "empty grid";
+    return DTMM_EINVAL;
+  }
+  if (!modes || !epsa) {
+    dtmm::last_error_slot() = "null pointer";
+    return DTMM_EINVAL;
+  }
+  if (nmodes < 1 || nmodes > kMaxModes) {
+    dtmm::last_error_slot() = "nmodes must be 1..16";
+    return DTMM_EINVAL;
+  }
+  ModeSet mp, mt;
+  mp.n = mt.n = nmodes;
+  mp.scale = amp_phi;
+  mt.scale = amp_tilt;
+  for (int i = 0; i < nmodes; ++i) {
+    mp.ax[i] = modes[3 * i];
+    mp.ay[i] = modes[3 * i + 1];
+    mp.c[i] = modes[3 * i + 2];
+    mt.ax[i] = modes[3 * (nmodes + i)];
+    mt.ay[i] = modes[3 * (nmodes + i) + 1];
+    mt.c[i] = modes[3 * (nmodes + i) + 2];
+  }
+  const long long hw = (long long)height * width;
+  const unsigned blocks = (unsigned)std::min<long long>((hw + 255) / 256, 152LL * 8);
+  k_twisted_angles<<<blocks, 256, 0, (cudaStream_t)stream>>>(nlayers, height, width, mp, mt, twist, tilt, epsa);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    dtmm::last_error_slot() = std::string("k_twisted_angles: ") + cudaGetErrorString(e);
     return DTMM_ECUDA;
   }
   return DTMM_OK;

@@ -120,17 +120,30 @@ def twisted_nematic_device(shape, nlayers, no=1.5, ne=1.7, twist=np.pi / 2, tilt
 
     dev = device or torch.device("cuda", torch.cuda.current_device())
     h, w = shape
+    epsa = torch.empty((nlayers, h, w, 3), dtype=torch.float64, device=dev)
     if host_modes:
         dphi = torch.from_numpy(smooth_field(shape, nmodes, kmax, amplitude, seed=seed)).to(dev)
         dtilt = torch.from_numpy(smooth_field(shape, nmodes, kmax, amplitude, seed=seed + 7919)).to(dev)
+        z = torch.arange(nlayers, dtype=torch.float64, device=dev)
+        epsa[..., 0] = 0.0
+        epsa[..., 1] = (np.pi / 2 - (dtilt + tilt))[None]
+        epsa[..., 2] = (z * twist / nlayers)[:, None, None] + dphi[None]
     else:
-        dphi = smooth_field_device(shape, nmodes, kmax, amplitude, seed=seed, device=dev)
-        dtilt = smooth_field_device(shape, nmodes, kmax, amplitude, seed=seed + 7919, device=dev)
-    z = torch.arange(nlayers, dtype=torch.float64, device=dev)
-    epsa = torch.empty((nlayers, h, w, 3), dtype=torch.float64, device=dev)
-    epsa[..., 0] = 0.0
-    epsa[..., 1] = (np.pi / 2 - (dtilt + tilt))[None]
-    epsa[..., 2] = (z * twist / nlayers)[:, None, None] + dphi[None]
+        # one kernel, the modes passed by value (dtmm_twisted_nematic_angles)
+        import ctypes
+
+        from . import _lib
+
+        rows = []
+        for sd in (seed, seed + 7919):
+            m = np.asarray(_smooth_modes(shape, nmodes, kmax, sd), np.float64)
+            rows.append(np.stack([2 * np.pi * m[:, 0] / w, 2 * np.pi * m[:, 1] / h, m[:, 2]], axis=1))
+        modes = np.ascontiguousarray(np.concatenate(rows))
+        lib = _lib.load()
+        _lib.check(lib.dtmm_twisted_nematic_angles(
+            int(nlayers), int(h), int(w), modes.ctypes.data_as(ctypes.c_void_p), int(nmodes),
+            float(amplitude / nmodes), float(amplitude / nmodes), float(twist), float(tilt),
+            ctypes.c_void_p(epsa.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
     epsv = torch.empty(3, dtype=torch.float64, device=dev)  # filled on the device: no blocking upload
     epsv[:2] = no * no
     epsv[2] = ne * ne

@@ -270,6 +270,16 @@ int dtmm_director2data(long long nvox, const void* director, int director_double
 int dtmm_q2data(long long nvox, const double* qtensor, const void* mask, double no, double ne, double nhost,
                 double scale_factor, int biaxial, double* epsv, double* epsa, void* stream);
 
+/* Synthetic twisted-nematic Euler angles for benchmarks and serving tests
+   (no reference counterpart; the seeded director of
+   dtmm_gb300.samples.twisted_nematic): epsa[L][H][W][3] (device float64) =
+   (0, pi/2 - (d_tilt + tilt), l twist / L + d_phi) with d_phi = amp_phi sum_i
+   cos(ax_i x + ay_i y + c_i) over the first nmodes rows of `modes` and d_tilt
+   = amp_tilt times the same sum over the next nmodes rows; modes: host
+   float64 [2 nmodes][3] (ax, ay, c), nmodes <= 16. */
+int dtmm_twisted_nematic_angles(int nlayers, int height, int width, const double* modes, int nmodes, double amp_phi,
+                                double amp_tilt, double twist, double tilt, double* epsa, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

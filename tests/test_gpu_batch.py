@@ -64,6 +64,21 @@ def test_device_material_matches_host():
     assert mat.ev_strides == (0, 0, 0)
 
 
+def test_device_material_kernel_matches_host():
+    """The one-kernel generator (modes by value, FP64 cosines on the device)
+    equals the host generator to FP64 rounding (1e-13 absolute on angles)."""
+    import torch
+
+    from dtmm_gb300 import samples
+
+    for shape, nl, seed in (((40, 48), 5, 17), ((64, 96), 3, 4), ((16, 16), 120, 9)):
+        d, epsv, epsa = samples.twisted_nematic(shape, nl, seed=seed)
+        mat = samples.twisted_nematic_device(shape, nl, seed=seed, host_modes=False)
+        torch.cuda.synchronize()
+        assert np.abs(mat.epsa.cpu().numpy() - epsa).max() < 1e-13
+        assert np.array_equal(mat.epsv.cpu().numpy(), np.asarray(epsv))
+
+
 @pytest.mark.parametrize("shape", [(48, 40), (64, 72), (96, 64)])
 def test_radix8_schedule_matches_oracle(shape):
     import torch
