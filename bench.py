@@ -146,12 +146,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def ncu_summary():
+    """The committed ncu summary of the dominant kernel ({} if absent)."""
+    p = os.path.join(ROOT, "profiles", "layer_row_traffic.json")
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
 def ncu_traffic():
     """DRAM bytes per launch of the dominant kernel, from the committed ncu summary (None if absent)."""
-    p = os.path.join(ROOT, "profiles", "layer_row_traffic.json")
-    if os.path.exists(p):
-        return json.load(open(p)).get("dram_bytes_per_launch_full")
-    return None
+    return ncu_summary().get("dram_bytes_per_launch_full")
 
 
 # ---------------------------------------------------------------------------
@@ -735,6 +738,8 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": ncu_traffic(), "kernel": "k_layer_row_reg<float,4,real,16,16>", "peak_source": peak_kind,
                 "kernel_share": row_ms / eager_ms,
+                "issue_bound": {k: ncu_summary().get(k) for k in ("smsp_issue_active", "sm_pipe_fma_cycles_active",
+                                                                   "sm_inst_executed_pipe_lsu", "note")},
                 "device_ms_per_step": {"layer_row": row_ms / args.steps, "layer_col": col_ms / args.steps,
                                        "voxel_op": op_ms / args.steps}}
 
