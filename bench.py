@@ -168,9 +168,11 @@ def run_reference(args, rank):
             rates.append(rate)
     value = float(np.median(rates))
     sample = "1 of 60 layers, 1 of 3 passes, full 256x256 grid, 9 wavelengths, 2 polarisations per step"
+    upd = SHAPE[0] * SHAPE[1] * NLAYERS * len(WAVELENGTHS) * 2 * OPTS["npass"]
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": upd / value * 1e3, "ms_per_step_extrapolated": True,
+        "updates_per_step": upd, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": CONFIG,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
