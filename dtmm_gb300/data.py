@@ -65,6 +65,13 @@ def director2data(director, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=
     return thickness, epsv, epsa
 
 
+def director2angles(director):
+    """Euler angles (0, theta, phi) of a director field [..., 3] (dtmm/data.py:975-990), from the
+    same kernel as ``director2data``; numpy in, numpy out, device tensors stay on the device."""
+    _, epsa, host, _ = _run(director, None, 1.5, 1.6, None, 1.0)
+    return epsa.cpu().numpy() if host else epsa
+
+
 _Q_ROWS = (0, 1, 2, 0, 0, 1)
 _Q_COLS = (0, 1, 2, 1, 2, 2)
 
@@ -135,4 +142,4 @@ def q_material(tensor, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_
     return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape, uniaxial=True)
 
 
-__all__ = ["director2data", "Q2data", "device_material", "q_material"]
+__all__ = ["director2data", "director2angles", "Q2data", "device_material", "q_material"]

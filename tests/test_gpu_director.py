@@ -25,6 +25,14 @@ def test_director2data_matches_reference():
     assert np.abs(ea - z["epsa_masked"]).max() < 4e-15
 
 
+def test_director2angles_matches_reference():
+    from dtmm_gb300 import data
+
+    z = np.load(os.path.join(HERE, "golden", "director.npz"))
+    ea = data.director2angles(z["director"])
+    assert np.abs(ea - z["epsa_default"]).max() < 4e-15
+
+
 def test_float32_director():
     import dtmm_oracle as O
     from dtmm_gb300 import data
