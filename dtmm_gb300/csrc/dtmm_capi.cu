@@ -99,8 +99,13 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->height > 16384 || d->width > 16384) return fail(DTMM_ENOTSUP, "grid side above 16384");
   if (d->nlam < 1 || d->npol < 1 || d->nray < 1) return fail(DTMM_EINVAL, "empty image axes");
   if (d->method != 4 && d->method != 2) return fail(DTMM_EINVAL, "method must be 4 (4x4) or 2 (2x2)");
-  if (d->diffraction < 1) return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path");
-  if (d->method == 4 && d->reflection != 1) return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1 on this path");
+  // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1)
+  const bool local4 = d->method == 4 && d->diffraction == 0 && d->reflection == 2;
+  if (d->diffraction < 0 || (d->diffraction < 1 && !local4))
+    return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2)");
+  if (d->method == 4 && d->reflection != 1 && !local4)
+    return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1, and mode 2 without diffraction, on this path");
+  if (local4 && d->npass != 1) return fail(DTMM_ENOTSUP, "4x4 reflection mode 2 supports npass = 1 on this path");
   if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
     return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
@@ -142,6 +147,10 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
+  if (d->method == 4 && d->diffraction == 0) {  // the per-voxel transfer needs the scalars only
+    L.total = off;
+    return L;
+  }
   L.part = take(sizeof(double) * std::max<size_t>(2 * kPartBlocks, 4 * kWinChunks * nrw));
   L.twH = take(L.cplx * H);
   L.permH = take(sizeof(int) * H);
@@ -678,8 +687,40 @@ struct Engine {
     return DTMM_OK;
   }
 
-  int setup() {
-    // host scalars -> workspace
+  // 4x4 reflection mode 2 without diffraction: the per-voxel transfer layer
+  // by layer (input -> field_out, then in place), each layer's result also
+  // into the bulk output when asked
+  int run_local4() {
+    int rc = scalars();
+    if (rc) return rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    Local4Params p;
+    p.epsv = d.epsv;
+    p.epsa = d.epsa;
+    for (int i = 0; i < 3; ++i) {
+      p.ev_s[i] = d.epsv_strides[i];
+      p.ea_s[i] = d.epsa_strides[i];
+    }
+    p.eps_complex = d.eps_complex;
+    p.ks = ks();
+    p.beta = rbeta();
+    p.phi = rphi();
+    const dim3 grid((unsigned)((L.HW + 127) / 128), (unsigned)d.nray);
+    for (int l = 0; l < d.nlayers; ++l) {
+      p.layer = l;
+      p.nst = d.nstep[l];
+      p.d = d.thickness[l] / d.nstep[l];
+      cpx<R>* slab = bulk ? bulk + (size_t)(l + 1) * NI * 4 * L.HW : nullptr;
+      k_local4<R><<<grid, 128, 0, st>>>(p, g, l == 0 ? (const cpx<R>*)fin : (const cpx<R>*)fout, fout, slab);
+      CKL("k_local4");
+    }
+    return DTMM_OK;
+  }
+
+  // host scalars -> workspace: ks | beta | phi | window offsets
+  int scalars() {
     std::vector<double> h(d.nlam + 4 * d.nray);
     for (int i = 0; i < d.nlam; ++i) h[i] = d.ks[i];
     const double dwin = d.diffraction > 1 ? 2.0 * d.betamax / (d.diffraction - 1) : 1.0;
@@ -697,6 +738,12 @@ struct Engine {
       k_set_scalars<<<1, 64, 0, st>>>(sc, ks());
       CKL("k_set_scalars");
     }
+    return DTMM_OK;
+  }
+
+  int setup() {
+    int rc = scalars();
+    if (rc) return rc;
     // FFT tables
     k_fft_tables<R><<<(d.height + 255) / 256, 256, 0, st>>>(pH, P(L.twH), A<int>(L.permH));
     CKL("k_fft_tables");
@@ -1080,8 +1127,13 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   e.g.nray = d->nray;
   make_plan(d->height, e.pH, d->fft_schedule == 3);
   make_plan(d->width, e.pW, d->fft_schedule == 3);
-  int rc = e.setup();
-  if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();
+  int rc;
+  if (d->method == 4 && d->diffraction == 0) {
+    rc = e.run_local4();
+  } else {
+    rc = e.setup();
+    if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();
+  }
   if (launches) *launches = e.launches;
   return rc;
 }

@@ -421,6 +421,175 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
 }
 
 // ---------------------------------------------------------------------------
+// 4x4 transfer without diffraction, reflection mode 2 (dtmm/propagate_4x4.py:18-52
+// with no diffraction matrices; dtmm/transfer.py:618-884 without the k-space
+// sweep): per pixel, field <- F . diag(exp(i k0 d alpha)) . F^-1 . field for
+// every layer and sub-step, with the voxel's Berreman field matrix F and
+// eigenvalues alpha for the ray's (beta, phi) (dtmm/tmm.py:124, :157-289,
+// rotated back by phi as dtmm/linalg.py:674).  F P F^-1 does not depend on
+// the scale of F's columns, so they are not normalised; a singular F gives a
+// zero operator, as the reference's inverse does (dtmm/linalg.py:460-518).
+// One thread per (pixel, ray) and layer: the FP64 solve once, then the
+// operator on every polarisation and wavelength of the ray.
+// ---------------------------------------------------------------------------
+struct Local4Params {
+  const void* epsv;   // (L?,H?,W?,3) float64 or complex128
+  const double* epsa; // (L?,H?,W?,3) float64
+  long long ev_s[3];
+  long long ea_s[3];
+  int eps_complex;
+  int layer;
+  double d;           // sub-step thickness (pixels, signed by direction)
+  int nst;            // sub-steps
+  const double* ks;   // [lam]
+  const double* beta; // [ray]
+  const double* phi;  // [ray]
+};
+
+// field matrix and eigenvalues of one voxel (isotropic or uniaxial)
+__device__ void local_fmat(double beta, double phi, const cpx<double> ev[3], double theta, double azim,
+                           cpx<double> F[4][4], cpx<double> al[4]) {
+  const cpx<double> z0 = mk<double>(0.0, 0.0);
+  for (int i = 0; i < 4; ++i) {
+    al[i] = z0;
+    for (int j = 0; j < 4; ++j) F[i][j] = z0;
+  }
+  const bool e01 = ev[0].re == ev[1].re && ev[0].im == ev[1].im;
+  const bool e12 = ev[1].re == ev[2].re && ev[1].im == ev[2].im;
+  if (e01 && e12) {
+    iso_alphaf(beta, phi, ev[0], al, F);  // already rotated by phi
+    return;
+  }
+  if (e01) {
+    double st, ct, sf, cf;
+    sincos(theta, &st, &ct);
+    sincos(azim - phi, &sf, &cf);
+    const cpx<double> eps11 = ev[0], delta = ev[2] - ev[0];
+    const cpx<double> u = eps11 + delta * (ct * ct);
+    cpx<double> evs, evpp, evpm;
+    if (beta == 0.0) {
+      evs = csqrt_d(eps11);
+      const cpx<double> w = eps11 * (eps11 + delta);
+      const cpx<double> sq = cdiv(csqrt_d(u * w), u);
+      evpp = sq;
+      evpm = -sq;
+      F[0][2] = evs * (-sf); F[1][2] = eps11 * (-sf); F[2][2] = evs * cf;    F[3][2] = eps11 * (-cf);
+      F[0][3] = evs * (-sf); F[1][3] = eps11 * sf;    F[2][3] = evs * cf;    F[3][3] = eps11 * cf;
+      F[0][0] = mk<double>(cf, 0.0); F[1][0] = evpp * cf; F[2][0] = mk<double>(sf, 0.0); F[3][0] = evpp * (-sf);
+      F[0][1] = mk<double>(cf, 0.0); F[1][1] = evpm * cf; F[2][1] = mk<double>(sf, 0.0); F[3][1] = evpm * (-sf);
+    } else {
+      const cpx<double> ev02 = mk<double>(eps11.re - beta * beta, eps11.im);
+      evs = csqrt_d(ev02);
+      const double gama = beta * cf;
+      const cpx<double> v = delta * (gama * 2.0 * st * ct);
+      const cpx<double> w = delta * (gama * gama * st * st) - eps11 * (ev02 + delta);
+      const cpx<double> u2 = u * 2.0;
+      const cpx<double> sq = cdiv(csqrt_d(v * v - u * w * 4.0), u2);
+      const cpx<double> vh = cdiv(v, u2);
+      evpp = sq - vh;
+      evpm = -vh - sq;
+      const double sfst = st * sf, cfst = cf * st, ctbeta = ct * beta;
+      const cpx<double> ie = cdiv(mk<double>(1.0, 0.0), eps11);
+      const cpx<double> ev02cfst = ev02 * cfst;
+      const cpx<double> evssfst = evs * sfst, evscfst = evs * cfst, evsctbeta = evs * ctbeta;
+      const cpx<double> eps11sfst = eps11 * sfst;
+      F[0][2] = evssfst;  F[1][2] = eps11sfst; F[2][2] = mk<double>(ctbeta, 0.0) - evscfst; F[3][2] = ev02cfst - evsctbeta;
+      F[0][3] = -evssfst; F[1][3] = eps11sfst; F[2][3] = evscfst + mk<double>(ctbeta, 0.0); F[3][3] = ev02cfst + evsctbeta;
+      F[0][0] = (evpp * ctbeta - ev02cfst) * ie;  F[1][0] = mk<double>(ctbeta, 0.0) - evpp * cfst;
+      F[2][0] = mk<double>(-sfst, 0.0);           F[3][0] = evpp * sfst;
+      F[0][1] = (ev02cfst - evpm * ctbeta) * ie;  F[1][1] = evpm * cfst - mk<double>(ctbeta, 0.0);
+      F[2][1] = mk<double>(sfst, 0.0);            F[3][1] = evpm * (-sfst);
+    }
+    al[0] = evpp; al[1] = evpm; al[2] = evs; al[3] = -evs;
+  } else {
+    return;  // biaxial voxels are refused by the host before the call
+  }
+  // rotate the field rows (Ex, Hy, Ey, Hx) back by phi
+  double s, c;
+  sincos(phi, &s, &c);
+  for (int m = 0; m < 4; ++m) {
+    const cpx<double> f0 = F[0][m], f1 = F[1][m], f2 = F[2][m], f3 = F[3][m];
+    F[0][m] = f0 * c - f2 * s;
+    F[1][m] = f1 * c + f3 * s;
+    F[2][m] = f0 * s + f2 * c;
+    F[3][m] = -(f1 * s) + f3 * c;
+  }
+}
+
+// exp(i kd alpha) of a complex eigenvalue in the bulk precision
+template <typename R>
+__device__ __forceinline__ cpx<R> local_phase(double kd, cpx<double> a) {
+  if constexpr (sizeof(R) == 4) {
+    const float e = __expf(-(float)(kd * a.im));
+    return phase_of<float>(f32_rn(kd * a.re), 1.0f) * e;
+  } else {
+    double s, c;
+    sincos(kd * a.re, &s, &c);
+    const double e = exp(-kd * a.im);
+    return mk<double>(e * c, e * s);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cpx<R>* in, cpx<R>* out,
+                                                cpx<R>* bulk_slab) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.y;
+  if (pix >= HW) return;
+  const int y = pix / g.W, x = pix - y * g.W;
+  const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
+  const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
+  cpx<double> ev[3];
+  if (p.eps_complex) {
+    const cpx<double>* e = (const cpx<double>*)p.epsv + eo;
+    ev[0] = e[0]; ev[1] = e[1]; ev[2] = e[2];
+  } else {
+    const double* e = (const double*)p.epsv + eo;
+    ev[0] = mk<double>(e[0], 0.0); ev[1] = mk<double>(e[1], 0.0); ev[2] = mk<double>(e[2], 0.0);
+  }
+  cpx<double> F[4][4], al[4], Fi[4][4];
+  local_fmat(p.beta[ray], p.phi[ray], ev, p.epsa[ao + 1], p.epsa[ao + 2], F, al);
+  inv4(F, Fi);
+  cpx<R> f[4][4], fi[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      f[i][j] = cvt<R>(F[i][j]);
+      fi[i][j] = cvt<R>(Fi[i][j]);
+    }
+  const int per = g.npol * g.nlam;
+  for (int q = 0; q < per; ++q) {
+    const int lam = q % g.nlam;
+    const int img = ray * per + q;
+    const double kd = p.ks[lam] * p.d;
+    cpx<R> ph[4];
+    for (int m = 0; m < 4; ++m) ph[m] = local_phase<R>(kd, al[m]);
+    const cpx<R>* src = in + (size_t)img * 4 * HW + pix;
+    cpx<R> v[4];
+    for (int c = 0; c < 4; ++c) v[c] = src[(size_t)c * HW];
+    for (int st = 0; st < p.nst; ++st) {
+      cpx<R> u[4];
+      for (int m = 0; m < 4; ++m) {
+        cpx<R> acc = mk<R>((R)0, (R)0);
+        for (int c = 0; c < 4; ++c) acc = cfma(fi[m][c], v[c], acc);
+        u[m] = acc * ph[m];
+      }
+      for (int c = 0; c < 4; ++c) {
+        cpx<R> acc = mk<R>((R)0, (R)0);
+        for (int m = 0; m < 4; ++m) acc = cfma(f[c][m], u[m], acc);
+        v[c] = acc;
+      }
+    }
+    cpx<R>* dst = out + (size_t)img * 4 * HW + pix;
+    for (int c = 0; c < 4; ++c) dst[(size_t)c * HW] = v[c];
+    if (bulk_slab) {
+      cpx<R>* b = bulk_slab + (size_t)img * 4 * HW + pix;
+      for (int c = 0; c < 4; ++c) b[(size_t)c * HW] = v[c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Window statistics and 1D window weight tables (diffraction > 1).
 //
 // Window (i, j) of the n x n grid is the tent cx_i(beta_x) * cy_j(beta_y),

@@ -360,7 +360,7 @@ def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffract
     d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
     d.method = 4 if method == "4x4" else 2
     d.diffraction, d.npass = int(diffraction), int(npass)
-    d.reflection = 1 if method == "4x4" else 0
+    d.reflection = (2 if int(diffraction) == 0 else 1) if method == "4x4" else 0
     d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
     d.betamax, d.nin, d.nout, d.smooth = BETAMAX, N_COVER, N_COVER, SMOOTH
     th = np.ones(int(nlayers))
@@ -398,6 +398,8 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     precision = _precision[0] if precision is None else precision
     if reflection is None:
         reflection = 0 if method == "2x2" else 1
+        if method == "4x4" and diffraction == 0:
+            reflection = 2
         if npass > 1:
             reflection = 1
     _check_path(method, reflection, npass, diffraction, DTMM_NORM_FFT)
@@ -427,13 +429,17 @@ def _check_path(method, reflection, npass, diffraction, norm):
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
     if method != "4x4" and npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
-    if reflection not in ((1,) if method == "4x4" else (0, 1)):
-        raise NotImplementedError("reflection mode %d (real-space reflections) is outside the GPU engine" % reflection)
+    # reflection mode 2 without diffraction: the per-voxel 4x4 transfer
+    local = method == "4x4" and reflection == 2 and diffraction == 0
+    if reflection not in ((1,) if method == "4x4" else (0, 1)) and not local:
+        raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
+    if local and npass != 1:
+        raise NotImplementedError("reflection mode 2 with npass > 1 is outside the GPU engine")
     if method != "4x4" and npass != 1:
         raise NotImplementedError("the 2x2 method with npass > 1 is outside the GPU engine")
     if not (0 <= diffraction < np.inf):
         raise NotImplementedError("full (modal) diffraction is outside the GPU engine")
-    if diffraction == 0:
+    if diffraction == 0 and not local:
         if method == "4x4":
             raise ValueError("Invalid diffraction value")
         raise NotImplementedError("diffraction=0 is outside the GPU engine")

@@ -1069,13 +1069,27 @@ def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, 
 # --------------------------------------------------------------------------
 # drivers (dtmm/transfer.py)
 # --------------------------------------------------------------------------
+def _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps):
+    """Reflection mode 2 without diffraction: F . P . F^-1 per voxel, nsteps
+    times, on the real-space field (dtmm/propagate_4x4.py:18-52 with dmatpn None)."""
+    d, epsv, epsa = layer
+    kd = ks * d
+    alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
+    p = phasem(alpha, kd[..., None, None])
+    for _ in range(nsteps):
+        field = dotmdmf(f, p, fi, field)
+    return field
+
+
 def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
                  reflection, multiray, norm, smooth, betamax, ret_bulk, out):
-    """4x4 pass x layer sweep in k-space, reflection mode 1 (dtmm/transfer.py:618-884)."""
+    """4x4 pass x layer sweep (dtmm/transfer.py:618-884): reflection mode 1 in
+    k-space, and reflection mode 2 without diffraction (the per-voxel 4x4
+    transfer) in real space."""
     if reflection not in (1, 2, 3, 4):
         raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
-    if reflection != 1:
-        raise NotImplementedError("oracle covers 4x4 reflection mode 1")
+    if reflection not in (1, 2) or (reflection == 2 and diffraction != 0):
+        raise NotImplementedError("oracle covers 4x4 reflection mode 1, and mode 2 without diffraction")
     if smooth < 0:
         smooth = 0.0
     if norm != DTMM_NORM_FFT:
@@ -1113,7 +1127,9 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     i0 = field2intensity(field0).sum(axis=(-2, -1))
     if not (0 <= diffraction < np.inf):
         raise NotImplementedError("oracle covers finite diffraction")
-    field = fft2(field)
+    work_in_fft = reflection != 2  # (dtmm/transfer.py:720-723)
+    if work_in_fft:
+        field = fft2(field)
     if npass > 1:
         pin_mat = projection_matrix(shape, ks, epsv=refind2eps([nin] * 3), mode=+1, betamax=betamax)
         pout_mat = projection_matrix(shape, ks, epsv=refind2eps([nout] * 3), mode=+1, betamax=betamax)
@@ -1122,12 +1138,16 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
         for j in indices:
             nsub, (thickness, ev, ea) = layers[j]
             _, (de, ee, ae) = eff_layers[j]
-            field = propagate_4x4_effective_1(field, ks, (thickness * direction, ev, ea), (de * direction, ee, ae),
-                                              beta, phi, nsub, diffraction, betamax)
+            if reflection == 2:
+                field = _transfer_ray_4x4_2(field, ks, (thickness * direction, ev, ea), beta, phi, nsub)
+            else:
+                field = propagate_4x4_effective_1(field, ks, (thickness * direction, ev, ea),
+                                                  (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             if bulk_out is not None:
                 bulk_out[j] = field
         indices.reverse()
-        field = ifft2(field)
+        if work_in_fft:
+            field = ifft2(field)
         if npass > 1:
             if i % 2 == 0:
                 if i == 0:
@@ -1152,11 +1172,13 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                     field_in[...] = field_in * fact
                     field = field0 - field
                     field_in[...] = field_in + field
-            field = fft2(field)
+            if work_in_fft:
+                field = fft2(field)
         else:
             field_out[...] = field
     if ret_bulk:
-        bulk_out[1:-1] = ifft2(bulk_out[1:-1])
+        if work_in_fft:
+            bulk_out[1:-1] = ifft2(bulk_out[1:-1])
         return bulk_out, wavelengths, pixelsize
     return field_out, wavelengths, pixelsize
 

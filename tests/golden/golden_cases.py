@@ -110,6 +110,29 @@ CASES = {
                             illum=dict(jones=(1, 0), n=1.0),
                             transfer=dict(method="4x4", diffraction=1, npass=3, nin=1.0, nout=1.33,
                                           betamax=0.9, beta=0.0, phi=0.0)),
+    # 4x4 without diffraction (reflection resolves to 2): the per-voxel 4x4 transfer
+    "nodiff_4x4": dict(shape=(16, 20), nlayers=5, wavelengths=[450.0, 600.0], pixelsize=100.0,
+                       material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=18,
+                       illum=dict(),
+                       transfer=dict(method="4x4", diffraction=0, beta=0.0, phi=0.0)),
+    "nodiff_4x4_offaxis_nstep2": dict(shape=(12, 14), nlayers=3, wavelengths=[520.0], pixelsize=100.0,
+                                      material=("twisted", dict(thickness=2.0)), seed=19,
+                                      illum=dict(beta=0.2, phi=0.7, jones=(1, 0.3j)),
+                                      transfer=dict(method="4x4", diffraction=0, nstep=2, beta=0.2, phi=0.7)),
+    "nodiff_4x4_mixed": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0, 650.0], pixelsize=100.0,
+                                       material=("mixed", dict()), seed=20,
+                                       illum=dict(beta=0.1, phi=1.2),
+                                       transfer=dict(method="4x4", diffraction=0, beta=0.1, phi=1.2)),
+    "nodiff_4x4_absorbing_bulk": dict(shape=(8, 10), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                      material=("absorbing", dict()), seed=21,
+                                      illum=dict(jones=(1, 0)),
+                                      transfer=dict(method="4x4", diffraction=0, beta=0.0, phi=0.0,
+                                                    ret_bulk=True)),
+    "nodiff_4x4_multiray": dict(shape=(12, 12), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                                material=("twisted", dict()), seed=22,
+                                illum=dict(beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0], jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=0, multiray=True,
+                                              beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0])),
 }
 
 

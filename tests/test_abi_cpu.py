@@ -71,6 +71,7 @@ def test_workspace_size_positive_for_valid_desc(lib):
     ("width", 2 * 41, "factor"),
     ("npass", 0, "npass"),
     ("fft_schedule", 4, "tuning"),
+    ("diffraction", -1, "diffraction"),
     ("row_group", -1, "tuning"),
     ("col_tile", -2, "tuning"),
 ])
@@ -78,6 +79,15 @@ def test_invalid_descriptors_are_rejected(lib, field, value, needle):
     d = _desc(**{field: value})
     assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) == 0
     assert needle in _lib.last_error()
+
+
+def test_local_4x4_descriptor_rules(lib):
+    """diffraction 0 is the per-voxel 4x4 transfer: reflection mode 2, npass 1 only."""
+    ok = _desc(diffraction=0, reflection=2)
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(ok)) > 0
+    for kw in (dict(diffraction=0, reflection=1), dict(diffraction=0, reflection=2, npass=2),
+               dict(diffraction=1, reflection=2)):
+        assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
 
 
 def test_transfer_rejects_small_workspace(lib):
