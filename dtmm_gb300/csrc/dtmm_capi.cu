@@ -146,7 +146,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     return o;
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
-  L.small = take(sizeof(double) * (d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
+  L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
   if (d->method == 4 && d->diffraction == 0) {  // the per-voxel transfer needs the scalars only
     L.total = off;
     return L;
@@ -334,6 +334,7 @@ struct Engine {
   double* i0() const { return epseff() + 4; }
   double* i0f() const { return i0() + NI; }
   double* fact() const { return i0f() + NI; }
+  double* blim() const { return fact() + NI; }  // [lam] band limits of the W axis
 
   int launch_rows(cpx<R>* data, int C, bool inv, double scale) {
     const int nlines = NI * C * d.height;
@@ -416,6 +417,10 @@ struct Engine {
                  int j_only = -1) {
     ColParams p;
     p.ktab_ray_stride = ktab_ray_stride;
+    // the engine's diagonal tables are cut at d.betamax; the register row
+    // pass reads out-of-band columns as zero, so skipped tiles need no writes
+    p.band_skip = row_reg() ? 2 : 1;
+    p.blim = blim();
     p.j_only = j_only;
     p.cy_rows = L.ny;
     p.cin = cin;
@@ -527,6 +532,7 @@ struct Engine {
   int launch_row(const cpx<R>* Ub, cpx<R>* Xb, const void* op, double dir, int win_only = -1, bool use_cx = true,
                  bool accumulate = false) {
     RowParams p;
+    p.blim = blim();
     p.win_only = win_only;
     p.use_cx = use_cx ? 1 : 0;
     p.accumulate = accumulate ? 1 : 0;
@@ -744,6 +750,16 @@ struct Engine {
   int setup() {
     int rc = scalars();
     if (rc) return rc;
+    {  // band limits of the W axis per wavelength (host, by value)
+      for (int o = 0; o < d.nlam; o += 64) {
+        Scalars64 sc;
+        sc.n = std::min(64, d.nlam - o);
+        sc.off = o;
+        for (int i = 0; i < sc.n; ++i) sc.v[i] = (double)band_limit(d.width, d.ks[o + i], d.betamax);
+        k_set_scalars<<<1, 64, 0, st>>>(sc, blim());
+        CKL("k_set_scalars");
+      }
+    }
     // FFT tables
     k_fft_tables<R><<<(d.height + 255) / 256, 256, 0, st>>>(pH, P(L.twH), A<int>(L.permH));
     CKL("k_fft_tables");

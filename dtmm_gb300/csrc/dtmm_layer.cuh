@@ -30,6 +30,25 @@ __device__ __forceinline__ int img_ray(const Grid& g, int img) { return img / (g
 // fftfreq(n)[i] * n
 __host__ __device__ __forceinline__ int fsigned(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
 
+// |beta_x| of FFT column x is below betamax: the same expression as the
+// k-space tables' cut test at ky = 0 (the smallest beta of the column;
+// correctly rounded operations only, so host and device agree)
+__host__ __device__ inline bool in_band(int x, int n, double ks, double betamax) {
+  const double xx = (double)fsigned(x, n) * (1.0 / n);
+  return (2.0 * M_PI / fabs(ks)) * sqrt(xx * xx + 0.0 * 0.0) < betamax;
+}
+
+// largest |fsigned| index of an n-point axis inside the band (-1: none);
+// formed on the host once per wavelength
+__host__ __device__ inline int band_limit(int n, double ks, double betamax) {
+  int lim = -1;
+  for (int i = 0; i <= n / 2; ++i) {
+    if (!in_band(i, n, ks, betamax)) break;
+    lim = i;
+  }
+  return lim;
+}
+
 // ---------------------------------------------------------------------------
 // Column pass of one layer step (all along ky, a tile of columns of one
 // image): forward column FFT -> k-space operator -> for each window row j:
@@ -41,6 +60,13 @@ struct ColParams {
   int kop;                 // KOp
   size_t ktab_ray_stride;  // elements between the tables of consecutive rays (0 = shared)
   const void* ktab;        // KOP_DIAG: [lam][H][W][2]; KOP_MAT: [lam][H][W][cout][cin]
+  // band skip (register column pass, KOP_DIAG): the diagonal operator is zero
+  // for beta >= betamax, so a tile whose columns all have |beta_x| >= betamax
+  // at the image's wavelength produces zeros without any transform.
+  // 1: such tiles write zeros; 2: they write nothing (the register row pass
+  // reads those columns as zero without loading them)
+  int band_skip;
+  const double* blim;      // [lam] band limit: largest in-band |column frequency index| (-1: none)
   int ny;                  // window rows (1 = no windows)
   const void* cy;          // [ray][j][lam][H] (null = weight 1)
   int j_only;              // >= 0: emit only window row j_only (into U slot 0)
@@ -62,6 +88,7 @@ struct ColParams {
 // ---------------------------------------------------------------------------
 struct RowParams {
   int C;                 // 4 (Epn) or 2 (E)
+  const double* blim;    // [lam] band limit: columns with |frequency index| > limit read as zero
   int nx, ny;            // windows per axis (1, 1 without windows)
   const void* cx;        // [ray][i][lam][W] (null = weight 1)
   const int* wzero;      // [ray][nx*ny]

@@ -75,7 +75,11 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
   // phase scale k0 * direction of each wavelength of the block (formed once, in FP64)
   __shared__ R s_kph[kMaxRowGroup];
-  for (int g2 = threadIdx.x; g2 < G; g2 += blockDim.x) s_kph[g2] = (R)(p.ks[lam0 + g2] * p.dir);
+  __shared__ int s_lim[kMaxRowGroup];  // band limit of each wavelength (columns beyond read as zero)
+  for (int g2 = threadIdx.x; g2 < G; g2 += blockDim.x) {
+    s_kph[g2] = (R)(p.ks[lam0 + g2] * p.dir);
+    s_lim[g2] = (int)p.blim[lam0 + g2];
+  }
   const R sc = (R)p.in_scale;
   __syncthreads();
   const int line = threadIdx.x / N1, t = threadIdx.x % N1;
@@ -104,10 +108,13 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
         const cpx<R>* src = Uj + (((size_t)img * C + c) * H + y) * W;
         const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
         cpx<R> v[N2];
+        const int lim = s_lim[gl];
 #pragma unroll
         for (int m = 0; m < N2; ++m) {
-          cpx<R> a = src[t + N1 * m];
-          v[m] = cxl ? a * cxl[t + N1 * m] : a;
+          const int xk = t + N1 * m;
+          const int fx = xk < (W + 1) / 2 ? xk : W - xk;  // |fsigned(xk)|
+          cpx<R> a = fx <= lim ? src[xk] : mk<R>((R)0, (R)0);
+          v[m] = cxl ? a * cxl[xk] : a;
         }
         TS::template step1<R, true>(v, xl, 1, TWREG ? trow : nullptr, tw, t);
         __syncwarp(gm);
@@ -259,6 +266,24 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
   const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;
   const int lcc = lc / TX, lxc = lc - lcc * TX;
   const bool lin = (int)threadIdx.x < ystep * CT && x0 + lxc < W;
+  if (p.band_skip && p.kop == KOP_DIAG) {
+    const int lim = (int)p.blim[lam];
+    bool any = false;
+    for (int xc = 0; xc < TX && x0 + xc < W; ++xc) {
+      const int xk = x0 + xc;
+      any = any || (xk < (W + 1) / 2 ? xk : W - xk) <= lim;
+    }
+    if (!any) {  // the whole block leaves together
+      if (p.band_skip == 1) {
+        for (int jj = 0; jj < p.ny; ++jj) {
+          cpx<R>* udst = U + (size_t)jj * g.NI * C * H * W + ((size_t)img * C + lcc) * H * W + x0 + lxc;
+          if (lin)
+            for (int y = threadIdx.x / CT; y < H; y += ystep) udst[(size_t)y * W] = mk<R>((R)0, (R)0);
+        }
+      }
+      return;
+    }
+  }
   const cpx<R>* xsrc = X + ((size_t)img * C + lcc) * H * W + x0 + lxc;
   if (lin)
     for (int y = threadIdx.x / CT; y < H; y += ystep) tileA[y * RS + lc] = xsrc[(size_t)y * W];
