@@ -260,6 +260,7 @@ template <typename R>
 struct Engine {
   Prof* prof = nullptr;
   int launches = 0;
+  int blim_max = 1 << 30;  // largest band limit of the W axis over the wavelengths (set by setup)
   // k-space table cache of this call: (kind, thickness, medium) -> slot
   struct Slot {
     int what = -1;
@@ -521,7 +522,8 @@ struct Engine {
       rl.grid = dim3(d.height, d.nray * ngrp * npg);
       rl.st = st;
       mark(PROF_ROW);
-      const cudaError_t e = row_reg_dispatch(d.width, C, re, rl, p, g, Ub, Xb);
+      const int band = re ? row_band_pick(d.width, blim_max) : 0;
+      const cudaError_t e = row_reg_dispatch(d.width, C, re, band, rl, p, g, Ub, Xb);
       mark(PROF_ROW);
       ++launches;
       if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_row_reg: %s", cudaGetErrorString(e));
@@ -751,11 +753,16 @@ struct Engine {
     int rc = scalars();
     if (rc) return rc;
     {  // band limits of the W axis per wavelength (host, by value)
+      blim_max = -1;
       for (int o = 0; o < d.nlam; o += 64) {
         Scalars64 sc;
         sc.n = std::min(64, d.nlam - o);
         sc.off = o;
-        for (int i = 0; i < sc.n; ++i) sc.v[i] = (double)band_limit(d.width, d.ks[o + i], d.betamax);
+        for (int i = 0; i < sc.n; ++i) {
+          const int lim = band_limit(d.width, d.ks[o + i], d.betamax);
+          blim_max = std::max(blim_max, lim);
+          sc.v[i] = (double)lim;
+        }
         k_set_scalars<<<1, 64, 0, st>>>(sc, blim());
         CKL("k_set_scalars");
       }

@@ -192,6 +192,116 @@ struct RegDFTg {
 };
 
 // ---------------------------------------------------------------------------
+// DFT of an input known to be zero outside a compile-time mask (bit m set:
+// x[m] may be non-zero).  The decimation of RegDFTg is followed, but a
+// sub-transform whose inputs are all zero is left out, one with a single
+// non-zero input x[m0] becomes the rotations x[m0] W_N^(m0 k), and the
+// combining DFTs only see the sub-transforms that exist.  A band-limited
+// line (entries m < KB and m >= N - KB) costs about half the butterflies of
+// the dense transform in its first stage.  Entries outside the mask must
+// hold zeros (a dense prime-length stage still reads them).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr unsigned full_mask(int n) { return n >= 32 ? 0xffffffffu : ((1u << n) - 1u); }
+
+// entries m < kb and m >= n - kb of an n-point line
+__host__ __device__ constexpr unsigned band_mask(int n, int kb) {
+  unsigned s = 0;
+  for (int m = 0; m < n; ++m)
+    if (m < kb || m >= n - kb) s |= 1u << m;
+  return s;
+}
+
+// mask of the Q entries p + P m of a mask
+__host__ __device__ constexpr unsigned stride_mask(unsigned mask, int p, int P, int Q) {
+  unsigned s = 0;
+  for (int m = 0; m < Q; ++m)
+    if ((mask >> (p + P * m)) & 1u) s |= 1u << m;
+  return s;
+}
+
+__host__ __device__ constexpr int mask_count(unsigned m) {
+  int c = 0;
+  for (; m; m &= m - 1) ++c;
+  return c;
+}
+
+__host__ __device__ constexpr int mask_low(unsigned m) {
+  int i = 0;
+  while (!((m >> i) & 1u)) ++i;
+  return i;
+}
+
+template <typename R, int N, bool INV, unsigned MASK>
+struct RegDFTs {
+  static constexpr int P = first_radix<N>();
+  static constexpr int Q = N / P;
+
+  // which of the P sub-transforms have a non-zero input
+  __host__ __device__ static constexpr unsigned pmask() {
+    unsigned s = 0;
+    for (int p = 0; p < P; ++p)
+      if (stride_mask(MASK, p, P, Q)) s |= 1u << p;
+    return s;
+  }
+
+  template <int M0, int K>
+  __host__ __device__ static __forceinline__ void rotations(cpx<R>* v, const cpx<R> x) {
+    if constexpr (K < N) {
+      v[K] = rotc<R, (long long)M0 * K, N, INV>(x);
+      rotations<M0, K + 1>(v, x);
+    }
+  }
+
+  template <int I>
+  __host__ __device__ static __forceinline__ void subs(cpx<R> (&y)[P][Q], const cpx<R>* v) {
+    if constexpr (I < P) {
+      constexpr unsigned sm = stride_mask(MASK, I, P, Q);
+      if constexpr (sm != 0) {
+#pragma unroll
+        for (int m = 0; m < Q; ++m) y[I][m] = v[I + P * m];
+        RegDFTs<R, Q, INV, sm>::run(y[I]);
+      }
+      subs<I + 1>(y, v);
+    }
+  }
+
+  template <int K, int I>
+  __host__ __device__ static __forceinline__ void gather(cpx<R> (&t)[P], const cpx<R> (&y)[P][Q]) {
+    if constexpr (I < P) {
+      if constexpr ((pmask() >> I) & 1u)
+        t[I] = rotc<R, (long long)I * K, N, INV>(y[I][K]);
+      else
+        t[I] = mk<R>((R)0, (R)0);
+      gather<K, I + 1>(t, y);
+    }
+  }
+
+  template <int K>
+  __host__ __device__ static __forceinline__ void combine(cpx<R>* v, const cpx<R> (&y)[P][Q]) {
+    if constexpr (K < Q) {
+      cpx<R> t[P];
+      gather<K, 0>(t, y);
+      RegDFTs<R, P, INV, pmask()>::run(t);
+#pragma unroll
+      for (int r = 0; r < P; ++r) v[K + Q * r] = t[r];
+      combine<K + 1>(v, y);
+    }
+  }
+
+  __host__ __device__ static __forceinline__ void run(cpx<R>* v) {
+    if constexpr (MASK == full_mask(N) || Q == 1) {
+      RegDFTg<R, N, INV>::run(v);  // dense, or a prime length (reads the zeros)
+    } else if constexpr (mask_count(MASK) == 1) {
+      rotations<mask_low(MASK), 0>(v, v[mask_low(MASK)]);
+    } else {
+      cpx<R> y[P][Q];
+      subs<0>(y, v);
+      combine<0>(v, y);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Two-step line transform, N = N1 * N2 (see the file comment).  Exchange
 // element (k1, s) lives at xch[(k1 * N1 + (s ^ (k1 & (N1 - 1)))) * xs]: the
 // writes of one k1 (lanes s) and the reads of one k1 (entries s) both touch
@@ -215,10 +325,11 @@ struct TwoStep {
 
   // step 1: v[m] = x[t + N1 m] in; DFT over m, twiddle, write to the exchange.
   // Twiddles W_N^(t k1) come from `trow` (registers) or the lane-major table `twt`.
-  template <typename R, bool INV>
+  // MASK: the entries m that may be non-zero (the others hold zeros).
+  template <typename R, bool INV, unsigned MASK = full_mask(N2)>
   __host__ __device__ static __forceinline__ void step1(cpx<R> (&v)[N2], cpx<R>* xch, int xs, const cpx<R>* trow,
                                                         const cpx<R>* twt, int t) {
-    RegDFTg<R, N2, INV>::run(v);
+    RegDFTs<R, N2, INV, MASK>::run(v);
 #pragma unroll
     for (int k1 = 1; k1 < N2; ++k1) {
       cpx<R> w = trow ? trow[k1] : twt[k1 * N1 + t];

@@ -48,7 +48,27 @@ constexpr int kMaxRowGroup = 64;
 
 __host__ __device__ constexpr int reg_row_stride(int n1, int w) { return n1 == 4 ? w + 4 : (n1 == 8 ? w + 8 : w); }
 
-template <typename R, int C, bool REAL, int N1, int N2>
+// Band variants of the row pass.  The window rows arrive band-limited: every
+// entry with |f_x| beyond the wavelength's band limit lim is zero.  Variant
+// b > 0 loads only the entries m < KB and m >= N2 - KB of a lane (KB =
+// row_band_slots) and runs the sparse step-1 DFT; it is exact when every
+// wavelength of the launch has lim < KB N1 (the other entries then lie
+// beyond the band: t + N1 m >= N1 KB for m >= KB on the positive side,
+// W - (t + N1 m) > N1 KB for m < N2 - KB on the negative side).
+__host__ __device__ constexpr int row_band_slots(int n2, int b) {
+  return b == 0 ? 0 : ((b == 1 ? n2 / 8 : n2 / 4) > 1 ? (b == 1 ? n2 / 8 : n2 / 4) : 1);
+}
+__host__ __device__ constexpr bool row_band_ok(int n2, int b) { return b == 0 || 2 * row_band_slots(n2, b) < n2; }
+
+// the band variant of an n-point row for the largest band limit of a launch
+__host__ __device__ constexpr int row_band_pick(int n, int lim) {
+  const int n1 = reg_lanes(n), n2 = n1 > 0 ? n / n1 : 0;
+  for (int b = 1; b <= 2; ++b)
+    if (n1 > 0 && row_band_ok(n2, b) && lim < row_band_slots(n2, b) * n1) return b;
+  return 0;
+}
+
+template <typename R, int C, bool REAL, int N1, int N2, int BAND>
 __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
                                                          cpx<R>* __restrict__ X) {
   using T = typename std::conditional<REAL, R, cpx<R>>::type;
@@ -109,14 +129,20 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
         const R* cxl = (p.cx && p.use_cx) ? (const R*)p.cx + (((size_t)ray * p.nx + i) * g.nlam + lam) * W : nullptr;
         cpx<R> v[N2];
         const int lim = s_lim[gl];
+        constexpr int KB = row_band_slots(N2, BAND);
 #pragma unroll
         for (int m = 0; m < N2; ++m) {
-          const int xk = t + N1 * m;
-          const int fx = xk < (W + 1) / 2 ? xk : W - xk;  // |fsigned(xk)|
-          cpx<R> a = fx <= lim ? src[xk] : mk<R>((R)0, (R)0);
-          v[m] = cxl ? a * cxl[xk] : a;
+          if (BAND == 0 || m < KB || m >= N2 - KB) {
+            const int xk = t + N1 * m;
+            const int fx = xk < (W + 1) / 2 ? xk : W - xk;  // |fsigned(xk)|
+            cpx<R> a = fx <= lim ? src[xk] : mk<R>((R)0, (R)0);
+            v[m] = cxl ? a * cxl[xk] : a;
+          } else {
+            v[m] = mk<R>((R)0, (R)0);
+          }
         }
-        TS::template step1<R, true>(v, xl, 1, TWREG ? trow : nullptr, tw, t);
+        TS::template step1<R, true, BAND == 0 ? full_mask(N2) : band_mask(N2, KB)>(v, xl, 1, TWREG ? trow : nullptr,
+                                                                                    tw, t);
         __syncwarp(gm);
         cpx<R> u[TS::J][N1];
         TS::template step2<R, true>(u, xl, 1, t);
@@ -461,21 +487,31 @@ struct RegLaunch {
 // row variants: every (C, REAL) for power-of-two sides, real records for the others
 __host__ __device__ constexpr bool reg_row_variant(int n, bool real) { return reg_lanes(n) > 0 && (real || is_pow2(n)); }
 
-template <int N1, int N2, int C, bool REAL>
+template <int N1, int N2, int C, bool REAL, int BAND = 0>
 cudaError_t row_reg_variant(const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, void* X) {
-  auto kern = k_layer_row_reg<float, C, REAL, N1, N2>;
+  auto kern = k_layer_row_reg<float, C, REAL, N1, N2, BAND>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
   if (e != cudaSuccess) return e;
   kern<<<L.grid, L.threads, L.smem, L.st>>>(p, g, (const cpx<float>*)U, (cpx<float>*)X);
   return cudaGetLastError();
 }
 
+// real records with a band variant b (row_band_pick), every (C, REAL) dense
+template <int N1, int N2, int C>
+cudaError_t row_reg_real(int band, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, void* X) {
+  if constexpr (row_band_ok(N2, 1))
+    if (band == 1) return row_reg_variant<N1, N2, C, true, 1>(L, p, g, U, X);
+  if constexpr (row_band_ok(N2, 2))
+    if (band == 2) return row_reg_variant<N1, N2, C, true, 2>(L, p, g, U, X);
+  return row_reg_variant<N1, N2, C, true, 0>(L, p, g, U, X);
+}
+
 template <int N1, int N2>
-cudaError_t row_reg_launch(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U,
-                           void* X) {
+cudaError_t row_reg_launch(int C, bool real, int band, const RegLaunch& L, const RowParams& p, const Grid& g,
+                           const void* U, void* X) {
   constexpr int N = N1 * N2;
-  if (C == 4 && real) return row_reg_variant<N1, N2, 4, true>(L, p, g, U, X);
-  if (C == 2 && real) return row_reg_variant<N1, N2, 2, true>(L, p, g, U, X);
+  if (C == 4 && real) return row_reg_real<N1, N2, 4>(band, L, p, g, U, X);
+  if (C == 2 && real) return row_reg_real<N1, N2, 2>(band, L, p, g, U, X);
   if constexpr (is_pow2(N)) {
     if (C == 4) return row_reg_variant<N1, N2, 4, false>(L, p, g, U, X);
     if (C == 2) return row_reg_variant<N1, N2, 2, false>(L, p, g, U, X);
@@ -508,16 +544,16 @@ cudaError_t fft_rows_reg_launch(bool inv, const RegLaunch& L, const void* src, v
   X(432) X(448) X(480) X(512) X(1024)
 
 #define DTMM_REG_DECLARE(N)                                                                                      \
-  cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
-                          void* X);                                                                            \
+  cudaError_t row_reg_##N(int C, bool real, int band, const RegLaunch& L, const RowParams& p, const Grid& g,     \
+                          const void* U, void* X);                                                             \
   cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out);     \
   cudaError_t fft_rows_reg_##N(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw, \
                                float scale);
 
 #define DTMM_REG_DEFINE(N)                                                                                       \
-  cudaError_t row_reg_##N(int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, \
-                          void* X) {                                                                           \
-    return row_reg_launch<reg_lanes(N), N / reg_lanes(N)>(C, real, L, p, g, U, X);                             \
+  cudaError_t row_reg_##N(int C, bool real, int band, const RegLaunch& L, const RowParams& p, const Grid& g,     \
+                          const void* U, void* X) {                                                            \
+    return row_reg_launch<reg_lanes(N), N / reg_lanes(N)>(C, real, band, L, p, g, U, X);                       \
   }                                                                                                            \
   cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {    \
     return col_reg_launch<reg_lanes(N), N / reg_lanes(N)>(L, p, g, in, out);                                   \
@@ -530,11 +566,11 @@ cudaError_t fft_rows_reg_launch(bool inv, const RegLaunch& L, const void* src, v
 DTMM_REG_SIDES(DTMM_REG_DECLARE)
 
 // dispatch on the side (cudaErrorNotSupported for a side without a transform)
-inline cudaError_t row_reg_dispatch(int n, int C, bool real, const RegLaunch& L, const RowParams& p, const Grid& g,
-                                    const void* U, void* X) {
+inline cudaError_t row_reg_dispatch(int n, int C, bool real, int band, const RegLaunch& L, const RowParams& p,
+                                    const Grid& g, const void* U, void* X) {
   switch (n) {
 #define DTMM_REG_ROW_CASE(N) \
-  case N: return row_reg_##N(C, real, L, p, g, U, X);
+  case N: return row_reg_##N(C, real, band, L, p, g, U, X);
     DTMM_REG_SIDES(DTMM_REG_ROW_CASE)
 #undef DTMM_REG_ROW_CASE
     default: return cudaErrorNotSupported;

@@ -103,6 +103,70 @@ static void check_two_step() {
   report(INV ? "two_step_inv" : "two_step_fwd", N, rel_err(got, direct(x, INV)), 1e-13);
 }
 
+// DFT of an input that is zero outside the band mask (entries m < KB, m >= N - KB)
+template <int N, int KB, bool INV>
+static void check_sparse() {
+  constexpr unsigned M = band_mask(N, KB);
+  std::vector<C> x = input(N, 7 + INV);
+  for (int m = 0; m < N; ++m)
+    if (!((M >> m) & 1u)) x[m] = 0;
+  cpx<double> v[N];
+  for (int i = 0; i < N; ++i) v[i] = mk<double>(x[i].real(), x[i].imag());
+  RegDFTs<double, N, INV, M>::run(v);
+  std::vector<C> got(N);
+  for (int i = 0; i < N; ++i) got[i] = C(v[i].re, v[i].im);
+  report(INV ? "sparse_dft_inv" : "sparse_dft_fwd", N * 100 + KB, rel_err(got, direct(x, INV)), 1e-14);
+}
+
+template <int N>
+static void check_sparse_all() {
+  check_sparse<N, 1, false>(); check_sparse<N, 1, true>();
+  if constexpr (N > 4) { check_sparse<N, 2, false>(); check_sparse<N, 2, true>(); }
+  if constexpr (N > 8) { check_sparse<N, N / 4, false>(); check_sparse<N, N / 4, true>(); }
+  if constexpr (N > 16) { check_sparse<N, N / 8, false>(); check_sparse<N, N / 8, true>(); }
+}
+
+// two-step inverse transform of a band-limited line (|f| < KB N1) with the
+// sparse step 1, lanes loading only their band entries
+template <int N1, int N2, int KB>
+static void check_band_line() {
+  using TS = TwoStep<N1, N2>;
+  constexpr int N = N1 * N2;
+  std::vector<C> x = input(N, 11);
+  for (int k = 0; k < N; ++k) {
+    const int f = k < (N + 1) / 2 ? k : N - k;
+    if (f >= KB * N1) x[k] = 0;
+  }
+  std::vector<cpx<double>> xch(N), out(N), tw(N), twt(N);
+  for (int e = 0; e < N; ++e) {
+    const double a = -2.0 * M_PI * e / N;
+    tw[e] = mk<double>(std::cos(a), std::sin(a));
+  }
+  for (int e = 0; e < N; ++e) twt[e] = TS::twiddle_entry(tw.data(), e);
+  for (int t = 0; t < N1; ++t) {
+    cpx<double> v[N2];
+    for (int m = 0; m < N2; ++m)
+      v[m] = (m < KB || m >= N2 - KB) ? mk<double>(x[t + N1 * m].real(), x[t + N1 * m].imag()) : mk<double>(0, 0);
+    TS::template step1<double, true, band_mask(N2, KB)>(v, xch.data(), 1, nullptr, twt.data(), t);
+  }
+  for (int t = 0; t < N1; ++t) {
+    cpx<double> u[TS::J][N1];
+    TS::template step2<double, true>(u, xch.data(), 1, t);
+    TS::template store<double>(u, out.data(), 1, t, 1.0);
+  }
+  std::vector<C> got(N);
+  for (int i = 0; i < N; ++i) got[i] = C(out[i].re, out[i].im);
+  report("band_line_inv", N * 100 + KB, rel_err(got, direct(x, true)), 1e-13);
+}
+
+template <int N>
+static void check_band() {
+  constexpr int N1 = reg_lanes(N), N2 = N / N1;
+  constexpr int K1 = N2 / 8 > 1 ? N2 / 8 : 1, K2 = N2 / 4 > 1 ? N2 / 4 : 1;
+  if constexpr (2 * K1 < N2) check_band_line<N1, N2, K1>();
+  if constexpr (2 * K2 < N2) check_band_line<N1, N2, K2>();
+}
+
 template <int N>
 static void check_line() {
   constexpr int N1 = reg_lanes(N);
@@ -133,6 +197,16 @@ int main() {
   check_line<256>(); check_line<288>(); check_line<320>(); check_line<336>(); check_line<384>();
   check_line<400>(); check_line<432>(); check_line<448>(); check_line<480>(); check_line<512>();
   check_line<1024>();
+  check_sparse_all<4>(); check_sparse_all<5>(); check_sparse_all<6>(); check_sparse_all<7>();
+  check_sparse_all<8>(); check_sparse_all<9>(); check_sparse_all<10>(); check_sparse_all<12>();
+  check_sparse_all<14>(); check_sparse_all<15>(); check_sparse_all<16>(); check_sparse_all<18>();
+  check_sparse_all<20>(); check_sparse_all<21>(); check_sparse_all<24>(); check_sparse_all<25>();
+  check_sparse_all<27>(); check_sparse_all<28>(); check_sparse_all<30>(); check_sparse_all<32>();
+  check_band<64>(); check_band<80>(); check_band<96>(); check_band<112>(); check_band<128>();
+  check_band<144>(); check_band<160>(); check_band<192>(); check_band<224>(); check_band<240>();
+  check_band<256>(); check_band<288>(); check_band<320>(); check_band<336>(); check_band<384>();
+  check_band<400>(); check_band<432>(); check_band<448>(); check_band<480>(); check_band<512>();
+  check_band<1024>();
   std::printf(g_worst == 0.0 ? "OK\n" : "FAILED\n");
   return g_worst == 0.0 ? 0 : 1;
 }

@@ -6,7 +6,9 @@ in-register DFTs of 2..32 points and the two-step transform of every line
 length that has one (lanes executed one after another, the lane barrier
 between the steps) in complex128, and compares them with a direct DFT:
 twiddles within 4e-16 of a long-double reference, transforms within 1e-13
-relative L2.
+relative L2.  Sparse-input DFTs (entries outside a band mask known to be
+zero) and the band variants of the two-step inverse transform used by the
+row pass are checked the same way.
 """
 import os
 import subprocess
@@ -34,3 +36,6 @@ def test_register_transforms_on_host(tmp_path):
     assert lines[-1] == "OK"
     sizes = {int(l.split()[2]) for l in lines if l.startswith("max_err two_step_fwd")}
     assert {80, 96, 144, 240, 336, 480, 512, 1024} <= sizes
+    band = {int(l.split()[2]) // 100 for l in lines if l.startswith("max_err band_line_inv")}
+    assert {64, 256, 512, 1024} <= band
+    assert any(l.startswith("max_err sparse_dft_fwd") for l in lines)
