@@ -260,7 +260,8 @@ template <typename R>
 struct Engine {
   Prof* prof = nullptr;
   int launches = 0;
-  int blim_max = 1 << 30;  // largest band limit of the W axis over the wavelengths (set by setup)
+  int blim_max = 1 << 30;   // largest band limit of the W axis over the wavelengths (set by setup)
+  int blimH_max = 1 << 30;  // the same for the H axis
   // k-space table cache of this call: (kind, thickness, medium) -> slot
   struct Slot {
     int what = -1;
@@ -405,7 +406,9 @@ struct Engine {
       rl.grid = dim3((d.width + tx - 1) / tx, NI);
       rl.st = st;
       mark(PROF_COL);
-      const cudaError_t e = col_reg_dispatch(d.height, rl, p, g, in, out);
+      // the diagonal table is cut at betamax: band variants of the inverse transforms
+      const int band = p.kop == KOP_DIAG ? row_band_pick(d.height, blimH_max) : 0;
+      const cudaError_t e = col_reg_dispatch(d.height, band, rl, p, g, in, out);
       mark(PROF_COL);
       ++launches;
       if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_col_reg: %s", cudaGetErrorString(e));
@@ -754,6 +757,8 @@ struct Engine {
     if (rc) return rc;
     {  // band limits of the W axis per wavelength (host, by value)
       blim_max = -1;
+      blimH_max = -1;
+      for (int i = 0; i < d.nlam; ++i) blimH_max = std::max(blimH_max, band_limit(d.height, d.ks[i], d.betamax));
       for (int o = 0; o < d.nlam; o += 64) {
         Scalars64 sc;
         sc.n = std::min(64, d.nlam - o);
@@ -1285,7 +1290,7 @@ int diffract_impl(int H, int W, int nimg, int nlam, const void* dmat, const void
     cl.threads = std::max(32, ((4 * tx * n1 + 31) / 32) * 32);
     cl.grid = dim3((W + tx - 1) / tx, nimg);
     cl.st = st;
-    const cudaError_t e = col_reg_dispatch(H, cl, p, g, X, out);
+    const cudaError_t e = col_reg_dispatch(H, 0, cl, p, g, X, out);
     ++launches;
     if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_col_reg: %s", cudaGetErrorString(e));
   } else {

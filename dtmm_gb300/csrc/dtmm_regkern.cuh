@@ -270,8 +270,12 @@ __host__ __device__ constexpr bool reg_even(int n) { return reg_lanes(n) > 0 && 
 __host__ __device__ constexpr int reg_col_tiles(int n, int ny) { return (!reg_even(n) && ny > 1) ? 2 : 1; }
 
 // Column pass, k-space operator KOP_NONE, KOP_DIAG or KOP_MAT (C x C per k,
-// exchanged through the tile; see the file comment).
-template <typename R, int N1, int N2>
+// exchanged through the tile; see the file comment).  BAND > 0 (KOP_DIAG
+// only, N2 % N1 == 0): the diagonal table is zero beyond betamax, so after it
+// a lane's spectrum entries outside m < KB, m >= N2 - KB are exact zeros
+// whenever the H axis's band limit is below KB N1; the window-row inverse
+// transforms then weight only those entries and run the sparse step 1.
+template <typename R, int N1, int N2, int BAND>
 __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, const cpx<R>* __restrict__ X,
                                                          cpx<R>* __restrict__ U) {
   using TS = TwoStep<N1, N2>;
@@ -374,11 +378,17 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
       __syncthreads();  // the previous window's stores (and the forward exchange) are done with the tile
       if (active) {
         const R* cyj = p.cy ? (const R*)p.cy + (((size_t)ray * p.cy_rows + j) * g.nlam + lam) * H : nullptr;
+        constexpr int KB = row_band_slots(N2, BAND);
         cpx<R> w[N2];
 #pragma unroll
-        for (int m = 0; m < N2; ++m) w[m] = cyj ? v[m] * cyj[t + N1 * m] : v[m];
+        for (int m = 0; m < N2; ++m) {
+          if (BAND == 0 || m < KB || m >= N2 - KB)
+            w[m] = cyj ? v[m] * cyj[t + N1 * m] : v[m];
+          else
+            w[m] = mk<R>((R)0, (R)0);
+        }
         if (p.inverse_out) {
-          TS::template step1<R, true>(w, colA, RS, nullptr, tw, t);
+          TS::template step1<R, true, BAND == 0 ? full_mask(N2) : band_mask(N2, KB)>(w, colA, RS, nullptr, tw, t);
           __syncwarp(gm);
           cpx<R> u[TS::J][N1];
           TS::template step2<R, true>(u, colA, RS, t);
@@ -519,13 +529,26 @@ cudaError_t row_reg_launch(int C, bool real, int band, const RegLaunch& L, const
   return cudaErrorNotSupported;
 }
 
-template <int N1, int N2>
-cudaError_t col_reg_launch(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {
-  auto kern = k_layer_col_reg<float, N1, N2>;
+template <int N1, int N2, int BAND>
+cudaError_t col_reg_variant(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {
+  auto kern = k_layer_col_reg<float, N1, N2, BAND>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
   if (e != cudaSuccess) return e;
   kern<<<L.grid, L.threads, L.smem, L.st>>>(p, g, (const cpx<float>*)in, (cpx<float>*)out);
   return cudaGetLastError();
+}
+
+// band variants (row_band_pick of the H axis) for the diagonal operator of
+// sides with N2 % N1 == 0; the caller passes band 0 for any other operator
+template <int N1, int N2>
+cudaError_t col_reg_launch(int band, const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {
+  if constexpr (N2 % N1 == 0) {
+    if constexpr (row_band_ok(N2, 1))
+      if (band == 1) return col_reg_variant<N1, N2, 1>(L, p, g, in, out);
+    if constexpr (row_band_ok(N2, 2))
+      if (band == 2) return col_reg_variant<N1, N2, 2>(L, p, g, in, out);
+  }
+  return col_reg_variant<N1, N2, 0>(L, p, g, in, out);
 }
 
 template <int N1, int N2>
@@ -546,7 +569,8 @@ cudaError_t fft_rows_reg_launch(bool inv, const RegLaunch& L, const void* src, v
 #define DTMM_REG_DECLARE(N)                                                                                      \
   cudaError_t row_reg_##N(int C, bool real, int band, const RegLaunch& L, const RowParams& p, const Grid& g,     \
                           const void* U, void* X);                                                             \
-  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out);     \
+  cudaError_t col_reg_##N(int band, const RegLaunch& L, const ColParams& p, const Grid& g, const void* in,       \
+                          void* out);                                                                          \
   cudaError_t fft_rows_reg_##N(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw, \
                                float scale);
 
@@ -555,8 +579,9 @@ cudaError_t fft_rows_reg_launch(bool inv, const RegLaunch& L, const void* src, v
                           const void* U, void* X) {                                                            \
     return row_reg_launch<reg_lanes(N), N / reg_lanes(N)>(C, real, band, L, p, g, U, X);                       \
   }                                                                                                            \
-  cudaError_t col_reg_##N(const RegLaunch& L, const ColParams& p, const Grid& g, const void* in, void* out) {    \
-    return col_reg_launch<reg_lanes(N), N / reg_lanes(N)>(L, p, g, in, out);                                   \
+  cudaError_t col_reg_##N(int band, const RegLaunch& L, const ColParams& p, const Grid& g, const void* in,       \
+                          void* out) {                                                                         \
+    return col_reg_launch<reg_lanes(N), N / reg_lanes(N)>(band, L, p, g, in, out);                             \
   }                                                                                                            \
   cudaError_t fft_rows_reg_##N(bool inv, const RegLaunch& L, const void* src, void* dst, int nlines, const void* tw, \
                                float scale) {                                                                  \
@@ -577,11 +602,11 @@ inline cudaError_t row_reg_dispatch(int n, int C, bool real, int band, const Reg
   }
 }
 
-inline cudaError_t col_reg_dispatch(int n, const RegLaunch& L, const ColParams& p, const Grid& g, const void* in,
-                                    void* out) {
+inline cudaError_t col_reg_dispatch(int n, int band, const RegLaunch& L, const ColParams& p, const Grid& g,
+                                    const void* in, void* out) {
   switch (n) {
 #define DTMM_REG_COL_CASE(N) \
-  case N: return col_reg_##N(L, p, g, in, out);
+  case N: return col_reg_##N(band, L, p, g, in, out);
     DTMM_REG_SIDES(DTMM_REG_COL_CASE)
 #undef DTMM_REG_COL_CASE
     default: return cudaErrorNotSupported;
