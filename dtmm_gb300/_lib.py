@@ -25,7 +25,7 @@ ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_s
                "dtmm_diffract_workspace_size", "dtmm_diffract", "dtmm_q2data", "dtmm_wave_field",
                "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields",
                "dtmm_twisted_nematic_angles")
-ABI_VERSION = 2
+ABI_VERSION = 3
 STATIC_SCRATCH_BYTES = 64 << 20
 
 
@@ -61,6 +61,7 @@ class TransferDesc(ctypes.Structure):
         ("row_group", ctypes.c_int),
         ("col_tile", ctypes.c_int),
         ("fft_schedule", ctypes.c_int),
+        ("biaxial", ctypes.c_int),
     ]
 
 

@@ -452,7 +452,7 @@ struct Engine {
     return DTMM_OK;
   }
 
-  bool real_ops() const { return d.real_path && !d.eps_complex; }
+  bool real_ops() const { return d.real_path && !d.eps_complex && !d.biaxial; }
   // one real eps for every voxel: the real-path solve's window constants are tables
   bool uniform_real() const {
     return real_ops() && d.epsv_strides[0] == 0 && d.epsv_strides[1] == 0 && d.epsv_strides[2] == 0;
@@ -684,14 +684,19 @@ struct Engine {
     p.wc2 = wc2();
     if (real_ops()) {
       if (p.four)
-        k_voxel_op<R, true, true><<<grid, 128, 0, s>>>(p, g, op);
+        k_voxel_op<R, true, true, false><<<grid, 128, 0, s>>>(p, g, op);
       else
-        k_voxel_op<R, true, false><<<grid, 128, 0, s>>>(p, g, op);
+        k_voxel_op<R, true, false, false><<<grid, 128, 0, s>>>(p, g, op);
+    } else if (d.biaxial) {
+      if (p.four)
+        k_voxel_op<R, false, true, true><<<grid, 128, 0, s>>>(p, g, op);
+      else
+        k_voxel_op<R, false, false, true><<<grid, 128, 0, s>>>(p, g, op);
     } else {
       if (p.four)
-        k_voxel_op<R, false, true><<<grid, 128, 0, s>>>(p, g, op);
+        k_voxel_op<R, false, true, false><<<grid, 128, 0, s>>>(p, g, op);
       else
-        k_voxel_op<R, false, false><<<grid, 128, 0, s>>>(p, g, op);
+        k_voxel_op<R, false, false, false><<<grid, 128, 0, s>>>(p, g, op);
     }
     mark_on(PROF_OP, s);
     CKL("k_voxel_op");
@@ -1407,7 +1412,7 @@ std::string& last_error_slot() { return g_err; }
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 2; }
+int dtmm_abi_version(void) { return 3; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 

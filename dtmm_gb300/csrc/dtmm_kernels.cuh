@@ -10,6 +10,7 @@
 #include <type_traits>
 
 #include "dtmm_common.cuh"
+#include "dtmm_eig4.cuh"
 #include "dtmm_layer.cuh"
 
 namespace dtmm {
@@ -169,6 +170,14 @@ __device__ inline void voxel_inv(const double* e, double theta, VoxelInv& vi) {
   vi.kw = delta * (vi.st * vi.st);
 }
 
+// The biaxial solve with the angles of the voxel and the beam
+__device__ __forceinline__ void biaxial_fmat_call(double beta, const cpx<double>* ev, double psi, double ct, double st,
+                                               double cf, double sf, cpx<double> (*F)[4], cpx<double>* al) {
+  double sps, cps;
+  sincos(psi, &sps, &cps);
+  biaxial_fmat(beta, ev, cps, sps, ct, st, cf, sf, F, al);
+}
+
 // Uniaxial / isotropic E rows (Ex, Ey of the four modes) and eigenvalues in
 // real FP64 arithmetic (dtmm/tmm.py:157-278), valid when every eigenvalue
 // and the effective medium exceed beta^2 (the host proves this before
@@ -223,7 +232,10 @@ __device__ __forceinline__ bool voxel_E_real(double beta, const VoxelInv& vi, do
   return false;
 }
 
-template <typename R, bool REAL, bool FOUR>
+// BIAX: the material holds biaxial voxels, which take the general
+// eigen-solve (complex path only; without BIAX every voxel is isotropic or
+// uniaxial and the kernel keeps the registers of those closed forms)
+template <typename R, bool REAL, bool FOUR, bool BIAX>
 __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int HW = g.H * g.W;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -341,6 +353,15 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     E[0][1] = h; E[1][1] = z0;
     E[0][2] = z0; E[1][2] = h;
     E[0][3] = z0; E[1][3] = h;
+  } else if (BIAX && (ev[0].re != ev[1].re || ev[0].im != ev[1].im)) {
+    // biaxial: general eigen-solve and Poynting sort (dtmm/tmm.py:395-401);
+    // a failed sort gives a zero F and so a zero operator
+    cpx<double> F[4][4];
+    biaxial_fmat_call(beta, ev, p.epsa[ao], ct, st, cfw, sfw, F, al);
+    for (int m = 0; m < 4; ++m) {
+      E[0][m] = F[0][m];
+      E[1][m] = F[2][m];
+    }
   } else {
     // uniaxial, optic axis rotated by (theta, azimuth - phi) (dtmm/tmm.py:157-278,
     // rotation dtmm/rotation.py:176-194 via :390)
@@ -446,8 +467,8 @@ struct Local4Params {
   const double* phi;  // [ray]
 };
 
-// field matrix and eigenvalues of one voxel (isotropic or uniaxial)
-__device__ void local_fmat(double beta, double phi, const cpx<double> ev[3], double theta, double azim,
+// field matrix and eigenvalues of one voxel (isotropic, uniaxial or biaxial)
+__device__ void local_fmat(double beta, double phi, const cpx<double> ev[3], double psi, double theta, double azim,
                            cpx<double> F[4][4], cpx<double> al[4]) {
   const cpx<double> z0 = mk<double>(0.0, 0.0);
   for (int i = 0; i < 4; ++i) {
@@ -502,7 +523,10 @@ __device__ void local_fmat(double beta, double phi, const cpx<double> ev[3], dou
     }
     al[0] = evpp; al[1] = evpm; al[2] = evs; al[3] = -evs;
   } else {
-    return;  // biaxial voxels are refused by the host before the call
+    double st, ct, sf, cf;
+    sincos(theta, &st, &ct);
+    sincos(azim - phi, &sf, &cf);
+    biaxial_fmat_call(beta, ev, psi, ct, st, cf, sf, F, al);
   }
   // rotate the field rows (Ex, Hy, Ey, Hx) back by phi
   double s, c;
@@ -549,7 +573,7 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
     ev[0] = mk<double>(e[0], 0.0); ev[1] = mk<double>(e[1], 0.0); ev[2] = mk<double>(e[2], 0.0);
   }
   cpx<double> F[4][4], al[4], Fi[4][4];
-  local_fmat(p.beta[ray], p.phi[ray], ev, p.epsa[ao + 1], p.epsa[ao + 2], F, al);
+  local_fmat(p.beta[ray], p.phi[ray], ev, p.epsa[ao], p.epsa[ao + 1], p.epsa[ao + 2], F, al);
   inv4(F, Fi);
   cpx<R> f[4][4], fi[4][4];
   for (int i = 0; i < 4; ++i)

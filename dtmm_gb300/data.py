@@ -132,14 +132,18 @@ def device_material(director, shape=None, mask=None, no=1.5, ne=1.6, nhost=None,
     return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape)
 
 
-def q_material(tensor, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, thickness=None):
-    """Uniaxial ``Q2data`` kept on the device as a ``DeviceMaterial`` for ``plan_transfer``."""
+def q_material(tensor, shape=None, mask=None, no=1.5, ne=1.6, nhost=None, scale_factor=1.0, thickness=None,
+               biaxial=False):
+    """``Q2data`` kept on the device as a ``DeviceMaterial`` for ``plan_transfer``
+    (``biaxial=True`` keeps the three eigenvalues; the transfer then takes the
+    general eigen-solve)."""
     from .transfer import DeviceMaterial
 
-    epsv, epsa, _, _ = _q_run(tensor, mask, no, ne, nhost, scale_factor, False)
+    epsv, epsa, _, _ = _q_run(tensor, mask, no, ne, nhost, scale_factor, biaxial)
     nl = epsv.shape[0]
     th = np.ones((nl,)) if thickness is None else np.asarray(thickness, np.float64)
-    return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape, uniaxial=True)
+    return DeviceMaterial(th, epsv, epsa, tuple(epsv.shape[1:3]) if shape is None else shape,
+                          uniaxial=not biaxial)
 
 
 __all__ = ["director2data", "director2angles", "Q2data", "device_material", "q_material"]

@@ -178,9 +178,8 @@ class _Material:
         # no host copies of arrays that already have the engine's dtype and layout
         ev = np.require(ev, np.complex128 if self.eps_complex else np.float64, ("C", "W"))
         flat = ev.reshape(-1, 3)
-        if not np.all(flat[:, 0] == flat[:, 1]):
-            raise NotImplementedError(
-                "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
+        # biaxial voxels take the general eigen-solve (complex FP64 path)
+        self.biaxial = not bool(np.all(flat[:, 0] == flat[:, 1]))
         self.eps_min = float(np.min(ev)) if not self.eps_complex else None
         self.epsv = torch.from_numpy(ev).to(device)
         self.epsa = torch.from_numpy(np.require(ea, np.float64, ("C", "W"))).to(device)
@@ -199,9 +198,10 @@ class DeviceMaterial:
     """
 
     def __init__(self, thickness, epsv, epsa, shape, eps_min=None, uniaxial=None):
-        """``eps_min`` (smallest real eps) and ``uniaxial=True`` may be given
-        by a caller that knows them, which skips the device reductions (and
-        their host synchronisation) that would otherwise establish them."""
+        """``eps_min`` (smallest real eps) and ``uniaxial=True`` (no biaxial
+        voxel) may be given by a caller that knows them, which skips the
+        device reductions (and their host synchronisation) that would
+        otherwise establish them."""
         import torch
 
         self.thickness = np.asarray(thickness, np.float64).reshape(-1)
@@ -217,9 +217,7 @@ class DeviceMaterial:
         self.ev_strides = tuple(int(x) for x in ev.stride()[:3])
         self.ea_strides = tuple(int(x) for x in ea.stride()[:3])
         self.eps_complex = bool(ev.is_complex())
-        if not uniaxial and not bool(torch.all(epsv[..., 0] == epsv[..., 1])):
-            raise NotImplementedError(
-                "biaxial voxels (eps[0] != eps[1]) are not supported by the GPU engine")
+        self.biaxial = False if uniaxial else not bool(torch.all(epsv[..., 0] == epsv[..., 1]))
         if self.eps_complex:
             self.eps_min = None
         else:
@@ -278,9 +276,11 @@ class DevicePlan:
         d.phi = k["phi"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         d.op_cache_bytes = 0
         # real-arithmetic eigen-solve when every radicand is provably positive:
-        # real eps with all eigenvalues above the largest beam beta squared
+        # real uniaxial / isotropic eps with all eigenvalues above the largest
+        # beam beta squared (biaxial voxels need the general complex solve)
         bmax = max(float(betamax), float(np.max(np.abs(k["beta"]))))
-        d.real_path = int(mat.eps_min is not None and mat.eps_min > bmax * bmax)
+        d.real_path = int(mat.eps_min is not None and not mat.biaxial and mat.eps_min > bmax * bmax)
+        d.biaxial = int(mat.biaxial)
         self.desc = d
         self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))

@@ -79,6 +79,11 @@ typedef struct dtmm_transfer_desc {
   int row_group;
   int col_tile;
   int fft_schedule;
+  /* 1: some voxels are biaxial (eps[0] != eps[1]); their eigen-modes come
+     from the general 4 x 4 eigen-solve and Poynting sort (dtmm/tmm.py:395-401)
+     and real_path is ignored.  0: the caller guarantees eps[0] == eps[1] for
+     every voxel (isotropic / uniaxial closed forms only). */
+  int biaxial;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -106,7 +111,8 @@ typedef struct dtmm_kernel_times {
   int total_launches;      /* every kernel launched by the call                                          */
 } dtmm_kernel_times;
 
-/* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation). */
+/* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
+   3: the biaxial field of dtmm_transfer_desc). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

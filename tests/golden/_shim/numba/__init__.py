@@ -119,6 +119,17 @@ def _parse_layout(layout):
     return group(ins), group(outs)
 
 
+class _AnyLayout(np.ndarray):
+    """A core argument of a guvectorize kernel.  The reference declares every
+    core argument with an any-layout array type (``[:]``, ``[:,:]``), and
+    numba's ``ravel`` of such an array is ``flatten`` -- a copy (only arrays
+    typed C-contiguous ravel to a view).  numpy would return a view of a
+    contiguous core slice, so the stand-in copies here, as numba does."""
+
+    def ravel(self, order="C"):
+        return np.array(self, copy=True).reshape(-1)
+
+
 def guvectorize(signatures, layout, **kwargs):
     core_in, core_out = _parse_layout(layout)
     nin = len(core_in)
@@ -168,8 +179,9 @@ def guvectorize(signatures, layout, **kwargs):
             bouts = [np.broadcast_to(o, lshape + o.shape[o.ndim - len(c):]) if o.shape[: o.ndim - len(c)] != lshape else o
                      for o, c in zip(out, core_out)]
             for idx in np.ndindex(*lshape):
-                iv = [a[idx] if len(c) else a[idx].reshape(1) for a, c in zip(barrs, core_in)]
-                ov = [o[idx] if len(c) else o.reshape(o.shape + (1,))[idx] for o, c in zip(bouts, core_out)]
+                iv = [(a[idx] if len(c) else a[idx].reshape(1)).view(_AnyLayout) for a, c in zip(barrs, core_in)]
+                ov = [(o[idx] if len(c) else o.reshape(o.shape + (1,))[idx]).view(_AnyLayout)
+                      for o, c in zip(bouts, core_out)]
                 func(*iv, *ov)
             return out[0] if len(out) == 1 else out
 

@@ -33,8 +33,24 @@ def _mixed_voxels(shape, nlayers, seed):
     return d, epsv, epsa
 
 
+def _biaxial(shape, nlayers, seed, absorbing=False):
+    """Biaxial voxels (three distinct eigenvalues, a seeded psi per voxel) with
+    uniaxial and isotropic voxels among them, on a twisted director."""
+    d, _, epsa = samples.twisted_nematic(shape, nlayers, seed=seed, amplitude=0.3)
+    epsa = np.array(epsa)
+    rng = np.random.Generator(np.random.PCG64(seed + 5))
+    epsa[..., 0] = rng.uniform(-np.pi, np.pi, size=epsa.shape[:-1])
+    epsv = np.empty(epsa.shape, np.complex128 if absorbing else np.float64)
+    epsv[...] = (2.25 + 0.03j, 2.42 + 0.01j, 2.89 + 0.05j) if absorbing else (2.25, 2.42, 2.89)
+    kind = rng.integers(0, 5, size=epsv.shape[:-1])
+    epsv[kind == 0] = (2.3, 2.3, 2.7)
+    epsv[kind == 1] = (2.35, 2.35, 2.35)
+    return d, epsv, epsa
+
+
 MATERIALS = {
     "twisted": _twisted,
+    "biaxial": _biaxial,
     "inplane": lambda shape, nlayers, seed, **kw: samples.inplane_nematic(shape, nlayers, seed=seed, **kw),
     "absorbing": _absorbing,
     "mixed": _mixed_voxels,
@@ -133,6 +149,27 @@ CASES = {
                                 illum=dict(beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0], jones=(1, 0)),
                                 transfer=dict(method="4x4", diffraction=0, multiray=True,
                                               beta=[0.0, 0.1, 0.2], phi=[0.0, np.pi / 2, 0.0])),
+    # biaxial voxels (the general eigen-solve and Poynting sort of dtmm/tmm.py:395-401)
+    "fourx4_biaxial": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                           material=("biaxial", dict()), seed=23,
+                           illum=dict(beta=0.1, phi=0.5, jones=(1, 0)),
+                           transfer=dict(method="4x4", diffraction=1, beta=0.1, phi=0.5)),
+    "fourx4_biaxial_d3_npass2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                     material=("biaxial", dict()), seed=24,
+                                     illum=dict(),
+                                     transfer=dict(method="4x4", diffraction=3, npass=2, beta=0.0, phi=0.0)),
+    "fourx4_biaxial_absorbing": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                     material=("biaxial", dict(absorbing=True)), seed=25,
+                                     illum=dict(beta=0.05, jones=(0, 1)),
+                                     transfer=dict(method="4x4", diffraction=1, beta=0.05, phi=0.0)),
+    "twox2_biaxial": dict(shape=(12, 16), nlayers=3, wavelengths=[550.0, 650.0], pixelsize=100.0,
+                          material=("biaxial", dict()), seed=26,
+                          illum=dict(beta=0.1, phi=1.1),
+                          transfer=dict(method="2x2", diffraction=1, beta=0.1, phi=1.1)),
+    "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                               material=("biaxial", dict()), seed=27,
+                               illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),
+                               transfer=dict(method="4x4", diffraction=0, beta=0.15, phi=0.4)),
 }
 
 

@@ -235,6 +235,25 @@ def save_tcmf(dtmm):
     print("tcmf                   %d cases" % len(TCMF_CASES))
 
 
+def save_alphaf_biaxial_kat(dtmm):
+    """Reference alphaf / inv on random biaxial voxels (general eigen-solve and
+    Poynting sort), lossless and absorbing, both beta branches."""
+    rng = np.random.Generator(np.random.PCG64(4321))
+    n = 64
+    beta = rng.uniform(0.0, 0.8, n)
+    beta[:8] = 0.0
+    phi = rng.uniform(-np.pi, np.pi, n)
+    e0 = rng.uniform(1.9, 2.6, n)
+    epsv = np.stack([e0, e0 + rng.uniform(0.05, 0.4, n), e0 + rng.uniform(0.5, 0.9, n)], axis=-1).astype(np.complex128)
+    epsv[16:28] = epsv[16:28] + rng.uniform(0.0, 0.05, (12, 3)) * 1j
+    epsa = np.stack([rng.uniform(-np.pi, np.pi, n), rng.uniform(0, np.pi, n), rng.uniform(-np.pi, np.pi, n)], axis=-1)
+    alpha, f = dtmm.tmm.alphaf(beta, phi, epsv, epsa)
+    fi = dtmm.linalg.inv(f)
+    np.savez_compressed(os.path.join(HERE, "kat_alphaf_biaxial.npz"), beta=beta, phi=phi, epsv=epsv, epsa=epsa,
+                        alpha=alpha, f=f, fi=fi)
+    print("kat_alphaf_biaxial     %d voxels" % n)
+
+
 def main(argv):
     import refload
 
@@ -245,6 +264,7 @@ def main(argv):
         if name == "kat":
             save_wave_kat(dtmm)
             save_alphaf_kat(dtmm)
+            save_alphaf_biaxial_kat(dtmm)
         elif name == "illum":
             save_illum(dtmm)
         elif name == "pom":

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 3
 
 
 def _desc(**kw):

@@ -145,3 +145,31 @@ def test_transfer_through_q_material():
     ref = O.transfer_field((fd[0].copy(), fd[1], fd[2]), od, **opts)[0]
     got = fout.cpu().numpy()
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-10
+
+
+@pytest.mark.parametrize("diffraction", [0, 1])
+def test_transfer_through_biaxial_q_material(diffraction):
+    """Biaxial Q2data kept on the device, through the general eigen-solve of
+    the transfer, against the oracle on the oracle's own biaxial block (c128,
+    1e-10; layer 1 of the fixture holds biaxial tensors)."""
+    import torch
+
+    import dtmm_oracle as O
+    from dtmm_gb300 import data, illumination_data
+    from dtmm_gb300.transfer import plan_transfer
+
+    z = np.load(os.path.join(HERE, "golden", "qtensor.npz"))
+    q = np.ascontiguousarray(np.repeat(z["Q"], 2, axis=2)[:, :, :12])
+    fd = illumination_data((6, 12), [510.0, 600.0], pixelsize=70.0, beta=0.1, phi=0.3)
+    mat = data.q_material(torch.from_numpy(q).cuda(), no=1.5, ne=1.65, biaxial=True)
+    assert mat.biaxial
+    opts = dict(method="4x4", diffraction=diffraction, beta=0.1, phi=0.3)
+    plan = plan_transfer(fd[0].shape, fd[1], fd[2], mat, precision="double", **opts)
+    fin = torch.from_numpy(fd[0]).cuda()
+    fout = torch.empty_like(fin)
+    plan.run(fin, fout)
+    torch.cuda.synchronize()
+    od = [O.Q2data(q, no=1.5, ne=1.65, biaxial=True)]
+    ref = O.transfer_field((fd[0].copy(), fd[1], fd[2]), od, **opts)[0]
+    got = fout.cpu().numpy()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-10

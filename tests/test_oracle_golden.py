@@ -30,6 +30,19 @@ def test_oracle_matches_reference_transfer(name, golden):
     assert rel_l2(field_in, z["field_in_after"]) < GOLDEN_TOL
 
 
+def test_oracle_alphaf_biaxial_matches_reference(golden):
+    """Biaxial voxels: the general eigen-solve and the Poynting sort give the
+    reference's eigenvalues and field matrices (both call LAPACK; the rotated
+    tensor is formed in a different operation order, which moves the
+    eigenvectors of the closer eigenvalue pairs by up to a few 1e-13)."""
+    z = golden("kat_alphaf_biaxial")
+    alpha, f = O.alphaf(z["beta"], z["phi"], z["epsv"], z["epsa"])
+    assert np.all(np.isfinite(z["alpha"]))
+    assert np.abs(alpha - z["alpha"]).max() < 1e-13
+    assert np.abs(f - z["f"]).max() < 1e-11
+    assert np.abs(O.inv(f) - z["fi"]).max() < 1e-11
+
+
 def test_oracle_wave_known_answers(golden):
     z = golden("kat_wave")
     shape = tuple(int(s) for s in z["shape"])
