@@ -18,6 +18,7 @@ DTMM_ENOTSUP = -4
 
 PRECISION_MIXED = 0
 PRECISION_DOUBLE = 1
+DIFFRACTION_FULL = -1  # diffraction = inf
 
 ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_size", "dtmm_transfer",
                "dtmm_transfer_timed", "dtmm_transfer_noalloc", "dtmm_planewave_field", "dtmm_pom_field",

@@ -88,6 +88,7 @@ struct Layout {
   size_t slots, slot_bytes, dslots, dslot_bytes;
   int nslots, ndslots;
   size_t F, X, U, field0, op, Xw, Xa;
+  size_t fbeta, fphi, fmodes;  // diffraction = inf: per-wavelength grid beta / phi, sorted modes + counts
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -99,13 +100,21 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->height > 16384 || d->width > 16384) return fail(DTMM_ENOTSUP, "grid side above 16384");
   if (d->nlam < 1 || d->npol < 1 || d->nray < 1) return fail(DTMM_EINVAL, "empty image axes");
   if (d->method != 4 && d->method != 2) return fail(DTMM_EINVAL, "method must be 4 (4x4) or 2 (2x2)");
-  // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1)
+  // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1);
+  // diffraction = inf (DTMM_DIFFRACTION_FULL): every eigenwave exactly (4x4, npass 1,
+  // any reflection mode: the reference takes the same path for all of them)
   const bool local4 = d->method == 4 && d->diffraction == 0 && d->reflection == 2;
-  if (d->diffraction < 0 || (d->diffraction < 1 && !local4))
-    return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2)");
-  if (d->method == 4 && d->reflection != 1 && !local4)
+  const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
+  if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
+    return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
+  if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
+    return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2, or inf)");
+  if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
+    return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
+  if (d->method == 4 && d->reflection != 1 && !local4 && !full4)
     return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1, and mode 2 without diffraction, on this path");
-  if (local4 && d->npass != 1) return fail(DTMM_ENOTSUP, "4x4 reflection mode 2 supports npass = 1 on this path");
+  if ((local4 || full4) && d->npass != 1)
+    return fail(DTMM_ENOTSUP, "4x4 without diffraction or with diffraction = inf supports npass = 1 on this path");
   if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
     return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
@@ -148,6 +157,18 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
   if (d->method == 4 && d->diffraction == 0) {  // the per-voxel transfer needs the scalars only
+    L.total = off;
+    return L;
+  }
+  if (d->diffraction == DTMM_DIFFRACTION_FULL) {
+    // beta, phi and the sorted mode list per wavelength and grid point, the
+    // row DFTs and the mode amplitudes (FP64)
+    const size_t grid = (size_t)d->nlam * L.HW;
+    L.fbeta = take(sizeof(double) * grid);
+    L.fphi = take(sizeof(double) * grid);
+    L.fmodes = take(sizeof(int) * (grid + d->nlam));
+    L.X = take(16 * NI * 4 * L.HW);
+    L.F = take(16 * NI * 4 * L.HW);
     L.total = off;
     return L;
   }
@@ -706,6 +727,65 @@ struct Engine {
   // 4x4 reflection mode 2 without diffraction: the per-voxel transfer layer
   // by layer (input -> field_out, then in place), each layer's result also
   // into the bulk output when asked
+  // 4x4 with diffraction = inf: the sorted mode list once, then per layer and
+  // sub-step the mode amplitudes of the current field and their plane waves
+  // through the voxels (input -> field_out, then in place); each layer's
+  // result also into the bulk output when asked
+  int run_full4() {
+    int rc = scalars();
+    if (rc) return rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    FullParams fp;
+    fp.ks = ks();
+    fp.betamax = d.betamax;
+    fp.beta = A<double>(L.fbeta);
+    fp.phi = A<double>(L.fphi);
+    fp.modes = A<int>(L.fmodes);
+    fp.count = fp.modes + (size_t)d.nlam * L.HW;
+    int limx = -1;
+    for (int i = 0; i < d.nlam; ++i) limx = std::max(limx, band_limit(d.width, d.ks[i], d.betamax));
+    fp.limx = std::max(limx, 0);
+    fp.S = 2 * fp.limx + 1 >= d.width ? d.width : 2 * fp.limx + 1;
+    CK(cudaMemsetAsync(fp.count, 0, sizeof(int) * d.nlam, st));
+    const dim3 gk((unsigned)((L.HW + 127) / 128), (unsigned)d.nlam);
+    k_full_betaphi<<<gk, 128, 0, st>>>(fp, g);
+    CKL("k_full_betaphi");
+    k_full_rank<<<gk, 128, 0, st>>>(fp, g);
+    CKL("k_full_rank");
+    Local4Params q;
+    q.epsv = d.epsv;
+    q.epsa = d.epsa;
+    for (int i = 0; i < 3; ++i) {
+      q.ev_s[i] = d.epsv_strides[i];
+      q.ea_s[i] = d.epsa_strides[i];
+    }
+    q.eps_complex = d.eps_complex;
+    q.ks = ks();
+    q.beta = rbeta();
+    q.phi = rphi();
+    cpx<double>* Ab = A<cpx<double>>(L.X);
+    cpx<double>* amp = A<cpx<double>>(L.F);
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    for (int l = 0; l < d.nlayers; ++l) {
+      q.layer = l;
+      q.nst = d.nstep[l];
+      q.d = d.thickness[l] / d.nstep[l];
+      for (int s = 0; s < d.nstep[l]; ++s) {
+        const cpx<R>* src = (l == 0 && s == 0) ? (const cpx<R>*)fin : (const cpx<R>*)fout;
+        k_full_rowdft<R><<<dim3((unsigned)d.height, (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, src, Ab);
+        CKL("k_full_rowdft");
+        k_full_coldft<<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, Ab, amp);
+        CKL("k_full_coldft");
+        k_full_apply<R><<<gk, 128, 0, st>>>(fp, q, g, amp, fout);
+        CKL("k_full_apply");
+      }
+      if (bulk) CK(cudaMemcpyAsync(bulk + (size_t)(l + 1) * NI * 4 * L.HW, fout, bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    return DTMM_OK;
+  }
+
   int run_local4() {
     int rc = scalars();
     if (rc) return rc;
@@ -1163,6 +1243,8 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   int rc;
   if (d->method == 4 && d->diffraction == 0) {
     rc = e.run_local4();
+  } else if (d->diffraction == DTMM_DIFFRACTION_FULL) {
+    rc = e.run_full4();
   } else {
     rc = e.setup();
     if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();

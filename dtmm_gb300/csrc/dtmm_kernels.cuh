@@ -614,6 +614,174 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
 }
 
 // ---------------------------------------------------------------------------
+// 4x4 transfer with diffraction = inf (dtmm/propagate_4x4.py:515-560): per
+// wavelength, the FFT amplitude of every eigenwave with beta < betamax is
+// carried as a plane wave through every voxel's F . P . F^-1 for that
+// wave's own (beta, phi), and the waves are summed in real space, in order
+// of increasing beta (ties in FFT-grid order) as the reference sums them.
+//   k_full_betaphi  beta, phi of every FFT-grid point (dtmm/wave.py:54)
+//   k_full_rank     the sorted in-band mode list of each wavelength
+//   k_full_rowdft   amplitudes, step 1: DFT of every row at the in-band
+//                   columns (|f_x| <= the largest band limit)
+//   k_full_coldft   step 2: the column DFT at each mode's row frequency
+//   k_full_apply    the plane waves through the voxels, summed per pixel
+// Everything but the stored field is FP64 in both precisions; the sums over
+// pixels run in a fixed order (no atomics), so results are deterministic.
+// ---------------------------------------------------------------------------
+struct FullParams {
+  const double* ks;    // [lam]
+  double betamax;
+  double* beta;        // [lam][H W]
+  double* phi;         // [lam][H W]
+  int* modes;          // [lam][H W] FFT-grid index of the m-th mode
+  int* count;          // [lam] in-band modes
+  int limx;            // in-band column half width; S = 2 limx + 1 slots, or all W columns
+  int S;
+};
+
+__host__ __device__ __forceinline__ int full_slot_ix(const FullParams& p, int s, int W) {
+  return p.S == W ? s : (s - p.limx + W) % W;
+}
+
+__global__ void k_full_betaphi(FullParams p, Grid g) {
+  const int HW = g.H * g.W;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lam = blockIdx.y;
+  if (k >= HW) return;
+  const int iy = k / g.W, ix = k - iy * g.W;
+  // numpy.fft.fftfreq: the signed index times 1 / n; the same expression as
+  // the band limit of the W axis at yy = 0, so every in-band mode's column
+  // lies within the band limit
+  const double xx = (double)fsigned(ix, g.W) * (1.0 / g.W), yy = (double)fsigned(iy, g.H) * (1.0 / g.H);
+  p.beta[(size_t)lam * HW + k] = (2.0 * M_PI / fabs(p.ks[lam])) * sqrt(xx * xx + yy * yy);
+  p.phi[(size_t)lam * HW + k] = atan2(yy, xx);
+}
+
+__global__ void k_full_rank(FullParams p, Grid g) {
+  const int HW = g.H * g.W;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lam = blockIdx.y;
+  if (k >= HW) return;
+  const double* b = p.beta + (size_t)lam * HW;
+  const double bk = b[k];
+  if (!(bk < p.betamax)) return;
+  int rank = 0;
+  for (int j = 0; j < HW; ++j) {
+    const double bj = b[j];
+    rank += (bj < p.betamax) && (bj < bk || (bj == bk && j < k));
+  }
+  p.modes[(size_t)lam * HW + rank] = k;
+  atomicAdd(p.count + lam, 1);
+}
+
+template <typename R>
+__global__ void k_full_rowdft(FullParams p, Grid g, const cpx<R>* __restrict__ field, cpx<double>* __restrict__ A) {
+  const int y = blockIdx.x, line = blockIdx.y;  // line = img * 4 + c
+  const int W = g.W;
+  const cpx<R>* row = field + ((size_t)line * g.H + y) * W;
+  for (int s = threadIdx.x; s < p.S; s += blockDim.x) {
+    const int ix = full_slot_ix(p, s, W);
+    cpx<double> acc = mk<double>(0.0, 0.0);
+    for (int x = 0; x < W; ++x) {
+      double sn, cs;
+      sincospi(-2.0 * (double)(((long long)ix * x) % W) / W, &sn, &cs);
+      const cpx<R> v = row[x];
+      acc = acc + mk<double>((double)v.re, (double)v.im) * mk<double>(cs, sn);
+    }
+    A[((size_t)line * g.H + y) * p.S + s] = acc;
+  }
+}
+
+__global__ void k_full_coldft(FullParams p, Grid g, const cpx<double>* __restrict__ A, cpx<double>* __restrict__ amp) {
+  const int HW = g.H * g.W;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int line = blockIdx.y, img = line / 4;
+  const int lam = img_lam(g, img);
+  if (m >= p.count[lam]) return;
+  const int k = p.modes[(size_t)lam * HW + m];
+  const int iy = k / g.W, ix = k - iy * g.W;
+  const int s = p.S == g.W ? ix : fsigned(ix, g.W) + p.limx;
+  if (s < 0 || s >= p.S) {  // not reached: in-band modes lie within the band limit
+    amp[(size_t)line * HW + m] = mk<double>(0.0, 0.0);
+    return;
+  }
+  const cpx<double>* col = A + (size_t)line * g.H * p.S + s;
+  cpx<double> acc = mk<double>(0.0, 0.0);
+  for (int y = 0; y < g.H; ++y) {
+    double sn, cs;
+    sincospi(-2.0 * (double)(((long long)iy * y) % g.H) / g.H, &sn, &cs);
+    acc = acc + col[(size_t)y * p.S] * mk<double>(cs, sn);
+  }
+  amp[(size_t)line * HW + m] = acc;
+}
+
+constexpr int kFullImg = 4;  // images of one wavelength accumulated per sweep over the modes
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_full_apply(FullParams p, Local4Params q, Grid g,
+                                                    const cpx<double>* __restrict__ amp, cpx<R>* __restrict__ out) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lam = blockIdx.y;
+  if (pix >= HW) return;
+  const int y = pix / g.W, x = pix - y * g.W;
+  const long long eo = q.layer * q.ev_s[0] + y * q.ev_s[1] + x * q.ev_s[2];
+  const long long ao = q.layer * q.ea_s[0] + y * q.ea_s[1] + x * q.ea_s[2];
+  cpx<double> ev[3];
+  if (q.eps_complex) {
+    const cpx<double>* e = (const cpx<double>*)q.epsv + eo;
+    ev[0] = e[0]; ev[1] = e[1]; ev[2] = e[2];
+  } else {
+    const double* e = (const double*)q.epsv + eo;
+    ev[0] = mk<double>(e[0], 0.0); ev[1] = mk<double>(e[1], 0.0); ev[2] = mk<double>(e[2], 0.0);
+  }
+  const double psi = q.epsa[ao], theta = q.epsa[ao + 1], azim = q.epsa[ao + 2];
+  const int nm = p.count[lam];
+  const double kd = p.ks[lam] * q.d;
+  const double inv_n = 1.0 / ((double)g.H * g.W);
+  const int per = g.nray * g.npol;  // images of this wavelength
+  for (int q0 = 0; q0 < per; q0 += kFullImg) {
+    const int nq = min(kFullImg, per - q0);
+    cpx<double> acc[kFullImg][4];
+    for (int i = 0; i < kFullImg; ++i)
+      for (int c = 0; c < 4; ++c) acc[i][c] = mk<double>(0.0, 0.0);
+    for (int m = 0; m < nm; ++m) {
+      const int k = p.modes[(size_t)lam * HW + m];
+      const int iy = k / g.W, ix = k - iy * g.W;
+      cpx<double> F[4][4], Fi[4][4], al[4];
+      local_fmat(p.beta[(size_t)lam * HW + k], p.phi[(size_t)lam * HW + k], ev, psi, theta, azim, F, al);
+      inv4(F, Fi);
+      cpx<double> ph[4];
+      for (int i = 0; i < 4; ++i) ph[i] = cexp_i(al[i] * kd);
+      double sn, cs;
+      const double r = (double)(((long long)iy * y) % g.H) / g.H + (double)(((long long)ix * x) % g.W) / g.W;
+      sincospi(2.0 * r, &sn, &cs);
+      const cpx<double> wave = mk<double>(cs * inv_n, sn * inv_n);
+      for (int i = 0; i < kFullImg; ++i) {
+        if (i >= nq) break;
+        const int img = (q0 + i) * g.nlam + lam;
+        cpx<double> w[4], u[4];
+        for (int c = 0; c < 4; ++c) w[c] = amp[((size_t)img * 4 + c) * HW + m] * wave;
+        for (int a = 0; a < 4; ++a) {
+          cpx<double> t = mk<double>(0.0, 0.0);
+          for (int c = 0; c < 4; ++c) t = t + Fi[a][c] * w[c];
+          u[a] = t * ph[a];
+        }
+        for (int c = 0; c < 4; ++c) {
+          cpx<double> t = mk<double>(0.0, 0.0);
+          for (int a = 0; a < 4; ++a) t = t + F[c][a] * u[a];
+          acc[i][c] = acc[i][c] + t;
+        }
+      }
+    }
+    for (int i = 0; i < nq; ++i) {
+      const int img = (q0 + i) * g.nlam + lam;
+      for (int c = 0; c < 4; ++c) out[((size_t)img * 4 + c) * HW + pix] = cvt<R>(acc[i][c]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Window statistics and 1D window weight tables (diffraction > 1).
 //
 // Window (i, j) of the n x n grid is the tent cx_i(beta_x) * cy_j(beta_y),

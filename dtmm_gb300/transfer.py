@@ -258,7 +258,7 @@ class DevicePlan:
         d.height, d.width = int(h), int(w)
         d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
         d.method = 4 if method == "4x4" else 2
-        d.diffraction = int(diffraction)
+        d.diffraction = _lib.DIFFRACTION_FULL if diffraction == np.inf else int(diffraction)
         d.reflection = int(reflection)
         d.npass = int(npass)
         d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
@@ -359,8 +359,10 @@ def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffract
     d.height, d.width = int(shape[0]), int(shape[1])
     d.nlam, d.npol, d.nray = int(nlam), int(npol), int(nray)
     d.method = 4 if method == "4x4" else 2
-    d.diffraction, d.npass = int(diffraction), int(npass)
-    d.reflection = (2 if int(diffraction) == 0 else 1) if method == "4x4" else 0
+    full = diffraction == np.inf
+    d.diffraction = _lib.DIFFRACTION_FULL if full else int(diffraction)
+    d.npass = int(npass)
+    d.reflection = (2 if not full and int(diffraction) == 0 else 1) if method == "4x4" else 0
     d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
     d.betamax, d.nin, d.nout, d.smooth = BETAMAX, N_COVER, N_COVER, SMOOTH
     th = np.ones(int(nlayers))
@@ -429,16 +431,20 @@ def _check_path(method, reflection, npass, diffraction, norm):
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
     if method != "4x4" and npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
-    # reflection mode 2 without diffraction: the per-voxel 4x4 transfer
+    # reflection mode 2 without diffraction: the per-voxel 4x4 transfer;
+    # diffraction = inf: every eigenwave exactly (any 4x4 reflection mode)
     local = method == "4x4" and reflection == 2 and diffraction == 0
-    if reflection not in ((1,) if method == "4x4" else (0, 1)) and not local:
+    full = diffraction == np.inf
+    if full and method != "4x4":
+        raise NotImplementedError("diffraction = inf is built for the 4x4 method")
+    if reflection not in ((1,) if method == "4x4" else (0, 1)) and not local and not full:
         raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
-    if local and npass != 1:
-        raise NotImplementedError("reflection mode 2 with npass > 1 is outside the GPU engine")
+    if (local or full) and npass != 1:
+        raise NotImplementedError("4x4 without diffraction or with diffraction = inf supports npass = 1")
     if method != "4x4" and npass != 1:
         raise NotImplementedError("the 2x2 method with npass > 1 is outside the GPU engine")
-    if not (0 <= diffraction < np.inf):
-        raise NotImplementedError("full (modal) diffraction is outside the GPU engine")
+    if not (0 <= diffraction <= np.inf):
+        raise ValueError("Invalid diffraction value")
     if diffraction == 0 and not local:
         if method == "4x4":
             raise ValueError("Invalid diffraction value")

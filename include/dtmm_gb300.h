@@ -33,6 +33,10 @@ extern "C" {
 #define DTMM_ECUDA (-3)       /* a CUDA call failed                                     */
 #define DTMM_ENOTSUP (-4)     /* option combination outside this engine                 */
 
+/* diffraction = inf: every eigenwave below betamax through the voxels exactly
+   (dtmm/propagate_4x4.py:515-560); 4x4, npass 1 */
+#define DTMM_DIFFRACTION_FULL (-1)
+
 #define DTMM_PRECISION_MIXED 0  /* complex64 bulk, FP64 eigen-solve and operator tables */
 #define DTMM_PRECISION_DOUBLE 1 /* complex128 bulk (the reference's default precision)  */
 
@@ -43,7 +47,8 @@ typedef struct dtmm_transfer_desc {
   int nlam, npol, nray;
   /* method and options (resolved by the caller as dtmm/transfer.py:433-465 does) */
   int method;        /* 4 = "4x4", 2 = "2x2"                                   */
-  int diffraction;   /* >= 1; n > 1 groups modes into n x n windows             */
+  int diffraction;   /* >= 1; n > 1 groups modes into n x n windows; 0 (4x4
+                        reflection 2) none; DTMM_DIFFRACTION_FULL = inf      */
   int reflection;    /* 4x4: 1 ; 2x2: 0 or 1                                    */
   int npass;         /* 4x4: >= 1 ; 2x2: 1                                      */
   int precision;     /* DTMM_PRECISION_*                                        */

@@ -1081,15 +1081,48 @@ def _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps):
     return field
 
 
+def propagate_4x4_full(field, ks, layer, nsteps, betamax):
+    """diffraction = inf (dtmm/propagate_4x4.py:515-560): per wavelength the
+    field's FFT amplitudes of every eigenwave with beta < betamax, taken in
+    order of increasing beta, each as a plane wave through the voxels'
+    F . P . F^-1 for that wave's (beta, phi), summed in real space."""
+    shape = field.shape[-2:]
+    d, epsv, epsa = layer
+    kd = ks * d / nsteps
+    out = np.empty_like(field)
+    ii, jj = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    yy, xx = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    for _ in range(nsteps):
+        for i in range(len(ks)):
+            ffield = fft2(field[..., i, :, :, :])
+            ofield = np.zeros_like(out[..., i, :, :, :])
+            b, p = betaphi(shape, ks[i])
+            mask = b < betamax
+            amplitude = ffield[..., mask]
+            order = sorted(zip(range(int(mask.sum())), b[mask], p[mask], ii[mask], jj[mask]), key=lambda e: e[1])
+            for j, beta_, phi_, ie, je in order:
+                alpha, f, fi = alphaffi(beta_, phi_, epsv, epsa)
+                pm = phasem(alpha, kd[i])
+                wave = np.exp(2j * np.pi * ((ie * yy % shape[0]) / shape[0] + (je * xx % shape[1]) / shape[1]))
+                w = amplitude[..., j][..., None, None] * (wave / (shape[0] * shape[1]))
+                ofield = ofield + dotmdmf(f, pm, fi, w)
+            out[..., i, :, :, :] = ofield
+        field = out.copy()
+    return field
+
+
 def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
                  reflection, multiray, norm, smooth, betamax, ret_bulk, out):
     """4x4 pass x layer sweep (dtmm/transfer.py:618-884): reflection mode 1 in
-    k-space, and reflection mode 2 without diffraction (the per-voxel 4x4
-    transfer) in real space."""
+    k-space, reflection mode 2 without diffraction (the per-voxel 4x4
+    transfer) and diffraction = inf (every eigenwave exactly, any reflection
+    mode) in real space."""
     if reflection not in (1, 2, 3, 4):
         raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
-    if reflection not in (1, 2) or (reflection == 2 and diffraction != 0):
-        raise NotImplementedError("oracle covers 4x4 reflection mode 1, and mode 2 without diffraction")
+    full = diffraction == np.inf
+    if not full and (reflection not in (1, 2) or (reflection == 2 and diffraction != 0)):
+        raise NotImplementedError("oracle covers 4x4 reflection mode 1, mode 2 without diffraction and "
+                                  "diffraction = inf")
     if smooth < 0:
         smooth = 0.0
     if norm != DTMM_NORM_FFT:
@@ -1125,9 +1158,9 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
     field = field_in.copy()
     i0 = field2intensity(field0).sum(axis=(-2, -1))
-    if not (0 <= diffraction < np.inf):
-        raise NotImplementedError("oracle covers finite diffraction")
-    work_in_fft = reflection != 2  # (dtmm/transfer.py:720-723)
+    if not (0 <= diffraction <= np.inf):
+        raise ValueError("Invalid diffraction value")
+    work_in_fft = reflection not in (2, 4) and not full  # (dtmm/transfer.py:720-723)
     if work_in_fft:
         field = fft2(field)
     if npass > 1:
@@ -1138,7 +1171,9 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
         for j in indices:
             nsub, (thickness, ev, ea) = layers[j]
             _, (de, ee, ae) = eff_layers[j]
-            if reflection == 2:
+            if full:
+                field = propagate_4x4_full(field, ks, (thickness * direction, ev, ea), nsub, betamax)
+            elif reflection == 2:
                 field = _transfer_ray_4x4_2(field, ks, (thickness * direction, ev, ea), beta, phi, nsub)
             else:
                 field = propagate_4x4_effective_1(field, ks, (thickness * direction, ev, ea),

@@ -166,6 +166,22 @@ CASES = {
                           material=("biaxial", dict()), seed=26,
                           illum=dict(beta=0.1, phi=1.1),
                           transfer=dict(method="2x2", diffraction=1, beta=0.1, phi=1.1)),
+    # diffraction = inf: every eigenwave below betamax through the voxels exactly
+    # (dtmm/propagate_4x4.py:515-560), in real space
+    "full_4x4": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=150.0,
+                     material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=28,
+                     illum=dict(jones=(1, 0)),
+                     transfer=dict(method="4x4", diffraction=np.inf, beta=0.0, phi=0.0)),
+    "full_4x4_offaxis_nstep2_bulk": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=200.0,
+                                         material=("twisted", dict(thickness=2.0)), seed=29,
+                                         illum=dict(beta=0.1, phi=0.4),
+                                         transfer=dict(method="4x4", diffraction=np.inf, nstep=2, beta=0.1,
+                                                       phi=0.4, ret_bulk=True)),
+    "full_4x4_biaxial_multiray": dict(shape=(10, 10), nlayers=2, wavelengths=[520.0, 600.0], pixelsize=150.0,
+                                      material=("biaxial", dict()), seed=30,
+                                      illum=dict(beta=[0.0, 0.15], phi=[0.0, 0.5], jones=(1, 0)),
+                                      transfer=dict(method="4x4", diffraction=np.inf, multiray=True,
+                                                    reflection=2, beta=[0.0, 0.15], phi=[0.0, 0.5])),
     "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),

@@ -71,7 +71,7 @@ def test_workspace_size_positive_for_valid_desc(lib):
     ("width", 2 * 41, "factor"),
     ("npass", 0, "npass"),
     ("fft_schedule", 4, "tuning"),
-    ("diffraction", -1, "diffraction"),
+    ("diffraction", -2, "diffraction"),
     ("row_group", -1, "tuning"),
     ("col_tile", -2, "tuning"),
 ])
@@ -87,6 +87,18 @@ def test_local_4x4_descriptor_rules(lib):
     assert lib.dtmm_transfer_workspace_size(ctypes.byref(ok)) > 0
     for kw in (dict(diffraction=0, reflection=1), dict(diffraction=0, reflection=2, npass=2),
                dict(diffraction=1, reflection=2)):
+        assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
+
+
+def test_full_diffraction_descriptor_rules(lib):
+    """diffraction = inf (DTMM_DIFFRACTION_FULL): the 4x4 method, any
+    reflection mode 1..4, npass 1; the workspace holds the mode tables."""
+    for r in (1, 2, 3, 4):
+        d = _desc(diffraction=_lib.DIFFRACTION_FULL, reflection=r)
+        assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) > 2 * 16 * 16 * 16
+    for kw in (dict(diffraction=_lib.DIFFRACTION_FULL, npass=2),
+               dict(diffraction=_lib.DIFFRACTION_FULL, reflection=5),
+               dict(diffraction=_lib.DIFFRACTION_FULL, method=2, reflection=1)):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
 
 
