@@ -771,7 +771,11 @@ struct Engine {
     for (int l = 0; l < d.nlayers; ++l) {
       q.layer = l;
       q.nst = d.nstep[l];
-      q.d = d.thickness[l] / d.nstep[l];
+      // the layer list already holds the sub-step thickness d / nstep
+      // (dtmm/transfer.py:926-975) and propagate_4x4_full divides it by
+      // nsteps once more (dtmm/propagate_4x4.py:521): each of the nstep
+      // sub-steps advances d / nstep^2
+      q.d = d.thickness[l] / ((double)d.nstep[l] * d.nstep[l]);
       for (int s = 0; s < d.nstep[l]; ++s) {
         const cpx<R>* src = (l == 0 && s == 0) ? (const cpx<R>*)fin : (const cpx<R>*)fout;
         k_full_rowdft<R><<<dim3((unsigned)d.height, (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, src, Ab);

@@ -1085,7 +1085,9 @@ def propagate_4x4_full(field, ks, layer, nsteps, betamax):
     """diffraction = inf (dtmm/propagate_4x4.py:515-560): per wavelength the
     field's FFT amplitudes of every eigenwave with beta < betamax, taken in
     order of increasing beta, each as a plane wave through the voxels'
-    F . P . F^-1 for that wave's (beta, phi), summed in real space."""
+    F . P . F^-1 for that wave's (beta, phi), summed in real space.  The
+    layer's thickness is already the sub-step d / nstep and is divided by
+    nsteps again here, as the reference does."""
     shape = field.shape[-2:]
     d, epsv, epsa = layer
     kd = ks * d / nsteps
