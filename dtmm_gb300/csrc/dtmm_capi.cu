@@ -89,6 +89,7 @@ struct Layout {
   int nslots, ndslots;
   size_t F, X, U, field0, op, Xw, Xa;
   size_t fbeta, fphi, fmodes;  // diffraction = inf: per-wavelength grid beta / phi, sorted modes + counts
+  size_t fA, famp;             // diffraction = inf: row DFTs and mode amplitudes (FP64)
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -113,8 +114,6 @@ int check_desc(const dtmm_transfer_desc* d) {
     return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
   if (d->method == 4 && d->reflection != 1 && !local4 && !full4)
     return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1, and mode 2 without diffraction, on this path");
-  if ((local4 || full4) && d->npass != 1)
-    return fail(DTMM_ENOTSUP, "4x4 without diffraction or with diffraction = inf supports npass = 1 on this path");
   if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
     return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
@@ -156,10 +155,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
-  if (d->method == 4 && d->diffraction == 0) {  // the per-voxel transfer needs the scalars only
-    L.total = off;
-    return L;
-  }
+  const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
     // beta, phi and the sorted mode list per wavelength and grid point, the
     // row DFTs and the mode amplitudes (FP64)
@@ -167,8 +163,10 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     L.fbeta = take(sizeof(double) * grid);
     L.fphi = take(sizeof(double) * grid);
     L.fmodes = take(sizeof(int) * (grid + d->nlam));
-    L.X = take(16 * NI * 4 * L.HW);
-    L.F = take(16 * NI * 4 * L.HW);
+    L.fA = take(16 * NI * 4 * L.HW);
+    L.famp = take(16 * NI * 4 * L.HW);
+  }
+  if (real_space && d->npass == 1) {  // the per-voxel / modal sweep alone needs nothing more
     L.total = off;
     return L;
   }
@@ -200,7 +198,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
       if (d->nstep[l] > 1) L.chains = true;
   L.Xw = take(L.chains ? field : 0);
   L.Xa = take(L.chains ? field : 0);
-  L.op_one = L.cplx * nrw * OP_REC * L.HW;
+  L.op_one = real_space ? 0 : L.cplx * nrw * OP_REC * L.HW;  // the real-space paths keep no operator records
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
   // per-layer cache, or two buffers that alternate between the layer being
@@ -281,6 +279,7 @@ template <typename R>
 struct Engine {
   Prof* prof = nullptr;
   int launches = 0;
+  FullParams fullp{};  // diffraction = inf: mode tables (full_prepare)
   int blim_max = 1 << 30;   // largest band limit of the W axis over the wavelengths (set by setup)
   int blimH_max = 1 << 30;  // the same for the H axis
   // k-space table cache of this call: (kind, thickness, medium) -> slot
@@ -727,17 +726,26 @@ struct Engine {
   // 4x4 reflection mode 2 without diffraction: the per-voxel transfer layer
   // by layer (input -> field_out, then in place), each layer's result also
   // into the bulk output when asked
-  // 4x4 with diffraction = inf: the sorted mode list once, then per layer and
-  // sub-step the mode amplitudes of the current field and their plane waves
-  // through the voxels (input -> field_out, then in place); each layer's
-  // result also into the bulk output when asked
-  int run_full4() {
-    int rc = scalars();
-    if (rc) return rc;
-    cpx<R>* fin = (cpx<R>*)io.field_in;
-    cpx<R>* fout = (cpx<R>*)io.field_out;
-    cpx<R>* bulk = (cpx<R>*)io.bulk;
-    FullParams fp;
+  // Parameters of the per-voxel kernels (reflection mode 2 without
+  // diffraction, and diffraction = inf) for layer l; d is set per layer.
+  Local4Params local_params() {
+    Local4Params p;
+    p.epsv = d.epsv;
+    p.epsa = d.epsa;
+    for (int i = 0; i < 3; ++i) {
+      p.ev_s[i] = d.epsv_strides[i];
+      p.ea_s[i] = d.epsa_strides[i];
+    }
+    p.eps_complex = d.eps_complex;
+    p.ks = ks();
+    p.beta = rbeta();
+    p.phi = rphi();
+    return p;
+  }
+
+  // diffraction = inf: beta, phi and the sorted in-band mode list of every
+  // wavelength (once per call)
+  int full_prepare(FullParams& fp) {
     fp.ks = ks();
     fp.betamax = d.betamax;
     fp.beta = A<double>(L.fbeta);
@@ -754,67 +762,96 @@ struct Engine {
     CKL("k_full_betaphi");
     k_full_rank<<<gk, 128, 0, st>>>(fp, g);
     CKL("k_full_rank");
-    Local4Params q;
-    q.epsv = d.epsv;
-    q.epsa = d.epsa;
-    for (int i = 0; i < 3; ++i) {
-      q.ev_s[i] = d.epsv_strides[i];
-      q.ea_s[i] = d.epsa_strides[i];
+    return DTMM_OK;
+  }
+
+  // diffraction = inf, one layer (signed by dir) from src into dst (may be
+  // src): per sub-step the mode amplitudes of the current field, then their
+  // plane waves through the voxels.  The layer list already holds the
+  // sub-step thickness d / nstep (dtmm/transfer.py:926-975) and
+  // propagate_4x4_full divides it by nsteps once more
+  // (dtmm/propagate_4x4.py:521): each sub-step advances d / nstep^2.
+  int full_layer(const FullParams& fp, Local4Params& q, int l, double dir, const cpx<R>* src, cpx<R>* dst) {
+    q.layer = l;
+    q.nst = d.nstep[l];
+    q.d = dir * d.thickness[l] / ((double)d.nstep[l] * d.nstep[l]);
+    cpx<double>* Ab = A<cpx<double>>(L.fA);
+    cpx<double>* amp = A<cpx<double>>(L.famp);
+    const dim3 gk((unsigned)((L.HW + 127) / 128), (unsigned)d.nlam);
+    for (int s = 0; s < d.nstep[l]; ++s) {
+      const cpx<R>* in = s == 0 ? src : (const cpx<R>*)dst;
+      k_full_rowdft<R><<<dim3((unsigned)d.height, (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, in, Ab);
+      CKL("k_full_rowdft");
+      k_full_coldft<<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, Ab, amp);
+      CKL("k_full_coldft");
+      k_full_apply<R><<<gk, 128, 0, st>>>(fp, q, g, amp, dst);
+      CKL("k_full_apply");
     }
-    q.eps_complex = d.eps_complex;
-    q.ks = ks();
-    q.beta = rbeta();
-    q.phi = rphi();
-    cpx<double>* Ab = A<cpx<double>>(L.X);
-    cpx<double>* amp = A<cpx<double>>(L.F);
+    return DTMM_OK;
+  }
+
+  // reflection mode 2 without diffraction, one layer (signed by dir) from src
+  // into dst (may be src), also into slab when given
+  int local_layer(Local4Params& p, int l, double dir, const cpx<R>* src, cpx<R>* dst, cpx<R>* slab) {
+    p.layer = l;
+    p.nst = d.nstep[l];
+    p.d = dir * d.thickness[l] / d.nstep[l];
+    const dim3 grid((unsigned)((L.HW + 127) / 128), (unsigned)d.nray);
+    k_local4<R><<<grid, 128, 0, st>>>(p, g, src, dst, slab);
+    CKL("k_local4");
+    return DTMM_OK;
+  }
+
+  // One pass of the real-space 4x4 paths over F (in place): layer order and
+  // thickness sign alternate with the pass as in dtmm/transfer.py:735-747
+  int sweep_real4(int pass) {
+    const double dir = (pass % 2 == 0) ? 1.0 : -1.0;
+    std::vector<int> order;
+    layer_order(pass % 2 == 0 ? 1 : -1, order);
+    cpx<R>* F = P(L.F);
+    Local4Params p = local_params();
+    int rc;
+    for (int l : order) {
+      if (d.diffraction == DTMM_DIFFRACTION_FULL)
+        rc = full_layer(fullp, p, l, dir, F, F);
+      else
+        rc = local_layer(p, l, dir, F, F, nullptr);
+      if (rc) return rc;
+    }
+    return DTMM_OK;
+  }
+
+  // 4x4 with diffraction = inf, npass 1: input -> field_out, then in place;
+  // each layer's result also into the bulk output when asked
+  int run_full4() {
+    int rc = scalars();
+    if (rc) return rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    if ((rc = full_prepare(fullp))) return rc;
+    Local4Params q = local_params();
     const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
     for (int l = 0; l < d.nlayers; ++l) {
-      q.layer = l;
-      q.nst = d.nstep[l];
-      // the layer list already holds the sub-step thickness d / nstep
-      // (dtmm/transfer.py:926-975) and propagate_4x4_full divides it by
-      // nsteps once more (dtmm/propagate_4x4.py:521): each of the nstep
-      // sub-steps advances d / nstep^2
-      q.d = d.thickness[l] / ((double)d.nstep[l] * d.nstep[l]);
-      for (int s = 0; s < d.nstep[l]; ++s) {
-        const cpx<R>* src = (l == 0 && s == 0) ? (const cpx<R>*)fin : (const cpx<R>*)fout;
-        k_full_rowdft<R><<<dim3((unsigned)d.height, (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, src, Ab);
-        CKL("k_full_rowdft");
-        k_full_coldft<<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)(NI * 4)), 128, 0, st>>>(fp, g, Ab, amp);
-        CKL("k_full_coldft");
-        k_full_apply<R><<<gk, 128, 0, st>>>(fp, q, g, amp, fout);
-        CKL("k_full_apply");
-      }
+      if ((rc = full_layer(fullp, q, l, 1.0, l == 0 ? (const cpx<R>*)fin : (const cpx<R>*)fout, fout))) return rc;
       if (bulk) CK(cudaMemcpyAsync(bulk + (size_t)(l + 1) * NI * 4 * L.HW, fout, bytes, cudaMemcpyDeviceToDevice, st));
     }
     return DTMM_OK;
   }
 
+  // 4x4 reflection mode 2 without diffraction, npass 1: the per-voxel
+  // transfer layer by layer (input -> field_out, then in place), each
+  // layer's result also into the bulk output when asked
   int run_local4() {
     int rc = scalars();
     if (rc) return rc;
     cpx<R>* fin = (cpx<R>*)io.field_in;
     cpx<R>* fout = (cpx<R>*)io.field_out;
     cpx<R>* bulk = (cpx<R>*)io.bulk;
-    Local4Params p;
-    p.epsv = d.epsv;
-    p.epsa = d.epsa;
-    for (int i = 0; i < 3; ++i) {
-      p.ev_s[i] = d.epsv_strides[i];
-      p.ea_s[i] = d.epsa_strides[i];
-    }
-    p.eps_complex = d.eps_complex;
-    p.ks = ks();
-    p.beta = rbeta();
-    p.phi = rphi();
-    const dim3 grid((unsigned)((L.HW + 127) / 128), (unsigned)d.nray);
+    Local4Params p = local_params();
     for (int l = 0; l < d.nlayers; ++l) {
-      p.layer = l;
-      p.nst = d.nstep[l];
-      p.d = d.thickness[l] / d.nstep[l];
       cpx<R>* slab = bulk ? bulk + (size_t)(l + 1) * NI * 4 * L.HW : nullptr;
-      k_local4<R><<<grid, 128, 0, st>>>(p, g, l == 0 ? (const cpx<R>*)fin : (const cpx<R>*)fout, fout, slab);
-      CKL("k_local4");
+      if ((rc = local_layer(p, l, 1.0, l == 0 ? (const cpx<R>*)fin : (const cpx<R>*)fout, fout, slab))) return rc;
     }
     return DTMM_OK;
   }
@@ -1135,8 +1172,14 @@ struct Engine {
     }
     CK(cudaMemcpyAsync(F, fin, bytes, cudaMemcpyDeviceToDevice, st));
     cpx<R>* bulk = (cpx<R>*)io.bulk;
+    // the real-space paths (no diffraction, or diffraction = inf) sweep F in
+    // place; the reference's bulk slabs alias its pass-end field there, which
+    // this path does not restate
+    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL;
+    if (real_space && bulk) return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for diffraction >= 1");
+    if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;
     for (int i = 0; i < npass; ++i) {
-      if ((rc = sweep4(i, bulk))) return rc;
+      if ((rc = real_space ? sweep_real4(i) : sweep4(i, bulk))) return rc;
       if (npass > 1) {
         const double sigma = d.smooth * (npass - i) / npass;
         if (i % 2 == 0) {
@@ -1245,9 +1288,9 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   make_plan(d->height, e.pH, d->fft_schedule == 3);
   make_plan(d->width, e.pW, d->fft_schedule == 3);
   int rc;
-  if (d->method == 4 && d->diffraction == 0) {
+  if (d->method == 4 && d->diffraction == 0 && d->npass == 1) {
     rc = e.run_local4();
-  } else if (d->diffraction == DTMM_DIFFRACTION_FULL) {
+  } else if (d->diffraction == DTMM_DIFFRACTION_FULL && d->npass == 1) {
     rc = e.run_full4();
   } else {
     rc = e.setup();

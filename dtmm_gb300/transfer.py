@@ -439,8 +439,7 @@ def _check_path(method, reflection, npass, diffraction, norm):
         raise NotImplementedError("diffraction = inf is built for the 4x4 method")
     if reflection not in ((1,) if method == "4x4" else (0, 1)) and not local and not full:
         raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
-    if (local or full) and npass != 1:
-        raise NotImplementedError("4x4 without diffraction or with diffraction = inf supports npass = 1")
+
     if method != "4x4" and npass != 1:
         raise NotImplementedError("the 2x2 method with npass > 1 is outside the GPU engine")
     if not (0 <= diffraction <= np.inf):
@@ -480,6 +479,8 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         raise NotImplementedError("optical data with more than one block is outside the GPU engine")
     if ret_bulk and method != "4x4":
         raise NotImplementedError("ret_bulk is implemented for the 4x4 method")
+    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf):
+        raise NotImplementedError("ret_bulk with npass > 1 is implemented for diffraction >= 1")
     ks = k0(wavelengths, pixelsize)
     cdt = torch.complex128 if precision == "double" else torch.complex64
     dev = torch.device("cuda", torch.cuda.current_device())

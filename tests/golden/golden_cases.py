@@ -182,6 +182,17 @@ CASES = {
                                       illum=dict(beta=[0.0, 0.15], phi=[0.0, 0.5], jones=(1, 0)),
                                       transfer=dict(method="4x4", diffraction=np.inf, multiray=True,
                                                     reflection=2, beta=[0.0, 0.15], phi=[0.0, 0.5])),
+    # npass > 1 on the real-space paths (beta 0: the reference warns that the
+    # 4x4 method without diffraction does not support npass > 1 off axis; with
+    # npass > 1 reflection resolves to 1, so mode 2 is asked for explicitly)
+    "nodiff_4x4_npass3": dict(shape=(12, 10), nlayers=3, wavelengths=[500.0, 650.0], pixelsize=100.0,
+                              material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=31,
+                              illum=dict(),
+                              transfer=dict(method="4x4", diffraction=0, reflection=2, npass=3, beta=0.0, phi=0.0)),
+    "full_4x4_npass2": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=150.0,
+                            material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=32,
+                            illum=dict(jones=(1, 0)),
+                            transfer=dict(method="4x4", diffraction=np.inf, npass=2, beta=0.0, phi=0.0)),
     "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),

@@ -85,19 +85,22 @@ def test_local_4x4_descriptor_rules(lib):
     """diffraction 0 is the per-voxel 4x4 transfer: reflection mode 2, npass 1 only."""
     ok = _desc(diffraction=0, reflection=2)
     assert lib.dtmm_transfer_workspace_size(ctypes.byref(ok)) > 0
-    for kw in (dict(diffraction=0, reflection=1), dict(diffraction=0, reflection=2, npass=2),
-               dict(diffraction=1, reflection=2)):
+    for kw in (dict(diffraction=0, reflection=1), dict(diffraction=1, reflection=2)):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
+    # npass > 1 adds the between-pass projection buffers
+    two = _desc(diffraction=0, reflection=2, npass=2)
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(two)) > lib.dtmm_transfer_workspace_size(ctypes.byref(ok))
 
 
 def test_full_diffraction_descriptor_rules(lib):
     """diffraction = inf (DTMM_DIFFRACTION_FULL): the 4x4 method, any
-    reflection mode 1..4, npass 1; the workspace holds the mode tables."""
+    reflection mode 1..4, any npass; the workspace holds the mode tables."""
     for r in (1, 2, 3, 4):
         d = _desc(diffraction=_lib.DIFFRACTION_FULL, reflection=r)
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) > 2 * 16 * 16 * 16
-    for kw in (dict(diffraction=_lib.DIFFRACTION_FULL, npass=2),
-               dict(diffraction=_lib.DIFFRACTION_FULL, reflection=5),
+    d = _desc(diffraction=_lib.DIFFRACTION_FULL, npass=3)
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) > 0
+    for kw in (dict(diffraction=_lib.DIFFRACTION_FULL, reflection=5),
                dict(diffraction=_lib.DIFFRACTION_FULL, method=2, reflection=1)):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
 
