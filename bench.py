@@ -622,6 +622,7 @@ def main():
     import torch
 
     import dtmm_gb300
+    from dtmm_gb300.replicas import job_throughput, job_time_ms
     from dtmm_gb300.transfer import plan_transfer
 
     torch.cuda.set_device(local)
@@ -655,10 +656,10 @@ def main():
         res = {"batch": run_batch, "serve": run_serve, "2x2": run_2x2}[args.workload](args, dev)
         barrier()
         if dist is not None:
-            t = torch.tensor([res["ms_per_step"]], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            res["ms_per_step"] = float(t.item())
-            res["value"] = res["value"] * world
+            ms_rank = res["ms_per_step"]
+            res["ms_per_step"] = job_time_ms(ms_rank, dist, dev)
+            # every rank ran the same workload: its units over the slowest rank's time
+            res["value"] = job_throughput(res["value"] * ms_rank / 1e3, res["ms_per_step"], world)
             res["n_gpus"] = world
         if rank == 0:
             print(json.dumps(res))
@@ -718,13 +719,9 @@ def main():
         eager_ms += e0.elapsed_time(e1)
     torch.cuda.synchronize()
     clocks = clk.summary()
-    total_ms = float(sum(times))
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = job_time_ms(float(sum(times)), dist, dev)
     upd = plan.updates
-    value = upd * args.steps * world / (total_ms / 1e3)
+    value = job_throughput(upd * args.steps, total_ms, world)
     out_mixed = fout.to(torch.complex128).cpu().numpy()
 
     # dominant kernel: the fused row pass
