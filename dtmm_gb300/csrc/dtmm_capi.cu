@@ -90,6 +90,7 @@ struct Layout {
   size_t F, X, U, field0, op, Xw, Xa;
   size_t fbeta, fphi, fmodes;  // diffraction = inf: per-wavelength grid beta / phi, sorted modes + counts
   size_t fA, famp;             // diffraction = inf: row DFTs and mode amplitudes (FP64)
+  size_t r4part;               // reflection mode 4 with windows: the window's part of the field
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -104,16 +105,20 @@ int check_desc(const dtmm_transfer_desc* d) {
   // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1);
   // diffraction = inf (DTMM_DIFFRACTION_FULL): every eigenwave exactly (4x4, npass 1,
   // any reflection mode: the reference takes the same path for all of them)
-  const bool local4 = d->method == 4 && d->diffraction == 0 && d->reflection == 2;
+  const bool local4 = d->method == 4 && d->diffraction == 0 && (d->reflection == 2 || d->reflection == 4);
   const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
+  // reflection mode 4 with diffraction: real-space half steps around the
+  // corrected field diffraction matrix (one ray: the matrices follow its beam)
+  const bool refl4 = d->method == 4 && d->reflection == 4 && d->diffraction >= 1;
+  if (refl4 && d->nray != 1) return fail(DTMM_ENOTSUP, "4x4 reflection mode 4 with diffraction is supported for one ray");
   if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
     return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
   if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
     return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2, or inf)");
   if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
     return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
-  if (d->method == 4 && d->reflection != 1 && !local4 && !full4)
-    return fail(DTMM_ENOTSUP, "4x4 supports reflection mode 1, and mode 2 without diffraction, on this path");
+  if (d->method == 4 && d->reflection != 1 && !local4 && !full4 && !refl4)
+    return fail(DTMM_ENOTSUP, "4x4 supports reflection modes 1 and 4, and 2 without diffraction, on this path");
   if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
     return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
@@ -155,7 +160,8 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
-  const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL);
+  const bool refl4 = d->method == 4 && d->reflection == 4 && d->diffraction >= 1;
+  const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL || refl4);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
     // beta, phi and the sorted mode list per wavelength and grid point, the
     // row DFTs and the mode amplitudes (FP64)
@@ -166,7 +172,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     L.fA = take(16 * NI * 4 * L.HW);
     L.famp = take(16 * NI * 4 * L.HW);
   }
-  if (real_space && d->npass == 1) {  // the per-voxel / modal sweep alone needs nothing more
+  if (real_space && d->npass == 1 && !refl4) {  // the per-voxel / modal sweep alone needs nothing more
     L.total = off;
     return L;
   }
@@ -198,6 +204,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
       if (d->nstep[l] > 1) L.chains = true;
   L.Xw = take(L.chains ? field : 0);
   L.Xa = take(L.chains ? field : 0);
+  L.r4part = take(refl4 && L.nwin > 1 ? field : 0);  // reflection mode 4: one window's part
   L.op_one = real_space ? 0 : L.cplx * nrw * OP_REC * L.HW;  // the real-space paths keep no operator records
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
@@ -636,7 +643,9 @@ struct Engine {
       if (sl[i].used < sl[pick].used) pick = i;
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
-    int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false) : launch_ktab(what, dd, dst);
+    int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
+             : (what == KT_WINMAT || what == KT_CFD) ? launch_ktab(what, dd, dst, proj_mode)
+                                                     : launch_ktab(what, dd, dst);
     if (rc) return rc;
     sl[pick].what = what;
     sl[pick].d = dd;
@@ -802,21 +811,80 @@ struct Engine {
     return DTMM_OK;
   }
 
+  // F . P . F^-1 of every voxel over thickness dd (one step) for the beam of
+  // window w of ray 0, in place
+  int local_step(Local4Params& p, int l, double dd, int w, cpx<R>* f) {
+    p.layer = l;
+    p.nst = 1;
+    p.d = dd;
+    p.beta = wbeta() + w;
+    p.phi = wphi() + w;
+    const dim3 grid((unsigned)((L.HW + 127) / 128), 1u);
+    k_local4<R><<<grid, 128, 0, st>>>(p, g, f, f, nullptr);
+    CKL("k_local4");
+    return DTMM_OK;
+  }
+
+  // reflection mode 4 with diffraction, one layer of sub-steps ds (signed)
+  // on F: per window (one for diffraction 1) the part of the field in the
+  // window, then per sub-step F P F^-1 over ds/2, the corrected field
+  // diffraction matrix over ds, F P F^-1 over ds/2; the parts summed
+  // (dtmm/propagate_4x4.py:55-77, :233-287)
+  int refl4_layer(Local4Params& p, int l, double ds) {
+    cpx<R>* F = P(L.F);
+    const int nst = d.nstep[l];
+    int rc;
+    if (L.nwin == 1) {
+      const cpx<R>* cfd;
+      if ((rc = table(KT_CFD, ds, cfd, 0))) return rc;
+      for (int s = 0; s < nst; ++s) {
+        if ((rc = local_step(p, l, ds / 2, 0, F))) return rc;
+        if ((rc = diffract(F, F, cfd))) return rc;
+        if ((rc = local_step(p, l, ds / 2, 0, F))) return rc;
+      }
+      return DTMM_OK;
+    }
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    cpx<R>* acc = P(L.X);
+    cpx<R>* part = P(L.r4part);
+    CK(cudaMemsetAsync(acc, 0, bytes, st));
+    for (int w = 0; w < L.nwin; ++w) {
+      const cpx<R>* win;
+      if ((rc = table(KT_WINMAT, 0.0, win, w))) return rc;
+      if ((rc = diffract(part, F, win))) return rc;
+      const cpx<R>* cfd;
+      if ((rc = table(KT_CFD, ds, cfd, w))) return rc;
+      for (int s = 0; s < nst; ++s) {
+        if ((rc = local_step(p, l, ds / 2, w, part))) return rc;
+        if ((rc = diffract(part, part, cfd))) return rc;
+        if ((rc = local_step(p, l, ds / 2, w, part))) return rc;
+      }
+      if ((rc = axpby(acc, acc, nullptr, 1.0, part, nullptr, 1.0))) return rc;
+    }
+    CK(cudaMemcpyAsync(F, acc, bytes, cudaMemcpyDeviceToDevice, st));
+    return DTMM_OK;
+  }
+
   // One pass of the real-space 4x4 paths over F (in place): layer order and
-  // thickness sign alternate with the pass as in dtmm/transfer.py:735-747
-  int sweep_real4(int pass) {
+  // thickness sign alternate with the pass as in dtmm/transfer.py:735-747;
+  // with bulk (npass 1) each layer's result also into its slab
+  int sweep_real4(int pass, cpx<R>* bulk) {
     const double dir = (pass % 2 == 0) ? 1.0 : -1.0;
     std::vector<int> order;
     layer_order(pass % 2 == 0 ? 1 : -1, order);
     cpx<R>* F = P(L.F);
     Local4Params p = local_params();
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
     int rc;
     for (int l : order) {
       if (d.diffraction == DTMM_DIFFRACTION_FULL)
         rc = full_layer(fullp, p, l, dir, F, F);
-      else
+      else if (d.diffraction == 0)
         rc = local_layer(p, l, dir, F, F, nullptr);
+      else
+        rc = refl4_layer(p, l, dir * d.thickness[l] / d.nstep[l]);
       if (rc) return rc;
+      if (bulk) CK(cudaMemcpyAsync(bulk + (size_t)(l + 1) * NI * 4 * L.HW, F, bytes, cudaMemcpyDeviceToDevice, st));
     }
     return DTMM_OK;
   }
@@ -1175,11 +1243,12 @@ struct Engine {
     // the real-space paths (no diffraction, or diffraction = inf) sweep F in
     // place; the reference's bulk slabs alias its pass-end field there, which
     // this path does not restate
-    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL;
-    if (real_space && bulk) return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for diffraction >= 1");
+    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection == 4;
+    if (real_space && bulk && npass > 1)
+      return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for reflection mode 1 with diffraction >= 1");
     if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;
     for (int i = 0; i < npass; ++i) {
-      if ((rc = real_space ? sweep_real4(i) : sweep4(i, bulk))) return rc;
+      if ((rc = real_space ? sweep_real4(i, bulk) : sweep4(i, bulk))) return rc;
       if (npass > 1) {
         const double sigma = d.smooth * (npass - i) / npass;
         if (i % 2 == 0) {

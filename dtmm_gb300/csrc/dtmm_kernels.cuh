@@ -913,7 +913,15 @@ enum KTab {
   KT_DIAG = 3,   // (e+, e-) = exp(+/- i k0 d a_k), stored [lam][kx][ky] (D1 . D2 of two half steps)
   KT_2IN = 4,    // 2x4 [E(d) . t_in] . P_in[rows Ex, Ey]   (2x2 method entry)
   KT_2OUT = 5,   // 4x2 [sum_w win_w ; sum_w win_w E2H_w] . t_out . E(d)   (2x2 method exit)
+  KT_WINMAT = 6, // 4x4 window w (proj_mode) of the n x n grid times I     (dtmm/mode.py:11-50)
+  KT_CFD = 7,    // 4x4 C . D(d) . C, D = F . P(d) . F^-1 per k, C the correction of window /
+                 // beam proj_mode over -d/2 (corrected_field_diffraction_matrix, dtmm/matrix.py:86-93)
 };
+
+// the module default of betamax, which the reference's windowed reflection
+// mode 4 passes to its diffraction matrices instead of the caller's
+// (dtmm/conf.py:148, dtmm/propagate_4x4.py:262-264)
+constexpr double kDefaultBetamax = 0.8;
 
 struct KTabParams {
   int what;
@@ -1080,6 +1088,67 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   double beta, phi;
   betaphi_k(g, ks, ky, kx, beta, phi);
   cpx<double> al[4], F[4][4], Fi[4][4];
+  if (p.what == KT_WINMAT) {
+    // window w = proj_mode of ray 0: tent(beta_x) tent(beta_y), zero beyond betamax
+    const int n = p.nwin_axis, w = p.proj_mode;
+    double c = 1.0;
+    if (n > 1) {
+      const int i = w / n, j = w % n;
+      const int xt = (i == 0) ? -1 : ((i == n - 1) ? 1 : 0);
+      const int yt = (j == 0) ? -1 : ((j == n - 1) ? 1 : 0);
+      const double l = 2.0 * M_PI / ks;
+      const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
+      const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
+      const double b = sqrt(bx * bx + by * by);
+      c = 0.0;
+      if (b < p.win.betamax)
+        c = tent((bx - (win_center(p.win, i) + p.win.xoff[0])) / p.win.step, xt) *
+            tent((by - (win_center(p.win, j) + p.win.yoff[0])) / p.win.step, yt);
+    }
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(mk<double>(i == j ? c : 0.0, 0.0));
+    return;
+  }
+  if (p.what == KT_CFD) {
+    // D: the isotropic layer over d (cut at betamax); C: the beam's own mode
+    // over -d/2, uncut (alphaffi, not the diffraction eigen-data)
+    const double bmax = p.nwin_axis > 1 ? kDefaultBetamax : p.betamax;
+    iso_k(beta, phi, p.eps, bmax, al, F, Fi);
+    cpx<double> D[4][4], Cb[4][4], Fb[4][4], Fbi[4][4], alb[4], T[4][4];
+    cpx<double> pd[4], pc[4];
+    for (int m = 0; m < 4; ++m) pd[m] = cexp_i(al[m] * (ks * p.d));
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + F[i][m] * pd[m] * Fi[m][j];
+        D[i][j] = s;
+      }
+    const int w = p.proj_mode;
+    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    inv4(Fb, Fbi);
+    for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * p.d / 2));
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + Fb[i][m] * pc[m] * Fbi[m][j];
+        Cb[i][j] = s;
+      }
+    for (int i = 0; i < 4; ++i)  // T = D . C
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + D[i][m] * Cb[m][j];
+        T[i][j] = s;
+      }
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)  // C . T
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + Cb[i][m] * T[m][j];
+        o[i * 4 + j] = cvt<R>(s);
+      }
+    return;
+  }
   if (p.what == KT_PROJ) {
     iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
     // F . diag(modes) . F^-1 over the forward (or backward) pair (dtmm/diffract.py:242)

@@ -1081,6 +1081,80 @@ def _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps):
     return field
 
 
+def field_diffraction_matrix(shape, ks, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), mode="b", betamax=BETAMAX):
+    """Per-k F . P . F^-1 of a homogeneous layer, field basis (dtmm/diffract.py:125-136)."""
+    ks = np.asarray(ks, FDTYPE)
+    alpha, f, fi = diffraction_alphaffi(shape, ks, epsv=np.asarray(epsv, CDTYPE), epsa=np.asarray(epsa, FDTYPE),
+                                        betamax=betamax)
+    pmat = phase_matrix(alpha, ks * d, mode=mode)
+    return dotmdm(f, pmat, fi)
+
+
+def correction_matrix(beta, phi, ks, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0)):
+    """F . P(-k d) . F^-1 of the beam's own mode (dtmm/matrix.py:17-22)."""
+    alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
+    kd = -np.asarray(ks) * d
+    pmat = phase_matrix(alpha, kd)
+    return dotmdm(f, pmat, fi)
+
+
+def corrected_field_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0),
+                                       betamax=BETAMAX):
+    """C . D . C with D the field diffraction matrix over d and C the
+    correction over d / 2 (dtmm/matrix.py:86-93)."""
+    dmat = field_diffraction_matrix(shape, ks, d, epsv, epsa, betamax=betamax)
+    cmat = correction_matrix(beta, phi, ks, d / 2, epsv, epsa)
+    dmat = dotmm(dmat, cmat)
+    return dotmm(cmat, dmat)
+
+
+def _transfer_ray_4x4_4(field, ks, layer, beta, phi, nsteps, dmat):
+    """Reflection mode 4 (dtmm/propagate_4x4.py:55-77): F . P . F^-1 over half
+    the layer, the corrected field diffraction matrix, F . P . F^-1 again;
+    without a matrix the whole layer at once."""
+    d, epsv, epsa = layer
+    kd = ks * d if dmat is None else ks * d / 2
+    alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
+    p = phasem(alpha, kd[..., None, None])
+    for _ in range(nsteps):
+        field = dotmdmf(f, p, fi, field)
+        if dmat is not None:
+            field = diffract(field, dmat)
+            field = dotmdmf(f, p, fi, field)
+    return field
+
+
+def propagate_4x4_effective_4(field, ks, layer, eff_layer, beta, phi, nsteps, diffraction, betamax):
+    """Reflection mode 4 with diffraction (dtmm/propagate_4x4.py:233-287): one
+    corrected matrix for diffraction 1; n x n mode windows otherwise, each
+    part taken to real space and sent through mode 4 with its window's beta,
+    phi (whose matrices are built with the default betamax, as there)."""
+    d_eff, epsv_eff, epsa_eff = eff_layer
+    shape = field.shape[-2:]
+    if diffraction <= 1:
+        dmat = None if diffraction == 0 else corrected_field_diffraction_matrix(
+            shape, ks, beta, phi, d_eff, epsv_eff, epsa_eff, betamax=betamax)
+        return _transfer_ray_4x4_4(field, ks, layer, beta, phi, nsteps, dmat)
+    fout = np.zeros_like(field)
+    field = fft2(field)
+    try:
+        broadcast_shape = beta.shape
+        beta = beta[..., 0]
+        phi = phi[..., 0]
+    except IndexError:
+        broadcast_shape = ()
+    windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), betax_off=beta * np.cos(phi),
+                                      betay_off=beta * np.sin(phi), betamax=betamax)
+    n = len(windows)
+    betas = betas.reshape((n,) + broadcast_shape)
+    phis = phis.reshape((n,) + broadcast_shape)
+    dmats = corrected_field_diffraction_matrix(shape, ks, betas, phis, d_eff, epsv_eff, epsa_eff)
+    for window, b, p, dmat in zip(windows, betas, phis, dmats):
+        fpart = ifft2(field * window)
+        fout = fout + _transfer_ray_4x4_4(fpart, ks, layer, b, p, nsteps, dmat)
+    return fout
+
+
 def propagate_4x4_full(field, ks, layer, nsteps, betamax):
     """diffraction = inf (dtmm/propagate_4x4.py:515-560): per wavelength the
     field's FFT amplitudes of every eigenwave with beta < betamax, taken in
@@ -1122,8 +1196,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if reflection not in (1, 2, 3, 4):
         raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
     full = diffraction == np.inf
-    if not full and (reflection not in (1, 2) or (reflection == 2 and diffraction != 0)):
-        raise NotImplementedError("oracle covers 4x4 reflection mode 1, mode 2 without diffraction and "
+    if not full and (reflection == 3 or (reflection == 2 and diffraction != 0)):
+        raise NotImplementedError("oracle covers 4x4 reflection modes 1 and 4, mode 2 without diffraction and "
                                   "diffraction = inf")
     if smooth < 0:
         smooth = 0.0
@@ -1175,6 +1249,9 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
             _, (de, ee, ae) = eff_layers[j]
             if full:
                 field = propagate_4x4_full(field, ks, (thickness * direction, ev, ea), nsub, betamax)
+            elif reflection == 4:
+                field = propagate_4x4_effective_4(field, ks, (thickness * direction, ev, ea),
+                                                  (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             elif reflection == 2:
                 field = _transfer_ray_4x4_2(field, ks, (thickness * direction, ev, ea), beta, phi, nsub)
             else:

@@ -105,6 +105,21 @@ def test_full_diffraction_descriptor_rules(lib):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
 
 
+def test_reflection4_descriptor_rules(lib):
+    """Reflection mode 4: without diffraction the per-voxel transfer, with
+    diffraction the real-space half steps around the corrected field
+    diffraction matrix (one ray; windows add one field of workspace)."""
+    d0 = _desc(diffraction=0, reflection=4)
+    d1 = _desc(diffraction=1, reflection=4)
+    d3 = _desc(diffraction=3, reflection=4)
+    s0, s1, s3 = (lib.dtmm_transfer_workspace_size(ctypes.byref(x)) for x in (d0, d1, d3))
+    assert s0 > 0 and s1 > s0 and s3 > s1
+    two_rays = _desc(diffraction=1, reflection=4, nray=2)
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(two_rays)) == 0
+    assert "one ray" in _lib.last_error()
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(diffraction=1, reflection=3))) == 0
+
+
 def test_transfer_rejects_small_workspace(lib):
     d = _desc()
     io = _lib.TransferIO()
