@@ -107,10 +107,11 @@ int check_desc(const dtmm_transfer_desc* d) {
   // any reflection mode: the reference takes the same path for all of them)
   const bool local4 = d->method == 4 && d->diffraction == 0 && (d->reflection == 2 || d->reflection == 4);
   const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
-  // reflection mode 4 with diffraction: real-space half steps around the
-  // corrected field diffraction matrix (one ray: the matrices follow its beam)
-  const bool refl4 = d->method == 4 && d->reflection == 4 && d->diffraction >= 1;
-  if (refl4 && d->nray != 1) return fail(DTMM_ENOTSUP, "4x4 reflection mode 4 with diffraction is supported for one ray");
+  // reflection modes 2 and 4 with diffraction: real-space half steps around
+  // the corrected diffraction matrices (one ray: the matrices follow its beam)
+  const bool refl4 = d->method == 4 && (d->reflection == 4 || d->reflection == 2) && d->diffraction >= 1;
+  if (refl4 && d->nray != 1)
+    return fail(DTMM_ENOTSUP, "4x4 reflection modes 2 and 4 with diffraction are supported for one ray");
   if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
     return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
   if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
@@ -160,7 +161,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
-  const bool refl4 = d->method == 4 && d->reflection == 4 && d->diffraction >= 1;
+  const bool refl4 = d->method == 4 && (d->reflection == 4 || d->reflection == 2) && d->diffraction >= 1;
   const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL || refl4);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
     // beta, phi and the sorted mode list per wavelength and grid point, the
@@ -644,7 +645,7 @@ struct Engine {
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
     int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
-             : (what == KT_WINMAT || what == KT_CFD) ? launch_ktab(what, dd, dst, proj_mode)
+             : (what == KT_WINMAT || what == KT_CFD || what == KT_CEPN) ? launch_ktab(what, dd, dst, proj_mode)
                                                      : launch_ktab(what, dd, dst);
     if (rc) return rc;
     sl[pick].what = what;
@@ -749,6 +750,7 @@ struct Engine {
     p.ks = ks();
     p.beta = rbeta();
     p.phi = rphi();
+    p.op = 0;
     return p;
   }
 
@@ -811,12 +813,14 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // F . P . F^-1 of every voxel over thickness dd (one step) for the beam of
-  // window w of ray 0, in place
-  int local_step(Local4Params& p, int l, double dd, int w, cpx<R>* f) {
+  // the per-voxel operator `op` (F P F^-1, E P F^-1 or F P E^-1) of every
+  // voxel over thickness dd (one step) for the beam of window w of ray 0,
+  // in place
+  int local_step(Local4Params& p, int l, double dd, int w, int op, cpx<R>* f) {
     p.layer = l;
     p.nst = 1;
     p.d = dd;
+    p.op = op;
     p.beta = wbeta() + w;
     p.phi = wphi() + w;
     const dim3 grid((unsigned)((L.HW + 127) / 128), 1u);
@@ -825,22 +829,28 @@ struct Engine {
     return DTMM_OK;
   }
 
-  // reflection mode 4 with diffraction, one layer of sub-steps ds (signed)
-  // on F: per window (one for diffraction 1) the part of the field in the
-  // window, then per sub-step F P F^-1 over ds/2, the corrected field
-  // diffraction matrix over ds, F P F^-1 over ds/2; the parts summed
-  // (dtmm/propagate_4x4.py:55-77, :233-287)
+  // reflection modes 2 and 4 with diffraction, one layer of sub-steps ds
+  // (signed) on F: per window (one for diffraction 1) the part of the field
+  // in the window, then per sub-step a per-voxel half step, the corrected
+  // diffraction matrix over ds, the second half step; the parts summed.
+  // Mode 4: F P F^-1, the corrected field diffraction matrix, F P F^-1
+  // (dtmm/propagate_4x4.py:55-77, :233-287); mode 2: E P F^-1, the corrected
+  // E matrices of the forward and backward modes, F P E^-1
+  // (dtmm/propagate_4x4.py:18-52, :156-230).
   int refl4_layer(Local4Params& p, int l, double ds) {
     cpx<R>* F = P(L.F);
     const int nst = d.nstep[l];
+    const bool two = d.reflection == 2;
+    const int kind = two ? KT_CEPN : KT_CFD;
+    const int op_a = two ? 1 : 0, op_b = two ? 2 : 0;
     int rc;
     if (L.nwin == 1) {
       const cpx<R>* cfd;
-      if ((rc = table(KT_CFD, ds, cfd, 0))) return rc;
+      if ((rc = table(kind, ds, cfd, 0))) return rc;
       for (int s = 0; s < nst; ++s) {
-        if ((rc = local_step(p, l, ds / 2, 0, F))) return rc;
+        if ((rc = local_step(p, l, ds / 2, 0, op_a, F))) return rc;
         if ((rc = diffract(F, F, cfd))) return rc;
-        if ((rc = local_step(p, l, ds / 2, 0, F))) return rc;
+        if ((rc = local_step(p, l, ds / 2, 0, op_b, F))) return rc;
       }
       return DTMM_OK;
     }
@@ -853,11 +863,11 @@ struct Engine {
       if ((rc = table(KT_WINMAT, 0.0, win, w))) return rc;
       if ((rc = diffract(part, F, win))) return rc;
       const cpx<R>* cfd;
-      if ((rc = table(KT_CFD, ds, cfd, w))) return rc;
+      if ((rc = table(kind, ds, cfd, w))) return rc;
       for (int s = 0; s < nst; ++s) {
-        if ((rc = local_step(p, l, ds / 2, w, part))) return rc;
+        if ((rc = local_step(p, l, ds / 2, w, op_a, part))) return rc;
         if ((rc = diffract(part, part, cfd))) return rc;
-        if ((rc = local_step(p, l, ds / 2, w, part))) return rc;
+        if ((rc = local_step(p, l, ds / 2, w, op_b, part))) return rc;
       }
       if ((rc = axpby(acc, acc, nullptr, 1.0, part, nullptr, 1.0))) return rc;
     }
@@ -1243,7 +1253,8 @@ struct Engine {
     // the real-space paths (no diffraction, or diffraction = inf) sweep F in
     // place; the reference's bulk slabs alias its pass-end field there, which
     // this path does not restate
-    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection == 4;
+    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection == 4 ||
+                            d.reflection == 2;
     if (real_space && bulk && npass > 1)
       return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for reflection mode 1 with diffraction >= 1");
     if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;

@@ -465,6 +465,10 @@ struct Local4Params {
   const double* ks;   // [lam]
   const double* beta; // [ray]
   const double* phi;  // [ray]
+  // operator: 0 F . P . F^-1; 1 E . P . F^-1 and 2 F . P . E^-1 with E the
+  // block matrix of the forward (rows/columns 0, 2) and backward (1, 3)
+  // E parts (dtmm/tmm.py:974-996), the half steps of reflection mode 2
+  int op;
 };
 
 // field matrix and eigenvalues of one voxel (isotropic, uniaxial or biaxial)
@@ -575,6 +579,19 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
   cpx<double> F[4][4], al[4], Fi[4][4];
   local_fmat(p.beta[ray], p.phi[ray], ev, p.epsa[ao], p.epsa[ao + 1], p.epsa[ao + 2], F, al);
   inv4(F, Fi);
+  if (p.op != 0) {
+    cpx<double> E[4][4];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) E[i][j] = mk<double>(0.0, 0.0);
+    E[0][0] = F[0][0]; E[0][2] = F[0][2]; E[2][0] = F[2][0]; E[2][2] = F[2][2];
+    E[1][1] = F[0][1]; E[1][3] = F[0][3]; E[3][1] = F[2][1]; E[3][3] = F[2][3];
+    if (p.op == 1) {
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) F[i][j] = E[i][j];
+    } else {
+      inv4(E, Fi);
+    }
+  }
   cpx<R> f[4][4], fi[4][4];
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) {
@@ -916,6 +933,9 @@ enum KTab {
   KT_WINMAT = 6, // 4x4 window w (proj_mode) of the n x n grid times I     (dtmm/mode.py:11-50)
   KT_CFD = 7,    // 4x4 C . D(d) . C, D = F . P(d) . F^-1 per k, C the correction of window /
                  // beam proj_mode over -d/2 (corrected_field_diffraction_matrix, dtmm/matrix.py:86-93)
+  KT_CEPN = 8,   // 4x4 with the 2x2 C . D(d) . C of the forward modes on rows / columns 0, 2 and
+                 // of the backward modes on 1, 3, D = j . P(d) . j^-1 of the E parts, C over -d/2
+                 // (corrected_Epn_diffraction_matrix, dtmm/matrix.py:38-68)
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1147,6 +1167,38 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
         for (int m = 0; m < 4; ++m) s = s + Cb[i][m] * T[m][j];
         o[i * 4 + j] = cvt<R>(s);
       }
+    return;
+  }
+  if (p.what == KT_CEPN) {
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    const bool cut = beta >= p.betamax;
+    const int w = p.proj_mode;
+    cpx<double> alb[4], Fb[4][4];
+    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    cpx<double> M[4][4];
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) M[i][j] = mk<double>(0.0, 0.0);
+    for (int m = 0; m < 2; ++m) {  // m = 0 forward (columns 0, 2), 1 backward (1, 3)
+      cpx<double> J[2][2], Ji[2][2], Jb[2][2], Jbi[2][2], D[2][2], Cm[2][2], T[2][2];
+      J[0][0] = F[0][m]; J[0][1] = F[0][m + 2]; J[1][0] = F[2][m]; J[1][1] = F[2][m + 2];
+      Jb[0][0] = Fb[0][m]; Jb[0][1] = Fb[0][m + 2]; Jb[1][0] = Fb[2][m]; Jb[1][1] = Fb[2][m + 2];
+      inv2(J, Ji);
+      inv2(Jb, Jbi);
+      const cpx<double> pd[2] = {cexp_i(al[m] * (ks * p.d)), cexp_i(al[m + 2] * (ks * p.d))};
+      const cpx<double> pc[2] = {cexp_i(alb[m] * (-ks * p.d / 2)), cexp_i(alb[m + 2] * (-ks * p.d / 2))};
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+          D[i][j] = cut ? mk<double>(0.0, 0.0) : J[i][0] * pd[0] * Ji[0][j] + J[i][1] * pd[1] * Ji[1][j];
+          Cm[i][j] = Jb[i][0] * pc[0] * Jbi[0][j] + Jb[i][1] * pc[1] * Jbi[1][j];
+        }
+      for (int i = 0; i < 2; ++i)  // T = D . C
+        for (int j = 0; j < 2; ++j) T[i][j] = D[i][0] * Cm[0][j] + D[i][1] * Cm[1][j];
+      for (int i = 0; i < 2; ++i)  // C . T into the rows / columns of the direction
+        for (int j = 0; j < 2; ++j) M[2 * i + m][2 * j + m] = Cm[i][0] * T[0][j] + Cm[i][1] * T[1][j];
+    }
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(M[i][j]);
     return;
   }
   if (p.what == KT_PROJ) {

@@ -432,14 +432,14 @@ def _check_path(method, reflection, npass, diffraction, norm):
     if method != "4x4" and npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
     # reflection mode 2 or 4 without diffraction: the per-voxel 4x4 transfer;
-    # reflection mode 4 with diffraction: real-space half steps around the
-    # corrected field diffraction matrix; diffraction = inf: every eigenwave
+    # reflection modes 2 and 4 with diffraction: real-space half steps around
+    # the corrected diffraction matrices; diffraction = inf: every eigenwave
     # exactly (any 4x4 reflection mode)
     local = method == "4x4" and reflection in (2, 4) and diffraction == 0
     full = diffraction == np.inf
     if full and method != "4x4":
         raise NotImplementedError("diffraction = inf is built for the 4x4 method")
-    if reflection not in ((1, 4) if method == "4x4" else (0, 1)) and not local and not full:
+    if reflection not in ((1, 2, 4) if method == "4x4" else (0, 1)) and not local and not full:
         raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
 
     if method != "4x4" and npass != 1:
@@ -481,7 +481,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         raise NotImplementedError("optical data with more than one block is outside the GPU engine")
     if ret_bulk and method != "4x4":
         raise NotImplementedError("ret_bulk is implemented for the 4x4 method")
-    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf or reflection == 4):
+    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf or reflection in (2, 4)):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
     ks = k0(wavelengths, pixelsize)
     cdt = torch.complex128 if precision == "double" else torch.complex64

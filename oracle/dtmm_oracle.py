@@ -652,6 +652,21 @@ def second_E_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), eps
     return dotmm(dmat, cmat)
 
 
+def corrected_E_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1,
+                                   betamax=BETAMAX):
+    """C . D . C of one direction, 2x2, C over d / 2 (dtmm/matrix.py:38-43)."""
+    dmat = E_diffraction_matrix(shape, ks, d, epsv, epsa, mode=mode, betamax=betamax)
+    cmat = E_correction_matrix(beta, phi, ks, d / 2.0, epsv, epsa, mode=mode)
+    return dotmm(cmat, dotmm(dmat, cmat))
+
+
+def corrected_Epn_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
+    """The forward and backward corrected E diffraction matrices (dtmm/matrix.py:61-68)."""
+    ep = corrected_E_diffraction_matrix(shape, ks, beta, phi, d=d, epsv=epsv, epsa=epsa, mode=+1, betamax=betamax)
+    en = corrected_E_diffraction_matrix(shape, ks, beta, phi, d=d, epsv=epsv, epsa=epsa, mode=-1, betamax=betamax)
+    return ep, en
+
+
 def first_Epn_diffraction_matrix(shape, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), betamax=BETAMAX):
     """field -> Epn diffraction over d: E . P . F^-1 (dtmm/matrix.py:110)."""
     ks = np.asarray(ks, FDTYPE)
@@ -1069,16 +1084,62 @@ def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, 
 # --------------------------------------------------------------------------
 # drivers (dtmm/transfer.py)
 # --------------------------------------------------------------------------
-def _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps):
-    """Reflection mode 2 without diffraction: F . P . F^-1 per voxel, nsteps
-    times, on the real-space field (dtmm/propagate_4x4.py:18-52 with dmatpn None)."""
+def _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps, dmatpn=None):
+    """Reflection mode 2 (dtmm/propagate_4x4.py:18-52): without diffraction
+    matrices F . P . F^-1 per voxel over the layer, nsteps times; with them,
+    per step E . P . F^-1 over half the layer (E the block E matrix of the
+    forward and backward modes), the forward (0, 2) and backward (1, 3)
+    components diffracted by their corrected E matrices, F . P . E^-1."""
     d, epsv, epsa = layer
-    kd = ks * d
+    kd = ks * d if dmatpn is None else ks * d / 2
     alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
     p = phasem(alpha, kd[..., None, None])
+    if dmatpn is not None:
+        dmatp, dmatn = dmatpn
+        e = E_mat(f)
+        ei = inv(e)
     for _ in range(nsteps):
-        field = dotmdmf(f, p, fi, field)
+        if dmatpn is None:
+            field = dotmdmf(f, p, fi, field)
+        else:
+            field = dotmdmf(e, p, fi, field)
+            field = np.array(field)
+            field[..., 0::2, :, :] = diffract(field[..., 0::2, :, :], dmatp)
+            field[..., 1::2, :, :] = diffract(field[..., 1::2, :, :], dmatn)
+            field = dotmdmf(f, p, ei, field)
     return field
+
+
+def propagate_4x4_effective_2(field, ks, layer, eff_layer, beta, phi, nsteps, diffraction, betamax):
+    """Reflection mode 2 with diffraction (dtmm/propagate_4x4.py:156-230): one
+    pair of corrected E matrices for diffraction 1; n x n mode windows
+    otherwise, each part in real space through mode 2 with its window's
+    beta, phi, summed."""
+    d_eff, epsv_eff, epsa_eff = eff_layer
+    shape = field.shape[-2:]
+    if diffraction <= 1:
+        dmatpn = None if diffraction == 0 else corrected_Epn_diffraction_matrix(
+            shape, ks, beta, phi, d=d_eff, epsv=epsv_eff, epsa=epsa_eff, betamax=betamax)
+        return _transfer_ray_4x4_2(field, ks, layer, beta, phi, nsteps, dmatpn)
+    fout = np.zeros_like(field)
+    field = fft2(field)
+    try:
+        broadcast_shape = beta.shape
+        beta = beta[..., 0]
+        phi = phi[..., 0]
+    except IndexError:
+        broadcast_shape = ()
+    windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), betax_off=beta * np.cos(phi),
+                                      betay_off=beta * np.sin(phi), betamax=betamax)
+    n = len(windows)
+    betas = betas.reshape((n,) + broadcast_shape)
+    phis = phis.reshape((n,) + broadcast_shape)
+    dmatps, dmatns = corrected_Epn_diffraction_matrix(shape, ks, betas, phis, d=d_eff, epsv=epsv_eff,
+                                                      epsa=epsa_eff, betamax=betamax)
+    for window, b, p, dmatp, dmatn in zip(windows, betas, phis, dmatps, dmatns):
+        fpart = ifft2(field * window)
+        fout = fout + _transfer_ray_4x4_2(fpart, ks, layer, b, p, nsteps, (dmatp, dmatn))
+    return fout
 
 
 def field_diffraction_matrix(shape, ks, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0), mode="b", betamax=BETAMAX):
@@ -1196,9 +1257,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if reflection not in (1, 2, 3, 4):
         raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
     full = diffraction == np.inf
-    if not full and (reflection == 3 or (reflection == 2 and diffraction != 0)):
-        raise NotImplementedError("oracle covers 4x4 reflection modes 1 and 4, mode 2 without diffraction and "
-                                  "diffraction = inf")
+    if not full and reflection == 3:
+        raise NotImplementedError("oracle covers 4x4 reflection modes 1, 2 and 4, and diffraction = inf")
     if smooth < 0:
         smooth = 0.0
     if norm != DTMM_NORM_FFT:
@@ -1253,7 +1313,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                 field = propagate_4x4_effective_4(field, ks, (thickness * direction, ev, ea),
                                                   (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             elif reflection == 2:
-                field = _transfer_ray_4x4_2(field, ks, (thickness * direction, ev, ea), beta, phi, nsub)
+                field = propagate_4x4_effective_2(field, ks, (thickness * direction, ev, ea),
+                                                  (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             else:
                 field = propagate_4x4_effective_1(field, ks, (thickness * direction, ev, ea),
                                                   (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)

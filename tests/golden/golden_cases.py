@@ -209,6 +209,23 @@ CASES = {
                                 illum=dict(jones=(1, 0)),
                                 transfer=dict(method="4x4", diffraction=1, reflection=4, npass=3, beta=0.0,
                                               phi=0.0)),
+    # reflection mode 2 with diffraction (dtmm/propagate_4x4.py:18-52, :156-230):
+    # E P F^-1 and F P E^-1 half steps around the corrected E matrices of the
+    # forward and backward modes
+    "refl2_4x4_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                         material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=36,
+                         illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                         transfer=dict(method="4x4", diffraction=1, reflection=2, beta=0.1, phi=0.3)),
+    "refl2_4x4_d3_nstep2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                material=("twisted", dict(thickness=2.0)), seed=37,
+                                illum=dict(),
+                                transfer=dict(method="4x4", diffraction=3, reflection=2, nstep=2, beta=0.0,
+                                              phi=0.0)),
+    "refl2_4x4_d1_npass3": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=38,
+                                illum=dict(jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, reflection=2, npass=3, beta=0.0,
+                                              phi=0.0)),
     "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),
