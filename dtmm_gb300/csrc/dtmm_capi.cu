@@ -109,9 +109,9 @@ int check_desc(const dtmm_transfer_desc* d) {
   const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
   // reflection modes 2 and 4 with diffraction: real-space half steps around
   // the corrected diffraction matrices (one ray: the matrices follow its beam)
-  const bool refl4 = d->method == 4 && (d->reflection == 4 || d->reflection == 2) && d->diffraction >= 1;
+  const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
   if (refl4 && d->nray != 1)
-    return fail(DTMM_ENOTSUP, "4x4 reflection modes 2 and 4 with diffraction are supported for one ray");
+    return fail(DTMM_ENOTSUP, "4x4 reflection modes 2-4 with diffraction are supported for one ray");
   if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
     return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
   if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
@@ -161,7 +161,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
-  const bool refl4 = d->method == 4 && (d->reflection == 4 || d->reflection == 2) && d->diffraction >= 1;
+  const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
   const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL || refl4);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
     // beta, phi and the sorted mode list per wavelength and grid point, the
@@ -645,7 +645,8 @@ struct Engine {
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
     int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
-             : (what == KT_WINMAT || what == KT_CFD || what == KT_CEPN) ? launch_ktab(what, dd, dst, proj_mode)
+             : (what == KT_WINMAT || what == KT_CFD || what == KT_CEPN || what == KT_CD || what == KT_DC)
+                 ? launch_ktab(what, dd, dst, proj_mode)
                                                      : launch_ktab(what, dd, dst);
     if (rc) return rc;
     sl[pick].what = what;
@@ -837,21 +838,35 @@ struct Engine {
   // (dtmm/propagate_4x4.py:55-77, :233-287); mode 2: E P F^-1, the corrected
   // E matrices of the forward and backward modes, F P E^-1
   // (dtmm/propagate_4x4.py:18-52, :156-230).
+  // Mode 3 (its field lives in k-space between layers in the reference; the
+  // same operators on the real-space field): C . D over ds/2, F P F^-1 over
+  // ds, D . C over ds/2 (dtmm/propagate_4x4.py:135-153, :447-512).
+  int refl_chain(Local4Params& p, int l, double ds, int w, cpx<R>* f) {
+    int rc;
+    if (d.reflection == 3) {
+      const cpx<R>* cd;
+      const cpx<R>* dc;
+      if ((rc = table(KT_CD, ds / 2, cd, w))) return rc;
+      if ((rc = diffract(f, f, cd))) return rc;
+      if ((rc = local_step(p, l, ds, w, 0, f))) return rc;
+      if ((rc = table(KT_DC, ds / 2, dc, w))) return rc;
+      return diffract(f, f, dc);
+    }
+    const bool two = d.reflection == 2;
+    const cpx<R>* cfd;
+    if ((rc = table(two ? KT_CEPN : KT_CFD, ds, cfd, w))) return rc;
+    if ((rc = local_step(p, l, ds / 2, w, two ? 1 : 0, f))) return rc;
+    if ((rc = diffract(f, f, cfd))) return rc;
+    return local_step(p, l, ds / 2, w, two ? 2 : 0, f);
+  }
+
   int refl4_layer(Local4Params& p, int l, double ds) {
     cpx<R>* F = P(L.F);
     const int nst = d.nstep[l];
-    const bool two = d.reflection == 2;
-    const int kind = two ? KT_CEPN : KT_CFD;
-    const int op_a = two ? 1 : 0, op_b = two ? 2 : 0;
     int rc;
     if (L.nwin == 1) {
-      const cpx<R>* cfd;
-      if ((rc = table(kind, ds, cfd, 0))) return rc;
-      for (int s = 0; s < nst; ++s) {
-        if ((rc = local_step(p, l, ds / 2, 0, op_a, F))) return rc;
-        if ((rc = diffract(F, F, cfd))) return rc;
-        if ((rc = local_step(p, l, ds / 2, 0, op_b, F))) return rc;
-      }
+      for (int s = 0; s < nst; ++s)
+        if ((rc = refl_chain(p, l, ds, 0, F))) return rc;
       return DTMM_OK;
     }
     const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
@@ -862,13 +877,8 @@ struct Engine {
       const cpx<R>* win;
       if ((rc = table(KT_WINMAT, 0.0, win, w))) return rc;
       if ((rc = diffract(part, F, win))) return rc;
-      const cpx<R>* cfd;
-      if ((rc = table(kind, ds, cfd, w))) return rc;
-      for (int s = 0; s < nst; ++s) {
-        if ((rc = local_step(p, l, ds / 2, w, op_a, part))) return rc;
-        if ((rc = diffract(part, part, cfd))) return rc;
-        if ((rc = local_step(p, l, ds / 2, w, op_b, part))) return rc;
-      }
+      for (int s = 0; s < nst; ++s)
+        if ((rc = refl_chain(p, l, ds, w, part))) return rc;
       if ((rc = axpby(acc, acc, nullptr, 1.0, part, nullptr, 1.0))) return rc;
     }
     CK(cudaMemcpyAsync(F, acc, bytes, cudaMemcpyDeviceToDevice, st));
@@ -1253,8 +1263,7 @@ struct Engine {
     // the real-space paths (no diffraction, or diffraction = inf) sweep F in
     // place; the reference's bulk slabs alias its pass-end field there, which
     // this path does not restate
-    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection == 4 ||
-                            d.reflection == 2;
+    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection >= 2;
     if (real_space && bulk && npass > 1)
       return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for reflection mode 1 with diffraction >= 1");
     if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;

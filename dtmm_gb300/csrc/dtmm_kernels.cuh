@@ -936,6 +936,8 @@ enum KTab {
   KT_CEPN = 8,   // 4x4 with the 2x2 C . D(d) . C of the forward modes on rows / columns 0, 2 and
                  // of the backward modes on 1, 3, D = j . P(d) . j^-1 of the E parts, C over -d/2
                  // (corrected_Epn_diffraction_matrix, dtmm/matrix.py:38-68)
+  KT_CD = 9,     // 4x4 C . D(d), C the correction over -d        (second_field_diffraction_matrix,
+  KT_DC = 10,    // 4x4 D(d) . C                                  first_field_..., dtmm/matrix.py:95-107)
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1130,10 +1132,11 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(mk<double>(i == j ? c : 0.0, 0.0));
     return;
   }
-  if (p.what == KT_CFD) {
+  if (p.what == KT_CFD || p.what == KT_CD || p.what == KT_DC) {
     // D: the isotropic layer over d (cut at betamax); C: the beam's own mode
-    // over -d/2, uncut (alphaffi, not the diffraction eigen-data)
-    const double bmax = p.nwin_axis > 1 ? kDefaultBetamax : p.betamax;
+    // over -d/2 (KT_CFD) or -d, uncut (alphaffi, not the diffraction eigen-data)
+    const double bmax = (p.what == KT_CFD && p.nwin_axis > 1) ? kDefaultBetamax : p.betamax;
+    const double dc = p.what == KT_CFD ? p.d / 2 : p.d;
     iso_k(beta, phi, p.eps, bmax, al, F, Fi);
     cpx<double> D[4][4], Cb[4][4], Fb[4][4], Fbi[4][4], alb[4], T[4][4];
     cpx<double> pd[4], pc[4];
@@ -1147,20 +1150,34 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     const int w = p.proj_mode;
     iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
     inv4(Fb, Fbi);
-    for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * p.d / 2));
+    for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * dc));
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j) {
         cpx<double> s = mk<double>(0.0, 0.0);
         for (int m = 0; m < 4; ++m) s = s + Fb[i][m] * pc[m] * Fbi[m][j];
         Cb[i][j] = s;
       }
+    cpx<R>* o = tab + (size_t)t * 16;
+    if (p.what == KT_CD) {  // C . D
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+          cpx<double> s = mk<double>(0.0, 0.0);
+          for (int m = 0; m < 4; ++m) s = s + Cb[i][m] * D[m][j];
+          o[i * 4 + j] = cvt<R>(s);
+        }
+      return;
+    }
     for (int i = 0; i < 4; ++i)  // T = D . C
       for (int j = 0; j < 4; ++j) {
         cpx<double> s = mk<double>(0.0, 0.0);
         for (int m = 0; m < 4; ++m) s = s + D[i][m] * Cb[m][j];
         T[i][j] = s;
       }
-    cpx<R>* o = tab + (size_t)t * 16;
+    if (p.what == KT_DC) {
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(T[i][j]);
+      return;
+    }
     for (int i = 0; i < 4; ++i)  // C . T
       for (int j = 0; j < 4; ++j) {
         cpx<double> s = mk<double>(0.0, 0.0);

@@ -439,7 +439,9 @@ def _check_path(method, reflection, npass, diffraction, norm):
     full = diffraction == np.inf
     if full and method != "4x4":
         raise NotImplementedError("diffraction = inf is built for the 4x4 method")
-    if reflection not in ((1, 2, 4) if method == "4x4" else (0, 1)) and not local and not full:
+    if method == "4x4" and reflection == 3 and diffraction == 0:
+        raise NotImplementedError("reflection mode 3 without diffraction (the reference has no such path)")
+    if reflection not in ((1, 2, 3, 4) if method == "4x4" else (0, 1)) and not local and not full:
         raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
 
     if method != "4x4" and npass != 1:
@@ -481,7 +483,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         raise NotImplementedError("optical data with more than one block is outside the GPU engine")
     if ret_bulk and method != "4x4":
         raise NotImplementedError("ret_bulk is implemented for the 4x4 method")
-    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf or reflection in (2, 4)):
+    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf or reflection in (2, 3, 4)):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
     ks = k0(wavelengths, pixelsize)
     cdt = torch.complex128 if precision == "double" else torch.complex64

@@ -1169,6 +1169,69 @@ def corrected_field_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1.0, 1
     return dotmm(cmat, dmat)
 
 
+def first_field_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0),
+                                   betamax=BETAMAX):
+    """D . C, both over d (dtmm/matrix.py:95-100)."""
+    dmat = field_diffraction_matrix(shape, ks, d, epsv, epsa, betamax=betamax)
+    cmat = correction_matrix(beta, phi, ks, d, epsv, epsa)
+    return dotmm(dmat, cmat)
+
+
+def second_field_diffraction_matrix(shape, ks, beta, phi, d=1.0, epsv=(1.0, 1.0, 1.0), epsa=(0.0, 0.0, 0.0),
+                                    betamax=BETAMAX):
+    """C . D, both over d (dtmm/matrix.py:102-107)."""
+    dmat = field_diffraction_matrix(shape, ks, d, epsv, epsa, betamax=betamax)
+    cmat = correction_matrix(beta, phi, ks, d, epsv, epsa)
+    return dotmm(cmat, dmat)
+
+
+def _transfer_ray_4x4_3(field, ks, layer, dmat1, dmat2, beta, phi, nsteps):
+    """Reflection mode 3 (dtmm/propagate_4x4.py:135-153): on the k-space
+    field, per step dmat1, to real space, F . P . F^-1 over the layer, back,
+    dmat2."""
+    d, epsv, epsa = layer
+    alpha, f, fi = alphaffi(beta, phi, epsv, epsa)
+    p = phasem(alpha, (ks * d)[..., None, None])
+    for _ in range(nsteps):
+        field = dotmf(dmat1, field)
+        field = ifft2(field)
+        field = dotmdmf(f, p, fi, field)
+        field = fft2(field)
+        field = dotmf(dmat2, field)
+    return field
+
+
+def propagate_4x4_effective_3(field, ks, layer, eff_layer, beta, phi, nsteps, diffraction, betamax):
+    """Reflection mode 3 with diffraction (dtmm/propagate_4x4.py:447-512):
+    C . D and D . C over half the effective layer around the voxels, per mode
+    window for diffraction > 1 (k-space field in and out)."""
+    d_eff, epsv_eff, epsa_eff = eff_layer
+    shape = field.shape[-2:]
+    if diffraction == 1:
+        dmat1 = second_field_diffraction_matrix(shape, ks, beta, phi, d_eff / 2, epsv_eff, epsa_eff, betamax=betamax)
+        dmat2 = first_field_diffraction_matrix(shape, ks, beta, phi, d_eff / 2, epsv_eff, epsa_eff, betamax=betamax)
+        return _transfer_ray_4x4_3(field, ks, layer, dmat1, dmat2, beta, phi, nsteps)
+    if diffraction < 1:
+        raise ValueError("Invalid diffraction value")
+    fout = np.zeros_like(field)
+    try:
+        broadcast_shape = beta.shape
+        beta = beta[..., 0]
+        phi = phi[..., 0]
+    except IndexError:
+        broadcast_shape = ()
+    windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), betax_off=beta * np.cos(phi),
+                                      betay_off=beta * np.sin(phi), betamax=betamax)
+    n = len(windows)
+    betas = betas.reshape((n,) + broadcast_shape)
+    phis = phis.reshape((n,) + broadcast_shape)
+    dmats1 = second_field_diffraction_matrix(shape, ks, betas, phis, d_eff / 2, epsv_eff, epsa_eff, betamax=betamax)
+    dmats2 = first_field_diffraction_matrix(shape, ks, betas, phis, d_eff / 2, epsv_eff, epsa_eff, betamax=betamax)
+    for window, b, p, dmat1, dmat2 in zip(windows, betas, phis, dmats1, dmats2):
+        fout = fout + _transfer_ray_4x4_3(field * window, ks, layer, dmat1, dmat2, b, p, nsteps)
+    return fout
+
+
 def _transfer_ray_4x4_4(field, ks, layer, beta, phi, nsteps, dmat):
     """Reflection mode 4 (dtmm/propagate_4x4.py:55-77): F . P . F^-1 over half
     the layer, the corrected field diffraction matrix, F . P . F^-1 again;
@@ -1257,8 +1320,6 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if reflection not in (1, 2, 3, 4):
         raise ValueError("Invalid reflection. The 4x4 method is either reflection mode 1 or 2.")
     full = diffraction == np.inf
-    if not full and reflection == 3:
-        raise NotImplementedError("oracle covers 4x4 reflection modes 1, 2 and 4, and diffraction = inf")
     if smooth < 0:
         smooth = 0.0
     if norm != DTMM_NORM_FFT:
@@ -1309,6 +1370,9 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
             _, (de, ee, ae) = eff_layers[j]
             if full:
                 field = propagate_4x4_full(field, ks, (thickness * direction, ev, ea), nsub, betamax)
+            elif reflection == 3:
+                field = propagate_4x4_effective_3(field, ks, (thickness * direction, ev, ea),
+                                                  (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             elif reflection == 4:
                 field = propagate_4x4_effective_4(field, ks, (thickness * direction, ev, ea),
                                                   (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)

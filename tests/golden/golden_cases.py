@@ -226,6 +226,22 @@ CASES = {
                                 illum=dict(jones=(1, 0)),
                                 transfer=dict(method="4x4", diffraction=1, reflection=2, npass=3, beta=0.0,
                                               phi=0.0)),
+    # reflection mode 3 (dtmm/propagate_4x4.py:135-153, :447-512): k-space,
+    # C . D and D . C field diffraction matrices around F P F^-1
+    "refl3_4x4_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                         material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=39,
+                         illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                         transfer=dict(method="4x4", diffraction=1, reflection=3, beta=0.1, phi=0.3)),
+    "refl3_4x4_d3_nstep2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                material=("twisted", dict(thickness=2.0)), seed=40,
+                                illum=dict(),
+                                transfer=dict(method="4x4", diffraction=3, reflection=3, nstep=2, beta=0.0,
+                                              phi=0.0)),
+    "refl3_4x4_d1_npass3": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=41,
+                                illum=dict(jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, reflection=3, npass=3, beta=0.0,
+                                              phi=0.0)),
     "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),

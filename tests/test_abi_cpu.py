@@ -66,7 +66,7 @@ def test_workspace_size_positive_for_valid_desc(lib):
 @pytest.mark.parametrize("field,value,needle", [
     ("method", 3, "method"),
     ("diffraction", 0, "diffraction"),
-    ("reflection", 3, "reflection"),
+    ("reflection", 5, "reflection"),
     ("height", 37, "factor"),
     ("width", 2 * 41, "factor"),
     ("npass", 0, "npass"),
@@ -85,7 +85,7 @@ def test_local_4x4_descriptor_rules(lib):
     """diffraction 0 is the per-voxel 4x4 transfer: reflection mode 2, npass 1 only."""
     ok = _desc(diffraction=0, reflection=2)
     assert lib.dtmm_transfer_workspace_size(ctypes.byref(ok)) > 0
-    for kw in (dict(diffraction=0, reflection=1), dict(diffraction=1, reflection=3)):
+    for kw in (dict(diffraction=0, reflection=1), dict(diffraction=0, reflection=3)):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
     # npass > 1 adds the between-pass projection buffers
     two = _desc(diffraction=0, reflection=2, npass=2)
@@ -117,9 +117,9 @@ def test_reflection4_descriptor_rules(lib):
     two_rays = _desc(diffraction=1, reflection=4, nray=2)
     assert lib.dtmm_transfer_workspace_size(ctypes.byref(two_rays)) == 0
     assert "one ray" in _lib.last_error()
-    assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(diffraction=1, reflection=3))) == 0
-    # reflection mode 2 with diffraction takes the same real-space path
-    assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(diffraction=1, reflection=2))) == s1
+    # reflection modes 2 and 3 with diffraction take the same real-space path
+    for r in (2, 3):
+        assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(diffraction=1, reflection=r))) == s1
 
 
 def test_transfer_rejects_small_workspace(lib):
