@@ -107,11 +107,9 @@ int check_desc(const dtmm_transfer_desc* d) {
   // any reflection mode: the reference takes the same path for all of them)
   const bool local4 = d->method == 4 && d->diffraction == 0 && (d->reflection == 2 || d->reflection == 4);
   const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
-  // reflection modes 2 and 4 with diffraction: real-space half steps around
-  // the corrected diffraction matrices (one ray: the matrices follow its beam)
+  // reflection modes 2-4 with diffraction: real-space steps around the
+  // corrected diffraction matrices (tables per ray: they follow its beam)
   const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
-  if (refl4 && d->nray != 1)
-    return fail(DTMM_ENOTSUP, "4x4 reflection modes 2-4 with diffraction are supported for one ray");
   if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
     return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
   if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
@@ -189,7 +187,9 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   // k-space table slots: entry / exit / projection tables (reused across
   // passes when they repeat) and the inter-layer diagonal tables
   L.nslots = passes ? 6 : 3;
-  L.slot_bytes = L.cplx * kt * (16 > 8 * (size_t)d->nray ? 16 : 8 * (size_t)d->nray);
+  // 4x4 tables (one per ray for the window / beam tables of reflection modes
+  // 2-4), the 2x2 exit table 4x2 per ray
+  L.slot_bytes = L.cplx * kt * std::max<size_t>(16 * (refl4 ? (size_t)d->nray : 1), 8 * (size_t)d->nray);
   L.slots = take(L.slot_bytes * L.nslots);
   L.ndslots = 2;
   L.dslot_bytes = L.cplx * kt * 2;
@@ -618,11 +618,15 @@ struct Engine {
     p.wzero = wzero();
     p.win = winp();
     const int n = d.nlam * d.height * d.width;
-    // the 2x2 exit table depends on the ray's windows: one slab per ray
-    const int rays = (what == KT_2OUT) ? d.nray : 1;
+    // the 2x2 exit table and the window / beam tables of reflection modes
+    // 2-4 depend on the ray's windows: one slab per ray
+    const bool per_ray = what == KT_2OUT || what == KT_WINMAT || what == KT_CFD || what == KT_CEPN ||
+                         what == KT_CD || what == KT_DC;
+    const int rays = per_ray ? d.nray : 1;
+    const size_t slab = (size_t)n * (what == KT_2OUT ? 8 : 16);
     for (int r = 0; r < rays; ++r) {
       p.ray = r;
-      k_ktab<R><<<(n + 127) / 128, 128, 0, st>>>(p, g, tab + (size_t)r * n * 8);
+      k_ktab<R><<<(n + 127) / 128, 128, 0, st>>>(p, g, tab + (size_t)r * slab);
       CKL("k_ktab");
     }
     return DTMM_OK;
@@ -751,6 +755,7 @@ struct Engine {
     p.ks = ks();
     p.beta = rbeta();
     p.phi = rphi();
+    p.bstride = 1;
     p.op = 0;
     return p;
   }
@@ -824,7 +829,8 @@ struct Engine {
     p.op = op;
     p.beta = wbeta() + w;
     p.phi = wphi() + w;
-    const dim3 grid((unsigned)((L.HW + 127) / 128), 1u);
+    p.bstride = L.nwin;
+    const dim3 grid((unsigned)((L.HW + 127) / 128), (unsigned)d.nray);
     k_local4<R><<<grid, 128, 0, st>>>(p, g, f, f, nullptr);
     CKL("k_local4");
     return DTMM_OK;
@@ -842,21 +848,22 @@ struct Engine {
   // same operators on the real-space field): C . D over ds/2, F P F^-1 over
   // ds, D . C over ds/2 (dtmm/propagate_4x4.py:135-153, :447-512).
   int refl_chain(Local4Params& p, int l, double ds, int w, cpx<R>* f) {
+    const size_t rs = (size_t)d.nlam * L.HW * 16;  // one 4x4 table per ray
     int rc;
     if (d.reflection == 3) {
       const cpx<R>* cd;
       const cpx<R>* dc;
       if ((rc = table(KT_CD, ds / 2, cd, w))) return rc;
-      if ((rc = diffract(f, f, cd))) return rc;
+      if ((rc = diffract(f, f, cd, rs))) return rc;
       if ((rc = local_step(p, l, ds, w, 0, f))) return rc;
       if ((rc = table(KT_DC, ds / 2, dc, w))) return rc;
-      return diffract(f, f, dc);
+      return diffract(f, f, dc, rs);
     }
     const bool two = d.reflection == 2;
     const cpx<R>* cfd;
     if ((rc = table(two ? KT_CEPN : KT_CFD, ds, cfd, w))) return rc;
     if ((rc = local_step(p, l, ds / 2, w, two ? 1 : 0, f))) return rc;
-    if ((rc = diffract(f, f, cfd))) return rc;
+    if ((rc = diffract(f, f, cfd, rs))) return rc;
     return local_step(p, l, ds / 2, w, two ? 2 : 0, f);
   }
 
@@ -876,7 +883,7 @@ struct Engine {
     for (int w = 0; w < L.nwin; ++w) {
       const cpx<R>* win;
       if ((rc = table(KT_WINMAT, 0.0, win, w))) return rc;
-      if ((rc = diffract(part, F, win))) return rc;
+      if ((rc = diffract(part, F, win, (size_t)d.nlam * L.HW * 16))) return rc;
       for (int s = 0; s < nst; ++s)
         if ((rc = refl_chain(p, l, ds, w, part))) return rc;
       if ((rc = axpby(acc, acc, nullptr, 1.0, part, nullptr, 1.0))) return rc;
@@ -1215,12 +1222,14 @@ struct Engine {
   }
 
   // f <- ifft2(P . fft2(src))
-  int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab) {
+  // ray_stride: elements between the tables of consecutive rays (0 = shared)
+  int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab, size_t ray_stride = 0) {
     int rc;
     const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
     if (f != src) CK(cudaMemcpyAsync(f, src, bytes, cudaMemcpyDeviceToDevice, st));
     if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
-    if ((rc = launch_col(f, P(L.U), 4, 4, KOP_MAT, Ptab, 1, nullptr, true, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_col(f, P(L.U), 4, 4, KOP_MAT, Ptab, 1, nullptr, true, true, 1.0 / d.height, ray_stride)))
+      return rc;
     if ((rc = launch_rows(P(L.U), 4, true, 1.0 / d.width))) return rc;
     CK(cudaMemcpyAsync(f, P(L.U), bytes, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;

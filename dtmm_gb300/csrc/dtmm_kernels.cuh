@@ -463,8 +463,9 @@ struct Local4Params {
   double d;           // sub-step thickness (pixels, signed by direction)
   int nst;            // sub-steps
   const double* ks;   // [lam]
-  const double* beta; // [ray]
-  const double* phi;  // [ray]
+  const double* beta; // [ray * bstride]
+  const double* phi;  // [ray * bstride]
+  int bstride;        // 1 for the rays' beams, the windows per ray for one window's beams
   // operator: 0 F . P . F^-1; 1 E . P . F^-1 and 2 F . P . E^-1 with E the
   // block matrix of the forward (rows/columns 0, 2) and backward (1, 3)
   // E parts (dtmm/tmm.py:974-996), the half steps of reflection mode 2
@@ -577,7 +578,7 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
     ev[0] = mk<double>(e[0], 0.0); ev[1] = mk<double>(e[1], 0.0); ev[2] = mk<double>(e[2], 0.0);
   }
   cpx<double> F[4][4], al[4], Fi[4][4];
-  local_fmat(p.beta[ray], p.phi[ray], ev, p.epsa[ao], p.epsa[ao + 1], p.epsa[ao + 2], F, al);
+  local_fmat(p.beta[ray * p.bstride], p.phi[ray * p.bstride], ev, p.epsa[ao], p.epsa[ao + 1], p.epsa[ao + 2], F, al);
   inv4(F, Fi);
   if (p.op != 0) {
     cpx<double> E[4][4];
@@ -1111,7 +1112,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   betaphi_k(g, ks, ky, kx, beta, phi);
   cpx<double> al[4], F[4][4], Fi[4][4];
   if (p.what == KT_WINMAT) {
-    // window w = proj_mode of ray 0: tent(beta_x) tent(beta_y), zero beyond betamax
+    // window w = proj_mode of ray p.ray: tent(beta_x) tent(beta_y), zero beyond betamax
     const int n = p.nwin_axis, w = p.proj_mode;
     double c = 1.0;
     if (n > 1) {
@@ -1124,8 +1125,8 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
       const double b = sqrt(bx * bx + by * by);
       c = 0.0;
       if (b < p.win.betamax)
-        c = tent((bx - (win_center(p.win, i) + p.win.xoff[0])) / p.win.step, xt) *
-            tent((by - (win_center(p.win, j) + p.win.yoff[0])) / p.win.step, yt);
+        c = tent((bx - (win_center(p.win, i) + p.win.xoff[p.ray])) / p.win.step, xt) *
+            tent((by - (win_center(p.win, j) + p.win.yoff[p.ray])) / p.win.step, yt);
     }
     cpx<R>* o = tab + (size_t)t * 16;
     for (int i = 0; i < 4; ++i)
@@ -1147,7 +1148,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
         for (int m = 0; m < 4; ++m) s = s + F[i][m] * pd[m] * Fi[m][j];
         D[i][j] = s;
       }
-    const int w = p.proj_mode;
+    const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;  // window of this ray
     iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
     inv4(Fb, Fbi);
     for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * dc));
@@ -1189,7 +1190,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   if (p.what == KT_CEPN) {
     iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
     const bool cut = beta >= p.betamax;
-    const int w = p.proj_mode;
+    const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;  // window of this ray
     cpx<double> alb[4], Fb[4][4];
     iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
     cpx<double> M[4][4];

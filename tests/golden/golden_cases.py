@@ -242,6 +242,22 @@ CASES = {
                                 illum=dict(jones=(1, 0)),
                                 transfer=dict(method="4x4", diffraction=1, reflection=3, npass=3, beta=0.0,
                                               phi=0.0)),
+    # reflection modes 2-4 with diffraction and several rays (tables per ray)
+    "refl4_4x4_d1_multiray": dict(shape=(10, 12), nlayers=2, wavelengths=[520.0, 600.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=42,
+                                  illum=dict(beta=[0.0, 0.15], phi=[0.0, 0.5], jones=(1, 0)),
+                                  transfer=dict(method="4x4", diffraction=1, reflection=4, multiray=True,
+                                                beta=[0.0, 0.15], phi=[0.0, 0.5])),
+    "refl2_4x4_d3_multiray": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=43,
+                                  illum=dict(beta=[0.0, 0.1], phi=[0.0, 1.0], jones=(1, 0)),
+                                  transfer=dict(method="4x4", diffraction=3, reflection=2, multiray=True,
+                                                beta=[0.0, 0.1], phi=[0.0, 1.0])),
+    "refl3_4x4_d1_multiray": dict(shape=(10, 10), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=44,
+                                  illum=dict(beta=[0.05, 0.2], phi=[0.3, -0.4]),
+                                  transfer=dict(method="4x4", diffraction=1, reflection=3, multiray=True,
+                                                beta=[0.05, 0.2], phi=[0.3, -0.4])),
     "nodiff_4x4_biaxial": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),
