@@ -57,17 +57,17 @@ MATERIALS = {
 }
 
 CASES = {
-    # BASELINE config 0 at full size: 64x64, 20 layers, 550 nm, 100 nm pixels
+    # the plain workload at full size: 64x64, 20 layers, 550 nm, 100 nm pixels
     "cfg0_4x4": dict(shape=(64, 64), nlayers=20, wavelengths=[550.0], pixelsize=100.0,
                      material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.2)), seed=0,
                      illum=dict(jones=(1, 0)),
                      transfer=dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)),
-    # BASELINE config 1 options (4x4, diffraction 3, npass 3, both polarisations) on a small grid
+    # the precision workload's options (4x4, diffraction 3, npass 3, both polarisations) on a small grid
     "cfg1_small": dict(shape=(24, 30), nlayers=4, wavelengths=[400.0, 600.0], pixelsize=50.0,
                        material=("twisted", dict(no=1.52, ne=1.71, amplitude=0.3)), seed=1,
                        illum=dict(),
                        transfer=dict(method="4x4", diffraction=3, npass=3, beta=0.0, phi=0.0)),
-    # BASELINE config 3 options (2x2, diffraction 5, no reflection) on a small grid
+    # the 2x2 workload's options (2x2, diffraction 5, no reflection) on a small grid
     "cfg3_small": dict(shape=(30, 24), nlayers=4, wavelengths=[450.0, 550.0, 650.0], pixelsize=100.0,
                        material=("inplane", dict(no=1.5, ne=1.6)), seed=3,
                        illum=dict(),
