@@ -1020,14 +1020,29 @@ def propagate_4x4_effective_1(field, ks, layer, eff_layer, beta, phi, nsteps, di
     raise ValueError("Invalid diffraction value")
 
 
-def _transfer_ray_2x2_1(fft_field, ks, layer, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat=None):
-    """2x2 E-only split step; ``tmat`` is the interface transmission applied
-    before the first step when reflections are on and no reflected waves are
-    tracked (dtmm/propagate_2x2.py:19-87)."""
+def _transfer_ray_2x2_1(fft_field, ks, layer, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat=None, rmat=None,
+                        refl=None):
+    """2x2 E-only split step (dtmm/propagate_2x2.py:19-87).  ``tmat`` is the
+    interface transmission applied before the first step when reflections
+    are on.  With tracked reflected waves (``refl``, npass > 1) the interface
+    also stores ``rmat`` times the incoming field in ``refl`` and adds the
+    wave stored there before; going backward (mode -1) the field past the
+    interface is added to ``bulk`` (E and H parts).  Returns the field, and
+    ``refl`` when it is tracked."""
     d, epsv, epsa = layer
-    if tmat is not None:
-        fft_field = dotmf(tmat, fft_field)
     alpha, fmat = alphaf(beta, phi, epsv, epsa)
+    if tmat is not None:
+        if refl is not None:
+            trans = refl.copy()
+            refl[...] = dotmf(rmat, fft_field)
+            fft_field = dotmf(tmat, fft_field) + trans
+            if mode == -1 and bulk is not None:
+                field = ifft2(fft_field)
+                e2h = E2H_mat(fmat, mode=mode)
+                bulk[..., ::2, :, :] += field
+                bulk[..., 1::2, :, :] += dotmf(e2h, field)
+        else:
+            fft_field = dotmf(tmat, fft_field)
     e = E_mat(fmat, mode=mode)
     ei = inv(e)
     p = phase_mat(alpha, (ks * d)[..., None, None], mode=mode)
@@ -1048,21 +1063,24 @@ def _transfer_ray_2x2_1(fft_field, ks, layer, dmat1, dmat2, beta, phi, nsteps, m
 
 
 def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, nsteps, diffraction, betamax, mode,
-                              bulk, reflection=0):
-    """(dtmm/propagate_2x2.py:193, no reflected-wave tracking, split_diffraction ignored)"""
+                              bulk, reflection=0, refl=None):
+    """(dtmm/propagate_2x2.py:193-284, split_diffraction ignored).  ``refl``:
+    the interface's tracked reflected wave (npass > 1), updated in place;
+    with windows each window's part of it enters that window's transfer and
+    the new reflections of the windows are summed."""
     d_out, epsv_out, epsa_out = eff_out
     shape = field.shape[-2:]
-    tmat = None
+    tmat = rmat = None
     if reflection:
-        tmat, _ = E_tr_matrix(shape, ks, epsv_in=eff_in[1], epsa_in=eff_in[2], epsv_out=epsv_out, epsa_out=epsa_out,
-                              mode=mode, betamax=betamax)
+        tmat, rmat = E_tr_matrix(shape, ks, epsv_in=eff_in[1], epsa_in=eff_in[2], epsv_out=epsv_out,
+                                 epsa_out=epsa_out, mode=mode, betamax=betamax)
     if diffraction <= 1:
         if diffraction == 1:
             dmat1 = first_E_diffraction_matrix(shape, ks, beta, phi, d_out / 2, epsv_out, epsa_out, mode, betamax)
             dmat2 = second_E_diffraction_matrix(shape, ks, beta, phi, d_out / 2, epsv_out, epsa_out, mode, betamax)
         else:
             dmat1 = dmat2 = None
-        return _transfer_ray_2x2_1(field, ks, layer_out, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat)
+        return _transfer_ray_2x2_1(field, ks, layer_out, dmat1, dmat2, beta, phi, nsteps, mode, bulk, tmat, rmat, refl)
     try:
         bshape = beta.shape
         b0, p0 = beta[..., 0], phi[..., 0]
@@ -1076,8 +1094,15 @@ def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, 
     dm1 = first_E_diffraction_matrix(shape, ks, betas, phis, d_out / 2, epsv_out, epsa_out, mode, betamax)
     dm2 = second_E_diffraction_matrix(shape, ks, betas, phis, d_out / 2, epsv_out, epsa_out, mode, betamax)
     fout = np.zeros_like(field)
+    new_refl = None if refl is None else np.zeros_like(refl)
     for w, b, p, m1, m2 in zip(windows, betas, phis, dm1, dm2):
-        fout = fout + _transfer_ray_2x2_1(field * w, ks, layer_out, m1, m2, b, p, nsteps, mode, bulk, tmat)
+        part = None if refl is None else refl * w
+        fout = fout + _transfer_ray_2x2_1(field * w, ks, layer_out, m1, m2, b, p, nsteps, mode, bulk, tmat, rmat,
+                                          part)
+        if refl is not None and reflection != 0:
+            new_refl = new_refl + part
+    if refl is not None:
+        refl[...] = new_refl
     return fout
 
 
@@ -1424,11 +1449,16 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
 
 def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
                  reflection, multiray, betamax, ret_bulk, out):
-    """2x2 interface sweep in k-space, one pass (dtmm/transfer.py:1009-1183)."""
+    """2x2 interface sweep in k-space (dtmm/transfer.py:1009-1183): npass
+    passes alternating in direction, the reflected wave of every interface
+    kept between passes (npass > 1, reflection 1); backward passes add the
+    field leaving the stack into the input field."""
     if reflection not in (0, 1, 2):
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
-    if reflection not in (0, 1) or npass != 1:
-        raise NotImplementedError("oracle covers 2x2 with reflection 0/1 and npass 1")
+    if reflection not in (0, 1):
+        raise NotImplementedError("oracle covers 2x2 with reflection 0/1")
+    if npass > 1 and reflection == 0:
+        raise ValueError("Reflection mode `0` not compatible with npass > 1")
     if ret_bulk:
         raise NotImplementedError("oracle covers ret_bulk for 4x4 only")
     field_in, wavelengths, pixelsize = field_data
@@ -1446,15 +1476,33 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if not (0 < diffraction < np.inf):
         raise NotImplementedError("oracle covers 0 < diffraction < inf for 2x2")
     field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
-    field = fft2(field0[..., ::2, :, :])
-    for j in range(n):
-        jout = j + 1
-        nsub, (thickness, ev, ea) = layers[jout]
-        _, eff_in = eff_layers[j]
-        _, (de, ee, ae) = eff_layers[jout]
-        bulk = field_out if jout == n else None
-        field = propagate_2x2_effective_1(field, ks, (thickness, ev, ea), eff_in, (de, ee, ae), beta, phi, nsub,
-                                          diffraction, betamax, +1, bulk, reflection)
+    field = field0[..., ::2, :, :].copy()
+    refl = None
+    if npass > 1:
+        field_in[...] = field0
+        refl = np.zeros((n + 1,) + field.shape[:-3] + (2,) + field.shape[-2:], CDTYPE)
+    field = fft2(field)
+    indices = list(range(n))
+    for i in range(npass):
+        if i > 0:
+            field = np.zeros_like(field)
+        direction = (-1) ** i
+        for j in indices:
+            jin = j + (1 - direction) // 2
+            jout = j + (1 + direction) // 2
+            nsub, (thickness, ev, ea) = layers[jout]
+            _, (di, ei_, ai) = eff_layers[jin]
+            _, (de, ee, ae) = eff_layers[jout]
+            if jout == 0:
+                bulk = field_in
+            elif jout == n:
+                bulk = field_out
+            else:
+                bulk = None
+            field = propagate_2x2_effective_1(field, ks, (thickness * direction, ev, ea), (di * direction, ei_, ai),
+                                              (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax,
+                                              direction, bulk, reflection, None if refl is None else refl[j])
+        indices.reverse()
     return field_out, wavelengths, pixelsize
 
 

@@ -265,6 +265,22 @@ CASES = {
 }
 
 
+# Cases the oracle is pinned on ahead of the engine (2x2 with npass > 1:
+# the reflected wave of every interface kept between passes); the GPU parity
+# tests do not run them.
+ORACLE_CASES = {
+    "twox2_npass3_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 600.0], pixelsize=100.0,
+                            material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=45,
+                            illum=dict(jones=(1, 0)),
+                            transfer=dict(method="2x2", diffraction=1, npass=3, beta=0.0, phi=0.0)),
+    "twox2_npass2_d3_offaxis": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                    material=("twisted", dict()), seed=46,
+                                    illum=dict(beta=0.1, phi=0.4),
+                                    transfer=dict(method="2x2", diffraction=3, reflection=1, npass=2, beta=0.1,
+                                                  phi=0.4)),
+}
+
+
 def build_optical_data(case):
     kind, kw = case["material"]
     return [MATERIALS[kind](case["shape"], case["nlayers"], case["seed"], **kw)]

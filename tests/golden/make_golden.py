@@ -23,12 +23,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from golden_cases import (CASES, ILLUM_CASES, ILLUM_WINDOW_CASES, POM_CASES, RAYS_CASES, TCMF_CASES,  # noqa: E402
+from golden_cases import (CASES, ORACLE_CASES, ILLUM_CASES, ILLUM_WINDOW_CASES, POM_CASES, RAYS_CASES, TCMF_CASES,  # noqa: E402
                           TCMF_TABLES, WINDOW_CASES, build_inputs, raised_cosine_window)
 
 
 def run_case(name, dtmm):
-    case = CASES[name]
+    case = CASES[name] if name in CASES else ORACLE_CASES[name]
     field_data, optical_data = build_inputs(case, dtmm.illumination_data)
     field_in = field_data[0]
     saved_in = field_in.copy()
@@ -258,7 +258,7 @@ def main(argv):
     import refload
 
     dtmm = refload.load_reference()
-    names = argv[1:] or (["kat", "illum"] + list(CASES) + ["pom", "director", "files", "qtensor", "illum_window",
+    names = argv[1:] or (["kat", "illum"] + list(CASES) + list(ORACLE_CASES) + ["pom", "director", "files", "qtensor", "illum_window",
                                                             "tcmf"])
     for name in names:
         if name == "kat":

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import dtmm_oracle as O
-from golden_cases import CASES, build_optical_data
+from golden_cases import CASES, ORACLE_CASES, build_optical_data
 
 GOLDEN_TOL = 1e-11
 
@@ -17,9 +17,9 @@ def rel_l2(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", sorted(CASES) + sorted(ORACLE_CASES))
 def test_oracle_matches_reference_transfer(name, golden):
-    case = CASES[name]
+    case = CASES[name] if name in CASES else ORACLE_CASES[name]
     z = golden(name)
     field_in = z["field_in"].copy()
     out = O.transfer_field((field_in, z["wavelengths"], float(z["pixelsize"])), build_optical_data(case),
