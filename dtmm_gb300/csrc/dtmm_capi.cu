@@ -112,6 +112,9 @@ int check_desc(const dtmm_transfer_desc* d) {
   const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
   if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
     return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
+  // the modal DFT kernels take one grid row per (image, component) line
+  if (full4 && (long long)d->nray * d->npol * d->nlam * 4 > 65535)
+    return fail(DTMM_ENOTSUP, "diffraction = inf is supported for at most 16383 images");
   if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
     return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2, or inf)");
   if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
