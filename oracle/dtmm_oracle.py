@@ -604,6 +604,45 @@ def tr_mat(fmatin, fmatout, fmatini=None, mode=+1):
     return dotmm(et, ei), dotmm(er, eri)
 
 
+def S_mat(fmatin, fmatout, fmatini=None, mode=+1):
+    """Transmission / reflection blocks of F_in^-1 . F_out (dtmm/tmm.py:850-878)."""
+    if fmatini is None:
+        fmatini = inv(fmatin)
+    S = dotmm(fmatini, fmatout)
+    if mode == +1:
+        return S[..., ::2, ::2], S[..., 1::2, 0::2]
+    return S[..., 1::2, 1::2], S[..., 0::2, 1::2]
+
+
+def Eti_mat(fmatin, fmatout, fmatini=None, mode=+1):
+    """Inverse E matrix through an interface without reflections (dtmm/tmm.py:999-1022)."""
+    Ai = inv(E_mat(fmatin, mode=mode))
+    St, _ = S_mat(fmatin, fmatout, fmatini=fmatini, mode=mode)
+    return dotmm(inv(St), Ai)
+
+
+def projection_mat(fmat, fmati=None, mode=+1):
+    """F . diag(forward or backward modes) . F^-1 (dtmm/tmm.py:742-768)."""
+    if fmati is None:
+        fmati = inv(fmat)
+    diag = np.zeros(fmat.shape[:-1], fmat.dtype)
+    if mode == 1:
+        diag[..., 0::2] = 1.0
+    else:
+        diag[..., 1::2] = 1.0
+    return dotmdm(fmat, diag, fmati)
+
+
+def transmitted_field_direct(field, beta, phi, n=1.0):
+    """The forward part of a field for one beam direction, in real space
+    (dtmm/transfer.py:94-101)."""
+    ev = refind2eps([n] * 3)
+    ea = np.zeros_like(ev)
+    alpha, fmat = alphaf(beta, phi, ev, ea)
+    pmat = projection_mat(fmat)
+    return np.moveaxis(dotmv(pmat, np.moveaxis(field, -3, -1)), -1, -3)
+
+
 def E_tr_matrix(shape, ks, epsv_in=(1.0, 1.0, 1.0), epsa_in=(0.0, 0.0, 0.0), epsv_out=(1.0, 1.0, 1.0),
                 epsa_out=(0.0, 0.0, 0.0), mode=+1, betamax=BETAMAX):
     """Per-k Fresnel t, r matrices between two homogeneous layers (dtmm/diffract.py:215)."""
@@ -1062,6 +1101,100 @@ def _transfer_ray_2x2_1(fft_field, ks, layer, dmat1, dmat2, beta, phi, nsteps, m
     return fft_field
 
 
+def _transfer_ray_2x2_2(field, ks, in_layer, out_layer, dmat, beta, phi, nsteps, mode, reflection, refl, bulk):
+    """2x2 reflection mode 2 on the real-space E field (dtmm/propagate_2x2.py:91-190):
+    per step E . P(d/2) . E^-1 halves around the corrected E matrix; at the
+    first step the per-voxel interface from the input layer (transmission
+    and reflection with tracked waves, or the inverse E matrix through the
+    interface without them).  Returns the field and the reflected wave."""
+    if in_layer is not None:
+        _, epsv_in, epsa_in = in_layer
+        _, fmat_in = alphaf(beta, phi, epsv_in, epsa_in)
+    d, epsv, epsa = out_layer
+    alpha, fmat = alphaf(beta, phi, epsv, epsa)
+    e = E_mat(fmat, mode=mode)
+    kd = ks * d / 2
+    p = phase_mat(alpha, kd[..., None, None], mode=mode)
+    ei0 = inv(e)
+    ei = ei0
+    for j in range(nsteps):
+        if j == 0 and reflection != 0:
+            if refl is not None:
+                tmat, rmat = tr_mat(fmat_in, fmat, mode=mode)
+                trans = refl.copy()
+                refl[...] = field - dotmf(tmat, field)  # in place, as the reference's out= writes
+                field = dotmf(tmat, field) + trans
+                if mode == -1 and bulk is not None:
+                    e2h = E2H_mat(fmat, mode=mode)
+                    bulk[..., ::2, :, :] += field
+                    bulk[..., 1::2, :, :] += dotmf(e2h, field)
+                field = dotmf(ei, field)
+                if d != 0.0:
+                    field = dotmf(e * p[..., None, :], field)
+                else:
+                    field = dotmf(e, field)
+                ei = ei0
+            else:
+                ei = Eti_mat(fmat_in, fmat, mode=mode)
+                field = dotmdmf(e, p, ei, field)
+                ei = ei0
+        else:
+            if d != 0.0:
+                field = dotmdmf(e, p, ei, field)
+        if dmat is not None:
+            field = diffract(field, dmat)
+        if d != 0.0:
+            field = dotmdmf(e, p, ei, field)
+    if mode == +1 and bulk is not None:
+        e2h = E2H_mat(fmat, mode=mode)
+        bulk[..., 1::2, :, :] += dotmf(e2h, field)
+        bulk[..., ::2, :, :] += field
+    return field, refl
+
+
+def propagate_2x2_effective_2(field, ks, layer_in, layer_out, eff_in, eff_out, beta, phi, nsteps, diffraction,
+                              reflection, betamax, mode, refl, bulk):
+    """(dtmm/propagate_2x2.py:286-377, split_diffraction ignored): one corrected
+    E matrix (diffraction 1), none (0), or n x n windows, each part (and its
+    part of the tracked reflected wave) taken to real space and through mode 2."""
+    shape = field.shape[-2:]
+    d_eff, epsv_eff, epsa_eff = eff_out
+    if diffraction <= 1:
+        dmat = corrected_E_diffraction_matrix(shape, ks, beta, phi, d=d_eff, epsv=epsv_eff, epsa=epsa_eff, mode=mode,
+                                              betamax=betamax) if diffraction else None
+        return _transfer_ray_2x2_2(field, ks, layer_in, layer_out, dmat, beta, phi, nsteps, mode, reflection, refl,
+                                   bulk)
+    fout = 0.0
+    ffield = fft2(field)
+    if refl is not None:
+        frefl = fft2(refl)
+        new_refl = 0.0
+    try:
+        bshape = beta.shape
+        beta = beta[..., 0]
+        phi = phi[..., 0]
+    except IndexError:
+        bshape = ()
+    windows, (betas, phis) = fft_mask(field.shape, ks, int(diffraction), betax_off=beta * np.cos(phi),
+                                      betay_off=beta * np.sin(phi), betamax=betamax)
+    n = len(windows)
+    betas = betas.reshape((n,) + bshape)
+    phis = phis.reshape((n,) + bshape)
+    dmats = corrected_E_diffraction_matrix(shape, ks, betas, phis, d=d_eff, epsv=epsv_eff, epsa=epsa_eff, mode=mode,
+                                           betamax=betamax)
+    for window, b, p, dmat in zip(windows, betas, phis, dmats):
+        fpart = ifft2(ffield * window)
+        rpart = None if refl is None else ifft2(frefl * window)
+        out, r = _transfer_ray_2x2_2(fpart, ks, layer_in, layer_out, dmat, b, p, nsteps, mode, reflection, rpart,
+                                     bulk)
+        fout = fout + out
+        if refl is not None and reflection != 0:
+            new_refl = new_refl + r
+    if refl is not None:
+        refl[...] = new_refl
+    return fout, refl
+
+
 def propagate_2x2_effective_1(field, ks, layer_out, eff_in, eff_out, beta, phi, nsteps, diffraction, betamax, mode,
                               bulk, reflection=0, refl=None):
     """(dtmm/propagate_2x2.py:193-284, split_diffraction ignored).  ``refl``:
@@ -1449,14 +1582,14 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
 
 def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
                  reflection, multiray, betamax, ret_bulk, out):
-    """2x2 interface sweep in k-space (dtmm/transfer.py:1009-1183): npass
-    passes alternating in direction, the reflected wave of every interface
-    kept between passes (npass > 1, reflection 1); backward passes add the
-    field leaving the stack into the input field."""
+    """2x2 interface sweep (dtmm/transfer.py:1009-1183): in k-space for
+    reflection 0 / 1 with 0 < diffraction < inf and for reflection 1, in real
+    space otherwise (reflection 2, or diffraction 0); npass passes alternating
+    in direction, the reflected wave of every interface kept between passes
+    (npass > 1); backward passes add the field leaving the stack into the
+    input field."""
     if reflection not in (0, 1, 2):
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
-    if reflection not in (0, 1):
-        raise NotImplementedError("oracle covers 2x2 with reflection 0/1")
     if npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
     if ret_bulk:
@@ -1473,15 +1606,20 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     else:
         out[...] = 0.0
         field_out = out
-    if not (0 < diffraction < np.inf):
-        raise NotImplementedError("oracle covers 0 < diffraction < inf for 2x2")
-    field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
+    if not (0 <= diffraction < np.inf):
+        raise NotImplementedError("oracle covers finite diffraction for 2x2")
+    if diffraction > 0:
+        field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
+    else:
+        field0 = transmitted_field_direct(field_in, beta, phi, n=nin)
     field = field0[..., ::2, :, :].copy()
     refl = None
     if npass > 1:
         field_in[...] = field0
         refl = np.zeros((n + 1,) + field.shape[:-3] + (2,) + field.shape[-2:], CDTYPE)
-    field = fft2(field)
+    work_in_fft = (reflection in (0, 1) and 0 < diffraction < np.inf) or reflection == 1
+    if work_in_fft:
+        field = fft2(field)
     indices = list(range(n))
     for i in range(npass):
         if i > 0:
@@ -1499,9 +1637,16 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                 bulk = field_out
             else:
                 bulk = None
-            field = propagate_2x2_effective_1(field, ks, (thickness * direction, ev, ea), (di * direction, ei_, ai),
-                                              (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax,
-                                              direction, bulk, reflection, None if refl is None else refl[j])
+            r = None if refl is None else refl[j]
+            if work_in_fft:
+                field = propagate_2x2_effective_1(field, ks, (thickness * direction, ev, ea),
+                                                  (di * direction, ei_, ai), (de * direction, ee, ae), beta, phi,
+                                                  nsub, diffraction, betamax, direction, bulk, reflection, r)
+            else:
+                _, (tin, evin, eain) = layers[jin]
+                field, _ = propagate_2x2_effective_2(field, ks, (tin, evin, eain), (thickness * direction, ev, ea),
+                                                     (di * direction, ei_, ai), (de * direction, ee, ae), beta, phi,
+                                                     nsub, diffraction, reflection, betamax, direction, r, bulk)
         indices.reverse()
     return field_out, wavelengths, pixelsize
 

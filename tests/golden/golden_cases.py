@@ -269,6 +269,20 @@ CASES = {
 # the reflected wave of every interface kept between passes); the GPU parity
 # tests do not run them.
 ORACLE_CASES = {
+    # 2x2 in real space: no diffraction (reflection resolves to 0), and
+    # reflection mode 2 with windows (dtmm/propagate_2x2.py:91-190, :286-377)
+    "twox2_d0": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                     material=("twisted", dict()), seed=47,
+                     illum=dict(beta=0.1, phi=0.3),
+                     transfer=dict(method="2x2", diffraction=0, beta=0.1, phi=0.3)),
+    "twox2_d3_refl2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                           material=("twisted", dict()), seed=48,
+                           illum=dict(jones=(1, 0)),
+                           transfer=dict(method="2x2", diffraction=3, reflection=2, beta=0.0, phi=0.0)),
+    "twox2_npass2_d3": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                            material=("twisted", dict()), seed=49,
+                            illum=dict(jones=(1, 0)),
+                            transfer=dict(method="2x2", diffraction=3, npass=2, beta=0.0, phi=0.0)),
     "twox2_npass3_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 600.0], pixelsize=100.0,
                             material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=45,
                             illum=dict(jones=(1, 0)),
