@@ -30,6 +30,17 @@ def test_oracle_matches_reference_transfer(name, golden):
     assert rel_l2(field_in, z["field_in_after"]) < GOLDEN_TOL
 
 
+def test_oracle_only_cases_are_separate_and_have_fixtures():
+    """Cases pinned ahead of the engine stay out of the GPU parity set and each
+    has its reference fixture."""
+    import os
+
+    assert not set(ORACLE_CASES) & set(CASES)
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    for name in list(CASES) + list(ORACLE_CASES):
+        assert os.path.exists(os.path.join(here, name + ".npz")), name
+
+
 def test_oracle_alphaf_biaxial_matches_reference(golden):
     """Biaxial voxels: the general eigen-solve and the Poynting sort give the
     reference's eigenvalues and field matrices (both call LAPACK; the rotated
