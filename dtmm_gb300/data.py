@@ -22,6 +22,57 @@ import numpy as np
 from . import _lib
 
 
+class EpsilonDispersive:
+    """Eps eigenvalues as a function of the wavelength, from per-voxel
+    coefficients (the reference's dispersive materials, dtmm/data.py:1124-1204).
+
+    ``values`` has a last axis of ``n`` coefficients after the three eigenvalue
+    axes: ``(..., 3, n)`` (e.g. ``(L, 3, n)`` per layer or ``(L, H, W, 3, n)``
+    per voxel); without values, ``shape`` and ``n`` give coefficients that
+    evaluate to eps 1.  Calling the object with a wavelength in nanometres
+    returns the eps values ``(..., 3)``; ``transfer_field`` evaluates it once
+    per wavelength with ``split_wavelengths=True``, as the reference requires.
+    """
+
+    def __init__(self, values=None, shape=None, n=None):
+        if values is None:
+            if shape is None or n is None:
+                raise ValueError("Coefficients were not set, so you need to provide n and shape parameters.")
+            c = np.zeros(tuple(shape) + (3, int(n)), np.float64)
+            c[..., 0] = 1.0
+            self.coefficients = c
+        else:
+            c = np.asarray(values, np.float64)
+            self.coefficients = np.broadcast_to(c, np.broadcast_shapes(c.shape, (3, c.shape[-1] if c.ndim else 1)))
+
+    def __getitem__(self, index):
+        return self.__class__(self.coefficients[index])
+
+
+class EpsilonCauchy(EpsilonDispersive):
+    """Cauchy dispersion: n = c0 + sum_i c_i / w^(2 i), eps = n^2, w in microns."""
+
+    def __call__(self, wavelength):
+        w = float(wavelength) / 1000.0
+        c = self.coefficients
+        n = np.array(c[..., 0])
+        for i in range(1, c.shape[-1]):
+            n = n + c[..., i] / w ** (2 * i)
+        return n * n
+
+
+class EpsilonSellmeier(EpsilonDispersive):
+    """Sellmeier dispersion: eps = c0 + sum_i c_(2i+1) w^2 / (w^2 - c_(2i+2)), w in microns."""
+
+    def __call__(self, wavelength):
+        w = float(wavelength) / 1000.0
+        c = self.coefficients
+        eps = np.array(c[..., 0])
+        for i in range((c.shape[-1] - 1) // 2):
+            eps = eps + (c[..., 1 + 2 * i] * w ** 2) / (w ** 2 - c[..., 2 + 2 * i])
+        return eps
+
+
 def _run(director, mask, no, ne, nhost, scale_factor):
     import torch
 

@@ -68,7 +68,8 @@ def k0(wavelength, pixelsize=1.0):
 def _validate_block(block, shape):
     thickness, material, angles = block
     if callable(material):
-        raise NotImplementedError("dispersive (callable) material data: use split_wavelengths=True")
+        # the reference's message for dispersive data outside split_wavelengths (dtmm/transfer.py:542-543)
+        raise ValueError("You are using dispersive data, so you must use `split_wavelengths=True`")
     thickness = np.asarray(thickness, np.float64)
     material = np.asarray(material)
     material = material.astype(np.complex128 if np.iscomplexobj(material) else np.float64, copy=False)
@@ -102,6 +103,31 @@ def validate_optical_data(data, shape):
     warnings.warn("A single-block optical data must be a list of length 1. Converting optical data to list. "
                   "In the future, exception will be raised.", DeprecationWarning)
     return validate_optical_data([data], shape)
+
+
+def is_optical_data_dispersive(optical_data):
+    """True when a block's eps values are a callable of the wavelength (dtmm/data.py:1116-1122)."""
+    blocks = optical_data if isinstance(optical_data, list) else [optical_data]
+    return any(callable(b[1]) for b in blocks)
+
+
+def evaluate_optical_data(optical_data, wavelength):
+    """Blocks with callable (dispersive) eps values evaluated at one wavelength in
+    nanometres (dtmm/data.py:684-693, as validate_optical_block does for
+    split_wavelengths, dtmm/data.py:575-586); other blocks are returned as they are."""
+    if not is_optical_data_dispersive(optical_data):
+        return optical_data
+    if np.ndim(wavelength) != 0:
+        raise ValueError("dispersive optical data is evaluated at one wavelength per transfer; "
+                         "use split_wavelengths=True")
+
+    def ev(b):
+        d, e, a = b
+        return (d, e(wavelength) if callable(e) else e, a)
+
+    if isinstance(optical_data, list):
+        return [ev(b) for b in optical_data]
+    return ev(optical_data)
 
 
 def _compact(a, full_shape):
@@ -613,43 +639,70 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
         raise NotImplementedError("split_layers is outside the GPU engine")
     field_in, wavelengths, pixelsize = field_data
     if split_wavelengths and not isinstance(field_in, tuple) and not ret_bulk:
+        # one transfer per wavelength, dispersive eps evaluated at it (dtmm/transfer.py:497-528);
+        # a given out passes its wavelength slice on (4x4 keeps its reflected part), without
+        # one every slice starts from zeros
         field_in = np.asarray(field_in)
-        out_field = np.empty_like(field_in) if out is None else out
+        out_field = np.zeros_like(field_in, dtype=np.complex128) if out is None else out
         for i in range(len(wavelengths)):
+            wl = np.asarray(wavelengths)[i]
             fi = field_in[..., i:i + 1, :, :, :]
             fcopy = np.array(fi)
-            r = transfer_field((fcopy, np.asarray(wavelengths)[i:i + 1], pixelsize), optical_data, beta, phi, nin,
-                               nout, npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
-                               split_rays, split_diffraction, False, False, eff_data, False, None, precision)
+            oi = None if out is None else out_field[..., i:i + 1, :, :, :]
+            r = transfer_field((fcopy, np.asarray([wl]), pixelsize), evaluate_optical_data(optical_data, float(wl)),
+                               beta, phi, nin, nout, npass, nstep, diffraction, reflection, method, multiray, norm,
+                               betamax, smooth, split_rays, split_diffraction, False, False, eff_data, False, oi,
+                               precision)
             out_field[..., i, :, :, :] = r[0][..., 0, :, :, :]
             if npass > 1:
                 field_in[..., i, :, :, :] = fcopy[..., 0, :, :, :]
         return out_field, wavelengths, pixelsize
     if isinstance(field_in, tuple):
+        # one transfer per tuple entry (dtmm/transfer.py:510-528); a scalar wavelength
+        # goes with a field that has no wavelength axis
         outs = []
         olist = out if out is not None else [None] * len(field_in)
         for f, wl, o in zip(field_in, wavelengths, olist):
-            r = transfer_field((f, [wl] if np.ndim(wl) == 0 else wl, pixelsize), optical_data, beta, phi, nin, nout,
+            od = evaluate_optical_data(optical_data, wl)
+            scalar = np.ndim(wl) == 0
+            if scalar:
+                f = np.asarray(f)[..., None, :, :, :]
+                o = None if o is None else np.asarray(o)[..., None, :, :, :]
+            r = transfer_field((f, [wl] if scalar else wl, pixelsize), od, beta, phi, nin, nout,
                                npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
                                split_rays, split_diffraction, False, False, eff_data, ret_bulk, o, precision)
+            if scalar:
+                r = (r[0][..., 0, :, :, :], wl, pixelsize)
             outs.append(r)
         return tuple(outs)
+    if is_optical_data_dispersive(optical_data):
+        raise ValueError("You are using dispersive data, so you must use `split_wavelengths=True`")
     if split_rays:
+        # ray by ray into the caller's out (its ray i, or [:, i] of a bulk), as
+        # dtmm/transfer.py:575-600; without out the result starts from zeros
         field_in = np.asarray(field_in)
         nrays = len(field_in)
-        res = np.empty((len(optical_data[0][0]) + 2,) + field_in.shape, np.complex128) if ret_bulk else \
-            (np.empty_like(field_in) if out is None else out)
+        given = out is not None
+        if given:
+            res = out
+        elif ret_bulk:
+            blocks = optical_data if isinstance(optical_data, list) else [optical_data]
+            res = np.zeros((len(np.atleast_1d(blocks[0][0])) + 2,) + field_in.shape, np.complex128)
+        else:
+            res = np.zeros_like(field_in, dtype=np.complex128)
         bl = [None] * nrays if beta is None else list(np.broadcast_to(beta, (nrays,)))
         pl = [None] * nrays if phi is None else list(np.broadcast_to(phi, (nrays,)))
         for i in range(nrays):
             fi = field_in[i]
+            o = (res[:, i] if ret_bulk else res[i]) if given else None
             r = _transfer_single(fi, wavelengths, pixelsize, optical_data, bl[i], pl[i], nin, nout, npass, nstep,
-                                 diffraction, reflection, method, False, norm, betamax, smooth, ret_bulk, None,
+                                 diffraction, reflection, method, False, norm, betamax, smooth, ret_bulk, o,
                                  precision)
-            if ret_bulk:
-                res[:, i] = r
-            else:
-                res[i] = r
+            if not given:
+                if ret_bulk:
+                    res[:, i] = r
+                else:
+                    res[i] = r
         return res, wavelengths, pixelsize
     res = _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
                            diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision)
@@ -657,4 +710,4 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
 
 
 __all__ = ["transfer_field", "plan_transfer", "DevicePlan", "DeviceMaterial", "set_precision", "DTMM_NORM_FFT",
-           "DTMM_NORM_REF"]
+           "DTMM_NORM_REF", "evaluate_optical_data", "is_optical_data_dispersive"]

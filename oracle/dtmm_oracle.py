@@ -1664,8 +1664,21 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     betamax = opt("betamax", betamax)
     if eff_data not in (0, "isotropic"):
         raise NotImplementedError("oracle covers isotropic effective data")
-    if split_rays or split_wavelengths or split_layers:
-        raise NotImplementedError("oracle covers unsplit transfer")
+    if split_rays or split_layers:
+        raise NotImplementedError("oracle covers unsplit transfer and split_wavelengths")
+    if split_wavelengths and not isinstance(field_data[0], tuple) and not ret_bulk:
+        # one transfer per wavelength with dispersive eps evaluated at it
+        # (dtmm/transfer.py:497-528, dtmm/data.py:575-586); each slice is a view,
+        # so the npass > 1 rewrite reaches the caller's field_in
+        field_in, wavelengths, pixelsize = field_data
+        out_field = np.empty_like(field_in) if out is None else out
+        for i, w in enumerate(np.asarray(wavelengths)):
+            od = [(d, e(w) if callable(e) else e, a) for d, e, a in optical_data]
+            r = transfer_field((field_in[..., i:i + 1, :, :, :], np.asarray([w]), pixelsize), od, beta, phi, nin,
+                               nout, npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
+                               False, split_diffraction, False, False, eff_data, False, None)
+            out_field[..., i, :, :, :] = r[0][..., 0, :, :, :]
+        return out_field, wavelengths, pixelsize
     if method == "4x4" and npass > 1 and diffraction == False:  # noqa: E712
         warnings.warn("The 4x4 method with diffraction disabled is not yet supported for input fields with beta >0.")
     if npass == -1 or npass == np.inf:

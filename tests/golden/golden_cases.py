@@ -48,11 +48,27 @@ def _biaxial(shape, nlayers, seed, absorbing=False):
     return d, epsv, epsa
 
 
+def _cauchy(shape, nlayers, seed):
+    """Dispersive twisted nematic: per-layer Cauchy coefficients (n = c0 + c1 / w^2,
+    w in microns) of slightly different ordinary / extraordinary indices."""
+    from dtmm_gb300.data import EpsilonCauchy
+
+    d, _, epsa = samples.twisted_nematic(shape, nlayers, seed=seed, amplitude=0.3)
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+    c = np.empty((nlayers, 3, 2))
+    c[:, :2, 0] = 1.49 + rng.uniform(0.0, 0.01, (nlayers, 1))
+    c[:, 2, 0] = 1.64 + rng.uniform(0.0, 0.01, nlayers)
+    c[:, :2, 1] = 0.0045
+    c[:, 2, 1] = 0.011
+    return d, EpsilonCauchy(c), epsa
+
+
 MATERIALS = {
     "twisted": _twisted,
     "biaxial": _biaxial,
     "inplane": lambda shape, nlayers, seed, **kw: samples.inplane_nematic(shape, nlayers, seed=seed, **kw),
     "absorbing": _absorbing,
+    "cauchy": _cauchy,
     "mixed": _mixed_voxels,
 }
 
@@ -113,6 +129,19 @@ CASES = {
                              material=("twisted", dict(thickness=2.0)), seed=14,
                              illum=dict(jones=(1, 0)),
                              transfer=dict(method="4x4", diffraction=3, nstep=2, beta=0.0, phi=0.0)),
+    # dispersive eps (Cauchy coefficients per layer) evaluated per wavelength under
+    # split_wavelengths; npass 1, because the reference's split path hands transfer_4x4
+    # an uninitialised out array whose reflected part npass > 1 would keep
+    "fourx4_cauchy_split": dict(shape=(16, 18), nlayers=3, wavelengths=[450.0, 550.0, 650.0], pixelsize=100.0,
+                                material=("cauchy", dict()), seed=16,
+                                illum=dict(jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, split_wavelengths=True,
+                                              beta=0.0, phi=0.0)),
+    "twox2_cauchy_split": dict(shape=(14, 16), nlayers=3, wavelengths=[480.0, 620.0], pixelsize=100.0,
+                               material=("cauchy", dict()), seed=17,
+                               illum=dict(beta=0.1, phi=0.5),
+                               transfer=dict(method="2x2", diffraction=1, split_wavelengths=True,
+                                             beta=0.1, phi=0.5)),
     "fourx4_bulk": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                         material=("twisted", dict()), seed=15,
                         illum=dict(jones=(1, 0)),

@@ -1,9 +1,9 @@
 """Generate the golden transfer_field fixtures from the unmodified reference.
 
-Run in the build container (where the reference tree is present):
+Run where a reference checkout is present, naming it in DTMM_REFERENCE_ROOT:
 
-    python tests/golden/make_golden.py            # all cases
-    python tests/golden/make_golden.py cfg0_4x4   # one case
+    DTMM_REFERENCE_ROOT=/root/reference python tests/golden/make_golden.py            # all cases
+    DTMM_REFERENCE_ROOT=/root/reference python tests/golden/make_golden.py cfg0_4x4   # one case
 
 Each case builds its inputs with the reference's own ``illumination_data``
 and the seeded director generators of ``dtmm_gb300.samples``, runs
@@ -27,9 +27,25 @@ from golden_cases import (CASES, ORACLE_CASES, ILLUM_CASES, ILLUM_WINDOW_CASES, 
                           TCMF_TABLES, WINDOW_CASES, build_inputs, raised_cosine_window)
 
 
+def reference_materials(optical_data, dtmm):
+    """The reference's own dispersive eps classes in place of the product's
+    (same coefficients), so that the fixture pins the reference's evaluation."""
+    from dtmm_gb300 import data as gdata
+
+    out = []
+    for d, e, a in optical_data:
+        if isinstance(e, gdata.EpsilonCauchy):
+            e = dtmm.data.EpsilonCauchy(np.array(e.coefficients))
+        elif isinstance(e, gdata.EpsilonSellmeier):
+            e = dtmm.data.EpsilonSellmeier(np.array(e.coefficients))
+        out.append((d, e, a))
+    return out
+
+
 def run_case(name, dtmm):
     case = CASES[name] if name in CASES else ORACLE_CASES[name]
     field_data, optical_data = build_inputs(case, dtmm.illumination_data)
+    optical_data = reference_materials(optical_data, dtmm)
     field_in = field_data[0]
     saved_in = field_in.copy()
     kwargs = dict(case["transfer"])

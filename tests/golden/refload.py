@@ -13,16 +13,26 @@ import tempfile
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("DTMM_REFERENCE_ROOT", "/root/reference")
 _SHIM = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_shim")
+
+
+def reference_root():
+    """The reference checkout named by ``DTMM_REFERENCE_ROOT`` (required: a
+    checkout elsewhere must not silently import nothing, or another dtmm)."""
+    root = os.environ.get("DTMM_REFERENCE_ROOT")
+    if not root:
+        raise ImportError("set DTMM_REFERENCE_ROOT to the reference checkout (the directory holding dtmm/) "
+                          "to generate golden fixtures")
+    if not os.path.isdir(os.path.join(root, "dtmm")):
+        raise ImportError("DTMM_REFERENCE_ROOT=%s holds no dtmm/ package" % root)
+    return root
 
 
 def load_reference():
     """Return the imported reference ``dtmm`` module (double precision)."""
     if "dtmm" in sys.modules:
         return sys.modules["dtmm"]
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "dtmm")):
-        raise ImportError("reference tree not found at %s" % REFERENCE_ROOT)
+    root = reference_root()
     sys.dont_write_bytecode = True
     os.environ.setdefault("DTMM_DOUBLE_PRECISION", "1")
     home = tempfile.mkdtemp(prefix="dtmm_home_")
@@ -30,7 +40,7 @@ def load_reference():
     os.environ["HOME"] = home
     if not hasattr(np, "alltrue"):
         np.alltrue = np.all
-    for p in (_SHIM, REFERENCE_ROOT):
+    for p in (_SHIM, root):
         if p not in sys.path:
             sys.path.insert(0, p)
     import dtmm  # noqa: E402
