@@ -120,7 +120,9 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
     return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
   if (d->method == 4 && d->reflection != 1 && !local4 && !full4 && !refl4)
-    return fail(DTMM_ENOTSUP, "4x4 supports reflection modes 1 and 4, and 2 without diffraction, on this path");
+    return fail(DTMM_ENOTSUP, "4x4 accepts reflection 1 with diffraction >= 1, 2-4 with diffraction >= 1, 2 and 4 "
+                              "with diffraction 0, and any mode with diffraction = inf (reflection %d, diffraction "
+                              "%d given)", d->reflection, d->diffraction);
   if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
     return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
@@ -1660,13 +1662,21 @@ int dtmm_transfer_noalloc(const dtmm_transfer_desc* desc, const dtmm_transfer_io
   g_err.clear();
   int rc = check_desc(desc);
   if (rc) return rc;
-  const size_t need = layout_of(desc).total;
-  if (need > DTMM_STATIC_SCRATCH_BYTES)
-    return fail(DTMM_ENOSPACE, "transfer needs %zu bytes of scratch; the static scratch holds %zu", need,
+  // npass > 1 caches every layer's operators when they fit the default limit;
+  // when that layout is too large for the static scratch, the two alternating
+  // operator buffers of the uncached schedule are tried (same results)
+  dtmm_transfer_desc dd = *desc;
+  Layout L = layout_of(&dd);
+  if (L.total > DTMM_STATIC_SCRATCH_BYTES && L.cache_ops) {
+    dd.op_cache_bytes = 1;
+    L = layout_of(&dd);
+  }
+  if (L.total > DTMM_STATIC_SCRATCH_BYTES)
+    return fail(DTMM_ENOSPACE, "transfer needs %zu bytes of scratch; the static scratch holds %zu", L.total,
                 (size_t)DTMM_STATIC_SCRATCH_BYTES);
   void* ws = nullptr;
   if ((rc = static_scratch(&ws))) return rc;
-  return transfer_impl(desc, io, ws, DTMM_STATIC_SCRATCH_BYTES, stream, nullptr, nullptr);
+  return transfer_impl(&dd, io, ws, DTMM_STATIC_SCRATCH_BYTES, stream, nullptr, nullptr);
 }
 
 int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,

@@ -34,7 +34,7 @@ extern "C" {
 #define DTMM_ENOTSUP (-4)     /* option combination outside this engine                 */
 
 /* diffraction = inf: every eigenwave below betamax through the voxels exactly
-   (dtmm/propagate_4x4.py:515-560); 4x4, npass 1 */
+   (dtmm/propagate_4x4.py:515-560); 4x4, any reflection mode, any npass */
 #define DTMM_DIFFRACTION_FULL (-1)
 
 #define DTMM_PRECISION_MIXED 0  /* complex64 bulk, FP64 eigen-solve and operator tables */
@@ -47,9 +47,12 @@ typedef struct dtmm_transfer_desc {
   int nlam, npol, nray;
   /* method and options (resolved by the caller as dtmm/transfer.py:433-465 does) */
   int method;        /* 4 = "4x4", 2 = "2x2"                                   */
-  int diffraction;   /* >= 1; n > 1 groups modes into n x n windows; 0 (4x4
-                        reflection 2) none; DTMM_DIFFRACTION_FULL = inf      */
-  int reflection;    /* 4x4: 1 ; 2x2: 0 or 1                                    */
+  int diffraction;   /* >= 1: n > 1 groups modes into n x n windows; 0: no
+                        diffraction (4x4 with reflection 2 or 4);
+                        DTMM_DIFFRACTION_FULL: inf (4x4)                     */
+  int reflection;    /* 4x4: 1 (diffraction >= 1), 2 and 4 (any diffraction),
+                        3 (diffraction >= 1), any with DTMM_DIFFRACTION_FULL;
+                        2x2: 0 or 1                                          */
   int npass;         /* 4x4: >= 1 ; 2x2: 1                                      */
   int precision;     /* DTMM_PRECISION_*                                        */
   double betamax, nin, nout, smooth;
@@ -128,10 +131,18 @@ const char* dtmm_last_error(void);
 size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc);
 
 /* Transfer the input field through the optical block: the work of
-   transfer_4x4 / transfer_2x2 (dtmm/transfer.py:618, :1009) for the
-   k-space ("effective", reflection mode 1 / 0-1) split-step method.
-   `stream` is a cudaStream_t (NULL = legacy default stream).  The call
-   enqueues the work and returns; results are ready when the stream is. */
+   transfer_4x4 / transfer_2x2 (dtmm/transfer.py:618, :1009) after option
+   resolution.  4x4: the k-space split step (reflection 1,
+   dtmm/propagate_4x4.py:376-444), the real-space reflection modes 2-4 with
+   diffraction (dtmm/propagate_4x4.py:18-287, :447-512), the per-voxel
+   transfer without diffraction (reflection 2 or 4) and the exact modal
+   transfer (DTMM_DIFFRACTION_FULL, dtmm/propagate_4x4.py:515-560), each
+   with any npass.  2x2: the k-space split step with reflection 0 or 1
+   (dtmm/propagate_2x2.py:19-87, :193-284), npass 1.  `stream` is a
+   cudaStream_t (NULL = legacy default stream).  The call enqueues the work
+   and returns; results are ready when the stream is.  The first call on a
+   stream creates that stream's side stream (kept for the process), on
+   which the per-layer operators run beside the transforms. */
 int dtmm_transfer(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, void* workspace,
                   size_t workspace_bytes, void* stream);
 
@@ -159,7 +170,11 @@ int dtmm_transfer_timed(const dtmm_transfer_desc* desc, const dtmm_transfer_io* 
      (cudaGetSymbolAddress) with that device current; make that first call
      before any stream capture.
    - Transfers whose workspace (dtmm_transfer_workspace_size) exceeds the
-     array are rejected with DTMM_ENOSPACE and a message giving both sizes.
+     array are rejected with DTMM_ENOSPACE and a message giving both sizes;
+     an npass > 1 transfer whose every-layer operator cache does not fit is
+     first retried with two alternating operator buffers (same results).
+   - The first call on a stream creates that stream's side stream, as
+     dtmm_transfer does; later calls on it create nothing.
    - Every call shares the one array: calls that overlap on the GPU (other
      streams, other host threads) race and must be serialised by the caller.
      No part of the scratch has to start at zero: every buffer is written
