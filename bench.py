@@ -159,25 +159,30 @@ def ncu_traffic():
 
 # ---------------------------------------------------------------------------
 def run_reference(args, rank):
+    """Reference arm: every step is one bounded sample of the workload (1 of the
+    60 layers, 1 of the 3 passes, the full grid, every wavelength and
+    polarisation) through the CPU restatement on all host cores; value and
+    ms_per_step are that sample's own, nothing is extrapolated."""
     if rank != 0:
         return
-    rates = []
+    times = []
     for i in range(args.warmup + args.steps):
         rate, cores, dt = cpu_sample_rate()
         if i >= args.warmup:
-            rates.append(rate)
-    value = float(np.median(rates))
-    sample = "1 of 60 layers, 1 of 3 passes, full 256x256 grid, 9 wavelengths, 2 polarisations per step"
-    upd = SHAPE[0] * SHAPE[1] * NLAYERS * len(WAVELENGTHS) * 2 * OPTS["npass"]
+            times.append(dt)
+    upd = SHAPE[0] * SHAPE[1] * len(WAVELENGTHS) * 2  # one layer, one pass
+    ms = float(np.mean(times)) * 1e3
+    value = upd / (ms / 1e3)
+    sample = ("each step: 1 of 60 layers x 1 of 3 passes of the workload (full 256x256 grid, 9 wavelengths, "
+              "2 polarisations) = %d updates" % upd)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": upd / value * 1e3, "ms_per_step_extrapolated": True,
-        "updates_per_step": upd, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": CONFIG,
+        "warmup": args.warmup, "ms_per_step": ms, "updates_per_step": upd, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "config": CONFIG,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "CPU restatement of the reference's algorithm (numpy/scipy, complex128); the reference's numba "
-                "path needs numba, which is not installed on this image",
+        "note": "CPU restatement of the reference's algorithm (numpy/scipy, complex128, oracle/dtmm_oracle.py); the "
+                "reference's numba path needs numba, which is not installed on this image",
     }))
 
 
@@ -390,15 +395,74 @@ def run_2x2(args, dev):
                                "%d layers, 100 nm pixels, wavelengths 450/550/650 nm, x+y polarisation, in-plane "
                                "nematic (16-mode azimuth, ne 1.6, no 1.5), complex64 bulk + FP64 eigen-solve" % nl,
                    "l2": "flushed between timed steps (256 MiB write); fields (100 MB) are near L2 size"},
-        "roofline": {"bound": "hbm", "achieved": bpu * upd / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": bpu * upd / (ms / 1e3) / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
-                     "kernel": "whole transfer (algorithmic bytes / step time)",
-                     "row_kernel_achieved": achieved_row,
+        "roofline": {"bound": "hbm", "achieved": achieved_row, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_row / peak, "traffic": None, "peak_source": peak_kind,
+                     "kernel": "k_layer_row_reg (2x2, 1024-point rows, 25 windows)",
+                     "bytes_per_update": bpu,
+                     "step_achieved": bpu * upd / (ms / 1e3) / 1e9,
                      "device_ms_per_step": {"layer_row": row_ms / args.steps,
                                             "layer_col": sum(k.layer_col_ms for k in kts) / args.steps,
                                             "voxel_op": sum(k.voxel_op_ms for k in kts) / args.steps}},
         "gpu_launches": sum(k.total_launches for k in kts), "clocks": clocks, "updates_per_step": upd,
     }
+
+
+# ---------------------------------------------------------------------------
+# the plain method: 4x4, diffraction 1, npass 1, 64x64, 20 layers, 550 nm
+# ---------------------------------------------------------------------------
+def run_plain(args, dev):
+    """The plain workload in complex128 (its stated precision) and mixed; one
+    step = one transfer replayed from a CUDA graph, L2 flushed between steps.
+    Launch-bound at this size (81,920 updates per step)."""
+    import torch
+
+    from dtmm_gb300 import illumination_data, samples
+    from dtmm_gb300.transfer import plan_transfer
+
+    shape, nl, wl = (64, 64), 20, [550.0]
+    fd = illumination_data(shape, wl, pixelsize=100.0, jones=(1, 0))
+    od = [samples.twisted_nematic(shape, nl, no=1.5, ne=1.7, amplitude=0.2, seed=0)]
+    opts = dict(method="4x4", diffraction=1, npass=1, beta=0.0, phi=0.0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    peak, peak_kind = measured_peaks()
+    out = {"workload": "transfer_field 4x4, diffraction 1, npass 1, 64x64 grid, 20 layers, 100 nm pixels, 550 nm, "
+                       "x polarisation, twisted nematic (no 1.5, ne 1.7, amp 0.2)"}
+    for prec in ("double", "mixed"):
+        plan = plan_transfer(fd[0].shape, fd[1], fd[2], od, precision=prec, device=dev, **opts)
+        fin = torch.from_numpy(fd[0]).to(dev).to(plan.dtype).contiguous()
+        fout = torch.empty_like(fin)
+        graph = plan.capture(fin, fout)
+        for _ in range(args.warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            graph.replay()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        kts = [plan.run(fin, fout, timed=True) for _ in range(2)]
+        ms = float(np.mean(times))
+        cb = 16 if prec == "double" else 8
+        bpu = 2 * 4 * cb + 48.0
+        row_ms = sum(k.layer_row_ms for k in kts) / sum(k.layer_row_launches for k in kts)
+        per_launch = shape[0] * shape[1]
+        achieved = bpu * per_launch / (row_ms / 1e3) / 1e9
+        out["c128" if prec == "double" else "mixed"] = {
+            "value": plan.updates / (ms / 1e3), "ms_per_step": ms,
+            "roofline": {"bound": "hbm", "kernel": "row pass (%s)" % ("k_layer_row" if prec == "double"
+                                                                      else "k_layer_row_reg"),
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "bytes_per_update": bpu, "peak_source": peak_kind},
+            "gpu_launches_per_step": kts[-1].total_launches}
+        del graph, plan, fin, fout
+    out["unit"] = UNIT
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -584,6 +648,42 @@ def run_serve(args, dev):
     }
 
 
+def _g(d, *keys):
+    for k in keys:
+        if not isinstance(d, dict) or k not in d:
+            return None
+        d = d[k]
+    return d
+
+
+def _r(x, n=4):
+    return None if x is None else float("%.*g" % (n, x))
+
+
+def summary(res):
+    """The line's key figures in a few hundred characters, printed last so that
+    a reader of the line's tail sees them: the headline and its kernel, the
+    complex128 comparison, the 2x2 and plain workloads, batch and serving."""
+    s = {"precision_mixed": {"value": _r(res.get("value")), "ms": _r(res.get("ms_per_step")),
+                             "row_frac": _r(_g(res, "roofline", "frac"), 3),
+                             "e2e": _r(_g(res, "e2e", "value"))},
+         "c128": {"value": _r(_g(res, "c128", "value")), "mixed_speedup": _r(_g(res, "c128", "mixed_speedup"), 3),
+                  "mixed_rel_l2_vs_c128": _r(_g(res, "c128", "mixed_rel_l2_vs_c128"), 3)},
+         "twox2": {"value": _r(_g(res, "twox2", "value")), "ms": _r(_g(res, "twox2", "ms_per_step")),
+                   "row_gbs": _r(_g(res, "twox2", "roofline", "achieved")),
+                   "row_frac": _r(_g(res, "twox2", "roofline", "frac"), 3),
+                   "row_ms": _r(_g(res, "twox2", "roofline", "device_ms_per_step", "layer_row")),
+                   "op_ms": _r(_g(res, "twox2", "roofline", "device_ms_per_step", "voxel_op"))},
+         "plain": {"c128": _r(_g(res, "plain", "c128", "value")), "mixed": _r(_g(res, "plain", "mixed", "value")),
+                   "c128_ms": _r(_g(res, "plain", "c128", "ms_per_step"))},
+         "batch": {"value": _r(_g(res, "batch", "value")), "e2e": _r(_g(res, "batch", "e2e", "value")),
+                   "launches": _g(res, "batch", "gpu_launches")},
+         "serve": {"rps": _r(_g(res, "serve", "requests_per_s")), "p50_ms": _r(_g(res, "serve", "latency_ms", "p50")),
+                   "p99_ms": _r(_g(res, "serve", "latency_ms", "p99"))},
+         "cpu": _r(_g(res, "cpu_baseline", "value"))}
+    return s
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -609,6 +709,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="precision workload: skip the serving summary")
     ap.add_argument("--rows", default="all",
                     help="rows workload: comma list of pom_image, diffract, director2data, q2data (default all)")
+    ap.add_argument("--no-2x2", action="store_true", help="precision workload: skip the 2x2 workload summary")
+    ap.add_argument("--no-plain", action="store_true", help="precision workload: skip the plain workload summary")
     ap.add_argument("--no-rows", action="store_true",
                     help="precision workload: skip the POM / refocus / director / Q-tensor kernel summary")
     args = ap.parse_args()
@@ -825,12 +927,31 @@ def main():
         except Exception as e:
             result["rows"] = {"error": "%s: %s" % (type(e).__name__, e)}
         torch.cuda.empty_cache()
+    if rank == 0 and not args.no_2x2:
+        try:
+            a2 = copy.copy(args)
+            a2.steps, a2.warmup, a2.layers = 5, 3, NLAYERS
+            t2 = run_2x2(a2, dev)
+            result["twox2"] = {k: t2[k] for k in ("value", "ms_per_step", "config", "roofline", "gpu_launches",
+                                                   "clocks", "updates_per_step") if k in t2}
+        except Exception as e:
+            result["twox2"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_plain:
+        try:
+            a2 = copy.copy(args)
+            a2.steps, a2.warmup = 20, 5
+            result["plain"] = run_plain(a2, dev)
+        except Exception as e:
+            result["plain"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu and world == 1:
         rate, cores, dt = cpu_sample_rate()
         result["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                   "sample": "1 of 60 layers, 1 of 3 passes, full 256x256 grid, 9 wavelengths, "
                                             "2 polarisations (%.1f s of CPU work)" % dt}
     if rank == 0:
+        result["summary"] = summary(result)
         print(json.dumps(result))
     if dist is not None:
         dist.destroy_process_group()
