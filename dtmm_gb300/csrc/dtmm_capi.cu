@@ -91,6 +91,9 @@ struct Layout {
   size_t fbeta, fphi, fmodes;  // diffraction = inf: per-wavelength grid beta / phi, sorted modes + counts
   size_t fA, famp;             // diffraction = inf: row DFTs and mode amplitudes (FP64)
   size_t r4part;               // reflection mode 4 with windows: the window's part of the field
+  size_t r2in, r2out, y2;      // 2x2 k-space, npass > 1: reflected waves of the outer interfaces, exit state
+  size_t r2;                   // 2x2 real space, npass > 1: reflected wave of every interface
+  size_t w2;                   // 2x2 real space with windows: window part, sum, reflected part and sum
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -115,25 +118,40 @@ int check_desc(const dtmm_transfer_desc* d) {
   // the modal DFT kernels take one grid row per (image, component) line
   if (full4 && (long long)d->nray * d->npol * d->nlam * 4 > 65535)
     return fail(DTMM_ENOTSUP, "diffraction = inf is supported for at most 16383 images");
-  if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4))
-    return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2, or inf)");
+  // 2x2 without diffraction: real space (reflection 0 or 2) or k-space with
+  // the interfaces' betamax cut only (reflection 1)
+  const bool nodiff2 = d->method == 2 && d->diffraction == 0;
+  if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4 && !nodiff2))
+    return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2 or 4, or "
+                              "with 2x2; inf with 4x4)");
   if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
     return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
   if (d->method == 4 && d->reflection != 1 && !local4 && !full4 && !refl4)
     return fail(DTMM_ENOTSUP, "4x4 accepts reflection 1 with diffraction >= 1, 2-4 with diffraction >= 1, 2 and 4 "
                               "with diffraction 0, and any mode with diffraction = inf (reflection %d, diffraction "
                               "%d given)", d->reflection, d->diffraction);
-  if (d->method == 2 && d->reflection != 0 && d->reflection != 1)
-    return fail(DTMM_ENOTSUP, "2x2 supports reflection modes 0 and 1 on this path");
+  if (d->method == 2 && (d->reflection < 0 || d->reflection > 2))
+    return fail(DTMM_EINVAL, "Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.");
   if (d->npass < 1) return fail(DTMM_EINVAL, "npass must be >= 1");
-  if (d->method == 2 && d->npass != 1) return fail(DTMM_ENOTSUP, "2x2 supports npass = 1 on this path");
+  if (d->method == 2 && d->npass > 1 && d->reflection == 0)
+    return fail(DTMM_EINVAL, "Reflection mode `0` not compatible with npass > 1");
+  // the reference's tracked reflection step applies its first diffraction
+  // matrix, which it does not form without diffraction (dtmm/propagate_2x2.py:61)
+  if (d->method == 2 && d->npass > 1 && d->reflection == 1 && d->diffraction == 0)
+    return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction is not supported with npass > 1 (the "
+                              "reference's tracked reflections need diffraction matrices)");
   if (d->precision != DTMM_PRECISION_MIXED && d->precision != DTMM_PRECISION_DOUBLE)
     return fail(DTMM_EINVAL, "unknown precision");
   if (d->nlayers < 1) return fail(DTMM_EINVAL, "no layers");
   if (!d->thickness || !d->nstep || !d->ks || !d->beta || !d->phi) return fail(DTMM_EINVAL, "null host array");
   if (!d->epsv || !d->epsa) return fail(DTMM_EINVAL, "null material pointer");
-  for (int l = 0; l < d->nlayers; ++l)
+  for (int l = 0; l < d->nlayers; ++l) {
     if (d->nstep[l] < 1) return fail(DTMM_EINVAL, "nstep must be >= 1");
+    // the k-space sweep cuts every step at betamax; the reference's sub-steps
+    // without diffraction matrices do not
+    if (nodiff2 && d->reflection == 1 && d->nstep[l] > 1)
+      return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction supports nstep = 1");
+  }
   FFTPlan p;
   if (!make_plan(d->height, p) || !make_plan(d->width, p))
     return fail(DTMM_ENOTSUP, "grid sides must factor into primes up to 31 (got %dx%d)", d->height, d->width);
@@ -141,6 +159,11 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->row_group < 0 || d->col_tile < 0 || d->fft_schedule < 0 || d->fft_schedule > 3)
     return fail(DTMM_EINVAL, "invalid tuning fields");
   return DTMM_OK;
+}
+
+// 2x2 in real space: reflection mode 2, or no diffraction without reflections
+bool is_real2(const dtmm_transfer_desc* d) {
+  return d->method == 2 && (d->reflection == 2 || (d->diffraction == 0 && d->reflection == 0));
 }
 
 Layout layout_of(const dtmm_transfer_desc* d) {
@@ -176,6 +199,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
     L.fA = take(16 * NI * 4 * L.HW);
     L.famp = take(16 * NI * 4 * L.HW);
   }
+  const bool real2 = is_real2(d);
   if (real_space && d->npass == 1 && !refl4) {  // the per-voxel / modal sweep alone needs nothing more
     L.total = off;
     return L;
@@ -188,10 +212,10 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.cx = take(rsz * d->nray * L.nx * d->nlam * W);
   L.cy = take(rsz * d->nray * L.ny * d->nlam * H);
   const size_t kt = (size_t)d->nlam * L.HW;
-  const bool passes = d->method == 4 && d->npass > 1;
+  const bool passes = d->npass > 1;
   // k-space table slots: entry / exit / projection tables (reused across
   // passes when they repeat) and the inter-layer diagonal tables
-  L.nslots = passes ? 6 : 3;
+  L.nslots = passes ? (d->method == 2 ? 8 : 6) : (real2 ? 4 : 3);
   // 4x4 tables (one per ray for the window / beam tables of reflection modes
   // 2-4), the 2x2 exit table 4x2 per ray
   L.slot_bytes = L.cplx * kt * std::max<size_t>(16 * (refl4 ? (size_t)d->nray : 1), 8 * (size_t)d->nray);
@@ -203,7 +227,7 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.F = take(field);
   L.X = take(field);
   L.U = take(field * (size_t)(L.ny > 1 ? L.ny : 1));
-  L.field0 = take(passes ? field : 0);
+  L.field0 = take(passes && d->method == 4 ? field : 0);
   L.chains = false;
   if (L.nwin > 1)
     for (int l = 0; l < d->nlayers; ++l)
@@ -211,7 +235,15 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.Xw = take(L.chains ? field : 0);
   L.Xa = take(L.chains ? field : 0);
   L.r4part = take(refl4 && L.nwin > 1 ? field : 0);  // reflection mode 4: one window's part
-  L.op_one = real_space ? 0 : L.cplx * nrw * OP_REC * L.HW;  // the real-space paths keep no operator records
+  const size_t field2 = field / 2;
+  const bool kpass2 = d->method == 2 && !real2 && passes;
+  L.r2in = take(kpass2 ? field2 : 0);
+  L.r2out = take(kpass2 ? field2 : 0);
+  L.y2 = take(kpass2 ? field2 : 0);
+  L.r2 = take(real2 && passes ? field2 * (size_t)(d->nlayers + 1) : 0);
+  L.w2 = take(real2 && L.nwin > 1 ? 4 * field2 : 0);
+  // the real-space paths keep no operator records
+  L.op_one = (real_space || real2) ? 0 : L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
   // per-layer cache, or two buffers that alternate between the layer being
@@ -622,19 +654,47 @@ struct Engine {
     p.wphi = wphi();
     p.wzero = wzero();
     p.win = winp();
+    // 2x2 tables: proj_mode carries the mode (and for KT_2CE the window, 2 w +
+    // (mode < 0)); entry interfaces go from the input medium into the effective
+    // one, exit interfaces from the effective medium into the output medium
+    // (forward) or back into the input medium (backward)
+    p.mode = 1;
+    p.ta = 1;
+    p.tb = 0;
+    // without diffraction the input is projected for the beam direction first
+    // (transmitted_field_direct, dtmm/transfer.py:1075-1078)
+    p.proj_in = d.diffraction > 0 ? 1 : 0;
+    if (what == KT_2E || what == KT_2TE || what == KT_2R || what == KT_2OUT || what == KT_2X) {
+      p.mode = proj_mode < 0 ? -1 : 1;
+      p.ta = 0;
+      p.tb = p.mode > 0 ? 2 : 1;
+    } else if (what == KT_2CE) {
+      p.mode = (proj_mode & 1) ? -1 : 1;
+      p.proj_mode = proj_mode >> 1;
+    }
     const int n = d.nlam * d.height * d.width;
-    // the 2x2 exit table and the window / beam tables of reflection modes
-    // 2-4 depend on the ray's windows: one slab per ray
+    // the exit / reflection tables and the window / beam tables depend on the
+    // ray's windows: one slab per ray
     const bool per_ray = what == KT_2OUT || what == KT_WINMAT || what == KT_CFD || what == KT_CEPN ||
-                         what == KT_CD || what == KT_DC;
+                         what == KT_CD || what == KT_DC || what == KT_2RIN || what == KT_2R || what == KT_2X ||
+                         what == KT_2CE || what == KT_2WIN;
     const int rays = per_ray ? d.nray : 1;
-    const size_t slab = (size_t)n * (what == KT_2OUT ? 8 : 16);
+    const size_t slab = (size_t)n * ktab_entries(what);
     for (int r = 0; r < rays; ++r) {
       p.ray = r;
       k_ktab<R><<<(n + 127) / 128, 128, 0, st>>>(p, g, tab + (size_t)r * slab);
       CKL("k_ktab");
     }
     return DTMM_OK;
+  }
+
+  // complex entries of one k-space table per (lam, ky, kx)
+  static int ktab_entries(int what) {
+    switch (what) {
+      case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
+      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: return 4;
+      default: return 16;
+    }
   }
 
   // table of kind `what` for thickness dd (medium eps_re for projections),
@@ -654,9 +714,7 @@ struct Engine {
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
     int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
-             : (what == KT_WINMAT || what == KT_CFD || what == KT_CEPN || what == KT_CD || what == KT_DC)
-                 ? launch_ktab(what, dd, dst, proj_mode)
-                                                     : launch_ktab(what, dd, dst);
+                               : launch_ktab(what, dd, dst, proj_mode);
     if (rc) return rc;
     sl[pick].what = what;
     sl[pick].d = dd;
@@ -668,6 +726,10 @@ struct Engine {
   }
 
   const cpx<R>* kdiag_cur = nullptr;
+  // thickness factor of the diagonal tables between sub-steps: the pass
+  // direction (4x4: the backward modes' phase follows the signed thickness);
+  // 2x2: 1 (the e+ entry serves both directions), 0 without diffraction
+  double kdir = 1.0;
   // (e+, e-) table of the merged half steps
   int diag_table(double dd) { return table(KT_DIAG, dd, kdiag_cur); }
 
@@ -709,7 +771,9 @@ struct Engine {
     p.wsin = wsin();
     p.waw = waw();
     p.nwin = L.nwin;
-    p.four = d.method == 4;
+    // both mode blocks for 4x4, and for 2x2 passes that alternate in direction
+    p.four = d.method == 4 || d.npass > 1;
+    p.uncorrected = d.method == 2 && d.diffraction == 0;
     p.nray = d.nray;
     // every ray of a voxel in one thread (its trigonometry computed once)
     // while that still leaves at least 4 blocks per SM
@@ -1066,7 +1130,7 @@ struct Engine {
         if (s == 0) {
           if ((rc = launch_col(in, U, cin, C, kop0, ktab0, L.ny, cy, true, true, 1.0, ktab0_ray))) return rc;
         } else {
-          if ((rc = diag_table(dir * ds))) return rc;
+          if ((rc = diag_table(kdir * ds))) return rc;
           if ((rc = launch_col(X, U, C, C, KOP_DIAG, kdiag_cur, 1, nullptr, true, true, 1.0))) return rc;
         }
         if ((rc = launch_row(U, X, op, dir))) return rc;
@@ -1083,7 +1147,7 @@ struct Engine {
         if (s == 0) {
           if ((rc = launch_col(in, U, cin, C, kop0, ktab0, 1, cy, true, true, 1.0, ktab0_ray, j))) return rc;
         } else {
-          if ((rc = diag_table(dir * ds))) return rc;
+          if ((rc = diag_table(kdir * ds))) return rc;
           if ((rc = launch_col(Xw, U, C, C, KOP_DIAG, kdiag_cur, 1, nullptr, true, true, 1.0))) return rc;
         }
         if ((rc = launch_row(U, dst, op, dir, w, s == 0, s + 1 == nst && w > 0))) return rc;
@@ -1151,6 +1215,7 @@ struct Engine {
   // state F (real space, 4 components) -> propagated through all layers -> F
   int sweep4(int pass, cpx<R>* bulk) {
     const double dir = (pass % 2 == 0) ? 1.0 : -1.0;
+    kdir = dir;
     std::vector<int> order;
     layer_order(pass % 2 == 0 ? 1 : -1, order);
     cpx<R>* F = P(L.F);
@@ -1228,21 +1293,22 @@ struct Engine {
 
   // f <- ifft2(P . fft2(src))
   // ray_stride: elements between the tables of consecutive rays (0 = shared)
-  int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab, size_t ray_stride = 0) {
+  int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab, size_t ray_stride = 0, int C = 4) {
     int rc;
-    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * C * L.HW;
     if (f != src) CK(cudaMemcpyAsync(f, src, bytes, cudaMemcpyDeviceToDevice, st));
-    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
-    if ((rc = launch_col(f, P(L.U), 4, 4, KOP_MAT, Ptab, 1, nullptr, true, true, 1.0 / d.height, ray_stride)))
+    if ((rc = launch_rows(f, C, false, 1.0))) return rc;
+    if ((rc = launch_col(f, P(L.U), C, C, KOP_MAT, Ptab, 1, nullptr, true, true, 1.0 / d.height, ray_stride)))
       return rc;
-    if ((rc = launch_rows(P(L.U), 4, true, 1.0 / d.width))) return rc;
+    if ((rc = launch_rows(P(L.U), C, true, 1.0 / d.width))) return rc;
     CK(cudaMemcpyAsync(f, P(L.U), bytes, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;
   }
 
-  int axpby(cpx<R>* out, const cpx<R>* x, const double* ax, double sx, const cpx<R>* y, const double* by, double sy) {
-    const size_t n = (size_t)NI * 4 * L.HW;
-    k_axpby<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, x, ax, sx, y, by, sy, g, 4);
+  int axpby(cpx<R>* out, const cpx<R>* x, const double* ax, double sx, const cpx<R>* y, const double* by, double sy,
+            int C = 4) {
+    const size_t n = (size_t)NI * C * L.HW;
+    k_axpby<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, x, ax, sx, y, by, sy, g, C);
     CKL("k_axpby");
     return DTMM_OK;
   }
@@ -1316,6 +1382,21 @@ struct Engine {
     return DTMM_OK;
   }
 
+  // byte offset of the backward-mode records in a voxel's operator records
+  size_t back_records() const { return (size_t)7 * L.HW * (real_ops() ? sizeof(R) : sizeof(cpx<R>)); }
+
+  // 2x2 method in k-space (reflection 0 or 1; dtmm/propagate_2x2.py:19-87,
+  // :193-284 driven by dtmm/transfer.py:1074-1183) over npass passes that
+  // alternate in direction.  The inner interfaces join identical effective
+  // media (t = 1, r = 0 within betamax), so with npass > 1 only the reflected
+  // waves of the two outer interfaces are kept between passes, x-transformed
+  // ([image][2][H][W], rows along x in k-space): each pass after the first
+  // enters the stack with the wave its entry interface reflected in the
+  // previous pass; forward passes add the field leaving the stack to
+  // field_out, backward passes to field_in, which first becomes the input's
+  // forward part (dtmm/transfer.py:1075-1080).  Without diffraction
+  // (reflection 1) the voxels' operators are the plain E P E^-1 and the
+  // k-space steps only the interfaces' betamax cut.
   int run2() {
     int rc;
     cpx<R>* fin = (cpx<R>*)io.field_in;
@@ -1323,55 +1404,259 @@ struct Engine {
     cpx<R>* F = P(L.F);
     cpx<R>* U = P(L.U);
     const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
-    std::vector<int> order;
-    layer_order(1, order);
-    CK(cudaMemcpyAsync(F, fin, bytes4, cudaMemcpyDeviceToDevice, st));
-    std::vector<double> dsub(order.size());
-    for (size_t q = 0; q < order.size(); ++q) dsub[q] = d.thickness[order[q]] / d.nstep[order[q]];
-    OpFeed feed;
-    if ((rc = feed_begin(0, order, dsub, feed))) return rc;
-    if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
-    const cpx<R>* cur = F;
-    int cin = 4;
-    double dprev = 0.0;
-    for (size_t q = 0; q < order.size(); ++q) {
-      const int l = order[q];
-      const int nst = d.nstep[l];
-      const double ds = dsub[q];
-      const void* op;
-      if ((rc = feed_get(0, q, order, dsub, feed, op))) return rc;
-      int kop;
-      const void* ktab;
-      if (q == 0) {
-        // entry: transmitted part in n_in, interface n_in -> effective, half step
-        const cpx<R>* t1;
-        if ((rc = table(KT_2IN, ds / 2, t1))) return rc;
-        kop = KOP_MAT;
-        ktab = t1;
-      } else {
-        if ((rc = diag_table(0.5 * (dprev + ds)))) return rc;
-        kop = KOP_DIAG;
-        ktab = kdiag_cur;
-      }
-      cpx<R>* out = nullptr;
-      if ((rc = layer(cur, cin, kop, ktab, 0, out, op, 1.0, nst, ds))) return rc;
-      if ((rc = feed_done(q, feed))) return rc;
-      if (out != P(L.X) && q + 1 < order.size() && L.chains) {
-        CK(cudaMemcpyAsync(P(L.X), out, sizeof(cpx<R>) * (size_t)NI * 2 * L.HW, cudaMemcpyDeviceToDevice, st));
-        out = P(L.X);
-      }
-      cur = out;
-      cin = 2;
-      dprev = ds;
+    const size_t bytes2 = bytes4 / 2;
+    const int npass = d.npass;
+    const double hd = d.diffraction == 0 ? 0.0 : 1.0;  // half steps of the effective medium
+    const size_t ray8 = (size_t)d.nlam * L.HW * 8, ray4 = (size_t)d.nlam * L.HW * 4;
+    const double ih = 1.0 / d.height, iw = 1.0 / d.width;
+    cpx<R>* Rin = npass > 1 ? P(L.r2in) : nullptr;
+    cpx<R>* Rout = npass > 1 ? P(L.r2out) : nullptr;
+    if (npass > 1) {
+      const cpx<R>* pin;
+      if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
+      if ((rc = diffract(fin, fin, pin))) return rc;
     }
-    // exit: half step, interface effective -> n_out, windows and E -> H
-    const cpx<R>* t2;
-    if ((rc = table(KT_2OUT, dprev / 2, t2))) return rc;
-    if ((rc = launch_col(cur, U, 2, 4, KOP_MAT, t2, 1, nullptr, true, true, 1.0 / d.height,
-                         (size_t)d.nlam * L.HW * 8)))
-      return rc;
-    if ((rc = launch_rows(U, 4, true, 1.0 / d.width))) return rc;
-    CK(cudaMemcpyAsync(fout, U, bytes4, cudaMemcpyDeviceToDevice, st));
+    kdir = hd;
+    for (int i = 0; i < npass; ++i) {
+      const int dir = i % 2 == 0 ? 1 : -1;
+      std::vector<int> order;
+      layer_order(dir, order);
+      std::vector<double> dsub(order.size());
+      for (size_t q = 0; q < order.size(); ++q) dsub[q] = d.thickness[order[q]] / d.nstep[order[q]];
+      OpFeed feed;
+      if ((rc = feed_begin(i, order, dsub, feed))) return rc;
+      const cpx<R>* cur = F;
+      int cin;
+      const cpx<R>* t1;
+      if (i == 0) {
+        // entry: the input's forward part through the interface n_in -> effective,
+        // half step; its reflection kept for the next pass
+        CK(cudaMemcpyAsync(F, fin, bytes4, cudaMemcpyDeviceToDevice, st));
+        if (d.diffraction == 0) {
+          k_project_beam<R><<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)d.nray), 128, 0, st>>>(
+              F, rbeta(), rphi(), d.nin * d.nin, g);
+          CKL("k_project_beam");
+        }
+        if ((rc = launch_rows(F, 4, false, 1.0))) return rc;
+        if (npass > 1) {
+          const cpx<R>* rt;
+          if ((rc = table(KT_2RIN, 0.0, rt))) return rc;
+          if ((rc = launch_col(F, Rin, 4, 2, KOP_MAT, rt, 1, nullptr, true, true, ih, ray8))) return rc;
+        }
+        if ((rc = table(KT_2IN, hd * dsub[0] / 2, t1))) return rc;
+        cin = 4;
+      } else {
+        // entry: the wave reflected back into the stack in the previous pass
+        cpx<R>* Rs = dir > 0 ? Rin : Rout;
+        CK(cudaMemcpyAsync(F, Rs, bytes2, cudaMemcpyDeviceToDevice, st));
+        if ((rc = table(KT_2E, dir * hd * dsub[0] / 2, t1, dir))) return rc;
+        cin = 2;
+      }
+      double dprev = 0.0;
+      for (size_t q = 0; q < order.size(); ++q) {
+        const int l = order[q];
+        const double ds = dsub[q];
+        const void* op;
+        if ((rc = feed_get(i, q, order, dsub, feed, op))) return rc;
+        if (dir < 0) op = (const char*)op + back_records();
+        int kop;
+        const void* ktab;
+        if (q == 0) {
+          kop = KOP_MAT;
+          ktab = t1;
+        } else {
+          if ((rc = diag_table(hd * 0.5 * (dprev + ds)))) return rc;
+          kop = KOP_DIAG;
+          ktab = kdiag_cur;
+        }
+        cpx<R>* out = nullptr;
+        if ((rc = layer(cur, cin, kop, ktab, 0, out, op, (double)dir, d.nstep[l], ds))) return rc;
+        if ((rc = feed_done(q, feed))) return rc;
+        if (out != P(L.X) && q + 1 < order.size() && L.chains) {
+          CK(cudaMemcpyAsync(P(L.X), out, bytes2, cudaMemcpyDeviceToDevice, st));
+          out = P(L.X);
+        }
+        cur = out;
+        cin = 2;
+        dprev = ds;
+      }
+      if (dir > 0) {
+        // exit: half step, interface effective -> n_out, windows and E -> H, into field_out
+        const cpx<R>* t2;
+        if ((rc = table(KT_2OUT, hd * dprev / 2, t2, 1))) return rc;
+        if ((rc = launch_col(cur, U, 2, 4, KOP_MAT, t2, 1, nullptr, true, true, ih, ray8))) return rc;
+        if ((rc = launch_rows(U, 4, true, iw))) return rc;
+        if (i == 0)
+          CK(cudaMemcpyAsync(fout, U, bytes4, cudaMemcpyDeviceToDevice, st));
+        else if ((rc = axpby(fout, fout, nullptr, 1.0, U, nullptr, 1.0)))
+          return rc;
+        if (i + 1 < npass) {  // the wave the exit interface reflects back
+          const cpx<R>* tr;
+          if ((rc = table(KT_2R, hd * dprev / 2, tr, 1))) return rc;
+          if ((rc = launch_col(cur, Rout, 2, 2, KOP_MAT, tr, 1, nullptr, true, true, ih, ray4))) return rc;
+        }
+      } else {
+        // exit into n_in: t . (half step) + the input's reflection kept at the
+        // entry, windows and E -> H of the backward modes, added to field_in
+        cpx<R>* Y = P(L.y2);
+        const cpx<R>* te;
+        if ((rc = table(KT_2TE, -hd * dprev / 2, te, -1))) return rc;
+        if ((rc = launch_col(cur, Y, 2, 2, KOP_MAT, te, 1, nullptr, true, true, ih))) return rc;
+        if ((rc = axpby(Y, Y, nullptr, 1.0, Rin, nullptr, 1.0, 2))) return rc;
+        if (i + 1 < npass) {
+          const cpx<R>* tr;
+          if ((rc = table(KT_2R, -hd * dprev / 2, tr, -1))) return rc;
+          if ((rc = launch_col(cur, Rin, 2, 2, KOP_MAT, tr, 1, nullptr, true, true, ih, ray4))) return rc;
+        }
+        const cpx<R>* tx;
+        if ((rc = table(KT_2X, 0.0, tx, -1))) return rc;
+        if ((rc = launch_col(Y, U, 2, 4, KOP_MAT, tx, 1, nullptr, true, true, ih, ray8))) return rc;
+        if ((rc = launch_rows(U, 4, true, iw))) return rc;
+        if ((rc = axpby(fin, fin, nullptr, 1.0, U, nullptr, 1.0))) return rc;
+      }
+    }
+    return DTMM_OK;
+  }
+
+  // 2x2 method in real space: reflection mode 2 (per-voxel interfaces and the
+  // corrected E diffraction matrix between half steps, n x n windows each
+  // through its own chain; dtmm/propagate_2x2.py:91-190, :286-377) and no
+  // diffraction without reflections (the voxels' E P E^-1 alone).  The layer
+  // list is n_in, the block's layers, n_out (dtmm/transfer.py:926-1005); with
+  // npass > 1 every interface keeps its reflected wave between passes.
+  Local2Params local2_params() {
+    Local2Params p;
+    p.epsv = d.epsv;
+    p.epsa = d.epsa;
+    for (int i = 0; i < 3; ++i) {
+      p.ev_s[i] = d.epsv_strides[i];
+      p.ea_s[i] = d.epsa_strides[i];
+    }
+    p.eps_complex = d.eps_complex;
+    p.nin2 = d.nin * d.nin;
+    p.nout2 = d.nout * d.nout;
+    p.ks = ks();
+    p.reps = 1;
+    p.dzero = 0;
+    return p;
+  }
+
+  int local2(Local2Params& p, int op, cpx<R>* f, cpx<R>* refl, cpx<R>* bulk) {
+    p.op = op;
+    const dim3 grid((unsigned)((L.HW + 127) / 128), (unsigned)d.nray);
+    k_local2<R><<<grid, 128, 0, st>>>(p, g, f, refl, bulk);
+    CKL("k_local2");
+    return DTMM_OK;
+  }
+
+  // one interface call of the reference's _transfer_ray_2x2_2 on f (its
+  // window's part): dd the signed sub-step thickness of the output layer
+  int chain2(Local2Params& p, int w, int jout, int nst, double dd, cpx<R>* f, cpx<R>* r) {
+    int rc;
+    const int n = d.nlayers + 1;
+    const bool tracked = r != nullptr;
+    p.beta = wbeta() + w;
+    p.phi = wphi() + w;
+    p.bstride = L.nwin;
+    p.d = dd / 2;
+    const bool zero = dd == 0.0;
+    const size_t ray4 = (size_t)d.nlam * L.HW * 4;
+    for (int s = 0; s < nst; ++s) {
+      if (s == 0 && d.reflection != 0) {
+        p.dzero = zero ? 1 : 0;
+        cpx<R>* b = (tracked && p.mode < 0 && jout == 0) ? (cpx<R>*)io.field_in : nullptr;
+        rc = local2(p, tracked ? L2_TR : L2_ETI, f, r, b);
+        p.dzero = 0;
+        if (rc) return rc;
+      } else if (!zero) {
+        p.reps = d.diffraction == 0 ? 2 : 1;  // both halves at once without a diffraction step between
+        rc = local2(p, L2_HALF, f, nullptr, nullptr);
+        p.reps = 1;
+        if (rc) return rc;
+        if (d.diffraction == 0) continue;
+      }
+      if (d.diffraction > 0) {
+        const cpx<R>* ce;
+        if ((rc = table(KT_2CE, dd, ce, 2 * w + (p.mode < 0 ? 1 : 0)))) return rc;
+        if ((rc = diffract(f, f, ce, ray4, 2))) return rc;
+      }
+      if (!zero && (rc = local2(p, L2_HALF, f, nullptr, nullptr))) return rc;
+    }
+    if (p.mode > 0 && jout == n) return local2(p, L2_BULK, f, nullptr, (cpx<R>*)io.field_out);
+    return DTMM_OK;
+  }
+
+  int run2_real() {
+    int rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* F2 = P(L.F);
+    cpx<R>* G4 = P(L.X);
+    const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    const size_t bytes2 = bytes4 / 2;
+    const size_t n2 = (size_t)NI * 2 * L.HW;
+    const int npass = d.npass;
+    const int n = d.nlayers + 1;  // interfaces
+    const bool tracked = npass > 1;
+    cpx<R>* refl = tracked ? P(L.r2) : nullptr;
+    if (tracked) CK(cudaMemsetAsync(refl, 0, bytes2 * (size_t)n, st));
+    // the input's forward part: per k in the input medium, or for the beam
+    // direction without diffraction (dtmm/transfer.py:1075-1078)
+    if (d.diffraction > 0) {
+      const cpx<R>* pin;
+      if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
+      if ((rc = diffract(G4, fin, pin))) return rc;
+    } else {
+      CK(cudaMemcpyAsync(G4, fin, bytes4, cudaMemcpyDeviceToDevice, st));
+      k_project_beam<R><<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)d.nray), 128, 0, st>>>(
+          G4, rbeta(), rphi(), d.nin * d.nin, g);
+      CKL("k_project_beam");
+    }
+    if (tracked) CK(cudaMemcpyAsync(fin, G4, bytes4, cudaMemcpyDeviceToDevice, st));
+    k_epart<R><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(G4, F2, g);
+    CKL("k_epart");
+    CK(cudaMemsetAsync(fout, 0, bytes4, st));
+    Local2Params p = local2_params();
+    const bool win = L.nwin > 1;
+    cpx<R>* P2 = win ? P(L.w2) : nullptr;
+    cpx<R>* A2 = win ? P2 + n2 : nullptr;
+    cpx<R>* RP = win ? A2 + n2 : nullptr;
+    cpx<R>* RA = win ? RP + n2 : nullptr;
+    const size_t ray4 = (size_t)d.nlam * L.HW * 4;
+    for (int i = 0; i < npass; ++i) {
+      const int dir = i % 2 == 0 ? 1 : -1;
+      if (i > 0) CK(cudaMemsetAsync(F2, 0, bytes2, st));
+      p.mode = dir;
+      for (int q = 0; q < n; ++q) {
+        const int j = dir > 0 ? q : n - 1 - q;
+        const int jin = dir > 0 ? j : j + 1, jout = dir > 0 ? j + 1 : j;
+        // layer list index -> layer of the block (-1 input medium, -2 output medium)
+        auto lay = [&](int k) { return k == 0 ? -1 : (k == n ? -2 : k - 1); };
+        p.lin = lay(jin);
+        p.lout = lay(jout);
+        const bool inner = p.lout >= 0;
+        const int nst = inner ? d.nstep[p.lout] : 1;
+        const double dd = inner ? dir * d.thickness[p.lout] / d.nstep[p.lout] : 0.0;
+        cpx<R>* Rj = tracked ? refl + (size_t)j * n2 : nullptr;
+        if (!win) {
+          if ((rc = chain2(p, 0, jout, nst, dd, F2, Rj))) return rc;
+          continue;
+        }
+        CK(cudaMemsetAsync(A2, 0, bytes2, st));
+        if (tracked) CK(cudaMemsetAsync(RA, 0, bytes2, st));
+        for (int w = 0; w < L.nwin; ++w) {
+          const cpx<R>* wt;
+          if ((rc = table(KT_2WIN, 0.0, wt, w))) return rc;
+          if ((rc = diffract(P2, F2, wt, ray4, 2))) return rc;
+          if (tracked && (rc = diffract(RP, Rj, wt, ray4, 2))) return rc;
+          if ((rc = chain2(p, w, jout, nst, dd, P2, tracked ? RP : nullptr))) return rc;
+          if ((rc = axpby(A2, A2, nullptr, 1.0, P2, nullptr, 1.0, 2))) return rc;
+          if (tracked && (rc = axpby(RA, RA, nullptr, 1.0, RP, nullptr, 1.0, 2))) return rc;
+        }
+        CK(cudaMemcpyAsync(F2, A2, bytes2, cudaMemcpyDeviceToDevice, st));
+        if (tracked) CK(cudaMemcpyAsync(Rj, RA, bytes2, cudaMemcpyDeviceToDevice, st));
+      }
+    }
     return DTMM_OK;
   }
 };
@@ -1397,7 +1682,7 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
     rc = e.run_full4();
   } else {
     rc = e.setup();
-    if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : e.run2();
+    if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : (is_real2(d) ? e.run2_real() : e.run2());
   }
   if (launches) *launches = e.launches;
   return rc;

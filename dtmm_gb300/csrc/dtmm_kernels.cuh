@@ -138,6 +138,9 @@ struct OpParams {
   const double* wev02;
   const double* wevs;
   const double* wc2;
+  // 1: no beam correction (a_w = 0): the plain E P E^-1 of a transfer without
+  // diffraction matrices (2x2, reflection 1, diffraction 0)
+  int uncorrected;
 };
 
 // Records per voxel and window, [ray][window][record][H][W]: complex, or real
@@ -260,7 +263,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       const double cp = p.wcos[rw], sp = p.wsin[rw];
       // cos / sin of (azimuth - phi) by the angle-difference identities
       const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
-      const double aw = p.waw[rw];
+      const double aw = p.uncorrected ? 0.0 : p.waw[rw];
       double ev02, evs, c2;
       if (p.wev02 != nullptr) {
         ev02 = p.wev02[rw];
@@ -336,7 +339,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
     ev[1] = mk<double>(e[1], 0.0);
     ev[2] = mk<double>(e[2], 0.0);
   }
-  cpx<double> aw = csqrt_d(mk<double>(p.eps_eff.re - beta * beta, p.eps_eff.im));
+  cpx<double> aw = p.uncorrected ? mk<double>(0.0, 0.0) : csqrt_d(mk<double>(p.eps_eff.re - beta * beta, p.eps_eff.im));
   cpx<double> E[2][4];  // rows Ex, Ey of the four mode columns
   cpx<double> al[4];
   bool zero = false;
@@ -629,6 +632,246 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
       for (int c = 0; c < 4; ++c) b[(size_t)c * HW] = v[c];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// 2x2 method in real space (reflection mode 2, and diffraction 0 without
+// reflections): one step of the reference's _transfer_ray_2x2_2
+// (dtmm/propagate_2x2.py:91-190) per (pixel, beam).  The FP64 field matrices
+// of the voxels on both sides of the interface (dtmm/tmm.py:124-403, rotated
+// back by phi), then, on every image of the beam's ray (polarisations x
+// wavelengths), one E-field operator of the mode's columns:
+//   L2_HALF  f <- E P E^-1 f, `reps` times (E, P of the output voxel)
+//   L2_ETI   f <- E P Eti f, Eti = St^-1 A^-1 (interface without tracked
+//            reflections, dtmm/tmm.py:999-1022)
+//   L2_TR    with the interface t (dtmm/tmm.py:925-949) and the tracked wave
+//            R: R' = f - t f, g = t f + R; with `bulk` (backward modes, the
+//            input medium): bulk += [g ; E2H g]; then f <- E P E^-1 g (E E^-1 g
+//            when the output layer has no thickness)
+//   L2_BULK  bulk += [f ; E2H f]   (E2H of the output voxel, dtmm/tmm.py:1051)
+// Fields: f and R [image][2][H][W], bulk [image][4][H][W].  A singular
+// matrix inverts to zero, as the reference's inverse does.
+// ---------------------------------------------------------------------------
+enum { L2_HALF = 0, L2_ETI = 1, L2_TR = 2, L2_BULK = 3 };
+
+struct Local2Params {
+  const void* epsv;   // (L?,H?,W?,3) float64 or complex128
+  const double* epsa; // (L?,H?,W?,3) float64
+  long long ev_s[3];
+  long long ea_s[3];
+  int eps_complex;
+  int lin, lout;      // layers on both sides: >= 0 a layer of the block, -1 the input medium, -2 the output medium
+  double nin2, nout2; // eps of the isotropic boundary media
+  double d;           // phase thickness (pixels, signed by the direction)
+  int dzero;          // the output layer has no thickness (E E^-1 instead of E P E^-1)
+  int mode;           // +1 forward, -1 backward modes
+  int reps;           // L2_HALF: applications
+  int op;
+  const double* ks;   // [lam]
+  const double* beta; // [ray * bstride]
+  const double* phi;
+  int bstride;
+};
+
+__device__ __forceinline__ void local2_voxel(const Local2Params& p, int layer, int y, int x, double beta, double phi,
+                                             cpx<double> F[4][4], cpx<double> al[4]) {
+  cpx<double> ev[3];
+  double psi = 0.0, theta = 0.0, azim = 0.0;
+  if (layer < 0) {
+    const double e = layer == -1 ? p.nin2 : p.nout2;
+    ev[0] = ev[1] = ev[2] = mk<double>(e, 0.0);
+  } else {
+    const long long eo = layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
+    const long long ao = layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
+    if (p.eps_complex) {
+      const cpx<double>* e = (const cpx<double>*)p.epsv + eo;
+      ev[0] = e[0]; ev[1] = e[1]; ev[2] = e[2];
+    } else {
+      const double* e = (const double*)p.epsv + eo;
+      ev[0] = mk<double>(e[0], 0.0); ev[1] = mk<double>(e[1], 0.0); ev[2] = mk<double>(e[2], 0.0);
+    }
+    psi = p.epsa[ao];
+    theta = p.epsa[ao + 1];
+    azim = p.epsa[ao + 2];
+  }
+  local_fmat(beta, phi, ev, psi, theta, azim, F, al);
+}
+
+__device__ __forceinline__ void mul2(const cpx<double> a[2][2], const cpx<double> b[2][2], cpx<double> o[2][2]) {
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) o[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j];
+}
+
+template <typename R>
+__device__ __forceinline__ void apply2(const cpx<R> m[2][2], cpx<R> v[2]) {
+  const cpx<R> a = cfma(m[0][1], v[1], m[0][0] * v[0]);
+  const cpx<R> b = cfma(m[1][1], v[1], m[1][0] * v[0]);
+  v[0] = a;
+  v[1] = b;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_local2(Local2Params p, Grid g, cpx<R>* f, cpx<R>* refl, cpx<R>* bulk) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.y;
+  if (pix >= HW) return;
+  const int y = pix / g.W, x = pix - y * g.W;
+  const double beta = p.beta[ray * p.bstride], phi = p.phi[ray * p.bstride];
+  const int m = p.mode < 0 ? 1 : 0;
+  cpx<double> Fb[4][4], alb[4];
+  local2_voxel(p, p.lout, y, x, beta, phi, Fb, alb);
+  cpx<double> E[2][2], Ei[2][2], A[2][2], L[2][2], T[2][2], H[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) E[i][j] = Fb[2 * i][2 * j + m];
+  inv2(E, Ei);
+  const cpx<double> z = mk<double>(0.0, 0.0), one = mk<double>(1.0, 0.0);
+  // L: the right factor of E P L (E^-1, or Eti through the interface); T: t
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      L[i][j] = Ei[i][j];
+      T[i][j] = i == j ? one : z;
+      H[i][j] = z;
+    }
+  if (p.op == L2_ETI || p.op == L2_TR) {
+    cpx<double> Fa[4][4], ala[4], Fai[4][4];
+    local2_voxel(p, p.lin, y, x, beta, phi, Fa, ala);
+    inv4(Fa, Fai);
+    cpx<double> St[2][2], Sti[2][2], Ai[2][2], ei[2][2];
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) {
+        cpx<double> s = z;
+        for (int q = 0; q < 4; ++q) s = s + Fai[2 * i + m][q] * Fb[q][2 * j + m];
+        St[i][j] = s;
+        A[i][j] = Fa[2 * i][2 * j + m];
+      }
+    inv2(St, Sti);
+    inv2(A, Ai);
+    mul2(Sti, Ai, ei);
+    if (p.op == L2_ETI) {
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) L[i][j] = ei[i][j];
+    } else {
+      mul2(E, ei, T);  // t = Et . ei
+    }
+  }
+  if (p.op == L2_BULK || (p.op == L2_TR && bulk != nullptr)) {
+    cpx<double> B[2][2], Ai2[2][2];
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) B[i][j] = Fb[2 * i + 1][2 * j + m];
+    inv2(E, Ai2);
+    mul2(B, Ai2, H);
+  }
+  cpx<R> e[2][2], l[2][2], t[2][2], h[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      e[i][j] = cvt<R>(E[i][j]);
+      l[i][j] = cvt<R>(L[i][j]);
+      t[i][j] = cvt<R>(T[i][j]);
+      h[i][j] = cvt<R>(H[i][j]);
+    }
+  // E L of a layer without thickness (no phase), in FP64 as the reference forms it
+  cpx<R> eei[2][2];
+  if (p.dzero) {
+    cpx<double> M[2][2];
+    mul2(E, L, M);
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) eei[i][j] = cvt<R>(M[i][j]);
+  }
+  const int per = g.npol * g.nlam;
+  for (int q = 0; q < per; ++q) {
+    const int lam = q % g.nlam;
+    const int img = ray * per + q;
+    cpx<R>* fs = f + (size_t)img * 2 * HW + pix;
+    cpx<R> v[2] = {fs[0], fs[HW]};
+    if (p.op == L2_BULK) {
+      cpx<R>* b = bulk + (size_t)img * 4 * HW + pix;
+      cpx<R> hv[2] = {v[0], v[1]};
+      apply2(h, hv);
+      b[0] = b[0] + v[0];
+      b[(size_t)2 * HW] = b[(size_t)2 * HW] + v[1];
+      b[(size_t)HW] = b[(size_t)HW] + hv[0];
+      b[(size_t)3 * HW] = b[(size_t)3 * HW] + hv[1];
+      continue;
+    }
+    if (p.op == L2_TR) {
+      cpx<R>* rs = refl + (size_t)img * 2 * HW + pix;
+      cpx<R> tv[2] = {v[0], v[1]};
+      apply2(t, tv);
+      const cpx<R> r0 = rs[0], r1 = rs[HW];
+      rs[0] = v[0] - tv[0];
+      rs[HW] = v[1] - tv[1];
+      v[0] = tv[0] + r0;
+      v[1] = tv[1] + r1;
+      if (bulk != nullptr) {
+        cpx<R>* b = bulk + (size_t)img * 4 * HW + pix;
+        cpx<R> hv[2] = {v[0], v[1]};
+        apply2(h, hv);
+        b[0] = b[0] + v[0];
+        b[(size_t)2 * HW] = b[(size_t)2 * HW] + v[1];
+        b[(size_t)HW] = b[(size_t)HW] + hv[0];
+        b[(size_t)3 * HW] = b[(size_t)3 * HW] + hv[1];
+      }
+    }
+    if (p.dzero) {
+      apply2(eei, v);
+    } else {
+      const double kd = p.ks[lam] * p.d;
+      const cpx<R> ph0 = local_phase<R>(kd, alb[m]), ph1 = local_phase<R>(kd, alb[m + 2]);
+      const int reps = p.op == L2_HALF ? p.reps : 1;
+      for (int r = 0; r < reps; ++r) {
+        cpx<R> u[2] = {v[0], v[1]};
+        apply2(l, u);
+        u[0] = u[0] * ph0;
+        u[1] = u[1] * ph1;
+        apply2(e, u);
+        v[0] = u[0];
+        v[1] = u[1];
+      }
+    }
+    fs[0] = v[0];
+    fs[HW] = v[1];
+  }
+}
+
+// The forward part of a field for its ray's beam direction in the isotropic
+// medium eps, in real space: F diag(1, 0, 1, 0) F^-1 per pixel
+// (transmitted_field_direct, dtmm/transfer.py:94-101); in place on [image][4][H][W].
+template <typename R>
+__global__ void k_project_beam(cpx<R>* f, const double* beta, const double* phi, double eps, Grid g) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ray = blockIdx.y;
+  if (pix >= HW) return;
+  cpx<double> al[4], F[4][4], Fi[4][4];
+  iso_alphaf(beta[ray], phi[ray], mk<double>(eps, 0.0), al, F);
+  inv4(F, Fi);
+  cpx<R> P[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) P[i][j] = cvt<R>(F[i][0] * Fi[0][j] + F[i][2] * Fi[2][j]);
+  const int per = g.npol * g.nlam;
+  for (int q = 0; q < per; ++q) {
+    cpx<R>* v = f + (size_t)(ray * per + q) * 4 * HW + pix;
+    cpx<R> a[4], o[4];
+    for (int c = 0; c < 4; ++c) a[c] = v[(size_t)c * HW];
+    for (int i = 0; i < 4; ++i) {
+      cpx<R> acc = mk<R>((R)0, (R)0);
+      for (int j = 0; j < 4; ++j) acc = cfma(P[i][j], a[j], acc);
+      o[i] = acc;
+    }
+    for (int c = 0; c < 4; ++c) v[(size_t)c * HW] = o[c];
+  }
+}
+
+// E part (components Ex, Ey) of [image][4][H][W] fields into [image][2][H][W]
+template <typename R>
+__global__ void k_epart(const cpx<R>* __restrict__ f4, cpx<R>* __restrict__ f2, Grid g) {
+  const size_t HW = (size_t)g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * 2 * HW) return;
+  const size_t img = t / (2 * HW), r = t - img * 2 * HW;
+  const size_t c = r / HW, k = r - c * HW;
+  f2[t] = f4[(img * 4 + 2 * c) * HW + k];
 }
 
 // ---------------------------------------------------------------------------
@@ -939,6 +1182,17 @@ enum KTab {
                  // (corrected_Epn_diffraction_matrix, dtmm/matrix.py:38-68)
   KT_CD = 9,     // 4x4 C . D(d), C the correction over -d        (second_field_diffraction_matrix,
   KT_DC = 10,    // 4x4 D(d) . C                                  first_field_..., dtmm/matrix.py:95-107)
+  // 2x2 method, E fields of the forward (mode +1) or backward (mode -1) modes;
+  // T, Rm the interface transmission / reflection from medium ta into tb
+  // (dtmm/diffract.py:215 E_tr_matrix), E(d) the effective medium over d
+  // (dtmm/diffract.py:173), wsum the sum of the ray's window weights at k
+  KT_2RIN = 11,  // 2x4 wsum . Rm . P_in[rows Ex, Ey]        (entry reflection of the input field)
+  KT_2E = 12,    // 2x2 E(d)
+  KT_2TE = 13,   // 2x2 T . E(d)
+  KT_2R = 14,    // 2x2 wsum . Rm . E(d)
+  KT_2X = 15,    // 4x2 [sum_w win_w ; sum_w win_w E2H_w] (E2H in medium tb), masked
+  KT_2CE = 16,   // 2x2 C . E(d) . C of window proj_mode (corrected_E_diffraction_matrix, dtmm/matrix.py:38-43)
+  KT_2WIN = 17,  // 2x2 window proj_mode of the n x n grid times I
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -956,6 +1210,10 @@ struct KTabParams {
   cpx<double> eps_out; // 2x2: medium above the stack (exit interface, and the E2H medium)
   cpx<double> eps_p;   // 2x2 entry: projection medium of the input field
   int with_t;          // 2x2: apply the interface transmission
+  int proj_in;         // 2x2 entry: 1 the input's forward part per k, 0 the input as it is (already projected)
+  int mode;            // 2x2: +1 forward, -1 backward modes
+  int ta, tb;          // 2x2: interface media (from, into): 0 the effective medium, 1 eps_in, 2 eps_out;
+                       // tb is also the E2H medium of KT_2OUT / KT_2X
   double betamax;
   const double* ks;
   // KT_2OUT windows
@@ -1011,27 +1269,59 @@ __device__ inline void iso_k(double beta, double phi, cpx<double> eps, double be
   }
 }
 
-// transmission of the 2x2 interface in -> out at k (dtmm/tmm.py:925-1049)
-__device__ inline void tmat_k(double beta, double phi, cpx<double> ein, cpx<double> eout, double betamax,
-                              cpx<double> t[2][2]) {
-  cpx<double> al[4], Fin[4][4], Finv[4][4], Fout[4][4], Fouti[4][4];
-  iso_k(beta, phi, ein, betamax, al, Fin, Finv);
-  iso_k(beta, phi, eout, betamax, al, Fout, Fouti);
-  cpx<double> St[2][2], A[2][2], Sti[2][2], Ai[2][2];
+// 2x2 interface transmission t and reflection r at k from isotropic medium a
+// into b for the forward (mode +1) or backward (-1) modes: with S = Fa^-1 Fb,
+// St / Sr its transmitted / reflected blocks, A and Er the E parts of Fa's
+// mode and opposite-mode columns and Et of Fb's, ei = St^-1 A^-1,
+// t = Et ei, r = Er Sr ei (dtmm/tmm.py:850-878, :925-949, :1025-1048); zero
+// where beta >= betamax (the reference's masked eigen-data)
+__device__ inline void tr_k(double beta, double phi, cpx<double> ea, cpx<double> eb, double betamax, int mode,
+                            cpx<double> t[2][2], cpx<double> r[2][2]) {
+  cpx<double> al[4], Fa[4][4], Fai[4][4], Fb[4][4], Fbi[4][4];
+  iso_k(beta, phi, ea, betamax, al, Fa, Fai);
+  iso_k(beta, phi, eb, betamax, al, Fb, Fbi);
+  const int m = mode < 0 ? 1 : 0, o = 1 - m;
+  cpx<double> St[2][2], Sr[2][2], A[2][2], Er[2][2], Et[2][2], Sti[2][2], Ai[2][2], ei[2][2];
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j) {
-      cpx<double> s = mk<double>(0.0, 0.0);
-      for (int q = 0; q < 4; ++q) s = s + Finv[2 * i][q] * Fout[q][2 * j];
-      St[i][j] = s;
-      A[i][j] = Fin[2 * i][2 * j];
+      cpx<double> st = mk<double>(0.0, 0.0), sr = mk<double>(0.0, 0.0);
+      for (int q = 0; q < 4; ++q) {
+        st = st + Fai[2 * i + m][q] * Fb[q][2 * j + m];
+        sr = sr + Fai[2 * i + o][q] * Fb[q][2 * j + m];
+      }
+      St[i][j] = st;
+      Sr[i][j] = sr;
+      A[i][j] = Fa[2 * i][2 * j + m];
+      Er[i][j] = Fa[2 * i][2 * j + o];
+      Et[i][j] = Fb[2 * i][2 * j + m];
     }
   inv2(St, Sti);
   inv2(A, Ai);
-  cpx<double> ei[2][2];
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j) ei[i][j] = Sti[i][0] * Ai[0][j] + Sti[i][1] * Ai[1][j];
   for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j) t[i][j] = Fout[2 * i][0] * ei[0][j] + Fout[2 * i][2] * ei[1][j];
+    for (int j = 0; j < 2; ++j) {
+      t[i][j] = Et[i][0] * ei[0][j] + Et[i][1] * ei[1][j];
+      r[i][j] = mk<double>(0.0, 0.0);
+      for (int q = 0; q < 2; ++q) r[i][j] = r[i][j] + Er[i][q] * (Sr[q][0] * ei[0][j] + Sr[q][1] * ei[1][j]);
+    }
+}
+
+// tent weight of window w (of n x n) of ray `ray` at grid point (ky, kx), zero beyond betamax
+// (dtmm/mode.py:11-50); 1 without windows
+__device__ inline double win_weight(const WinParams& wp, const Grid& g, double ks, int n, int w, int ray, int ky,
+                                    int kx) {
+  if (n <= 1) return 1.0;
+  const int i = w / n, j = w % n;
+  const int xt = (i == 0) ? -1 : ((i == n - 1) ? 1 : 0);
+  const int yt = (j == 0) ? -1 : ((j == n - 1) ? 1 : 0);
+  const double l = 2.0 * M_PI / ks;
+  const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
+  const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
+  const double b = sqrt(bx * bx + by * by);
+  if (!(b < wp.betamax)) return 0.0;
+  return tent((bx - (win_center(wp, i) + wp.xoff[ray])) / wp.step, xt) *
+         tent((by - (win_center(wp, j) + wp.yoff[ray])) / wp.step, yt);
 }
 
 // beta and (cos, sin) of phi at grid point k without the angle itself
@@ -1228,77 +1518,125 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(F[i][m0] * Fi[m0][j] + F[i][m0 + 2] * Fi[m0 + 2][j]);
     return;
   }
+  if (p.what == KT_2WIN) {
+    const double c = win_weight(p.win, g, ks, p.nwin_axis, p.proj_mode, p.ray, ky, kx);
+    cpx<R>* o = tab + (size_t)t * 4;
+    o[0] = o[3] = cvt<R>(mk<double>(c, 0.0));
+    o[1] = o[2] = cvt<R>(mk<double>(0.0, 0.0));
+    return;
+  }
+  const int m = p.mode < 0 ? 1 : 0;  // the mode's columns m, m + 2
+  if (p.what == KT_2CE) {
+    // C . E(d) . C: E(d) = j P(d) j^-1 of the medium (masked), C = jb P(-d/2) jb^-1
+    // of the window's own beam (uncut), 2x2 of the mode
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    const bool cut = beta >= p.betamax;
+    const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;
+    cpx<double> alb[4], Fb[4][4];
+    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    cpx<double> J[2][2], Ji[2][2], Jb[2][2], Jbi[2][2], D[2][2], Cm[2][2], T2[2][2];
+    J[0][0] = F[0][m]; J[0][1] = F[0][m + 2]; J[1][0] = F[2][m]; J[1][1] = F[2][m + 2];
+    Jb[0][0] = Fb[0][m]; Jb[0][1] = Fb[0][m + 2]; Jb[1][0] = Fb[2][m]; Jb[1][1] = Fb[2][m + 2];
+    inv2(J, Ji);
+    inv2(Jb, Jbi);
+    const cpx<double> pd[2] = {cexp_i(al[m] * (ks * p.d)), cexp_i(al[m + 2] * (ks * p.d))};
+    const cpx<double> pc[2] = {cexp_i(alb[m] * (-ks * p.d / 2)), cexp_i(alb[m + 2] * (-ks * p.d / 2))};
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) {
+        D[i][j] = cut ? mk<double>(0.0, 0.0) : J[i][0] * pd[0] * Ji[0][j] + J[i][1] * pd[1] * Ji[1][j];
+        Cm[i][j] = Jb[i][0] * pc[0] * Jbi[0][j] + Jb[i][1] * pc[1] * Jbi[1][j];
+      }
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) T2[i][j] = D[i][0] * Cm[0][j] + D[i][1] * Cm[1][j];
+    cpx<R>* o = tab + (size_t)t * 4;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) o[i * 2 + j] = cvt<R>(Cm[i][0] * T2[0][j] + Cm[i][1] * T2[1][j]);
+    return;
+  }
   // 2x2 method: E-basis diffraction over d, e(d) * I for the isotropic medium
   // (dtmm/diffract.py:173 with alphaEEi; masked -> 0)
   iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
   cpx<double> Ed[2][2], Edi[2][2], Edm[2][2];
-  Ed[0][0] = F[0][0]; Ed[0][1] = F[0][2]; Ed[1][0] = F[2][0]; Ed[1][1] = F[2][2];
+  Ed[0][0] = F[0][m]; Ed[0][1] = F[0][m + 2]; Ed[1][0] = F[2][m]; Ed[1][1] = F[2][m + 2];
   inv2(Ed, Edi);
-  const cpx<double> pd0 = cexp_i(al[0] * (ks * p.d)), pd2 = cexp_i(al[2] * (ks * p.d));
+  const cpx<double> pd0 = cexp_i(al[m] * (ks * p.d)), pd2 = cexp_i(al[m + 2] * (ks * p.d));
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j) Edm[i][j] = Ed[i][0] * pd0 * Edi[0][j] + Ed[i][1] * pd2 * Edi[1][j];
-  cpx<double> T[2][2];
+  if (p.what == KT_2E) {
+    cpx<R>* o = tab + (size_t)t * 4;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) o[i * 2 + j] = cvt<R>(Edm[i][j]);
+    return;
+  }
+  cpx<double> T[2][2], Rm[2][2];
+  const cpx<double> med_a = p.ta == 0 ? p.eps : (p.ta == 1 ? p.eps_in : p.eps_out);
+  const cpx<double> med_b = p.tb == 0 ? p.eps : (p.tb == 1 ? p.eps_in : p.eps_out);
   if (p.with_t) {
-    if (p.what == KT_2IN)
-      tmat_k(beta, phi, p.eps_in, p.eps, p.betamax, T);
-    else
-      tmat_k(beta, phi, p.eps, p.eps_out, p.betamax, T);
+    tr_k(beta, phi, med_a, med_b, p.betamax, p.mode, T, Rm);
   } else {
     T[0][0] = T[1][1] = mk<double>(1.0, 0.0);
     T[0][1] = T[1][0] = mk<double>(0.0, 0.0);
+    Rm[0][0] = Rm[0][1] = Rm[1][0] = Rm[1][1] = mk<double>(0.0, 0.0);
   }
-  if (p.what == KT_2IN) {
+  // window sum and the window-weighted E2H of medium tb for each window's beam
+  // (dtmm/tmm.py:1051): only the exit and reflection tables need them
+  const int n = p.nwin_axis;
+  const int nw = n * n;
+  double wsum = 0.0;
+  cpx<double> H[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) H[i][j] = mk<double>(0.0, 0.0);
+  const bool exit_tab = p.what == KT_2OUT || p.what == KT_2X;
+  if (exit_tab || p.what == KT_2R || p.what == KT_2RIN) {
+    for (int w = 0; w < nw; ++w) {
+      const int idx = p.ray * nw + w;
+      if (n > 1 && p.wzero[idx]) continue;
+      const double c = win_weight(p.win, g, ks, n, w, p.ray, ky, kx);
+      if (n > 1 && c == 0.0) continue;
+      wsum += c;
+      if (!exit_tab) continue;
+      cpx<double> alw[4], Fw[4][4];
+      iso_alphaf(p.wbeta[idx], p.wphi[idx], med_b, alw, Fw);
+      cpx<double> A[2][2], Ai[2][2];
+      A[0][0] = Fw[0][m]; A[0][1] = Fw[0][m + 2]; A[1][0] = Fw[2][m]; A[1][1] = Fw[2][m + 2];
+      inv2(A, Ai);
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+          H[i][j] = H[i][j] + (Fw[2 * i + 1][m] * Ai[0][j] + Fw[2 * i + 1][m + 2] * Ai[1][j]) * c;
+    }
+  }
+  if (p.what == KT_2IN || p.what == KT_2RIN) {
     // rows Ex, Ey of the forward projection in the input medium
     cpx<double> alp[4], Fp[4][4], Fpi[4][4], P[2][4];
     iso_k(beta, phi, p.eps_p, p.betamax, alp, Fp, Fpi);
     for (int i = 0; i < 2; ++i)
-      for (int j = 0; j < 4; ++j) P[i][j] = Fp[2 * i][0] * Fpi[0][j] + Fp[2 * i][2] * Fpi[2][j];
+      for (int j = 0; j < 4; ++j)
+        P[i][j] = p.proj_in ? Fp[2 * i][0] * Fpi[0][j] + Fp[2 * i][2] * Fpi[2][j]
+                            : mk<double>(j == 2 * i ? 1.0 : 0.0, 0.0);
     cpx<double> DT[2][2];
     for (int i = 0; i < 2; ++i)
-      for (int j = 0; j < 2; ++j) DT[i][j] = Edm[i][0] * T[0][j] + Edm[i][1] * T[1][j];
+      for (int j = 0; j < 2; ++j)
+        DT[i][j] = p.what == KT_2IN ? Edm[i][0] * T[0][j] + Edm[i][1] * T[1][j] : Rm[i][j] * wsum;
     cpx<R>* o = tab + (size_t)t * 8;
     for (int i = 0; i < 2; ++i)
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(DT[i][0] * P[0][j] + DT[i][1] * P[1][j]);
     return;
   }
-  // KT_2OUT: [sum_w win_w ; sum_w win_w E2H_w] . T . E(d), masked
+  if (p.what == KT_2TE || p.what == KT_2R) {
+    cpx<R>* o = tab + (size_t)t * 4;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) {
+        const cpx<double> v = p.what == KT_2TE ? T[i][0] * Edm[0][j] + T[i][1] * Edm[1][j]
+                                               : (Rm[i][0] * Edm[0][j] + Rm[i][1] * Edm[1][j]) * wsum;
+        o[i * 2 + j] = cvt<R>(v);
+      }
+    return;
+  }
+  // KT_2OUT: [sum_w win_w ; sum_w win_w E2H_w] . T . E(d); KT_2X: the same without T . E(d); masked
   cpx<double> TD[2][2];
   for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j) TD[i][j] = T[i][0] * Edm[0][j] + T[i][1] * Edm[1][j];
-  double wsum = 0.0;
-  cpx<double> H[2][2];
-  for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j) H[i][j] = mk<double>(0.0, 0.0);
-  const int n = p.nwin_axis;
-  const int nw = n * n;
-  for (int w = 0; w < nw; ++w) {
-    double c = 1.0;
-    const int idx = p.ray * nw + w;
-    if (n > 1) {
-      if (p.wzero[idx]) continue;
-      const int i = w / n, j = w % n;
-      const int xt = (i == 0) ? -1 : ((i == n - 1) ? 1 : 0);
-      const int yt = (j == 0) ? -1 : ((j == n - 1) ? 1 : 0);
-      const double l = 2.0 * M_PI / ks;
-      const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
-      const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
-      const double b = sqrt(bx * bx + by * by);
-      c = 0.0;
-      if (b < p.win.betamax)
-        c = tent((bx - (win_center(p.win, i) + p.win.xoff[p.ray])) / p.win.step, xt) *
-            tent((by - (win_center(p.win, j) + p.win.yoff[p.ray])) / p.win.step, yt);
-      if (c == 0.0) continue;
-    }
-    // E2H of the outgoing medium for the window's beam (dtmm/tmm.py:1051)
-    cpx<double> alw[4], Fw[4][4];
-    iso_alphaf(p.wbeta[idx], p.wphi[idx], p.eps_out, alw, Fw);
-    cpx<double> A[2][2], Ai[2][2];
-    A[0][0] = Fw[0][0]; A[0][1] = Fw[0][2]; A[1][0] = Fw[2][0]; A[1][1] = Fw[2][2];
-    inv2(A, Ai);
-    for (int i = 0; i < 2; ++i)
-      for (int j = 0; j < 2; ++j) H[i][j] = H[i][j] + (Fw[2 * i + 1][0] * Ai[0][j] + Fw[2 * i + 1][2] * Ai[1][j]) * c;
-    wsum += c;
-  }
+    for (int j = 0; j < 2; ++j)
+      TD[i][j] = p.what == KT_2X ? mk<double>(i == j ? 1.0 : 0.0, 0.0) : T[i][0] * Edm[0][j] + T[i][1] * Edm[1][j];
   const bool masked = beta >= p.betamax;
   cpx<R>* o = tab + (size_t)t * 8;
   // rows: Ex, Hy, Ey, Hx of the output field; columns: Ex, Ey of the state

@@ -430,6 +430,8 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
             reflection = 2
         if npass > 1:
             reflection = 1
+            if diffraction > 1 and method == "2x2":
+                reflection = 2
     _check_path(method, reflection, npass, diffraction, DTMM_NORM_FFT)
     shape = tuple(field_shape[-2:])
     dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -457,27 +459,26 @@ def _check_path(method, reflection, npass, diffraction, norm):
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
     if method != "4x4" and npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
-    # reflection mode 2 or 4 without diffraction: the per-voxel 4x4 transfer;
-    # reflection modes 2 and 4 with diffraction: real-space half steps around
-    # the corrected diffraction matrices; diffraction = inf: every eigenwave
-    # exactly (any 4x4 reflection mode)
+    # 4x4: reflection mode 2 or 4 without diffraction: the per-voxel transfer;
+    # reflection modes 2-4 with diffraction: real-space half steps around the
+    # corrected diffraction matrices; diffraction = inf: every eigenwave
+    # exactly (any reflection mode).  2x2: reflection 0 / 1 in k-space (1 also
+    # without diffraction), reflection 2 and no diffraction without
+    # reflections in real space; any npass
     local = method == "4x4" and reflection in (2, 4) and diffraction == 0
     full = diffraction == np.inf
     if full and method != "4x4":
         raise NotImplementedError("diffraction = inf is built for the 4x4 method")
     if method == "4x4" and reflection == 3 and diffraction == 0:
         raise NotImplementedError("reflection mode 3 without diffraction (the reference has no such path)")
-    if reflection not in ((1, 2, 3, 4) if method == "4x4" else (0, 1)) and not local and not full:
-        raise NotImplementedError("reflection mode %d with diffraction is outside the GPU engine" % reflection)
-
-    if method != "4x4" and npass != 1:
-        raise NotImplementedError("the 2x2 method with npass > 1 is outside the GPU engine")
     if not (0 <= diffraction <= np.inf):
         raise ValueError("Invalid diffraction value")
-    if diffraction == 0 and not local:
-        if method == "4x4":
-            raise ValueError("Invalid diffraction value")
-        raise NotImplementedError("diffraction=0 is outside the GPU engine")
+    if diffraction == 0 and not local and method == "4x4":
+        raise ValueError("Invalid diffraction value")
+    if method != "4x4" and npass > 1 and reflection == 1 and diffraction == 0:
+        # the reference's tracked reflection applies a diffraction matrix it does
+        # not form without diffraction (dtmm/propagate_2x2.py:61) and fails
+        raise NotImplementedError("2x2 reflection 1 without diffraction is not supported with npass > 1")
     if norm != DTMM_NORM_FFT and method == "4x4" and npass > 1:
         raise NotImplementedError("norm modes other than DTMM_NORM_FFT are outside the GPU engine")
 
@@ -574,7 +575,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         res = _to_host(fout_dev, out)
     else:
         res = fout_dev.to(torch.complex128).cpu().numpy()
-    if npass > 1 and method == "4x4":
+    if npass > 1:
         # the reference rewrites the caller's input with the reflected field
         _to_host(fin_dev, field_in)
     return res

@@ -291,13 +291,7 @@ CASES = {
                                material=("biaxial", dict()), seed=27,
                                illum=dict(beta=0.15, phi=0.4, jones=(1, 0)),
                                transfer=dict(method="4x4", diffraction=0, beta=0.15, phi=0.4)),
-}
 
-
-# Cases the oracle is pinned on ahead of the engine (2x2 with npass > 1:
-# the reflected wave of every interface kept between passes); the GPU parity
-# tests do not run them.
-ORACLE_CASES = {
     # 2x2 in real space: no diffraction (reflection resolves to 0), and
     # reflection mode 2 with windows (dtmm/propagate_2x2.py:91-190, :286-377)
     "twox2_d0": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
@@ -321,7 +315,52 @@ ORACLE_CASES = {
                                     illum=dict(beta=0.1, phi=0.4),
                                     transfer=dict(method="2x2", diffraction=3, reflection=1, npass=2, beta=0.1,
                                                   phi=0.4)),
+    # more of the 2x2 option space: reflection 1 without diffraction (k-space, the
+    # interfaces' betamax cut only; with npass > 1 the reference itself fails), reflection 2 without and with
+    # diffraction matrices and tracked waves, several rays, sub-steps with windows,
+    # biaxial voxels in real space
+    "twox2_refl1_d0": dict(shape=(12, 16), nlayers=3, wavelengths=[500.0, 600.0], pixelsize=100.0,
+                           material=("twisted", dict()), seed=50,
+                           illum=dict(beta=0.1, phi=0.3),
+                           transfer=dict(method="2x2", diffraction=0, reflection=1, beta=0.1, phi=0.3)),
+    "twox2_refl2_d0_npass2": dict(shape=(12, 10), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                  material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=51,
+                                  illum=dict(beta=0.15, phi=1.1),
+                                  transfer=dict(method="2x2", diffraction=0, reflection=2, npass=2, beta=0.15,
+                                                phi=1.1)),
+    "twox2_refl2_d1": dict(shape=(14, 12), nlayers=3, wavelengths=[480.0, 640.0], pixelsize=100.0,
+                           material=("twisted", dict()), seed=52,
+                           illum=dict(beta=0.1, phi=0.2, jones=(1, 0)),
+                           transfer=dict(method="2x2", diffraction=1, reflection=2, beta=0.1, phi=0.2)),
+    "twox2_refl2_d1_npass3": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                  material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=53,
+                                  illum=dict(jones=(1, 0)),
+                                  transfer=dict(method="2x2", diffraction=1, reflection=2, npass=3, beta=0.0,
+                                                phi=0.0)),
+    "twox2_npass2_multiray": dict(shape=(16, 16), nlayers=2, wavelengths=[520.0, 620.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=54,
+                                  illum=dict(beta=[0.0, 0.1], phi=[0.0, np.pi / 2], jones=(1, 0)),
+                                  transfer=dict(method="2x2", diffraction=1, npass=2, multiray=True,
+                                                beta=[0.0, 0.1], phi=[0.0, np.pi / 2])),
+    "twox2_npass2_d3_nstep2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                   material=("twisted", dict(thickness=2.0)), seed=55,
+                                   illum=dict(jones=(1, 0)),
+                                   transfer=dict(method="2x2", diffraction=3, reflection=1, npass=2, nstep=2,
+                                                 beta=0.0, phi=0.0)),
+    "twox2_refl2_d3_nstep2_npass2": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                         material=("twisted", dict(thickness=2.0)), seed=56,
+                                         illum=dict(jones=(1, 0)),
+                                         transfer=dict(method="2x2", diffraction=3, npass=2, nstep=2, beta=0.0,
+                                                       phi=0.0)),
+    "twox2_d0_biaxial": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                             material=("biaxial", dict()), seed=57,
+                             illum=dict(beta=0.1, phi=0.5),
+                             transfer=dict(method="2x2", diffraction=0, beta=0.1, phi=0.5)),
 }
+
+
+# every case with a reference fixture is also a GPU parity case
+ORACLE_CASES = {}
 
 
 def build_optical_data(case):
