@@ -48,12 +48,12 @@ typedef struct dtmm_transfer_desc {
   /* method and options (resolved by the caller as dtmm/transfer.py:433-465 does) */
   int method;        /* 4 = "4x4", 2 = "2x2"                                   */
   int diffraction;   /* >= 1: n > 1 groups modes into n x n windows; 0: no
-                        diffraction (4x4 with reflection 2 or 4);
+                        diffraction (4x4 with reflection 2 or 4; 2x2);
                         DTMM_DIFFRACTION_FULL: inf (4x4)                     */
   int reflection;    /* 4x4: 1 (diffraction >= 1), 2 and 4 (any diffraction),
                         3 (diffraction >= 1), any with DTMM_DIFFRACTION_FULL;
-                        2x2: 0 or 1                                          */
-  int npass;         /* 4x4: >= 1 ; 2x2: 1                                      */
+                        2x2: 0, 1 or 2 (1 without diffraction: npass 1)      */
+  int npass;         /* >= 1 (2x2 with npass > 1: reflection 1 or 2)            */
   int precision;     /* DTMM_PRECISION_*                                        */
   double betamax, nin, nout, smooth;
   /* layers of the (single) optical block */
@@ -101,7 +101,8 @@ typedef struct dtmm_transfer_io {
   void* field_in;
   void* field_out;
   int out_given;  /* 4x4: field_out holds the caller's out= array; its reflected
-                     part is kept (dtmm/transfer.py:674) */
+                     part is kept (dtmm/transfer.py:674); 2x2 zeroes it, as the
+                     reference does (dtmm/transfer.py:1054) */
   /* optional (4x4): [(nlayers + 2)][images][4][H][W]; when set, receives the
      field after every layer (ret_bulk); field_in/field_out must then point at
      its first / last slab */
@@ -138,7 +139,10 @@ size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc);
    transfer without diffraction (reflection 2 or 4) and the exact modal
    transfer (DTMM_DIFFRACTION_FULL, dtmm/propagate_4x4.py:515-560), each
    with any npass.  2x2: the k-space split step with reflection 0 or 1
-   (dtmm/propagate_2x2.py:19-87, :193-284), npass 1.  `stream` is a
+   (dtmm/propagate_2x2.py:19-87, :193-284) and the real-space reflection
+   mode 2 / no-diffraction transfer (dtmm/propagate_2x2.py:91-190, :286-377),
+   any npass (the reflected waves kept per interface, backward passes adding
+   into field_in, dtmm/transfer.py:1074-1183).  `stream` is a
    cudaStream_t (NULL = legacy default stream).  The call enqueues the work
    and returns; results are ready when the stream is.  The first call on a
    stream creates that stream's side stream (kept for the process), on
