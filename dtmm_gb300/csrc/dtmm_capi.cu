@@ -568,7 +568,7 @@ struct Engine {
     // about 8 lines per block measured best (256-pixel rows, 4x4, 2 polarisations)
     int G = std::max(1, 8 / perG);
     if (d.row_group > 0) G = d.row_group;
-    while (G > 1 && ((size_t)G * perG * line_bytes > 110 * 1024 || G * perG * n1 > 512)) --G;
+    while (G > 1 && ((size_t)G * perG * line_bytes > 110 * 1024 || G * perG * n1 > reg_row_max_threads(d.width))) --G;
     return std::min(std::min(G, d.nlam), kMaxRowGroup);
   }
 
@@ -580,7 +580,7 @@ struct Engine {
       const int nl = p.G * p.PB * C;
       const size_t smem =
           2 * (size_t)nl * reg_row_stride(n1, d.width) * sizeof(cpx<R>) + d.width * sizeof(cpx<R>);
-      if (smem > 220 * 1024 || nl * n1 > 512)
+      if (smem > 220 * 1024 || nl * n1 > reg_row_max_threads(d.width))
         return fail(DTMM_ENOTSUP, "row of %d pixels too large for one block", d.width);
       RegLaunch rl;
       rl.smem = smem;
@@ -624,7 +624,7 @@ struct Engine {
       p.G = row_group_reg();
       const int n1 = reg_lanes(d.width);
       if (2 * (size_t)d.npol * L.C * reg_row_stride(n1, d.width) * sizeof(cpx<R>) > 200 * 1024 ||
-          d.npol * L.C * n1 > 512)
+          d.npol * L.C * n1 > reg_row_max_threads(d.width))
         p.PB = 1;
       return launch_row_reg(p, Ub, Xb, L.C, re);
     }

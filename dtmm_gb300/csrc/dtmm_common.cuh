@@ -94,6 +94,40 @@ __host__ __device__ __forceinline__ float to_r<float>(double d) {
   return f32_rn(d);
 }
 
+#ifdef __CUDACC__
+// An FP32 value widened to FP64 exactly, in integer arithmetic (normal
+// floats; others take the hardware conversion, which issues at the FP64 rate)
+__device__ __forceinline__ double f64_of(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long u = ((unsigned long long)(b & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)u);
+}
+
+// Square root of x > 0 for results stored in FP32: the FP32 reciprocal square
+// root of x (its input truncated to FP32 in integer arithmetic) refined by
+// one Newton-Raphson step for 1/sqrt(x), y <- y (3 - x y^2) / 2, whose error
+// is about 1.5 e^2 for a seed error e (<= 1e-6 here, so <= 2e-12), then
+// sqrt(x) = x y: five FP64 operations.  Arguments outside the float range
+// (and non-positive ones) take the library square root.
+__device__ __forceinline__ double sqrt_pos_fast(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // FP32 biased exponent
+  if ((hi & 0x80000000u) || e < 2 || e > 252) return sqrt(x);
+  const float xf = __uint_as_float(((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | ((unsigned)u >> 29));
+  const double y0 = f64_of(rsqrtf(xf));
+  const double hy = (0.5 * x) * y0;
+  const double y = y0 * fma(-hy, y0, 1.5);
+  return x * y;
+}
+
+// d == 0 (either sign), in integer arithmetic
+__device__ __forceinline__ bool is_zero_d(double d) { return (__double_as_longlong(d) << 1) == 0; }
+#endif
+
 __device__ __forceinline__ cpx<double> cvt_d(cpx<float> a) { return mk<double>(a.re, a.im); }
 __device__ __forceinline__ cpx<double> cvt_d(cpx<double> a) { return a; }
 template <typename R>

@@ -255,6 +255,94 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   // the voxel's trigonometry and invariants, shared by every ray and window
   double sa, ca;
   sincos(azim, &sa, &ca);
+  if constexpr (REAL && sizeof(R) == 4) {
+    // complex64 records: the eigen-solve in FP64 with the discriminant in the
+    // form u c2 - eps11 delta st^2 gamma^2 (the delta^2 terms of v^2 - 4 u w
+    // cancel), its square root from sqrt_pos_fast, the determinants from the
+    // local-frame E (a rotation keeps them); only the rotation of the E rows
+    // back to the lab frame, whose entries are stored in FP32, runs in FP32
+    VoxelInv vi;
+    voxel_inv((const double*)p.epsv + eo, theta, vi);
+    const double u4 = 4.0 * vi.u, b4 = 4.0 * vi.ev[0] * vi.kw;
+    for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
+      const double beta = p.wbeta[rw];
+      const double cp = p.wcos[rw], sp = p.wsin[rw];
+      const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
+      const double aw = p.uncorrected ? 0.0 : p.waw[rw];
+      double ev02, evs, c2;
+      if (p.wev02 != nullptr) {
+        ev02 = p.wev02[rw];
+        evs = p.wevs[rw];
+        c2 = p.wc2[rw];
+      } else {
+        ev02 = vi.ev[0] - beta * beta;
+        evs = sqrt_pos_fast(ev02);
+        c2 = vi.ev[0] * (ev02 + (vi.ev[2] - vi.ev[0]));
+      }
+      double E[2][4], al[4];
+      bool zero = false;
+      if (vi.iso || beta == 0.0) {
+        zero = voxel_E_real<FOUR>(beta, vi, ev02, evs, c2, sf, cf, E, al);
+      } else {
+        const double st = vi.st, ct = vi.ct;
+        const double gama = beta * cf;
+        const double disc = fma(-b4, gama * gama, u4 * c2);
+        const double sq = sqrt_pos_fast(disc) * vi.iu2;
+        const double vh = (vi.kv * gama) * vi.iu2;
+        const double evpp = sq - vh;
+        const double ctbeta = ct * beta;
+        const double cfst = cf * st, sfst = st * sf;
+        const double ev02cf = ev02 * cfst;
+        E[0][0] = (evpp * ctbeta - ev02cf) * vi.ie;  E[1][0] = -sfst;
+        E[0][2] = evs * sfst;                        E[1][2] = ctbeta - evs * cfst;
+        al[0] = evpp;
+        al[2] = evs;
+        if (FOUR) {
+          const double evpm = -vh - sq;
+          E[0][1] = (ev02cf - evpm * ctbeta) * vi.ie;  E[1][1] = sfst;
+          E[0][3] = -evs * sfst;                       E[1][3] = evs * cfst + ctbeta;
+          al[1] = evpm;
+          al[3] = -evs;
+        }
+      }
+      const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
+      double detb = 1.0;
+      if (FOUR) detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
+      if (is_zero_d(detf) || is_zero_d(detb)) zero = true;
+      R rec[nrec];
+      if (zero) {
+#pragma unroll
+        for (int i = 0; i < nrec; ++i) rec[i] = (R)0;
+      } else {
+        // rotate the E rows back by the beam azimuth phi, in FP32
+        const float cpf = f32_rn(cp), spf = f32_rn(sp);
+        float ef[2][4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          if (!FOUR && (m & 1)) continue;
+          const float ex = f32_rn(E[0][m]), ey = f32_rn(E[1][m]);
+          ef[0][m] = ex * cpf - ey * spf;
+          ef[1][m] = ex * spf + ey * cpf;
+        }
+        const float df = f32_rn(detf);
+        rec[0] = ef[0][0]; rec[1] = ef[0][2]; rec[2] = ef[1][0]; rec[3] = ef[1][2];
+        rec[4] = fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf);
+        rec[5] = f32_rn((al[0] - aw) * p.d);
+        rec[6] = f32_rn((al[2] - aw) * p.d);
+        if (FOUR) {
+          const float db = f32_rn(detb);
+          rec[7] = ef[0][1]; rec[8] = ef[0][3]; rec[9] = ef[1][1]; rec[10] = ef[1][3];
+          rec[11] = fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb);
+          rec[12] = f32_rn((al[1] + aw) * p.d);
+          rec[13] = f32_rn((al[3] + aw) * p.d);
+        }
+      }
+      R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
+#pragma unroll
+      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
+    }
+    return;
+  }
   if constexpr (REAL) {
     VoxelInv vi;
     voxel_inv((const double*)p.epsv + eo, theta, vi);

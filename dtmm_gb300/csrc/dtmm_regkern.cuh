@@ -60,6 +60,11 @@ __host__ __device__ constexpr int row_band_slots(int n2, int b) {
 }
 __host__ __device__ constexpr bool row_band_ok(int n2, int b) { return b == 0 || 2 * row_band_slots(n2, b) < n2; }
 
+// largest block of the register row pass for an n-point row (its launch bounds)
+__host__ __device__ constexpr int reg_row_max_threads(int n) {
+  return reg_lanes(n) > 0 && n / reg_lanes(n) >= 32 ? 512 : 256;
+}
+
 // the band variant of an n-point row for the largest band limit of a launch
 __host__ __device__ constexpr int row_band_pick(int n, int lim) {
   const int n1 = reg_lanes(n), n2 = n1 > 0 ? n / n1 : 0;
@@ -68,8 +73,12 @@ __host__ __device__ constexpr int row_band_pick(int n, int lim) {
   return 0;
 }
 
+// Launch bounds: rows of up to 16 points per lane run at most 256 threads a
+// block and keep at most 85 registers, so that six 128-thread blocks share an
+// SM (measured 8 % faster than four at 117 registers for 256-point rows);
+// 32 points per lane need the registers of a whole 512-thread block.
 template <typename R, int C, bool REAL, int N1, int N2, int BAND>
-__global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
+__global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
                                                          cpx<R>* __restrict__ X) {
   using T = typename std::conditional<REAL, R, cpx<R>>::type;
   using TS = TwoStep<N1, N2>;
@@ -105,8 +114,8 @@ __global__ void __launch_bounds__(512, 1) k_layer_row_reg(RowParams p, Grid g, c
   const int line = threadIdx.x / N1, t = threadIdx.x % N1;
   const bool active = line < nlines;
   const unsigned gm = group_mask<N1>();
-  // the lane's twiddles W_N^(t k1) in registers when they fit
-  constexpr bool TWREG = N2 <= 16;
+  // the lane's twiddles W_N^(t k1) in registers when they are few
+  constexpr bool TWREG = N2 <= 8;
   cpx<R> trow[TWREG ? N2 : 1];
   if (TWREG) {
 #pragma unroll
