@@ -1291,6 +1291,40 @@ struct Engine {
     return launch_rows(f, 4, true, 1.0 / d.width);
   }
 
+  // f (real space) -> notch * fact * ifft2(P . fft2(f)) with fact the clamped
+  // ratio of the total intensities of f and of the projection
+  // (project_normalized_total, dtmm/transfer.py:123-155, then the notch of
+  // denoise_field): the projection's intensity summed in k-space (the
+  // Poynting form is sesquilinear, so the grid sum of a transform is H W times
+  // the real-space sum)
+  int project_total(cpx<R>* f, const cpx<R>* Ptab, double sigma) {
+    int rc;
+    cpx<R>* K = P(L.U);
+    k_total_intensity<R><<<NI, 256, 0, st>>>(f, g, i0f());
+    CKL("k_total_intensity");
+    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(f, K, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;
+    NotchParams off;
+    off.on = 0;
+    off.ks = ks();
+    const size_t n = (size_t)NI * L.HW;
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, 0, off);
+    CKL("k_kproject");
+    k_total_intensity<R><<<NI, 256, 0, st>>>(K, g, fact());
+    CKL("k_total_intensity");
+    k_total_fact<<<(NI + 255) / 256, 256, 0, st>>>(i0f(), fact(), (double)L.HW, NI);
+    CKL("k_total_fact");
+    NotchParams nt;
+    nt.on = 1;
+    nt.x0 = d.nin;
+    nt.sigma = sigma;
+    nt.ks = ks();
+    k_kscale<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, fact(), g, nt);
+    CKL("k_kscale");
+    if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
+    return launch_rows(f, 4, true, 1.0 / d.width);
+  }
+
   // f <- ifft2(P . fft2(src))
   // ray_stride: elements between the tables of consecutive rays (0 = shared)
   int diffract(cpx<R>* f, const cpx<R>* src, const cpx<R>* Ptab, size_t ray_stride = 0, int C = 4) {
@@ -1355,7 +1389,7 @@ struct Engine {
           if (i == 0 && (rc = axpby(F, F, nullptr, 1.0, fout, nullptr, -1.0))) return rc;
           if (i != npass - 1) {
             if ((rc = table(KT_PROJ, 0.0, pout, 1, d.nout * d.nout))) return rc;
-            if ((rc = project(F, pout, true, sigma))) return rc;
+            if ((rc = d.norm_total ? project_total(F, pout, sigma) : project(F, pout, true, sigma))) return rc;
           }
           if ((rc = axpby(fout, fout, nullptr, 1.0, F, nullptr, 1.0))) return rc;
           CK(cudaMemcpyAsync(F, fout, bytes, cudaMemcpyDeviceToDevice, st));
@@ -1929,7 +1963,7 @@ std::string& last_error_slot() { return g_err; }
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 3; }
+int dtmm_abi_version(void) { return 4; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 

@@ -2079,6 +2079,35 @@ __global__ void k_axpby(cpx<R>* out, const cpx<R>* x, const double* ax, double s
   out[t] = r;
 }
 
+// "total" normalisation factor of each image: |clamp(i1 / i2, -1, 1)| with i2 =
+// ik / hw the real-space total of a k-space grid sum ik; a zero i2 gives 0
+// (normalize_field_total, dtmm/transfer.py:123-132); written over ik
+__global__ void k_total_fact(const double* i1, double* ik, double hw, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const double i2 = ik[t] / hw;
+  double f = i2 == 0.0 ? 0.0 : i1[t] / i2;
+  if (f <= -1.0) f = -1.0;
+  if (f >= 1.0) f = 1.0;
+  ik[t] = fabs(f);
+}
+
+// k-space: f <- notch * fact[image] * f
+template <typename R>
+__global__ void k_kscale(cpx<R>* __restrict__ f, const double* fact, Grid g, NotchParams nt) {
+  const int HW = g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * HW) return;
+  const int img = (int)(t / HW), k = (int)(t - (size_t)img * HW);
+  const int lam = img % g.nlam;
+  const int ky = k / g.W, kx = k - ky * g.W;
+  const R s = (R)(fact[img] * notch_k(nt, g, lam, ky, kx));
+  for (int c = 0; c < 4; ++c) {
+    cpx<R>& v = f[((size_t)img * 4 + c) * HW + k];
+    v = v * s;
+  }
+}
+
 // per-image ratio a / b (the total-intensity rescale of odd passes)
 __global__ void k_ratio(const double* a, const double* b, double* out, int n) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;

@@ -138,7 +138,11 @@ def _compact(a, full_shape):
     idx = []
     for ax in range(3):
         idx.append(slice(None) if (b.strides[ax] != 0 and b.shape[ax] > 1) else slice(0, 1))
-    base = np.ascontiguousarray(b[tuple(idx)])
+    if a.shape == tuple(full_shape) and all(i == slice(None) for i in idx):
+        # nothing to compact: the caller's own (writeable) array, copied only if not contiguous
+        base = np.ascontiguousarray(a)
+    else:
+        base = np.ascontiguousarray(b[tuple(idx)])
     strides = []
     step = 3
     for ax in (2, 1, 0):
@@ -189,6 +193,10 @@ def _field2betaphi(field, ks, multiray):
 # ---------------------------------------------------------------------------
 # the engine call
 # ---------------------------------------------------------------------------
+def _writeable(a):
+    return a if a.flags.writeable else a.copy()
+
+
 class _Material:
     """Optical block resident on the device (uploaded once per call, or kept by the caller)."""
 
@@ -202,13 +210,14 @@ class _Material:
         ea, self.ea_strides = _compact(epsa, full)
         self.eps_complex = bool(np.iscomplexobj(ev))
         # no host copies of arrays that already have the engine's dtype and layout
-        ev = np.require(ev, np.complex128 if self.eps_complex else np.float64, ("C", "W"))
+        # (read-only views of broadcast data are copied: torch wants writeable memory)
+        ev = _writeable(np.ascontiguousarray(ev, np.complex128 if self.eps_complex else np.float64))
         flat = ev.reshape(-1, 3)
         # biaxial voxels take the general eigen-solve (complex FP64 path)
         self.biaxial = not bool(np.all(flat[:, 0] == flat[:, 1]))
         self.eps_min = float(np.min(ev)) if not self.eps_complex else None
         self.epsv = torch.from_numpy(ev).to(device)
-        self.epsa = torch.from_numpy(np.require(ea, np.float64, ("C", "W"))).to(device)
+        self.epsa = torch.from_numpy(_writeable(np.ascontiguousarray(ea, np.float64))).to(device)
         self.thickness = np.asarray(d, np.float64)
         self.nlayers = L
 
@@ -261,7 +270,7 @@ class DevicePlan:
     """
 
     def __init__(self, field_shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
-                 nstep, betamax, nin, nout, smooth, precision, device, tuning=None):
+                 nstep, betamax, nin, nout, smooth, precision, device, tuning=None, norm=DTMM_NORM_FFT):
         import torch
 
         self.lib = _lib.load()
@@ -307,6 +316,8 @@ class DevicePlan:
         bmax = max(float(betamax), float(np.max(np.abs(k["beta"]))))
         d.real_path = int(mat.eps_min is not None and not mat.biaxial and mat.eps_min > bmax * bmax)
         d.biaxial = int(mat.biaxial)
+        # norm = 0: the reference's "total" renormalisation between passes
+        d.norm_total = int(not (int(norm) & DTMM_NORM_FFT))
         self.desc = d
         self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
@@ -409,7 +420,7 @@ def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffract
 
 def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, phi=0.0, nin=None, nout=None,
                   npass=None, nstep=1, diffraction=None, reflection=None, method=None, betamax=None, smooth=SMOOTH,
-                  precision=None, device=None, tuning=None):
+                  precision=None, device=None, tuning=None, norm=DTMM_NORM_FFT):
     """Resolve options like transfer_field and bind a DevicePlan (explicit beta, phi).
 
     ``optical_data`` is the reference's list with one optical block, or a
@@ -432,7 +443,7 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
             reflection = 1
             if diffraction > 1 and method == "2x2":
                 reflection = 2
-    _check_path(method, reflection, npass, diffraction, DTMM_NORM_FFT)
+    _check_path(method, reflection, npass, diffraction, norm)
     shape = tuple(field_shape[-2:])
     dev = device or torch.device("cuda", torch.cuda.current_device())
     if isinstance(optical_data, DeviceMaterial):
@@ -448,7 +459,7 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     npol = int(np.prod(field_shape[:-3])) // (nray * nlam)
     return DevicePlan(field_shape, mat, k0(wavelengths, pixelsize), beta, phi, nray, npol,
                       nlam, method, diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, dev,
-                      tuning)
+                      tuning, norm)
 
 
 def _check_path(method, reflection, npass, diffraction, norm):
@@ -479,8 +490,9 @@ def _check_path(method, reflection, npass, diffraction, norm):
         # the reference's tracked reflection applies a diffraction matrix it does
         # not form without diffraction (dtmm/propagate_2x2.py:61) and fails
         raise NotImplementedError("2x2 reflection 1 without diffraction is not supported with npass > 1")
-    if norm != DTMM_NORM_FFT and method == "4x4" and npass > 1:
-        raise NotImplementedError("norm modes other than DTMM_NORM_FFT are outside the GPU engine")
+    if norm not in (0, DTMM_NORM_FFT) and method == "4x4" and npass > 1:
+        # DTMM_NORM_REF propagates a 2x2 reference field beside the transfer (dtmm/transfer.py:780-785)
+        raise NotImplementedError("norm modes with DTMM_NORM_REF are outside the GPU engine")
 
 
 def _require_cuda():
@@ -563,10 +575,10 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
             fout_dev = torch.empty_like(fdev)
             out_given = 0
     plan = DevicePlan(field_in.shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
-                      nstep, betamax, nin, nout, smooth, precision, dev)
+                      nstep, betamax, nin, nout, smooth, precision, dev, norm=norm)
     plan.run(fin_dev, fout_dev, bulk=bulk_dev, out_given=out_given)
     if ret_bulk:
-        res = bulk_dev.to(torch.complex128).cpu().numpy()
+        res = _new_host(bulk_dev)
         if out is not None:
             out[...] = res
             res = out
@@ -574,11 +586,23 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     if out is not None:
         res = _to_host(fout_dev, out)
     else:
-        res = fout_dev.to(torch.complex128).cpu().numpy()
+        res = _new_host(fout_dev)
     if npass > 1:
         # the reference rewrites the caller's input with the reflected field
         _to_host(fin_dev, field_in)
     return res
+
+
+def _new_host(t):
+    """A new complex128 numpy array holding device tensor ``t``: page-locked
+    host memory from torch's caching host allocator, so the copy is one DMA
+    (a pageable destination costs several times more) and freed results are
+    reused by later calls."""
+    import torch
+
+    h = torch.empty(tuple(t.shape), dtype=torch.complex128, pin_memory=True)
+    h.copy_(t.to(torch.complex128))
+    return h.numpy()
 
 
 def _to_host(t, dest):

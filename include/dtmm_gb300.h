@@ -92,6 +92,11 @@ typedef struct dtmm_transfer_desc {
      and real_path is ignored.  0: the caller guarantees eps[0] == eps[1] for
      every voxel (isotropic / uniaxial closed forms only). */
   int biaxial;
+  /* 4x4 with npass > 1: 1 renormalises each image's total intensity after the
+     output projection (the reference's norm = 0, "total",
+     dtmm/transfer.py:140-155); 0 each k's intensity (DTMM_NORM_FFT,
+     dtmm/transfer.py:78-90).  ABI 4. */
+  int norm_total;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -121,7 +126,7 @@ typedef struct dtmm_kernel_times {
 } dtmm_kernel_times;
 
 /* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
-   3: the biaxial field of dtmm_transfer_desc). */
+   3: the biaxial field of dtmm_transfer_desc; 4: norm_total). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

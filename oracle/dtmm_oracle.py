@@ -846,6 +846,19 @@ def project_normalized_fft(field, dmat):
     return ifft2(normalize_field(f2, i1, i2))
 
 
+def project_normalized_total(field, dmat):
+    """Project in k-space and restore the total intensity of each image, |ratio|
+    clamped to 1 (dtmm/transfer.py:123-155, norm "total", ref=None)."""
+    i1 = total_intensity(field)
+    out = ifft2(dotmf(dmat, fft2(field)))
+    i2 = total_intensity(out)
+    m = i2 == 0.0
+    i2 = np.where(m, 1.0, i2)
+    i1 = np.where(m, 0.0, i1)
+    fact = np.abs(np.clip(i1 / i2, -1, 1))
+    return out * fact[..., None, None, None]
+
+
 def exp_notch_filter(x, x0, sigma):
     """Attenuation around beta = x0 (dtmm/denoise.py:21)."""
     return np.asarray((1 - np.exp(-np.abs(x - x0).clip(0, x0) / sigma)) / (1 - np.exp(-x0 / sigma)), FDTYPE)
@@ -1480,8 +1493,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     full = diffraction == np.inf
     if smooth < 0:
         smooth = 0.0
-    if norm != DTMM_NORM_FFT:
-        raise NotImplementedError("oracle covers norm=DTMM_NORM_FFT")
+    if norm not in (0, DTMM_NORM_FFT):
+        raise NotImplementedError("oracle covers norm=DTMM_NORM_FFT and 0 (total)")
     field_in, wavelengths, pixelsize = field_data
     shape = field_in.shape[-2:]
     layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
@@ -1551,7 +1564,10 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                     field = field - field_out
                 if i != npass - 1:
                     sigma = smooth * (npass - i) / npass
-                    field = project_normalized_fft(field, pout_mat)
+                    if norm == DTMM_NORM_FFT:
+                        field = project_normalized_fft(field, pout_mat)
+                    else:
+                        field = project_normalized_total(field, pout_mat)
                     field = denoise_field(field, ks, nin, sigma)
                 field_out[...] = field_out + field
                 field = field_out.copy()

@@ -142,6 +142,17 @@ CASES = {
                                illum=dict(beta=0.1, phi=0.5),
                                transfer=dict(method="2x2", diffraction=1, split_wavelengths=True,
                                              beta=0.1, phi=0.5)),
+    # npass > 1 with norm = 0: the reference's "total" renormalisation of each image
+    "fourx4_norm_total_npass3": dict(shape=(16, 14), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                                     material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=18,
+                                     illum=dict(beta=0.1, phi=0.6),
+                                     transfer=dict(method="4x4", diffraction=1, npass=3, norm=0, beta=0.1,
+                                                   phi=0.6)),
+    "fourx4_norm_total_d3_npass4": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                        material=("twisted", dict()), seed=19,
+                                        illum=dict(jones=(1, 0)),
+                                        transfer=dict(method="4x4", diffraction=3, npass=4, norm=0, beta=0.0,
+                                                      phi=0.0)),
     "fourx4_bulk": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                         material=("twisted", dict()), seed=15,
                         illum=dict(jones=(1, 0)),

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 3
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 4
 
 
 def _desc(**kw):
@@ -120,6 +120,35 @@ def test_reflection4_descriptor_rules(lib):
     # reflection modes 2 and 3 with diffraction take the same real-space path
     for r in (2, 3):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(diffraction=1, reflection=r))) == s1
+
+
+def test_2x2_descriptor_rules(lib):
+    """2x2: reflection 0 / 1 in k-space (1 also without diffraction, npass 1),
+    reflection 2 and diffraction 0 without reflections in real space; npass >
+    1 keeps reflected waves (two outer ones in k-space, one per interface in
+    real space); reflection 0 with npass > 1 is the reference's ValueError,
+    reflection 1 without diffraction and npass > 1 fails in the reference
+    itself and is refused; diffraction = inf is not built for 2x2."""
+    size = lambda **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(method=2, **kw)))
+    k1 = size(reflection=1)
+    assert k1 > 0 and size(reflection=0) > 0 and size(reflection=1, diffraction=0) > 0
+    assert size(reflection=1, npass=3) > k1  # the two outer reflected waves and the exit state
+    r2 = size(reflection=2)
+    assert r2 > 0 and size(reflection=0, diffraction=0) > 0
+    # every interface (3 layers -> 4) keeps its reflected wave
+    assert size(reflection=2, npass=2) - r2 >= 4 * 16 * 16 * 2 * 8
+    assert size(reflection=2, diffraction=3) > r2  # window parts
+    assert size(reflection=0, npass=2) == 0 and "npass" in _lib.last_error()
+    assert size(reflection=1, diffraction=0, npass=2) == 0 and "diffraction" in _lib.last_error()
+    assert size(reflection=3) == 0 and "reflection" in _lib.last_error()
+    assert size(reflection=1, diffraction=_lib.DIFFRACTION_FULL) == 0
+
+
+def test_norm_total_field(lib):
+    """norm_total (the reference's norm = 0) needs no workspace of its own."""
+    a = lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(npass=3)))
+    b = lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(npass=3, norm_total=1)))
+    assert a == b > 0
 
 
 def test_transfer_rejects_small_workspace(lib):
