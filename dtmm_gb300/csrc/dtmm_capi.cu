@@ -1445,6 +1445,31 @@ struct Engine {
     const double ih = 1.0 / d.height, iw = 1.0 / d.width;
     cpx<R>* Rin = npass > 1 ? P(L.r2in) : nullptr;
     cpx<R>* Rout = npass > 1 ? P(L.r2out) : nullptr;
+    // ret_bulk (no windows): slab l + 1 collects block layer l's field and its
+    // H part, E2H of the voxel for the ray's beam (dtmm/propagate_2x2.py:48-53, :80-85)
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    const size_t n4 = (size_t)NI * 4 * L.HW;
+    if (bulk) CK(cudaMemsetAsync(bulk + n4, 0, bytes4 * (size_t)d.nlayers, st));
+    Local2Params pb = local2_params();
+    pb.beta = rbeta();
+    pb.phi = rphi();
+    pb.bstride = 1;
+    // the layer's field in real space (x-transformed state through its half
+    // step E(dh) of mode `mode`, or as it is) added to its slab
+    auto bulk_add = [&](int l, int mode, const cpx<R>* xs, double dh, bool half) -> int {
+      int rc2;
+      if (half) {
+        const cpx<R>* te;
+        if ((rc2 = table(KT_2E, dh, te, mode))) return rc2;
+        if ((rc2 = launch_col(xs, U, 2, 2, KOP_MAT, te, 1, nullptr, true, true, 1.0 / d.height))) return rc2;
+      } else {
+        CK(cudaMemcpyAsync(U, xs, bytes4 / 2, cudaMemcpyDeviceToDevice, st));
+      }
+      if ((rc2 = launch_rows(U, 2, true, 1.0 / d.width))) return rc2;
+      pb.lout = l;
+      pb.mode = mode;
+      return local2(pb, L2_BULK, U, nullptr, bulk + (size_t)(l + 1) * n4);
+    };
     if (npass > 1) {
       const cpx<R>* pin;
       if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
@@ -1490,6 +1515,9 @@ struct Engine {
       for (size_t q = 0; q < order.size(); ++q) {
         const int l = order[q];
         const double ds = dsub[q];
+        // backward: the field entering layer l from above (the reflected wave
+        // at the top, else the layer above through its half step)
+        if (bulk && dir < 0 && (rc = bulk_add(l, -1, cur, -hd * dprev / 2, q > 0))) return rc;
         const void* op;
         if ((rc = feed_get(i, q, order, dsub, feed, op))) return rc;
         if (dir < 0) op = (const char*)op + back_records();
@@ -1513,6 +1541,7 @@ struct Engine {
         cur = out;
         cin = 2;
         dprev = ds;
+        if (bulk && dir > 0 && (rc = bulk_add(l, 1, cur, hd * ds / 2, true))) return rc;
       }
       if (dir > 0) {
         // exit: half step, interface effective -> n_out, windows and E -> H, into field_out
@@ -1585,9 +1614,10 @@ struct Engine {
 
   // one interface call of the reference's _transfer_ray_2x2_2 on f (its
   // window's part): dd the signed sub-step thickness of the output layer
-  int chain2(Local2Params& p, int w, int jout, int nst, double dd, cpx<R>* f, cpx<R>* r) {
+  // bo: the field array of the output layer jout (field_in, field_out or a
+  // bulk slab) that the reference adds the layer's field to, or null
+  int chain2(Local2Params& p, int w, int jout, int nst, double dd, cpx<R>* f, cpx<R>* r, cpx<R>* bo) {
     int rc;
-    const int n = d.nlayers + 1;
     const bool tracked = r != nullptr;
     p.beta = wbeta() + w;
     p.phi = wphi() + w;
@@ -1598,8 +1628,7 @@ struct Engine {
     for (int s = 0; s < nst; ++s) {
       if (s == 0 && d.reflection != 0) {
         p.dzero = zero ? 1 : 0;
-        cpx<R>* b = (tracked && p.mode < 0 && jout == 0) ? (cpx<R>*)io.field_in : nullptr;
-        rc = local2(p, tracked ? L2_TR : L2_ETI, f, r, b);
+        rc = local2(p, tracked ? L2_TR : L2_ETI, f, r, (tracked && p.mode < 0) ? bo : nullptr);
         p.dzero = 0;
         if (rc) return rc;
       } else if (!zero) {
@@ -1616,7 +1645,8 @@ struct Engine {
       }
       if (!zero && (rc = local2(p, L2_HALF, f, nullptr, nullptr))) return rc;
     }
-    if (p.mode > 0 && jout == n) return local2(p, L2_BULK, f, nullptr, (cpx<R>*)io.field_out);
+    (void)jout;
+    if (p.mode > 0 && bo != nullptr) return local2(p, L2_BULK, f, nullptr, bo);
     return DTMM_OK;
   }
 
@@ -1628,7 +1658,7 @@ struct Engine {
     cpx<R>* G4 = P(L.X);
     const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
     const size_t bytes2 = bytes4 / 2;
-    const size_t n2 = (size_t)NI * 2 * L.HW;
+    const size_t n2 = (size_t)NI * 2 * L.HW, n4 = 2 * n2;
     const int npass = d.npass;
     const int n = d.nlayers + 1;  // interfaces
     const bool tracked = npass > 1;
@@ -1650,6 +1680,15 @@ struct Engine {
     k_epart<R><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(G4, F2, g);
     CKL("k_epart");
     CK(cudaMemsetAsync(fout, 0, bytes4, st));
+    // ret_bulk: slab k of the layer list (0 field_in, n field_out) collects
+    // the fields of its layer; the block's slabs start at zero
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    if (bulk) CK(cudaMemsetAsync(bulk + n4, 0, bytes4 * (size_t)d.nlayers, st));
+    auto bslab = [&](int k) -> cpx<R>* {
+      if (k == 0) return fin;
+      if (k == n) return fout;
+      return bulk ? bulk + (size_t)k * n4 : nullptr;
+    };
     Local2Params p = local2_params();
     const bool win = L.nwin > 1;
     cpx<R>* P2 = win ? P(L.w2) : nullptr;
@@ -1672,8 +1711,9 @@ struct Engine {
         const int nst = inner ? d.nstep[p.lout] : 1;
         const double dd = inner ? dir * d.thickness[p.lout] / d.nstep[p.lout] : 0.0;
         cpx<R>* Rj = tracked ? refl + (size_t)j * n2 : nullptr;
+        cpx<R>* bo = bslab(jout);
         if (!win) {
-          if ((rc = chain2(p, 0, jout, nst, dd, F2, Rj))) return rc;
+          if ((rc = chain2(p, 0, jout, nst, dd, F2, Rj, bo))) return rc;
           continue;
         }
         CK(cudaMemsetAsync(A2, 0, bytes2, st));
@@ -1683,7 +1723,7 @@ struct Engine {
           if ((rc = table(KT_2WIN, 0.0, wt, w))) return rc;
           if ((rc = diffract(P2, F2, wt, ray4, 2))) return rc;
           if (tracked && (rc = diffract(RP, Rj, wt, ray4, 2))) return rc;
-          if ((rc = chain2(p, w, jout, nst, dd, P2, tracked ? RP : nullptr))) return rc;
+          if ((rc = chain2(p, w, jout, nst, dd, P2, tracked ? RP : nullptr, bo))) return rc;
           if ((rc = axpby(A2, A2, nullptr, 1.0, P2, nullptr, 1.0, 2))) return rc;
           if (tracked && (rc = axpby(RA, RA, nullptr, 1.0, RP, nullptr, 1.0, 2))) return rc;
         }
@@ -1920,7 +1960,9 @@ int transfer_impl(const dtmm_transfer_desc* desc, const dtmm_transfer_io* io, vo
   int rc = check_desc(desc);
   if (rc) return rc;
   if (io == nullptr || io->field_in == nullptr || io->field_out == nullptr) return fail(DTMM_EINVAL, "null field buffer");
-  if (io->bulk != nullptr && desc->method != 4) return fail(DTMM_ENOTSUP, "bulk output is implemented for 4x4");
+  // the 2x2 k-space sweep carries the sum over windows, whose E -> H conversion differs per window
+  if (io->bulk != nullptr && desc->method == 2 && !is_real2(desc) && desc->diffraction > 1)
+    return fail(DTMM_ENOTSUP, "2x2 bulk output in k-space is implemented without windows (diffraction <= 1)");
   Layout L = layout_of(desc);
   if (workspace == nullptr || workspace_bytes < L.total)
     return fail(DTMM_ENOSPACE, "workspace of %zu bytes, %zu needed", workspace_bytes, L.total);

@@ -520,10 +520,12 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     od = validate_optical_data(optical_data, shape)
     if len(od) != 1:
         raise NotImplementedError("optical data with more than one block is outside the GPU engine")
-    if ret_bulk and method != "4x4":
-        raise NotImplementedError("ret_bulk is implemented for the 4x4 method")
-    if ret_bulk and npass > 1 and (diffraction == 0 or diffraction == np.inf or reflection in (2, 3, 4)):
+    if ret_bulk and method == "4x4" and npass > 1 and (diffraction == 0 or diffraction == np.inf or
+                                                        reflection in (2, 3, 4)):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
+    if ret_bulk and method != "4x4" and reflection in (0, 1) and diffraction > 1 and diffraction != np.inf:
+        # the k-space sweep carries the sum of the windows, whose E -> H conversions differ
+        raise NotImplementedError("2x2 ret_bulk in k-space (reflection 0 / 1) is implemented for diffraction <= 1")
     ks = k0(wavelengths, pixelsize)
     cdt = torch.complex128 if precision == "double" else torch.complex64
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -562,7 +564,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         fin_dev = bulk_dev[0]
         fout_dev = bulk_dev[-1]
         out_given = 0
-        if out is not None:
+        if out is not None and method == "4x4":  # 2x2 zeroes the caller's out (dtmm/transfer.py:1054)
             ob = np.asarray(out)
             bulk_dev[-1] = torch.from_numpy(np.ascontiguousarray(ob[-1], np.complex128)).to(dev).to(cdt)
             out_given = 1
@@ -587,8 +589,9 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         res = _to_host(fout_dev, out)
     else:
         res = _new_host(fout_dev)
-    if npass > 1:
+    if npass > 1 and not ret_bulk:
         # the reference rewrites the caller's input with the reflected field
+        # (with ret_bulk it rewrites the bulk's first slab instead)
         _to_host(fin_dev, field_in)
     return res
 

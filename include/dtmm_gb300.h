@@ -108,9 +108,11 @@ typedef struct dtmm_transfer_io {
   int out_given;  /* 4x4: field_out holds the caller's out= array; its reflected
                      part is kept (dtmm/transfer.py:674); 2x2 zeroes it, as the
                      reference does (dtmm/transfer.py:1054) */
-  /* optional (4x4): [(nlayers + 2)][images][4][H][W]; when set, receives the
-     field after every layer (ret_bulk); field_in/field_out must then point at
-     its first / last slab */
+  /* optional: [(nlayers + 2)][images][4][H][W]; when set, receives the field
+     after every layer (ret_bulk, dtmm/transfer.py:657-673, :1039-1062);
+     field_in/field_out must then point at its first / last slab.  4x4: npass
+     > 1 with reflection 1 only; 2x2: k-space (reflection 0 / 1) without
+     windows (diffraction <= 1), real space any */
   void* bulk;
 } dtmm_transfer_io;
 

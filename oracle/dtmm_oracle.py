@@ -1608,8 +1608,6 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
         raise ValueError("Invalid reflection. The 2x2 method supports reflection mode 0,1 or 2.")
     if npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
-    if ret_bulk:
-        raise NotImplementedError("oracle covers ret_bulk for 4x4 only")
     field_in, wavelengths, pixelsize = field_data
     layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
     ks = k0(wavelengths, pixelsize)
@@ -1617,11 +1615,25 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if beta is None and phi is None:
         beta, phi = field2betaphi(field_in, ks, multiray)
     beta, phi = _validate_betaphi(beta, phi, extendeddim=field_in.ndim - 2)
+    # with ret_bulk the input and output are the first and last slabs of the
+    # bulk, every interface's output layer adds its field there
+    # (dtmm/transfer.py:1039-1062, :1137-1146)
+    bulk_out = None
     if out is None:
-        field_out = np.zeros_like(field_in)
+        if ret_bulk:
+            bulk_out = np.zeros((n + 1,) + field_in.shape, field_in.dtype)
+        else:
+            field_out = np.zeros_like(field_in)
     else:
         out[...] = 0.0
-        field_out = out
+        if ret_bulk:
+            bulk_out = out
+        else:
+            field_out = out
+    if bulk_out is not None:
+        bulk_out[0] = field_in
+        field_in = bulk_out[0]
+        field_out = bulk_out[-1]
     if not (0 <= diffraction < np.inf):
         raise NotImplementedError("oracle covers finite diffraction for 2x2")
     if diffraction > 0:
@@ -1652,7 +1664,7 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
             elif jout == n:
                 bulk = field_out
             else:
-                bulk = None
+                bulk = None if bulk_out is None else bulk_out[jout]
             r = None if refl is None else refl[j]
             if work_in_fft:
                 field = propagate_2x2_effective_1(field, ks, (thickness * direction, ev, ea),
@@ -1664,6 +1676,8 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                                                      (di * direction, ei_, ai), (de * direction, ee, ae), beta, phi,
                                                      nsub, diffraction, reflection, betamax, direction, r, bulk)
         indices.reverse()
+    if bulk_out is not None:
+        return bulk_out, wavelengths, pixelsize
     return field_out, wavelengths, pixelsize
 
 

@@ -363,6 +363,30 @@ CASES = {
                                          illum=dict(jones=(1, 0)),
                                          transfer=dict(method="2x2", diffraction=3, npass=2, nstep=2, beta=0.0,
                                                        phi=0.0)),
+    # ret_bulk: every layer's field (E and H) inside the stack
+    "twox2_bulk_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[500.0, 610.0], pixelsize=100.0,
+                          material=("twisted", dict()), seed=58,
+                          illum=dict(beta=0.1, phi=0.4),
+                          transfer=dict(method="2x2", diffraction=1, beta=0.1, phi=0.4, ret_bulk=True)),
+    "twox2_bulk_d1_npass2": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                 material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=59,
+                                 illum=dict(jones=(1, 0)),
+                                 transfer=dict(method="2x2", diffraction=1, npass=2, beta=0.0, phi=0.0,
+                                               ret_bulk=True)),
+    "twox2_bulk_refl2_d3": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                material=("twisted", dict()), seed=60,
+                                illum=dict(jones=(1, 0)),
+                                transfer=dict(method="2x2", diffraction=3, reflection=2, beta=0.0, phi=0.0,
+                                              ret_bulk=True)),
+    "twox2_bulk_refl2_d1_npass3": dict(shape=(10, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                       material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=61,
+                                       illum=dict(beta=0.1, phi=1.0, jones=(1, 0)),
+                                       transfer=dict(method="2x2", diffraction=1, reflection=2, npass=3, beta=0.1,
+                                                     phi=1.0, ret_bulk=True)),
+    "twox2_bulk_d0": dict(shape=(10, 12), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                          material=("twisted", dict()), seed=62,
+                          illum=dict(beta=0.1, phi=0.3),
+                          transfer=dict(method="2x2", diffraction=0, beta=0.1, phi=0.3, ret_bulk=True)),
     "twox2_d0_biaxial": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
                              material=("biaxial", dict()), seed=57,
                              illum=dict(beta=0.1, phi=0.5),
