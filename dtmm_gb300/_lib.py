@@ -64,6 +64,7 @@ class TransferDesc(ctypes.Structure):
         ("fft_schedule", ctypes.c_int),
         ("biaxial", ctypes.c_int),
         ("norm_total", ctypes.c_int),
+        ("layer_block", ctypes.POINTER(ctypes.c_int)),
     ]
 
 

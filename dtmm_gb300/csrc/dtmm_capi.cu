@@ -94,6 +94,7 @@ struct Layout {
   size_t r2in, r2out, y2;      // 2x2 k-space, npass > 1: reflected waves of the outer interfaces, exit state
   size_t r2;                   // 2x2 real space, npass > 1: reflected wave of every interface
   size_t w2;                   // 2x2 real space with windows: window part, sum, reflected part and sum
+  size_t effb, awb;            // per block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -152,6 +153,17 @@ int check_desc(const dtmm_transfer_desc* d) {
     if (nodiff2 && d->reflection == 1 && d->nstep[l] > 1)
       return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction supports nstep = 1");
   }
+  if (d->layer_block) {
+    for (int l = 0; l < d->nlayers; ++l) {
+      const int prev = l ? d->layer_block[l - 1] : 0;
+      if (d->layer_block[l] != prev && d->layer_block[l] != prev + 1)
+        return fail(DTMM_EINVAL, "layer_block must start at 0 and grow by 0 or 1 from layer to layer");
+    }
+    // the reflections of the inner interfaces between different effective media are not kept
+    if (d->method == 2 && !(d->reflection == 2 || (d->diffraction == 0 && d->reflection == 0)) && d->npass > 1 &&
+        d->layer_block[d->nlayers - 1] > 0)
+      return fail(DTMM_ENOTSUP, "2x2 reflection 0 / 1 with several optical blocks is supported with npass = 1");
+  }
   FFTPlan p;
   if (!make_plan(d->height, p) || !make_plan(d->width, p))
     return fail(DTMM_ENOTSUP, "grid sides must factor into primes up to 31 (got %dx%d)", d->height, d->width);
@@ -160,6 +172,9 @@ int check_desc(const dtmm_transfer_desc* d) {
     return fail(DTMM_EINVAL, "invalid tuning fields");
   return DTMM_OK;
 }
+
+// blocks of the layer list (layer_block null: one)
+int nblocks(const dtmm_transfer_desc* d) { return d->layer_block ? d->layer_block[d->nlayers - 1] + 1 : 1; }
 
 // 2x2 in real space: reflection mode 2, or no diffraction without reflections
 bool is_real2(const dtmm_transfer_desc* d) {
@@ -187,6 +202,8 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   };
   const size_t nrw = (size_t)d->nray * L.nwin;
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
+  L.effb = take(sizeof(double) * 2 * nblocks(d));
+  L.awb = take(sizeof(double) * nrw * nblocks(d));
   const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
   const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL || refl4);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
@@ -332,6 +349,7 @@ struct Engine {
     int what = -1;
     double d = 0, e = 0;
     int mode = 0;
+    int blk = -1;  // block of the effective medium (-1: independent of it)
     long long used = 0;
   };
   Slot slot[8], dslot[2];
@@ -402,6 +420,12 @@ struct Engine {
   double* i0f() const { return i0() + NI; }
   double* fact() const { return i0f() + NI; }
   double* blim() const { return fact() + NI; }  // [lam] band limits of the W axis
+  // per optical block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
+  double* effb(int b) const { return A<double>(L.effb) + 2 * b; }
+  double* awb(int b) const { return A<double>(L.awb) + (size_t)b * d.nray * L.nwin; }
+  int blk_of(int l) const { return d.layer_block ? d.layer_block[l] : 0; }
+  // the block whose effective medium the k-space tables fetched now use
+  int cur_blk = 0;
 
   int launch_rows(cpx<R>* data, int C, bool inv, double scale) {
     const int nlines = NI * C * d.height;
@@ -640,7 +664,12 @@ struct Engine {
     memset(&p, 0, sizeof(p));
     p.what = what;
     p.proj_mode = proj_mode;
-    p.eps_dev = eff ? epseff() : nullptr;
+    p.eps_dev = eff ? effb(cur_blk) : nullptr;
+    p.eps_dev2 = nullptr;
+    if (what == KT_D12 || what == KT_2BX) {  // the block before the boundary and its half step
+      p.eps_dev2 = effb(proj_mode);
+      p.d2 = eps_re;
+    }
     p.eps = mk<double>(eps_re, eps_im);
     p.d = dd;
     p.betamax = d.betamax;
@@ -703,9 +732,10 @@ struct Engine {
     const bool diag = what == KT_DIAG;
     Slot* sl = diag ? dslot : slot;
     const int n = diag ? L.ndslots : L.nslots;
+    const int blk = (what == KT_PROJ || what == KT_WINMAT || what == KT_2WIN) ? -1 : cur_blk;
     int pick = 0;
     for (int i = 0; i < n; ++i) {
-      if (sl[i].what == what && sl[i].d == dd && sl[i].e == eps_re && sl[i].mode == proj_mode) {
+      if (sl[i].what == what && sl[i].d == dd && sl[i].e == eps_re && sl[i].mode == proj_mode && sl[i].blk == blk) {
         sl[i].used = ++tick;
         out = P((diag ? L.dslots : L.slots) + (size_t)i * (diag ? L.dslot_bytes : L.slot_bytes));
         return DTMM_OK;
@@ -714,12 +744,13 @@ struct Engine {
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
     int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
-                               : launch_ktab(what, dd, dst, proj_mode);
+                               : launch_ktab(what, dd, dst, proj_mode, eps_re);
     if (rc) return rc;
     sl[pick].what = what;
     sl[pick].d = dd;
     sl[pick].e = eps_re;
     sl[pick].mode = proj_mode;
+    sl[pick].blk = blk;
     sl[pick].used = ++tick;
     out = dst;
     return DTMM_OK;
@@ -754,7 +785,7 @@ struct Engine {
     if (s == nullptr) s = st;
     OpParams p;
     memset(&p, 0, sizeof(p));
-    p.eps_dev = epseff();
+    p.eps_dev = effb(blk_of(layer));
     p.permW = row_reg() ? nullptr : A<int>(L.permW);
     p.epsv = d.epsv;
     p.epsa = d.epsa;
@@ -769,7 +800,7 @@ struct Engine {
     p.wphi = wphi();
     p.wcos = wcos();
     p.wsin = wsin();
-    p.waw = waw();
+    p.waw = awb(blk_of(layer));
     p.nwin = L.nwin;
     // both mode blocks for 4x4, and for 2x2 passes that alternate in direction
     p.four = d.method == 4 || d.npass > 1;
@@ -973,6 +1004,7 @@ struct Engine {
     const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
     int rc;
     for (int l : order) {
+      cur_blk = blk_of(l);
       if (d.diffraction == DTMM_DIFFRACTION_FULL)
         rc = full_layer(fullp, p, l, dir, F, F);
       else if (d.diffraction == 0)
@@ -1067,16 +1099,20 @@ struct Engine {
     CKL("k_fft_tables");
     k_fft_tables<R><<<(d.width + 255) / 256, 256, 0, st>>>(pW, P(L.twW), A<int>(L.permW));
     CKL("k_fft_tables");
-    // effective medium
-    {
-      const long long nvox = (long long)d.nlayers * d.height * d.width;
+    // effective medium of every optical block: the mean eps of its voxels
+    for (int l0 = 0; l0 < d.nlayers;) {
+      int l1 = l0 + 1;
+      while (l1 < d.nlayers && blk_of(l1) == blk_of(l0)) ++l1;
+      const long long nvox = (long long)(l1 - l0) * d.height * d.width;
       int blocks = (int)((nvox + 1023) / 1024);
       if (blocks > kPartBlocks) blocks = kPartBlocks;
-      k_eps_mean<<<blocks, 256, 0, st>>>(d.epsv, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1],
-                                         d.epsv_strides[2], d.nlayers, d.height, d.width, A<double>(L.part));
+      const char* e0 = (const char*)d.epsv + (size_t)l0 * d.epsv_strides[0] * (d.eps_complex ? 16 : 8);
+      k_eps_mean<<<blocks, 256, 0, st>>>(e0, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
+                                         l1 - l0, d.height, d.width, A<double>(L.part));
       CKL("k_eps_mean");
-      k_eps_final<<<1, 32, 0, st>>>(A<double>(L.part), blocks, nvox, epseff());
+      k_eps_final<<<1, 32, 0, st>>>(A<double>(L.part), blocks, nvox, effb(blk_of(l0)));
       CKL("k_eps_final");
+      l0 = l1;
     }
     // windows
     if (d.diffraction > 1) {
@@ -1098,10 +1134,12 @@ struct Engine {
       k_sincos<<<(d.nray + 127) / 128, 128, 0, st>>>(wphi(), wcos(), wsin(), d.nray);
       CKL("k_sincos");
     }
-    k_window_aw<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(wbeta(), epseff(), waw(), L.nwin * d.nray,
-                                                              uniform_real() ? (const double*)d.epsv : nullptr,
-                                                              wev02(), wevs(), wc2());
-    CKL("k_window_aw");
+    for (int b = 0; b < nblocks(&d); ++b) {
+      k_window_aw<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(wbeta(), effb(b), awb(b), L.nwin * d.nray,
+                                                                uniform_real() ? (const double*)d.epsv : nullptr,
+                                                                wev02(), wevs(), wc2());
+      CKL("k_window_aw");
+    }
     return DTMM_OK;
   }
 
@@ -1236,11 +1274,20 @@ struct Engine {
       if ((rc = feed_get(pass, q, order, dsub, feed, op))) return rc;
       int kop;
       const void* ktab;
+      const int bprev = cur_blk;
+      cur_blk = blk_of(l);
       if (q == 0) {
         const cpx<R>* t1;
         if ((rc = table(KT_D1, dir * ds / 2, t1))) return rc;
         kop = KOP_MAT;
         ktab = t1;
+      } else if (cur_blk != bprev) {
+        // a boundary between blocks of different effective media: the two
+        // half steps as one matrix per k
+        const cpx<R>* t12;
+        if ((rc = table(KT_D12, dir * ds / 2, t12, bprev, dir * dprev / 2))) return rc;
+        kop = KOP_MAT;
+        ktab = t12;
       } else {
         if ((rc = diag_table(dir * 0.5 * (dprev + ds)))) return rc;
         kop = KOP_DIAG;
@@ -1502,12 +1549,14 @@ struct Engine {
           if ((rc = table(KT_2RIN, 0.0, rt))) return rc;
           if ((rc = launch_col(F, Rin, 4, 2, KOP_MAT, rt, 1, nullptr, true, true, ih, ray8))) return rc;
         }
+        cur_blk = blk_of(order[0]);
         if ((rc = table(KT_2IN, hd * dsub[0] / 2, t1))) return rc;
         cin = 4;
       } else {
         // entry: the wave reflected back into the stack in the previous pass
         cpx<R>* Rs = dir > 0 ? Rin : Rout;
         CK(cudaMemcpyAsync(F, Rs, bytes2, cudaMemcpyDeviceToDevice, st));
+        cur_blk = blk_of(order[0]);
         if ((rc = table(KT_2E, dir * hd * dsub[0] / 2, t1, dir))) return rc;
         cin = 2;
       }
@@ -1523,9 +1572,18 @@ struct Engine {
         if (dir < 0) op = (const char*)op + back_records();
         int kop;
         const void* ktab;
+        const int bprev = cur_blk;
+        cur_blk = blk_of(l);
         if (q == 0) {
           kop = KOP_MAT;
           ktab = t1;
+        } else if (cur_blk != bprev) {
+          // a boundary between blocks: half step, interface between the two
+          // effective media, half step (npass 1)
+          const cpx<R>* tb;
+          if ((rc = table(KT_2BX, hd * ds / 2, tb, bprev, hd * dprev / 2))) return rc;
+          kop = KOP_MAT;
+          ktab = tb;
         } else {
           if ((rc = diag_table(hd * 0.5 * (dprev + ds)))) return rc;
           kop = KOP_DIAG;
@@ -1708,6 +1766,7 @@ struct Engine {
         p.lin = lay(jin);
         p.lout = lay(jout);
         const bool inner = p.lout >= 0;
+        if (inner) cur_blk = blk_of(p.lout);  // boundary layers have no thickness: any block's medium
         const int nst = inner ? d.nstep[p.lout] : 1;
         const double dd = inner ? dir * d.thickness[p.lout] / d.nstep[p.lout] : 0.0;
         cpx<R>* Rj = tracked ? refl + (size_t)j * n2 : nullptr;

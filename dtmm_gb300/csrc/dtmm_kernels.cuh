@@ -1281,6 +1281,9 @@ enum KTab {
   KT_2X = 15,    // 4x2 [sum_w win_w ; sum_w win_w E2H_w] (E2H in medium tb), masked
   KT_2CE = 16,   // 2x2 C . E(d) . C of window proj_mode (corrected_E_diffraction_matrix, dtmm/matrix.py:38-43)
   KT_2WIN = 17,  // 2x2 window proj_mode of the n x n grid times I
+  // boundaries between blocks of different effective media (eps here, eps2 before)
+  KT_D12 = 18,   // 4x4 D1(eps, d) . D2(eps2, d2): the merged half steps E P F^-1 . F P E^-1
+  KT_2BX = 19,   // 2x2 E(eps, d) . T(eps2 -> eps) . E(eps2, d2), forward modes
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1292,6 +1295,9 @@ struct KTabParams {
   int what;
   int proj_mode;       // KT_PROJ: +1 forward, -1 backward modes
   const double* eps_dev; // if set: (re, im) of the effective medium, overrides eps
+  const double* eps_dev2;  // KT_D12 / KT_2BX: (re, im) of the effective medium before the boundary
+  cpx<double> eps2;
+  double d2;               // KT_D12 / KT_2BX: thickness of the half step before the boundary
   double d;            // phase thickness (pixels, signed)
   cpx<double> eps;     // effective medium (or the projection medium)
   cpx<double> eps_in;  // 2x2: medium below the stack (entry interface n_in -> effective)
@@ -1427,6 +1433,40 @@ __device__ inline void betacs_k(const Grid& g, double ks, int ky, int kx, double
   }
 }
 
+// Closed forms of the isotropic medium's half steps (a = sqrt(eps - beta^2),
+// eigenvalues (a, -a, a, -a), e+- = exp(+-i a kd)): E P F^-1 (first, field ->
+// E of both directions, dtmm/matrix.py:110) or F P E^-1 (dtmm/matrix.py:121),
+// the products of the field matrices written out, with the same cut: zero
+// where beta >= betamax or a = 0.
+__device__ inline void iso_half_step(bool first, cpx<double> eps, double beta, double c, double s, double kd,
+                                     double betamax, cpx<double> M[4][4]) {
+  const cpx<double> z = mk<double>(0.0, 0.0);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) M[i][j] = z;
+  const cpx<double> a = csqrt_d(mk<double>(eps.re - beta * beta, eps.im));
+  if ((beta >= betamax) || (a.re == 0.0 && a.im == 0.0)) return;
+  const cpx<double> ep = cexp_i(a * kd), em = cexp_i(-a * kd);
+  const double cc = c * c, ss = s * s, cs = c * s;
+  if (first) {
+    // with igp = a / eps, ia = 1 / a: P = igp c^2 + ia s^2, Q = cs (ia - igp), S = igp s^2 + ia c^2
+    const cpx<double> igp = cdiv(a, eps), ia = cdiv(mk<double>(1.0, 0.0), a);
+    const cpx<double> P = igp * cc + ia * ss, Q = (ia - igp) * cs, S = igp * ss + ia * cc;
+    const cpx<double> hp = ep * 0.5, hm = em * 0.5;
+    M[0][0] = hp; M[0][1] = hp * P;  M[0][3] = hp * Q;
+    M[2][1] = -(hp * Q); M[2][2] = hp; M[2][3] = -(hp * S);
+    M[1][0] = hm; M[1][1] = -(hm * P); M[1][3] = -(hm * Q);
+    M[3][1] = hm * Q; M[3][2] = hm; M[3][3] = hm * S;
+  } else {
+    // with gp = eps / a: P = gp c^2 + a s^2, Q = cs (gp - a), S = gp s^2 + a c^2
+    const cpx<double> gp = cdiv(eps, a);
+    const cpx<double> P = gp * cc + a * ss, Q = (gp - a) * cs, S = gp * ss + a * cc;
+    M[0][0] = ep; M[0][1] = em;
+    M[1][0] = ep * P; M[1][1] = -(em * P); M[1][2] = ep * Q; M[1][3] = -(em * Q);
+    M[2][2] = ep; M[2][3] = em;
+    M[3][0] = -(ep * Q); M[3][1] = em * Q; M[3][2] = -(ep * S); M[3][3] = em * S;
+  }
+}
+
 template <typename R>
 __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int HW = g.H * g.W;
@@ -1436,50 +1476,33 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int ky = k / g.W, kx = k - ky * g.W;
   const double ks = p.ks[lam];
   if (p.eps_dev != nullptr) p.eps = mk<double>(p.eps_dev[0], p.eps_dev[1]);
-  if (p.what == KT_DIAG || p.what == KT_D1 || p.what == KT_D2) {
-    // Closed forms for the isotropic medium (a = sqrt(eps - beta^2), the
-    // eigenvalues (a, -a, a, -a), e+- = exp(+-i a ks d)); they equal the
-    // products of the field matrices E P F^-1 and F P E^-1 written out, with
-    // the same cut: zero where beta >= betamax or a = 0.
+  if (p.eps_dev2 != nullptr) p.eps2 = mk<double>(p.eps_dev2[0], p.eps_dev2[1]);
+  if (p.what == KT_DIAG || p.what == KT_D1 || p.what == KT_D2 || p.what == KT_D12) {
     double beta, c, s;
     betacs_k(g, ks, ky, kx, beta, c, s);
-    const cpx<double> a = csqrt_d(mk<double>(p.eps.re - beta * beta, p.eps.im));
-    const bool cut = (beta >= p.betamax) || (a.re == 0.0 && a.im == 0.0);
-    const cpx<double> z = mk<double>(0.0, 0.0);
-    const cpx<double> ep = cut ? z : cexp_i(a * (ks * p.d));
-    const cpx<double> em = cut ? z : cexp_i(-a * (ks * p.d));
     if (p.what == KT_DIAG) {
+      const cpx<double> a = csqrt_d(mk<double>(p.eps.re - beta * beta, p.eps.im));
+      const bool cut = (beta >= p.betamax) || (a.re == 0.0 && a.im == 0.0);
+      const cpx<double> z = mk<double>(0.0, 0.0);
       // column-major (lam, kx, ky) so that column passes read it coalesced
       const size_t tt = ((size_t)lam * g.W + kx) * g.H + ky;
-      tab[tt * 2 + 0] = cvt<R>(ep);
-      tab[tt * 2 + 1] = cvt<R>(em);
+      tab[tt * 2 + 0] = cvt<R>(cut ? z : cexp_i(a * (ks * p.d)));
+      tab[tt * 2 + 1] = cvt<R>(cut ? z : cexp_i(-a * (ks * p.d)));
       return;
     }
     cpx<double> M[4][4];
-    for (int i = 0; i < 4; ++i)
-      for (int j = 0; j < 4; ++j) M[i][j] = z;
-    if (!cut) {
-      const double cc = c * c, ss = s * s, cs = c * s;
-      if (p.what == KT_D1) {
-        // E P F^-1 (dtmm/matrix.py:110): with igp = a / eps, ia = 1 / a,
-        // P = igp c^2 + ia s^2, Q = cs (ia - igp), S = igp s^2 + ia c^2
-        const cpx<double> igp = cdiv(a, p.eps), ia = cdiv(mk<double>(1.0, 0.0), a);
-        const cpx<double> P = igp * cc + ia * ss, Q = (ia - igp) * cs, S = igp * ss + ia * cc;
-        const cpx<double> hp = ep * 0.5, hm = em * 0.5;
-        M[0][0] = hp; M[0][1] = hp * P;  M[0][3] = hp * Q;
-        M[2][1] = -(hp * Q); M[2][2] = hp; M[2][3] = -(hp * S);
-        M[1][0] = hm; M[1][1] = -(hm * P); M[1][3] = -(hm * Q);
-        M[3][1] = hm * Q; M[3][2] = hm; M[3][3] = hm * S;
-      } else {
-        // F P E^-1 (dtmm/matrix.py:121): with gp = eps / a,
-        // P = gp c^2 + a s^2, Q = cs (gp - a), S = gp s^2 + a c^2
-        const cpx<double> gp = cdiv(p.eps, a);
-        const cpx<double> P = gp * cc + a * ss, Q = (gp - a) * cs, S = gp * ss + a * cc;
-        M[0][0] = ep; M[0][1] = em;
-        M[1][0] = ep * P; M[1][1] = -(em * P); M[1][2] = ep * Q; M[1][3] = -(em * Q);
-        M[2][2] = ep; M[2][3] = em;
-        M[3][0] = -(ep * Q); M[3][1] = em * Q; M[3][2] = -(ep * S); M[3][3] = em * S;
-      }
+    if (p.what == KT_D12) {
+      cpx<double> M1[4][4], M2[4][4];
+      iso_half_step(true, p.eps, beta, c, s, ks * p.d, p.betamax, M1);
+      iso_half_step(false, p.eps2, beta, c, s, ks * p.d2, p.betamax, M2);
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+          cpx<double> acc = mk<double>(0.0, 0.0);
+          for (int m = 0; m < 4; ++m) acc = acc + M1[i][m] * M2[m][j];
+          M[i][j] = acc;
+        }
+    } else {
+      iso_half_step(p.what == KT_D1, p.eps, beta, c, s, ks * p.d, p.betamax, M);
     }
     cpx<R>* o = tab + (size_t)t * 16;
     for (int i = 0; i < 4; ++i)
@@ -1708,6 +1731,29 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     cpx<R>* o = tab + (size_t)t * 8;
     for (int i = 0; i < 2; ++i)
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(DT[i][0] * P[0][j] + DT[i][1] * P[1][j]);
+    return;
+  }
+  if (p.what == KT_2BX) {
+    // E(eps, d) . T(eps2 -> eps) . E(eps2, d2), forward modes
+    cpx<double> al2[4], F2[4][4], F2i[4][4], Ed2[2][2], Ed2i[2][2], Edm2[2][2], T2[2][2], R2[2][2];
+    iso_k(beta, phi, p.eps2, p.betamax, al2, F2, F2i);
+    Ed2[0][0] = F2[0][0]; Ed2[0][1] = F2[0][2]; Ed2[1][0] = F2[2][0]; Ed2[1][1] = F2[2][2];
+    inv2(Ed2, Ed2i);
+    const cpx<double> q0 = cexp_i(al2[0] * (ks * p.d2)), q2 = cexp_i(al2[2] * (ks * p.d2));
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) Edm2[i][j] = Ed2[i][0] * q0 * Ed2i[0][j] + Ed2[i][1] * q2 * Ed2i[1][j];
+    if (p.with_t) {
+      tr_k(beta, phi, p.eps2, p.eps, p.betamax, 1, T2, R2);
+    } else {
+      T2[0][0] = T2[1][1] = mk<double>(1.0, 0.0);
+      T2[0][1] = T2[1][0] = mk<double>(0.0, 0.0);
+    }
+    cpx<double> TE[2][2];
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) TE[i][j] = T2[i][0] * Edm2[0][j] + T2[i][1] * Edm2[1][j];
+    cpx<R>* o = tab + (size_t)t * 4;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) o[i * 2 + j] = cvt<R>(Edm[i][0] * TE[0][j] + Edm[i][1] * TE[1][j]);
     return;
   }
   if (p.what == KT_2TE || p.what == KT_2R) {

@@ -197,12 +197,45 @@ def _writeable(a):
     return a if a.flags.writeable else a.copy()
 
 
-class _Material:
-    """Optical block resident on the device (uploaded once per call, or kept by the caller)."""
+def split_blocks(optical_data):
+    """One single-layer block per layer, each with its own effective medium
+    (layered_data, dtmm/data.py:1516-1528), of validated blocks."""
+    out = []
+    for d, ev, ea in optical_data:
+        for i in range(len(d)):
+            out.append((d[i:i + 1], ev[i:i + 1] if ev.shape[0] > 1 else ev, ea[i:i + 1] if ea.shape[0] > 1 else ea))
+    return out
 
-    def __init__(self, block, shape, device):
+
+def _joined(blocks, shape):
+    """Validated blocks as one (thickness, epsv, epsa) of the whole stack: each
+    block broadcast over the (y, x) axes along which any block varies, then
+    concatenated along the layers; and the block of every layer."""
+    var = [any(np.broadcast_shapes(b[k].shape, (1, 1, 1, 3))[ax] > 1 and np.asarray(b[k]).strides[ax] != 0
+               for b in blocks for k in (1, 2)) for ax in (1, 2)]
+    hv, wv = (shape[0] if var[0] else 1), (shape[1] if var[1] else 1)
+    cplx = any(np.iscomplexobj(b[1]) for b in blocks)
+    ev = np.concatenate([np.broadcast_to(np.asarray(b[1]), (len(b[0]), hv, wv, 3)) for b in blocks])
+    ea = np.concatenate([np.broadcast_to(np.asarray(b[2]), (len(b[0]), hv, wv, 3)) for b in blocks])
+    ev = ev.astype(np.complex128 if cplx else np.float64, copy=False)
+    d = np.concatenate([np.asarray(b[0], np.float64) for b in blocks])
+    lb = np.repeat(np.arange(len(blocks), dtype=np.int32), [len(b[0]) for b in blocks])
+    return (d, ev, ea), lb
+
+
+class _Material:
+    """Optical data resident on the device (uploaded once per call, or kept by
+    the caller): one block, or several joined along the layers with the block
+    of every layer (each block keeps its own effective medium)."""
+
+    def __init__(self, blocks, shape, device):
         import torch
 
+        if isinstance(blocks, list) and len(blocks) > 1:
+            block, self.layer_block = _joined(blocks, shape)
+        else:
+            block = blocks[0] if isinstance(blocks, list) else blocks
+            self.layer_block = None
         d, epsv, epsa = block
         L = len(d)
         full = (L,) + tuple(shape) + (3,)
@@ -249,6 +282,7 @@ class DeviceMaterial:
         if ev.stride(3) != 1 or ea.stride(3) != 1:
             raise ValueError("the last (component) axis of epsv and epsa must be contiguous")
         self.epsv, self.epsa = ev, ea
+        self.layer_block = None
         self.ev_strides = tuple(int(x) for x in ev.stride()[:3])
         self.ea_strides = tuple(int(x) for x in ea.stride()[:3])
         self.eps_complex = bool(ev.is_complex())
@@ -281,6 +315,10 @@ class DevicePlan:
         self.mat = mat
         h, w = field_shape[-2:]
         L = mat.nlayers
+        if mat.layer_block is not None and np.ndim(nstep) > 0:
+            # the reference broadcasts nstep over each block's layers (dtmm/transfer.py:933)
+            counts = np.bincount(mat.layer_block)
+            nstep = np.concatenate([np.broadcast_to(np.asarray(nstep, np.int32), (c,)) for c in counts])
         self._keep = dict(
             thick=np.ascontiguousarray(mat.thickness, np.float64),
             nst=np.ascontiguousarray(np.broadcast_to(np.asarray(nstep, np.int32), (L,)), np.int32),
@@ -318,6 +356,9 @@ class DevicePlan:
         d.biaxial = int(mat.biaxial)
         # norm = 0: the reference's "total" renormalisation between passes
         d.norm_total = int(not (int(norm) & DTMM_NORM_FFT))
+        if mat.layer_block is not None:
+            k["lb"] = np.ascontiguousarray(mat.layer_block, np.int32)
+            d.layer_block = k["lb"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
         self.desc = d
         self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
@@ -449,10 +490,7 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     if isinstance(optical_data, DeviceMaterial):
         mat = optical_data
     else:
-        od = validate_optical_data(optical_data, shape)
-        if len(od) != 1:
-            raise NotImplementedError("optical data with more than one block is outside the GPU engine")
-        mat = _Material(od[0], shape, dev)
+        mat = _Material(validate_optical_data(optical_data, shape), shape, dev)
     beta = np.asarray(beta, np.float64)
     nray = 1 if beta.ndim == 0 else len(beta)
     nlam = field_shape[-4]
@@ -504,7 +542,8 @@ def _require_cuda():
 
 
 def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
-                     diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision):
+                     diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision,
+                     split_layers=False):
     torch = _require_cuda()
     _check_path(method, reflection, npass, diffraction, norm)
     if smooth < 0:
@@ -518,8 +557,8 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     if wavelengths.ndim != 1 or len(wavelengths) != nlam:
         raise ValueError("Incompatible wavelengths shape.")
     od = validate_optical_data(optical_data, shape)
-    if len(od) != 1:
-        raise NotImplementedError("optical data with more than one block is outside the GPU engine")
+    if split_layers:
+        od = split_blocks(od)
     if ret_bulk and method == "4x4" and npass > 1 and (diffraction == 0 or diffraction == np.inf or
                                                         reflection in (2, 3, 4)):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
@@ -554,7 +593,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         nray = 1
     nimg = int(np.prod(field_in.shape[:-3]))
     npol = nimg // (nray * nlam)
-    mat = _Material(od[0], shape, dev)
+    mat = _Material(od, shape, dev)
     fdev = field_dev.to(cdt).contiguous()
     L = mat.nlayers
     bulk_dev = None
@@ -663,8 +702,6 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
                 reflection = 2
     if eff_data not in (0, "isotropic"):
         raise NotImplementedError("only isotropic effective data (eff_data=0) is supported by the GPU engine")
-    if split_layers:
-        raise NotImplementedError("split_layers is outside the GPU engine")
     field_in, wavelengths, pixelsize = field_data
     if split_wavelengths and not isinstance(field_in, tuple) and not ret_bulk:
         # one transfer per wavelength, dispersive eps evaluated at it (dtmm/transfer.py:497-528);
@@ -679,7 +716,7 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
             oi = None if out is None else out_field[..., i:i + 1, :, :, :]
             r = transfer_field((fcopy, np.asarray([wl]), pixelsize), evaluate_optical_data(optical_data, float(wl)),
                                beta, phi, nin, nout, npass, nstep, diffraction, reflection, method, multiray, norm,
-                               betamax, smooth, split_rays, split_diffraction, False, False, eff_data, False, oi,
+                               betamax, smooth, split_rays, split_diffraction, False, split_layers, eff_data, False, oi,
                                precision)
             out_field[..., i, :, :, :] = r[0][..., 0, :, :, :]
             if npass > 1:
@@ -698,7 +735,7 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
                 o = None if o is None else np.asarray(o)[..., None, :, :, :]
             r = transfer_field((f, [wl] if scalar else wl, pixelsize), od, beta, phi, nin, nout,
                                npass, nstep, diffraction, reflection, method, multiray, norm, betamax, smooth,
-                               split_rays, split_diffraction, False, False, eff_data, ret_bulk, o, precision)
+                               split_rays, split_diffraction, False, split_layers, eff_data, ret_bulk, o, precision)
             if scalar:
                 r = (r[0][..., 0, :, :, :], wl, pixelsize)
             outs.append(r)
@@ -725,7 +762,7 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
             o = (res[:, i] if ret_bulk else res[i]) if given else None
             r = _transfer_single(fi, wavelengths, pixelsize, optical_data, bl[i], pl[i], nin, nout, npass, nstep,
                                  diffraction, reflection, method, False, norm, betamax, smooth, ret_bulk, o,
-                                 precision)
+                                 precision, split_layers)
             if not given:
                 if ret_bulk:
                     res[:, i] = r
@@ -733,7 +770,8 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
                     res[i] = r
         return res, wavelengths, pixelsize
     res = _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
-                           diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision)
+                           diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision,
+                           split_layers)
     return res, wavelengths, pixelsize
 
 

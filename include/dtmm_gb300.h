@@ -97,6 +97,13 @@ typedef struct dtmm_transfer_desc {
      dtmm/transfer.py:140-155); 0 each k's intensity (DTMM_NORM_FFT,
      dtmm/transfer.py:78-90).  ABI 4. */
   int norm_total;
+  /* host [nlayers] or null: the optical-data block of every layer (0, then
+     each layer's block equal to or one above the previous layer's).  Each
+     block has its own isotropic effective medium, the mean eps of its voxels
+     (dtmm/transfer.py:926-1005 builds the layer list block by block; one
+     block per layer with split_layers).  Null: one block.  2x2 reflection 0 /
+     1 with several blocks: npass 1.  ABI 4. */
+  const int* layer_block;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -128,7 +135,7 @@ typedef struct dtmm_kernel_times {
 } dtmm_kernel_times;
 
 /* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
-   3: the biaxial field of dtmm_transfer_desc; 4: norm_total). */
+   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

@@ -1694,8 +1694,8 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     betamax = opt("betamax", betamax)
     if eff_data not in (0, "isotropic"):
         raise NotImplementedError("oracle covers isotropic effective data")
-    if split_rays or split_layers:
-        raise NotImplementedError("oracle covers unsplit transfer and split_wavelengths")
+    if split_rays:
+        raise NotImplementedError("oracle covers unsplit rays")
     if split_wavelengths and not isinstance(field_data[0], tuple) and not ret_bulk:
         # one transfer per wavelength with dispersive eps evaluated at it
         # (dtmm/transfer.py:497-528, dtmm/data.py:575-586); each slice is a view,
@@ -1723,6 +1723,10 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
                 reflection = 2
     field_in, wavelengths, pixelsize = field_data
     od = validate_optical_data(optical_data, shape=field_in.shape[-2:])
+    if split_layers:
+        # one block (and effective medium) per layer (dtmm/transfer.py:531-533, dtmm/data.py:1516-1528)
+        od = [(d[i:i + 1], ev[i:i + 1] if ev.shape[0] > 1 else ev, ea[i:i + 1] if ea.shape[0] > 1 else ea)
+              for d, ev, ea in od for i in range(len(d))]
     if method == "4x4":
         return transfer_4x4((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
                             diffraction, reflection, multiray, norm, smooth, betamax, ret_bulk, out)

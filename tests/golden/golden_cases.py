@@ -63,12 +63,20 @@ def _cauchy(shape, nlayers, seed):
     return d, EpsilonCauchy(c), epsa
 
 
+def _isotropic(shape, nlayers, seed, eps=2.1):
+    """Homogeneous isotropic layers of eps (a glass or a cover block)."""
+    d = np.ones(nlayers)
+    epsv = np.tile(np.asarray((eps, eps, eps)), (nlayers, 1, 1, 1))
+    return d, epsv, np.zeros((nlayers, 1, 1, 3))
+
+
 MATERIALS = {
     "twisted": _twisted,
     "biaxial": _biaxial,
     "inplane": lambda shape, nlayers, seed, **kw: samples.inplane_nematic(shape, nlayers, seed=seed, **kw),
     "absorbing": _absorbing,
     "cauchy": _cauchy,
+    "iso": _isotropic,
     "mixed": _mixed_voxels,
 }
 
@@ -153,6 +161,34 @@ CASES = {
                                         illum=dict(jones=(1, 0)),
                                         transfer=dict(method="4x4", diffraction=3, npass=4, norm=0, beta=0.0,
                                                       phi=0.0)),
+    # several optical blocks (each its own effective medium), and split_layers (one per layer)
+    "fourx4_blocks": dict(shape=(14, 16), nlayers=5, wavelengths=[520.0, 640.0], pixelsize=100.0,
+                          blocks=[("twisted", dict(no=1.5, ne=1.7), 2), ("iso", dict(eps=2.3), 1),
+                                  ("twisted", dict(no=1.55, ne=1.65, amplitude=0.3), 2)], seed=20,
+                          illum=dict(beta=0.1, phi=0.5, jones=(1, 0)),
+                          transfer=dict(method="4x4", diffraction=1, beta=0.1, phi=0.5)),
+    "fourx4_blocks_d3_npass2": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                    blocks=[("twisted", dict(), 2), ("iso", dict(eps=2.0), 1)], seed=21,
+                                    illum=dict(jones=(1, 0)),
+                                    transfer=dict(method="4x4", diffraction=3, npass=2, beta=0.0, phi=0.0)),
+    "fourx4_split_layers": dict(shape=(12, 14), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                material=("mixed", dict()), seed=22,
+                                illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, split_layers=True, beta=0.1, phi=0.3)),
+    "fourx4_blocks_refl4": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                blocks=[("twisted", dict(), 2), ("iso", dict(eps=2.2), 1)], seed=23,
+                                illum=dict(beta=0.1, phi=0.2, jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, reflection=4, beta=0.1, phi=0.2)),
+    "twox2_blocks": dict(shape=(14, 12), nlayers=3, wavelengths=[500.0, 600.0], pixelsize=100.0,
+                         blocks=[("twisted", dict(), 2), ("iso", dict(eps=2.4), 1)], seed=24,
+                         illum=dict(beta=0.1, phi=0.4, jones=(1, 0)),
+                         transfer=dict(diffraction=1, beta=0.1, phi=0.4)),
+    "twox2_blocks_refl2_npass2": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                      blocks=[("twisted", dict(no=1.45, ne=1.6), 1), ("twisted", dict(), 2)],
+                                      seed=25,
+                                      illum=dict(jones=(1, 0)),
+                                      transfer=dict(method="2x2", diffraction=1, reflection=2, npass=2, beta=0.0,
+                                                    phi=0.0)),
     "fourx4_bulk": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                         material=("twisted", dict()), seed=15,
                         illum=dict(jones=(1, 0)),
@@ -399,6 +435,10 @@ ORACLE_CASES = {}
 
 
 def build_optical_data(case):
+    """The case's optical data: one block, or with ``blocks`` = [(kind, kwargs,
+    layers), ...] several blocks of their own materials and effective media."""
+    if "blocks" in case:
+        return [MATERIALS[k](case["shape"], nl, case["seed"] + i, **kw) for i, (k, kw, nl) in enumerate(case["blocks"])]
     kind, kw = case["material"]
     return [MATERIALS[kind](case["shape"], case["nlayers"], case["seed"], **kw)]
 
