@@ -108,23 +108,27 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->method != 4 && d->method != 2) return fail(DTMM_EINVAL, "method must be 4 (4x4) or 2 (2x2)");
   // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1);
   // diffraction = inf (DTMM_DIFFRACTION_FULL): every eigenwave exactly (4x4, npass 1,
-  // any reflection mode: the reference takes the same path for all of them)
+  // any reflection mode: the reference takes the same path for all of them;
+  // 2x2 with reflection 0 or 2, any npass)
   const bool local4 = d->method == 4 && d->diffraction == 0 && (d->reflection == 2 || d->reflection == 4);
   const bool full4 = d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL;
+  const bool full2 = d->method == 2 && d->diffraction == DTMM_DIFFRACTION_FULL;
   // reflection modes 2-4 with diffraction: real-space steps around the
   // corrected diffraction matrices (tables per ray: they follow its beam)
   const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
-  if (d->diffraction == DTMM_DIFFRACTION_FULL && !full4)
-    return fail(DTMM_ENOTSUP, "diffraction = inf is built for the 4x4 method");
+  // the reference's 2x2 reflection 1 moves the field to k-space, and its modal
+  // step transforms that field once more (dtmm/transfer.py:1091-1098, :1172)
+  if (full2 && d->reflection == 1)
+    return fail(DTMM_ENOTSUP, "2x2 with diffraction = inf is supported with reflection 0 or 2");
   // the modal DFT kernels take one grid row per (image, component) line
-  if (full4 && (long long)d->nray * d->npol * d->nlam * 4 > 65535)
-    return fail(DTMM_ENOTSUP, "diffraction = inf is supported for at most 16383 images");
+  if ((full4 || full2) && (long long)d->nray * d->npol * d->nlam * (full4 ? 4 : 2) > 65535)
+    return fail(DTMM_ENOTSUP, "diffraction = inf is supported for at most %d images", full4 ? 16383 : 32767);
   // 2x2 without diffraction: real space (reflection 0 or 2) or k-space with
   // the interfaces' betamax cut only (reflection 1)
   const bool nodiff2 = d->method == 2 && d->diffraction == 0;
-  if ((d->diffraction < 0 && !full4) || (d->diffraction < 1 && !local4 && !full4 && !nodiff2))
+  if ((d->diffraction < 0 && !full4 && !full2) || (d->diffraction < 1 && !local4 && !full4 && !full2 && !nodiff2))
     return fail(DTMM_ENOTSUP, "diffraction must be >= 1 on this path (0 with 4x4 reflection mode 2 or 4, or "
-                              "with 2x2; inf with 4x4)");
+                              "with 2x2; or inf)");
   if (d->method == 4 && (d->reflection < 1 || d->reflection > 4))
     return fail(DTMM_EINVAL, "4x4 reflection mode must be 1..4");
   if (d->method == 4 && d->reflection != 1 && !local4 && !full4 && !refl4)
@@ -259,8 +263,8 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.y2 = take(kpass2 ? field2 : 0);
   L.r2 = take(real2 && passes ? field2 * (size_t)(d->nlayers + 1) : 0);
   L.w2 = take(real2 && L.nwin > 1 ? 4 * field2 : 0);
-  // the real-space paths keep no operator records
-  L.op_one = (real_space || real2) ? 0 : L.cplx * nrw * OP_REC * L.HW;
+  // the real-space and modal paths keep no operator records
+  L.op_one = (real_space || real2 || d->diffraction == DTMM_DIFFRACTION_FULL) ? 0 : L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
   L.cache_ops = passes && L.op_one * (size_t)d->nlayers <= limit;
   // per-layer cache, or two buffers that alternate between the layer being
@@ -873,6 +877,7 @@ struct Engine {
     for (int i = 0; i < d.nlam; ++i) limx = std::max(limx, band_limit(d.width, d.ks[i], d.betamax));
     fp.limx = std::max(limx, 0);
     fp.S = 2 * fp.limx + 1 >= d.width ? d.width : 2 * fp.limx + 1;
+    fp.C = L.C;
     CK(cudaMemsetAsync(fp.count, 0, sizeof(int) * d.nlam, st));
     const dim3 gk((unsigned)((L.HW + 127) / 128), (unsigned)d.nlam);
     k_full_betaphi<<<gk, 128, 0, st>>>(fp, g);
@@ -1792,6 +1797,79 @@ struct Engine {
     }
     return DTMM_OK;
   }
+
+  // mode amplitudes (FP64, in order of increasing beta) of the 2-component
+  // field f into amp: the row DFT at the in-band columns, then the column DFT
+  int full_amps2(const cpx<R>* f, cpx<double>* amp) {
+    cpx<double>* Ab = A<cpx<double>>(L.fA);
+    k_full_rowdft<R><<<dim3((unsigned)d.height, (unsigned)(NI * 2)), 128, 0, st>>>(fullp, g, f, Ab);
+    CKL("k_full_rowdft");
+    k_full_coldft<<<dim3((unsigned)((L.HW + 127) / 128), (unsigned)(NI * 2)), 128, 0, st>>>(fullp, g, Ab, amp);
+    CKL("k_full_coldft");
+    return DTMM_OK;
+  }
+
+  // 2x2 with diffraction = inf (dtmm/transfer.py:1009-1183 with
+  // dtmm/propagate_2x2.py:379-464): the input's forward part per k in the
+  // input medium, then per pass and interface (layer list n_in, the layers,
+  // n_out) one modal step over the output layer's sub-step thickness d / nstep
+  // (the reference takes one), through the interface with reflection 2; with
+  // npass > 1 every interface keeps its reflected wave between passes.  The
+  // field of each output layer is added to its slab (field_in, field_out or
+  // the bulk output).
+  int run2_full() {
+    int rc;
+    cpx<R>* fin = (cpx<R>*)io.field_in;
+    cpx<R>* fout = (cpx<R>*)io.field_out;
+    cpx<R>* F2 = P(L.F);
+    cpx<R>* G4 = P(L.X);
+    const size_t bytes4 = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    const size_t bytes2 = bytes4 / 2;
+    const size_t n2 = (size_t)NI * 2 * L.HW, n4 = 2 * n2;
+    const int n = d.nlayers + 1;  // interfaces
+    const bool tracked = d.npass > 1;
+    cpx<R>* refl = tracked ? P(L.r2) : nullptr;
+    if (tracked) CK(cudaMemsetAsync(refl, 0, bytes2 * (size_t)n, st));
+    const cpx<R>* pin;
+    if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
+    if ((rc = diffract(G4, fin, pin))) return rc;
+    if (tracked) CK(cudaMemcpyAsync(fin, G4, bytes4, cudaMemcpyDeviceToDevice, st));
+    k_epart<R><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(G4, F2, g);
+    CKL("k_epart");
+    CK(cudaMemsetAsync(fout, 0, bytes4, st));
+    cpx<R>* bulk = (cpx<R>*)io.bulk;
+    if (bulk) CK(cudaMemsetAsync(bulk + n4, 0, bytes4 * (size_t)d.nlayers, st));
+    auto bslab = [&](int k) -> cpx<R>* {
+      if (k == 0) return fin;
+      if (k == n) return fout;
+      return bulk ? bulk + (size_t)k * n4 : nullptr;
+    };
+    if ((rc = full_prepare(fullp))) return rc;
+    cpx<double>* amp = A<cpx<double>>(L.famp);
+    cpx<double>* tamp = amp + n2;
+    Local2Params p = local2_params();
+    p.op = d.reflection != 0;
+    const dim3 gk((unsigned)((L.HW + 127) / 128), (unsigned)d.nlam);
+    for (int i = 0; i < d.npass; ++i) {
+      const int dir = i % 2 == 0 ? 1 : -1;
+      if (i > 0) CK(cudaMemsetAsync(F2, 0, bytes2, st));
+      p.mode = dir;
+      for (int q = 0; q < n; ++q) {
+        const int j = dir > 0 ? q : n - 1 - q;
+        const int jin = dir > 0 ? j : j + 1, jout = dir > 0 ? j + 1 : j;
+        auto lay = [&](int k) { return k == 0 ? -1 : (k == n ? -2 : k - 1); };
+        p.lin = lay(jin);
+        p.lout = lay(jout);
+        p.d = p.lout >= 0 ? dir * d.thickness[p.lout] / d.nstep[p.lout] : 0.0;
+        cpx<R>* Rj = tracked ? refl + (size_t)j * n2 : nullptr;
+        if ((rc = full_amps2(F2, amp))) return rc;
+        if (tracked && (rc = full_amps2(Rj, tamp))) return rc;
+        k_full2_apply<R><<<gk, 128, 0, st>>>(fullp, p, g, amp, tracked ? tamp : nullptr, F2, Rj, bslab(jout));
+        CKL("k_full2_apply");
+      }
+    }
+    return DTMM_OK;
+  }
 };
 
 template <typename R>
@@ -1811,11 +1889,18 @@ int run_engine(const dtmm_transfer_desc* d, const dtmm_transfer_io* io, void* ws
   int rc;
   if (d->method == 4 && d->diffraction == 0 && d->npass == 1) {
     rc = e.run_local4();
-  } else if (d->diffraction == DTMM_DIFFRACTION_FULL && d->npass == 1) {
+  } else if (d->method == 4 && d->diffraction == DTMM_DIFFRACTION_FULL && d->npass == 1) {
     rc = e.run_full4();
   } else {
     rc = e.setup();
-    if (rc == DTMM_OK) rc = d->method == 4 ? e.run4() : (is_real2(d) ? e.run2_real() : e.run2());
+    if (rc == DTMM_OK) {
+      if (d->method == 4)
+        rc = e.run4();
+      else if (d->diffraction == DTMM_DIFFRACTION_FULL)
+        rc = e.run2_full();
+      else
+        rc = is_real2(d) ? e.run2_real() : e.run2();
+    }
   }
   if (launches) *launches = e.launches;
   return rc;

@@ -986,6 +986,7 @@ struct FullParams {
   int* count;          // [lam] in-band modes
   int limx;            // in-band column half width; S = 2 limx + 1 slots, or all W columns
   int S;
+  int C;               // field components per image (4: 4x4, 2: the 2x2 E field)
 };
 
 __host__ __device__ __forceinline__ int full_slot_ix(const FullParams& p, int s, int W) {
@@ -1044,7 +1045,7 @@ __global__ void k_full_rowdft(FullParams p, Grid g, const cpx<R>* __restrict__ f
 __global__ void k_full_coldft(FullParams p, Grid g, const cpx<double>* __restrict__ A, cpx<double>* __restrict__ amp) {
   const int HW = g.H * g.W;
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  const int line = blockIdx.y, img = line / 4;
+  const int line = blockIdx.y, img = line / p.C;
   const int lam = img_lam(g, img);
   if (m >= p.count[lam]) return;
   const int k = p.modes[(size_t)lam * HW + m];
@@ -1126,6 +1127,135 @@ __global__ void __launch_bounds__(128) k_full_apply(FullParams p, Local4Params q
     for (int i = 0; i < nq; ++i) {
       const int img = (q0 + i) * g.nlam + lam;
       for (int c = 0; c < 4; ++c) out[((size_t)img * 4 + c) * HW + pix] = cvt<R>(acc[i][c]);
+    }
+  }
+}
+
+// 2x2 with diffraction = inf (dtmm/propagate_2x2.py:379-464): per pixel and
+// wavelength, every in-band eigenwave (amplitudes amp, in order of
+// increasing beta) through the output voxel's E P E^-1 for its own (beta,
+// phi) of the mode's columns; when the step passes the interface (q.op = 1)
+// E P Eti with the input voxel, or with a tracked wave (tamp) E P (ei w +
+// E^-1 t), whose reflected part Ein . eri . w is summed into refl; the
+// summed waves replace the field, and with `bulk` they and their H parts
+// (E2H of the output voxel) are added to it.  FP64 throughout but the stored
+// fields; q.d is the signed thickness of the one step the reference takes.
+template <typename R>
+__global__ void __launch_bounds__(128) k_full2_apply(FullParams p, Local2Params q, Grid g,
+                                                     const cpx<double>* __restrict__ amp,
+                                                     const cpx<double>* __restrict__ tamp, cpx<R>* __restrict__ out,
+                                                     cpx<R>* __restrict__ refl, cpx<R>* __restrict__ bulk) {
+  const int HW = g.H * g.W;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lam = blockIdx.y;
+  if (pix >= HW) return;
+  const int y = pix / g.W, x = pix - y * g.W;
+  const int m = q.mode < 0 ? 1 : 0, o = 1 - m;
+  const bool iface = q.op != 0, tracked = iface && tamp != nullptr;
+  const int nm = p.count[lam];
+  const double kd = p.ks[lam] * q.d;
+  const double inv_n = 1.0 / ((double)g.H * g.W);
+  const int per = g.nray * g.npol;  // images of this wavelength
+  const cpx<double> z = mk<double>(0.0, 0.0);
+  for (int q0 = 0; q0 < per; q0 += kFullImg) {
+    const int nq = min(kFullImg, per - q0);
+    cpx<double> acc[kFullImg][2], racc[kFullImg][2], bacc[kFullImg][4];
+    for (int i = 0; i < kFullImg; ++i) {
+      acc[i][0] = acc[i][1] = racc[i][0] = racc[i][1] = z;
+      for (int c = 0; c < 4; ++c) bacc[i][c] = z;
+    }
+    for (int mm = 0; mm < nm; ++mm) {
+      const int k = p.modes[(size_t)lam * HW + mm];
+      const int iy = k / g.W, ix = k - iy * g.W;
+      const double beta = p.beta[(size_t)lam * HW + k], phi = p.phi[(size_t)lam * HW + k];
+      cpx<double> Fb[4][4], alb[4];
+      local2_voxel(q, q.lout, y, x, beta, phi, Fb, alb);
+      cpx<double> E[2][2], Ei[2][2], Lw[2][2], RM[2][2], H[2][2];
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+          E[i][j] = Fb[2 * i][2 * j + m];
+          RM[i][j] = H[i][j] = z;
+        }
+      inv2(E, Ei);
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) Lw[i][j] = Ei[i][j];
+      if (iface) {
+        cpx<double> Fa[4][4], ala[4], Fai[4][4], St[2][2], Sr[2][2], A[2][2], Sti[2][2], Ai[2][2], ei[2][2];
+        local2_voxel(q, q.lin, y, x, beta, phi, Fa, ala);
+        inv4(Fa, Fai);
+        for (int i = 0; i < 2; ++i)
+          for (int j = 0; j < 2; ++j) {
+            cpx<double> st = z, sr = z;
+            for (int c = 0; c < 4; ++c) {
+              st = st + Fai[2 * i + m][c] * Fb[c][2 * j + m];
+              sr = sr + Fai[2 * i + o][c] * Fb[c][2 * j + m];
+            }
+            St[i][j] = st;
+            Sr[i][j] = sr;
+            A[i][j] = Fa[2 * i][2 * j + m];
+          }
+        inv2(St, Sti);
+        inv2(A, Ai);
+        mul2(Sti, Ai, ei);
+        for (int i = 0; i < 2; ++i)
+          for (int j = 0; j < 2; ++j) Lw[i][j] = ei[i][j];
+        if (tracked) {
+          cpx<double> eri[2][2], Ein[2][2];
+          mul2(Sr, ei, eri);
+          for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j) Ein[i][j] = Fa[2 * i][2 * j + o];
+          mul2(Ein, eri, RM);
+        }
+      }
+      if (bulk != nullptr) {
+        cpx<double> B[2][2];
+        for (int i = 0; i < 2; ++i)
+          for (int j = 0; j < 2; ++j) B[i][j] = Fb[2 * i + 1][2 * j + m];
+        mul2(B, Ei, H);
+      }
+      const cpx<double> ph[2] = {cexp_i(alb[m] * kd), cexp_i(alb[m + 2] * kd)};
+      double sn, cs;
+      const double r = (double)(((long long)iy * y) % g.H) / g.H + (double)(((long long)ix * x) % g.W) / g.W;
+      sincospi(2.0 * r, &sn, &cs);
+      const cpx<double> wave = mk<double>(cs * inv_n, sn * inv_n);
+      for (int i = 0; i < kFullImg; ++i) {
+        if (i >= nq) break;
+        const int img = (q0 + i) * g.nlam + lam;
+        cpx<double> w[2], v[2];
+        for (int c = 0; c < 2; ++c) w[c] = amp[((size_t)img * 2 + c) * HW + mm] * wave;
+        for (int a = 0; a < 2; ++a) v[a] = Lw[a][0] * w[0] + Lw[a][1] * w[1];
+        if (tracked) {
+          cpx<double> t[2];
+          for (int c = 0; c < 2; ++c) t[c] = tamp[((size_t)img * 2 + c) * HW + mm] * wave;
+          for (int a = 0; a < 2; ++a) {
+            racc[i][a] = racc[i][a] + RM[a][0] * w[0] + RM[a][1] * w[1];
+            v[a] = v[a] + Ei[a][0] * t[0] + Ei[a][1] * t[1];
+          }
+        }
+        v[0] = v[0] * ph[0];
+        v[1] = v[1] * ph[1];
+        const cpx<double> e0 = E[0][0] * v[0] + E[0][1] * v[1], e1 = E[1][0] * v[0] + E[1][1] * v[1];
+        acc[i][0] = acc[i][0] + e0;
+        acc[i][1] = acc[i][1] + e1;
+        if (bulk != nullptr) {
+          bacc[i][0] = bacc[i][0] + e0;
+          bacc[i][2] = bacc[i][2] + e1;
+          bacc[i][1] = bacc[i][1] + H[0][0] * e0 + H[0][1] * e1;
+          bacc[i][3] = bacc[i][3] + H[1][0] * e0 + H[1][1] * e1;
+        }
+      }
+    }
+    for (int i = 0; i < nq; ++i) {
+      const int img = (q0 + i) * g.nlam + lam;
+      for (int c = 0; c < 2; ++c) {
+        out[((size_t)img * 2 + c) * HW + pix] = cvt<R>(acc[i][c]);
+        if (tracked) refl[((size_t)img * 2 + c) * HW + pix] = cvt<R>(racc[i][c]);
+      }
+      if (bulk != nullptr)
+        for (int c = 0; c < 4; ++c) {
+          cpx<R>& b = bulk[((size_t)img * 4 + c) * HW + pix];
+          b = cvt<R>(cvt_d(b) + bacc[i][c]);
+        }
     }
   }
 }

@@ -440,7 +440,10 @@ def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffract
     full = diffraction == np.inf
     d.diffraction = _lib.DIFFRACTION_FULL if full else int(diffraction)
     d.npass = int(npass)
-    d.reflection = (2 if not full and int(diffraction) == 0 else 1) if method == "4x4" else 0
+    if method == "4x4":
+        d.reflection = 2 if not full and int(diffraction) == 0 else 1
+    else:  # the 2x2 defaults of transfer_field
+        d.reflection = 0 if npass == 1 else (2 if full or int(diffraction) > 1 else 1)
     d.precision = _lib.PRECISION_DOUBLE if precision == "double" else _lib.PRECISION_MIXED
     d.betamax, d.nin, d.nout, d.smooth = BETAMAX, N_COVER, N_COVER, SMOOTH
     th = np.ones(int(nlayers))
@@ -513,11 +516,14 @@ def _check_path(method, reflection, npass, diffraction, norm):
     # corrected diffraction matrices; diffraction = inf: every eigenwave
     # exactly (any reflection mode).  2x2: reflection 0 / 1 in k-space (1 also
     # without diffraction), reflection 2 and no diffraction without
-    # reflections in real space; any npass
+    # reflections in real space, diffraction = inf with reflection 0 or 2; any
+    # npass
     local = method == "4x4" and reflection in (2, 4) and diffraction == 0
     full = diffraction == np.inf
-    if full and method != "4x4":
-        raise NotImplementedError("diffraction = inf is built for the 4x4 method")
+    if full and method != "4x4" and reflection == 1:
+        # the reference moves the field to k-space for reflection 1 and its modal
+        # step transforms it once more (dtmm/transfer.py:1091-1098, :1172)
+        raise NotImplementedError("2x2 with diffraction = inf is supported with reflection 0 or 2")
     if method == "4x4" and reflection == 3 and diffraction == 0:
         raise NotImplementedError("reflection mode 3 without diffraction (the reference has no such path)")
     if not (0 <= diffraction <= np.inf):

@@ -1482,6 +1482,72 @@ def propagate_4x4_full(field, ks, layer, nsteps, betamax):
     return field
 
 
+def Etri_mat(fmatin, fmatout, mode=+1):
+    """Inverse E matrix through an interface with reflections and its reflected
+    part (dtmm/tmm.py:1025-1048)."""
+    A = E_mat(fmatin, mode=mode)
+    St, Sr = S_mat(fmatin, fmatout, mode=mode)
+    ei = dotmm(inv(St), inv(A))
+    return ei, dotmm(Sr, ei)
+
+
+def propagate_2x2_full(field, ks, layer, input_layer, nsteps, mode, reflection, betamax, refl, bulk):
+    """2x2 with diffraction = inf (dtmm/propagate_2x2.py:379-464): per
+    wavelength every in-band eigenwave of the E field (in order of increasing
+    beta) through the voxels' E . P . E^-1 for its own (beta, phi); with
+    reflections the first step passes the interface (Eti, or Etri with the
+    tracked wave, whose reflected part is summed into refl); the summed waves
+    (and their H parts) also added to bulk."""
+    shape = field.shape[-2:]
+    d, epsv, epsa = layer
+    _, epsv_in, epsa_in = input_layer
+    kd = ks * d / nsteps
+    out = np.empty_like(field)
+    ii, jj = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    yy, xx = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    npix = shape[0] * shape[1]
+    for step in range(nsteps):
+        for i in range(len(ks)):
+            ffield = fft2(field[..., i, :, :, :])
+            ofield = np.zeros_like(out[..., i, :, :, :])
+            b, p = betaphi(shape, ks[i])
+            mask = b < betamax
+            amplitude = ffield[..., mask]
+            if refl is not None:
+                tampl = fft2(refl[..., i, :, :, :])[..., mask]
+                orefl = refl[..., i, :, :, :]
+                orefl[...] = 0.0
+            order = sorted(zip(range(int(mask.sum())), b[mask], p[mask], ii[mask], jj[mask]), key=lambda e: e[1])
+            for j, beta_, phi_, ie, je in order:
+                alpha, fmat_out = alphaf(beta_, phi_, epsv, epsa)
+                e = E_mat(fmat_out, mode=mode)
+                ei0 = inv(e)
+                pm = phase_mat(alpha, kd[i], mode=mode)
+                wave = np.exp(2j * np.pi * ((ie * yy % shape[0]) / shape[0] + (je * xx % shape[1]) / shape[1])) / npix
+                w = amplitude[..., j][..., None, None] * wave
+                if step == 0 and reflection:
+                    _, fmat_in = alphaf(beta_, phi_, epsv_in, epsa_in)
+                    if refl is not None:
+                        ei, eri = Etri_mat(fmat_in, fmat_out, mode=mode)
+                        ein = E_mat(fmat_in, mode=-mode)
+                        t = tampl[..., j][..., None, None] * wave
+                        orefl += dotmf(ein, dotmf(eri, w))
+                        w = dotmf(ei0, t) + dotmf(ei, w)
+                    else:
+                        w = dotmf(Eti_mat(fmat_in, fmat_out, mode=mode), w)
+                    w = dotmf(e * pm[..., None, :], w)
+                else:
+                    w = dotmdmf(e, pm, ei0, w)
+                ofield = ofield + w
+                if bulk is not None:
+                    obulk = bulk[..., i, :, :, :]
+                    obulk[..., 1::2, :, :] += dotmf(E2H_mat(fmat_out, mode=mode), w)
+                    obulk[..., ::2, :, :] += w
+            out[..., i, :, :, :] = ofield
+        field = out
+    return out, refl
+
+
 def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
                  reflection, multiray, norm, smooth, betamax, ret_bulk, out):
     """4x4 pass x layer sweep (dtmm/transfer.py:618-884): reflection mode 1 in
@@ -1634,8 +1700,12 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
         bulk_out[0] = field_in
         field_in = bulk_out[0]
         field_out = bulk_out[-1]
-    if not (0 <= diffraction < np.inf):
-        raise NotImplementedError("oracle covers finite diffraction for 2x2")
+    if not (0 <= diffraction <= np.inf):
+        raise ValueError("Invalid diffraction value")
+    if diffraction == np.inf and reflection == 1:
+        # the reference transforms the field to k-space for reflection 1 and its
+        # modal step transforms it again (dtmm/transfer.py:1091-1098)
+        raise NotImplementedError("oracle covers 2x2 diffraction = inf with reflection 0 or 2")
     if diffraction > 0:
         field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
     else:
@@ -1666,7 +1736,11 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
             else:
                 bulk = None if bulk_out is None else bulk_out[jout]
             r = None if refl is None else refl[j]
-            if work_in_fft:
+            if diffraction == np.inf:
+                _, (tin, evin, eain) = layers[jin]
+                field, _ = propagate_2x2_full(field, ks, (thickness * direction, ev, ea), (tin, evin, eain), 1,
+                                              direction, reflection, betamax, r, bulk)
+            elif work_in_fft:
                 field = propagate_2x2_effective_1(field, ks, (thickness * direction, ev, ea),
                                                   (di * direction, ei_, ai), (de * direction, ee, ae), beta, phi,
                                                   nsub, diffraction, betamax, direction, bulk, reflection, r)

@@ -423,6 +423,35 @@ CASES = {
                           material=("twisted", dict()), seed=62,
                           illum=dict(beta=0.1, phi=0.3),
                           transfer=dict(method="2x2", diffraction=0, beta=0.1, phi=0.3, ret_bulk=True)),
+    # 2x2 with diffraction = inf: every in-band eigenwave exactly, without and with
+    # interfaces (reflection 2), tracked reflections (npass 2), ret_bulk, biaxial voxels
+    "twox2_modal": dict(shape=(10, 12), nlayers=2, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                       material=("twisted", dict()), seed=63,
+                       illum=dict(beta=0.1, phi=0.3),
+                       transfer=dict(method="2x2", diffraction=np.inf, beta=0.1, phi=0.3)),
+    "twox2_modal_refl2": dict(shape=(8, 10), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                             material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=64,
+                             illum=dict(jones=(1, 0)),
+                             transfer=dict(method="2x2", diffraction=np.inf, reflection=2, beta=0.0, phi=0.0)),
+    "twox2_modal_npass2_bulk": dict(shape=(8, 8), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                   material=("twisted", dict()), seed=65,
+                                   illum=dict(beta=0.1, phi=0.7, jones=(1, 0)),
+                                   transfer=dict(method="2x2", diffraction=np.inf, npass=2, beta=0.1, phi=0.7,
+                                                 ret_bulk=True)),
+    "twox2_modal_biaxial": dict(shape=(8, 10), nlayers=2, wavelengths=[520.0], pixelsize=100.0,
+                               material=("biaxial", dict()), seed=66,
+                               illum=dict(jones=(1, 0)),
+                               transfer=dict(method="2x2", diffraction=np.inf, reflection=2, beta=0.0, phi=0.0)),
+    # the reference's modal 2x2 step advances one sub-step (d / nstep) per layer
+    "twox2_modal_nstep2": dict(shape=(10, 8), nlayers=2, wavelengths=[480.0, 590.0], pixelsize=100.0,
+                               material=("twisted", dict(amplitude=0.4)), seed=67,
+                               illum=dict(beta=0.05, phi=1.1),
+                               transfer=dict(method="2x2", diffraction=np.inf, nstep=2, beta=0.05, phi=1.1)),
+    "twox2_modal_blocks_npass3": dict(shape=(8, 10), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                      blocks=[("twisted", dict(no=1.45, ne=1.6), 1), ("twisted", dict(amplitude=0.5), 2)],
+                                      seed=68,
+                                      illum=dict(jones=(0, 1)),
+                                      transfer=dict(method="2x2", diffraction=np.inf, npass=3, beta=0.0, phi=0.0)),
     "twox2_d0_biaxial": dict(shape=(10, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
                              material=("biaxial", dict()), seed=57,
                              illum=dict(beta=0.1, phi=0.5),

@@ -93,8 +93,9 @@ def test_local_4x4_descriptor_rules(lib):
 
 
 def test_full_diffraction_descriptor_rules(lib):
-    """diffraction = inf (DTMM_DIFFRACTION_FULL): the 4x4 method, any
-    reflection mode 1..4, any npass; the workspace holds the mode tables."""
+    """diffraction = inf (DTMM_DIFFRACTION_FULL): the 4x4 method with any
+    reflection mode 1..4 and the 2x2 method with reflection 0 or 2, any npass;
+    the workspace holds the mode tables."""
     for r in (1, 2, 3, 4):
         d = _desc(diffraction=_lib.DIFFRACTION_FULL, reflection=r)
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) > 2 * 16 * 16 * 16
@@ -103,6 +104,16 @@ def test_full_diffraction_descriptor_rules(lib):
     for kw in (dict(diffraction=_lib.DIFFRACTION_FULL, reflection=5),
                dict(diffraction=_lib.DIFFRACTION_FULL, method=2, reflection=1)):
         assert lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw))) == 0
+    # 2x2: the E field's mode amplitudes, and with npass > 1 every interface's reflected wave
+    size2 = lambda **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(
+        _desc(method=2, diffraction=_lib.DIFFRACTION_FULL, **kw)))
+    s0 = size2(reflection=0)
+    assert s0 > 2 * 16 * 16 * 16 and size2(reflection=2) > 0
+    assert size2(reflection=2, npass=3) - size2(reflection=2) >= 4 * 16 * 16 * 2 * 8
+    assert size2(reflection=0, npass=2) == 0 and "npass" in _lib.last_error()
+    assert size2(reflection=1) == 0 and "reflection 0 or 2" in _lib.last_error()
+    # one DFT grid row per (image, E component)
+    assert size2(reflection=0, npol=2, nlam=16384) == 0 and "32767" in _lib.last_error()
 
 
 def test_reflection4_descriptor_rules(lib):
@@ -128,7 +139,7 @@ def test_2x2_descriptor_rules(lib):
     1 keeps reflected waves (two outer ones in k-space, one per interface in
     real space); reflection 0 with npass > 1 is the reference's ValueError,
     reflection 1 without diffraction and npass > 1 fails in the reference
-    itself and is refused; diffraction = inf is not built for 2x2."""
+    itself and is refused; so is reflection 1 with diffraction = inf."""
     size = lambda **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(method=2, **kw)))
     k1 = size(reflection=1)
     assert k1 > 0 and size(reflection=0) > 0 and size(reflection=1, diffraction=0) > 0

@@ -35,7 +35,11 @@ def test_oracle_only_cases_are_separate_and_have_fixtures():
     has its reference fixture."""
     import os
 
+    from make_fullsize import FULL_CASES
+
     assert not set(ORACLE_CASES) & set(CASES)
+    # the full-grid fixtures share the directory: no case may reuse their names
+    assert not (set(CASES) | set(ORACLE_CASES)) & set(FULL_CASES)
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
     for name in list(CASES) + list(ORACLE_CASES):
         assert os.path.exists(os.path.join(here, name + ".npz")), name
