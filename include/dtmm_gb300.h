@@ -49,10 +49,11 @@ typedef struct dtmm_transfer_desc {
   int method;        /* 4 = "4x4", 2 = "2x2"                                   */
   int diffraction;   /* >= 1: n > 1 groups modes into n x n windows; 0: no
                         diffraction (4x4 with reflection 2 or 4; 2x2);
-                        DTMM_DIFFRACTION_FULL: inf (4x4)                     */
+                        DTMM_DIFFRACTION_FULL: inf                           */
   int reflection;    /* 4x4: 1 (diffraction >= 1), 2 and 4 (any diffraction),
                         3 (diffraction >= 1), any with DTMM_DIFFRACTION_FULL;
-                        2x2: 0, 1 or 2 (1 without diffraction: npass 1)      */
+                        2x2: 0, 1 or 2 (1 without diffraction: npass 1; 0 or
+                        2 with DTMM_DIFFRACTION_FULL)                        */
   int npass;         /* >= 1 (2x2 with npass > 1: reflection 1 or 2)            */
   int precision;     /* DTMM_PRECISION_*                                        */
   double betamax, nin, nout, smooth;
@@ -154,8 +155,9 @@ size_t dtmm_transfer_workspace_size(const dtmm_transfer_desc* desc);
    transfer (DTMM_DIFFRACTION_FULL, dtmm/propagate_4x4.py:515-560), each
    with any npass.  2x2: the k-space split step with reflection 0 or 1
    (dtmm/propagate_2x2.py:19-87, :193-284) and the real-space reflection
-   mode 2 / no-diffraction transfer (dtmm/propagate_2x2.py:91-190, :286-377),
-   any npass (the reflected waves kept per interface, backward passes adding
+   mode 2 / no-diffraction transfer (dtmm/propagate_2x2.py:91-190, :286-377)
+   and the exact modal transfer (DTMM_DIFFRACTION_FULL with reflection 0 or
+   2, dtmm/propagate_2x2.py:379-464), any npass (the reflected waves kept per interface, backward passes adding
    into field_in, dtmm/transfer.py:1074-1183).  `stream` is a
    cudaStream_t (NULL = legacy default stream).  The call enqueues the work
    and returns; results are ready when the stream is.  The first call on a
