@@ -124,6 +124,48 @@ __device__ __forceinline__ double sqrt_pos_fast(double x) {
   return x * y;
 }
 
+// Square root of x > 0 in three FP64 operations from an FP32 seed: with y0
+// the FP32 reciprocal square root of x (input truncated to FP32 in integer
+// arithmetic), r0 = x y0, hy0 = y0 / 2 and e = x - r0^2, sqrt(x) is
+// fma(hy0, e, r0): one Newton-Raphson step for the square root, relative
+// error about 1.5 s^2 for a seed error s (<= 3e-7 here, so <= 2e-13).  The
+// parts are returned so that a caller can fold a term into the last fma.
+// Arguments outside the float range, and non-positive ones, take the library
+// square root (r0 = sqrt(x), hy0 = e = 0).
+__device__ __forceinline__ void sqrt_newton(double x, double& r0, double& hy0, double& e) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32);
+  const int ex = (int)((hi >> 20) & 0x7ffu) - 896;  // FP32 biased exponent
+  if ((hi & 0x80000000u) || ex < 2 || ex > 252) {
+    r0 = sqrt(x);
+    hy0 = 0.0;
+    e = 0.0;
+    return;
+  }
+  const float xf = __uint_as_float(((unsigned)ex << 23) | ((hi & 0xfffffu) << 3) | ((unsigned)u >> 29));
+  const float yf = rsqrtf(xf);
+  r0 = x * f64_of(yf);
+  hy0 = f64_of(0.5f * yf);
+  e = fma(-r0, r0, x);
+}
+
+// 1 / x for a normal x from the FP32 reciprocal of x (input truncated to FP32
+// in integer arithmetic) and two Newton-Raphson steps y <- y + y (1 - x y):
+// four FP64 operations; the seed error (<= 2e-7) squares twice, so the result
+// is within a few FP64 roundings of 1 / x.
+// Arguments outside the float range take the FP64 division.
+__device__ __forceinline__ double rcp_newton(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32);
+  const int ex = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (ex < 2 || ex > 252) return 1.0 / x;
+  const float xf = __uint_as_float((hi & 0x80000000u) | ((unsigned)ex << 23) | ((hi & 0xfffffu) << 3) |
+                                   ((unsigned)u >> 29));
+  double y = f64_of(__frcp_rn(xf));
+  y = fma(y, fma(-x, y, 1.0), y);
+  return fma(y, fma(-x, y, 1.0), y);
+}
+
 // d == 0 (either sign), in integer arithmetic
 __device__ __forceinline__ bool is_zero_d(double d) { return (__double_as_longlong(d) << 1) == 0; }
 #endif

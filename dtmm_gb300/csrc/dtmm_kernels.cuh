@@ -235,6 +235,179 @@ __device__ __forceinline__ bool voxel_E_real(double beta, const VoxelInv& vi, do
   return false;
 }
 
+// Lean solve for complex64 records (real eps above beta^2, uniaxial or
+// isotropic voxels): the per-(ray, window) constants of the launch sit in
+// shared memory (beam terms beta cos phi, beta sin phi; with one eps for
+// every voxel eps11 - beta^2, its square root, eps11 (eps11 - beta^2 +
+// delta) and the ordinary mode's phase record), and per voxel and window the
+// FP64 solve of dtmm/tmm.py:157-278 takes about 24 operations (32 with the
+// backward modes):
+//   gamma = beta cos(az - phi) = cos(az) beta cos(phi) + sin(az) beta sin(phi)
+//   q = u c2 - eps11 kw gamma^2   (a quarter of the discriminant v^2 - 4 u w,
+//                                  whose delta^2 terms cancel)
+//   alpha+- = (-kvh gamma +- sqrt(q)) / u   (kvh = delta sin(t) cos(t); sqrt
+//                                  from an FP32 seed and one Newton step)
+// with sin(t) folded into the cos / sin of (az - phi) of the E entries.  The
+// E rows are rounded to FP32 and rotated back by phi there; the determinants
+// stay FP64 (a rotation keeps them) and are inverted in FP32.
+struct LeanWin {
+  double beta, cp, sp, bcp, bsp;  // beam: beta, cos / sin phi, beta cos / sin phi
+  double ev02, evs, c2;           // one eps for every voxel: eps11 - beta^2, its root, eps11 (ev02 + delta)
+  double awd;                     // a_w d
+  float cpf, spf, r6;             // cos / sin phi in FP32; (evs - a_w) d (one eps for every voxel)
+};
+constexpr int kLeanChunk = 32;  // windows per shared-memory chunk (<= the block size)
+
+template <bool FOUR>
+__device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, float* __restrict__ opv, int pix,
+                                              int ray0, int ray1) {
+  __shared__ LeanWin wc[kLeanChunk];
+  constexpr int nrec = FOUR ? OP_REC : 7;
+  const int HW = g.H * g.W;
+  const bool active = pix < HW;
+  const bool uni = p.wev02 != nullptr;
+  // the voxel's invariants, shared by every ray and window
+  double e0 = 0.0, delta = 0.0, ie = 0.0, iu = 0.0, ct = 0.0, ca = 0.0, sa = 0.0, sca = 0.0, ssa = 0.0;
+  double kvh = 0.0, qb = 0.0, u = 0.0;
+  bool iso = false;
+  size_t slot = 0;
+  if (active) {
+    const int y = pix / g.W, x = pix - y * g.W;
+    const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
+    const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
+    const double* e = (const double*)p.epsv + eo;
+    e0 = e[0];
+    iso = e[0] == e[1] && e[1] == e[2];
+    delta = e[2] - e[0];
+    double st;
+    sincos(p.epsa[ao + 1], &st, &ct);
+    sincos(p.epsa[ao + 2], &sa, &ca);
+    ie = rcp_newton(e0);
+    u = fma(delta, ct * ct, e0);
+    iu = rcp_newton(u);
+    kvh = delta * (st * ct);
+    qb = e0 * (delta * (st * st));
+    sca = st * ca;
+    ssa = st * sa;
+    slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
+  }
+  const int rw0 = ray0 * p.nwin, rw1 = ray1 * p.nwin;
+  for (int c0 = rw0; c0 < rw1; c0 += kLeanChunk) {
+    const int n = min(kLeanChunk, rw1 - c0);
+    __syncthreads();  // the previous chunk is read
+    if ((int)threadIdx.x < n) {
+      const int rw = c0 + threadIdx.x;
+      LeanWin w;
+      w.beta = p.wbeta[rw];
+      w.cp = p.wcos[rw];
+      w.sp = p.wsin[rw];
+      w.bcp = w.beta * w.cp;
+      w.bsp = w.beta * w.sp;
+      const double aw = p.uncorrected ? 0.0 : p.waw[rw];
+      w.awd = aw * p.d;
+      w.cpf = f32_rn(w.cp);
+      w.spf = f32_rn(w.sp);
+      if (uni) {
+        w.ev02 = p.wev02[rw];
+        w.evs = p.wevs[rw];
+        w.c2 = p.wc2[rw];
+        w.r6 = f32_rn((w.evs - aw) * p.d);
+      } else {
+        w.ev02 = w.evs = w.c2 = 0.0;
+        w.r6 = 0.0f;
+      }
+      wc[threadIdx.x] = w;
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int k = 0; k < n; ++k) {
+      const LeanWin& w = wc[k];
+      double ev02, evs, c2;
+      float r6;
+      if (uni) {
+        ev02 = w.ev02;
+        evs = w.evs;
+        c2 = w.c2;
+        r6 = w.r6;
+      } else {
+        ev02 = e0 - w.beta * w.beta;
+        evs = sqrt_pos_fast(ev02);
+        c2 = e0 * (ev02 + delta);
+        r6 = f32_rn(fma(evs, p.d, -w.awd));
+      }
+      // E rows (Ex, Ey) of the forward modes 0, 2 (backward 1, 3), in the beam frame
+      double E00, E10, E02, E12, E01 = 0.0, E11 = 0.0, E03 = 0.0, E13 = 0.0, al0, al1 = 0.0;
+      bool zero = false;
+      if (iso) {
+        al0 = evs;
+        al1 = -evs;
+        E00 = 0.5; E10 = 0.0; E02 = 0.0; E12 = 0.5;
+        if (FOUR) { E01 = 0.5; E11 = 0.0; E03 = 0.0; E13 = 0.5; }
+        zero = evs == 0.0;
+      } else if (w.beta == 0.0) {
+        const double cf = fma(ca, w.cp, sa * w.sp), sf = fma(sa, w.cp, -ca * w.sp);
+        const double sq = sqrt(u * c2) * iu;
+        al0 = sq;
+        al1 = -sq;
+        E00 = cf; E10 = sf; E02 = -evs * sf; E12 = evs * cf;
+        if (FOUR) { E01 = cf; E11 = sf; E03 = -evs * sf; E13 = evs * cf; }
+      } else {
+        const double gama = fma(ca, w.bcp, sa * w.bsp);
+        const double g2 = gama * gama;
+        const double q = fma(-qb, g2, u * c2);
+        double r0, hy0, eq;
+        sqrt_newton(q, r0, hy0, eq);
+        const double kvg = kvh * gama;
+        al0 = fma(hy0, eq, r0 - kvg) * iu;
+        const double cfst = fma(sca, w.cp, ssa * w.sp), sfst = fma(ssa, w.cp, -sca * w.sp);
+        const double ctbeta = ct * w.beta;
+        const double ev02cf = ev02 * cfst;
+        E00 = fma(al0, ctbeta, -ev02cf) * ie;  E10 = -sfst;
+        E02 = evs * sfst;                      E12 = fma(-evs, cfst, ctbeta);
+        if (FOUR) {
+          al1 = -fma(hy0, eq, r0 + kvg) * iu;
+          E01 = fma(-al1, ctbeta, ev02cf) * ie;  E11 = sfst;
+          E03 = -E02;                            E13 = fma(evs, cfst, ctbeta);
+        }
+      }
+      const double x2 = E02 * E10;
+      const double detf = fma(E00, E12, -x2);
+      const double detb = FOUR ? fma(E01, E13, -(E03 * E11)) : 1.0;
+      if (is_zero_d(detf) || is_zero_d(detb)) zero = true;
+      float rec[nrec];
+      if (zero) {
+#pragma unroll
+        for (int i = 0; i < nrec; ++i) rec[i] = 0.0f;
+      } else {
+        // the E rows back to the lab frame (rotation by phi), in FP32
+        const float ex0 = f32_rn(E00), ey0 = f32_rn(E10), ex2 = f32_rn(E02), ey2 = f32_rn(E12);
+        rec[0] = ex0 * w.cpf - ey0 * w.spf;
+        rec[1] = ex2 * w.cpf - ey2 * w.spf;
+        rec[2] = ex0 * w.spf + ey0 * w.cpf;
+        rec[3] = ex2 * w.spf + ey2 * w.cpf;
+        const float df = f32_rn(detf);
+        rec[4] = fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf);
+        rec[5] = iso ? r6 : f32_rn(fma(al0, p.d, -w.awd));
+        rec[6] = r6;
+        if (FOUR) {
+          const float ex1 = f32_rn(E01), ey1 = f32_rn(E11), ex3 = f32_rn(E03), ey3 = f32_rn(E13);
+          rec[7] = ex1 * w.cpf - ey1 * w.spf;
+          rec[8] = ex3 * w.cpf - ey3 * w.spf;
+          rec[9] = ex1 * w.spf + ey1 * w.cpf;
+          rec[10] = ex3 * w.spf + ey3 * w.cpf;
+          const float db = f32_rn(detb);
+          rec[11] = fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb);
+          rec[12] = iso ? -r6 : f32_rn(fma(al1, p.d, w.awd));
+          rec[13] = -r6;
+        }
+      }
+      float* o = opv + (size_t)(c0 + k) * OP_REC * HW + slot;
+#pragma unroll
+      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
+    }
+  }
+}
+
 // BIAX: the material holds biaxial voxels, which take the general
 // eigen-solve (complex path only; without BIAX every voxel is isotropic or
 // uniaxial and the kernel keeps the registers of those closed forms)
@@ -244,6 +417,10 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
   const int ray0 = blockIdx.y * p.rays_per_thread;
   const int ray1 = min(ray0 + p.rays_per_thread, p.nray);
+  if constexpr (REAL && sizeof(R) == 4) {  // every thread of the block: the solve shares window tables
+    voxel_op_lean<FOUR>(p, g, (float*)opv, pix, ray0, ray1);
+    return;
+  }
   if (pix >= HW) return;
   const int y = pix / g.W, x = pix - y * g.W;
   const long long eo = p.layer * p.ev_s[0] + y * p.ev_s[1] + x * p.ev_s[2];
@@ -255,94 +432,6 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   // the voxel's trigonometry and invariants, shared by every ray and window
   double sa, ca;
   sincos(azim, &sa, &ca);
-  if constexpr (REAL && sizeof(R) == 4) {
-    // complex64 records: the eigen-solve in FP64 with the discriminant in the
-    // form u c2 - eps11 delta st^2 gamma^2 (the delta^2 terms of v^2 - 4 u w
-    // cancel), its square root from sqrt_pos_fast, the determinants from the
-    // local-frame E (a rotation keeps them); only the rotation of the E rows
-    // back to the lab frame, whose entries are stored in FP32, runs in FP32
-    VoxelInv vi;
-    voxel_inv((const double*)p.epsv + eo, theta, vi);
-    const double u4 = 4.0 * vi.u, b4 = 4.0 * vi.ev[0] * vi.kw;
-    for (int rw = ray0 * p.nwin; rw < ray1 * p.nwin; ++rw) {
-      const double beta = p.wbeta[rw];
-      const double cp = p.wcos[rw], sp = p.wsin[rw];
-      const double cf = ca * cp + sa * sp, sf = sa * cp - ca * sp;
-      const double aw = p.uncorrected ? 0.0 : p.waw[rw];
-      double ev02, evs, c2;
-      if (p.wev02 != nullptr) {
-        ev02 = p.wev02[rw];
-        evs = p.wevs[rw];
-        c2 = p.wc2[rw];
-      } else {
-        ev02 = vi.ev[0] - beta * beta;
-        evs = sqrt_pos_fast(ev02);
-        c2 = vi.ev[0] * (ev02 + (vi.ev[2] - vi.ev[0]));
-      }
-      double E[2][4], al[4];
-      bool zero = false;
-      if (vi.iso || beta == 0.0) {
-        zero = voxel_E_real<FOUR>(beta, vi, ev02, evs, c2, sf, cf, E, al);
-      } else {
-        const double st = vi.st, ct = vi.ct;
-        const double gama = beta * cf;
-        const double disc = fma(-b4, gama * gama, u4 * c2);
-        const double sq = sqrt_pos_fast(disc) * vi.iu2;
-        const double vh = (vi.kv * gama) * vi.iu2;
-        const double evpp = sq - vh;
-        const double ctbeta = ct * beta;
-        const double cfst = cf * st, sfst = st * sf;
-        const double ev02cf = ev02 * cfst;
-        E[0][0] = (evpp * ctbeta - ev02cf) * vi.ie;  E[1][0] = -sfst;
-        E[0][2] = evs * sfst;                        E[1][2] = ctbeta - evs * cfst;
-        al[0] = evpp;
-        al[2] = evs;
-        if (FOUR) {
-          const double evpm = -vh - sq;
-          E[0][1] = (ev02cf - evpm * ctbeta) * vi.ie;  E[1][1] = sfst;
-          E[0][3] = -evs * sfst;                       E[1][3] = evs * cfst + ctbeta;
-          al[1] = evpm;
-          al[3] = -evs;
-        }
-      }
-      const double detf = E[0][0] * E[1][2] - E[0][2] * E[1][0];
-      double detb = 1.0;
-      if (FOUR) detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
-      if (is_zero_d(detf) || is_zero_d(detb)) zero = true;
-      R rec[nrec];
-      if (zero) {
-#pragma unroll
-        for (int i = 0; i < nrec; ++i) rec[i] = (R)0;
-      } else {
-        // rotate the E rows back by the beam azimuth phi, in FP32
-        const float cpf = f32_rn(cp), spf = f32_rn(sp);
-        float ef[2][4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          if (!FOUR && (m & 1)) continue;
-          const float ex = f32_rn(E[0][m]), ey = f32_rn(E[1][m]);
-          ef[0][m] = ex * cpf - ey * spf;
-          ef[1][m] = ex * spf + ey * cpf;
-        }
-        const float df = f32_rn(detf);
-        rec[0] = ef[0][0]; rec[1] = ef[0][2]; rec[2] = ef[1][0]; rec[3] = ef[1][2];
-        rec[4] = fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf);
-        rec[5] = f32_rn((al[0] - aw) * p.d);
-        rec[6] = f32_rn((al[2] - aw) * p.d);
-        if (FOUR) {
-          const float db = f32_rn(detb);
-          rec[7] = ef[0][1]; rec[8] = ef[0][3]; rec[9] = ef[1][1]; rec[10] = ef[1][3];
-          rec[11] = fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb);
-          rec[12] = f32_rn((al[1] + aw) * p.d);
-          rec[13] = f32_rn((al[3] + aw) * p.d);
-        }
-      }
-      R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
-#pragma unroll
-      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
-    }
-    return;
-  }
   if constexpr (REAL) {
     VoxelInv vi;
     voxel_inv((const double*)p.epsv + eo, theta, vi);
