@@ -615,11 +615,17 @@ struct Engine {
       rl.threads = std::max(((nl * n1 + 31) / 32) * 32, 32);
       const int ngrp = (d.nlam + p.G - 1) / p.G;
       const int npg = (d.npol + p.PB - 1) / p.PB;
-      rl.grid = dim3(d.height, d.nray * ngrp * npg);
+      // one layer's operator records beyond half of L2 (128 MB): the groups of
+      // a row run next to each other and share the row's records in L2
+      const size_t rec_bytes = (re ? sizeof(R) : sizeof(cpx<R>)) * (size_t)d.nray * L.nwin *
+                               (L.C == 4 ? OP_REC : 7) * L.HW;
+      RowParams q = p;
+      q.groups_inner = rec_bytes > ((size_t)64 << 20) ? 1 : 0;
+      rl.grid = q.groups_inner ? dim3(d.nray * ngrp * npg, d.height) : dim3(d.height, d.nray * ngrp * npg);
       rl.st = st;
       mark(PROF_ROW);
       const int band = re ? row_band_pick(d.width, blim_max) : 0;
-      const cudaError_t e = row_reg_dispatch(d.width, C, re, band, rl, p, g, Ub, Xb);
+      const cudaError_t e = row_reg_dispatch(d.width, C, re, band, rl, q, g, Ub, Xb);
       mark(PROF_ROW);
       ++launches;
       if (e != cudaSuccess) return fail(DTMM_ECUDA, "launch k_layer_row_reg: %s", cudaGetErrorString(e));

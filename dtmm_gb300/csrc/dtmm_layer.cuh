@@ -104,6 +104,7 @@ struct RowParams {
   int win_only;          // >= 0: only this window (its own sub-step chain), -1: all
   int use_cx;            // apply the window's beta_x weight (first sub-step of a chain)
   int accumulate;        // add the result to X instead of overwriting it
+  int groups_inner;      // register row pass: blockIdx.x the group, blockIdx.y the row (else the reverse)
 };
 
 template <typename R>

@@ -88,8 +88,12 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
   const int H = g.H;
   const int ngrp = (g.nlam + p.G - 1) / p.G;
   const int npg = (g.npol + p.PB - 1) / p.PB;
-  const int y = blockIdx.x;
-  const int pg = blockIdx.y % npg, rg = blockIdx.y / npg;
+  // groups_inner: the groups of one row are neighbours in the launch order,
+  // so that the row's operator records (shared by every wavelength and
+  // polarisation) come from HBM once and from L2 for the other groups
+  const int y = p.groups_inner ? blockIdx.y : blockIdx.x;
+  const int gi = p.groups_inner ? blockIdx.x : blockIdx.y;
+  const int pg = gi % npg, rg = gi / npg;
   const int ray = rg / ngrp, grp = rg - ray * ngrp;
   const int lam0 = grp * p.G, pol0 = pg * p.PB;
   const int G = min(p.G, g.nlam - lam0);
@@ -160,42 +164,56 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
       }
       __syncthreads();
       const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
-      for (int x = threadIdx.x; x < W; x += blockDim.x) {
-        T ef[4], arg_f[2], idf;
-        T eb[4], arg_b[2], idb;
+      // XU pixels per thread and round: their records are loaded together, so
+      // that several rounds of global loads are in flight (long rows hold
+      // few blocks per SM)
+      constexpr int XU = (C == 2 && N2 >= 32) ? 4 : 1;
+      for (int x0 = threadIdx.x; x0 < W; x0 += XU * blockDim.x) {
+        T ef[XU][4], arg_f[XU][2], idf[XU];
+        T eb[XU][4], arg_b[XU][2], idb[XU];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + x];
-        idf = opw[(size_t)4 * HW + x] * sc;
-        arg_f[0] = opw[(size_t)5 * HW + x];
-        arg_f[1] = opw[(size_t)6 * HW + x];
-        if (C == 4) {
+        for (int k = 0; k < XU; ++k) {
+          const int x = x0 + k * blockDim.x;
+          if (x >= W) break;
 #pragma unroll
-          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + x];
-          idb = opw[(size_t)11 * HW + x] * sc;
-          arg_b[0] = opw[(size_t)12 * HW + x];
-          arg_b[1] = opw[(size_t)13 * HW + x];
-        }
-        for (int g2 = 0; g2 < G; ++g2) {
-          const R kph = s_kph[g2];
-          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
-          cpx<R> pb0, pb1;
+          for (int r = 0; r < 4; ++r) ef[k][r] = opw[(size_t)r * HW + x];
+          idf[k] = opw[(size_t)4 * HW + x] * sc;
+          arg_f[k][0] = opw[(size_t)5 * HW + x];
+          arg_f[k][1] = opw[(size_t)6 * HW + x];
           if (C == 4) {
-            pb0 = phase_of(arg_b[0], kph) * idb;
-            pb1 = phase_of(arg_b[1], kph) * idb;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) eb[k][r] = opw[(size_t)(7 + r) * HW + x];
+            idb[k] = opw[(size_t)11 * HW + x] * sc;
+            arg_b[k][0] = opw[(size_t)12 * HW + x];
+            arg_b[k][1] = opw[(size_t)13 * HW + x];
           }
-          for (int q = 0; q < NP; ++q) {
-            const int l0 = (g2 * NP + q) * C;
-            const cpx<R>* h = tmp + (size_t)l0 * LS + x;
-            cpx<R>* a = acc + (size_t)l0 * LS + x;
+        }
+#pragma unroll
+        for (int k = 0; k < XU; ++k) {
+          const int x = x0 + k * blockDim.x;
+          if (x >= W) break;
+          for (int g2 = 0; g2 < G; ++g2) {
+            const R kph = s_kph[g2];
+            const cpx<R> pf0 = phase_of(arg_f[k][0], kph) * idf[k], pf1 = phase_of(arg_f[k][1], kph) * idf[k];
+            cpx<R> pb0, pb1;
             if (C == 4) {
-              cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
-              apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
-              a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
-            } else {
-              cpx<R> a0 = a[0], a1 = a[LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
-              a[0] = a0; a[LS] = a1;
+              pb0 = phase_of(arg_b[k][0], kph) * idb[k];
+              pb1 = phase_of(arg_b[k][1], kph) * idb[k];
+            }
+            for (int q = 0; q < NP; ++q) {
+              const int l0 = (g2 * NP + q) * C;
+              const cpx<R>* h = tmp + (size_t)l0 * LS + x;
+              cpx<R>* a = acc + (size_t)l0 * LS + x;
+              if (C == 4) {
+                cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
+                apply_block<R, T>(ef[k], pf0, pf1, h[0], h[2 * LS], a0, a2);
+                apply_block<R, T>(eb[k], pb0, pb1, h[LS], h[3 * LS], a1, a3);
+                a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
+              } else {
+                cpx<R> a0 = a[0], a1 = a[LS];
+                apply_block<R, T>(ef[k], pf0, pf1, h[0], h[LS], a0, a1);
+                a[0] = a0; a[LS] = a1;
+              }
             }
           }
         }
