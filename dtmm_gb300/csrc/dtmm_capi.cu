@@ -617,8 +617,7 @@ struct Engine {
       const int npg = (d.npol + p.PB - 1) / p.PB;
       // one layer's operator records beyond half of L2 (128 MB): the groups of
       // a row run next to each other and share the row's records in L2
-      const size_t rec_bytes = (re ? sizeof(R) : sizeof(cpx<R>)) * (size_t)d.nray * L.nwin *
-                               (L.C == 4 ? OP_REC : 7) * L.HW;
+      const size_t rec_bytes = (re ? sizeof(R) : sizeof(cpx<R>)) * (size_t)d.nray * L.nwin * p.rec_stride * L.HW;
       RowParams q = p;
       q.groups_inner = rec_bytes > ((size_t)64 << 20) ? 1 : 0;
       rl.grid = q.groups_inner ? dim3(d.nray * ngrp * npg, d.height) : dim3(d.height, d.nray * ngrp * npg);
@@ -647,6 +646,8 @@ struct Engine {
     p.cx = L.nx > 1 ? (const void*)A<R>(L.cx) : nullptr;
     p.wzero = L.nwin > 1 ? wzero() : nullptr;
     p.op = op;
+    // records per voxel: both mode blocks for 4x4 and for 2x2 passes that alternate in direction
+    p.rec_stride = (d.method == 4 || d.npass > 1) ? OP_REC : REC_BLOCK;
     p.ks = ks();
     p.dir = dir;
     p.in_scale = 1.0 / ((double)d.width * (double)d.height);
@@ -814,6 +815,7 @@ struct Engine {
     p.nwin = L.nwin;
     // both mode blocks for 4x4, and for 2x2 passes that alternate in direction
     p.four = d.method == 4 || d.npass > 1;
+    p.scale = 1.0 / ((double)d.width * (double)d.height);
     p.uncorrected = d.method == 2 && d.diffraction == 0;
     p.nray = d.nray;
     // every ray of a voxel in one thread (its trigonometry computed once)
@@ -1475,7 +1477,7 @@ struct Engine {
   }
 
   // byte offset of the backward-mode records in a voxel's operator records
-  size_t back_records() const { return (size_t)7 * L.HW * (real_ops() ? sizeof(R) : sizeof(cpx<R>)); }
+  size_t back_records() const { return (size_t)REC_BLOCK * (real_ops() ? sizeof(R) : sizeof(cpx<R>)); }
 
   // 2x2 method in k-space (reflection 0 or 1; dtmm/propagate_2x2.py:19-87,
   // :193-284 driven by dtmm/transfer.py:1074-1183) over npass passes that

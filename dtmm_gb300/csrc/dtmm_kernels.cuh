@@ -141,10 +141,12 @@ struct OpParams {
   // 1: no beam correction (a_w = 0): the plain E P E^-1 of a transfer without
   // diffraction matrices (2x2, reflection 1, diffraction 0)
   int uncorrected;
+  double scale;          // folded into the records (the row pass's inverse-transform scale)
 };
 
-// Records per voxel and window, [ray][window][record][H][W]: complex, or real
-// when the host has proven the real path (real eps above beta^2 everywhere).
+// Records per voxel and window, [ray][window][H][W][record] (REC_BLOCK per
+// mode block): complex, or real when the host has proven the real path (real
+// eps above beta^2 everywhere).
 
 // Uniaxial / isotropic E rows and eigenvalues in real FP64 arithmetic, valid
 // when every eigenvalue and the effective medium exceed beta^2 (then every
@@ -262,7 +264,8 @@ template <bool FOUR>
 __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, float* __restrict__ opv, int pix,
                                               int ray0, int ray1) {
   __shared__ LeanWin wc[kLeanChunk];
-  constexpr int nrec = FOUR ? OP_REC : 7;
+  constexpr int nrec = FOUR ? OP_REC : REC_BLOCK;
+  const float scf = f32_rn(p.scale);
   const int HW = g.H * g.W;
   const bool active = pix < HW;
   const bool uni = p.wev02 != nullptr;
@@ -379,31 +382,30 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
 #pragma unroll
         for (int i = 0; i < nrec; ++i) rec[i] = 0.0f;
       } else {
-        // the E rows back to the lab frame (rotation by phi), in FP32
+        // the E rows back to the lab frame (rotation by phi), in FP32; the
+        // first column times scale / det (formed in FP32 from the FP64 det)
         const float ex0 = f32_rn(E00), ey0 = f32_rn(E10), ex2 = f32_rn(E02), ey2 = f32_rn(E12);
-        rec[0] = ex0 * w.cpf - ey0 * w.spf;
-        rec[1] = ex2 * w.cpf - ey2 * w.spf;
-        rec[2] = ex0 * w.spf + ey0 * w.cpf;
-        rec[3] = ex2 * w.spf + ey2 * w.cpf;
         const float df = f32_rn(detf);
-        rec[4] = fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf);
-        rec[5] = iso ? r6 : f32_rn(fma(al0, p.d, -w.awd));
-        rec[6] = r6;
+        const float sf = (fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf)) * scf;
+        rec[0] = (ex0 * w.cpf - ey0 * w.spf) * sf;
+        rec[1] = ex2 * w.cpf - ey2 * w.spf;
+        rec[2] = (ex0 * w.spf + ey0 * w.cpf) * sf;
+        rec[3] = ex2 * w.spf + ey2 * w.cpf;
+        rec[4] = iso ? r6 : f32_rn(fma(al0, p.d, -w.awd));
+        rec[5] = r6;
         if (FOUR) {
           const float ex1 = f32_rn(E01), ey1 = f32_rn(E11), ex3 = f32_rn(E03), ey3 = f32_rn(E13);
-          rec[7] = ex1 * w.cpf - ey1 * w.spf;
-          rec[8] = ex3 * w.cpf - ey3 * w.spf;
-          rec[9] = ex1 * w.spf + ey1 * w.cpf;
-          rec[10] = ex3 * w.spf + ey3 * w.cpf;
           const float db = f32_rn(detb);
-          rec[11] = fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb);
-          rec[12] = iso ? -r6 : f32_rn(fma(al1, p.d, w.awd));
-          rec[13] = -r6;
+          const float sb = (fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb)) * scf;
+          rec[6] = (ex1 * w.cpf - ey1 * w.spf) * sb;
+          rec[7] = ex3 * w.cpf - ey3 * w.spf;
+          rec[8] = (ex1 * w.spf + ey1 * w.cpf) * sb;
+          rec[9] = ex3 * w.spf + ey3 * w.cpf;
+          rec[10] = iso ? -r6 : f32_rn(fma(al1, p.d, w.awd));
+          rec[11] = -r6;
         }
       }
-      float* o = opv + (size_t)(c0 + k) * OP_REC * HW + slot;
-#pragma unroll
-      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
+      store_recs<nrec, float>(opv + ((size_t)(c0 + k) * HW + slot) * nrec, rec);
     }
   }
 }
@@ -427,7 +429,7 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const long long ao = p.layer * p.ea_s[0] + y * p.ea_s[1] + x * p.ea_s[2];
   const double theta = p.epsa[ao + 1], azim = p.epsa[ao + 2];
   if (p.eps_dev != nullptr) p.eps_eff = mk<double>(p.eps_dev[0], p.eps_dev[1]);
-  constexpr int nrec = FOUR ? OP_REC : 7;
+  constexpr int nrec = FOUR ? OP_REC : REC_BLOCK;
   const size_t slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
   // the voxel's trigonometry and invariants, shared by every ray and window
   double sa, ca;
@@ -465,36 +467,24 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
       double detb = 1.0;
       if (FOUR) detb = E[0][1] * E[1][3] - E[0][3] * E[1][1];
       if (detf == 0.0 || detb == 0.0) zero = true;
-      // records in the bulk precision; with complex64 records the FP64
-      // determinant is rounded to FP32 and inverted there (correctly rounded
-      // FP32 reciprocal: the stored value differs from the rounded FP64
-      // quotient by at most one FP32 ulp), which spares the FP64 division;
-      // determinants too small for FP32 keep the FP64 division
+      // records in the bulk precision, the first column times scale / det
       R rec[nrec];
       if (zero) {
 #pragma unroll
         for (int i = 0; i < nrec; ++i) rec[i] = (R)0;
       } else {
-        rec[0] = to_r<R>(E[0][0]); rec[1] = to_r<R>(E[0][2]); rec[2] = to_r<R>(E[1][0]); rec[3] = to_r<R>(E[1][2]);
-        if constexpr (sizeof(R) == 4)
-          rec[4] = fabs(detf) > 1e-30 ? __frcp_rn(f32_rn(detf)) : f32_rn(1.0 / detf);
-        else
-          rec[4] = 1.0 / detf;
-        rec[5] = to_r<R>((al[0] - aw) * p.d);
-        rec[6] = to_r<R>((al[2] - aw) * p.d);
+        const double sfd = p.scale / detf;
+        rec[0] = to_r<R>(E[0][0] * sfd); rec[1] = to_r<R>(E[0][2]); rec[2] = to_r<R>(E[1][0] * sfd); rec[3] = to_r<R>(E[1][2]);
+        rec[4] = to_r<R>((al[0] - aw) * p.d);
+        rec[5] = to_r<R>((al[2] - aw) * p.d);
         if (FOUR) {
-          rec[7] = to_r<R>(E[0][1]); rec[8] = to_r<R>(E[0][3]); rec[9] = to_r<R>(E[1][1]); rec[10] = to_r<R>(E[1][3]);
-          if constexpr (sizeof(R) == 4)
-            rec[11] = fabs(detb) > 1e-30 ? __frcp_rn(f32_rn(detb)) : f32_rn(1.0 / detb);
-          else
-            rec[11] = 1.0 / detb;
-          rec[12] = to_r<R>((al[1] + aw) * p.d);
-          rec[13] = to_r<R>((al[3] + aw) * p.d);
+          const double sbd = p.scale / detb;
+          rec[6] = to_r<R>(E[0][1] * sbd); rec[7] = to_r<R>(E[0][3]); rec[8] = to_r<R>(E[1][1] * sbd); rec[9] = to_r<R>(E[1][3]);
+          rec[10] = to_r<R>((al[1] + aw) * p.d);
+          rec[11] = to_r<R>((al[3] + aw) * p.d);
         }
       }
-      R* o = (R*)opv + (size_t)rw * OP_REC * HW + slot;
-#pragma unroll
-      for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = rec[i];
+      store_recs<nrec, R>((R*)opv + ((size_t)rw * HW + slot) * nrec, rec);
     }
     return;
   }
@@ -599,25 +589,23 @@ __global__ void k_voxel_op(OpParams p, Grid g, void* __restrict__ opv) {
   const bool zf = (detf.re == 0.0 && detf.im == 0.0);
   const bool zb = (detb.re == 0.0 && detb.im == 0.0);
   if (zf || (FOUR && zb)) zero = true;
-  cpx<double> rec[OP_REC];
+  cpx<R> rec[nrec];
   if (zero) {
-    for (int i = 0; i < OP_REC; ++i) rec[i] = z0;
+    for (int i = 0; i < nrec; ++i) rec[i] = cvt<R>(z0);
   } else {
-    rec[0] = E[0][0]; rec[1] = E[0][2]; rec[2] = E[1][0]; rec[3] = E[1][2];
-    rec[4] = cdiv(mk<double>(1.0, 0.0), detf);
-    rec[5] = (al[0] - aw) * p.d;
-    rec[6] = (al[2] - aw) * p.d;
+    // first column times scale / det
+    const cpx<double> sfc = cdiv(mk<double>(p.scale, 0.0), detf);
+    rec[0] = cvt<R>(E[0][0] * sfc); rec[1] = cvt<R>(E[0][2]); rec[2] = cvt<R>(E[1][0] * sfc); rec[3] = cvt<R>(E[1][2]);
+    rec[4] = cvt<R>((al[0] - aw) * p.d);
+    rec[5] = cvt<R>((al[2] - aw) * p.d);
     if (FOUR) {
-      rec[7] = E[0][1]; rec[8] = E[0][3]; rec[9] = E[1][1]; rec[10] = E[1][3];
-      rec[11] = cdiv(mk<double>(1.0, 0.0), detb);
-      rec[12] = (al[1] + aw) * p.d;
-      rec[13] = (al[3] + aw) * p.d;
-    } else {
-      for (int i = 7; i < OP_REC; ++i) rec[i] = z0;
+      const cpx<double> sbc = cdiv(mk<double>(p.scale, 0.0), detb);
+      rec[6] = cvt<R>(E[0][1] * sbc); rec[7] = cvt<R>(E[0][3]); rec[8] = cvt<R>(E[1][1] * sbc); rec[9] = cvt<R>(E[1][3]);
+      rec[10] = cvt<R>((al[1] + aw) * p.d);
+      rec[11] = cvt<R>((al[3] + aw) * p.d);
     }
   }
-  cpx<R>* o = (cpx<R>*)opv + (size_t)rw * OP_REC * HW + slot;
-  for (int i = 0; i < nrec; ++i) o[(size_t)i * HW] = cvt<R>(rec[i]);
+  store_recs<nrec, cpx<R>>((cpx<R>*)opv + ((size_t)rw * HW + slot) * nrec, rec);
   }
 }
 
@@ -2126,7 +2114,6 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
   const int nwin = p.nx * p.ny;
   for (int t = threadIdx.x; t < W; t += blockDim.x) tw[t] = ((const cpx<R>*)p.tw)[t];
   for (int t = threadIdx.x; t < nlines * LS; t += blockDim.x) acc[t] = mk<R>(0, 0);
-  const R sc = (R)p.in_scale;
   __syncthreads();
   // line l <-> (image = (g, pol), component c): l = (g * NP + pol) * C + c
   for (int j = 0; j < p.ny; ++j) {
@@ -2154,29 +2141,21 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
       fft_dif<R, true>(tmp, 1, LS, nlines, true, tw, p.plan);
       // per-voxel operator of window w; records are stored in the row's
       // digit-reversed order (slot q), so these loads are coalesced
-      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      const int rs = p.rec_stride;
+      const T* opw = (const T*)p.op + (((size_t)ray * nwin + w) * HW + (size_t)y * W) * rs;
+      constexpr int NR = C == 4 ? OP_REC : REC_BLOCK;
       for (int q = threadIdx.x; q < W; q += blockDim.x) {
-        T ef[4], arg_f[2], idf;
-        T eb[4], arg_b[2], idb;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) ef[r] = opw[(size_t)r * HW + q];
-        idf = opw[(size_t)4 * HW + q];
-        arg_f[0] = opw[(size_t)5 * HW + q];
-        arg_f[1] = opw[(size_t)6 * HW + q];
-        if (C == 4) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) eb[r] = opw[(size_t)(7 + r) * HW + q];
-          idb = opw[(size_t)11 * HW + q];
-          arg_b[0] = opw[(size_t)12 * HW + q];
-          arg_b[1] = opw[(size_t)13 * HW + q];
-        }
+        T rec[NR];
+        load_recs<NR, T>(opw + (size_t)q * rs, rec);
+        const T* ef = rec;
+        const T* eb = rec + (C == 4 ? REC_BLOCK : 0);
         for (int gl = 0; gl < G; ++gl) {
           const R kph = (R)(p.ks[lam0 + gl] * p.dir);
-          const cpx<R> pf0 = phase_of(arg_f[0], kph) * idf, pf1 = phase_of(arg_f[1], kph) * idf;
+          const cpx<R> pf0 = phase_of(ef[4], kph), pf1 = phase_of(ef[5], kph);
           cpx<R> pb0, pb1;
           if (C == 4) {
-            pb0 = phase_of(arg_b[0], kph) * idb;
-            pb1 = phase_of(arg_b[1], kph) * idb;
+            pb0 = phase_of(eb[4], kph);
+            pb1 = phase_of(eb[5], kph);
           }
           for (int pol = 0; pol < NP; ++pol) {
             const int l0 = (gl * NP + pol) * C;
@@ -2184,12 +2163,12 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
             cpx<R>* a = acc + (size_t)l0 * LS + q;
             if (C == 4) {
               cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[2 * LS] * sc, a0, a2);
-              apply_block<R, T>(eb, pb0, pb1, h[LS] * sc, h[3 * LS] * sc, a1, a3);
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
+              apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
               a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
             } else {
               cpx<R> a0 = a[0], a1 = a[LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0] * sc, h[LS] * sc, a0, a1);
+              apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
               a[0] = a0; a[LS] = a1;
             }
           }

@@ -7,14 +7,23 @@
 //                          image = (ray * npol + pol) * nlam + lam
 //                          (the reference's ([rays],[pols],lambda,4,H,W) order)
 //   window-row buffers   : [j][image][component][H][W]
-//   layer operators      : [ray][window][record][H][W]   (14 records)
+//   layer operators      : [ray][window][H][W][record], 6 records per mode
+//                          block (forward, then backward with both blocks)
 #pragma once
 
 #include "dtmm_common.cuh"
 
 namespace dtmm {
 
-constexpr int OP_REC = 14;  // records of one per-voxel layer operator
+// Records of one per-voxel layer operator, per mode block (forward modes 0,
+// 2; backward 1, 3): the 2x2 block E of the block's E rows with its first
+// column scaled by the scale of the pass over det(E), and the two phase
+// arguments, (e0 s, e1, e2 s, e3, arg0, arg1) with s = scale / det(E).
+// E' = E diag(s, 1) has det(E') = scale, so E' diag(p) adj(E') = scale E
+// diag(p) E^-1.  A voxel keeps its records next to each other (REC_BLOCK
+// or 2 REC_BLOCK of them), so they are read with vector loads.
+constexpr int REC_BLOCK = 6;
+constexpr int OP_REC = 2 * REC_BLOCK;  // records of both blocks
 
 enum KOp { KOP_NONE = 0, KOP_DIAG = 1, KOP_MAT = 2 };
 
@@ -92,7 +101,8 @@ struct RowParams {
   int nx, ny;            // windows per axis (1, 1 without windows)
   const void* cx;        // [ray][i][lam][W] (null = weight 1)
   const int* wzero;      // [ray][nx*ny]
-  const void* op;        // [ray][win][OP_REC][H][W]
+  const void* op;        // [ray][win][H][W][rec_stride] (offset to the block the pass uses)
+  int rec_stride;        // records per voxel: REC_BLOCK, or OP_REC with both blocks
   const double* ks;      // [lam]
   double dir;            // propagation direction (+1 / -1)
   double in_scale;       // 1/W of the inverse row transform (and 1/H of the column one)
@@ -133,7 +143,61 @@ __device__ __forceinline__ cpx<R> phase_of(R arg, R k) {
   }
 }
 
-// one 2x2 block of the per-voxel operator: out += E . diag(P') . adj(E) . h
+// the n records of one voxel, in 16-byte loads when n records fill whole
+// 16-byte words (every voxel's records then start on a 16-byte boundary),
+// else in 8-byte loads (six FP32 records: 8-byte boundaries)
+template <int N, typename T>
+__device__ __forceinline__ void load_recs(const T* __restrict__ src, T (&r)[N]) {
+  constexpr int B = N * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
+    union {
+      float4 v[B / 16];
+      T t[N];
+    } u;
+#pragma unroll
+    for (int i = 0; i < B / 16; ++i) u.v[i] = ((const float4*)src)[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = u.t[i];
+  } else {
+    static_assert(B % 8 == 0, "records fill 8-byte words");
+    union {
+      float2 v[B / 8];
+      T t[N];
+    } u;
+#pragma unroll
+    for (int i = 0; i < B / 8; ++i) u.v[i] = ((const float2*)src)[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) r[i] = u.t[i];
+  }
+}
+
+template <int N, typename T>
+__device__ __forceinline__ void store_recs(T* __restrict__ dst, const T (&r)[N]) {
+  constexpr int B = N * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
+    union {
+      float4 v[B / 16];
+      T t[N];
+    } u;
+#pragma unroll
+    for (int i = 0; i < N; ++i) u.t[i] = r[i];
+#pragma unroll
+    for (int i = 0; i < B / 16; ++i) ((float4*)dst)[i] = u.v[i];
+  } else {
+    static_assert(B % 8 == 0, "records fill 8-byte words");
+    union {
+      float2 v[B / 8];
+      T t[N];
+    } u;
+#pragma unroll
+    for (int i = 0; i < N; ++i) u.t[i] = r[i];
+#pragma unroll
+    for (int i = 0; i < B / 8; ++i) ((float2*)dst)[i] = u.v[i];
+  }
+}
+
+// one 2x2 block of the per-voxel operator: out += E' . diag(P) . adj(E') . h
+// (E' the block's records, first column carrying scale / det)
 template <typename R, typename T>
 __device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
                                             cpx<R>& a1) {

@@ -113,7 +113,6 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
     s_kph[g2] = (R)(p.ks[lam0 + g2] * p.dir);
     s_lim[g2] = (int)p.blim[lam0 + g2];
   }
-  const R sc = (R)p.in_scale;
   __syncthreads();
   const int line = threadIdx.x / N1, t = threadIdx.x % N1;
   const bool active = line < nlines;
@@ -163,42 +162,34 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
         TS::template store<R>(u, xl, 1, t);  // the 1/W of the inverse rides on the operator's 1/det
       }
       __syncthreads();
-      const T* opw = (const T*)p.op + ((size_t)ray * nwin + w) * OP_REC * HW + (size_t)y * W;
+      const int rs = p.rec_stride;
+      const T* opw = (const T*)p.op + (((size_t)ray * nwin + w) * HW + (size_t)y * W) * rs;
       // XU pixels per thread and round: their records are loaded together, so
       // that several rounds of global loads are in flight (long rows hold
       // few blocks per SM)
       constexpr int XU = (C == 2 && N2 >= 32) ? 4 : 1;
+      constexpr int NR = C == 4 ? OP_REC : REC_BLOCK;  // records this pass reads per voxel
       for (int x0 = threadIdx.x; x0 < W; x0 += XU * blockDim.x) {
-        T ef[XU][4], arg_f[XU][2], idf[XU];
-        T eb[XU][4], arg_b[XU][2], idb[XU];
+        T rec[XU][NR];
 #pragma unroll
         for (int k = 0; k < XU; ++k) {
           const int x = x0 + k * blockDim.x;
           if (x >= W) break;
-#pragma unroll
-          for (int r = 0; r < 4; ++r) ef[k][r] = opw[(size_t)r * HW + x];
-          idf[k] = opw[(size_t)4 * HW + x] * sc;
-          arg_f[k][0] = opw[(size_t)5 * HW + x];
-          arg_f[k][1] = opw[(size_t)6 * HW + x];
-          if (C == 4) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) eb[k][r] = opw[(size_t)(7 + r) * HW + x];
-            idb[k] = opw[(size_t)11 * HW + x] * sc;
-            arg_b[k][0] = opw[(size_t)12 * HW + x];
-            arg_b[k][1] = opw[(size_t)13 * HW + x];
-          }
+          load_recs<NR, T>(opw + (size_t)x * rs, rec[k]);
         }
 #pragma unroll
         for (int k = 0; k < XU; ++k) {
           const int x = x0 + k * blockDim.x;
           if (x >= W) break;
+          const T* ef = rec[k];
+          const T* eb = rec[k] + (C == 4 ? REC_BLOCK : 0);
           for (int g2 = 0; g2 < G; ++g2) {
             const R kph = s_kph[g2];
-            const cpx<R> pf0 = phase_of(arg_f[k][0], kph) * idf[k], pf1 = phase_of(arg_f[k][1], kph) * idf[k];
+            const cpx<R> pf0 = phase_of(ef[4], kph), pf1 = phase_of(ef[5], kph);
             cpx<R> pb0, pb1;
             if (C == 4) {
-              pb0 = phase_of(arg_b[k][0], kph) * idb[k];
-              pb1 = phase_of(arg_b[k][1], kph) * idb[k];
+              pb0 = phase_of(eb[4], kph);
+              pb1 = phase_of(eb[5], kph);
             }
             for (int q = 0; q < NP; ++q) {
               const int l0 = (g2 * NP + q) * C;
@@ -206,12 +197,12 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
               cpx<R>* a = acc + (size_t)l0 * LS + x;
               if (C == 4) {
                 cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
-                apply_block<R, T>(ef[k], pf0, pf1, h[0], h[2 * LS], a0, a2);
-                apply_block<R, T>(eb[k], pb0, pb1, h[LS], h[3 * LS], a1, a3);
+                apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
+                apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
                 a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
               } else {
                 cpx<R> a0 = a[0], a1 = a[LS];
-                apply_block<R, T>(ef[k], pf0, pf1, h[0], h[LS], a0, a1);
+                apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
                 a[0] = a0; a[LS] = a1;
               }
             }
