@@ -2114,6 +2114,7 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
   const int nwin = p.nx * p.ny;
   for (int t = threadIdx.x; t < W; t += blockDim.x) tw[t] = ((const cpx<R>*)p.tw)[t];
   for (int t = threadIdx.x; t < nlines * LS; t += blockDim.x) acc[t] = mk<R>(0, 0);
+  const R sc = (R)p.in_scale;  // det of each block's records
   __syncthreads();
   // line l <-> (image = (g, pol), component c): l = (g * NP + pol) * C + c
   for (int j = 0; j < p.ny; ++j) {
@@ -2151,11 +2152,17 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
         const T* eb = rec + (C == 4 ? REC_BLOCK : 0);
         for (int gl = 0; gl < G; ++gl) {
           const R kph = (R)(p.ks[lam0 + gl] * p.dir);
-          const cpx<R> pf0 = phase_of(ef[4], kph), pf1 = phase_of(ef[5], kph);
-          cpx<R> pb0, pb1;
+          // projector form of each block: q = p1 scale, dp = p0 - p1
+          cpx<R> qf, dpf, qb, dpb;
+          {
+            const cpx<R> f0 = phase_of(ef[4], kph), f1 = phase_of(ef[5], kph);
+            qf = f1 * sc;
+            dpf = f0 - f1;
+          }
           if (C == 4) {
-            pb0 = phase_of(eb[4], kph);
-            pb1 = phase_of(eb[5], kph);
+            const cpx<R> b0 = phase_of(eb[4], kph), b1 = phase_of(eb[5], kph);
+            qb = b1 * sc;
+            dpb = b0 - b1;
           }
           for (int pol = 0; pol < NP; ++pol) {
             const int l0 = (gl * NP + pol) * C;
@@ -2163,12 +2170,12 @@ __global__ void __launch_bounds__(256, 3) k_layer_row(RowParams p, Grid g, const
             cpx<R>* a = acc + (size_t)l0 * LS + q;
             if (C == 4) {
               cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
-              apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
+              apply_block<R, T>(ef, qf, dpf, h[0], h[2 * LS], a0, a2);
+              apply_block<R, T>(eb, qb, dpb, h[LS], h[3 * LS], a1, a3);
               a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
             } else {
               cpx<R> a0 = a[0], a1 = a[LS];
-              apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
+              apply_block<R, T>(ef, qf, dpf, h[0], h[LS], a0, a1);
               a[0] = a0; a[LS] = a1;
             }
           }

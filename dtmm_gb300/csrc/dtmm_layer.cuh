@@ -196,15 +196,17 @@ __device__ __forceinline__ void store_recs(T* __restrict__ dst, const T (&r)[N])
   }
 }
 
-// one 2x2 block of the per-voxel operator: out += E' . diag(P) . adj(E') . h
-// (E' the block's records, first column carrying scale / det)
+// one 2x2 block of the per-voxel operator, out += E' diag(p0, p1) adj(E') h
+// (E' the block's records, first column carrying scale / det, so det(E') =
+// scale), in projector form: with c0 = (e0', e2') and r0 = (e3, -e1),
+// E' diag(p0, p1) adj(E') = p1 scale I + (p0 - p1) c0 r0.  The caller forms
+// q = p1 scale and dp = p0 - p1 once per voxel and wavelength.
 template <typename R, typename T>
-__device__ __forceinline__ void apply_block(const T e[4], cpx<R> p0, cpx<R> p1, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
+__device__ __forceinline__ void apply_block(const T e[4], cpx<R> q, cpx<R> dp, cpx<R> h0, cpx<R> h1, cpx<R>& a0,
                                             cpx<R>& a1) {
-  const cpx<R> w0 = (e[3] * h0 - e[1] * h1) * p0;
-  const cpx<R> w1 = (e[0] * h1 - e[2] * h0) * p1;
-  a0 = a0 + e[0] * w0 + e[1] * w1;
-  a1 = a1 + e[2] * w0 + e[3] * w1;
+  const cpx<R> s = (e[3] * h0 - e[1] * h1) * dp;
+  a0 = cfma(q, h0, a0) + e[0] * s;
+  a1 = cfma(q, h1, a1) + e[2] * s;
 }
 
 }  // namespace dtmm

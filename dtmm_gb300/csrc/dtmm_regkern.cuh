@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
     s_kph[g2] = (R)(p.ks[lam0 + g2] * p.dir);
     s_lim[g2] = (int)p.blim[lam0 + g2];
   }
+  const R sc = (R)p.in_scale;  // det of each block's records
   __syncthreads();
   const int line = threadIdx.x / N1, t = threadIdx.x % N1;
   const bool active = line < nlines;
@@ -185,11 +186,17 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
           const T* eb = rec[k] + (C == 4 ? REC_BLOCK : 0);
           for (int g2 = 0; g2 < G; ++g2) {
             const R kph = s_kph[g2];
-            const cpx<R> pf0 = phase_of(ef[4], kph), pf1 = phase_of(ef[5], kph);
-            cpx<R> pb0, pb1;
+            // projector form of each block: q = p1 scale, dp = p0 - p1
+            cpx<R> qf, dpf, qb, dpb;
+            {
+              const cpx<R> f0 = phase_of(ef[4], kph), f1 = phase_of(ef[5], kph);
+              qf = f1 * sc;
+              dpf = f0 - f1;
+            }
             if (C == 4) {
-              pb0 = phase_of(eb[4], kph);
-              pb1 = phase_of(eb[5], kph);
+              const cpx<R> b0 = phase_of(eb[4], kph), b1 = phase_of(eb[5], kph);
+              qb = b1 * sc;
+              dpb = b0 - b1;
             }
             for (int q = 0; q < NP; ++q) {
               const int l0 = (g2 * NP + q) * C;
@@ -197,12 +204,12 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
               cpx<R>* a = acc + (size_t)l0 * LS + x;
               if (C == 4) {
                 cpx<R> a0 = a[0], a1 = a[LS], a2 = a[2 * LS], a3 = a[3 * LS];
-                apply_block<R, T>(ef, pf0, pf1, h[0], h[2 * LS], a0, a2);
-                apply_block<R, T>(eb, pb0, pb1, h[LS], h[3 * LS], a1, a3);
+                apply_block<R, T>(ef, qf, dpf, h[0], h[2 * LS], a0, a2);
+                apply_block<R, T>(eb, qb, dpb, h[LS], h[3 * LS], a1, a3);
                 a[0] = a0; a[LS] = a1; a[2 * LS] = a2; a[3 * LS] = a3;
               } else {
                 cpx<R> a0 = a[0], a1 = a[LS];
-                apply_block<R, T>(ef, pf0, pf1, h[0], h[LS], a0, a1);
+                apply_block<R, T>(ef, qf, dpf, h[0], h[LS], a0, a1);
                 a[0] = a0; a[LS] = a1;
               }
             }
