@@ -1116,14 +1116,16 @@ struct Engine {
     for (int l0 = 0; l0 < d.nlayers;) {
       int l1 = l0 + 1;
       while (l1 < d.nlayers && blk_of(l1) == blk_of(l0)) ++l1;
-      const long long nvox = (long long)(l1 - l0) * d.height * d.width;
+      // one eps for every voxel (all strides 0): the mean of that voxel
+      const bool one = d.epsv_strides[0] == 0 && d.epsv_strides[1] == 0 && d.epsv_strides[2] == 0;
+      const long long nvox = one ? 1 : (long long)(l1 - l0) * d.height * d.width;
       int blocks = (int)((nvox + 1023) / 1024);
       if (blocks > kPartBlocks) blocks = kPartBlocks;
       const char* e0 = (const char*)d.epsv + (size_t)l0 * d.epsv_strides[0] * (d.eps_complex ? 16 : 8);
       k_eps_mean<<<blocks, 256, 0, st>>>(e0, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
-                                         l1 - l0, d.height, d.width, A<double>(L.part));
+                                         one ? 1 : l1 - l0, one ? 1 : d.height, one ? 1 : d.width, A<double>(L.part));
       CKL("k_eps_mean");
-      k_eps_final<<<1, 32, 0, st>>>(A<double>(L.part), blocks, nvox, effb(blk_of(l0)));
+      k_eps_final<<<1, 256, 0, st>>>(A<double>(L.part), blocks, nvox, effb(blk_of(l0)));
       CKL("k_eps_final");
       l0 = l1;
     }
@@ -1333,6 +1335,19 @@ struct Engine {
     return DTMM_OK;
   }
 
+  // per-image grid sums of the z-Poynting component of f into out[image]:
+  // chunk sums of every image (as many chunks as the partials buffer holds,
+  // at most 32), added in a fixed order
+  int total_intensity(const cpx<R>* f, double* out) {
+    const size_t cap = std::max<size_t>(2 * kPartBlocks, 4 * (size_t)kWinChunks * d.nray * L.nwin);
+    const int chunks = (int)std::max<size_t>(1, std::min<size_t>(32, cap / (size_t)NI));
+    k_total_intensity<R><<<dim3((unsigned)chunks, (unsigned)NI), 256, 0, st>>>(f, g, A<double>(L.part));
+    CKL("k_total_intensity");
+    k_total_sum<<<(NI + 255) / 256, 256, 0, st>>>(A<double>(L.part), chunks, out, NI);
+    CKL("k_total_sum");
+    return DTMM_OK;
+  }
+
   // f (real space) -> notch * P . fft2(f) [with per-k normalisation] -> ifft2 -> f
   int project(cpx<R>* f, const cpx<R>* Ptab, bool normalize, double sigma) {
     int rc;
@@ -1343,8 +1358,9 @@ struct Engine {
     nt.on = 1;
     nt.x0 = d.nin;
     nt.sigma = sigma;
+    nt.den = 1.0 - std::exp(-d.nin / sigma);
     nt.ks = ks();
-    const size_t n = (size_t)NI * L.HW;
+    const size_t n = (size_t)d.nlam * L.HW;  // one thread per (wavelength, k)
     k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, normalize ? 1 : 0, nt);
     CKL("k_kproject");
     if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
@@ -1360,24 +1376,24 @@ struct Engine {
   int project_total(cpx<R>* f, const cpx<R>* Ptab, double sigma) {
     int rc;
     cpx<R>* K = P(L.U);
-    k_total_intensity<R><<<NI, 256, 0, st>>>(f, g, i0f());
-    CKL("k_total_intensity");
+    if ((rc = total_intensity(f, i0f()))) return rc;
     if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
     if ((rc = launch_col(f, K, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;
     NotchParams off;
     off.on = 0;
+    off.den = 1.0;
     off.ks = ks();
-    const size_t n = (size_t)NI * L.HW;
+    const size_t n = (size_t)d.nlam * L.HW;  // one thread per (wavelength, k)
     k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, 0, off);
     CKL("k_kproject");
-    k_total_intensity<R><<<NI, 256, 0, st>>>(K, g, fact());
-    CKL("k_total_intensity");
+    if ((rc = total_intensity(K, fact()))) return rc;
     k_total_fact<<<(NI + 255) / 256, 256, 0, st>>>(i0f(), fact(), (double)L.HW, NI);
     CKL("k_total_fact");
     NotchParams nt;
     nt.on = 1;
     nt.x0 = d.nin;
     nt.sigma = sigma;
+    nt.den = 1.0 - std::exp(-d.nin / sigma);
     nt.ks = ks();
     k_kscale<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, fact(), g, nt);
     CKL("k_kscale");
@@ -1429,8 +1445,7 @@ struct Engine {
       if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
       field0 = P(L.field0);
       if ((rc = diffract(field0, fin, pin))) return rc;
-      k_total_intensity<R><<<NI, 256, 0, st>>>(field0, g, i0());
-      CKL("k_total_intensity");
+      if ((rc = total_intensity(field0, i0()))) return rc;
     }
     CK(cudaMemcpyAsync(F, fin, bytes, cudaMemcpyDeviceToDevice, st));
     cpx<R>* bulk = (cpx<R>*)io.bulk;
@@ -1458,8 +1473,7 @@ struct Engine {
           if (i != npass - 1) {
             if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
             if ((rc = project(F, pin, false, sigma))) return rc;
-            k_total_intensity<R><<<NI, 256, 0, st>>>(F, g, i0f());
-            CKL("k_total_intensity");
+            if ((rc = total_intensity(F, i0f()))) return rc;
             k_ratio<<<(NI + 255) / 256, 256, 0, st>>>(i0(), i0f(), fact(), NI);
             CKL("k_ratio");
             if ((rc = axpby(F, F, fact(), 1.0, nullptr, nullptr, 0.0))) return rc;
@@ -2266,10 +2280,15 @@ int dtmm_field_intensity(int height, int width, int nimg, int precision, const v
   g.W = width;
   g.NI = nimg;
   cudaStream_t st = (cudaStream_t)stream;
-  if (precision == DTMM_PRECISION_DOUBLE)
-    k_total_intensity<double><<<nimg, 256, 0, st>>>((const cpx<double>*)field, g, sums);
-  else
-    k_total_intensity<float><<<nimg, 256, 0, st>>>((const cpx<float>*)field, g, sums);
+  // one chunk per image (the sums land in sums directly), at most 65535 images a launch
+  const size_t per = 4 * (size_t)height * width;
+  for (int o = 0; o < nimg; o += 65535) {
+    const unsigned n = (unsigned)std::min(65535, nimg - o);
+    if (precision == DTMM_PRECISION_DOUBLE)
+      k_total_intensity<double><<<dim3(1, n), 256, 0, st>>>((const cpx<double>*)field + per * o, g, sums + o);
+    else
+      k_total_intensity<float><<<dim3(1, n), 256, 0, st>>>((const cpx<float>*)field + per * o, g, sums + o);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(DTMM_ECUDA, "k_total_intensity: %s", cudaGetErrorString(e));
   return DTMM_OK;

@@ -2244,61 +2244,74 @@ __device__ __forceinline__ double poynting(const cpx<R> f[4]) {
 
 struct NotchParams {
   int on;
-  double x0, sigma, betamax_unused;
+  double x0, sigma;
+  double den;  // 1 - exp(-x0 / sigma) (host)
   const double* ks;
 };
 
+// the notch of denoise_field at k: (1 - exp(-a / sigma)) / (1 - exp(-x0 / sigma)),
+// a = |beta - x0| clipped to [0, x0] (beta as in betaphi_k)
 __device__ __forceinline__ double notch_k(const NotchParams& n, const Grid& g, int lam, int ky, int kx) {
   if (!n.on) return 1.0;
-  double beta, phi;
-  betaphi_k(g, n.ks[lam], ky, kx, beta, phi);
+  const double xx = (double)fsigned(kx, g.W) * (1.0 / g.W);
+  const double yy = (double)fsigned(ky, g.H) * (1.0 / g.H);
+  const double beta = (2.0 * M_PI / fabs(n.ks[lam])) * sqrt(xx * xx + yy * yy);
   double a = fabs(beta - n.x0);
   if (a > n.x0) a = n.x0;
   if (a < 0.0) a = 0.0;
-  return (1.0 - exp(-a / n.sigma)) / (1.0 - exp(-n.x0 / n.sigma));
+  return (1.0 - exp(-a / n.sigma)) / n.den;
 }
 
 // k-space: f <- notch * P . f, optionally with the per-k intensity renormalisation
-// of project_normalized_fft (dtmm/transfer.py:67-90).
+// of project_normalized_fft (dtmm/transfer.py:67-90).  One thread per (lam, k):
+// the matrix and the notch once for every image of the wavelength.
 template <typename R>
 __global__ void k_kproject(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ P, Grid g, int normalize, NotchParams nt) {
   const int HW = g.H * g.W;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)g.NI * HW) return;
-  const int img = (int)(t / HW), k = (int)(t - (size_t)img * HW);
-  const int lam = img % g.nlam;
+  if (t >= (size_t)g.nlam * HW) return;
+  const int lam = (int)(t / HW), k = (int)(t - (size_t)lam * HW);
   const int ky = k / g.W, kx = k - ky * g.W;
-  cpx<R> v[4], o[4];
-  for (int c = 0; c < 4; ++c) v[c] = f[((size_t)img * 4 + c) * HW + k];
-  const cpx<R>* m = P + ((size_t)lam * HW + k) * 16;
-  for (int i = 0; i < 4; ++i) {
-    cpx<R> s = mk<R>(0, 0);
-    for (int j = 0; j < 4; ++j) s = cfma(m[i * 4 + j], v[j], s);
-    o[i] = s;
-  }
-  double fact = 1.0;
-  if (normalize) {
-    double i1 = poynting(v), i2 = poynting(o);
-    if (i2 == 0.0) {
-      i2 = 1.0;
-      i1 = 0.0;
+  cpx<R> m[16];
+  load_recs<16, cpx<R>>(P + ((size_t)lam * HW + k) * 16, m);
+  const double notch = notch_k(nt, g, lam, ky, kx);
+  const int per = g.nray * g.npol;
+  for (int q = 0; q < per; ++q) {
+    const size_t img = (size_t)q * g.nlam + lam;
+    cpx<R> v[4], o[4];
+    for (int c = 0; c < 4; ++c) v[c] = f[(img * 4 + c) * HW + k];
+    for (int i = 0; i < 4; ++i) {
+      cpx<R> s = mk<R>(0, 0);
+      for (int j = 0; j < 4; ++j) s = cfma(m[i * 4 + j], v[j], s);
+      o[i] = s;
     }
-    fact = i1 / i2;
-    if (fact <= -1) fact = -1;
-    if (fact >= 1) fact = 1;
-    fact = fabs(fact);
+    double fact = 1.0;
+    if (normalize) {
+      double i1 = poynting(v), i2 = poynting(o);
+      if (i2 == 0.0) {
+        i2 = 1.0;
+        i1 = 0.0;
+      }
+      fact = i1 / i2;
+      if (fact <= -1) fact = -1;
+      if (fact >= 1) fact = 1;
+      fact = fabs(fact);
+    }
+    fact *= notch;
+    for (int c = 0; c < 4; ++c) f[(img * 4 + c) * HW + k] = o[c] * (R)fact;
   }
-  fact *= notch_k(nt, g, lam, ky, kx);
-  for (int c = 0; c < 4; ++c) f[((size_t)img * 4 + c) * HW + k] = o[c] * (R)fact;
 }
 
-// per-image pixel sums of the z-Poynting component, FP64 accumulation
+// per-image pixel sums of the z-Poynting component, FP64 accumulation:
+// grid (chunks, images), block sums of each image's chunk of pixels into
+// part[img * chunks + chunk]; k_total_sum adds the chunks in a fixed order
 template <typename R>
-__global__ void k_total_intensity(const cpx<R>* __restrict__ f, Grid g, double* out) {
+__global__ void k_total_intensity(const cpx<R>* __restrict__ f, Grid g, double* part) {
   const int HW = g.H * g.W;
-  const int img = blockIdx.x;
+  const int img = blockIdx.y, chunk = blockIdx.x, nch = gridDim.x;
+  const int k0 = (int)(((long long)HW * chunk) / nch), k1 = (int)(((long long)HW * (chunk + 1)) / nch);
   double s = 0.0;
-  for (int k = threadIdx.x; k < HW; k += blockDim.x) {
+  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
     cpx<R> v[4];
     for (int c = 0; c < 4; ++c) v[c] = f[((size_t)img * 4 + c) * HW + k];
     s += poynting(v);
@@ -2310,7 +2323,15 @@ __global__ void k_total_intensity(const cpx<R>* __restrict__ f, Grid g, double* 
     if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[img] = red[0];
+  if (threadIdx.x == 0) part[(size_t)img * nch + chunk] = red[0];
+}
+
+__global__ void k_total_sum(const double* part, int chunks, double* out, int n) {
+  const int img = blockIdx.x * blockDim.x + threadIdx.x;
+  if (img >= n) return;
+  double s = 0.0;
+  for (int c = 0; c < chunks; ++c) s += part[(size_t)img * chunks + c];
+  out[img] = s;
 }
 
 // elementwise: out = a*x + b*y with per-image real factors (null = 1)
@@ -2343,19 +2364,24 @@ __global__ void k_total_fact(const double* i1, double* ik, double hw, int n) {
   ik[t] = fabs(f);
 }
 
-// k-space: f <- notch * fact[image] * f
+// k-space: f <- notch * fact[image] * f (one thread per (lam, k), the notch
+// once for every image of the wavelength)
 template <typename R>
 __global__ void k_kscale(cpx<R>* __restrict__ f, const double* fact, Grid g, NotchParams nt) {
   const int HW = g.H * g.W;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)g.NI * HW) return;
-  const int img = (int)(t / HW), k = (int)(t - (size_t)img * HW);
-  const int lam = img % g.nlam;
+  if (t >= (size_t)g.nlam * HW) return;
+  const int lam = (int)(t / HW), k = (int)(t - (size_t)lam * HW);
   const int ky = k / g.W, kx = k - ky * g.W;
-  const R s = (R)(fact[img] * notch_k(nt, g, lam, ky, kx));
-  for (int c = 0; c < 4; ++c) {
-    cpx<R>& v = f[((size_t)img * 4 + c) * HW + k];
-    v = v * s;
+  const double notch = notch_k(nt, g, lam, ky, kx);
+  const int per = g.nray * g.npol;
+  for (int q = 0; q < per; ++q) {
+    const size_t img = (size_t)q * g.nlam + lam;
+    const R s = (R)(fact[img] * notch);
+    for (int c = 0; c < 4; ++c) {
+      cpx<R>& v = f[(img * 4 + c) * HW + k];
+      v = v * s;
+    }
   }
 }
 
@@ -2427,16 +2453,29 @@ __global__ void k_eps_mean(const void* epsv, int eps_complex, long long s0, long
   }
 }
 
-// fixed-order sum of the block partials -> mean (re, im)
+// fixed-order sum of the block partials -> mean (re, im): one block of 256
+// threads, each adding a fixed strided subset, then a tree
 __global__ void k_eps_final(const double* part, int blocks, long long n, double* out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double sr = 0, si = 0;
-  for (int b = 0; b < blocks; ++b) {
+  for (int b = threadIdx.x; b < blocks; b += blockDim.x) {
     sr += part[2 * b];
     si += part[2 * b + 1];
   }
-  out[0] = sr / (double)n;
-  out[1] = si / (double)n;
+  __shared__ double red[2][256];
+  red[0][threadIdx.x] = sr;
+  red[1][threadIdx.x] = si;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + st];
+      red[1][threadIdx.x] += red[1][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = red[0][0] / (double)n;
+    out[1] = red[1][0] / (double)n;
+  }
 }
 
 // sqrt(eps_eff - beta_w^2) per window (real path)
