@@ -732,7 +732,7 @@ struct Engine {
   static int ktab_entries(int what) {
     switch (what) {
       case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
-      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: return 4;
+      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: return 4;
       default: return 16;
     }
   }

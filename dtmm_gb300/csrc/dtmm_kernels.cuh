@@ -1650,8 +1650,9 @@ __device__ inline void iso_half_step(bool first, cpx<double> eps, double beta, d
   const cpx<double> z = mk<double>(0.0, 0.0);
   for (int i = 0; i < 4; ++i)
     for (int j = 0; j < 4; ++j) M[i][j] = z;
+  if (beta >= betamax) return;
   const cpx<double> a = csqrt_d(mk<double>(eps.re - beta * beta, eps.im));
-  if ((beta >= betamax) || (a.re == 0.0 && a.im == 0.0)) return;
+  if (a.re == 0.0 && a.im == 0.0) return;
   const cpx<double> ep = cexp_i(a * kd), em = cexp_i(-a * kd);
   const double cc = c * c, ss = s * s, cs = c * s;
   if (first) {
@@ -1674,6 +1675,15 @@ __device__ inline void iso_half_step(bool first, cpx<double> eps, double beta, d
   }
 }
 
+// complex entries of one table per (lam, ky, kx) (the engine's ktab_entries)
+__device__ __forceinline__ int kt_entries(int what) {
+  switch (what) {
+    case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
+    case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: return 4;
+    default: return 16;
+  }
+}
+
 template <typename R>
 __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int HW = g.H * g.W;
@@ -1688,7 +1698,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     double beta, c, s;
     betacs_k(g, ks, ky, kx, beta, c, s);
     if (p.what == KT_DIAG) {
-      const cpx<double> a = csqrt_d(mk<double>(p.eps.re - beta * beta, p.eps.im));
+      const cpx<double> a = beta >= p.betamax ? mk<double>(0.0, 0.0) : csqrt_d(mk<double>(p.eps.re - beta * beta, p.eps.im));
       const bool cut = (beta >= p.betamax) || (a.re == 0.0 && a.im == 0.0);
       const cpx<double> z = mk<double>(0.0, 0.0);
       // column-major (lam, kx, ky) so that column passes read it coalesced
@@ -1715,6 +1725,19 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(M[i][j]);
     return;
+  }
+  // every table but C . D, D . C and C . D . C (cut at their own beta limit)
+  // vanishes for beta >= betamax: those points are written as zeros without
+  // the eigen-data
+  if (p.what != KT_CFD && p.what != KT_CD && p.what != KT_DC) {
+    double b0, c0, s0;
+    betacs_k(g, ks, ky, kx, b0, c0, s0);
+    if (b0 >= p.betamax) {
+      const int ne = kt_entries(p.what);
+      cpx<R>* o = tab + (size_t)t * ne;
+      for (int i = 0; i < ne; ++i) o[i] = mk<R>((R)0, (R)0);
+      return;
+    }
   }
   double beta, phi;
   betaphi_k(g, ks, ky, kx, beta, phi);
