@@ -496,7 +496,21 @@ struct Engine {
       RegLaunch rl;
       rl.smem = tiles * d.height * (C * tx + 1) * sizeof(cpx<R>) + d.height * sizeof(cpx<R>);
       rl.threads = std::max(32, ((C * tx * n1 + 31) / 32) * 32);
-      rl.grid = dim3((d.width + tx - 1) / tx, NI);
+      const int ntile = (d.width + tx - 1) / tx;
+      p.tile_lo = 0;
+      p.tile_hi0 = 0;
+      int nlaunch = ntile;
+      if (p.band_skip == 2 && p.kop == KOP_DIAG && blim_max >= 0) {
+        // tiles holding a column with |frequency index| <= the largest band limit
+        const int lo = (blim_max + 1 + tx - 1) / tx;        // columns 0 .. lim
+        const int hi0 = std::max(lo, (d.width - blim_max) / tx);  // columns W - lim .. W - 1
+        if (lo + (ntile - hi0) < ntile) {
+          p.tile_lo = lo;
+          p.tile_hi0 = hi0;
+          nlaunch = lo + (ntile - hi0);
+        }
+      }
+      rl.grid = dim3(nlaunch, NI);
       rl.st = st;
       mark(PROF_COL);
       // the diagonal table is cut at betamax: band variants of the inverse transforms

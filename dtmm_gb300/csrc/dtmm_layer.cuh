@@ -76,6 +76,8 @@ struct ColParams {
   // reads those columns as zero without loading them)
   int band_skip;
   const double* blim;      // [lam] band limit: largest in-band |column frequency index| (-1: none)
+  int tile_lo, tile_hi0;   // register column pass with band_skip 2: launched tiles [0, tile_lo) and
+                           // tile_hi0 on (tile_lo 0: every tile)
   int ny;                  // window rows (1 = no windows)
   const void* cy;          // [ray][j][lam][H] (null = weight 1)
   int j_only;              // >= 0: emit only window row j_only (into U slot 0)

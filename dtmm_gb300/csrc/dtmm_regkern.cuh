@@ -313,10 +313,12 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
   cpx<R>* tileB = tileA + (size_t)(ntiles - 1) * H * RS;  // [H][RS] exchange and outgoing rows (= A with one tile)
   cpx<R>* tw = tileA + (size_t)ntiles * H * RS;    // [H] twiddles, lane-major (TwoStep::twiddle_entry)
   const int img = blockIdx.y;
-  const int x0 = blockIdx.x * TX;
+  // tile_lo > 0: the launch covers the in-band tiles only, tiles [0, tile_lo)
+  // and from tile_hi0 on (the others write nothing with band_skip 2)
+  const int tile = (p.tile_lo > 0 && (int)blockIdx.x >= p.tile_lo) ? p.tile_hi0 + ((int)blockIdx.x - p.tile_lo)
+                                                                    : (int)blockIdx.x;
+  const int x0 = tile * TX;
   const int lam = img_lam(g, img), ray = img_ray(g, img);
-  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
-  // a half-warp covers one tile row (C x TX contiguous slots): conflict-free
   const int CT = C * TX;
   const int lc = threadIdx.x % CT, ystep = blockDim.x / CT;
   const int lcc = lc / TX, lxc = lc - lcc * TX;
@@ -339,6 +341,7 @@ __global__ void __launch_bounds__(256, 3) k_layer_col_reg(ColParams p, Grid g, c
       return;
     }
   }
+  for (int e = threadIdx.x; e < H; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
   const cpx<R>* xsrc = X + ((size_t)img * C + lcc) * H * W + x0 + lxc;
   if (lin)
     for (int y = threadIdx.x / CT; y < H; y += ystep) tileA[y * RS + lc] = xsrc[(size_t)y * W];
