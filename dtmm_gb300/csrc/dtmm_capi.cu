@@ -1147,7 +1147,7 @@ struct Engine {
     if (d.diffraction > 1) {
       WinParams w = winp();
       // partial sums over many blocks, then the per-window means
-      dim3 gs(kWinChunks, L.nwin, d.nray);
+      dim3 gs(kWinChunks, L.ny, d.nray);  // one block row per window row j
       k_window_stats<<<gs, 256, 0, st>>>(w, g, A<double>(L.part));
       CKL("k_window_stats");
       k_window_final<<<(L.nwin * d.nray + 127) / 128, 128, 0, st>>>(A<double>(L.part), kWinChunks, wbeta(), wphi(),

@@ -1371,49 +1371,62 @@ __device__ __forceinline__ double win_center(const WinParams& w, int i) {
 }
 
 // partial sums of w^2 bx, w^2 by, w^2 and the non-zero flag over (lam, ky, kx):
-// grid (chunks, window, ray); part[((ray * nwin + win) * chunks + chunk) * 4 + q].
-// The final means add the chunks in a fixed order, so results are bitwise
-// reproducible.
+// grid (chunks, window row j, ray); each element's beta and row weight once,
+// then every window (i, j) of the row; part[((ray * nwin + win) * chunks +
+// chunk) * 4 + q].  The final means add the chunks in a fixed order, so
+// results are bitwise reproducible.
+constexpr int kWinRowMax = 8;  // windows of a row accumulated in registers per sweep
+
 __global__ void k_window_stats(WinParams w, Grid g, double* part) {
-  const int ray = blockIdx.z, win = blockIdx.y;
-  const int i = win / w.n, j = win % w.n;
-  const int xt = (i == 0) ? -1 : ((i == w.n - 1) ? 1 : 0);
+  const int ray = blockIdx.z, j = blockIdx.y;
   const int yt = (j == 0) ? -1 : ((j == w.n - 1) ? 1 : 0);
-  const double cx0 = win_center(w, i) + w.xoff[ray];
   const double cy0 = win_center(w, j) + w.yoff[ray];
-  double sx = 0, sy = 0, sn = 0, nz = 0;
   const int total = g.nlam * g.H * g.W;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    const int lam = t / (g.H * g.W);
-    const int k = t - lam * g.H * g.W;
-    const int ky = k / g.W, kx = k - ky * g.W;
-    const double l = 2.0 * M_PI / w.ks[lam];
-    const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
-    const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
-    const double b = sqrt(bx * bx + by * by);
-    double c = 0.0;
-    if (b < w.betamax) c = tent((bx - cx0) / w.step, xt) * tent((by - cy0) / w.step, yt);
-    if (c > 0.0) {
-      nz = 1;
-      const double c2 = c * c;
-      sx += bx * c2;
-      sy += by * c2;
-      sn += c2;
+  __shared__ double red[4][256];
+  for (int i0 = 0; i0 < w.n; i0 += kWinRowMax) {
+    const int ni = min(kWinRowMax, w.n - i0);
+    double acc[kWinRowMax][4];
+    for (int a = 0; a < kWinRowMax; ++a) acc[a][0] = acc[a][1] = acc[a][2] = acc[a][3] = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+      const int lam = t / (g.H * g.W);
+      const int k = t - lam * g.H * g.W;
+      const int ky = k / g.W, kx = k - ky * g.W;
+      const double l = 2.0 * M_PI / w.ks[lam];
+      const double bx = l * ((double)fsigned(kx, g.W) * (1.0 / g.W));
+      const double by = l * ((double)fsigned(ky, g.H) * (1.0 / g.H));
+      const double b = sqrt(bx * bx + by * by);
+      if (!(b < w.betamax)) continue;
+      const double ty = tent((by - cy0) / w.step, yt);
+      if (ty == 0.0) continue;
+#pragma unroll
+      for (int a = 0; a < kWinRowMax; ++a) {
+        if (a >= ni) break;
+        const int i = i0 + a;
+        const int xt = (i == 0) ? -1 : ((i == w.n - 1) ? 1 : 0);
+        const double c = tent((bx - (win_center(w, i) + w.xoff[ray])) / w.step, xt) * ty;
+        if (c > 0.0) {
+          const double c2 = c * c;
+          acc[a][0] += bx * c2;
+          acc[a][1] += by * c2;
+          acc[a][2] += c2;
+          acc[a][3] = 1.0;
+        }
+      }
+    }
+    for (int a = 0; a < ni; ++a) {
+      __syncthreads();  // the previous window's reads of red are done
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] = acc[a][q];
+      __syncthreads();
+      for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+          for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + st];
+        __syncthreads();
+      }
+      const int win = (i0 + a) * w.n + j;
+      if (threadIdx.x < 4)
+        part[(((size_t)ray * w.n * w.n + win) * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = red[threadIdx.x][0];
     }
   }
-  __shared__ double red[4][256];
-  red[0][threadIdx.x] = sx;
-  red[1][threadIdx.x] = sy;
-  red[2][threadIdx.x] = sn;
-  red[3][threadIdx.x] = nz;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x < 4)
-    part[(((size_t)ray * w.n * w.n + win) * gridDim.x + blockIdx.x) * 4 + threadIdx.x] = red[threadIdx.x][0];
 }
 
 __global__ void k_window_final(const double* part, int chunks, double* wbeta, double* wphi, int* wzero, double* wcos,
@@ -1684,6 +1697,17 @@ __device__ __forceinline__ int kt_entries(int what) {
   }
 }
 
+// grid point (ky, kx) lies clearly beyond betamax at wavenumber ks: r^2 =
+// (kx / W)^2 + (ky / H)^2 above (betamax ks / 2 pi)^2 with a relative margin
+// far above the rounding of beta = (2 pi / ks) r, so the exact test beta >=
+// betamax agrees; points near the limit take the exact test
+__device__ __forceinline__ bool clearly_beyond(const Grid& g, double ks, double betamax, int ky, int kx) {
+  const double xx = (double)fsigned(kx, g.W) * (1.0 / g.W);
+  const double yy = (double)fsigned(ky, g.H) * (1.0 / g.H);
+  const double q = betamax * fabs(ks) * (0.5 / M_PI);
+  return xx * xx + yy * yy > q * q * (1.0 + 1e-9);
+}
+
 template <typename R>
 __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int HW = g.H * g.W;
@@ -1695,6 +1719,16 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   if (p.eps_dev != nullptr) p.eps = mk<double>(p.eps_dev[0], p.eps_dev[1]);
   if (p.eps_dev2 != nullptr) p.eps2 = mk<double>(p.eps_dev2[0], p.eps_dev2[1]);
   if (p.what == KT_DIAG || p.what == KT_D1 || p.what == KT_D2 || p.what == KT_D12) {
+    if (clearly_beyond(g, ks, p.betamax, ky, kx)) {  // zero tables there
+      if (p.what == KT_DIAG) {
+        const size_t tt = ((size_t)lam * g.W + kx) * g.H + ky;
+        tab[tt * 2 + 0] = tab[tt * 2 + 1] = mk<R>((R)0, (R)0);
+      } else {
+        cpx<R>* o = tab + (size_t)t * 16;
+        for (int i = 0; i < 16; ++i) o[i] = mk<R>((R)0, (R)0);
+      }
+      return;
+    }
     double beta, c, s;
     betacs_k(g, ks, ky, kx, beta, c, s);
     if (p.what == KT_DIAG) {
@@ -1730,8 +1764,8 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   // vanishes for beta >= betamax: those points are written as zeros without
   // the eigen-data
   if (p.what != KT_CFD && p.what != KT_CD && p.what != KT_DC) {
-    double b0, c0, s0;
-    betacs_k(g, ks, ky, kx, b0, c0, s0);
+    double b0 = 2.0 * p.betamax, c0, s0;
+    if (!clearly_beyond(g, ks, p.betamax, ky, kx)) betacs_k(g, ks, ky, kx, b0, c0, s0);
     if (b0 >= p.betamax) {
       const int ne = kt_entries(p.what);
       cpx<R>* o = tab + (size_t)t * ne;
