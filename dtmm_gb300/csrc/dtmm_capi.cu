@@ -634,6 +634,9 @@ struct Engine {
       const size_t rec_bytes = (re ? sizeof(R) : sizeof(cpx<R>)) * (size_t)d.nray * L.nwin * p.rec_stride * L.HW;
       RowParams q = p;
       q.groups_inner = rec_bytes > ((size_t)64 << 20) ? 1 : 0;
+      // 256-point rows of the 4x4 method, two images a block in every block:
+      // accumulators in registers, two pixels a thread
+      q.xr = (C == 4 && re && d.width == 256 && nl == kXrLines && d.nlam % p.G == 0 && d.npol % p.PB == 0) ? 2 : 0;
       rl.grid = q.groups_inner ? dim3(d.nray * ngrp * npg, d.height) : dim3(d.height, d.nray * ngrp * npg);
       rl.st = st;
       mark(PROF_ROW);

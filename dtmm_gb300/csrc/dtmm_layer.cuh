@@ -117,6 +117,7 @@ struct RowParams {
   int use_cx;            // apply the window's beta_x weight (first sub-step of a chain)
   int accumulate;        // add the result to X instead of overwriting it
   int groups_inner;      // register row pass: blockIdx.x the group, blockIdx.y the row (else the reverse)
+  int xr;                // register row pass variant with accumulators in registers, pixels a thread (0: none)
 };
 
 template <typename R>

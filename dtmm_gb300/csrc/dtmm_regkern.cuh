@@ -77,9 +77,16 @@ __host__ __device__ constexpr int row_band_pick(int n, int lim) {
 // block and keep at most 85 registers, so that six 128-thread blocks share an
 // SM (measured 8 % faster than four at 117 registers for 256-point rows);
 // 32 points per lane need the registers of a whole 512-thread block.
-template <typename R, int C, bool REAL, int N1, int N2, int BAND>
-__global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U,
-                                                         cpx<R>* __restrict__ X) {
+// XR > 0: the block holds exactly kXrLines lines (two images of the 4x4
+// method) and W / XR threads, and each thread keeps the accumulators of its
+// XR pixels in registers across the windows (no shared-memory
+// read-modify-write per window); 128 registers a thread at most.
+constexpr int kXrLines = 8;
+template <typename R, int C, bool REAL, int N1, int N2, int BAND, int XR = 0>
+__global__ void __launch_bounds__(XR > 0 ? (N1 * N2) / (XR > 0 ? XR : 1) : (N2 >= 32 ? 512 : 256),
+                                  XR > 0 ? 4 : (N2 >= 32 ? 1 : 3))
+    k_layer_row_reg(RowParams p, Grid g, const cpx<R>* __restrict__ U, cpx<R>* __restrict__ X) {
+  static_assert(XR == 0 || C == 4, "register accumulators: the 4x4 method's two-image blocks");
   using T = typename std::conditional<REAL, R, cpx<R>>::type;
   using TS = TwoStep<N1, N2>;
   constexpr int W = N1 * N2;
@@ -105,7 +112,15 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
   const int HW = H * W;
   const int nwin = p.nx * p.ny;
   for (int e = threadIdx.x; e < W; e += blockDim.x) tw[e] = TS::twiddle_entry((const cpx<R>*)p.tw, e);
-  for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
+  if (XR == 0)
+    for (int e = threadIdx.x; e < nlines * LS; e += blockDim.x) acc[e] = mk<R>(0, 0);
+  cpx<R> racc[XR > 0 ? XR : 1][kXrLines];
+  if (XR > 0) {
+#pragma unroll
+    for (int k = 0; k < (XR > 0 ? XR : 1); ++k)
+#pragma unroll
+      for (int l = 0; l < kXrLines; ++l) racc[k][l] = mk<R>((R)0, (R)0);
+  }
   // phase scale k0 * direction of each wavelength of the block (formed once, in FP64)
   __shared__ R s_kph[kMaxRowGroup];
   __shared__ int s_lim[kMaxRowGroup];  // band limit of each wavelength (columns beyond read as zero)
@@ -170,6 +185,36 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
       // few blocks per SM)
       constexpr int XU = (C == 2 && N2 >= 32) ? 4 : 1;
       constexpr int NR = C == 4 ? OP_REC : REC_BLOCK;  // records this pass reads per voxel
+      if constexpr (XR > 0) {
+        // pixels threadIdx.x + k W / XR; the block's two images b (G = 1 and
+        // two polarisations share the phases, G = 2 has its own per image)
+#pragma unroll
+        for (int k = 0; k < (XR > 0 ? XR : 1); ++k) {
+          const int x = threadIdx.x + k * (W / (XR > 0 ? XR : 1));
+          T rec[NR];
+          load_recs<NR, T>(opw + (size_t)x * rs, rec);
+          const T* ef = rec;
+          const T* eb = rec + REC_BLOCK;
+          cpx<R> qf, dpf, qb, dpb;
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            if (b == 0 || G == 2) {
+              const R kph = s_kph[G == 2 ? b : 0];
+              const cpx<R> f0 = phase_of(ef[4], kph), f1 = phase_of(ef[5], kph);
+              qf = f1 * sc;
+              dpf = f0 - f1;
+              const cpx<R> b0 = phase_of(eb[4], kph), b1 = phase_of(eb[5], kph);
+              qb = b1 * sc;
+              dpb = b0 - b1;
+            }
+            const cpx<R>* h = tmp + (size_t)(4 * b) * LS + x;
+            apply_block<R, T>(ef, qf, dpf, h[0], h[2 * LS], racc[k][4 * b], racc[k][4 * b + 2]);
+            apply_block<R, T>(eb, qb, dpb, h[LS], h[3 * LS], racc[k][4 * b + 1], racc[k][4 * b + 3]);
+          }
+        }
+        __syncthreads();
+        continue;
+      }
       for (int x0 = threadIdx.x; x0 < W; x0 += XU * blockDim.x) {
         T rec[XU][NR];
 #pragma unroll
@@ -218,6 +263,13 @@ __global__ void __launch_bounds__(N2 >= 32 ? 512 : 256, N2 >= 32 ? 1 : 3) k_laye
       }
       __syncthreads();
     }
+  }
+  if constexpr (XR > 0) {  // the accumulators into the rows of the forward transform
+#pragma unroll
+    for (int k = 0; k < (XR > 0 ? XR : 1); ++k)
+#pragma unroll
+      for (int l = 0; l < kXrLines; ++l) acc[(size_t)l * LS + threadIdx.x + k * (W / (XR > 0 ? XR : 1))] = racc[k][l];
+    __syncthreads();
   }
   if (active) {
     cpx<R> v[N2];
@@ -525,9 +577,9 @@ struct RegLaunch {
 // row variants: every (C, REAL) for power-of-two sides, real records for the others
 __host__ __device__ constexpr bool reg_row_variant(int n, bool real) { return reg_lanes(n) > 0 && (real || is_pow2(n)); }
 
-template <int N1, int N2, int C, bool REAL, int BAND = 0>
+template <int N1, int N2, int C, bool REAL, int BAND = 0, int XR = 0>
 cudaError_t row_reg_variant(const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, void* X) {
-  auto kern = k_layer_row_reg<float, C, REAL, N1, N2, BAND>;
+  auto kern = k_layer_row_reg<float, C, REAL, N1, N2, BAND, XR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem);
   if (e != cudaSuccess) return e;
   kern<<<L.grid, L.threads, L.smem, L.st>>>(p, g, (const cpx<float>*)U, (cpx<float>*)X);
@@ -535,8 +587,17 @@ cudaError_t row_reg_variant(const RegLaunch& L, const RowParams& p, const Grid& 
 }
 
 // real records with a band variant b (row_band_pick), every (C, REAL) dense
+// (p.xr > 0: the register-accumulator variant, built for 256-point rows of
+// the 4x4 method, XR = p.xr pixels a thread)
 template <int N1, int N2, int C>
 cudaError_t row_reg_real(int band, const RegLaunch& L, const RowParams& p, const Grid& g, const void* U, void* X) {
+  if constexpr (N1 == 16 && N2 == 16 && C == 4) {
+    if (p.xr == 2) {
+      if (band == 1) return row_reg_variant<N1, N2, C, true, 1, 2>(L, p, g, U, X);
+      if (band == 2) return row_reg_variant<N1, N2, C, true, 2, 2>(L, p, g, U, X);
+      return row_reg_variant<N1, N2, C, true, 0, 2>(L, p, g, U, X);
+    }
+  }
   if constexpr (row_band_ok(N2, 1))
     if (band == 1) return row_reg_variant<N1, N2, C, true, 1>(L, p, g, U, X);
   if constexpr (row_band_ok(N2, 2))
