@@ -671,6 +671,14 @@ def diffract(field, dmat):
     return ifft2(dotmf(dmat, fft2(field)))
 
 
+def jones2H(jones, ks, n=1.0, betamax=BETAMAX, mode=+1):
+    """H components of an E (Jones) field in the isotropic medium n, per k
+    through the medium's E2H matrix, zero beyond betamax (dtmm/transfer.py:255-267)."""
+    eps = refind2eps([n] * 3)
+    _, f, _ = diffraction_alphaffi(jones.shape[-2:], ks, epsv=eps, epsa=np.zeros(3, FDTYPE), betamax=betamax)
+    return diffract(jones, E2H_mat(f, mode=mode))
+
+
 def E_correction_matrix(beta, phi, ks, d=1.0, epsv=(1, 1, 1), epsa=(0, 0, 0.0), mode=+1):
     """Inverse phase of the beam's own 2x2 E mode over d (dtmm/matrix.py:32)."""
     alpha, j, ji = alphaEEi(beta, phi, epsv, epsa, mode=mode)
@@ -837,10 +845,20 @@ def normalize_field(field, intensity_in, intensity_out):
     return field * fact
 
 
-def project_normalized_fft(field, dmat):
-    """Project in k-space and restore each mode's intensity (dtmm/transfer.py:78, ref=None)."""
-    f1 = fft2(field)
-    i1 = field2intensity(f1)
+def project_normalized_fft(field, dmat, ref=None):
+    """Project in k-space and restore each mode's intensity (dtmm/transfer.py:78).
+    With ``ref`` the intensities are the reference field's, and the field
+    itself is not used: the reference's call passes out=field
+    (dtmm/transfer.py:830), so fft2(ref) overwrites the field before the
+    field's own transform, which then transforms fft2(ref) once more
+    (dtmm/transfer.py:79-82); the projected field is fft2(fft2(ref))."""
+    if ref is not None:
+        fref = fft2(ref)
+        i1 = field2intensity(fref)
+        f1 = fft2(fref)
+    else:
+        f1 = fft2(field)
+        i1 = field2intensity(f1)
     f2 = dotmf(dmat, f1)
     i2 = field2intensity(f2)
     return ifft2(normalize_field(f2, i1, i2))
@@ -1559,8 +1577,12 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     full = diffraction == np.inf
     if smooth < 0:
         smooth = 0.0
-    if norm not in (0, DTMM_NORM_FFT):
-        raise NotImplementedError("oracle covers norm=DTMM_NORM_FFT and 0 (total)")
+    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_FFT | DTMM_NORM_REF):
+        raise NotImplementedError("oracle covers norm = 0 (total), DTMM_NORM_FFT and DTMM_NORM_FFT | DTMM_NORM_REF")
+    # with DTMM_NORM_REF a 2x2 reference field goes through the forward passes
+    # beside the transfer and sets the intensities of the normalisation
+    # (dtmm/transfer.py:637-645, :710-713, :770-806, :824-834, :868-869)
+    calc_reference = bool(norm & DTMM_NORM_REF)
     field_in, wavelengths, pixelsize = field_data
     shape = field_in.shape[-2:]
     layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
@@ -1591,6 +1613,7 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     indices = list(range(1, n - 1))
     field0 = transmitted_field(field_in, ks, n=nin, betamax=betamax)
     field = field_in.copy()
+    ref = field.copy() if calc_reference else None
     i0 = field2intensity(field0).sum(axis=(-2, -1))
     if not (0 <= diffraction <= np.inf):
         raise ValueError("Invalid diffraction value")
@@ -1605,6 +1628,12 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
         for j in indices:
             nsub, (thickness, ev, ea) = layers[j]
             _, (de, ee, ae) = eff_layers[j]
+            if calc_reference and i % 2 == 0:
+                # the reference field's E part through the layer: 2x2 mode 2
+                # without reflections (the input layer only matters with them)
+                ref[..., ::2, :, :] = propagate_2x2_effective_2(
+                    ref[..., ::2, :, :], ks, layers[j - 1][1], (thickness * direction, ev, ea), None,
+                    (de * direction, ee, ae), beta, phi, nsub, diffraction, 0, betamax, direction, None, None)[0]
             if full:
                 field = propagate_4x4_full(field, ks, (thickness * direction, ev, ea), nsub, betamax)
             elif reflection == 3:
@@ -1621,6 +1650,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                                                   (de * direction, ee, ae), beta, phi, nsub, diffraction, betamax)
             if bulk_out is not None:
                 bulk_out[j] = field
+        if ref is not None:
+            ref[..., 1::2, :, :] = jones2H(ref[..., ::2, :, :], ks, n=nout, betamax=betamax)
         indices.reverse()
         if work_in_fft:
             field = ifft2(field)
@@ -1630,8 +1661,10 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                     field = field - field_out
                 if i != npass - 1:
                     sigma = smooth * (npass - i) / npass
-                    if norm == DTMM_NORM_FFT:
-                        field = project_normalized_fft(field, pout_mat)
+                    if ref is not None:
+                        ref = ref * (nin / nout) ** 0.5
+                    if norm & DTMM_NORM_FFT:
+                        field = project_normalized_fft(field, pout_mat, ref=ref)
                     else:
                         field = project_normalized_total(field, pout_mat)
                     field = denoise_field(field, ks, nin, sigma)
@@ -1651,6 +1684,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                     field_in[...] = field_in * fact
                     field = field0 - field
                     field_in[...] = field_in + field
+                    if calc_reference:
+                        ref = field.copy()
             if work_in_fft:
                 field = fft2(field)
         else:
