@@ -26,7 +26,7 @@ ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_s
                "dtmm_diffract_workspace_size", "dtmm_diffract", "dtmm_q2data", "dtmm_wave_field",
                "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields",
                "dtmm_twisted_nematic_angles")
-ABI_VERSION = 4
+ABI_VERSION = 5
 STATIC_SCRATCH_BYTES = 64 << 20
 
 
@@ -65,6 +65,7 @@ class TransferDesc(ctypes.Structure):
         ("biaxial", ctypes.c_int),
         ("norm_total", ctypes.c_int),
         ("layer_block", ctypes.POINTER(ctypes.c_int)),
+        ("norm_ref", ctypes.c_int),
     ]
 
 

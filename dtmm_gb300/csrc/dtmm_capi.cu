@@ -95,6 +95,7 @@ struct Layout {
   size_t r2;                   // 2x2 real space, npass > 1: reflected wave of every interface
   size_t w2;                   // 2x2 real space with windows: window part, sum, reflected part and sum
   size_t effb, awb;            // per block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
+  size_t ref, ref2, refw;      // 4x4 norm_ref: reference field, its E part, window part / sum / H part
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -147,6 +148,9 @@ int check_desc(const dtmm_transfer_desc* d) {
                               "reference's tracked reflections need diffraction matrices)");
   if (d->precision != DTMM_PRECISION_MIXED && d->precision != DTMM_PRECISION_DOUBLE)
     return fail(DTMM_EINVAL, "unknown precision");
+  // the reference's reference field takes int(diffraction) windows (dtmm/propagate_2x2.py:330)
+  if (d->method == 4 && d->npass > 1 && d->norm_ref && !d->norm_total && d->diffraction == DTMM_DIFFRACTION_FULL)
+    return fail(DTMM_ENOTSUP, "norm_ref is built for finite diffraction");
   if (d->nlayers < 1) return fail(DTMM_EINVAL, "no layers");
   if (!d->thickness || !d->nstep || !d->ks || !d->beta || !d->phi) return fail(DTMM_EINVAL, "null host array");
   if (!d->epsv || !d->epsa) return fail(DTMM_EINVAL, "null material pointer");
@@ -263,6 +267,10 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.y2 = take(kpass2 ? field2 : 0);
   L.r2 = take(real2 && passes ? field2 * (size_t)(d->nlayers + 1) : 0);
   L.w2 = take(real2 && L.nwin > 1 ? 4 * field2 : 0);
+  const bool refd = d->method == 4 && passes && d->norm_ref && !d->norm_total;
+  L.ref = take(refd ? field : 0);
+  L.ref2 = take(refd ? field2 : 0);
+  L.refw = take(refd ? 3 * field2 : 0);
   // the real-space and modal paths keep no operator records
   L.op_one = (real_space || real2 || d->diffraction == DTMM_DIFFRACTION_FULL) ? 0 : L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
@@ -749,7 +757,7 @@ struct Engine {
   static int ktab_entries(int what) {
     switch (what) {
       case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
-      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: return 4;
+      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: return 4;
       default: return 16;
     }
   }
@@ -760,7 +768,7 @@ struct Engine {
     const bool diag = what == KT_DIAG;
     Slot* sl = diag ? dslot : slot;
     const int n = diag ? L.ndslots : L.nslots;
-    const int blk = (what == KT_PROJ || what == KT_WINMAT || what == KT_2WIN) ? -1 : cur_blk;
+    const int blk = (what == KT_PROJ || what == KT_WINMAT || what == KT_2WIN || what == KT_2H) ? -1 : cur_blk;
     int pick = 0;
     for (int i = 0; i < n; ++i) {
       if (sl[i].what == what && sl[i].d == dd && sl[i].e == eps_re && sl[i].mode == proj_mode && sl[i].blk == blk) {
@@ -771,8 +779,8 @@ struct Engine {
       if (sl[i].used < sl[pick].used) pick = i;
     }
     cpx<R>* dst = P((diag ? L.dslots : L.slots) + (size_t)pick * (diag ? L.dslot_bytes : L.slot_bytes));
-    int rc = (what == KT_PROJ) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
-                               : launch_ktab(what, dd, dst, proj_mode, eps_re);
+    int rc = (what == KT_PROJ || what == KT_2H) ? launch_ktab(what, dd, dst, proj_mode, eps_re, 0.0, false)
+                                                : launch_ktab(what, dd, dst, proj_mode, eps_re);
     if (rc) return rc;
     sl[pick].what = what;
     sl[pick].d = dd;
@@ -1378,7 +1386,7 @@ struct Engine {
     nt.den = 1.0 - std::exp(-d.nin / sigma);
     nt.ks = ks();
     const size_t n = (size_t)d.nlam * L.HW;  // one thread per (wavelength, k)
-    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, normalize ? 1 : 0, nt);
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, normalize ? 1 : 0, nt, nullptr);
     CKL("k_kproject");
     if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
     return launch_rows(f, 4, true, 1.0 / d.width);
@@ -1401,7 +1409,7 @@ struct Engine {
     off.den = 1.0;
     off.ks = ks();
     const size_t n = (size_t)d.nlam * L.HW;  // one thread per (wavelength, k)
-    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, 0, off);
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, 0, off, nullptr);
     CKL("k_kproject");
     if ((rc = total_intensity(K, fact()))) return rc;
     k_total_fact<<<(NI + 255) / 256, 256, 0, st>>>(i0f(), fact(), (double)L.HW, NI);
@@ -1458,6 +1466,10 @@ struct Engine {
     cpx<R>* field0 = nullptr;
     const cpx<R>* pin = nullptr;
     const cpx<R>* pout = nullptr;
+    // norm_ref: the reference field starts as the caller's input (dtmm/transfer.py:710-711)
+    const bool use_ref = npass > 1 && d.norm_ref && !d.norm_total;
+    cpx<R>* ref = use_ref ? P(L.ref) : nullptr;
+    if (use_ref) CK(cudaMemcpyAsync(ref, fin, bytes, cudaMemcpyDeviceToDevice, st));
     if (npass > 1) {
       if ((rc = table(KT_PROJ, 0.0, pin, 1, d.nin * d.nin))) return rc;
       field0 = P(L.field0);
@@ -1474,6 +1486,8 @@ struct Engine {
       return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for reflection mode 1 with diffraction >= 1");
     if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;
     for (int i = 0; i < npass; ++i) {
+      // the reference field goes through the even passes whose normalisation uses it
+      if (use_ref && i % 2 == 0 && i != npass - 1 && (rc = ref_pass(ref))) return rc;
       if ((rc = real_space ? sweep_real4(i, bulk) : sweep4(i, bulk))) return rc;
       if (npass > 1) {
         const double sigma = d.smooth * (npass - i) / npass;
@@ -1481,7 +1495,11 @@ struct Engine {
           if (i == 0 && (rc = axpby(F, F, nullptr, 1.0, fout, nullptr, -1.0))) return rc;
           if (i != npass - 1) {
             if ((rc = table(KT_PROJ, 0.0, pout, 1, d.nout * d.nout))) return rc;
-            if ((rc = d.norm_total ? project_total(F, pout, sigma) : project(F, pout, true, sigma))) return rc;
+            if (use_ref)
+              rc = project_ref(F, ref, pout, sigma);
+            else
+              rc = d.norm_total ? project_total(F, pout, sigma) : project(F, pout, true, sigma);
+            if (rc) return rc;
           }
           if ((rc = axpby(fout, fout, nullptr, 1.0, F, nullptr, 1.0))) return rc;
           CK(cudaMemcpyAsync(F, fout, bytes, cudaMemcpyDeviceToDevice, st));
@@ -1498,12 +1516,98 @@ struct Engine {
             if ((rc = axpby(fin, fin, fact(), 1.0, nullptr, nullptr, 0.0))) return rc;
             if ((rc = axpby(F, field0, nullptr, 1.0, F, nullptr, -1.0))) return rc;
             if ((rc = axpby(fin, fin, nullptr, 1.0, F, nullptr, 1.0))) return rc;
+            if (use_ref) CK(cudaMemcpyAsync(ref, F, bytes, cudaMemcpyDeviceToDevice, st));  // dtmm/transfer.py:868-869
           }
         }
       } else {
         CK(cudaMemcpyAsync(fout, F, bytes, cudaMemcpyDeviceToDevice, st));
       }
     }
+    return DTMM_OK;
+  }
+
+  // The reference field of norm_ref (DTMM_NORM_FFT | DTMM_NORM_REF): its E
+  // part through every layer of a forward pass as the 2x2 method's mode 2
+  // without reflections (per window: E P E^-1 half steps around the
+  // corrected E diffraction matrix, dtmm/transfer.py:770-775 with
+  // dtmm/propagate_2x2.py:286-377), then its H part from E in the output
+  // medium (jones2H, dtmm/transfer.py:805-806, :255-267).
+  int ref_pass(cpx<R>* ref) {
+    int rc = DTMM_OK;
+    cpx<R>* E2 = P(L.ref2);
+    cpx<R>* P2 = P(L.refw);
+    cpx<R>* A2 = P2 + (size_t)NI * 2 * L.HW;
+    cpx<R>* H2 = A2 + (size_t)NI * 2 * L.HW;
+    const size_t n2 = (size_t)NI * 2 * L.HW;
+    const size_t bytes2 = sizeof(cpx<R>) * n2;
+    const size_t ray4 = (size_t)d.nlam * L.HW * 4;
+    k_epart<R><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(ref, E2, g);
+    CKL("k_epart");
+    Local2Params p = local2_params();
+    p.mode = 1;
+    p.lin = -1;
+    chain_refl = 0;
+    const int save_blk = cur_blk;
+    for (int l = 0; l < d.nlayers; ++l) {
+      cur_blk = blk_of(l);
+      p.lout = l;
+      const int nst = d.nstep[l];
+      const double dd = d.thickness[l] / nst;
+      if (L.nwin == 1) {
+        if ((rc = chain2(p, 0, 0, nst, dd, E2, nullptr, nullptr))) break;
+        continue;
+      }
+      CK(cudaMemsetAsync(A2, 0, bytes2, st));
+      for (int w = 0; w < L.nwin; ++w) {
+        const cpx<R>* wt;
+        if ((rc = table(KT_2WIN, 0.0, wt, w))) break;
+        if ((rc = diffract(P2, E2, wt, ray4, 2))) break;
+        if ((rc = chain2(p, w, 0, nst, dd, P2, nullptr, nullptr))) break;
+        if ((rc = axpby(A2, A2, nullptr, 1.0, P2, nullptr, 1.0, 2))) break;
+      }
+      if (rc) break;
+      CK(cudaMemcpyAsync(E2, A2, bytes2, cudaMemcpyDeviceToDevice, st));
+    }
+    chain_refl = -1;
+    cur_blk = save_blk;
+    if (rc) return rc;
+    const cpx<R>* th;
+    if ((rc = table(KT_2H, 0.0, th, 1, d.nout * d.nout))) return rc;
+    if ((rc = diffract(H2, E2, th, 0, 2))) return rc;
+    k_join_eh<R><<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(ref, E2, H2, g);
+    CKL("k_join_eh");
+    return DTMM_OK;
+  }
+
+  // The even passes' normalisation with the reference field: ref scaled by
+  // sqrt(nin / nout) in place, the intensities at each k from fft2(ref), and
+  // -- as the reference's call, whose output array is the field, leaves it --
+  // the projection of fft2(fft2(ref)) with the notch, back to real space in f
+  // (dtmm/transfer.py:78-90, :824-834)
+  int project_ref(cpx<R>* f, cpx<R>* ref, const cpx<R>* Ptab, double sigma) {
+    int rc;
+    cpx<R>* X = P(L.X);
+    cpx<R>* U = P(L.U);
+    const size_t bytes = sizeof(cpx<R>) * (size_t)NI * 4 * L.HW;
+    if ((rc = axpby(ref, ref, nullptr, std::sqrt(d.nin / d.nout), nullptr, nullptr, 0.0))) return rc;
+    CK(cudaMemcpyAsync(X, ref, bytes, cudaMemcpyDeviceToDevice, st));
+    if ((rc = launch_rows(X, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(X, U, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;  // U = fft2(ref)
+    CK(cudaMemcpyAsync(X, U, bytes, cudaMemcpyDeviceToDevice, st));
+    if ((rc = launch_rows(X, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(X, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;  // f = fft2(U)
+    NotchParams nt;
+    nt.on = 1;
+    nt.x0 = d.nin;
+    nt.sigma = sigma;
+    nt.den = 1.0 - std::exp(-d.nin / sigma);
+    nt.ks = ks();
+    const size_t n = (size_t)d.nlam * L.HW;
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(f, Ptab, g, 1, nt, U);
+    CKL("k_kproject");
+    if ((rc = launch_col(f, X, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_rows(X, 4, true, 1.0 / d.width))) return rc;
+    CK(cudaMemcpyAsync(f, X, bytes, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;
   }
 
@@ -1718,7 +1822,12 @@ struct Engine {
   // window's part): dd the signed sub-step thickness of the output layer
   // bo: the field array of the output layer jout (field_in, field_out or a
   // bulk slab) that the reference adds the layer's field to, or null
+  // the interface step of chain2 (-1: the descriptor's reflection mode; 0:
+  // none, for the 4x4 method's reference field)
+  int chain_refl = -1;
+
   int chain2(Local2Params& p, int w, int jout, int nst, double dd, cpx<R>* f, cpx<R>* r, cpx<R>* bo) {
+    const int refl_mode = chain_refl >= 0 ? chain_refl : d.reflection;
     int rc;
     const bool tracked = r != nullptr;
     p.beta = wbeta() + w;
@@ -1728,7 +1837,7 @@ struct Engine {
     const bool zero = dd == 0.0;
     const size_t ray4 = (size_t)d.nlam * L.HW * 4;
     for (int s = 0; s < nst; ++s) {
-      if (s == 0 && d.reflection != 0) {
+      if (s == 0 && refl_mode != 0) {
         p.dzero = zero ? 1 : 0;
         rc = local2(p, tracked ? L2_TR : L2_ETI, f, r, (tracked && p.mode < 0) ? bo : nullptr);
         p.dzero = 0;
@@ -2188,7 +2297,7 @@ std::string& last_error_slot() { return g_err; }
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 4; }
+int dtmm_abi_version(void) { return 5; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 

@@ -1039,6 +1039,19 @@ __global__ void k_epart(const cpx<R>* __restrict__ f4, cpx<R>* __restrict__ f2, 
   f2[t] = f4[(img * 4 + 2 * c) * HW + k];
 }
 
+// ref[image] = (E0, H0, E1, H1): the 4-component field of E parts e and H parts h
+// ([image][2][H][W] each)
+template <typename R>
+__global__ void k_join_eh(cpx<R>* __restrict__ ref, const cpx<R>* __restrict__ e, const cpx<R>* __restrict__ h, Grid g) {
+  const size_t HW = (size_t)g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * 2 * HW) return;
+  const size_t img = t / (2 * HW), r = t - img * 2 * HW;
+  const size_t c = r / HW, k = r - c * HW;
+  ref[(img * 4 + 2 * c) * HW + k] = e[t];
+  ref[(img * 4 + 2 * c + 1) * HW + k] = h[t];
+}
+
 // ---------------------------------------------------------------------------
 // 4x4 transfer with diffraction = inf (dtmm/propagate_4x4.py:515-560): per
 // wavelength, the FFT amplitude of every eigenwave with beta < betamax is
@@ -1504,6 +1517,7 @@ enum KTab {
   // boundaries between blocks of different effective media (eps here, eps2 before)
   KT_D12 = 18,   // 4x4 D1(eps, d) . D2(eps2, d2): the merged half steps E P F^-1 . F P E^-1
   KT_2BX = 19,   // 2x2 E(eps, d) . T(eps2 -> eps) . E(eps2, d2), forward modes
+  KT_2H = 20,    // 2x2 H from E of the forward modes in the isotropic medium eps (E2H, dtmm/transfer.py:255-267)
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1692,7 +1706,7 @@ __device__ inline void iso_half_step(bool first, cpx<double> eps, double beta, d
 __device__ __forceinline__ int kt_entries(int what) {
   switch (what) {
     case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
-    case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: return 4;
+    case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: return 4;
     default: return 16;
   }
 }
@@ -1891,6 +1905,18 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     cpx<R>* o = tab + (size_t)t * 16;
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j) o[i * 4 + j] = cvt<R>(F[i][m0] * Fi[m0][j] + F[i][m0 + 2] * Fi[m0 + 2][j]);
+    return;
+  }
+  if (p.what == KT_2H) {
+    // rows Hy, Hx from rows Ex, Ey of the forward modes: B A^-1 with A, B the
+    // E and H rows of the field matrix's columns 0, 2 (zero beyond betamax)
+    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    cpx<double> Am[2][2], Ai[2][2];
+    Am[0][0] = F[0][0]; Am[0][1] = F[0][2]; Am[1][0] = F[2][0]; Am[1][1] = F[2][2];
+    inv2(Am, Ai);
+    cpx<R>* o = tab + (size_t)t * 4;
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j) o[i * 2 + j] = cvt<R>(F[2 * i + 1][0] * Ai[0][j] + F[2 * i + 1][2] * Ai[1][j]);
     return;
   }
   if (p.what == KT_2WIN) {
@@ -2322,8 +2348,11 @@ __device__ __forceinline__ double notch_k(const NotchParams& n, const Grid& g, i
 // k-space: f <- notch * P . f, optionally with the per-k intensity renormalisation
 // of project_normalized_fft (dtmm/transfer.py:67-90).  One thread per (lam, k):
 // the matrix and the notch once for every image of the wavelength.
+// With iref (normalize only) the intensity to restore is iref's at each k
+// instead of the field's own (the reference field's spectrum).
 template <typename R>
-__global__ void k_kproject(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ P, Grid g, int normalize, NotchParams nt) {
+__global__ void k_kproject(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ P, Grid g, int normalize, NotchParams nt,
+                           const cpx<R>* __restrict__ iref) {
   const int HW = g.H * g.W;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)g.nlam * HW) return;
@@ -2345,6 +2374,11 @@ __global__ void k_kproject(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ P,
     double fact = 1.0;
     if (normalize) {
       double i1 = poynting(v), i2 = poynting(o);
+      if (iref != nullptr) {
+        cpx<R> rv[4];
+        for (int c = 0; c < 4; ++c) rv[c] = iref[(img * 4 + c) * HW + k];
+        i1 = poynting(rv);
+      }
       if (i2 == 0.0) {
         i2 = 1.0;
         i1 = 0.0;

@@ -354,8 +354,10 @@ class DevicePlan:
         bmax = max(float(betamax), float(np.max(np.abs(k["beta"]))))
         d.real_path = int(mat.eps_min is not None and not mat.biaxial and mat.eps_min > bmax * bmax)
         d.biaxial = int(mat.biaxial)
-        # norm = 0: the reference's "total" renormalisation between passes
+        # norm = 0: the reference's "total" renormalisation between passes;
+        # DTMM_NORM_FFT | DTMM_NORM_REF: the per-k one with a reference field
         d.norm_total = int(not (int(norm) & DTMM_NORM_FFT))
+        d.norm_ref = int(bool(int(norm) & DTMM_NORM_REF) and bool(int(norm) & DTMM_NORM_FFT))
         if mat.layer_block is not None:
             k["lb"] = np.ascontiguousarray(mat.layer_block, np.int32)
             d.layer_block = k["lb"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -534,9 +536,13 @@ def _check_path(method, reflection, npass, diffraction, norm):
         # the reference's tracked reflection applies a diffraction matrix it does
         # not form without diffraction (dtmm/propagate_2x2.py:61) and fails
         raise NotImplementedError("2x2 reflection 1 without diffraction is not supported with npass > 1")
-    if norm not in (0, DTMM_NORM_FFT) and method == "4x4" and npass > 1:
-        # DTMM_NORM_REF propagates a 2x2 reference field beside the transfer (dtmm/transfer.py:780-785)
-        raise NotImplementedError("norm modes with DTMM_NORM_REF are outside the GPU engine")
+    if norm & DTMM_NORM_REF and method == "4x4" and npass > 1 and diffraction == np.inf:
+        # the reference's reference field takes int(diffraction) windows (dtmm/propagate_2x2.py:330)
+        raise NotImplementedError("norm with DTMM_NORM_REF is built for finite diffraction")
+    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_FFT | DTMM_NORM_REF) and method == "4x4" and npass > 1:
+        # DTMM_NORM_REF alone: the reference's "local" normalisation, a per-pixel
+        # polarizer projection of the reference field (dtmm/transfer.py:103-136)
+        raise NotImplementedError("norm = DTMM_NORM_REF without DTMM_NORM_FFT (local) is outside the GPU engine")
 
 
 def _require_cuda():

@@ -105,6 +105,16 @@ typedef struct dtmm_transfer_desc {
      block per layer with split_layers).  Null: one block.  2x2 reflection 0 /
      1 with several blocks: npass 1.  ABI 4. */
   const int* layer_block;
+  /* 4x4 with npass > 1 and norm_total 0: 1 propagates a 2x2 reference field
+     (the input's E part, then each backward pass's result) through the
+     forward passes beside the transfer, 2x2 mode 2 without reflections, with
+     its H part in the output medium, and takes the intensities of the
+     per-k normalisation from it (the reference's DTMM_NORM_FFT |
+     DTMM_NORM_REF, dtmm/transfer.py:637-645, :710-713, :770-806, :824-869;
+     the reference's projection there transforms fft2(ref) where the field
+     was, dtmm/transfer.py:78-83, :830, and this does the same).  Finite
+     diffraction only.  ABI 5. */
+  int norm_ref;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -136,7 +146,7 @@ typedef struct dtmm_kernel_times {
 } dtmm_kernel_times;
 
 /* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
-   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block). */
+   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block; 5: norm_ref). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

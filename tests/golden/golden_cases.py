@@ -156,6 +156,22 @@ CASES = {
                                      illum=dict(beta=0.1, phi=0.6),
                                      transfer=dict(method="4x4", diffraction=1, npass=3, norm=0, beta=0.1,
                                                    phi=0.6)),
+    # npass > 1 with norm = DTMM_NORM_FFT | DTMM_NORM_REF (3): a 2x2 reference field
+    # through the forward passes sets the intensities of the per-mode normalisation
+    "fourx4_norm_ref_npass2": dict(shape=(14, 12), nlayers=3, wavelengths=[520.0], pixelsize=100.0,
+                                   material=("twisted", dict()), seed=69,
+                                   illum=dict(beta=0.1, phi=0.4, jones=(1, 0)),
+                                   transfer=dict(method="4x4", diffraction=1, npass=2, norm=3, beta=0.1, phi=0.4)),
+    "fourx4_norm_ref_d3_npass3": dict(shape=(12, 12), nlayers=2, wavelengths=[480.0, 600.0], pixelsize=100.0,
+                                      material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=70,
+                                      illum=dict(),
+                                      transfer=dict(method="4x4", diffraction=3, npass=3, norm=3, beta=0.0,
+                                                    phi=0.0)),
+    "fourx4_norm_ref_nstep2_npass4": dict(shape=(12, 14), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                          material=("twisted", dict(thickness=2.0)), seed=71,
+                                          illum=dict(jones=(0, 1)),
+                                          transfer=dict(method="4x4", diffraction=1, nstep=2, npass=4, norm=3,
+                                                        beta=0.0, phi=0.0)),
     "fourx4_norm_total_d3_npass4": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
                                         material=("twisted", dict()), seed=19,
                                         illum=dict(jones=(1, 0)),
@@ -459,25 +475,8 @@ CASES = {
 }
 
 
-# cases pinned against the reference ahead of the engine (CPU only)
-ORACLE_CASES = {
-    # npass > 1 with norm = DTMM_NORM_FFT | DTMM_NORM_REF (3): a 2x2 reference field
-    # through the forward passes sets the intensities of the per-mode normalisation
-    "fourx4_norm_ref_npass2": dict(shape=(14, 12), nlayers=3, wavelengths=[520.0], pixelsize=100.0,
-                                   material=("twisted", dict()), seed=69,
-                                   illum=dict(beta=0.1, phi=0.4, jones=(1, 0)),
-                                   transfer=dict(method="4x4", diffraction=1, npass=2, norm=3, beta=0.1, phi=0.4)),
-    "fourx4_norm_ref_d3_npass3": dict(shape=(12, 12), nlayers=2, wavelengths=[480.0, 600.0], pixelsize=100.0,
-                                      material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=70,
-                                      illum=dict(),
-                                      transfer=dict(method="4x4", diffraction=3, npass=3, norm=3, beta=0.0,
-                                                    phi=0.0)),
-    "fourx4_norm_ref_nstep2_npass4": dict(shape=(12, 14), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
-                                          material=("twisted", dict(thickness=2.0)), seed=71,
-                                          illum=dict(jones=(0, 1)),
-                                          transfer=dict(method="4x4", diffraction=1, nstep=2, npass=4, norm=3,
-                                                        beta=0.0, phi=0.0)),
-}
+# every case with a reference fixture is also a GPU parity case
+ORACLE_CASES = {}
 
 
 def build_optical_data(case):

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 4
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 5
 
 
 def _desc(**kw):
@@ -153,6 +153,20 @@ def test_2x2_descriptor_rules(lib):
     assert size(reflection=1, diffraction=0, npass=2) == 0 and "diffraction" in _lib.last_error()
     assert size(reflection=3) == 0 and "reflection" in _lib.last_error()
     assert size(reflection=1, diffraction=_lib.DIFFRACTION_FULL) == 0
+
+
+def test_norm_ref_descriptor_rules(lib):
+    """norm_ref (the reference's DTMM_NORM_FFT | DTMM_NORM_REF): 4x4 with npass > 1
+    keeps the reference field, its E part and the 2x2 window / H buffers; it is
+    refused with diffraction = inf (the reference takes int(diffraction)
+    windows for the reference field) and has no effect with npass 1."""
+    size = lambda **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw)))
+    a = size(npass=3)
+    b = size(npass=3, norm_ref=1)
+    assert b - a >= 2 * 16 * 16 * 4 * 8  # a field and two field halves at least
+    assert size(npass=1, norm_ref=1) == size(npass=1)
+    assert size(npass=3, norm_ref=1, diffraction=_lib.DIFFRACTION_FULL) == 0
+    assert "norm_ref" in _lib.last_error()
 
 
 def test_norm_total_field(lib):
