@@ -96,6 +96,7 @@ struct Layout {
   size_t w2;                   // 2x2 real space with windows: window part, sum, reflected part and sum
   size_t effb, awb;            // per block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
   size_t ref, ref2, refw;      // 4x4 norm_ref: reference field, its E part, window part / sum / H part
+  size_t fnorm;                // 4x4 norm_ref without norm FFT ("local"): the output medium's field matrix and inverse
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
   size_t op_one;  // bytes of one layer's operators
   size_t total;
@@ -149,7 +150,7 @@ int check_desc(const dtmm_transfer_desc* d) {
   if (d->precision != DTMM_PRECISION_MIXED && d->precision != DTMM_PRECISION_DOUBLE)
     return fail(DTMM_EINVAL, "unknown precision");
   // the reference's reference field takes int(diffraction) windows (dtmm/propagate_2x2.py:330)
-  if (d->method == 4 && d->npass > 1 && d->norm_ref && !d->norm_total && d->diffraction == DTMM_DIFFRACTION_FULL)
+  if (d->method == 4 && d->npass > 1 && d->norm_ref && d->diffraction == DTMM_DIFFRACTION_FULL)
     return fail(DTMM_ENOTSUP, "norm_ref is built for finite diffraction");
   if (d->nlayers < 1) return fail(DTMM_EINVAL, "no layers");
   if (!d->thickness || !d->nstep || !d->ks || !d->beta || !d->phi) return fail(DTMM_EINVAL, "null host array");
@@ -267,10 +268,11 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.y2 = take(kpass2 ? field2 : 0);
   L.r2 = take(real2 && passes ? field2 * (size_t)(d->nlayers + 1) : 0);
   L.w2 = take(real2 && L.nwin > 1 ? 4 * field2 : 0);
-  const bool refd = d->method == 4 && passes && d->norm_ref && !d->norm_total;
+  const bool refd = d->method == 4 && passes && d->norm_ref;
   L.ref = take(refd ? field : 0);
   L.ref2 = take(refd ? field2 : 0);
   L.refw = take(refd ? 3 * field2 : 0);
+  L.fnorm = take(refd && d->norm_total ? 32 * sizeof(cpx<double>) : 0);
   // the real-space and modal paths keep no operator records
   L.op_one = (real_space || real2 || d->diffraction == DTMM_DIFFRACTION_FULL) ? 0 : L.cplx * nrw * OP_REC * L.HW;
   const size_t limit = d->op_cache_bytes ? d->op_cache_bytes : ((size_t)48 << 30);
@@ -1467,7 +1469,7 @@ struct Engine {
     const cpx<R>* pin = nullptr;
     const cpx<R>* pout = nullptr;
     // norm_ref: the reference field starts as the caller's input (dtmm/transfer.py:710-711)
-    const bool use_ref = npass > 1 && d.norm_ref && !d.norm_total;
+    const bool use_ref = npass > 1 && d.norm_ref;
     cpx<R>* ref = use_ref ? P(L.ref) : nullptr;
     if (use_ref) CK(cudaMemcpyAsync(ref, fin, bytes, cudaMemcpyDeviceToDevice, st));
     if (npass > 1) {
@@ -1496,7 +1498,7 @@ struct Engine {
           if (i != npass - 1) {
             if ((rc = table(KT_PROJ, 0.0, pout, 1, d.nout * d.nout))) return rc;
             if (use_ref)
-              rc = project_ref(F, ref, pout, sigma);
+              rc = d.norm_total ? project_local(F, ref, pout, sigma) : project_ref(F, ref, pout, sigma);
             else
               rc = d.norm_total ? project_total(F, pout, sigma) : project(F, pout, true, sigma);
             if (rc) return rc;
@@ -1609,6 +1611,47 @@ struct Engine {
     if ((rc = launch_rows(X, 4, true, 1.0 / d.width))) return rc;
     CK(cudaMemcpyAsync(f, X, bytes, cudaMemcpyDeviceToDevice, st));
     return DTMM_OK;
+  }
+
+  // The "local" normalisation with the reference field (norm_ref with
+  // norm_total, the reference's DTMM_NORM_REF alone): f projected in k-space
+  // (no per-k normalisation), per pixel the polarizer split of the
+  // reference field (k_local_norm), then the notch (dtmm/transfer.py:103-136,
+  // :824-835)
+  int project_local(cpx<R>* f, cpx<R>* ref, const cpx<R>* Ptab, double sigma) {
+    int rc;
+    cpx<R>* K = P(L.U);
+    const size_t n = (size_t)d.nlam * L.HW;
+    const size_t npix = (size_t)NI * L.HW;
+    if ((rc = axpby(ref, ref, nullptr, std::sqrt(d.nin / d.nout), nullptr, nullptr, 0.0))) return rc;
+    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(f, K, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;
+    NotchParams off;
+    off.on = 0;
+    off.den = 1.0;
+    off.ks = ks();
+    k_kproject<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, Ptab, g, 0, off, nullptr);
+    CKL("k_kproject");
+    if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
+    if ((rc = launch_rows(f, 4, true, 1.0 / d.width))) return rc;
+    cpx<double>* fn = A<cpx<double>>(L.fnorm);
+    k_iso_fnorm<<<1, 32, 0, st>>>(d.nout * d.nout, fn);
+    CKL("k_iso_fnorm");
+    k_local_norm<R><<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(f, ref, fn, g);
+    CKL("k_local_norm");
+    // the notch of denoise_field
+    if ((rc = launch_rows(f, 4, false, 1.0))) return rc;
+    if ((rc = launch_col(f, K, 4, 4, KOP_NONE, nullptr, 1, nullptr, true, false, 1.0))) return rc;
+    NotchParams nt;
+    nt.on = 1;
+    nt.x0 = d.nin;
+    nt.sigma = sigma;
+    nt.den = 1.0 - std::exp(-d.nin / sigma);
+    nt.ks = ks();
+    k_kscale<R><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(K, nullptr, g, nt);
+    CKL("k_kscale");
+    if ((rc = launch_col(K, f, 4, 4, KOP_NONE, nullptr, 1, nullptr, false, true, 1.0 / d.height))) return rc;
+    return launch_rows(f, 4, true, 1.0 / d.width);
   }
 
   // byte offset of the backward-mode records in a voxel's operator records

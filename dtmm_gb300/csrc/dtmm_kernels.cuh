@@ -1052,6 +1052,84 @@ __global__ void k_join_eh(cpx<R>* __restrict__ ref, const cpx<R>* __restrict__ e
   ref[(img * 4 + 2 * c + 1) * HW + k] = h[t];
 }
 
+// The field matrix of the isotropic medium eps at normal incidence with its
+// columns scaled to unit z-Poynting (f_iso with normalize_f, dtmm/tmm.py:1074,
+// :701-724) and its inverse: out[0..15] F, out[16..31] F^-1 (one thread)
+__global__ void k_iso_fnorm(double eps, cpx<double>* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  cpx<double> al[4], F[4][4], Fi[4][4];
+  iso_alphaf(0.0, 0.0, mk<double>(eps, 0.0), al, F);
+  for (int i = 0; i < 4; ++i) {
+    const double t1 = F[0][i].re * F[1][i].re + F[0][i].im * F[1][i].im;
+    const double t2 = F[2][i].re * F[3][i].re + F[2][i].im * F[3][i].im;
+    const double n = sqrt(fabs(t1 - t2));
+    const double sc = n == 0.0 ? 0.0 : 1.0 / n;
+    for (int r = 0; r < 4; ++r) F[r][i] = F[r][i] * sc;
+  }
+  inv4(F, Fi);
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      out[r * 4 + c] = F[r][c];
+      out[16 + r * 4 + c] = Fi[r][c];
+    }
+}
+
+// The reference's "local" normalisation of a projected real-space field f
+// with the reference field ref, per pixel in FP64 (dtmm/transfer.py:103-136):
+// a = Fn^-1 f the eigen-amplitudes in the output medium at normal incidence,
+// J the polarizer of the normalised forward Jones vector (a0, a2), P1 = Fn
+// [J, conj J interleaved] Fn^-1; f <- f |clip(I(P1 ref) / I(f))| + (ref - P1 ref)
+template <typename R>
+__global__ void k_local_norm(cpx<R>* __restrict__ f, const cpx<R>* __restrict__ ref, const cpx<double>* __restrict__ fn,
+                             Grid g) {
+  const size_t HW = (size_t)g.H * g.W;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)g.NI * HW) return;
+  const size_t img = t / HW, k = t - img * HW;
+  cpx<double> v[4], r[4], a[4];
+  for (int c = 0; c < 4; ++c) {
+    v[c] = cvt_d(f[(img * 4 + c) * HW + k]);
+    r[c] = cvt_d(ref[(img * 4 + c) * HW + k]);
+  }
+  const cpx<double>* Fn = fn;
+  const cpx<double>* Fi = fn + 16;
+  for (int i = 0; i < 4; ++i) {
+    cpx<double> s = mk<double>(0.0, 0.0);
+    for (int c = 0; c < 4; ++c) s = s + Fi[i * 4 + c] * v[c];
+    a[i] = s;
+  }
+  const double nrm = sqrt(a[0].re * a[0].re + a[0].im * a[0].im + a[2].re * a[2].re + a[2].im * a[2].im);
+  const cpx<double> jc = mk<double>(a[0].re / nrm, a[0].im / nrm), js = mk<double>(a[2].re / nrm, a[2].im / nrm);
+  const cpx<double> J[2][2] = {{jc * conj(jc), jc * conj(js)}, {js * conj(jc), js * conj(js)}};
+  // P1 ref = Fn (M (Fn^-1 ref)), M = J on the forward modes, conj J on the backward ones
+  cpx<double> b[4], m[4], p[4];
+  for (int i = 0; i < 4; ++i) {
+    cpx<double> s = mk<double>(0.0, 0.0);
+    for (int c = 0; c < 4; ++c) s = s + Fi[i * 4 + c] * r[c];
+    b[i] = s;
+  }
+  m[0] = J[0][0] * b[0] + J[0][1] * b[2];
+  m[2] = J[1][0] * b[0] + J[1][1] * b[2];
+  m[1] = conj(J[0][0]) * b[1] + conj(J[0][1]) * b[3];
+  m[3] = conj(J[1][0]) * b[1] + conj(J[1][1]) * b[3];
+  for (int i = 0; i < 4; ++i) {
+    cpx<double> s = mk<double>(0.0, 0.0);
+    for (int c = 0; c < 4; ++c) s = s + Fn[i * 4 + c] * m[c];
+    p[i] = s;
+  }
+  double i1 = (p[0].re * p[1].re + p[0].im * p[1].im) - (p[2].re * p[3].re + p[2].im * p[3].im);
+  double i2 = (v[0].re * v[1].re + v[0].im * v[1].im) - (v[2].re * v[3].re + v[2].im * v[3].im);
+  if (i2 == 0.0) {
+    i2 = 1.0;
+    i1 = 0.0;
+  }
+  double fact = i1 / i2;
+  if (fact <= -1.0) fact = -1.0;
+  if (fact >= 1.0) fact = 1.0;
+  fact = fabs(fact);
+  for (int c = 0; c < 4; ++c) f[(img * 4 + c) * HW + k] = cvt<R>(v[c] * fact + (r[c] - p[c]));
+}
+
 // ---------------------------------------------------------------------------
 // 4x4 transfer with diffraction = inf (dtmm/propagate_4x4.py:515-560): per
 // wavelength, the FFT amplitude of every eigenwave with beta < betamax is
@@ -2468,7 +2546,7 @@ __global__ void k_kscale(cpx<R>* __restrict__ f, const double* fact, Grid g, Not
   const int per = g.nray * g.npol;
   for (int q = 0; q < per; ++q) {
     const size_t img = (size_t)q * g.nlam + lam;
-    const R s = (R)(fact[img] * notch);
+    const R s = (R)((fact ? fact[img] : 1.0) * notch);
     for (int c = 0; c < 4; ++c) {
       cpx<R>& v = f[(img * 4 + c) * HW + k];
       v = v * s;

@@ -357,7 +357,7 @@ class DevicePlan:
         # norm = 0: the reference's "total" renormalisation between passes;
         # DTMM_NORM_FFT | DTMM_NORM_REF: the per-k one with a reference field
         d.norm_total = int(not (int(norm) & DTMM_NORM_FFT))
-        d.norm_ref = int(bool(int(norm) & DTMM_NORM_REF) and bool(int(norm) & DTMM_NORM_FFT))
+        d.norm_ref = int(bool(int(norm) & DTMM_NORM_REF))
         if mat.layer_block is not None:
             k["lb"] = np.ascontiguousarray(mat.layer_block, np.int32)
             d.layer_block = k["lb"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -539,10 +539,8 @@ def _check_path(method, reflection, npass, diffraction, norm):
     if norm & DTMM_NORM_REF and method == "4x4" and npass > 1 and diffraction == np.inf:
         # the reference's reference field takes int(diffraction) windows (dtmm/propagate_2x2.py:330)
         raise NotImplementedError("norm with DTMM_NORM_REF is built for finite diffraction")
-    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_FFT | DTMM_NORM_REF) and method == "4x4" and npass > 1:
-        # DTMM_NORM_REF alone: the reference's "local" normalisation, a per-pixel
-        # polarizer projection of the reference field (dtmm/transfer.py:103-136)
-        raise NotImplementedError("norm = DTMM_NORM_REF without DTMM_NORM_FFT (local) is outside the GPU engine")
+    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_REF, DTMM_NORM_FFT | DTMM_NORM_REF) and method == "4x4" and npass > 1:
+        raise ValueError("norm must be a combination of DTMM_NORM_FFT and DTMM_NORM_REF")
 
 
 def _require_cuda():

@@ -105,15 +105,19 @@ typedef struct dtmm_transfer_desc {
      block per layer with split_layers).  Null: one block.  2x2 reflection 0 /
      1 with several blocks: npass 1.  ABI 4. */
   const int* layer_block;
-  /* 4x4 with npass > 1 and norm_total 0: 1 propagates a 2x2 reference field
-     (the input's E part, then each backward pass's result) through the
-     forward passes beside the transfer, 2x2 mode 2 without reflections, with
-     its H part in the output medium, and takes the intensities of the
-     per-k normalisation from it (the reference's DTMM_NORM_FFT |
-     DTMM_NORM_REF, dtmm/transfer.py:637-645, :710-713, :770-806, :824-869;
-     the reference's projection there transforms fft2(ref) where the field
-     was, dtmm/transfer.py:78-83, :830, and this does the same).  Finite
-     diffraction only.  ABI 5. */
+  /* 4x4 with npass > 1: 1 propagates a 2x2 reference field (the input's E
+     part, then each backward pass's result) through the forward passes
+     beside the transfer, 2x2 mode 2 without reflections, with its H part in
+     the output medium (dtmm/transfer.py:637-645, :710-713, :770-806).  With
+     norm_total 0 (the reference's DTMM_NORM_FFT | DTMM_NORM_REF) the
+     intensities of the per-k normalisation come from it (the reference's
+     projection there transforms fft2(ref) where the field was,
+     dtmm/transfer.py:78-83, :830, and this does the same).  With
+     norm_total 1 (the reference's DTMM_NORM_REF alone, "local",
+     dtmm/transfer.py:103-136, :824-835) the projected field is split per
+     pixel by the polarizer of its forward amplitudes at normal incidence in
+     the output medium: the reference field's polarised part sets the
+     intensity, its remainder is added.  Finite diffraction only.  ABI 5. */
   int norm_ref;
 } dtmm_transfer_desc;
 

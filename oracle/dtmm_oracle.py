@@ -877,6 +877,45 @@ def project_normalized_total(field, dmat):
     return out * fact[..., None, None, None]
 
 
+def project_normalized_local(field, dmat, nout, ref=None):
+    """Project in k-space, then per pixel split the field (or the reference
+    field) by the polarizer of the projection's forward amplitudes at normal
+    incidence in the output medium: the polarised part carries the
+    projection's intensity restored to the polarised part's, the rest is
+    added unchanged (dtmm/transfer.py:103-136; f_iso and fvec2avec
+    dtmm/tmm.py:1074, :1851; jonesvec and polarizer dtmm/jones.py:55, :236;
+    ray_jonesmat4x4 with jonesmat4x4 and as4x4 dtmm/jones4.py:205, :75,
+    dtmm/jones.py:371, at beta = phi = 0)."""
+    f = ifft2(dotmf(dmat, fft2(field)))
+    epsv = np.asarray(refind2eps([nout] * 3), CDTYPE)
+    _, fmat = alphaf(0.0, 0.0, epsv, np.zeros(3, FDTYPE))
+    fn = normalize_f(fmat)
+    fni = inv(fn)
+    a = dotmv(fni, np.moveaxis(f, -3, -1))  # eigen-amplitudes per pixel
+    jv = a[..., 0::2]
+    norm = (jv[..., 0] * jv[..., 0].conj() + jv[..., 1] * jv[..., 1].conj()) ** 0.5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        jv = jv / norm[..., None]
+    jmat = np.empty(jv.shape + (2,), CDTYPE)
+    c, sn = jv[..., 0], jv[..., 1]
+    jmat[..., 0, 0] = c * c.conj()
+    jmat[..., 0, 1] = c * sn.conj()
+    jmat[..., 1, 0] = sn * c.conj()
+    jmat[..., 1, 1] = sn * sn.conj()
+    m4 = np.zeros(jmat.shape[:-2] + (4, 4), CDTYPE)
+    m4[..., 0::2, 0::2] = jmat
+    m4[..., 1::2, 1::2] = np.conj(jmat)
+    pmat1 = dotmm(fn, dotmm(m4, fni))
+    pmat2 = -pmat1
+    for k in range(4):
+        pmat2[..., k, k] += 1
+    src = field if ref is None else ref
+    i1 = field2intensity(dotmf(pmat1, src))
+    rest = dotmf(pmat2, src)
+    i2 = field2intensity(f)
+    return normalize_field(f, i1, i2) + rest
+
+
 def exp_notch_filter(x, x0, sigma):
     """Attenuation around beta = x0 (dtmm/denoise.py:21)."""
     return np.asarray((1 - np.exp(-np.abs(x - x0).clip(0, x0) / sigma)) / (1 - np.exp(-x0 / sigma)), FDTYPE)
@@ -1577,8 +1616,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     full = diffraction == np.inf
     if smooth < 0:
         smooth = 0.0
-    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_FFT | DTMM_NORM_REF):
-        raise NotImplementedError("oracle covers norm = 0 (total), DTMM_NORM_FFT and DTMM_NORM_FFT | DTMM_NORM_REF")
+    if norm not in (0, DTMM_NORM_FFT, DTMM_NORM_REF, DTMM_NORM_FFT | DTMM_NORM_REF):
+        raise ValueError("norm must be a combination of DTMM_NORM_FFT and DTMM_NORM_REF")
     # with DTMM_NORM_REF a 2x2 reference field goes through the forward passes
     # beside the transfer and sets the intensities of the normalisation
     # (dtmm/transfer.py:637-645, :710-713, :770-806, :824-834, :868-869)
@@ -1665,6 +1704,8 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
                         ref = ref * (nin / nout) ** 0.5
                     if norm & DTMM_NORM_FFT:
                         field = project_normalized_fft(field, pout_mat, ref=ref)
+                    elif calc_reference:
+                        field = project_normalized_local(field, pout_mat, nout, ref=ref)
                     else:
                         field = project_normalized_total(field, pout_mat)
                     field = denoise_field(field, ks, nin, sigma)

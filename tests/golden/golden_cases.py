@@ -172,6 +172,17 @@ CASES = {
                                           illum=dict(jones=(0, 1)),
                                           transfer=dict(method="4x4", diffraction=1, nstep=2, npass=4, norm=3,
                                                         beta=0.0, phi=0.0)),
+    # npass > 1 with norm = DTMM_NORM_REF (2): the "local" per-pixel normalisation with the
+    # reference field
+    "fourx4_norm_local_npass2": dict(shape=(12, 14), nlayers=3, wavelengths=[540.0], pixelsize=100.0,
+                                     material=("twisted", dict()), seed=72,
+                                     illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                                     transfer=dict(method="4x4", diffraction=1, npass=2, norm=2, beta=0.1, phi=0.3)),
+    "fourx4_norm_local_d3_npass3": dict(shape=(12, 12), nlayers=2, wavelengths=[470.0, 610.0], pixelsize=100.0,
+                                        material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=73,
+                                        illum=dict(),
+                                        transfer=dict(method="4x4", diffraction=3, npass=3, norm=2, beta=0.0,
+                                                      phi=0.0)),
     "fourx4_norm_total_d3_npass4": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
                                         material=("twisted", dict()), seed=19,
                                         illum=dict(jones=(1, 0)),

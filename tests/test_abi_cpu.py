@@ -156,10 +156,12 @@ def test_2x2_descriptor_rules(lib):
 
 
 def test_norm_ref_descriptor_rules(lib):
-    """norm_ref (the reference's DTMM_NORM_FFT | DTMM_NORM_REF): 4x4 with npass > 1
-    keeps the reference field, its E part and the 2x2 window / H buffers; it is
-    refused with diffraction = inf (the reference takes int(diffraction)
-    windows for the reference field) and has no effect with npass 1."""
+    """norm_ref (the reference's DTMM_NORM_REF, with DTMM_NORM_FFT or alone):
+    4x4 with npass > 1 keeps the reference field, its E part and the 2x2
+    window / H buffers, and with norm_total ("local") the output medium's
+    field matrix and its inverse besides; it is refused with diffraction =
+    inf (the reference takes int(diffraction) windows for the reference
+    field) and has no effect with npass 1."""
     size = lambda **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_desc(**kw)))
     a = size(npass=3)
     b = size(npass=3, norm_ref=1)
@@ -167,6 +169,9 @@ def test_norm_ref_descriptor_rules(lib):
     assert size(npass=1, norm_ref=1) == size(npass=1)
     assert size(npass=3, norm_ref=1, diffraction=_lib.DIFFRACTION_FULL) == 0
     assert "norm_ref" in _lib.last_error()
+    c = size(npass=3, norm_total=1)
+    assert size(npass=3, norm_total=1, norm_ref=1) - c >= b - a + 2 * 16 * 16
+    assert size(npass=3, norm_total=1, norm_ref=1, diffraction=_lib.DIFFRACTION_FULL) == 0
 
 
 def test_norm_total_field(lib):
