@@ -21,7 +21,8 @@ k-space "effective" split-step operator) and ``method="2x2"`` with reflection
 mode 0, diffraction >= 1 (diffraction > 1 = tent-window mode grouping),
 npass >= 1 for 4x4 (norm "fft"), nstep >= 1, scalar or per-ray beta/phi or
 beta/phi estimated from the field, real or complex eps, isotropic / uniaxial /
-biaxial voxels, isotropic effective layers (eff_data 0).
+biaxial voxels, effective layers of isotropic, uniaxial or biaxial symmetry
+(eff_data 0 / 1 / 2, per block or per layer).
 """
 from __future__ import annotations
 
@@ -1047,7 +1048,128 @@ def _isotropic_mean(epsv):
     return np.asarray(m.mean())
 
 
-def _layers_list(block, nin, nout, nstep, is_first, is_last):
+_SYMMETRY_NAMES = {"isotropic": 0, "uniaxial": 1, "biaxial": 2}
+
+
+def _symmetry(arg):
+    """Symmetry identifier -> 0 / 1 / 2, or an array of them (dtmm/data.py:1344-1362)."""
+    if isinstance(arg, str):
+        if arg not in _SYMMETRY_NAMES:
+            raise ValueError("Invalid symmetry argument.")
+        return _SYMMETRY_NAMES[arg]
+    if np.ndim(arg) == 0:
+        if arg not in (0, 1, 2, -1):
+            raise ValueError("Invalid symmetry argument.")
+        return int(arg)
+    return np.asarray([_symmetry(a) for a in arg], int)
+
+
+def tensor_eig(eps6):
+    """Eigenvalues and eigenvectors (columns) of one symmetric 3x3 tensor given
+    as (00, 11, 22, 01, 02, 12), ordered so that the third is the most
+    distinct and the eigenvector matrix is a proper rotation
+    (dtmm/linalg.py:225-318, :364-423).  The reference follows Eberly's
+    non-iterative 3x3 eigensolver, whose eigenvalues come in increasing order
+    and whose eigenvectors form a right-handed frame; here numpy's solver
+    gives the increasing eigenvalues (real parts for a complex tensor) and the
+    frame is made right-handed by the sign of the first vector.  A tensor whose
+    scaled off-diagonal sum of squares is at most 1e-12 is taken as diagonal
+    (identity frame), as the reference does.  Then the cyclic permutation that
+    moves the most distinct eigenvalue to the third place
+    (``_sort_eigvec``, dtmm/linalg.py:166-218)."""
+    e = np.asarray(eps6, CDTYPE)
+    a = np.array([[e[0], e[3], e[4]], [e[3], e[1], e[5]], [e[4], e[5], e[2]]], CDTYPE)
+    scale = np.max(np.abs(e))
+    if scale == 0.0:
+        w, v = np.zeros(3, CDTYPE), np.eye(3, dtype=CDTYPE)
+    else:
+        sa = a / scale
+        off = sa[0, 1] ** 2 + sa[0, 2] ** 2 + sa[1, 2] ** 2
+        if abs(off) <= 1e-12:
+            w, v = np.array([a[0, 0], a[1, 1], a[2, 2]], CDTYPE), np.eye(3, dtype=CDTYPE)
+        else:
+            if np.all(a.imag == 0.0):
+                wr, vr = np.linalg.eigh(a.real)
+                w, v = wr.astype(CDTYPE), vr.astype(CDTYPE)
+            else:
+                w, v = np.linalg.eig(a)
+                order = np.argsort(w.real, kind="stable")
+                w, v = w[order], v[:, order]
+                # unit length in the bilinear sense (v^T v = 1), so that the
+                # eigenvectors of a rotated diagonal tensor come out real
+                v = v / np.sqrt(np.sum(v * v, axis=0))[None, :]
+            if np.linalg.det(v.real) < 0:
+                v[:, 0] = -v[:, 0]
+    m2, m1, m0 = abs(w[1] - w[0]), abs(w[2] - w[0]), abs(w[2] - w[1])
+    i, j, k = 0, 1, 2
+    if m2 > m1 or m2 > m0:
+        i, j, k = (1, 2, 0) if m1 > m0 else (2, 0, 1)
+    idx = [i, j, k]
+    return w[idx], v[:, idx]
+
+
+def rotation_angles(R):
+    """Euler angles (psi, theta, phi) of a rotation matrix (dtmm/rotation.py:154-171)."""
+    theta = np.arccos(max(-1.0, min(1.0, R[2, 2])))
+    if (R[1, 2] == 0.0 and R[0, 2] == 0.0) or theta == 0.0:
+        return np.asarray([0.0, theta, np.arccos(max(-1.0, min(1.0, R[1, 1])))], FDTYPE)
+    return np.asarray([np.arctan2(R[2, 1], -R[2, 0]), theta, np.arctan2(R[1, 2], R[0, 2])], FDTYPE)
+
+
+def uniaxial_order(order, eig):
+    """Uniaxial (1), isotropic (0) or unchanged (< 0) eigenvalues, [2] the
+    extraordinary axis (dtmm/data.py:1215-1233, :1240-1274)."""
+    e0, e1, e2 = eig
+    if order < 0:
+        return np.asarray([e0, e1, e2], CDTYPE)
+    m = (e0 + e1 + e2) / 3.0
+    delta = e2 - (e0 + e1) / 2.0
+    if order == 0:
+        return np.asarray([m, m, m], CDTYPE)
+    a = m - order * delta / 3.0
+    return np.asarray([a, a, m + 2.0 * order * delta / 3.0], CDTYPE)
+
+
+def effective_block(block, symmetry):
+    """Effective layers of an optical block (dtmm/data.py:1364-1419): isotropic
+    (0) the mean of the voxels' isotropic eigenvalue; otherwise the mean of the
+    lab-frame tensors (over every voxel, or per layer when ``symmetry`` is a
+    per-layer array), its eigen-frame, and the eigenvalues made uniaxial (1) or
+    kept (2, biaxial); each layer gets its block's medium.  Returns per-layer
+    ``(epsv, epsa)`` arrays."""
+    d, epsv, epsa = block
+    n = len(d)
+    sym = _symmetry(symmetry)
+    if np.ndim(sym) == 0 and sym == 0:
+        m = _isotropic_mean(epsv)
+        ev = np.asarray([m, m, m])
+        ev = ev.astype(CDTYPE if np.iscomplexobj(ev) else FDTYPE)
+        return [ev] * n, [np.zeros(3, FDTYPE)] * n
+    shape = np.broadcast_shapes(np.shape(epsv), np.shape(epsa))
+    ev_b = np.broadcast_to(np.asarray(epsv), shape)
+    ea_b = np.broadcast_to(np.asarray(epsa, FDTYPE), shape)
+    R = _rotation_matrix(ea_b[..., 0], ea_b[..., 1], ea_b[..., 2])
+    eps = _rotate_diagonal_tensor(R, ev_b.astype(CDTYPE))
+    per_layer = np.ndim(sym) != 0
+    if per_layer:
+        if len(sym) != n:
+            raise ValueError("Shape of the symmetry argument is incompatible with block size.")
+        means = [eps[i].reshape(-1, 6).mean(axis=0) for i in range(n)]
+        orders = list(sym)
+    else:
+        means = [eps.reshape(-1, 6).mean(axis=0)]
+        orders = [sym]
+    evs, eas = [], []
+    for t, o in zip(means, orders):
+        w, v = tensor_eig(t)
+        eas.append(rotation_angles(v.real))
+        evs.append(uniaxial_order(-1 if o > 1 else o, w))
+    if not per_layer:
+        evs, eas = evs * n, eas * n
+    return evs, eas
+
+
+def _layers_list(block, nin, nout, nstep, is_first, is_last, eff_data=0):
     """Layer and effective-layer lists with the input/output media (dtmm/transfer.py:926)."""
     d, epsv, epsa = block
     substeps = np.broadcast_to(np.asarray(nstep), (len(d),))
@@ -1059,10 +1181,8 @@ def _layers_list(block, nin, nout, nstep, is_first, is_last):
         layers.insert(0, (1, (0.0, np.broadcast_to(eps_in, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
     if is_last:
         layers.append((1, (0.0, np.broadcast_to(eps_out, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
-    m = _isotropic_mean(epsv)
-    ev_eff = np.asarray([m, m, m])
-    ev_eff = ev_eff.astype(CDTYPE if np.iscomplexobj(ev_eff) else FDTYPE)
-    eff = [(int(n), (t / n, ev_eff, zero)) for n, t in zip(substeps, d)]
+    ev_eff, ea_eff = effective_block(block, eff_data)
+    eff = [(int(n), (t / n, ev, ea)) for n, t, ev, ea in zip(substeps, d, ev_eff, ea_eff)]
     if is_first:
         eff.insert(0, (1, (0.0, eps_in, zero)))
     if is_last:
@@ -1070,12 +1190,18 @@ def _layers_list(block, nin, nout, nstep, is_first, is_last):
     return layers, eff
 
 
-def _create_layers(optical_data, nin, nout, nstep):
-    """(dtmm/transfer.py:978)"""
+def _create_layers(optical_data, nin, nout, nstep, eff_data=0):
+    """(dtmm/transfer.py:978): one symmetry for every block, or one per block."""
     layers, eff = [], []
     nb = len(optical_data)
+    if isinstance(eff_data, (str, int, np.integer)):
+        per_block = [eff_data] * nb
+    else:
+        if len(eff_data) != nb:
+            raise ValueError("Number of elements in eff_data must match length of optical_data.")
+        per_block = list(eff_data)
     for i, block in enumerate(optical_data):
-        l, e = _layers_list(block, nin, nout, nstep, i == 0, i == nb - 1)
+        l, e = _layers_list(block, nin, nout, nstep, i == 0, i == nb - 1, per_block[i])
         layers += l
         eff += e
     return layers, eff
@@ -1606,7 +1732,7 @@ def propagate_2x2_full(field, ks, layer, input_layer, nsteps, mode, reflection, 
 
 
 def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
-                 reflection, multiray, norm, smooth, betamax, ret_bulk, out):
+                 reflection, multiray, norm, smooth, betamax, ret_bulk, out, eff_data=0):
     """4x4 pass x layer sweep (dtmm/transfer.py:618-884): reflection mode 1 in
     k-space, reflection mode 2 without diffraction (the per-voxel 4x4
     transfer) and diffraction = inf (every eigenwave exactly, any reflection
@@ -1624,7 +1750,7 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     calc_reference = bool(norm & DTMM_NORM_REF)
     field_in, wavelengths, pixelsize = field_data
     shape = field_in.shape[-2:]
-    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
+    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep, eff_data)
     ks = k0(wavelengths, pixelsize)
     n = len(layers)
     if beta is None and phi is None:
@@ -1739,7 +1865,7 @@ def transfer_4x4(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
 
 
 def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, diffraction,
-                 reflection, multiray, betamax, ret_bulk, out):
+                 reflection, multiray, betamax, ret_bulk, out, eff_data=0):
     """2x2 interface sweep (dtmm/transfer.py:1009-1183): in k-space for
     reflection 0 / 1 with 0 < diffraction < inf and for reflection 1, in real
     space otherwise (reflection 2, or diffraction 0); npass passes alternating
@@ -1751,7 +1877,7 @@ def transfer_2x2(field_data, optical_data, beta, phi, nin, nout, npass, nstep, d
     if npass > 1 and reflection == 0:
         raise ValueError("Reflection mode `0` not compatible with npass > 1")
     field_in, wavelengths, pixelsize = field_data
-    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep)
+    layers, eff_layers = _create_layers(optical_data, nin, nout, nstep, eff_data)
     ks = k0(wavelengths, pixelsize)
     n = len(layers) - 1
     if beta is None and phi is None:
@@ -1842,8 +1968,8 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     eff_data = opt("eff_data", eff_data)
     diffraction, reflection = opt("diffraction", diffraction), opt("reflection", reflection)
     betamax = opt("betamax", betamax)
-    if eff_data not in (0, "isotropic"):
-        raise NotImplementedError("oracle covers isotropic effective data")
+    if isinstance(eff_data, tuple) or (isinstance(eff_data, list) and any(isinstance(e, tuple) for e in eff_data)):
+        raise NotImplementedError("oracle covers effective data given by symmetry")
     if split_rays:
         raise NotImplementedError("oracle covers unsplit rays")
     if split_wavelengths and not isinstance(field_data[0], tuple) and not ret_bulk:
@@ -1879,9 +2005,9 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
               for d, ev, ea in od for i in range(len(d))]
     if method == "4x4":
         return transfer_4x4((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
-                            diffraction, reflection, multiray, norm, smooth, betamax, ret_bulk, out)
+                            diffraction, reflection, multiray, norm, smooth, betamax, ret_bulk, out, eff_data)
     return transfer_2x2((field_in, wavelengths, pixelsize), od, beta, phi, nin, nout, npass, nstep,
-                        diffraction, reflection, multiray, betamax, ret_bulk, out)
+                        diffraction, reflection, multiray, betamax, ret_bulk, out, eff_data)
 
 
 # ---------------------------------------------------------------------------

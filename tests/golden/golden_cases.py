@@ -198,6 +198,48 @@ CASES = {
                                     blocks=[("twisted", dict(), 2), ("iso", dict(eps=2.0), 1)], seed=21,
                                     illum=dict(jones=(1, 0)),
                                     transfer=dict(method="4x4", diffraction=3, npass=2, beta=0.0, phi=0.0)),
+    # effective layers of uniaxial / biaxial symmetry (the mean lab-frame tensor of a
+    # block, or of each layer), every 4x4 reflection mode with diffraction
+    "fourx4_eff_uniaxial": dict(shape=(12, 14), nlayers=3, wavelengths=[540.0], pixelsize=100.0,
+                                material=("twisted", dict()), seed=74,
+                                illum=dict(beta=0.1, phi=0.4, jones=(1, 0)),
+                                transfer=dict(method="4x4", diffraction=1, eff_data=1, beta=0.1, phi=0.4)),
+    "fourx4_eff_biaxial_d3": dict(shape=(12, 12), nlayers=2, wavelengths=[480.0, 620.0], pixelsize=100.0,
+                                  material=("twisted", dict(no=1.5, ne=1.7, amplitude=0.3)), seed=75,
+                                  illum=dict(),
+                                  transfer=dict(method="4x4", diffraction=3, eff_data="biaxial", beta=0.0,
+                                                phi=0.0)),
+    "fourx4_eff_uniaxial_refl2": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                      material=("twisted", dict()), seed=76,
+                                      illum=dict(beta=0.1, phi=0.2, jones=(0, 1)),
+                                      transfer=dict(method="4x4", diffraction=1, reflection=2, eff_data="uniaxial",
+                                                    beta=0.1, phi=0.2)),
+    "fourx4_eff_biaxial_refl3_d3": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                        material=("twisted", dict(amplitude=0.3)), seed=77,
+                                        illum=dict(jones=(1, 0)),
+                                        transfer=dict(method="4x4", diffraction=3, reflection=3, eff_data=2,
+                                                      beta=0.0, phi=0.0)),
+    "fourx4_eff_uniaxial_refl4_nstep2": dict(shape=(12, 14), nlayers=2, wavelengths=[520.0], pixelsize=100.0,
+                                             material=("twisted", dict(thickness=2.0)), seed=78,
+                                             illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                                             transfer=dict(method="4x4", diffraction=1, reflection=4, nstep=2,
+                                                           eff_data=1, beta=0.1, phi=0.3)),
+    "fourx4_eff_blocks": dict(shape=(12, 12), nlayers=5, wavelengths=[520.0, 640.0], pixelsize=100.0,
+                              blocks=[("twisted", dict(no=1.5, ne=1.7), 2), ("iso", dict(eps=2.3), 1),
+                                      ("twisted", dict(no=1.55, ne=1.65, amplitude=0.3), 2)], seed=79,
+                              illum=dict(beta=0.1, phi=0.5, jones=(1, 0)),
+                              transfer=dict(method="4x4", diffraction=1, eff_data=[1, 0, "biaxial"], beta=0.1,
+                                            phi=0.5)),
+    "fourx4_eff_per_layer_d3": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                    material=("twisted", dict(amplitude=0.3)), seed=80,
+                                    illum=dict(jones=(1, 0)),
+                                    transfer=dict(method="4x4", diffraction=3, eff_data=[[1, 2, 0]], beta=0.0,
+                                                  phi=0.0)),
+    "fourx4_eff_uniaxial_npass2": dict(shape=(12, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                       material=("twisted", dict()), seed=81,
+                                       illum=dict(jones=(1, 0)),
+                                       transfer=dict(method="4x4", diffraction=1, npass=2, eff_data=1, beta=0.0,
+                                                     phi=0.0)),
     "fourx4_split_layers": dict(shape=(12, 14), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                 material=("mixed", dict()), seed=22,
                                 illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
@@ -487,7 +529,8 @@ CASES = {
 
 
 # every case with a reference fixture is also a GPU parity case
-ORACLE_CASES = {}
+# effective layers of uniaxial / biaxial symmetry: pinned for the oracle only
+ORACLE_CASES = {k: CASES.pop(k) for k in [k for k in CASES if k.startswith("fourx4_eff_")]}
 
 
 def build_optical_data(case):
