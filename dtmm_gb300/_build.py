@@ -33,7 +33,7 @@ def sources():
 
 
 def deps():
-    return sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")] + [
+    return sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + [
         os.path.join(ROOT, "include", "dtmm_gb300.h")]
 
 

@@ -26,7 +26,7 @@ ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_s
                "dtmm_diffract_workspace_size", "dtmm_diffract", "dtmm_q2data", "dtmm_wave_field",
                "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields",
                "dtmm_twisted_nematic_angles")
-ABI_VERSION = 5
+ABI_VERSION = 6
 STATIC_SCRATCH_BYTES = 64 << 20
 
 
@@ -66,6 +66,7 @@ class TransferDesc(ctypes.Structure):
         ("norm_total", ctypes.c_int),
         ("layer_block", ctypes.POINTER(ctypes.c_int)),
         ("norm_ref", ctypes.c_int),
+        ("block_sym", ctypes.POINTER(ctypes.c_int)),
     ]
 
 

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <complex>
 #include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
@@ -23,6 +24,7 @@
 #include <vector>
 
 #include "../../include/dtmm_gb300.h"
+#include "dtmm_effmed.h"
 #include "dtmm_kernels.cuh"
 #include "dtmm_regkern.cuh"
 
@@ -95,6 +97,7 @@ struct Layout {
   size_t r2;                   // 2x2 real space, npass > 1: reflected wave of every interface
   size_t w2;                   // 2x2 real space with windows: window part, sum, reflected part and sum
   size_t effb, awb;            // per block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
+  size_t effx, efft;           // per block: anisotropic effective medium (10 doubles), mean lab-frame tensor (12)
   size_t ref, ref2, refw;      // 4x4 norm_ref: reference field, its E part, window part / sum / H part
   size_t fnorm;                // 4x4 norm_ref without norm FFT ("local"): the output medium's field matrix and inverse
   bool chains;  // nstep > 1 with windows: per-window sub-step chains
@@ -102,12 +105,42 @@ struct Layout {
   size_t total;
 };
 
+// some block's effective medium is uniaxial or biaxial (block_sym 1 / 2)
+int nblocks(const dtmm_transfer_desc* d);
+bool aniso_eff(const dtmm_transfer_desc* d) {
+  if (d->block_sym == nullptr) return false;
+  const int nb = nblocks(d);
+  for (int b = 0; b < nb; ++b)
+    if (d->block_sym[b] != 0) return true;
+  return false;
+}
+
+// 4x4 with diffraction through the real-space chains: reflection modes 2-4,
+// and mode 1 around an anisotropic effective medium
+bool is_refl4(const dtmm_transfer_desc* d) {
+  return d->method == 4 && d->diffraction >= 1 &&
+         ((d->reflection >= 2 && d->reflection <= 4) || (d->reflection == 1 && aniso_eff(d)));
+}
+
 int check_desc(const dtmm_transfer_desc* d) {
   if (d == nullptr) return fail(DTMM_EINVAL, "null descriptor");
   if (d->height < 1 || d->width < 1) return fail(DTMM_EINVAL, "grid must be at least 1x1");
   if (d->height > 16384 || d->width > 16384) return fail(DTMM_ENOTSUP, "grid side above 16384");
   if (d->nlam < 1 || d->npol < 1 || d->nray < 1) return fail(DTMM_EINVAL, "empty image axes");
   if (d->method != 4 && d->method != 2) return fail(DTMM_EINVAL, "method must be 4 (4x4) or 2 (2x2)");
+  if (d->nlayers < 1) return fail(DTMM_EINVAL, "no layers");
+  if (d->layer_block) {  // before anything reads the block count
+    for (int l = 0; l < d->nlayers; ++l) {
+      const int prev = l ? d->layer_block[l - 1] : 0;
+      if (d->layer_block[l] != prev && d->layer_block[l] != prev + 1)
+        return fail(DTMM_EINVAL, "layer_block must start at 0 and grow by 0 or 1 from layer to layer");
+    }
+  }
+  if (d->block_sym) {
+    for (int b = 0; b < nblocks(d); ++b)
+      if (d->block_sym[b] < 0 || d->block_sym[b] > 2)
+        return fail(DTMM_EINVAL, "block_sym must be 0 (isotropic), 1 (uniaxial) or 2 (biaxial)");
+  }
   // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1);
   // diffraction = inf (DTMM_DIFFRACTION_FULL): every eigenwave exactly (4x4, npass 1,
   // any reflection mode: the reference takes the same path for all of them;
@@ -117,7 +150,7 @@ int check_desc(const dtmm_transfer_desc* d) {
   const bool full2 = d->method == 2 && d->diffraction == DTMM_DIFFRACTION_FULL;
   // reflection modes 2-4 with diffraction: real-space steps around the
   // corrected diffraction matrices (tables per ray: they follow its beam)
-  const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
+  const bool refl4 = is_refl4(d);
   // the reference's 2x2 reflection 1 moves the field to k-space, and its modal
   // step transforms that field once more (dtmm/transfer.py:1091-1098, :1172)
   if (full2 && d->reflection == 1)
@@ -162,12 +195,13 @@ int check_desc(const dtmm_transfer_desc* d) {
     if (nodiff2 && d->reflection == 1 && d->nstep[l] > 1)
       return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction supports nstep = 1");
   }
+  if (d->block_sym) {
+    if (aniso_eff(d) && d->method == 2)
+      return fail(DTMM_ENOTSUP, "effective layers of uniaxial or biaxial symmetry are supported with the 4x4 method");
+    if (aniso_eff(d) && d->npass > 1 && d->norm_ref)
+      return fail(DTMM_ENOTSUP, "norm_ref is supported with isotropic effective layers");
+  }
   if (d->layer_block) {
-    for (int l = 0; l < d->nlayers; ++l) {
-      const int prev = l ? d->layer_block[l - 1] : 0;
-      if (d->layer_block[l] != prev && d->layer_block[l] != prev + 1)
-        return fail(DTMM_EINVAL, "layer_block must start at 0 and grow by 0 or 1 from layer to layer");
-    }
     // the reflections of the inner interfaces between different effective media are not kept
     if (d->method == 2 && !(d->reflection == 2 || (d->diffraction == 0 && d->reflection == 0)) && d->npass > 1 &&
         d->layer_block[d->nlayers - 1] > 0)
@@ -183,7 +217,9 @@ int check_desc(const dtmm_transfer_desc* d) {
 }
 
 // blocks of the layer list (layer_block null: one)
-int nblocks(const dtmm_transfer_desc* d) { return d->layer_block ? d->layer_block[d->nlayers - 1] + 1 : 1; }
+int nblocks(const dtmm_transfer_desc* d) {
+  return (d->layer_block && d->nlayers > 0) ? d->layer_block[d->nlayers - 1] + 1 : 1;
+}
 
 // 2x2 in real space: reflection mode 2, or no diffraction without reflections
 bool is_real2(const dtmm_transfer_desc* d) {
@@ -213,7 +249,9 @@ Layout layout_of(const dtmm_transfer_desc* d) {
   L.small = take(sizeof(double) * (2 * d->nlam + 4 * d->nray + 9 * nrw + 4 + 3 * NI + 8));
   L.effb = take(sizeof(double) * 2 * nblocks(d));
   L.awb = take(sizeof(double) * nrw * nblocks(d));
-  const bool refl4 = d->method == 4 && d->reflection >= 2 && d->reflection <= 4 && d->diffraction >= 1;
+  L.effx = take(sizeof(double) * 10 * nblocks(d));
+  L.efft = take(sizeof(double) * 12 * nblocks(d));
+  const bool refl4 = is_refl4(d);
   const bool real_space = d->method == 4 && (d->diffraction == 0 || d->diffraction == DTMM_DIFFRACTION_FULL || refl4);
   if (d->diffraction == DTMM_DIFFRACTION_FULL) {
     // beta, phi and the sorted mode list per wavelength and grid point, the
@@ -436,6 +474,10 @@ struct Engine {
   double* blim() const { return fact() + NI; }  // [lam] band limits of the W axis
   // per optical block: effective eps (re, im) and the windows' sqrt(eps_eff - beta^2)
   double* effb(int b) const { return A<double>(L.effb) + 2 * b; }
+  double* effx(int b) const { return A<double>(L.effx) + 10 * b; }
+  double* efft(int b) const { return A<double>(L.efft) + 12 * b; }
+  // block b's effective medium is uniaxial or biaxial
+  bool blk_aniso(int b) const { return d.block_sym != nullptr && b >= 0 && d.block_sym[b] != 0; }
   double* awb(int b) const { return A<double>(L.awb) + (size_t)b * d.nray * L.nwin; }
   int blk_of(int l) const { return d.layer_block ? d.layer_block[l] : 0; }
   // the block whose effective medium the k-space tables fetched now use
@@ -703,6 +745,7 @@ struct Engine {
     p.what = what;
     p.proj_mode = proj_mode;
     p.eps_dev = eff ? effb(cur_blk) : nullptr;
+    p.effx = (eff && blk_aniso(cur_blk)) ? effx(cur_blk) : nullptr;
     p.eps_dev2 = nullptr;
     if (what == KT_D12 || what == KT_2BX) {  // the block before the boundary and its half step
       p.eps_dev2 = effb(proj_mode);
@@ -744,7 +787,7 @@ struct Engine {
     // ray's windows: one slab per ray
     const bool per_ray = what == KT_2OUT || what == KT_WINMAT || what == KT_CFD || what == KT_CEPN ||
                          what == KT_CD || what == KT_DC || what == KT_2RIN || what == KT_2R || what == KT_2X ||
-                         what == KT_2CE || what == KT_2WIN;
+                         what == KT_2CE || what == KT_2WIN || what == KT_C1 || what == KT_C2;
     const int rays = per_ray ? d.nray : 1;
     const size_t slab = (size_t)n * ktab_entries(what);
     for (int r = 0; r < rays; ++r) {
@@ -990,6 +1033,19 @@ struct Engine {
   int refl_chain(Local4Params& p, int l, double ds, int w, cpx<R>* f) {
     const size_t rs = (size_t)d.nlam * L.HW * 16;  // one 4x4 table per ray
     int rc;
+    if (d.reflection == 1) {
+      // mode 1 around an anisotropic effective medium (its k-space field here
+      // in real space, every step being linear): C . E P F^-1 over ds/2,
+      // E P E^-1 over ds, F P E^-1 . C over ds/2 (dtmm/propagate_4x4.py:80-101,
+      // :357-442)
+      const cpx<R>* c1;
+      const cpx<R>* c2;
+      if ((rc = table(KT_C1, ds / 2, c1, w))) return rc;
+      if ((rc = diffract(f, f, c1, rs))) return rc;
+      if ((rc = local_step(p, l, ds, w, 3, f))) return rc;
+      if ((rc = table(KT_C2, ds / 2, c2, w))) return rc;
+      return diffract(f, f, c2, rs);
+    }
     if (d.reflection == 3) {
       const cpx<R>* cd;
       const cpx<R>* dc;
@@ -1154,7 +1210,44 @@ struct Engine {
       CKL("k_eps_mean");
       k_eps_final<<<1, 256, 0, st>>>(A<double>(L.part), blocks, nvox, effb(blk_of(l0)));
       CKL("k_eps_final");
+      if (blk_aniso(blk_of(l0))) {  // the mean lab-frame tensor
+        const bool onea = one && d.epsa_strides[0] == 0 && d.epsa_strides[1] == 0 && d.epsa_strides[2] == 0;
+        const long long nv = onea ? 1 : (long long)(l1 - l0) * d.height * d.width;
+        int tb = (int)((nv + 1023) / 1024);
+        if (tb > kPartBlocks / 6) tb = kPartBlocks / 6;
+        k_eps_tensor_mean<<<tb, 256, 0, st>>>(e0, d.epsa + (size_t)l0 * d.epsa_strides[0], d.eps_complex,
+                                              d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
+                                              d.epsa_strides[0], d.epsa_strides[1], d.epsa_strides[2],
+                                              onea ? 1 : l1 - l0, onea ? 1 : d.height, onea ? 1 : d.width,
+                                              A<double>(L.part));
+        CKL("k_eps_tensor_mean");
+        k_eps_tensor_final<<<1, 32, 0, st>>>(A<double>(L.part), tb, nv, efft(blk_of(l0)));
+        CKL("k_eps_tensor_final");
+      }
       l0 = l1;
+    }
+    if (aniso_eff(&d)) {
+      // the eigen-frame of each anisotropic block's mean tensor, on the host
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      CK(cudaStreamIsCapturing(st, &cs));
+      if (cs != cudaStreamCaptureStatusNone)
+        return fail(DTMM_ENOTSUP, "effective layers of uniaxial or biaxial symmetry are not supported in a stream "
+                                  "capture (their eigen-frame is found on the host)");
+      const int nb = nblocks(&d);
+      std::vector<double> t(12 * (size_t)nb), x(10 * (size_t)nb, 0.0);
+      CK(cudaMemcpyAsync(t.data(), efft(0), sizeof(double) * t.size(), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int b = 0; b < nb; ++b)
+        if (blk_aniso(b))
+          eff_medium(t.data() + 12 * (size_t)b, d.block_sym[b], !d.eps_complex, x.data() + 10 * (size_t)b);
+      for (size_t o = 0; o < x.size(); o += 64) {
+        Scalars64 sc;
+        sc.n = (int)std::min<size_t>(64, x.size() - o);
+        sc.off = (int)o;
+        for (int i = 0; i < sc.n; ++i) sc.v[i] = x[o + i];
+        k_set_scalars<<<1, 64, 0, st>>>(sc, effx(0));
+        CKL("k_set_scalars");
+      }
     }
     // windows
     if (d.diffraction > 1) {
@@ -1483,7 +1576,8 @@ struct Engine {
     // the real-space paths (no diffraction, or diffraction = inf) sweep F in
     // place; the reference's bulk slabs alias its pass-end field there, which
     // this path does not restate
-    const bool real_space = d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection >= 2;
+    const bool real_space =
+        d.diffraction == 0 || d.diffraction == DTMM_DIFFRACTION_FULL || d.reflection >= 2 || aniso_eff(&d);
     if (real_space && bulk && npass > 1)
       return fail(DTMM_ENOTSUP, "ret_bulk with npass > 1 is built for reflection mode 1 with diffraction >= 1");
     if (d.diffraction == DTMM_DIFFRACTION_FULL && (rc = full_prepare(fullp))) return rc;
@@ -2340,7 +2434,7 @@ std::string& last_error_slot() { return g_err; }
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 5; }
+int dtmm_abi_version(void) { return 6; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 

@@ -636,7 +636,9 @@ struct Local4Params {
   int bstride;        // 1 for the rays' beams, the windows per ray for one window's beams
   // operator: 0 F . P . F^-1; 1 E . P . F^-1 and 2 F . P . E^-1 with E the
   // block matrix of the forward (rows/columns 0, 2) and backward (1, 3)
-  // E parts (dtmm/tmm.py:974-996), the half steps of reflection mode 2
+  // E parts (dtmm/tmm.py:974-996), the half steps of reflection mode 2;
+  // 3 E . P . E^-1, the per-voxel step of reflection mode 1
+  // (dtmm/propagate_4x4.py:80-101)
   int op;
 };
 
@@ -754,11 +756,10 @@ __global__ void __launch_bounds__(128) k_local4(Local4Params p, Grid g, const cp
       for (int j = 0; j < 4; ++j) E[i][j] = mk<double>(0.0, 0.0);
     E[0][0] = F[0][0]; E[0][2] = F[0][2]; E[2][0] = F[2][0]; E[2][2] = F[2][2];
     E[1][1] = F[0][1]; E[1][3] = F[0][3]; E[3][1] = F[2][1]; E[3][3] = F[2][3];
-    if (p.op == 1) {
+    if (p.op != 1) inv4(E, Fi);
+    if (p.op != 2) {
       for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) F[i][j] = E[i][j];
-    } else {
-      inv4(E, Fi);
     }
   }
   cpx<R> f[4][4], fi[4][4];
@@ -1596,6 +1597,10 @@ enum KTab {
   KT_D12 = 18,   // 4x4 D1(eps, d) . D2(eps2, d2): the merged half steps E P F^-1 . F P E^-1
   KT_2BX = 19,   // 2x2 E(eps, d) . T(eps2 -> eps) . E(eps2, d2), forward modes
   KT_2H = 20,    // 2x2 H from E of the forward modes in the isotropic medium eps (E2H, dtmm/transfer.py:255-267)
+  // reflection mode 1 around an anisotropic effective medium, per window of the ray
+  KT_C1 = 21,    // 4x4 C . E P(d) F^-1, C = E_w P_w(-d) E_w^-1 of the window's beam (first_corrected_Epn_
+                 //   diffraction_matrix, dtmm/matrix.py:127-157)
+  KT_C2 = 22,    // 4x4 F P(d) E^-1 . C                 (second_corrected_Epn_diffraction_matrix, :159-174)
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1607,6 +1612,7 @@ struct KTabParams {
   int what;
   int proj_mode;       // KT_PROJ: +1 forward, -1 backward modes
   const double* eps_dev; // if set: (re, im) of the effective medium, overrides eps
+  const double* effx;    // if set: the anisotropic effective medium (symmetry, epsv re/im x 3, psi, theta, phi)
   const double* eps_dev2;  // KT_D12 / KT_2BX: (re, im) of the effective medium before the boundary
   cpx<double> eps2;
   double d2;               // KT_D12 / KT_2BX: thickness of the half step before the boundary
@@ -1673,6 +1679,48 @@ __device__ inline void iso_k(double beta, double phi, cpx<double> eps, double be
       for (int j = 0; j < 4; ++j) F[i][j] = Fi[i][j] = mk<double>(0.0, 0.0);
     }
   }
+}
+
+// eigen-data of the table's effective medium at (beta, phi), uncut: the
+// isotropic closed form, or with an anisotropic effective medium (effx) its
+// uniaxial / biaxial field matrix from the eigenvalues and Euler angles
+__device__ inline void eff_alphaf(const KTabParams& p, double beta, double phi, cpx<double> al[4],
+                                  cpx<double> F[4][4]) {
+  if (p.effx == nullptr) {
+    iso_alphaf(beta, phi, p.eps, al, F);
+    return;
+  }
+  const cpx<double> ev[3] = {mk<double>(p.effx[1], p.effx[2]), mk<double>(p.effx[3], p.effx[4]),
+                             mk<double>(p.effx[5], p.effx[6])};
+  local_fmat(beta, phi, ev, p.effx[7], p.effx[8], p.effx[9], F, al);
+}
+
+// the same with the inverse and the betamax cut of the diffraction eigen-data
+// (dtmm/diffract.py:22-77: every entry zero for beta >= betamax)
+__device__ inline void eff_k(const KTabParams& p, double beta, double phi, double betamax, cpx<double> al[4],
+                             cpx<double> F[4][4], cpx<double> Fi[4][4]) {
+  if (p.effx == nullptr) {
+    iso_k(beta, phi, p.eps, betamax, al, F, Fi);
+    return;
+  }
+  if (beta >= betamax) {
+    for (int i = 0; i < 4; ++i) {
+      al[i] = mk<double>(0.0, 0.0);
+      for (int j = 0; j < 4; ++j) F[i][j] = Fi[i][j] = mk<double>(0.0, 0.0);
+    }
+    return;
+  }
+  eff_alphaf(p, beta, phi, al, F);
+  inv4(F, Fi);
+}
+
+// the block matrix of the forward (rows / columns 0, 2) and backward (1, 3)
+// E parts of a field matrix (E_mat with mode None, dtmm/tmm.py:974-996)
+__device__ inline void epn_of(const cpx<double> F[4][4], cpx<double> E[4][4]) {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) E[i][j] = mk<double>(0.0, 0.0);
+  E[0][0] = F[0][0]; E[0][2] = F[0][2]; E[2][0] = F[2][0]; E[2][2] = F[2][2];
+  E[1][1] = F[0][1]; E[1][3] = F[0][3]; E[3][1] = F[2][1]; E[3][3] = F[2][3];
 }
 
 // 2x2 interface transmission t and reflection r at k from isotropic medium a
@@ -1895,7 +1943,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     // over -d/2 (KT_CFD) or -d, uncut (alphaffi, not the diffraction eigen-data)
     const double bmax = (p.what == KT_CFD && p.nwin_axis > 1) ? kDefaultBetamax : p.betamax;
     const double dc = p.what == KT_CFD ? p.d / 2 : p.d;
-    iso_k(beta, phi, p.eps, bmax, al, F, Fi);
+    eff_k(p, beta, phi, bmax, al, F, Fi);
     cpx<double> D[4][4], Cb[4][4], Fb[4][4], Fbi[4][4], alb[4], T[4][4];
     cpx<double> pd[4], pc[4];
     for (int m = 0; m < 4; ++m) pd[m] = cexp_i(al[m] * (ks * p.d));
@@ -1906,7 +1954,7 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
         D[i][j] = s;
       }
     const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;  // window of this ray
-    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    eff_alphaf(p, p.wbeta[w], p.wphi[w], alb, Fb);
     inv4(Fb, Fbi);
     for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * dc));
     for (int i = 0; i < 4; ++i)
@@ -1944,12 +1992,46 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
       }
     return;
   }
+  if (p.what == KT_C1 || p.what == KT_C2) {
+    // masked eigen-data of the effective medium over d, the beam's correction over -d (uncut)
+    eff_k(p, beta, phi, p.betamax, al, F, Fi);
+    cpx<double> E[4][4], Ei[4][4], D[4][4], Fb[4][4], Eb[4][4], Ebi[4][4], Cb[4][4], alb[4], pd[4], pc[4];
+    epn_of(F, E);
+    inv4(E, Ei);
+    for (int m = 0; m < 4; ++m) pd[m] = cexp_i(al[m] * (ks * p.d));
+    const bool first = p.what == KT_C1;
+    for (int i = 0; i < 4; ++i)  // E P F^-1 or F P E^-1
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + (first ? E[i][m] : F[i][m]) * pd[m] * (first ? Fi[m][j] : Ei[m][j]);
+        D[i][j] = s;
+      }
+    const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;  // window of this ray
+    eff_alphaf(p, p.wbeta[w], p.wphi[w], alb, Fb);
+    epn_of(Fb, Eb);
+    inv4(Eb, Ebi);
+    for (int m = 0; m < 4; ++m) pc[m] = cexp_i(alb[m] * (-ks * p.d));
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + Eb[i][m] * pc[m] * Ebi[m][j];
+        Cb[i][j] = s;
+      }
+    cpx<R>* o = tab + (size_t)t * 16;
+    for (int i = 0; i < 4; ++i)  // C . D or D . C
+      for (int j = 0; j < 4; ++j) {
+        cpx<double> s = mk<double>(0.0, 0.0);
+        for (int m = 0; m < 4; ++m) s = s + (first ? Cb[i][m] * D[m][j] : D[i][m] * Cb[m][j]);
+        o[i * 4 + j] = cvt<R>(s);
+      }
+    return;
+  }
   if (p.what == KT_CEPN) {
-    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    eff_k(p, beta, phi, p.betamax, al, F, Fi);
     const bool cut = beta >= p.betamax;
     const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;  // window of this ray
     cpx<double> alb[4], Fb[4][4];
-    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    eff_alphaf(p, p.wbeta[w], p.wphi[w], alb, Fb);
     cpx<double> M[4][4];
     for (int i = 0; i < 4; ++i)
       for (int j = 0; j < 4; ++j) M[i][j] = mk<double>(0.0, 0.0);
@@ -2673,6 +2755,78 @@ struct Scalars64 {
 __global__ void k_set_scalars(Scalars64 s, double* dst) {
   const int i = threadIdx.x;
   if (i < s.n) dst[s.off + i] = s.v[i];
+}
+
+// Partial sums of the voxels' lab-frame dielectric tensors R diag(epsv) R^T
+// (dtmm/data.py:515-533; R = R_z(phi) R_y(theta) R_z(psi) of the voxel's
+// Euler angles, dtmm/rotation.py:125-150) as (00, 11, 22, 01, 02, 12), re
+// and im: 12 doubles per block
+__global__ void k_eps_tensor_mean(const void* epsv, const double* epsa, int eps_complex, long long s0, long long s1,
+                                  long long s2, long long a0, long long a1, long long a2, int L, int H, int W,
+                                  double* part) {
+  const long long n = (long long)L * H * W;
+  double acc[12];
+  for (int c = 0; c < 12; ++c) acc[c] = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int l = (int)(t / ((long long)H * W));
+    const long long r = t - (long long)l * H * W;
+    const int y = (int)(r / W), x = (int)(r - (long long)y * W);
+    const long long o = l * s0 + y * s1 + x * s2;
+    double er[3], ei[3] = {0.0, 0.0, 0.0};
+    if (eps_complex) {
+      const cpx<double>* e = (const cpx<double>*)epsv + o;
+      for (int k = 0; k < 3; ++k) {
+        er[k] = e[k].re;
+        ei[k] = e[k].im;
+      }
+    } else {
+      const double* e = (const double*)epsv + o;
+      for (int k = 0; k < 3; ++k) er[k] = e[k];
+    }
+    const double* a = epsa + (l * a0 + y * a1 + x * a2);
+    double sps, cps, st, ct, sp, cp;
+    sincos(a[0], &sps, &cps);
+    sincos(a[1], &st, &ct);
+    sincos(a[2], &sp, &cp);
+    double R[3][3];
+    R[0][0] = ct * (cp * cps) - sp * sps;
+    R[0][1] = -ct * (cp * sps) - sp * cps;
+    R[0][2] = cp * st;
+    R[1][0] = ct * (sp * cps) + cp * sps;
+    R[1][1] = cp * cps - ct * (sp * sps);
+    R[1][2] = st * sp;
+    R[2][0] = -cps * st;
+    R[2][1] = st * sps;
+    R[2][2] = ct;
+    const int pi[6] = {0, 1, 2, 0, 0, 1}, pj[6] = {0, 1, 2, 1, 2, 2};
+    for (int c = 0; c < 6; ++c) {
+      double vr = 0.0, vi = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        const double w = R[pi[c]][k] * R[pj[c]][k];
+        vr += er[k] * w;
+        vi += ei[k] * w;
+      }
+      acc[2 * c] += vr;
+      acc[2 * c + 1] += vi;
+    }
+  }
+  __shared__ double red[12][256];
+  for (int c = 0; c < 12; ++c) red[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 12; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x < 12) part[blockIdx.x * 12 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// fixed-order sum of the tensor partials -> the mean tensor (12 doubles)
+__global__ void k_eps_tensor_final(const double* part, int blocks, long long n, double* out) {
+  if (threadIdx.x >= 12) return;
+  double s = 0.0;
+  for (int b = 0; b < blocks; ++b) s += part[b * 12 + threadIdx.x];
+  out[threadIdx.x] = s / (double)n;
 }
 
 // cos, sin of the beam azimuths (one window per ray)

@@ -207,6 +207,62 @@ def split_blocks(optical_data):
     return out
 
 
+_SYMMETRY = {"isotropic": 0, "uniaxial": 1, "biaxial": 2}
+
+
+def _symmetry(arg):
+    """Symmetry identifier -> 0 (isotropic), 1 (uniaxial) or 2 (biaxial; -1
+    keeps the eigenvalues too), or a list of them (dtmm/data.py:1344-1362,
+    :1276-1310)."""
+    if isinstance(arg, str):
+        if arg not in _SYMMETRY:
+            raise ValueError("Invalid symmetry argument.")
+        return _SYMMETRY[arg]
+    if np.ndim(arg) == 0:
+        if arg not in (0, 1, 2, -1):
+            raise ValueError("Invalid symmetry argument.")
+        return 2 if arg == -1 else int(arg)
+    return [_symmetry(a) for a in arg]
+
+
+def effective_blocks(blocks, eff_data):
+    """The blocks of validated optical data as the engine's blocks, with the
+    symmetry of each one's effective medium (dtmm/transfer.py:926-1005,
+    dtmm/data.py:1364-1419): ``eff_data`` is one symmetry for every block or
+    one per block; a per-layer symmetry array averages each layer on its own,
+    so that block becomes one block per layer.  Returns ``(blocks, block_sym)``
+    with ``block_sym`` None when every block keeps one isotropic medium."""
+    nb = len(blocks)
+    if isinstance(eff_data, (str, int, np.integer)):
+        per = [eff_data] * nb
+    else:
+        if isinstance(eff_data, tuple) and len(eff_data) == 3 and not isinstance(eff_data[0], (str, int)):
+            per = [eff_data]
+        else:
+            per = list(eff_data)
+        if len(per) != nb:
+            raise ValueError("Number of elements in eff_data must match length of optical_data.")
+    out, sym, split = [], [], False
+    for (d, ev, ea), e in zip(blocks, per):
+        if isinstance(e, tuple):
+            # an explicit effective block (thickness and eps of its own)
+            raise NotImplementedError("effective data given as optical blocks is outside the GPU engine")
+        s = _symmetry(e)
+        if np.ndim(s) == 0:
+            out.append((d, ev, ea))
+            sym.append(s)
+            continue
+        if len(s) != len(d):
+            raise ValueError("Shape of the symmetry argument is incompatible with block size.")
+        split = True
+        for i in range(len(d)):
+            out.append((d[i:i + 1], ev[i:i + 1] if ev.shape[0] > 1 else ev, ea[i:i + 1] if ea.shape[0] > 1 else ea))
+            sym.append(s[i])
+    if not split and not any(sym):
+        return blocks, None
+    return out, sym
+
+
 def _joined(blocks, shape):
     """Validated blocks as one (thickness, epsv, epsa) of the whole stack: each
     block broadcast over the (y, x) axes along which any block varies, then
@@ -228,9 +284,10 @@ class _Material:
     the caller): one block, or several joined along the layers with the block
     of every layer (each block keeps its own effective medium)."""
 
-    def __init__(self, blocks, shape, device):
+    def __init__(self, blocks, shape, device, block_sym=None):
         import torch
 
+        self.block_sym = None if block_sym is None else np.ascontiguousarray(block_sym, np.int32)
         if isinstance(blocks, list) and len(blocks) > 1:
             block, self.layer_block = _joined(blocks, shape)
         else:
@@ -304,7 +361,8 @@ class DevicePlan:
     """
 
     def __init__(self, field_shape, mat, ks, beta, phi, nray, npol, nlam, method, diffraction, reflection, npass,
-                 nstep, betamax, nin, nout, smooth, precision, device, tuning=None, norm=DTMM_NORM_FFT):
+                 nstep, betamax, nin, nout, smooth, precision, device, tuning=None, norm=DTMM_NORM_FFT,
+                 block_sym=None):
         import torch
 
         self.lib = _lib.load()
@@ -361,6 +419,12 @@ class DevicePlan:
         if mat.layer_block is not None:
             k["lb"] = np.ascontiguousarray(mat.layer_block, np.int32)
             d.layer_block = k["lb"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        if block_sym is None:
+            block_sym = getattr(mat, "block_sym", None)
+        if block_sym is not None:
+            # the symmetry of every block's effective medium (0 isotropic, 1 uniaxial, 2 biaxial)
+            k["bs"] = np.ascontiguousarray(block_sym, np.int32)
+            d.block_sym = k["bs"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
         self.desc = d
         self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
@@ -466,11 +530,12 @@ def workspace_bytes(shape, nlayers, nlam, npol=2, nray=1, method="4x4", diffract
 
 def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, phi=0.0, nin=None, nout=None,
                   npass=None, nstep=1, diffraction=None, reflection=None, method=None, betamax=None, smooth=SMOOTH,
-                  precision=None, device=None, tuning=None, norm=DTMM_NORM_FFT):
+                  precision=None, device=None, tuning=None, norm=DTMM_NORM_FFT, eff_data=None):
     """Resolve options like transfer_field and bind a DevicePlan (explicit beta, phi).
 
     ``optical_data`` is the reference's list with one optical block, or a
-    ``DeviceMaterial`` already on the device.
+    ``DeviceMaterial`` already on the device (one block: ``eff_data`` one
+    symmetry).
     """
     torch = _require_cuda()
     nin = get_default_config_option("nin", nin)
@@ -480,6 +545,7 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     diffraction = get_default_config_option("diffraction", diffraction)
     reflection = get_default_config_option("reflection", reflection)
     betamax = get_default_config_option("betamax", betamax)
+    eff_data = get_default_config_option("eff_data", eff_data)
     precision = _precision[0] if precision is None else precision
     if reflection is None:
         reflection = 0 if method == "2x2" else 1
@@ -492,17 +558,23 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     _check_path(method, reflection, npass, diffraction, norm)
     shape = tuple(field_shape[-2:])
     dev = device or torch.device("cuda", torch.cuda.current_device())
+    block_sym = None
     if isinstance(optical_data, DeviceMaterial):
         mat = optical_data
+        s = _symmetry(eff_data)
+        if np.ndim(s) != 0:
+            raise NotImplementedError("a DeviceMaterial takes one effective-medium symmetry")
+        block_sym = [s] if s else None
     else:
-        mat = _Material(validate_optical_data(optical_data, shape), shape, dev)
+        od, bs = effective_blocks(validate_optical_data(optical_data, shape), eff_data)
+        mat = _Material(od, shape, dev, bs)
     beta = np.asarray(beta, np.float64)
     nray = 1 if beta.ndim == 0 else len(beta)
     nlam = field_shape[-4]
     npol = int(np.prod(field_shape[:-3])) // (nray * nlam)
     return DevicePlan(field_shape, mat, k0(wavelengths, pixelsize), beta, phi, nray, npol,
                       nlam, method, diffraction, reflection, npass, nstep, betamax, nin, nout, smooth, precision, dev,
-                      tuning, norm)
+                      tuning, norm, block_sym)
 
 
 def _check_path(method, reflection, npass, diffraction, norm):
@@ -553,7 +625,7 @@ def _require_cuda():
 
 def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
                      diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision,
-                     split_layers=False):
+                     split_layers=False, eff_data=0):
     torch = _require_cuda()
     _check_path(method, reflection, npass, diffraction, norm)
     if smooth < 0:
@@ -569,8 +641,14 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     od = validate_optical_data(optical_data, shape)
     if split_layers:
         od = split_blocks(od)
+    od, block_sym = effective_blocks(od, eff_data)
+    if block_sym is not None and any(block_sym) and method != "4x4":
+        raise NotImplementedError("effective layers of uniaxial or biaxial symmetry are implemented for the 4x4 method")
+    if block_sym is not None and any(block_sym) and npass > 1 and int(norm) & DTMM_NORM_REF:
+        raise NotImplementedError("norm with DTMM_NORM_REF is implemented for isotropic effective layers")
+    aniso = block_sym is not None and any(block_sym) and diffraction not in (0, np.inf)
     if ret_bulk and method == "4x4" and npass > 1 and (diffraction == 0 or diffraction == np.inf or
-                                                        reflection in (2, 3, 4)):
+                                                        reflection in (2, 3, 4) or aniso):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
     if ret_bulk and method != "4x4" and reflection in (0, 1) and diffraction > 1 and diffraction != np.inf:
         # the k-space sweep carries the sum of the windows, whose E -> H conversions differ
@@ -603,7 +681,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         nray = 1
     nimg = int(np.prod(field_in.shape[:-3]))
     npol = nimg // (nray * nlam)
-    mat = _Material(od, shape, dev)
+    mat = _Material(od, shape, dev, block_sym)
     fdev = field_dev.to(cdt).contiguous()
     L = mat.nlayers
     bulk_dev = None
@@ -710,8 +788,6 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
             reflection = 1
             if diffraction > 1 and method == "2x2":
                 reflection = 2
-    if eff_data not in (0, "isotropic"):
-        raise NotImplementedError("only isotropic effective data (eff_data=0) is supported by the GPU engine")
     field_in, wavelengths, pixelsize = field_data
     if split_wavelengths and not isinstance(field_in, tuple) and not ret_bulk:
         # one transfer per wavelength, dispersive eps evaluated at it (dtmm/transfer.py:497-528);
@@ -772,7 +848,7 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
             o = (res[:, i] if ret_bulk else res[i]) if given else None
             r = _transfer_single(fi, wavelengths, pixelsize, optical_data, bl[i], pl[i], nin, nout, npass, nstep,
                                  diffraction, reflection, method, False, norm, betamax, smooth, ret_bulk, o,
-                                 precision, split_layers)
+                                 precision, split_layers, eff_data)
             if not given:
                 if ret_bulk:
                     res[:, i] = r
@@ -781,7 +857,7 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
         return res, wavelengths, pixelsize
     res = _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
                            diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision,
-                           split_layers)
+                           split_layers, eff_data)
     return res, wavelengths, pixelsize
 
 

@@ -119,6 +119,21 @@ typedef struct dtmm_transfer_desc {
      the output medium: the reference field's polarised part sets the
      intensity, its remainder is added.  Finite diffraction only.  ABI 5. */
   int norm_ref;
+  /* host [nblocks] or null (every block isotropic): the symmetry of each
+     block's effective medium (dtmm/data.py:1364-1419, dtmm/transfer.py:
+     926-1005).  0: isotropic, the mean of the voxels' (e0 + e1 + e2) / 3;
+     1: uniaxial, 2: biaxial, from the mean of the voxels' lab-frame tensors
+     R diag(epsv) R^T: its eigenvalues ordered so that the third is the most
+     distinct (the first two averaged for 1) and its eigen-frame as Euler
+     angles.  The reference's per-layer symmetry is a block per layer.  4x4
+     only; a block of symmetry 1 or 2 takes the real-space chains of every
+     reflection mode (mode 1: C E P F^-1 per k, E P E^-1 per voxel,
+     F P E^-1 C per k) with the effective tensor's eigen-data in the k-space
+     matrices; diffraction 0 and inf do not use the effective medium.  Not
+     with norm_ref.  The tensor's eigen-frame is found on the host: the call
+     synchronises its stream once, and is refused inside a stream capture.
+     ABI 6. */
+  const int* block_sym;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -150,7 +165,7 @@ typedef struct dtmm_kernel_times {
 } dtmm_kernel_times;
 
 /* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
-   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block; 5: norm_ref). */
+   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block; 5: norm_ref; 6: block_sym). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

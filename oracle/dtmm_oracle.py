@@ -26,6 +26,7 @@ biaxial voxels, effective layers of isotropic, uniaxial or biaxial symmetry
 """
 from __future__ import annotations
 
+import cmath
 import math
 import os
 import warnings
@@ -1064,47 +1065,129 @@ def _symmetry(arg):
     return np.asarray([_symmetry(a) for a in arg], int)
 
 
-def tensor_eig(eps6):
-    """Eigenvalues and eigenvectors (columns) of one symmetric 3x3 tensor given
-    as (00, 11, 22, 01, 02, 12), ordered so that the third is the most
-    distinct and the eigenvector matrix is a proper rotation
-    (dtmm/linalg.py:225-318, :364-423).  The reference follows Eberly's
-    non-iterative 3x3 eigensolver, whose eigenvalues come in increasing order
-    and whose eigenvectors form a right-handed frame; here numpy's solver
-    gives the increasing eigenvalues (real parts for a complex tensor) and the
-    frame is made right-handed by the sign of the first vector.  A tensor whose
-    scaled off-diagonal sum of squares is at most 1e-12 is taken as diagonal
-    (identity frame), as the reference does.  Then the cyclic permutation that
-    moves the most distinct eigenvalue to the third place
-    (``_sort_eigvec``, dtmm/linalg.py:166-218)."""
-    e = np.asarray(eps6, CDTYPE)
-    a = np.array([[e[0], e[3], e[4]], [e[3], e[1], e[5]], [e[4], e[5], e[2]]], CDTYPE)
-    scale = np.max(np.abs(e))
-    if scale == 0.0:
-        w, v = np.zeros(3, CDTYPE), np.eye(3, dtype=CDTYPE)
+def _cross3(a, b):
+    return [a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]]
+
+
+def _abs2(v):
+    return sum(x.real ** 2 + x.imag ** 2 for x in v)
+
+
+def _eigvec0(a, e):
+    """Unit eigenvector of eigenvalue e: the largest pairwise cross product of
+    the rows of A - e I (dtmm/linalg.py:50-93)."""
+    r0 = [a[0][0] - e, a[0][1], a[0][2]]
+    r1 = [a[0][1], a[1][1] - e, a[1][2]]
+    r2 = [a[0][2], a[1][2], a[2][2] - e]
+    x = [_cross3(r0, r1), _cross3(r0, r2), _cross3(r1, r2)]
+    d = [_abs2(v) for v in x]
+    imax, dmax = 0, d[0]
+    if d[1] > dmax:
+        imax, dmax = 1, d[1]
+    if d[2] > dmax:
+        imax = 2
+    v = x[imax]
+    inv = 1.0 / cmath.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    return [c * inv for c in v]
+
+
+def _eigvec1(a, w, e):
+    """Eigenvector of eigenvalue e in the orthogonal complement of w
+    (dtmm/linalg.py:96-164)."""
+    if abs(w[0]) > abs(w[1]):
+        u = [-w[2], 0.0, w[0]]
     else:
-        sa = a / scale
-        off = sa[0, 1] ** 2 + sa[0, 2] ** 2 + sa[1, 2] ** 2
-        if abs(off) <= 1e-12:
-            w, v = np.array([a[0, 0], a[1, 1], a[2, 2]], CDTYPE), np.eye(3, dtype=CDTYPE)
-        else:
-            if np.all(a.imag == 0.0):
-                wr, vr = np.linalg.eigh(a.real)
-                w, v = wr.astype(CDTYPE), vr.astype(CDTYPE)
+        u = [0.0, w[2], -w[1]]
+    sc = 1.0 / _abs2(u) ** 0.5
+    u = [c * sc for c in u]
+    v = _cross3(w, u)
+    mul = lambda x: [a[i][0] * x[0] + a[i][1] * x[1] + a[i][2] * x[2] for i in range(3)]
+    dot = lambda x, y: x[0] * y[0] + x[1] * y[1] + x[2] * y[2]
+    au, av = mul(u), mul(v)
+    m00, m01, m11 = dot(u, au) - e, dot(u, av), dot(v, av) - e
+    a00, a01, a11 = abs(m00), abs(m01), abs(m11)
+    out = list(u)
+    if a00 >= a11:
+        if max(a00, a01) > 0:
+            if a00 >= a01:
+                m01 /= m00
+                m00 = 1 / (1 + m01 ** 2) ** 0.5
+                m01 *= m00
             else:
-                w, v = np.linalg.eig(a)
-                order = np.argsort(w.real, kind="stable")
-                w, v = w[order], v[:, order]
-                # unit length in the bilinear sense (v^T v = 1), so that the
-                # eigenvectors of a rotated diagonal tensor come out real
-                v = v / np.sqrt(np.sum(v * v, axis=0))[None, :]
-            if np.linalg.det(v.real) < 0:
-                v[:, 0] = -v[:, 0]
+                m00 /= m01
+                m01 = 1 / (1 + m00 ** 2) ** 0.5
+                m00 *= m01
+            out = [m01 * u[i] - m00 * v[i] for i in range(3)]
+    else:
+        if max(a11, a01) > 0:
+            if a11 >= a01:
+                m01 /= m11
+                m11 = 1 / (1 + m01 ** 2) ** 0.5
+                m01 *= m11
+            else:
+                m11 /= m01
+                m01 = 1 / (1 + m11 ** 2) ** 0.5
+                m11 *= m01
+            out = [m11 * u[i] - m01 * v[i] for i in range(3)]
+    return out
+
+
+def tensor_eig(eps6, is_real=True):
+    """Eigenvalues and eigenvectors (columns) of one symmetric 3x3 tensor given
+    as (00, 11, 22, 01, 02, 12), the third eigenvalue the most distinct
+    (dtmm/linalg.py:225-318, :364-423): Eberly's non-iterative solver
+    ("A Robust Eigensolver for 3x3 Symmetric Matrices", Geometric Tools) on
+    the tensor scaled by its largest entry -- eigenvalues in increasing order
+    from the trigonometric form (its argument clamped for a real tensor), the
+    outer eigenvalue's eigenvector from the rows' cross products, the middle
+    one in its orthogonal complement, the third their cross product; diagonal
+    when the scaled off-diagonal sum of squares is at most 1e-12 -- then the
+    cyclic permutation that moves the most distinct eigenvalue to the third
+    place (``_sort_eigvec``, dtmm/linalg.py:166-218)."""
+    t = [complex(x) for x in np.asarray(eps6, CDTYPE)]
+    vec = [[1.0 + 0j, 0j, 0j], [0j, 1.0 + 0j, 0j], [0j, 0j, 1.0 + 0j]]  # rows
+    scale = max(abs(x) for x in t)
+    if scale == 0.0:
+        eig = [0j, 0j, 0j]
+    else:
+        sm = 1.0 / scale
+        a00, a11, a22, a01, a02, a12 = [x * sm for x in t]
+        a = [[a00, a01, a02], [a01, a11, a12], [a02, a12, a22]]
+        q = (a00 + a11 + a22) / 3
+        b00, b11, b22 = a00 - q, a11 - q, a22 - q
+        norm = a01 ** 2 + a02 ** 2 + a12 ** 2
+        if abs(norm) > 1e-12:
+            p = ((b00 ** 2 + b11 ** 2 + b22 ** 2 + 2 * norm) / 6) ** 0.5
+            c00 = b11 * b22 - a12 * a12
+            c01 = a01 * b22 - a12 * a02
+            c02 = a01 * a12 - b11 * a02
+            half_det = (b00 * c00 - a01 * c01 + a02 * c02) / (p * p * p * 2)
+            if is_real:
+                half_det = complex(min(max(half_det.real, -1.0), 1.0))
+            phi = cmath.acos(half_det) / 3.0
+            twothirdspi = 2.09439510239319549
+            e0 = cmath.cos(phi + twothirdspi) * 2
+            e2 = cmath.cos(phi) * 2
+            e1 = -(e0 + e2)
+            e0, e1, e2 = e0 * p + q, e1 * p + q, e2 * p + q
+            if half_det.real >= 0:
+                vec[2] = _eigvec0(a, e2)
+                vec[1] = _eigvec1(a, vec[2], e1)
+                vec[0] = _cross3(vec[1], vec[2])
+            else:
+                vec[0] = _eigvec0(a, e0)
+                vec[1] = _eigvec1(a, vec[0], e1)
+                vec[2] = _cross3(vec[0], vec[1])
+            eig = [e0 * scale, e1 * scale, e2 * scale]
+        else:
+            eig = [a00 * scale, a11 * scale, a22 * scale]
+    w = np.asarray(eig, CDTYPE)
     m2, m1, m0 = abs(w[1] - w[0]), abs(w[2] - w[0]), abs(w[2] - w[1])
     i, j, k = 0, 1, 2
     if m2 > m1 or m2 > m0:
         i, j, k = (1, 2, 0) if m1 > m0 else (2, 0, 1)
     idx = [i, j, k]
+    v = np.asarray(vec, CDTYPE).T  # eigenvectors as columns
     return w[idx], v[:, idx]
 
 
@@ -1161,7 +1244,7 @@ def effective_block(block, symmetry):
         orders = [sym]
     evs, eas = [], []
     for t, o in zip(means, orders):
-        w, v = tensor_eig(t)
+        w, v = tensor_eig(t, is_real=not np.iscomplexobj(epsv))
         eas.append(rotation_angles(v.real))
         evs.append(uniaxial_order(-1 if o > 1 else o, w))
     if not per_layer:

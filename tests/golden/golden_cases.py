@@ -529,8 +529,7 @@ CASES = {
 
 
 # every case with a reference fixture is also a GPU parity case
-# effective layers of uniaxial / biaxial symmetry: pinned for the oracle only
-ORACLE_CASES = {k: CASES.pop(k) for k in [k for k in CASES if k.startswith("fourx4_eff_")]}
+ORACLE_CASES = {}
 
 
 def build_optical_data(case):

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 5
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 6
 
 
 def _desc(**kw):
@@ -230,3 +230,35 @@ def test_tuner_knows_the_register_transform_sides():
     units = "".join(open(os.path.join(ROOT, "dtmm_gb300", "csrc", f)).read()
                     for f in sorted(os.listdir(os.path.join(ROOT, "dtmm_gb300", "csrc"))) if f.startswith("dtmm_reg_"))
     assert sorted(int(n) for n in re.findall(r"DTMM_REG_DEFINE\((\d+)\)", units)) == list(SIDES_REG)
+
+
+def test_block_sym_descriptor_rules(lib):
+    """block_sym (the symmetry of each block's effective medium): values 0-2;
+    uniaxial / biaxial blocks take the 4x4 real-space chains (reflection 1
+    included, with its per-ray 4x4 tables), are refused with the 2x2 method
+    and with norm_ref, and change nothing without diffraction or with
+    diffraction = inf; all-isotropic block_sym is the default path."""
+    size = lambda sym, **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_with_sym(_desc(**kw), sym)))
+    assert size([0]) == size(None)
+    a1 = size([1])
+    assert a1 > 0 and size([2]) == a1
+    assert size([1], nray=2) > a1  # per-ray tables of the windows' beams
+    for bad in ([3], [-1]):
+        assert size(bad) == 0 and "block_sym" in _lib.last_error()
+    assert size([1], method=2, reflection=0) == 0 and "4x4" in _lib.last_error()
+    assert size([1], npass=3, norm_ref=1) == 0 and "norm_ref" in _lib.last_error()
+    assert size([1], diffraction=0, reflection=2) == size(None, diffraction=0, reflection=2)
+    assert size([1], reflection=4) == size(None, reflection=4)
+    # one entry per block of layer_block
+    lb = np.array([0, 0, 1], np.int32)
+    d = _with_sym(_desc(layer_block=lb.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), [0, 2])
+    d._keep2 = lb
+    assert lib.dtmm_transfer_workspace_size(ctypes.byref(d)) > 0
+
+
+def _with_sym(d, sym):
+    if sym is not None:
+        bs = np.ascontiguousarray(sym, np.int32)
+        d._bs = bs
+        d.block_sym = bs.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    return d
