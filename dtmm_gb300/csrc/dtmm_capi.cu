@@ -107,6 +107,7 @@ struct Layout {
 
 // some block's effective medium is uniaxial or biaxial (block_sym 1 / 2)
 int nblocks(const dtmm_transfer_desc* d);
+bool is_real2(const dtmm_transfer_desc* d);
 bool aniso_eff(const dtmm_transfer_desc* d) {
   if (d->block_sym == nullptr) return false;
   const int nb = nblocks(d);
@@ -196,10 +197,10 @@ int check_desc(const dtmm_transfer_desc* d) {
       return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction supports nstep = 1");
   }
   if (d->block_sym) {
-    if (aniso_eff(d) && d->method == 2)
-      return fail(DTMM_ENOTSUP, "effective layers of uniaxial or biaxial symmetry are supported with the 4x4 method");
-    if (aniso_eff(d) && d->npass > 1 && d->norm_ref)
-      return fail(DTMM_ENOTSUP, "norm_ref is supported with isotropic effective layers");
+    // the 2x2 k-space sweep folds the isotropic medium's window corrections into its voxel records
+    if (aniso_eff(d) && d->method == 2 && !is_real2(d) && d->diffraction != DTMM_DIFFRACTION_FULL)
+      return fail(DTMM_ENOTSUP, "2x2 effective layers of uniaxial or biaxial symmetry are supported with reflection "
+                                "2, without diffraction or with diffraction = inf");
   }
   if (d->layer_block) {
     // the reflections of the inner interfaces between different effective media are not kept

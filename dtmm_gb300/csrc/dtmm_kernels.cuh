@@ -2089,12 +2089,12 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
   const int m = p.mode < 0 ? 1 : 0;  // the mode's columns m, m + 2
   if (p.what == KT_2CE) {
     // C . E(d) . C: E(d) = j P(d) j^-1 of the medium (masked), C = jb P(-d/2) jb^-1
-    // of the window's own beam (uncut), 2x2 of the mode
-    iso_k(beta, phi, p.eps, p.betamax, al, F, Fi);
+    // of the window's own beam (uncut), 2x2 of the mode (any effective medium)
+    eff_k(p, beta, phi, p.betamax, al, F, Fi);
     const bool cut = beta >= p.betamax;
     const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;
     cpx<double> alb[4], Fb[4][4];
-    iso_alphaf(p.wbeta[w], p.wphi[w], p.eps, alb, Fb);
+    eff_alphaf(p, p.wbeta[w], p.wphi[w], alb, Fb);
     cpx<double> J[2][2], Ji[2][2], Jb[2][2], Jbi[2][2], D[2][2], Cm[2][2], T2[2][2];
     J[0][0] = F[0][m]; J[0][1] = F[0][m + 2]; J[1][0] = F[2][m]; J[1][1] = F[2][m + 2];
     Jb[0][0] = Fb[0][m]; Jb[0][1] = Fb[0][m + 2]; Jb[1][0] = Fb[2][m]; Jb[1][1] = Fb[2][m + 2];

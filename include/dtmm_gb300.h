@@ -125,12 +125,15 @@ typedef struct dtmm_transfer_desc {
      1: uniaxial, 2: biaxial, from the mean of the voxels' lab-frame tensors
      R diag(epsv) R^T: its eigenvalues ordered so that the third is the most
      distinct (the first two averaged for 1) and its eigen-frame as Euler
-     angles.  The reference's per-layer symmetry is a block per layer.  4x4
-     only; a block of symmetry 1 or 2 takes the real-space chains of every
-     reflection mode (mode 1: C E P F^-1 per k, E P E^-1 per voxel,
+     angles.  The reference's per-layer symmetry is a block per layer.  With
+     the 4x4 method a block of symmetry 1 or 2 takes the real-space chains of
+     every reflection mode (mode 1: C E P F^-1 per k, E P E^-1 per voxel,
      F P E^-1 C per k) with the effective tensor's eigen-data in the k-space
-     matrices; diffraction 0 and inf do not use the effective medium.  Not
-     with norm_ref.  The tensor's eigen-frame is found on the host: the call
+     matrices (also for the reference field of norm_ref); the 2x2 method
+     takes it on its real-space paths (reflection 2) and refuses it in
+     k-space (reflection 0 / 1 with diffraction); diffraction 0 and inf do
+     not use the effective medium.  The tensor's eigen-frame is found on the
+     host: the call
      synchronises its stream once, and is refused inside a stream capture.
      ABI 6. */
   const int* block_sym;

@@ -240,6 +240,28 @@ CASES = {
                                        illum=dict(jones=(1, 0)),
                                        transfer=dict(method="4x4", diffraction=1, npass=2, eff_data=1, beta=0.0,
                                                      phi=0.0)),
+    # the reference field's 2x2 pass and the 2x2 method's real-space sweep around an
+    # effective medium of uniaxial / biaxial symmetry
+    "fourx4_eff_norm_ref_npass2": dict(shape=(12, 14), nlayers=3, wavelengths=[530.0], pixelsize=100.0,
+                                       material=("twisted", dict()), seed=82,
+                                       illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                                       transfer=dict(method="4x4", diffraction=1, npass=2, norm=3, eff_data=1,
+                                                     beta=0.1, phi=0.3)),
+    "fourx4_eff_norm_local_d3_npass3": dict(shape=(12, 12), nlayers=2, wavelengths=[560.0], pixelsize=100.0,
+                                            material=("twisted", dict(amplitude=0.3)), seed=83,
+                                            illum=dict(jones=(0, 1)),
+                                            transfer=dict(method="4x4", diffraction=3, npass=3, norm=2,
+                                                          eff_data="biaxial", beta=0.0, phi=0.0)),
+    "twox2_eff_refl2_d3": dict(shape=(12, 12), nlayers=3, wavelengths=[500.0, 620.0], pixelsize=100.0,
+                               material=("twisted", dict()), seed=84,
+                               illum=dict(beta=0.1, phi=0.2, jones=(1, 0)),
+                               transfer=dict(method="2x2", diffraction=3, reflection=2, eff_data=1, beta=0.1,
+                                             phi=0.2)),
+    "twox2_eff_refl2_npass2": dict(shape=(14, 12), nlayers=2, wavelengths=[550.0], pixelsize=100.0,
+                                   material=("twisted", dict(amplitude=0.3)), seed=85,
+                                   illum=dict(jones=(1, 0)),
+                                   transfer=dict(method="2x2", diffraction=1, reflection=2, npass=2,
+                                                 eff_data="biaxial", beta=0.0, phi=0.0)),
     "fourx4_split_layers": dict(shape=(12, 14), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                 material=("mixed", dict()), seed=22,
                                 illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
