@@ -242,21 +242,24 @@ __device__ __forceinline__ bool voxel_E_real(double beta, const VoxelInv& vi, do
 // shared memory (beam terms beta cos phi, beta sin phi; with one eps for
 // every voxel eps11 - beta^2, its square root, eps11 (eps11 - beta^2 +
 // delta) and the ordinary mode's phase record), and per voxel and window the
-// FP64 solve of dtmm/tmm.py:157-278 takes about 24 operations (32 with the
-// backward modes):
+// eigenvalues of dtmm/tmm.py:157-278 take about 12 FP64 operations (16 with
+// the backward modes):
 //   gamma = beta cos(az - phi) = cos(az) beta cos(phi) + sin(az) beta sin(phi)
 //   q = u c2 - eps11 kw gamma^2   (a quarter of the discriminant v^2 - 4 u w,
 //                                  whose delta^2 terms cancel)
 //   alpha+- = (-kvh gamma +- sqrt(q)) / u   (kvh = delta sin(t) cos(t); sqrt
 //                                  from an FP32 seed and one Newton step)
-// with sin(t) folded into the cos / sin of (az - phi) of the E entries.  The
-// E rows are rounded to FP32 and rotated back by phi there; the determinants
-// stay FP64 (a rotation keeps them) and are inverted in FP32.
+// FP64 because the phase records (alpha - a_w) d cancel.  The E entries,
+// which the records keep in FP32, are formed in FP32 from the FP32-rounded
+// eigenvalue and voxel / beam terms (sin(t) folded into the cos / sin of
+// (az - phi)), rotated back by phi, and their determinants formed and
+// inverted in FP32: each entry within a few FP32 roundings of its FP64 value.
 struct LeanWin {
   double beta, cp, sp, bcp, bsp;  // beam: beta, cos / sin phi, beta cos / sin phi
   double ev02, evs, c2;           // one eps for every voxel: eps11 - beta^2, its root, eps11 (ev02 + delta)
   double awd;                     // a_w d
   float cpf, spf, r6;             // cos / sin phi in FP32; (evs - a_w) d (one eps for every voxel)
+  float betaf, ev02f, evsf;       // beta, and with one eps for every voxel ev02, evs, in FP32
 };
 constexpr int kLeanChunk = 32;  // windows per shared-memory chunk (<= the block size)
 
@@ -272,6 +275,7 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
   // the voxel's invariants, shared by every ray and window
   double e0 = 0.0, delta = 0.0, ie = 0.0, iu = 0.0, ct = 0.0, ca = 0.0, sa = 0.0, sca = 0.0, ssa = 0.0;
   double kvh = 0.0, qb = 0.0, u = 0.0;
+  float caf = 0.0f, saf = 0.0f, scaf = 0.0f, ssaf = 0.0f, ctf = 0.0f, ief = 0.0f;  // FP32 copies for E
   bool iso = false;
   size_t slot = 0;
   if (active) {
@@ -292,6 +296,12 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
     qb = e0 * (delta * (st * st));
     sca = st * ca;
     ssa = st * sa;
+    caf = f32_rn(ca);
+    saf = f32_rn(sa);
+    scaf = f32_rn(sca);
+    ssaf = f32_rn(ssa);
+    ctf = f32_rn(ct);
+    ief = f32_rn(ie);
     slot = (size_t)y * g.W + (p.permW ? p.permW[x] : x);
   }
   const int rw0 = ray0 * p.nwin, rw1 = ray1 * p.nwin;
@@ -310,14 +320,17 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
       w.awd = aw * p.d;
       w.cpf = f32_rn(w.cp);
       w.spf = f32_rn(w.sp);
+      w.betaf = f32_rn(w.beta);
       if (uni) {
         w.ev02 = p.wev02[rw];
         w.evs = p.wevs[rw];
         w.c2 = p.wc2[rw];
         w.r6 = f32_rn((w.evs - aw) * p.d);
+        w.ev02f = f32_rn(w.ev02);
+        w.evsf = f32_rn(w.evs);
       } else {
         w.ev02 = w.evs = w.c2 = 0.0;
-        w.r6 = 0.0f;
+        w.r6 = w.ev02f = w.evsf = 0.0f;
       }
       wc[threadIdx.x] = w;
     }
@@ -326,67 +339,72 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
     for (int k = 0; k < n; ++k) {
       const LeanWin& w = wc[k];
       double ev02, evs, c2;
-      float r6;
+      float r6, ev02f, evsf;
       if (uni) {
         ev02 = w.ev02;
         evs = w.evs;
         c2 = w.c2;
         r6 = w.r6;
+        ev02f = w.ev02f;
+        evsf = w.evsf;
       } else {
         ev02 = e0 - w.beta * w.beta;
         evs = sqrt_pos_fast(ev02);
         c2 = e0 * (ev02 + delta);
         r6 = f32_rn(fma(evs, p.d, -w.awd));
+        ev02f = f32_rn(ev02);
+        evsf = f32_rn(evs);
       }
-      // E rows (Ex, Ey) of the forward modes 0, 2 (backward 1, 3), in the beam frame
-      double E00, E10, E02, E12, E01 = 0.0, E11 = 0.0, E03 = 0.0, E13 = 0.0, al0, al1 = 0.0;
+      // E rows (Ex, Ey) of the forward modes 0, 2 (backward 1, 3), in the beam
+      // frame, in FP32; the eigenvalues in FP64
+      float E00, E10, E02, E12, E01 = 0.0f, E11 = 0.0f, E03 = 0.0f, E13 = 0.0f;
+      double al0, al1 = 0.0;
       bool zero = false;
       if (iso) {
         al0 = evs;
         al1 = -evs;
-        E00 = 0.5; E10 = 0.0; E02 = 0.0; E12 = 0.5;
-        if (FOUR) { E01 = 0.5; E11 = 0.0; E03 = 0.0; E13 = 0.5; }
+        E00 = 0.5f; E10 = 0.0f; E02 = 0.0f; E12 = 0.5f;
+        if (FOUR) { E01 = 0.5f; E11 = 0.0f; E03 = 0.0f; E13 = 0.5f; }
         zero = evs == 0.0;
       } else if (w.beta == 0.0) {
-        const double cf = fma(ca, w.cp, sa * w.sp), sf = fma(sa, w.cp, -ca * w.sp);
+        const float cf = fmaf(caf, w.cpf, saf * w.spf), sf = fmaf(saf, w.cpf, -caf * w.spf);
         const double sq = sqrt(u * c2) * iu;
         al0 = sq;
         al1 = -sq;
-        E00 = cf; E10 = sf; E02 = -evs * sf; E12 = evs * cf;
-        if (FOUR) { E01 = cf; E11 = sf; E03 = -evs * sf; E13 = evs * cf; }
+        E00 = cf; E10 = sf; E02 = -evsf * sf; E12 = evsf * cf;
+        if (FOUR) { E01 = cf; E11 = sf; E03 = E02; E13 = E12; }
       } else {
         const double gama = fma(ca, w.bcp, sa * w.bsp);
-        const double g2 = gama * gama;
-        const double q = fma(-qb, g2, u * c2);
+        const double q = fma(-qb, gama * gama, u * c2);
         double r0, hy0, eq;
         sqrt_newton(q, r0, hy0, eq);
         const double kvg = kvh * gama;
         al0 = fma(hy0, eq, r0 - kvg) * iu;
-        const double cfst = fma(sca, w.cp, ssa * w.sp), sfst = fma(ssa, w.cp, -sca * w.sp);
-        const double ctbeta = ct * w.beta;
-        const double ev02cf = ev02 * cfst;
-        E00 = fma(al0, ctbeta, -ev02cf) * ie;  E10 = -sfst;
-        E02 = evs * sfst;                      E12 = fma(-evs, cfst, ctbeta);
+        const float a0f = f32_rn(al0);
+        const float cfst = fmaf(scaf, w.cpf, ssaf * w.spf), sfst = fmaf(ssaf, w.cpf, -scaf * w.spf);
+        const float ctbeta = ctf * w.betaf;
+        const float ev02cf = ev02f * cfst;
+        E00 = fmaf(a0f, ctbeta, -ev02cf) * ief;  E10 = -sfst;
+        E02 = evsf * sfst;                       E12 = fmaf(-evsf, cfst, ctbeta);
         if (FOUR) {
           al1 = -fma(hy0, eq, r0 + kvg) * iu;
-          E01 = fma(-al1, ctbeta, ev02cf) * ie;  E11 = sfst;
-          E03 = -E02;                            E13 = fma(evs, cfst, ctbeta);
+          const float a1f = f32_rn(al1);
+          E01 = fmaf(-a1f, ctbeta, ev02cf) * ief;  E11 = sfst;
+          E03 = -E02;                              E13 = fmaf(evsf, cfst, ctbeta);
         }
       }
-      const double x2 = E02 * E10;
-      const double detf = fma(E00, E12, -x2);
-      const double detb = FOUR ? fma(E01, E13, -(E03 * E11)) : 1.0;
-      if (is_zero_d(detf) || is_zero_d(detb)) zero = true;
+      const float df = fmaf(E00, E12, -(E02 * E10));
+      const float db = FOUR ? fmaf(E01, E13, -(E03 * E11)) : 1.0f;
+      if (df == 0.0f || db == 0.0f) zero = true;
       float rec[nrec];
       if (zero) {
 #pragma unroll
         for (int i = 0; i < nrec; ++i) rec[i] = 0.0f;
       } else {
-        // the E rows back to the lab frame (rotation by phi), in FP32; the
-        // first column times scale / det (formed in FP32 from the FP64 det)
-        const float ex0 = f32_rn(E00), ey0 = f32_rn(E10), ex2 = f32_rn(E02), ey2 = f32_rn(E12);
-        const float df = f32_rn(detf);
-        const float sf = (fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / detf)) * scf;
+        // the E rows back to the lab frame (rotation by phi); the first
+        // column times scale / det
+        const float ex0 = E00, ey0 = E10, ex2 = E02, ey2 = E12;
+        const float sf = (fabsf(df) > 1e-30f ? __frcp_rn(df) : f32_rn(1.0 / (double)df)) * scf;
         rec[0] = (ex0 * w.cpf - ey0 * w.spf) * sf;
         rec[1] = ex2 * w.cpf - ey2 * w.spf;
         rec[2] = (ex0 * w.spf + ey0 * w.cpf) * sf;
@@ -394,9 +412,8 @@ __device__ __forceinline__ void voxel_op_lean(const OpParams& p, const Grid& g, 
         rec[4] = iso ? r6 : f32_rn(fma(al0, p.d, -w.awd));
         rec[5] = r6;
         if (FOUR) {
-          const float ex1 = f32_rn(E01), ey1 = f32_rn(E11), ex3 = f32_rn(E03), ey3 = f32_rn(E13);
-          const float db = f32_rn(detb);
-          const float sb = (fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / detb)) * scf;
+          const float ex1 = E01, ey1 = E11, ex3 = E03, ey3 = E13;
+          const float sb = (fabsf(db) > 1e-30f ? __frcp_rn(db) : f32_rn(1.0 / (double)db)) * scf;
           rec[6] = (ex1 * w.cpf - ey1 * w.spf) * sb;
           rec[7] = ex3 * w.cpf - ey3 * w.spf;
           rec[8] = (ex1 * w.spf + ey1 * w.cpf) * sb;
