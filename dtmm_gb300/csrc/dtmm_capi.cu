@@ -197,10 +197,12 @@ int check_desc(const dtmm_transfer_desc* d) {
       return fail(DTMM_ENOTSUP, "2x2 reflection 1 without diffraction supports nstep = 1");
   }
   if (d->block_sym) {
-    // the 2x2 k-space sweep folds the isotropic medium's window corrections into its voxel records
+    // the 2x2 k-space sweep folds the isotropic medium's window corrections into its voxel
+    // records; its reflection-0 step runs in real space instead, reflection 1 (interfaces
+    // between the effective media, tracked reflections) is not built
     if (aniso_eff(d) && d->method == 2 && !is_real2(d) && d->diffraction != DTMM_DIFFRACTION_FULL)
       return fail(DTMM_ENOTSUP, "2x2 effective layers of uniaxial or biaxial symmetry are supported with reflection "
-                                "2, without diffraction or with diffraction = inf");
+                                "0 or 2, or with diffraction = inf");
   }
   if (d->layer_block) {
     // the reflections of the inner interfaces between different effective media are not kept
@@ -223,8 +225,12 @@ int nblocks(const dtmm_transfer_desc* d) {
 }
 
 // 2x2 in real space: reflection mode 2, or no diffraction without reflections
+// -- and reflection 0 with diffraction around an anisotropic effective medium
+// (the reference's k-space step, here on the real-space field)
 bool is_real2(const dtmm_transfer_desc* d) {
-  return d->method == 2 && (d->reflection == 2 || (d->diffraction == 0 && d->reflection == 0));
+  return d->method == 2 &&
+         (d->reflection == 2 || (d->diffraction == 0 && d->reflection == 0) ||
+          (d->reflection == 0 && d->diffraction >= 1 && aniso_eff(d)));
 }
 
 Layout layout_of(const dtmm_transfer_desc* d) {
@@ -779,7 +785,7 @@ struct Engine {
       p.mode = proj_mode < 0 ? -1 : 1;
       p.ta = 0;
       p.tb = p.mode > 0 ? 2 : 1;
-    } else if (what == KT_2CE) {
+    } else if (what == KT_2CE || what == KT_2C1 || what == KT_2C2) {
       p.mode = (proj_mode & 1) ? -1 : 1;
       p.proj_mode = proj_mode >> 1;
     }
@@ -788,7 +794,8 @@ struct Engine {
     // ray's windows: one slab per ray
     const bool per_ray = what == KT_2OUT || what == KT_WINMAT || what == KT_CFD || what == KT_CEPN ||
                          what == KT_CD || what == KT_DC || what == KT_2RIN || what == KT_2R || what == KT_2X ||
-                         what == KT_2CE || what == KT_2WIN || what == KT_C1 || what == KT_C2;
+                         what == KT_2CE || what == KT_2WIN || what == KT_C1 || what == KT_C2 || what == KT_2C1 ||
+                         what == KT_2C2;
     const int rays = per_ray ? d.nray : 1;
     const size_t slab = (size_t)n * ktab_entries(what);
     for (int r = 0; r < rays; ++r) {
@@ -803,7 +810,8 @@ struct Engine {
   static int ktab_entries(int what) {
     switch (what) {
       case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
-      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: return 4;
+      case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: case KT_2C1:
+      case KT_2C2: return 4;
       default: return 16;
     }
   }
@@ -1964,6 +1972,35 @@ struct Engine {
   // none, for the 4x4 method's reference field)
   int chain_refl = -1;
 
+  // one interface call of the reference's _transfer_ray_2x2_1 with reflection
+  // 0 (dtmm/propagate_2x2.py:19-87, :193-284; its k-space field here in real
+  // space, every step being linear) on f, its window's part: per sub-step
+  // C . E(dd/2) per k, E P E^-1 of the output voxel over dd, E(dd/2) . C per k;
+  // then the layer's E and H parts into bo
+  int chain2k(Local2Params& p, int w, int nst, double dd, cpx<R>* f, cpx<R>* bo) {
+    int rc;
+    p.beta = wbeta() + w;
+    p.phi = wphi() + w;
+    p.bstride = L.nwin;
+    const size_t ray4 = (size_t)d.nlam * L.HW * 4;
+    const int pm = 2 * w + (p.mode < 0 ? 1 : 0);
+    for (int s = 0; s < nst; ++s) {
+      const cpx<R>* t1;
+      const cpx<R>* t2;
+      if ((rc = table(KT_2C1, dd / 2, t1, pm))) return rc;
+      if ((rc = diffract(f, f, t1, ray4, 2))) return rc;
+      if (dd != 0.0) {
+        p.d = dd;
+        p.reps = 1;
+        if ((rc = local2(p, L2_HALF, f, nullptr, nullptr))) return rc;
+      }
+      if ((rc = table(KT_2C2, dd / 2, t2, pm))) return rc;
+      if ((rc = diffract(f, f, t2, ray4, 2))) return rc;
+    }
+    if (p.mode > 0 && bo != nullptr) return local2(p, L2_BULK, f, nullptr, bo);
+    return DTMM_OK;
+  }
+
   int chain2(Local2Params& p, int w, int jout, int nst, double dd, cpx<R>* f, cpx<R>* r, cpx<R>* bo) {
     const int refl_mode = chain_refl >= 0 ? chain_refl : d.reflection;
     int rc;
@@ -2062,8 +2099,10 @@ struct Engine {
         const double dd = inner ? dir * d.thickness[p.lout] / d.nstep[p.lout] : 0.0;
         cpx<R>* Rj = tracked ? refl + (size_t)j * n2 : nullptr;
         cpx<R>* bo = bslab(jout);
+        // reflection 0 with diffraction: the reference's k-space step
+        const bool kstep = d.reflection == 0 && d.diffraction >= 1;
         if (!win) {
-          if ((rc = chain2(p, 0, jout, nst, dd, F2, Rj, bo))) return rc;
+          if ((rc = kstep ? chain2k(p, 0, nst, dd, F2, bo) : chain2(p, 0, jout, nst, dd, F2, Rj, bo))) return rc;
           continue;
         }
         CK(cudaMemsetAsync(A2, 0, bytes2, st));
@@ -2073,7 +2112,8 @@ struct Engine {
           if ((rc = table(KT_2WIN, 0.0, wt, w))) return rc;
           if ((rc = diffract(P2, F2, wt, ray4, 2))) return rc;
           if (tracked && (rc = diffract(RP, Rj, wt, ray4, 2))) return rc;
-          if ((rc = chain2(p, w, jout, nst, dd, P2, tracked ? RP : nullptr, bo))) return rc;
+          if ((rc = kstep ? chain2k(p, w, nst, dd, P2, bo) : chain2(p, w, jout, nst, dd, P2, tracked ? RP : nullptr, bo)))
+            return rc;
           if ((rc = axpby(A2, A2, nullptr, 1.0, P2, nullptr, 1.0, 2))) return rc;
           if (tracked && (rc = axpby(RA, RA, nullptr, 1.0, RP, nullptr, 1.0, 2))) return rc;
         }

@@ -1618,6 +1618,10 @@ enum KTab {
   KT_C1 = 21,    // 4x4 C . E P(d) F^-1, C = E_w P_w(-d) E_w^-1 of the window's beam (first_corrected_Epn_
                  //   diffraction_matrix, dtmm/matrix.py:127-157)
   KT_C2 = 22,    // 4x4 F P(d) E^-1 . C                 (second_corrected_Epn_diffraction_matrix, :159-174)
+  // the 2x2 method's k-space step around an anisotropic effective medium, per window of the ray
+  KT_2C1 = 23,   // 2x2 C . E(d), C = j_w P_w(-d) j_w^-1 of the window's beam (first_E_diffraction_matrix,
+                 //   dtmm/matrix.py:53-58)
+  KT_2C2 = 24,   // 2x2 E(d) . C                       (second_E_diffraction_matrix, :46-51)
 };
 
 // the module default of betamax, which the reference's windowed reflection
@@ -1849,7 +1853,8 @@ __device__ inline void iso_half_step(bool first, cpx<double> eps, double beta, d
 __device__ __forceinline__ int kt_entries(int what) {
   switch (what) {
     case KT_2IN: case KT_2OUT: case KT_2RIN: case KT_2X: return 8;
-    case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: return 4;
+    case KT_2E: case KT_2TE: case KT_2R: case KT_2CE: case KT_2WIN: case KT_2BX: case KT_2H: case KT_2C1:
+    case KT_2C2: return 4;
     default: return 16;
   }
 }
@@ -2104,9 +2109,10 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     return;
   }
   const int m = p.mode < 0 ? 1 : 0;  // the mode's columns m, m + 2
-  if (p.what == KT_2CE) {
+  if (p.what == KT_2CE || p.what == KT_2C1 || p.what == KT_2C2) {
     // C . E(d) . C: E(d) = j P(d) j^-1 of the medium (masked), C = jb P(-d/2) jb^-1
-    // of the window's own beam (uncut), 2x2 of the mode (any effective medium)
+    // of the window's own beam (uncut), 2x2 of the mode (any effective medium);
+    // KT_2C1 / KT_2C2: C over -d on one side only
     eff_k(p, beta, phi, p.betamax, al, F, Fi);
     const bool cut = beta >= p.betamax;
     const int w = p.ray * p.nwin_axis * p.nwin_axis + p.proj_mode;
@@ -2118,12 +2124,21 @@ __global__ void k_ktab(KTabParams p, Grid g, cpx<R>* __restrict__ tab) {
     inv2(J, Ji);
     inv2(Jb, Jbi);
     const cpx<double> pd[2] = {cexp_i(al[m] * (ks * p.d)), cexp_i(al[m + 2] * (ks * p.d))};
-    const cpx<double> pc[2] = {cexp_i(alb[m] * (-ks * p.d / 2)), cexp_i(alb[m + 2] * (-ks * p.d / 2))};
+    const double dc = p.what == KT_2CE ? p.d / 2 : p.d;
+    const cpx<double> pc[2] = {cexp_i(alb[m] * (-ks * dc)), cexp_i(alb[m + 2] * (-ks * dc))};
     for (int i = 0; i < 2; ++i)
       for (int j = 0; j < 2; ++j) {
         D[i][j] = cut ? mk<double>(0.0, 0.0) : J[i][0] * pd[0] * Ji[0][j] + J[i][1] * pd[1] * Ji[1][j];
         Cm[i][j] = Jb[i][0] * pc[0] * Jbi[0][j] + Jb[i][1] * pc[1] * Jbi[1][j];
       }
+    if (p.what != KT_2CE) {
+      cpx<R>* o = tab + (size_t)t * 4;
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
+          o[i * 2 + j] = cvt<R>(p.what == KT_2C1 ? Cm[i][0] * D[0][j] + Cm[i][1] * D[1][j]
+                                                 : D[i][0] * Cm[0][j] + D[i][1] * Cm[1][j]);
+      return;
+    }
     for (int i = 0; i < 2; ++i)
       for (int j = 0; j < 2; ++j) T2[i][j] = D[i][0] * Cm[0][j] + D[i][1] * Cm[1][j];
     cpx<R>* o = tab + (size_t)t * 4;

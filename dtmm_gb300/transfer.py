@@ -642,11 +642,10 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     if split_layers:
         od = split_blocks(od)
     od, block_sym = effective_blocks(od, eff_data)
-    if (block_sym is not None and any(block_sym) and method != "4x4" and reflection != 2 and
-            not (diffraction == 0 and reflection == 0) and diffraction != np.inf):
-        # the 2x2 k-space sweep folds the isotropic medium's window corrections into its voxel records
+    if block_sym is not None and any(block_sym) and method != "4x4" and reflection == 1 and diffraction != np.inf:
+        # reflection 1: the interfaces between the effective media and their tracked reflections
         raise NotImplementedError("2x2 effective layers of uniaxial or biaxial symmetry are implemented with "
-                                  "reflection 2, without diffraction or with diffraction = inf")
+                                  "reflection 0 or 2, or with diffraction = inf")
     aniso = block_sym is not None and any(block_sym) and diffraction not in (0, np.inf)
     if ret_bulk and method == "4x4" and npass > 1 and (diffraction == 0 or diffraction == np.inf or
                                                         reflection in (2, 3, 4) or aniso):

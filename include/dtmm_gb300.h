@@ -130,9 +130,10 @@ typedef struct dtmm_transfer_desc {
      every reflection mode (mode 1: C E P F^-1 per k, E P E^-1 per voxel,
      F P E^-1 C per k) with the effective tensor's eigen-data in the k-space
      matrices (also for the reference field of norm_ref); the 2x2 method
-     takes it on its real-space paths (reflection 2) and refuses it in
-     k-space (reflection 0 / 1 with diffraction); diffraction 0 and inf do
-     not use the effective medium.  The tensor's eigen-frame is found on the
+     takes it on its real-space paths (reflection 2; reflection 0 with
+     diffraction as the real-space chain C E(d/2) per k, E P E^-1 per
+     voxel, E(d/2) C per k) and refuses reflection 1; diffraction 0 and inf
+     do not use the effective medium.  The tensor's eigen-frame is found on the
      host: the call
      synchronises its stream once, and is refused inside a stream capture.
      ABI 6. */

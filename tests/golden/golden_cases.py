@@ -262,6 +262,24 @@ CASES = {
                                    illum=dict(jones=(1, 0)),
                                    transfer=dict(method="2x2", diffraction=1, reflection=2, npass=2,
                                                  eff_data="biaxial", beta=0.0, phi=0.0)),
+    "twox2_eff_uniaxial_d1": dict(shape=(12, 14), nlayers=3, wavelengths=[540.0], pixelsize=100.0,
+                                  material=("twisted", dict()), seed=86,
+                                  illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),
+                                  transfer=dict(method="2x2", diffraction=1, eff_data=1, beta=0.1, phi=0.3)),
+    "twox2_eff_biaxial_d3": dict(shape=(12, 12), nlayers=2, wavelengths=[480.0, 620.0], pixelsize=100.0,
+                                 material=("twisted", dict(amplitude=0.3)), seed=87,
+                                 illum=dict(),
+                                 transfer=dict(method="2x2", diffraction=3, eff_data="biaxial", beta=0.0, phi=0.0)),
+    "twox2_eff_blocks_nstep2": dict(shape=(12, 12), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
+                                    blocks=[("twisted", dict(thickness=2.0), 2), ("iso", dict(eps=2.3), 1)],
+                                    seed=88, illum=dict(jones=(1, 0)),
+                                    transfer=dict(method="2x2", diffraction=1, nstep=2, eff_data=[1, 0], beta=0.0,
+                                                  phi=0.0)),
+    "twox2_eff_uniaxial_bulk": dict(shape=(12, 12), nlayers=2, wavelengths=[520.0], pixelsize=100.0,
+                                    material=("twisted", dict()), seed=89,
+                                    illum=dict(beta=0.1, phi=0.5, jones=(0, 1)),
+                                    transfer=dict(method="2x2", diffraction=1, eff_data=1, ret_bulk=True, beta=0.1,
+                                                  phi=0.5)),
     "fourx4_split_layers": dict(shape=(12, 14), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                 material=("mixed", dict()), seed=22,
                                 illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),

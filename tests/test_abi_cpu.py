@@ -236,8 +236,8 @@ def test_block_sym_descriptor_rules(lib):
     """block_sym (the symmetry of each block's effective medium): values 0-2;
     uniaxial / biaxial blocks take the 4x4 real-space chains (reflection 1
     included, with its per-ray 4x4 tables), norm_ref included; the 2x2
-    method takes them on its real-space paths (reflection 2, no diffraction,
-    diffraction = inf) and refuses them in k-space; they change nothing
+    method takes them on its real-space paths (reflection 0 and 2, no
+    diffraction, diffraction = inf) and refuses reflection 1; they change nothing
     without diffraction or with diffraction = inf; all-isotropic block_sym is
     the default path."""
     size = lambda sym, **kw: lib.dtmm_transfer_workspace_size(ctypes.byref(_with_sym(_desc(**kw), sym)))
@@ -247,8 +247,8 @@ def test_block_sym_descriptor_rules(lib):
     assert size([1], nray=2) > a1  # per-ray tables of the windows' beams
     for bad in ([3], [-1]):
         assert size(bad) == 0 and "block_sym" in _lib.last_error()
-    assert size([1], method=2, reflection=0) == 0 and "reflection" in _lib.last_error()
-    assert size([1], method=2, reflection=1) == 0
+    assert size([1], method=2, reflection=0) > 0  # the k-space step in real space
+    assert size([1], method=2, reflection=1) == 0 and "reflection" in _lib.last_error()
     assert size([1], method=2, reflection=2) == size(None, method=2, reflection=2) > 0
     assert size([1], npass=3, norm_ref=1) > 0  # the real-space chains with the reference field
     assert size([1], diffraction=0, reflection=2) == size(None, diffraction=0, reflection=2)
