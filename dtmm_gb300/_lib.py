@@ -26,7 +26,7 @@ ABI_SYMBOLS = ("dtmm_abi_version", "dtmm_last_error", "dtmm_transfer_workspace_s
                "dtmm_diffract_workspace_size", "dtmm_diffract", "dtmm_q2data", "dtmm_wave_field",
                "dtmm_field_diffraction_matrix", "dtmm_field_intensity", "dtmm_scale_fields",
                "dtmm_twisted_nematic_angles")
-ABI_VERSION = 6
+ABI_VERSION = 7
 STATIC_SCRATCH_BYTES = 64 << 20
 
 
@@ -67,6 +67,7 @@ class TransferDesc(ctypes.Structure):
         ("layer_block", ctypes.POINTER(ctypes.c_int)),
         ("norm_ref", ctypes.c_int),
         ("block_sym", ctypes.POINTER(ctypes.c_int)),
+        ("block_eff", ctypes.POINTER(ctypes.c_double)),
     ]
 
 

@@ -108,11 +108,21 @@ struct Layout {
 // some block's effective medium is uniaxial or biaxial (block_sym 1 / 2)
 int nblocks(const dtmm_transfer_desc* d);
 bool is_real2(const dtmm_transfer_desc* d);
+// block b's effective medium is uniaxial or biaxial: the mean of symmetry 1
+// / 2, or a given medium (symmetry 3) without three equal eigenvalues
+bool blk_aniso_of(const dtmm_transfer_desc* d, int b) {
+  if (d->block_sym == nullptr) return false;
+  const int s = d->block_sym[b];
+  if (s == 1 || s == 2) return true;
+  if (s != 3 || d->block_eff == nullptr) return false;
+  const double* r = d->block_eff + 9 * (size_t)b;
+  return !(r[0] == r[2] && r[2] == r[4] && r[1] == r[3] && r[3] == r[5]);
+}
 bool aniso_eff(const dtmm_transfer_desc* d) {
   if (d->block_sym == nullptr) return false;
   const int nb = nblocks(d);
   for (int b = 0; b < nb; ++b)
-    if (d->block_sym[b] != 0) return true;
+    if (blk_aniso_of(d, b)) return true;
   return false;
 }
 
@@ -138,9 +148,12 @@ int check_desc(const dtmm_transfer_desc* d) {
     }
   }
   if (d->block_sym) {
-    for (int b = 0; b < nblocks(d); ++b)
-      if (d->block_sym[b] < 0 || d->block_sym[b] > 2)
-        return fail(DTMM_EINVAL, "block_sym must be 0 (isotropic), 1 (uniaxial) or 2 (biaxial)");
+    for (int b = 0; b < nblocks(d); ++b) {
+      if (d->block_sym[b] < 0 || d->block_sym[b] > 3)
+        return fail(DTMM_EINVAL, "block_sym must be 0 (isotropic), 1 (uniaxial), 2 (biaxial) or 3 (given)");
+      if (d->block_sym[b] == 3 && d->block_eff == nullptr)
+        return fail(DTMM_EINVAL, "block_sym 3 needs block_eff");
+    }
   }
   // reflection mode 2 without diffraction: the per-voxel 4x4 transfer (npass 1);
   // diffraction = inf (DTMM_DIFFRACTION_FULL): every eigenwave exactly (4x4, npass 1,
@@ -484,7 +497,9 @@ struct Engine {
   double* effx(int b) const { return A<double>(L.effx) + 10 * b; }
   double* efft(int b) const { return A<double>(L.efft) + 12 * b; }
   // block b's effective medium is uniaxial or biaxial
-  bool blk_aniso(int b) const { return d.block_sym != nullptr && b >= 0 && d.block_sym[b] != 0; }
+  bool blk_aniso(int b) const { return b >= 0 && blk_aniso_of(&d, b); }
+  // block b's effective medium is given (block_eff)
+  bool blk_given(int b) const { return d.block_sym != nullptr && b >= 0 && d.block_sym[b] == 3; }
   double* awb(int b) const { return A<double>(L.awb) + (size_t)b * d.nray * L.nwin; }
   int blk_of(int l) const { return d.layer_block ? d.layer_block[l] : 0; }
   // the block whose effective medium the k-space tables fetched now use
@@ -1214,6 +1229,18 @@ struct Engine {
       int blocks = (int)((nvox + 1023) / 1024);
       if (blocks > kPartBlocks) blocks = kPartBlocks;
       const char* e0 = (const char*)d.epsv + (size_t)l0 * d.epsv_strides[0] * (d.eps_complex ? 16 : 8);
+      if (blk_given(blk_of(l0))) {  // a given medium: its first eigenvalue (the isotropic one when all are equal)
+        const double* r = d.block_eff + 9 * (size_t)blk_of(l0);
+        Scalars64 sc;
+        sc.n = 2;
+        sc.off = 0;
+        sc.v[0] = r[0];
+        sc.v[1] = r[1];
+        k_set_scalars<<<1, 64, 0, st>>>(sc, effb(blk_of(l0)));
+        CKL("k_set_scalars");
+        l0 = l1;
+        continue;
+      }
       k_eps_mean<<<blocks, 256, 0, st>>>(e0, d.eps_complex, d.epsv_strides[0], d.epsv_strides[1], d.epsv_strides[2],
                                          one ? 1 : l1 - l0, one ? 1 : d.height, one ? 1 : d.width, A<double>(L.part));
       CKL("k_eps_mean");
@@ -1235,20 +1262,30 @@ struct Engine {
       }
       l0 = l1;
     }
+    bool means = false;  // some block's medium is the eigen-frame of its mean tensor
+    for (int b = 0; b < nblocks(&d); ++b) means = means || (blk_aniso(b) && !blk_given(b));
     if (aniso_eff(&d)) {
-      // the eigen-frame of each anisotropic block's mean tensor, on the host
-      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-      CK(cudaStreamIsCapturing(st, &cs));
-      if (cs != cudaStreamCaptureStatusNone)
-        return fail(DTMM_ENOTSUP, "effective layers of uniaxial or biaxial symmetry are not supported in a stream "
-                                  "capture (their eigen-frame is found on the host)");
       const int nb = nblocks(&d);
       std::vector<double> t(12 * (size_t)nb), x(10 * (size_t)nb, 0.0);
-      CK(cudaMemcpyAsync(t.data(), efft(0), sizeof(double) * t.size(), cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      for (int b = 0; b < nb; ++b)
-        if (blk_aniso(b))
-          eff_medium(t.data() + 12 * (size_t)b, d.block_sym[b], !d.eps_complex, x.data() + 10 * (size_t)b);
+      if (means) {  // the eigen-frame of each anisotropic block's mean tensor, on the host
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+          return fail(DTMM_ENOTSUP, "effective layers of uniaxial or biaxial symmetry are not supported in a stream "
+                                    "capture (their eigen-frame is found on the host)");
+        CK(cudaMemcpyAsync(t.data(), efft(0), sizeof(double) * t.size(), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+      }
+      for (int b = 0; b < nb; ++b) {
+        if (!blk_aniso(b)) continue;
+        double* xb = x.data() + 10 * (size_t)b;
+        if (blk_given(b)) {  // the given eigenvalues and angles
+          xb[0] = 3.0;
+          for (int i = 0; i < 9; ++i) xb[1 + i] = d.block_eff[9 * (size_t)b + i];
+        } else {
+          eff_medium(t.data() + 12 * (size_t)b, d.block_sym[b], !d.eps_complex, xb);
+        }
+      }
       for (size_t o = 0; o < x.size(); o += 64) {
         Scalars64 sc;
         sc.n = (int)std::min<size_t>(64, x.size() - o);
@@ -2475,7 +2512,7 @@ std::string& last_error_slot() { return g_err; }
 
 extern "C" {
 
-int dtmm_abi_version(void) { return 6; }
+int dtmm_abi_version(void) { return 7; }
 
 const char* dtmm_last_error(void) { return g_err.c_str(); }
 

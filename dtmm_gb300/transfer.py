@@ -225,32 +225,56 @@ def _symmetry(arg):
     return [_symmetry(a) for a in arg]
 
 
+def _is_effective_block(e):
+    """An explicit effective block ``(thickness, epsv, epsa)`` rather than a
+    symmetry (array): its eps values end in an axis of three (the reference
+    first tries the argument as an optical block, dtmm/transfer.py:941-947)."""
+    return (isinstance(e, tuple) and len(e) == 3 and not callable(e[1]) and np.ndim(e[1]) >= 1 and
+            np.shape(e[1])[-1] == 3)
+
+
 def effective_blocks(blocks, eff_data):
     """The blocks of validated optical data as the engine's blocks, with the
-    symmetry of each one's effective medium (dtmm/transfer.py:926-1005,
+    effective medium of each one (dtmm/transfer.py:926-1005,
     dtmm/data.py:1364-1419): ``eff_data`` is one symmetry for every block or
-    one per block; a per-layer symmetry array averages each layer on its own,
-    so that block becomes one block per layer.  Returns ``(blocks, block_sym)``
-    with ``block_sym`` None when every block keeps one isotropic medium."""
+    one entry per block -- a symmetry, a per-layer symmetry array (each layer
+    averaged on its own, so that block becomes one block per layer), or an
+    explicit effective block ``(thickness, epsv, epsa)`` homogeneous in each
+    layer (one block per layer, its medium given).  Returns ``(blocks,
+    block_sym, block_eff)``: ``block_sym`` per block 0 / 1 / 2 (isotropic /
+    uniaxial / biaxial mean) or 3 (given), None when every block keeps its
+    isotropic mean; ``block_eff`` the given media (rows of epsv re / im x 3,
+    psi, theta, phi) or None."""
     nb = len(blocks)
     if isinstance(eff_data, (str, int, np.integer)):
         per = [eff_data] * nb
     else:
-        if isinstance(eff_data, tuple) and len(eff_data) == 3 and not isinstance(eff_data[0], (str, int)):
-            per = [eff_data]
-        else:
-            per = list(eff_data)
+        per = list(eff_data)
         if len(per) != nb:
             raise ValueError("Number of elements in eff_data must match length of optical_data.")
-    out, sym, split = [], [], False
+    out, sym, given, split = [], [], [], False
     for (d, ev, ea), e in zip(blocks, per):
-        if isinstance(e, tuple):
-            # an explicit effective block (thickness and eps of its own)
-            raise NotImplementedError("effective data given as optical blocks is outside the GPU engine")
+        if _is_effective_block(e):
+            de, eve, eae = _validate_block(e, (1, 1))
+            if len(de) != len(d) or not np.array_equal(de, d):
+                # the effective layers' own thicknesses set the diffraction steps there
+                raise NotImplementedError("effective blocks with layer thicknesses other than the optical "
+                                          "block's are outside the GPU engine")
+            eve = np.broadcast_to(eve, (len(d), 1, 1, 3))
+            eae = np.broadcast_to(eae, (len(d), 1, 1, 3))
+            split = True
+            for i in range(len(d)):
+                out.append((d[i:i + 1], ev[i:i + 1] if ev.shape[0] > 1 else ev, ea[i:i + 1] if ea.shape[0] > 1 else ea))
+                sym.append(3)
+                v = np.asarray(eve[i, 0, 0], np.complex128)
+                given.append([v[0].real, v[0].imag, v[1].real, v[1].imag, v[2].real, v[2].imag,
+                              *np.asarray(eae[i, 0, 0], np.float64)])
+            continue
         s = _symmetry(e)
         if np.ndim(s) == 0:
             out.append((d, ev, ea))
             sym.append(s)
+            given.append([0.0] * 9)
             continue
         if len(s) != len(d):
             raise ValueError("Shape of the symmetry argument is incompatible with block size.")
@@ -258,9 +282,26 @@ def effective_blocks(blocks, eff_data):
         for i in range(len(d)):
             out.append((d[i:i + 1], ev[i:i + 1] if ev.shape[0] > 1 else ev, ea[i:i + 1] if ea.shape[0] > 1 else ea))
             sym.append(s[i])
+            given.append([0.0] * 9)
     if not split and not any(sym):
-        return blocks, None
-    return out, sym
+        return blocks, None, None
+    block_eff = np.ascontiguousarray(given, np.float64) if 3 in sym else None
+    return out, sym, block_eff
+
+
+def _aniso_blocks(block_sym, block_eff):
+    """Some block's effective medium is uniaxial or biaxial (given media with
+    three equal eigenvalues are isotropic)."""
+    if block_sym is None:
+        return False
+    for b, s in enumerate(block_sym):
+        if s in (1, 2):
+            return True
+        if s == 3:
+            r = block_eff[b]
+            if not (r[0] == r[2] == r[4] and r[1] == r[3] == r[5]):
+                return True
+    return False
 
 
 def _joined(blocks, shape):
@@ -284,10 +325,11 @@ class _Material:
     the caller): one block, or several joined along the layers with the block
     of every layer (each block keeps its own effective medium)."""
 
-    def __init__(self, blocks, shape, device, block_sym=None):
+    def __init__(self, blocks, shape, device, block_sym=None, block_eff=None):
         import torch
 
         self.block_sym = None if block_sym is None else np.ascontiguousarray(block_sym, np.int32)
+        self.block_eff = None if block_eff is None else np.ascontiguousarray(block_eff, np.float64)
         if isinstance(blocks, list) and len(blocks) > 1:
             block, self.layer_block = _joined(blocks, shape)
         else:
@@ -422,9 +464,14 @@ class DevicePlan:
         if block_sym is None:
             block_sym = getattr(mat, "block_sym", None)
         if block_sym is not None:
-            # the symmetry of every block's effective medium (0 isotropic, 1 uniaxial, 2 biaxial)
+            # the symmetry of every block's effective medium (0 isotropic, 1 uniaxial, 2 biaxial,
+            # 3 given in block_eff)
             k["bs"] = np.ascontiguousarray(block_sym, np.int32)
             d.block_sym = k["bs"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        block_eff = getattr(mat, "block_eff", None)
+        if block_eff is not None:
+            k["be"] = np.ascontiguousarray(block_eff, np.float64)
+            d.block_eff = k["be"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         self.desc = d
         self.set_tuning(**(tuning or {}))
         self.nbytes = int(self.lib.dtmm_transfer_workspace_size(ctypes.byref(d)))
@@ -561,13 +608,15 @@ def plan_transfer(field_shape, wavelengths, pixelsize, optical_data, beta=0.0, p
     block_sym = None
     if isinstance(optical_data, DeviceMaterial):
         mat = optical_data
+        if _is_effective_block(eff_data) or not isinstance(eff_data, (str, int, np.integer)):
+            raise NotImplementedError("a DeviceMaterial takes one effective-medium symmetry")
         s = _symmetry(eff_data)
         if np.ndim(s) != 0:
             raise NotImplementedError("a DeviceMaterial takes one effective-medium symmetry")
         block_sym = [s] if s else None
     else:
-        od, bs = effective_blocks(validate_optical_data(optical_data, shape), eff_data)
-        mat = _Material(od, shape, dev, bs)
+        od, bs, be = effective_blocks(validate_optical_data(optical_data, shape), eff_data)
+        mat = _Material(od, shape, dev, bs, be)
     beta = np.asarray(beta, np.float64)
     nray = 1 if beta.ndim == 0 else len(beta)
     nlam = field_shape[-4]
@@ -641,12 +690,13 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
     od = validate_optical_data(optical_data, shape)
     if split_layers:
         od = split_blocks(od)
-    od, block_sym = effective_blocks(od, eff_data)
-    if block_sym is not None and any(block_sym) and method != "4x4" and reflection == 1 and diffraction != np.inf:
+    od, block_sym, block_eff = effective_blocks(od, eff_data)
+    aniso = _aniso_blocks(block_sym, block_eff)
+    if aniso and method != "4x4" and reflection == 1 and diffraction != np.inf:
         # reflection 1: the interfaces between the effective media and their tracked reflections
         raise NotImplementedError("2x2 effective layers of uniaxial or biaxial symmetry are implemented with "
                                   "reflection 0 or 2, or with diffraction = inf")
-    aniso = block_sym is not None and any(block_sym) and diffraction not in (0, np.inf)
+    aniso = aniso and diffraction not in (0, np.inf)
     if ret_bulk and method == "4x4" and npass > 1 and (diffraction == 0 or diffraction == np.inf or
                                                         reflection in (2, 3, 4) or aniso):
         raise NotImplementedError("ret_bulk with npass > 1 is implemented for reflection mode 1 with diffraction >= 1")
@@ -681,7 +731,7 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         nray = 1
     nimg = int(np.prod(field_in.shape[:-3]))
     npol = nimg // (nray * nlam)
-    mat = _Material(od, shape, dev, block_sym)
+    mat = _Material(od, shape, dev, block_sym, block_eff)
     fdev = field_dev.to(cdt).contiguous()
     L = mat.nlayers
     bulk_dev = None

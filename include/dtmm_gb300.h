@@ -138,6 +138,13 @@ typedef struct dtmm_transfer_desc {
      synchronises its stream once, and is refused inside a stream capture.
      ABI 6. */
   const int* block_sym;
+  /* host [nblocks][9] or null: with block_sym 3 a block's effective medium
+     is given (the reference's eff_data as an optical block, homogeneous in
+     each layer, dtmm/transfer.py:941-948): epsv (re, im) x 3 and the Euler
+     angles psi, theta, phi.  Three equal eigenvalues make it isotropic (the
+     default path), otherwise it takes the real-space chains as block_sym 1
+     and 2 do; no host synchronisation.  ABI 7. */
+  const double* block_eff;
 } dtmm_transfer_desc;
 
 typedef struct dtmm_transfer_io {
@@ -169,7 +176,7 @@ typedef struct dtmm_kernel_times {
 } dtmm_kernel_times;
 
 /* ABI version of this header (2: tuning fields in dtmm_transfer_desc, plane-wave inputs, POM image formation;
-   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block; 5: norm_ref; 6: block_sym). */
+   3: the biaxial field of dtmm_transfer_desc; 4: norm_total, layer_block; 5: norm_ref; 6: block_sym; 7: block_eff). */
 int dtmm_abi_version(void);
 
 /* Message of the last failure on the calling thread ("" if none). */

@@ -22,7 +22,7 @@ mode 0, diffraction >= 1 (diffraction > 1 = tent-window mode grouping),
 npass >= 1 for 4x4 (norm "fft"), nstep >= 1, scalar or per-ray beta/phi or
 beta/phi estimated from the field, real or complex eps, isotropic / uniaxial /
 biaxial voxels, effective layers of isotropic, uniaxial or biaxial symmetry
-(eff_data 0 / 1 / 2, per block or per layer).
+(eff_data 0 / 1 / 2, per block or per layer) or given as optical blocks.
 """
 from __future__ import annotations
 
@@ -1252,8 +1252,17 @@ def effective_block(block, symmetry):
     return evs, eas
 
 
+def _is_effective_block(e):
+    """eff_data entry given as an optical block (its eps values end in an axis
+    of three); the reference tries the entry as a block first
+    (dtmm/transfer.py:941-947)."""
+    return (isinstance(e, tuple) and len(e) == 3 and not callable(e[1]) and np.ndim(e[1]) >= 1 and
+            np.shape(e[1])[-1] == 3)
+
+
 def _layers_list(block, nin, nout, nstep, is_first, is_last, eff_data=0):
-    """Layer and effective-layer lists with the input/output media (dtmm/transfer.py:926)."""
+    """Layer and effective-layer lists with the input/output media (dtmm/transfer.py:926);
+    the effective layers of a given effective block take its thicknesses and media."""
     d, epsv, epsa = block
     substeps = np.broadcast_to(np.asarray(nstep), (len(d),))
     layers = [(int(n), (t / n, ev, ea)) for n, t, ev, ea in zip(substeps, d, epsv, epsa)]
@@ -1264,8 +1273,17 @@ def _layers_list(block, nin, nout, nstep, is_first, is_last, eff_data=0):
         layers.insert(0, (1, (0.0, np.broadcast_to(eps_in, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
     if is_last:
         layers.append((1, (0.0, np.broadcast_to(eps_out, epsv[0].shape), np.broadcast_to(zero, epsa[0].shape))))
-    ev_eff, ea_eff = effective_block(block, eff_data)
-    eff = [(int(n), (t / n, ev, ea)) for n, t, ev, ea in zip(substeps, d, ev_eff, ea_eff)]
+    if _is_effective_block(eff_data):
+        d_eff, ev_e, ea_e = validate_optical_block(eff_data, shape=(1, 1))
+        ea_e = np.asarray(ea_e, FDTYPE)
+        if ea_e.ndim == 2:
+            ea_e = ea_e[:, None, None, :]
+        ev_e = np.broadcast_to(ev_e, (len(d_eff), 1, 1, 3))
+        ea_e = np.broadcast_to(ea_e, (len(d_eff), 1, 1, 3))
+        eff = [(int(n), (t / n, ev[0, 0], ea[0, 0])) for n, t, ev, ea in zip(substeps, d_eff, ev_e, ea_e)]
+    else:
+        ev_eff, ea_eff = effective_block(block, eff_data)
+        eff = [(int(n), (t / n, ev, ea)) for n, t, ev, ea in zip(substeps, d, ev_eff, ea_eff)]
     if is_first:
         eff.insert(0, (1, (0.0, eps_in, zero)))
     if is_last:
@@ -2051,8 +2069,6 @@ def transfer_field(field_data, optical_data, beta=None, phi=None, nin=None, nout
     eff_data = opt("eff_data", eff_data)
     diffraction, reflection = opt("diffraction", diffraction), opt("reflection", reflection)
     betamax = opt("betamax", betamax)
-    if isinstance(eff_data, tuple) or (isinstance(eff_data, list) and any(isinstance(e, tuple) for e in eff_data)):
-        raise NotImplementedError("oracle covers effective data given by symmetry")
     if split_rays:
         raise NotImplementedError("oracle covers unsplit rays")
     if split_wavelengths and not isinstance(field_data[0], tuple) and not ret_bulk:

@@ -280,6 +280,28 @@ CASES = {
                                     illum=dict(beta=0.1, phi=0.5, jones=(0, 1)),
                                     transfer=dict(method="2x2", diffraction=1, eff_data=1, ret_bulk=True, beta=0.1,
                                                   phi=0.5)),
+    # effective layers given as optical blocks (one homogeneous medium per layer)
+    "fourx4_eff_given": dict(shape=(12, 14), nlayers=3, wavelengths=[540.0], pixelsize=100.0,
+                             material=("twisted", dict()), seed=90,
+                             illum=dict(beta=0.1, phi=0.4, jones=(1, 0)),
+                             transfer=dict(method="4x4", diffraction=1, beta=0.1, phi=0.4,
+                                           eff_data=[(np.ones(3), np.array([[2.3, 2.3, 2.7], [2.28, 2.28, 2.75],
+                                                                            [2.31, 2.35, 2.7]]),
+                                                      np.array([[0.0, 0.9, 0.2], [0.0, 1.1, 0.7],
+                                                                [0.3, 1.0, 1.2]]))])),
+    "fourx4_eff_given_iso_d3_npass2": dict(shape=(12, 12), nlayers=2, wavelengths=[560.0], pixelsize=100.0,
+                                           material=("twisted", dict(amplitude=0.3)), seed=91,
+                                           illum=dict(jones=(0, 1)),
+                                           transfer=dict(method="4x4", diffraction=3, npass=2, beta=0.0, phi=0.0,
+                                                         eff_data=[(np.ones(2), np.array([[2.4, 2.4, 2.4],
+                                                                                          [2.5, 2.5, 2.5]]),
+                                                                    np.zeros((2, 3)))])),
+    "twox2_eff_given_d3": dict(shape=(12, 12), nlayers=2, wavelengths=[500.0, 610.0], pixelsize=100.0,
+                               material=("twisted", dict()), seed=92,
+                               illum=dict(jones=(1, 0)),
+                               transfer=dict(method="2x2", diffraction=3, beta=0.0, phi=0.0,
+                                             eff_data=[(np.ones(2), np.array([[2.3, 2.3, 2.7], [2.3, 2.3, 2.7]]),
+                                                        np.array([[0.0, 1.2, 0.4], [0.0, 1.2, 1.0]]))])),
     "fourx4_split_layers": dict(shape=(12, 14), nlayers=3, wavelengths=[550.0], pixelsize=100.0,
                                 material=("mixed", dict()), seed=22,
                                 illum=dict(beta=0.1, phi=0.3, jones=(1, 0)),

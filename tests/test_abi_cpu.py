@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 6
+    assert lib.dtmm_abi_version() == _lib.ABI_VERSION == 7
 
 
 def _desc(**kw):
@@ -245,8 +245,17 @@ def test_block_sym_descriptor_rules(lib):
     a1 = size([1])
     assert a1 > 0 and size([2]) == a1
     assert size([1], nray=2) > a1  # per-ray tables of the windows' beams
-    for bad in ([3], [-1]):
+    for bad in ([4], [-1], [3]):  # 3 without block_eff
         assert size(bad) == 0 and "block_sym" in _lib.last_error()
+    # given media (block_sym 3): three equal eigenvalues keep the default path
+    iso = np.array([2.4, 0.0, 2.4, 0.0, 2.4, 0.0, 0.0, 0.0, 0.0])
+    uni = np.array([2.3, 0.0, 2.3, 0.0, 2.7, 0.0, 0.0, 0.5, 0.1])
+    for rec, same in ((iso, True), (uni, False)):
+        dd = _with_sym(_desc(), [3])
+        dd._be = rec
+        dd.block_eff = rec.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        s3 = lib.dtmm_transfer_workspace_size(ctypes.byref(dd))
+        assert s3 > 0 and (s3 == size(None)) == same
     assert size([1], method=2, reflection=0) > 0  # the k-space step in real space
     assert size([1], method=2, reflection=1) == 0 and "reflection" in _lib.last_error()
     assert size([1], method=2, reflection=2) == size(None, method=2, reflection=2) > 0
