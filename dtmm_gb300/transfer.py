@@ -672,10 +672,31 @@ def _require_cuda():
     return torch
 
 
+def _beams(beta, phi, field_in):
+    """beta, phi as float64 arrays and the number of rays: scalars, or one value
+    per ray with the rays on the first field axis (dtmm/transfer.py:42-65)."""
+    beta = np.asarray(beta, np.float64)
+    phi = np.asarray(phi, np.float64)
+    if beta.ndim != phi.ndim:
+        raise ValueError("Beta nad phi should have same dimensions!")
+    if beta.ndim == 1:
+        if len(beta) != len(phi):
+            raise ValueError("Beta nad phi should have same length!")
+        nray = len(beta)
+        if field_in.ndim < 5 or field_in.shape[0] != nray:
+            if nray == 1:
+                return beta[0], phi[0], 1
+            raise ValueError("per-ray beta needs the rays on the first field axis")
+        return beta, phi, nray
+    if beta.ndim != 0:
+        raise ValueError("Only length 1 or scalar values are supported for beta and phi")
+    return beta, phi, 1
+
+
 def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, nin, nout, npass, nstep,
                      diffraction, reflection, method, multiray, norm, betamax, smooth, ret_bulk, out, precision,
                      split_layers=False, eff_data=0):
-    torch = _require_cuda()
+    # every option and shape is checked on the host before the device is touched
     _check_path(method, reflection, npass, diffraction, norm)
     if smooth < 0:
         smooth = 0.0
@@ -704,31 +725,18 @@ def _transfer_single(field_in, wavelengths, pixelsize, optical_data, beta, phi, 
         # the k-space sweep carries the sum of the windows, whose E -> H conversions differ
         raise NotImplementedError("2x2 ret_bulk in k-space (reflection 0 / 1) is implemented for diffraction <= 1")
     ks = k0(wavelengths, pixelsize)
+    if (beta is None) != (phi is None):
+        raise ValueError("Both beta and phi must be defined!")
+    given = beta is not None
+    if given:
+        beta, phi, nray = _beams(beta, phi, field_in)
+    torch = _require_cuda()
     cdt = torch.complex128 if precision == "double" else torch.complex64
     dev = torch.device("cuda", torch.cuda.current_device())
     field_dev = torch.from_numpy(np.ascontiguousarray(field_in, np.complex128)).to(dev)
-    if beta is None and phi is None:
+    if not given:
         beta, phi = _field2betaphi(field_dev, ks, multiray)
-    elif beta is None or phi is None:
-        raise ValueError("Both beta and phi must be defined!")
-    beta = np.asarray(beta, np.float64)
-    phi = np.asarray(phi, np.float64)
-    if beta.ndim != phi.ndim:
-        raise ValueError("Beta nad phi should have same dimensions!")
-    if beta.ndim == 1:
-        if len(beta) != len(phi):
-            raise ValueError("Beta nad phi should have same length!")
-        nray = len(beta)
-        if field_in.ndim < 5 or field_in.shape[0] != nray:
-            if nray == 1:
-                beta, phi = beta[0], phi[0]
-                nray = 1
-            else:
-                raise ValueError("per-ray beta needs the rays on the first field axis")
-    elif beta.ndim != 0:
-        raise ValueError("Only length 1 or scalar values are supported for beta and phi")
-    else:
-        nray = 1
+        beta, phi, nray = _beams(beta, phi, field_in)
     nimg = int(np.prod(field_in.shape[:-3]))
     npol = nimg // (nray * nlam)
     mat = _Material(od, shape, dev, block_sym, block_eff)
